@@ -1,0 +1,283 @@
+"""Headline benchmark: finite-element assembly throughput (Melem/s) of 3-D linear
+elasticity, QUADRATIC LAGRANGE TET10, QGauss FOURTH (Keast 11 points), on
+build_cube 48^3 split into 6 tets per hex (663,552 elements, 2,738,019 dofs,
+231,797,385 nonzeros), interior vertices jittered +-0.2h (seed 1), E_e ~
+lognormal(0, 0.5), nu = 0.3, nodal body force ~ U[-1, 1], clamp on x = 0.
+
+One step = one full assembly of K (CSR values) and F from zero through the C ABI.
+`value` has the inputs resident on the device; `e2e` refreshes the per-step
+inputs (E_e, f) from pinned host memory and copies K and F back to pinned host
+memory inside the timed region.  `--impl reference` times the CPU restatement of
+the reference's threaded assembly (FEMSystem-style element ranges, mutex-guarded
+insertion) on the host cores.  Under torchrun every rank assembles its own
+replica (assembly needs no exchange on one box): scaling "weak"."""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Melem/s assembled (FP64 drop-in vs mixed/batched at <=1e-6 rel err), % roofline"
+N_CUBE = 48
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def build_problem(n=N_CUBE):
+    import libmesh_gb300 as lm
+    mesh = lm.Mesh.build_cube(n, n, n, lm.TET10, jitter=0.2, seed=1)
+    dm = lm.DofMap(mesh, 3)
+    dm.add_dirichlet_boundary([4], [0, 1, 2])
+    rng = np.random.default_rng(1)
+    E = np.exp(rng.normal(0.0, 0.5, mesh.n_elem))
+    f = rng.uniform(-1.0, 1.0, (mesh.n_nodes, 3))
+    return mesh, dm, E, f
+
+
+def algorithmic(mesh, dm, nnz):
+    """Unique bytes and reference-form flops of one assembly (FMA = 2)."""
+    n_geo, n, q = 10, 10, 11
+    B = 24 * mesh.n_nodes + 4 * mesh.n_elem * n_geo + 8 * dm.n_dofs + 8 * mesh.n_elem + 8 * nnz + 8 * dm.n_dofs
+    per_elem = q * (2 * (6 * 6 * 3 * n + 3 * n * 3 * n * 6) + 18 * n) + q * (18 * n_geo + 60)
+    return B, per_elem * mesh.n_elem
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, dev):
+        self.dev, self.proc, self.path = dev, None, None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.dev), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": []}
+        if self.proc is None:
+            return out
+        time.sleep(0.25)
+        self.proc.terminate()
+        self.proc.wait()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax.append(float(p[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        os.unlink(self.path)
+        if sm:
+            out = {"sm_mhz": float(np.median(sm)), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                   "samples": len(sm)}
+        return out
+
+
+def cpu_sample(mesh, dm, E, f, rp, col, threads, budget_s=12.0):
+    """Times the oracle (restated reference assembly) on a bounded element sample."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import libmesh_gb300 as lm
+    import oracle as orc
+    t = {}
+    probe = max(threads * 4, 64)
+    orc.assemble(lm.ELASTICITY, lm.TET10, 2, 4, mesh.xyz, mesh.conn, 3, dm.elem_dofs, dm.n_dofs,
+                 dm.constrained, rp, col, coef=E, nodal_f=f, n_threads=threads, e_range=(0, probe), timing=t)
+    rate = probe / max(t["seconds"], 1e-6)
+    n = int(min(mesh.n_elem, max(probe, rate * budget_s)))
+    orc.assemble(lm.ELASTICITY, lm.TET10, 2, 4, mesh.xyz, mesh.conn, 3, dm.elem_dofs, dm.n_dofs,
+                 dm.constrained, rp, col, coef=E, nodal_f=f, n_threads=threads, e_range=(0, n), timing=t)
+    return n / t["seconds"] / 1e6, n, t["seconds"]
+
+
+def run_reference(args, rank):
+    if rank != 0:
+        return
+    import libmesh_gb300 as lm
+    mesh, dm, E, f = build_problem()
+    nnz = __import__("ctypes").c_int64()
+    from libmesh_gb300._capi import lib, ptr
+    npe = mesh.conn.shape[1]
+    lib().lmg_host_sparsity(mesh.n_elem, npe, 3, dm.n_dofs, ptr(dm.elem_dofs), nnz, None, None)
+    rp = np.empty(dm.n_dofs + 1, np.int32)
+    col = np.empty(nnz.value, np.int32)
+    lib().lmg_host_sparsity(mesh.n_elem, npe, 3, dm.n_dofs, ptr(dm.elem_dofs), nnz, ptr(rp), ptr(col))
+    cores = os.cpu_count() or 1
+    vals = []
+    budget = max(2.0, 60.0 / max(1, args.steps + args.warmup))
+    for i in range(args.warmup + args.steps):
+        v, n, s = cpu_sample(mesh, dm, E, f, rp, col, cores, budget_s=budget)
+        if i >= args.warmup:
+            vals.append(v)
+    v = float(np.median(vals))
+    sample = "elements [0, %d) of the 663,552-element mesh per step, %d threads" % (n, cores)
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "Melem/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": mesh.n_elem / (v * 1e6) * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic", "config": {"workload": "elasticity TET10 build_cube 48^3 x6 tets, QGauss FOURTH"},
+        "cpu_baseline": {"value": v, "unit": "Melem/s", "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": v, "unit": "Melem/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    local = int(os.environ.get("LOCAL_RANK", 0))
+    if args.impl == "reference":
+        return run_reference(args, rank)
+
+    import torch
+    import libmesh_gb300 as lm
+    from libmesh_gb300 import _build
+    _build.build()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    prec = lm.FP64 if args.precision == "fp64" else lm.MIXED
+    mesh, dm, E, f = build_problem()
+    asm = lm.GpuAssembly(lm.ELASTICITY, 2, 4, elem_coef=E, nodal_f=f, nu=0.3, device=local)
+    asm.init(mesh, dm)
+    stream = torch.cuda.current_stream()
+    asm.set_stream(stream.cuda_stream)
+    for _ in range(max(3, args.warmup)):
+        asm.assemble_device(prec)
+    asm.synchronize()
+
+    clocks = Clocks(local)
+    clocks.start()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    l0 = asm.launch_count()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        asm.assemble_device(prec)
+    ev1.record(stream)
+    ev1.synchronize()
+    asm.synchronize()
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1) / args.steps
+    launches = asm.launch_count() - l0
+    clk = clocks.stop()
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * mesh.n_elem / (ms * 1e-3) / 1e6
+
+    # per-stage times (PerfLog events) for the roofline
+    asm.perflog_enable(True)
+    for _ in range(5):
+        asm.assemble_device(prec)
+    el_ms, ga_ms, calls = asm.perflog_read()
+    asm.perflog_enable(False)
+    el_ms, ga_ms = el_ms / calls, ga_ms / calls
+
+    # end to end through the C ABI with host buffers
+    Kh = torch.empty(asm.nnz, dtype=torch.float64, pin_memory=True)
+    Fh = torch.empty(dm.n_dofs, dtype=torch.float64, pin_memory=True)
+    Eh = torch.from_numpy(E).pin_memory()
+    fh = torch.from_numpy(np.ascontiguousarray(f)).pin_memory()
+    e2e_steps = max(3, min(args.steps, 10))
+    for _ in range(2):
+        asm.update_inputs(elem_coef=Eh.numpy(), nodal_f=fh.numpy())
+        asm.assemble_into(Kh.data_ptr(), Fh.data_ptr(), prec)
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        asm.update_inputs(elem_coef=Eh.numpy(), nodal_f=fh.numpy())
+        asm.assemble_into(Kh.data_ptr(), Fh.data_ptr(), prec)
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    if dist:
+        t = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = world * mesh.n_elem / e2e_s / 1e6
+
+    B, flops = algorithmic(mesh, dm, asm.nnz)
+    hbm, hbm_src = peaks()
+    fp64 = lm.probe_fp64(local)
+    if el_ms >= ga_ms:
+        dom = {"kernel": "k_elem_affine<ELASTICITY,10,3>", "bound": "fp64", "unit": "TFLOP/s",
+               "achieved": flops / (el_ms * 1e-3) / 1e12, "peak": fp64,
+               "peak_source": "measured FP64 DFMA probe (lmg_probe_fp64) in this run"}
+    else:
+        dom = {"kernel": "k_gather<double>", "bound": "hbm", "unit": "GB/s",
+               "achieved": (8 * asm.nnz + 8 * dm.n_dofs) / (ga_ms * 1e-3) / 1e9, "peak": hbm,
+               "peak_source": hbm_src}
+    dom["frac"] = dom["achieved"] / dom["peak"]
+    dom["traffic"] = None
+    dom["stages_ms"] = {"elements": el_ms, "insertion": ga_ms}
+    dom["step_hbm"] = {"achieved_gbs": B / (ms * 1e-3) / 1e9, "peak_gbs": hbm, "frac": B / (ms * 1e-3) / 1e9 / hbm,
+                       "algorithmic_bytes": B}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        rp, col = asm.sparsity()
+        cores = os.cpu_count() or 1
+        v, n, s = cpu_sample(mesh, dm, E, f, rp, col, cores, budget_s=10.0)
+        cpu = {"value": v, "unit": "Melem/s", "cores": cores, "kind": "port",
+               "sample": "elements [0, %d) of the mesh, %.1f s, %d threads" % (n, s, cores)}
+    asm.close()
+    if rank == 0:
+        print(json.dumps({
+            "metric": METRIC, "value": value, "unit": "Melem/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64" if prec == lm.FP64 else "f32+f64",
+            "data": "synthetic (seeded mesh jitter, E_e, f)",
+            "config": {"workload": "elasticity TET10 build_cube 48^3 x6 tets, QGauss FOURTH",
+                       "n_elem": mesh.n_elem, "n_dofs": dm.n_dofs, "nnz": asm.nnz,
+                       "precision": args.precision, "l2": "inputs larger than L2 (4.8 GB element buffer)",
+                       "parallelism": "replica per GPU"},
+            "mdofs_per_s": value * dm.n_dofs / mesh.n_elem,
+            "e2e": {"value": e2e, "unit": "Melem/s", "h2d_bytes_per_step": 8 * (mesh.n_elem + 3 * mesh.n_nodes),
+                    "d2h_bytes_per_step": 8 * (asm.nnz + dm.n_dofs)},
+            "gpu_launches": launches, "clocks": clk, "roofline": dom, "cpu_baseline": cpu}))
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

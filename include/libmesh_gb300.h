@@ -1,0 +1,192 @@
+/*
+ * libmesh_gb300 — GB300-native finite-element assembly behind a C ABI.
+ *
+ * This header is the whole drop-in boundary.  It replaces libMesh's per-element
+ * assembly loop (the user callback run by System::assemble) with one device
+ * pass over the mesh, and it mirrors the host-side libMesh setup that feeds
+ * that loop (mesh generation, DofMap numbering, Dirichlet constraint sets,
+ * sparsity).  Plain C types only: pointers, sizes, int status codes.
+ * Nothing here throws; every call returns an lmg_status.
+ *
+ * Reference interfaces replaced (paths inside the libMesh source tree):
+ *   System::assemble / attach_assemble_function / attach_assemble_object
+ *       src/systems/system.C:554-561, 1959-1986; include/systems/system.h:157-171
+ *   FEBase::reinit + get_phi/get_dphi/get_JxW over QGauss
+ *       src/fe/fe.C:197-368; src/fe/fe_base.C:762-793; src/fe/fe_map.C:1167-1374
+ *   DofMap::distribute_dofs / dof_indices
+ *       src/base/dof_map.C:949-1116, 1417-1537, 2201-2314; include/base/dof_map.h:2619-2760
+ *   DofMap::compute_sparsity (SparsityPattern::Build)
+ *       src/base/dof_map.C:1960-1977; src/base/sparsity_pattern.C:96-363
+ *   DofMap::(heterogenously_)constrain_element_matrix_and_vector
+ *       src/base/dof_map_constraints.C:2439-2616, 3433-3540
+ *   SparseMatrix::add_matrix / NumericVector::add_vector (PETSc AIJ layout)
+ *       src/numerics/petsc_matrix.C:735-755; src/numerics/petsc_vector.C:174-195
+ *   MeshTools::Generation::build_cube, MeshTools::Modification::all_tri,
+ *   MeshBase::all_second_order, ReplicatedMesh::renumber_nodes_and_elements
+ *       src/mesh/mesh_generation.C:317-1937; src/mesh/mesh_modification.C:449-1180;
+ *       src/mesh/unstructured_mesh.C:60-640; src/mesh/replicated_mesh.C:700-860
+ */
+#ifndef LIBMESH_GB300_H
+#define LIBMESH_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int32_t lmg_status;
+
+/* Status codes.  libMesh raises C++ exceptions for the same conditions
+ * (libmesh_error_msg, DegenerateMap: include/base/libmesh_exceptions.h:65-207). */
+enum {
+  LMG_OK = 0,
+  LMG_ERR_ARG = 1,          /* bad argument (null pointer, size, unknown enum)          */
+  LMG_ERR_CUDA = 2,         /* a CUDA runtime call failed                               */
+  LMG_ERR_STATE = 3,        /* call order violated (e.g. assemble before sparsity)     */
+  LMG_ERR_DEGENERATE = 4,   /* detJ <= 0 at a quadrature point (fe_map.C:466-500)       */
+  LMG_ERR_BOUNDS = 5,       /* connectivity or dof index outside its range              */
+  LMG_ERR_NEW_NONZERO = 6,  /* element couples a pair not in the sparsity (petsc_matrix.C:330-336) */
+  LMG_ERR_OOM = 7,          /* device or host allocation failed                         */
+  LMG_ERR_UNSUPPORTED = 8   /* element type / order / form combination not built       */
+};
+
+/* Element types: the numeric values of libMesh's ElemType (include/enums/enum_elem_type.h). */
+enum { LMG_TET4 = 8, LMG_TET10 = 9, LMG_HEX8 = 10, LMG_HEX27 = 12, LMG_PRISM6 = 13 };
+
+/* Weak forms registered with the element kernels (examples the forms follow):
+ *   LMG_POISSON    Ke += k_e JxW dphi_i.dphi_j, Fe += JxW f phi_i
+ *                  (examples/introduction/introduction_ex4/introduction_ex4.C:467,536)
+ *   LMG_ELASTICITY Ke_var[i][k] += JxW C_ijkl(E_e, nu) dphi_b(l) dphi_a(j), Fe_var[i] += JxW f_i phi_a
+ *                  (examples/systems_of_equations/systems_of_equations_ex6/systems_of_equations_ex6.C:136-230) */
+enum { LMG_POISSON = 0, LMG_ELASTICITY = 1 };
+
+/* Arithmetic of the element contraction.  LMG_FP64 is the drop-in (matches
+ * libMesh to 1e-13 per entry).  LMG_MIXED keeps Jacobians, the global
+ * accumulation and the outputs in FP64 and contracts in FP32. */
+enum { LMG_FP64 = 0, LMG_MIXED = 1 };
+
+/* ------------------------------------------------------------------------- */
+/* Host mirror of libMesh's setup: mesh generation and DofMap.               */
+/* ------------------------------------------------------------------------- */
+
+typedef struct lmg_mesh lmg_mesh;
+
+/* MeshTools::Generation::build_cube(nx,ny,nz, 0..1 x3, type) followed by
+ * prepare_for_use (first-touch node renumbering), src/mesh/mesh_generation.C:317-1937.
+ * elem_type LMG_HEX8 or LMG_HEX27 gives the hex mesh; LMG_TET4 / LMG_TET10 gives
+ * build_cube(HEX8) -> jitter -> MeshTools::Modification::all_tri (6 tets per hex,
+ * src/mesh/mesh_modification.C:449-1180) [-> all_second_order for TET10].
+ * jitter > 0 moves every interior vertex of the HEX8 grid by an independent
+ * uniform offset in [-jitter*h, +jitter*h] per coordinate, drawn from a
+ * splitmix64 stream seeded with `seed`, before the tet split (so TET10 mid-edge
+ * nodes sit at edge midpoints and every tet stays affine). */
+lmg_status lmg_mesh_cube(int32_t nx, int32_t ny, int32_t nz, int32_t elem_type,
+                         double jitter, uint64_t seed, lmg_mesh **out);
+lmg_status lmg_mesh_info(const lmg_mesh *m, int64_t *n_nodes, int64_t *n_elem,
+                         int32_t *elem_type, int32_t *nodes_per_elem, int32_t *sides_per_elem);
+/* xyz [n_nodes][3]; conn [n_elem][nodes_per_elem] (libMesh local node order);
+ * side_bid [n_elem][sides_per_elem] boundary id of each side or -1. Any may be NULL. */
+lmg_status lmg_mesh_copy(const lmg_mesh *m, double *xyz, int32_t *conn, int8_t *side_bid);
+lmg_status lmg_mesh_free(lmg_mesh *m);
+
+/* DofMap::distribute_dofs (var-major, first touch over active elements,
+ * src/base/dof_map.C:1417-1537) for n_vars LAGRANGE variables of one
+ * VariableGroup with one dof per node, then DofMap::dof_indices for every
+ * element (include/base/dof_map.h:2619-2760): elem_dofs[e][v*npe + a].
+ * elem_dofs has n_elem * n_vars * npe entries. */
+lmg_status lmg_dofmap_distribute(int64_t n_nodes, int64_t n_elem, int32_t npe,
+                                 const int32_t *conn, int32_t n_vars,
+                                 int64_t *n_dofs, int32_t *elem_dofs);
+
+/* Dof set constrained by a homogeneous DirichletBoundary on the sides whose
+ * boundary id is in bids[0..n_bids) for the variables vars[0..n_vars_bc)
+ * (ConstrainDirichlet, src/base/dof_map_constraints.C:257-1560: for LAGRANGE
+ * every dof of every node on a matching side).  constrained[n_dofs] gets 0/1. */
+lmg_status lmg_dirichlet_dofs(int64_t n_elem, int32_t elem_type, int32_t n_vars,
+                              const int32_t *elem_dofs, const int8_t *side_bid,
+                              const int32_t *bids, int32_t n_bids,
+                              const int32_t *vars, int32_t n_vars_bc,
+                              int64_t n_dofs, uint8_t *constrained);
+
+/* DofMap::compute_sparsity on the host (the same pattern lmg_sparsity_build
+ * puts on the device): PETSc-AIJ CSR with sorted columns, full coupling of the
+ * dofs of each element.  Call with row_ptr = col_idx = NULL to get nnz. */
+lmg_status lmg_host_sparsity(int64_t n_elem, int32_t npe, int32_t n_vars, int64_t n_dofs,
+                             const int32_t *elem_dofs, int64_t *nnz, int32_t *row_ptr,
+                             int32_t *col_idx);
+
+/* ------------------------------------------------------------------------- */
+/* Device context: the assembly drop-in.                                     */
+/* ------------------------------------------------------------------------- */
+
+typedef struct lmg_ctx lmg_ctx;
+
+lmg_status lmg_context_create(lmg_ctx **ctx, int32_t device);
+lmg_status lmg_context_destroy(lmg_ctx *ctx);
+/* Run every kernel and copy of this context on `stream` (a cudaStream_t). */
+lmg_status lmg_context_set_stream(lmg_ctx *ctx, void *stream);
+
+/* Geometry: xyz [n_nodes][3], conn [n_elem][npe] in libMesh node order.
+ * Uniform element type per context.  The host arrays may be freed on return. */
+lmg_status lmg_mesh_upload(lmg_ctx *ctx, int64_t n_nodes, const double *xyz,
+                           int64_t n_elem, int32_t elem_type, const int32_t *conn);
+
+/* Exact DofMap::dof_indices output: elem_dofs[e][v*npe + a] for n_vars variables. */
+lmg_status lmg_dofmap_upload(lmg_ctx *ctx, int32_t n_vars, int64_t n_dofs,
+                             const int32_t *elem_dofs);
+
+/* Constrained dofs with empty constraint rows and zero values (homogeneous
+ * Dirichlet), as DofMap::_dof_constraints holds them. constrained[n_dofs]. */
+lmg_status lmg_constraints_upload(lmg_ctx *ctx, const uint8_t *constrained);
+
+/* DofMap::compute_sparsity: PETSc-AIJ CSR (sorted column indices per row). */
+lmg_status lmg_sparsity_build(lmg_ctx *ctx, int64_t *nnz);
+lmg_status lmg_sparsity_copy(lmg_ctx *ctx, int32_t *row_ptr, int32_t *col_idx);
+
+/* Weak form and its data.  fe_order: 1 FIRST / 2 SECOND LAGRANGE.
+ * q_order: QGauss order (libMesh Order value).  params: POISSON none;
+ * ELASTICITY {nu}.  elem_coef[n_elem]: k_e (POISSON) or E_e (ELASTICITY),
+ * NULL = 1.  nodal_f[n_nodes][n_vars]: load interpolated with phi, NULL = 0. */
+lmg_status lmg_form_set(lmg_ctx *ctx, int32_t form, int32_t fe_order, int32_t q_order,
+                        const double *params, int32_t n_params,
+                        const double *elem_coef, const double *nodal_f);
+
+/* Refresh the per-step inputs from host memory (any may be NULL = unchanged). */
+lmg_status lmg_inputs_update(lmg_ctx *ctx, const double *xyz, const double *elem_coef,
+                             const double *nodal_f);
+
+/* Assemble K (CSR values, nnz) and F (n_dofs) from zero.  K and F may be host
+ * or device pointers (out_on_device = 0 / 1); NULL keeps the result only in the
+ * context's own device buffers (see lmg_result_device). */
+lmg_status lmg_assemble(lmg_ctx *ctx, int32_t precision, double *K, double *F,
+                        int32_t out_on_device);
+lmg_status lmg_result_device(lmg_ctx *ctx, double **K, double **F);
+
+/* With device (or no) outputs lmg_assemble returns once the work is queued on
+ * the context's stream; lmg_synchronize waits for it and returns its status. */
+lmg_status lmg_synchronize(lmg_ctx *ctx);
+
+/* First failing element of the last call (-1 if none) and a message. */
+lmg_status lmg_last_error(lmg_ctx *ctx, int64_t *elem_id, char *msg, int32_t msg_len);
+
+/* PerfLog-style stage timing (the reference's PerfLog scopes "assemble()" /
+ * "matrix insertion", include/utils/perf_log.h:153-280): when enabled, every
+ * lmg_assemble records CUDA events around its element kernels and its global
+ * insertion; lmg_perflog_read waits for the stream, returns the summed times
+ * and the number of logged calls, and resets the totals. */
+lmg_status lmg_perflog_enable(lmg_ctx *ctx, int32_t on);
+lmg_status lmg_perflog_read(lmg_ctx *ctx, double *elements_ms, double *gather_ms, int64_t *calls);
+
+/* Number of kernels this context has launched since creation. */
+lmg_status lmg_launch_count(lmg_ctx *ctx, int64_t *count);
+
+/* Measured FP64 FMA throughput of `device` in TFLOP/s (independent DFMA
+ * chains on every SM): the roofline denominator of the FP64 element kernels. */
+lmg_status lmg_probe_fp64(int32_t device, double *tflops);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LIBMESH_GB300_H */

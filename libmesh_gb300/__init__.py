@@ -1,0 +1,226 @@
+"""libmesh_gb300: GB300-native finite-element assembly behind libMesh's assembly API.
+
+Python mirror of the libMesh objects the assembly path touches, over the C ABI
+in include/libmesh_gb300.h (liblmg.so):
+
+  Mesh.build_cube        MeshTools::Generation::build_cube (+ all_tri / all_second_order)
+  DofMap                 DofMap::distribute_dofs / dof_indices / add_dirichlet_boundary
+  GpuAssembly            a System::Assembly whose assemble() is one device pass
+  LinearImplicitSystem   attach_assemble_object / init (compute_sparsity) / assemble
+
+Every numeric path goes through the native library; a missing library raises."""
+import ctypes as C
+
+import numpy as np
+
+from . import _capi
+from ._capi import (ELASTICITY, FP64, HEX8, HEX27, MIXED, POISSON, PRISM6, TET4, TET10,
+                    DegenerateMap, LmgError, check, lib, ptr)
+
+FIRST, SECOND, THIRD, FOURTH, FIFTH = 1, 2, 3, 4, 5
+
+__all__ = ["Mesh", "DofMap", "GpuAssembly", "LinearImplicitSystem", "DegenerateMap", "LmgError",
+           "HEX8", "HEX27", "TET4", "TET10", "PRISM6", "POISSON", "ELASTICITY", "FP64", "MIXED",
+           "FIRST", "SECOND", "THIRD", "FOURTH", "FIFTH"]
+
+
+class Mesh:
+    """Host mesh: xyz [n_nodes,3], conn [n_elem,npe] (libMesh node order),
+    side_bid [n_elem,n_sides] (boundary id per side, -1 interior)."""
+
+    def __init__(self, xyz, conn, elem_type, side_bid=None):
+        self.xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+        self.conn = np.ascontiguousarray(conn, dtype=np.int32)
+        self.elem_type = int(elem_type)
+        self.side_bid = None if side_bid is None else np.ascontiguousarray(side_bid, dtype=np.int8)
+
+    @property
+    def n_nodes(self):
+        return self.xyz.shape[0]
+
+    @property
+    def n_elem(self):
+        return self.conn.shape[0]
+
+    @classmethod
+    def build_cube(cls, nx, ny, nz, elem_type=HEX8, jitter=0.0, seed=0):
+        L = lib()
+        h = C.c_void_p()
+        check(L.lmg_mesh_cube(nx, ny, nz, elem_type, float(jitter), int(seed), C.byref(h)))
+        try:
+            nn, ne = C.c_int64(), C.c_int64()
+            et, npe, ns = C.c_int32(), C.c_int32(), C.c_int32()
+            check(L.lmg_mesh_info(h, C.byref(nn), C.byref(ne), C.byref(et), C.byref(npe), C.byref(ns)))
+            xyz = np.empty((nn.value, 3), np.float64)
+            conn = np.empty((ne.value, npe.value), np.int32)
+            sb = np.empty((ne.value, ns.value), np.int8)
+            check(L.lmg_mesh_copy(h, ptr(xyz), ptr(conn), ptr(sb)))
+        finally:
+            L.lmg_mesh_free(h)
+        return cls(xyz, conn, et.value, sb)
+
+
+class DofMap:
+    """Var-major first-touch numbering of n_vars LAGRANGE variables (one
+    VariableGroup); elem_dofs[e] is DofMap::dof_indices(elem)."""
+
+    def __init__(self, mesh, n_vars=1):
+        self.mesh = mesh
+        self.n_vars = int(n_vars)
+        npe = mesh.conn.shape[1]
+        self.elem_dofs = np.empty((mesh.n_elem, self.n_vars * npe), np.int32)
+        nd = C.c_int64()
+        check(lib().lmg_dofmap_distribute(mesh.n_nodes, mesh.n_elem, npe, ptr(mesh.conn), self.n_vars,
+                                          C.byref(nd), ptr(self.elem_dofs)))
+        self.n_dofs = nd.value
+        self.constrained = np.zeros(self.n_dofs, np.uint8)
+
+    def dof_indices(self, e, var=None):
+        d = self.elem_dofs[e]
+        if var is None:
+            return d.copy()
+        npe = self.mesh.conn.shape[1]
+        return d[var * npe:(var + 1) * npe].copy()
+
+    def add_dirichlet_boundary(self, bids, variables):
+        """Homogeneous DirichletBoundary on the listed side ids / variables."""
+        bids = np.ascontiguousarray(bids, np.int32)
+        variables = np.ascontiguousarray(variables, np.int32)
+        c = np.zeros(self.n_dofs, np.uint8)
+        check(lib().lmg_dirichlet_dofs(self.mesh.n_elem, self.mesh.elem_type, self.n_vars,
+                                       ptr(self.elem_dofs), ptr(self.mesh.side_bid), ptr(bids),
+                                       len(bids), ptr(variables), len(variables), self.n_dofs, ptr(c)))
+        self.constrained |= c
+        return c
+
+    def is_constrained_dof(self, d):
+        return bool(self.constrained[d])
+
+
+class GpuAssembly:
+    """System::Assembly replacement: one device context per system holding the
+    mesh, dof map, constraints, sparsity, scatter plan and form data."""
+
+    def __init__(self, form, fe_order, q_order, elem_coef=None, nodal_f=None, nu=0.3, device=0):
+        self.form, self.fe_order, self.q_order = int(form), int(fe_order), int(q_order)
+        self.elem_coef = None if elem_coef is None else np.ascontiguousarray(elem_coef, np.float64)
+        self.nodal_f = None if nodal_f is None else np.ascontiguousarray(nodal_f, np.float64)
+        self.nu = float(nu)
+        self.device = device
+        self.ctx = None
+        self.nnz = 0
+
+    def _ok(self, st):
+        check(st, self.ctx)
+
+    def init(self, mesh, dof_map):
+        L = lib()
+        if self.ctx is None:
+            h = C.c_void_p()
+            check(L.lmg_context_create(C.byref(h), self.device))
+            self.ctx = h
+        self.mesh, self.dof_map = mesh, dof_map
+        self._ok(L.lmg_mesh_upload(self.ctx, mesh.n_nodes, ptr(mesh.xyz), mesh.n_elem, mesh.elem_type,
+                                   ptr(mesh.conn)))
+        self._ok(L.lmg_dofmap_upload(self.ctx, dof_map.n_vars, dof_map.n_dofs, ptr(dof_map.elem_dofs)))
+        self._ok(L.lmg_constraints_upload(self.ctx, ptr(dof_map.constrained)))
+        nnz = C.c_int64()
+        self._ok(L.lmg_sparsity_build(self.ctx, C.byref(nnz)))
+        self.nnz = nnz.value
+        params = np.array([self.nu], np.float64)
+        self._ok(L.lmg_form_set(self.ctx, self.form, self.fe_order, self.q_order, ptr(params), 1,
+                                ptr(self.elem_coef), ptr(self.nodal_f)))
+
+    def sparsity(self):
+        rp = np.empty(self.dof_map.n_dofs + 1, np.int32)
+        ci = np.empty(self.nnz, np.int32)
+        self._ok(lib().lmg_sparsity_copy(self.ctx, ptr(rp), ptr(ci)))
+        return rp, ci
+
+    def update_inputs(self, xyz=None, elem_coef=None, nodal_f=None):
+        self._ok(lib().lmg_inputs_update(self.ctx, ptr(xyz), ptr(elem_coef), ptr(nodal_f)))
+
+    def assemble(self, precision=FP64):
+        K = np.empty(self.nnz, np.float64)
+        F = np.empty(self.dof_map.n_dofs, np.float64)
+        self._ok(lib().lmg_assemble(self.ctx, precision, ptr(K), ptr(F), 0))
+        return K, F
+
+    def assemble_device(self, precision=FP64, K_dev=None, F_dev=None):
+        """Assemble into device buffers (raw pointers, e.g. torch data_ptr());
+        None keeps the result in the context's own buffers.  Asynchronous."""
+        on_dev = 1 if (K_dev is not None or F_dev is not None) else 0
+        self._ok(lib().lmg_assemble(self.ctx, precision,
+                                    None if K_dev is None else C.c_void_p(K_dev),
+                                    None if F_dev is None else C.c_void_p(F_dev), on_dev))
+
+    def synchronize(self):
+        self._ok(lib().lmg_synchronize(self.ctx))
+
+    def set_stream(self, stream_ptr):
+        self._ok(lib().lmg_context_set_stream(self.ctx, C.c_void_p(stream_ptr)))
+
+    def perflog_enable(self, on=True):
+        self._ok(lib().lmg_perflog_enable(self.ctx, 1 if on else 0))
+
+    def perflog_read(self):
+        """(element-kernel ms, insertion ms, calls) summed since the last read."""
+        a, b, n = C.c_double(), C.c_double(), C.c_int64()
+        self._ok(lib().lmg_perflog_read(self.ctx, C.byref(a), C.byref(b), C.byref(n)))
+        return a.value, b.value, n.value
+
+    def assemble_into(self, K_ptr, F_ptr, precision=FP64, on_device=False):
+        """Assemble into caller buffers given as raw addresses (host or device)."""
+        self._ok(lib().lmg_assemble(self.ctx, precision, C.c_void_p(K_ptr), C.c_void_p(F_ptr),
+                                    1 if on_device else 0))
+
+    def launch_count(self):
+        n = C.c_int64()
+        self._ok(lib().lmg_launch_count(self.ctx, C.byref(n)))
+        return n.value
+
+    def close(self):
+        if self.ctx is not None:
+            lib().lmg_context_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def probe_fp64(device=0):
+    """Measured FP64 FMA throughput (TFLOP/s) of the device."""
+    t = C.c_double()
+    check(lib().lmg_probe_fp64(device, C.byref(t)))
+    return t.value
+
+
+class LinearImplicitSystem:
+    """The parts of libMesh's LinearImplicitSystem the assembly path uses."""
+
+    def __init__(self, mesh, n_vars=1):
+        self.mesh = mesh
+        self.dof_map = DofMap(mesh, n_vars)
+        self.assembly = None
+        self.matrix = None
+        self.rhs = None
+
+    def attach_assemble_object(self, assembly):
+        self.assembly = assembly
+
+    def init(self):
+        self.assembly.init(self.mesh, self.dof_map)
+        self.row_ptr, self.col_idx = self.assembly.sparsity()
+
+    def assemble(self, precision=FP64):
+        K, F = self.assembly.assemble(precision)
+        self.matrix, self.rhs = K, F
+        return K, F
+
+    def matrix_csr(self):
+        import scipy.sparse as sp
+        n = self.dof_map.n_dofs
+        return sp.csr_matrix((self.matrix, self.col_idx, self.row_ptr), shape=(n, n))

@@ -1,0 +1,61 @@
+// Device-side declarations for the assembly kernels (sm_103a).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+
+namespace lmg {
+
+// Reference-element tables in device memory (one set per context).
+struct DevFE {
+  int n, q, n_geo;
+  const double *qw;     // [q]
+  const double *phi;    // [q][n]
+  const double *dphi;   // [q][n][3]
+  const double *gdphi;  // [q][n_geo][3]
+  const double *S;      // [9][n][n]
+  const double *M;      // [n][n]
+};
+
+// Everything an element kernel reads or writes.
+struct ElemArgs {
+  int64_t n_list;             // elements in `list`
+  const int32_t *list;        // element ids to process
+  int npe;                    // nodes per element (geometry)
+  const double *xyz;          // [n_nodes][3]
+  const int32_t *conn;        // [n_elem][npe]
+  const double *coef;         // [n_elem] or null (=1)
+  const double *nodal_f;      // [n_nodes][nv] or null (=0)
+  const uint64_t *cmask;      // [n_elem] constrained local dofs, bit v*n + a
+  double nu;                  // Poisson ratio (elasticity)
+  double *Ke;                 // [n_elem][n][n][nv][nv]
+  double *Fe;                 // [n_elem][n][nv]
+  float *Ke32;                // mixed form: FP32 element blocks (same layout) or null
+  int *status;                // [0] error code
+  unsigned long long *bad_elem;  // first failing element id
+  DevFE fe;
+};
+
+// Scatter plan: gather-by-slot segmented reduction into CSR values.
+struct GatherArgs {
+  int64_t n_dofs;
+  int bs;                     // dofs per block (node-interleaved variables)
+  int nb;                     // blocks per element
+  const int64_t *brow_ptr;    // [n_blocks+1]
+  const int32_t *row_ptr;     // [n_dofs+1]
+  const int32_t *bptr;        // [nnzb+1] contributions per block slot
+  const int32_t *bcontrib;    // (e*nb + a)*nb + b, ascending per slot
+  const int32_t *fptr;        // [n_blocks+1]
+  const int32_t *fcontrib;    // e*nb + a, ascending per block row
+  const double *Ke;
+  const float *Ke32;
+  const double *Fe;
+  double *K;
+  double *F;
+};
+
+void launch_elements(int form, int n, int nv, bool affine, const ElemArgs &a, int grid,
+                     cudaStream_t s);
+void launch_gather(const GatherArgs &g, bool mixed, cudaStream_t s);
+
+}  // namespace lmg

@@ -1,0 +1,697 @@
+// Device context of the assembly drop-in: uploads, sparsity, scatter plan,
+// assemble, and the C-ABI entry points that drive them.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "assemble.cuh"
+#include "lmg_internal.h"
+
+using namespace lmg;
+
+struct lmg_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  int n_sm = 152;
+  int64_t launches = 0;
+  std::string err;
+  int64_t err_elem = -1;
+  // mesh
+  int elem_type = 0, npe = 0;
+  int64_t n_nodes = 0, n_elem = 0;
+  std::vector<double> h_xyz;
+  std::vector<int32_t> h_conn;
+  double *d_xyz = nullptr;
+  int32_t *d_conn = nullptr;
+  std::vector<int32_t> h_aff, h_gen;  // affine / general element lists
+  int32_t *d_aff = nullptr, *d_gen = nullptr;
+  // dofmap
+  int n_vars = 0, nl = 0, bs = 1, nb = 0;
+  int64_t n_dofs = 0, n_blocks = 0;
+  std::vector<int32_t> h_elem_dofs, h_eb;
+  int32_t *d_eb = nullptr;
+  // constraints
+  std::vector<uint8_t> h_constrained;
+  uint64_t *d_cmask = nullptr;
+  // sparsity and plan
+  bool have_sparsity = false;
+  int64_t nnz = 0, nnzb = 0;
+  int64_t *d_brow_ptr = nullptr;
+  int32_t *d_bcol = nullptr, *d_row_ptr = nullptr, *d_col = nullptr;
+  int32_t *d_bptr = nullptr, *d_bcontrib = nullptr, *d_fptr = nullptr, *d_fcontrib = nullptr;
+  // form
+  bool have_form = false;
+  int form = 0, fe_order = 0, q_order = 0;
+  double nu = 0.3;
+  FETables tab;
+  double *d_tab = nullptr;
+  DevFE dfe{};
+  double *d_coef = nullptr, *d_f = nullptr;
+  // work and result buffers
+  double *d_Ke = nullptr, *d_Fe = nullptr, *d_K = nullptr, *d_F = nullptr;
+  float *d_Ke32 = nullptr;
+  int *d_status = nullptr;
+  unsigned long long *d_bad = nullptr;
+  // PerfLog-style stage timing (CUDA events on the context stream)
+  bool perflog = false;
+  std::vector<cudaEvent_t> ev;       // 3 per logged assemble call
+  double log_ms[2] = {0.0, 0.0};     // element kernels, gather
+  int64_t log_calls = 0;
+};
+
+namespace {
+
+template <typename T>
+void dfree(T *&p) {
+  if (p) cudaFree((void *)p);
+  p = nullptr;
+}
+
+lmg_status fail(lmg_ctx *c, lmg_status code, const std::string &msg, int64_t elem = -1) {
+  if (c) {
+    c->err = msg;
+    c->err_elem = elem;
+  }
+  return code;
+}
+
+#define LMG_CUDA(ctx, call)                                                        \
+  do {                                                                             \
+    cudaError_t e_ = (call);                                                       \
+    if (e_ != cudaSuccess)                                                         \
+      return fail(ctx, e_ == cudaErrorMemoryAllocation ? LMG_ERR_OOM : LMG_ERR_CUDA, \
+                  std::string(#call) + ": " + cudaGetErrorString(e_));             \
+  } while (0)
+
+template <typename T>
+cudaError_t dalloc(T *&p, size_t n) {
+  dfree(p);
+  if (n == 0) n = 1;
+  return cudaMalloc((void **)&p, n * sizeof(T));
+}
+
+template <typename T>
+cudaError_t dupload(lmg_ctx *c, T *&p, const T *h, size_t n) {
+  cudaError_t e = dalloc(p, n);
+  if (e != cudaSuccess) return e;
+  if (n) e = cudaMemcpyAsync(p, h, n * sizeof(T), cudaMemcpyHostToDevice, c->stream);
+  return e;
+}
+
+// ---------------------------------------------------------------- kernels
+__global__ void k_expand_cols(int64_t n_dofs, int bs, const int64_t *brow_ptr, const int32_t *bcol,
+                              const int32_t *row_ptr, int32_t *col) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < n_dofs;
+       r += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+    const int64_t P = r / bs;
+    const int64_t rb = brow_ptr[P];
+    const int64_t len = (brow_ptr[P + 1] - rb) * bs;
+    int32_t *out = col + row_ptr[r];
+    for (int64_t m = lane; m < len; m += 32) out[m] = (int32_t)(bs * bcol[rb + m / bs] + m % bs);
+  }
+}
+
+// Block slot of every element block pair (e, a, b) by binary search in the
+// block row; counts contributions per slot.
+__global__ void k_slots(int64_t n_elem, int nb, const int32_t *eb, const int64_t *brow_ptr,
+                        const int32_t *bcol, int32_t *slot, int32_t *cnt, int *status) {
+  const int64_t total = n_elem * nb * nb;
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t e = idx / (nb * nb);
+    const int ab = (int)(idx - e * nb * nb);
+    const int a = ab / nb, b = ab - a * nb;
+    const int32_t P = eb[e * nb + a], Q = eb[e * nb + b];
+    int64_t lo = brow_ptr[P], hi = brow_ptr[P + 1];
+    while (lo < hi) {
+      const int64_t mid = (lo + hi) >> 1;
+      if (bcol[mid] < Q) lo = mid + 1; else hi = mid;
+    }
+    if (lo >= brow_ptr[P + 1] || bcol[lo] != Q) {
+      atomicCAS(status, 0, LMG_ERR_NEW_NONZERO);
+      slot[idx] = -1;
+      continue;
+    }
+    slot[idx] = (int32_t)lo;
+    atomicAdd(&cnt[lo], 1);
+  }
+}
+
+__global__ void k_count_rows(int64_t n, const int32_t *eb, int32_t *cnt) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    atomicAdd(&cnt[eb[i]], 1);
+}
+
+__global__ void k_fill(int64_t n, const int32_t *key, const int32_t *ptr, int32_t *cur,
+                       int32_t *out) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t k = key[i];
+    if (k < 0) continue;
+    out[ptr[k] + atomicAdd(&cur[k], 1)] = (int32_t)i;
+  }
+}
+
+// Each segment is short (the elements sharing one block pair), so an
+// insertion sort per thread puts contributions in element order.
+__global__ void k_segsort(int64_t n_seg, const int32_t *ptr, int32_t *v) {
+  for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < n_seg;
+       s += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t b = ptr[s], e = ptr[s + 1];
+    for (int32_t i = b + 1; i < e; ++i) {
+      const int32_t x = v[i];
+      int32_t j = i - 1;
+      while (j >= b && v[j] > x) { v[j + 1] = v[j]; --j; }
+      v[j + 1] = x;
+    }
+  }
+}
+
+// Exclusive scan helpers: block-local scan, then scan of block sums.
+constexpr int SCAN_T = 1024;
+__global__ void k_scan_local(int64_t n, const int32_t *in, int32_t *out, int32_t *bsum) {
+  __shared__ int32_t ws[32];
+  const int64_t i = (int64_t)blockIdx.x * SCAN_T + threadIdx.x;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  int32_t v = (i < n) ? in[i] : 0, x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) ws[w] = x;
+  __syncthreads();
+  if (w == 0) {
+    int32_t s = ws[lane];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int32_t y = __shfl_up_sync(0xffffffffu, s, o);
+      if (lane >= o) s += y;
+    }
+    ws[lane] = s;
+  }
+  __syncthreads();
+  const int32_t off = w ? ws[w - 1] : 0;
+  if (i < n) out[i] = x - v + off;
+  if (threadIdx.x == SCAN_T - 1) bsum[blockIdx.x] = off + x;
+}
+__global__ void k_scan_add(int64_t n, int32_t *out, const int32_t *boff) {
+  const int64_t i = (int64_t)blockIdx.x * SCAN_T + threadIdx.x;
+  if (i < n) out[i] += boff[blockIdx.x];
+}
+
+}  // namespace
+
+namespace {
+
+int grid_for(lmg_ctx *c, int64_t items, int threads) {
+  int64_t b = (items + threads - 1) / threads;
+  const int64_t cap = (int64_t)c->n_sm * 16;
+  if (b > cap) b = cap;
+  return (int)(b < 1 ? 1 : b);
+}
+
+// out[0..n] = exclusive scan of in[0..n); out[n] = total.
+lmg_status scan_i32(lmg_ctx *c, const int32_t *in, int32_t *out, int64_t n) {
+  const int64_t nblk = (n + SCAN_T - 1) / SCAN_T;
+  int32_t *bsum = nullptr, *boff = nullptr;
+  LMG_CUDA(c, dalloc(bsum, (size_t)nblk + 1));
+  LMG_CUDA(c, dalloc(boff, (size_t)nblk + 1));
+  if (n > 0) {
+    k_scan_local<<<(unsigned)nblk, SCAN_T, 0, c->stream>>>(n, in, out, bsum);
+    c->launches++;
+    if (nblk > 1) {
+      lmg_status st = scan_i32(c, bsum, boff, nblk);
+      if (st != LMG_OK) { dfree(bsum); dfree(boff); return st; }
+      k_scan_add<<<(unsigned)nblk, SCAN_T, 0, c->stream>>>(n, out, boff);
+      c->launches++;
+      LMG_CUDA(c, cudaMemcpyAsync(out + n, boff + nblk, sizeof(int32_t), cudaMemcpyDeviceToDevice,
+                                  c->stream));
+    } else {
+      LMG_CUDA(c, cudaMemcpyAsync(out + n, bsum, sizeof(int32_t), cudaMemcpyDeviceToDevice, c->stream));
+    }
+  } else {
+    LMG_CUDA(c, cudaMemsetAsync(out, 0, sizeof(int32_t), c->stream));
+  }
+  LMG_CUDA(c, cudaStreamSynchronize(c->stream));
+  dfree(bsum);
+  dfree(boff);
+  return LMG_OK;
+}
+
+lmg_status check_status(lmg_ctx *c, const char *what) {
+  int st = 0;
+  unsigned long long bad = ~0ull;
+  LMG_CUDA(c, cudaMemcpyAsync(&st, c->d_status, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  LMG_CUDA(c, cudaMemcpyAsync(&bad, c->d_bad, sizeof(bad), cudaMemcpyDeviceToHost, c->stream));
+  LMG_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (st != 0) {
+    const int64_t e = (bad == ~0ull) ? -1 : (int64_t)bad;
+    std::string m = std::string(what) + ": ";
+    if (st == LMG_ERR_DEGENERATE) m += "Jacobian at or under tolerance 0 (degenerate element)";
+    else if (st == LMG_ERR_NEW_NONZERO) m += "element couples a dof pair outside the sparsity pattern";
+    else m += "device error";
+    return fail(c, st, m, e);
+  }
+  return LMG_OK;
+}
+
+lmg_status reset_status(lmg_ctx *c) {
+  LMG_CUDA(c, cudaMemsetAsync(c->d_status, 0, sizeof(int), c->stream));
+  LMG_CUDA(c, cudaMemsetAsync(c->d_bad, 0xff, sizeof(unsigned long long), c->stream));
+  return LMG_OK;
+}
+
+// Element -> block map, and whether the variables sit node-interleaved
+// (dof = bs * block + var), which lets the plan work on bs x bs blocks.
+void detect_blocks(lmg_ctx *c) {
+  block_structure(c->n_elem, c->npe, c->n_vars, c->h_elem_dofs.data(), c->bs, c->nb, c->h_eb);
+  c->n_blocks = c->n_dofs / c->bs;
+}
+
+lmg_status build_plan(lmg_ctx *c) {
+  const int nb = c->nb;
+  const int64_t npair = c->n_elem * nb * nb, nrow = c->n_elem * nb;
+  if (npair >= INT32_MAX) return fail(c, LMG_ERR_UNSUPPORTED, "mesh too large for 32-bit plan");
+  int32_t *slot = nullptr, *cnt = nullptr, *cur = nullptr;
+  LMG_CUDA(c, dalloc(slot, (size_t)npair));
+  LMG_CUDA(c, dalloc(cnt, (size_t)std::max(c->nnzb, c->n_blocks)));
+  LMG_CUDA(c, dalloc(cur, (size_t)std::max(c->nnzb, c->n_blocks)));
+  LMG_CUDA(c, dalloc(c->d_bptr, (size_t)c->nnzb + 1));
+  LMG_CUDA(c, dalloc(c->d_bcontrib, (size_t)npair));
+  LMG_CUDA(c, dalloc(c->d_fptr, (size_t)c->n_blocks + 1));
+  LMG_CUDA(c, dalloc(c->d_fcontrib, (size_t)nrow));
+  lmg_status st = reset_status(c);
+  if (st) return st;
+  // matrix plan
+  LMG_CUDA(c, cudaMemsetAsync(cnt, 0, sizeof(int32_t) * c->nnzb, c->stream));
+  k_slots<<<grid_for(c, npair, 256), 256, 0, c->stream>>>(c->n_elem, nb, c->d_eb, c->d_brow_ptr,
+                                                          c->d_bcol, slot, cnt, c->d_status);
+  c->launches++;
+  if ((st = scan_i32(c, cnt, c->d_bptr, c->nnzb))) return st;
+  LMG_CUDA(c, cudaMemsetAsync(cur, 0, sizeof(int32_t) * c->nnzb, c->stream));
+  k_fill<<<grid_for(c, npair, 256), 256, 0, c->stream>>>(npair, slot, c->d_bptr, cur, c->d_bcontrib);
+  k_segsort<<<grid_for(c, c->nnzb, 256), 256, 0, c->stream>>>(c->nnzb, c->d_bptr, c->d_bcontrib);
+  c->launches += 2;
+  // vector plan
+  LMG_CUDA(c, cudaMemsetAsync(cnt, 0, sizeof(int32_t) * c->n_blocks, c->stream));
+  k_count_rows<<<grid_for(c, nrow, 256), 256, 0, c->stream>>>(nrow, c->d_eb, cnt);
+  c->launches++;
+  if ((st = scan_i32(c, cnt, c->d_fptr, c->n_blocks))) return st;
+  LMG_CUDA(c, cudaMemsetAsync(cur, 0, sizeof(int32_t) * c->n_blocks, c->stream));
+  k_fill<<<grid_for(c, nrow, 256), 256, 0, c->stream>>>(nrow, c->d_eb, c->d_fptr, cur, c->d_fcontrib);
+  k_segsort<<<grid_for(c, c->n_blocks, 256), 256, 0, c->stream>>>(c->n_blocks, c->d_fptr,
+                                                                  c->d_fcontrib);
+  c->launches += 2;
+  LMG_CUDA(c, cudaStreamSynchronize(c->stream));
+  dfree(slot);
+  dfree(cnt);
+  dfree(cur);
+  return check_status(c, "sparsity plan");
+}
+
+void build_lists(lmg_ctx *c) {
+  c->h_aff.clear();
+  c->h_gen.clear();
+  for (int64_t e = 0; e < c->n_elem; ++e) {
+    double P[27 * 3];
+    for (int a = 0; a < c->npe; ++a)
+      for (int d = 0; d < 3; ++d)
+        P[3 * a + d] = c->h_xyz[(size_t)(3 * (int64_t)c->h_conn[(size_t)(e * c->npe + a)] + d)];
+    (elem_has_affine_map(c->elem_type, P) ? c->h_aff : c->h_gen).push_back((int32_t)e);
+  }
+}
+
+lmg_status upload_cmask(lmg_ctx *c) {
+  std::vector<uint64_t> m((size_t)c->n_elem, 0);
+  if (!c->h_constrained.empty())
+    for (int64_t e = 0; e < c->n_elem; ++e)
+      for (int l = 0; l < c->nl; ++l)
+        if (c->h_constrained[(size_t)c->h_elem_dofs[(size_t)(e * c->nl + l)]]) m[(size_t)e] |= 1ull << l;
+  LMG_CUDA(c, dupload(c, c->d_cmask, m.data(), m.size()));
+  LMG_CUDA(c, cudaStreamSynchronize(c->stream));
+  return LMG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+lmg_status lmg_context_create(lmg_ctx **out, int32_t device) {
+  if (!out) return LMG_ERR_ARG;
+  *out = nullptr;
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n <= 0) return LMG_ERR_CUDA;
+  if (device < 0 || device >= n) return LMG_ERR_ARG;
+  lmg_ctx *c = new (std::nothrow) lmg_ctx;
+  if (!c) return LMG_ERR_OOM;
+  c->device = device;
+  if (cudaSetDevice(device) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete c;
+    return LMG_ERR_CUDA;
+  }
+  c->own_stream = true;
+  cudaDeviceGetAttribute(&c->n_sm, cudaDevAttrMultiProcessorCount, device);
+  if (cudaMalloc((void **)&c->d_status, sizeof(int)) != cudaSuccess ||
+      cudaMalloc((void **)&c->d_bad, sizeof(unsigned long long)) != cudaSuccess) {
+    cudaStreamDestroy(c->stream);
+    delete c;
+    return LMG_ERR_OOM;
+  }
+  *out = c;
+  return LMG_OK;
+}
+
+lmg_status lmg_context_destroy(lmg_ctx *c) {
+  if (!c) return LMG_OK;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  dfree(c->d_xyz); dfree(c->d_conn); dfree(c->d_aff); dfree(c->d_gen); dfree(c->d_eb);
+  dfree(c->d_cmask); dfree(c->d_brow_ptr); dfree(c->d_bcol); dfree(c->d_row_ptr); dfree(c->d_col);
+  dfree(c->d_bptr); dfree(c->d_bcontrib); dfree(c->d_fptr); dfree(c->d_fcontrib); dfree(c->d_tab);
+  dfree(c->d_coef); dfree(c->d_f); dfree(c->d_Ke); dfree(c->d_Fe); dfree(c->d_K); dfree(c->d_F);
+  dfree(c->d_Ke32); dfree(c->d_status); dfree(c->d_bad);
+  if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return LMG_OK;
+}
+
+lmg_status lmg_context_set_stream(lmg_ctx *c, void *stream) {
+  if (!c) return LMG_ERR_ARG;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+  c->stream = (cudaStream_t)stream;
+  c->own_stream = false;
+  return LMG_OK;
+}
+
+lmg_status lmg_mesh_upload(lmg_ctx *c, int64_t n_nodes, const double *xyz, int64_t n_elem,
+                           int32_t elem_type, const int32_t *conn) {
+  if (!c || !xyz || !conn || n_nodes <= 0 || n_elem <= 0) return fail(c, LMG_ERR_ARG, "mesh_upload: bad argument");
+  const int npe = nodes_per_elem(elem_type);
+  if (!npe) return fail(c, LMG_ERR_UNSUPPORTED, "mesh_upload: element type not built");
+  if (n_elem * npe >= INT32_MAX || n_nodes >= INT32_MAX) return fail(c, LMG_ERR_UNSUPPORTED, "mesh too large");
+  for (int64_t i = 0; i < n_elem * npe; ++i)
+    if (conn[i] < 0 || conn[i] >= n_nodes) return fail(c, LMG_ERR_BOUNDS, "mesh_upload: node id out of range", i / npe);
+  cudaSetDevice(c->device);
+  c->elem_type = elem_type;
+  c->npe = npe;
+  c->n_nodes = n_nodes;
+  c->n_elem = n_elem;
+  c->h_xyz.assign(xyz, xyz + 3 * n_nodes);
+  c->h_conn.assign(conn, conn + n_elem * npe);
+  build_lists(c);
+  LMG_CUDA(c, dupload(c, c->d_xyz, xyz, (size_t)(3 * n_nodes)));
+  LMG_CUDA(c, dupload(c, c->d_conn, conn, (size_t)(n_elem * npe)));
+  LMG_CUDA(c, dupload(c, c->d_aff, c->h_aff.data(), c->h_aff.size()));
+  LMG_CUDA(c, dupload(c, c->d_gen, c->h_gen.data(), c->h_gen.size()));
+  LMG_CUDA(c, cudaStreamSynchronize(c->stream));
+  c->have_sparsity = false;
+  c->n_vars = 0;
+  return LMG_OK;
+}
+
+lmg_status lmg_dofmap_upload(lmg_ctx *c, int32_t n_vars, int64_t n_dofs, const int32_t *elem_dofs) {
+  if (!c || !elem_dofs || n_vars <= 0 || n_dofs <= 0) return fail(c, LMG_ERR_ARG, "dofmap_upload: bad argument");
+  if (!c->n_elem) return fail(c, LMG_ERR_STATE, "dofmap_upload: upload the mesh first");
+  const int nl = n_vars * c->npe;
+  if (nl > 64) return fail(c, LMG_ERR_UNSUPPORTED, "more than 64 dofs per element");
+  for (int64_t i = 0; i < c->n_elem * nl; ++i)
+    if (elem_dofs[i] < 0 || elem_dofs[i] >= n_dofs) return fail(c, LMG_ERR_BOUNDS, "dof id out of range", i / nl);
+  cudaSetDevice(c->device);
+  c->n_vars = n_vars;
+  c->nl = nl;
+  c->n_dofs = n_dofs;
+  c->h_elem_dofs.assign(elem_dofs, elem_dofs + c->n_elem * nl);
+  detect_blocks(c);
+  LMG_CUDA(c, dupload(c, c->d_eb, c->h_eb.data(), c->h_eb.size()));
+  c->h_constrained.clear();
+  c->have_sparsity = false;
+  return upload_cmask(c);
+}
+
+lmg_status lmg_constraints_upload(lmg_ctx *c, const uint8_t *constrained) {
+  if (!c || !constrained) return fail(c, LMG_ERR_ARG, "constraints_upload: bad argument");
+  if (!c->n_dofs) return fail(c, LMG_ERR_STATE, "constraints_upload: upload the dofmap first");
+  cudaSetDevice(c->device);
+  c->h_constrained.assign(constrained, constrained + c->n_dofs);
+  return upload_cmask(c);
+}
+
+lmg_status lmg_sparsity_build(lmg_ctx *c, int64_t *nnz) {
+  if (!c) return LMG_ERR_ARG;
+  if (!c->n_dofs) return fail(c, LMG_ERR_STATE, "sparsity_build: upload the dofmap first");
+  cudaSetDevice(c->device);
+  std::vector<int64_t> brow;
+  std::vector<int32_t> bcol;
+  const unsigned hw = std::thread::hardware_concurrency();
+  build_block_graph(c->n_elem, c->nb, c->h_eb.data(), c->n_blocks, brow, bcol, hw ? (int)hw : 4);
+  c->nnzb = (int64_t)bcol.size();
+  c->nnz = c->nnzb * c->bs * c->bs;
+  if (c->nnz >= INT32_MAX) return fail(c, LMG_ERR_UNSUPPORTED, "nnz exceeds 32-bit CSR");
+  std::vector<int32_t> row_ptr((size_t)c->n_dofs + 1);
+  row_ptr[0] = 0;
+  for (int64_t r = 0; r < c->n_dofs; ++r) {
+    const int64_t P = r / c->bs;
+    row_ptr[(size_t)r + 1] = row_ptr[(size_t)r] + (int32_t)((brow[(size_t)P + 1] - brow[(size_t)P]) * c->bs);
+  }
+  LMG_CUDA(c, dupload(c, c->d_brow_ptr, brow.data(), brow.size()));
+  LMG_CUDA(c, dupload(c, c->d_bcol, bcol.data(), bcol.size()));
+  LMG_CUDA(c, dupload(c, c->d_row_ptr, row_ptr.data(), row_ptr.size()));
+  LMG_CUDA(c, dalloc(c->d_col, (size_t)c->nnz));
+  k_expand_cols<<<grid_for(c, c->n_dofs * 32, 256), 256, 0, c->stream>>>(
+      c->n_dofs, c->bs, c->d_brow_ptr, c->d_bcol, c->d_row_ptr, c->d_col);
+  c->launches++;
+  lmg_status st = build_plan(c);
+  if (st) return st;
+  LMG_CUDA(c, dalloc(c->d_K, (size_t)c->nnz));
+  LMG_CUDA(c, dalloc(c->d_F, (size_t)c->n_dofs));
+  LMG_CUDA(c, dalloc(c->d_Ke, (size_t)(c->n_elem * c->nl * c->nl)));
+  LMG_CUDA(c, dalloc(c->d_Fe, (size_t)(c->n_elem * c->nl)));
+  c->have_sparsity = true;
+  if (nnz) *nnz = c->nnz;
+  return LMG_OK;
+}
+
+lmg_status lmg_sparsity_copy(lmg_ctx *c, int32_t *row_ptr, int32_t *col_idx) {
+  if (!c) return LMG_ERR_ARG;
+  if (!c->have_sparsity) return fail(c, LMG_ERR_STATE, "sparsity_copy: build the sparsity first");
+  cudaSetDevice(c->device);
+  if (row_ptr)
+    LMG_CUDA(c, cudaMemcpyAsync(row_ptr, c->d_row_ptr, sizeof(int32_t) * (c->n_dofs + 1),
+                                cudaMemcpyDeviceToHost, c->stream));
+  if (col_idx)
+    LMG_CUDA(c, cudaMemcpyAsync(col_idx, c->d_col, sizeof(int32_t) * c->nnz, cudaMemcpyDeviceToHost,
+                                c->stream));
+  LMG_CUDA(c, cudaStreamSynchronize(c->stream));
+  return LMG_OK;
+}
+
+}  // extern "C"
+
+extern "C" {
+
+lmg_status lmg_form_set(lmg_ctx *c, int32_t form, int32_t fe_order, int32_t q_order,
+                        const double *params, int32_t n_params, const double *elem_coef,
+                        const double *nodal_f) {
+  if (!c) return LMG_ERR_ARG;
+  if (!c->n_dofs) return fail(c, LMG_ERR_STATE, "form_set: upload the dofmap first");
+  if (form != LMG_POISSON && form != LMG_ELASTICITY) return fail(c, LMG_ERR_ARG, "form_set: unknown form");
+  if ((form == LMG_POISSON && c->n_vars != 1) || (form == LMG_ELASTICITY && c->n_vars != 3))
+    return fail(c, LMG_ERR_ARG, "form_set: variable count does not match the form");
+  cudaSetDevice(c->device);
+  FETables t;
+  std::string err = build_fe_tables(t, c->elem_type, fe_order, q_order);
+  if (!err.empty()) return fail(c, LMG_ERR_UNSUPPORTED, "form_set: " + err);
+  if (t.n != c->npe || t.n_geo != c->npe)
+    return fail(c, LMG_ERR_UNSUPPORTED, "form_set: only isoparametric LAGRANGE elements are built");
+  c->tab = t;
+  c->form = form;
+  c->fe_order = fe_order;
+  c->q_order = q_order;
+  c->nu = (form == LMG_ELASTICITY && params && n_params > 0) ? params[0] : 0.3;
+  std::vector<double> buf;
+  auto put = [&](const std::vector<double> &v) { size_t o = buf.size(); buf.insert(buf.end(), v.begin(), v.end()); return o; };
+  const size_t oqw = put(t.qw), ophi = put(t.phi), odphi = put(t.dphi), ogd = put(t.gdphi),
+               oS = put(t.S), oM = put(t.M);
+  LMG_CUDA(c, dupload(c, c->d_tab, buf.data(), buf.size()));
+  c->dfe.n = t.n;
+  c->dfe.q = t.q;
+  c->dfe.n_geo = t.n_geo;
+  c->dfe.qw = c->d_tab + oqw;
+  c->dfe.phi = c->d_tab + ophi;
+  c->dfe.dphi = c->d_tab + odphi;
+  c->dfe.gdphi = c->d_tab + ogd;
+  c->dfe.S = c->d_tab + oS;
+  c->dfe.M = c->d_tab + oM;
+  dfree(c->d_coef);
+  dfree(c->d_f);
+  if (elem_coef) LMG_CUDA(c, dupload(c, c->d_coef, elem_coef, (size_t)c->n_elem));
+  if (nodal_f) LMG_CUDA(c, dupload(c, c->d_f, nodal_f, (size_t)(c->n_nodes * c->n_vars)));
+  LMG_CUDA(c, cudaStreamSynchronize(c->stream));
+  c->have_form = true;
+  return LMG_OK;
+}
+
+lmg_status lmg_inputs_update(lmg_ctx *c, const double *xyz, const double *elem_coef,
+                             const double *nodal_f) {
+  if (!c) return LMG_ERR_ARG;
+  if (!c->have_form) return fail(c, LMG_ERR_STATE, "inputs_update: set the form first");
+  cudaSetDevice(c->device);
+  if (xyz) {
+    c->h_xyz.assign(xyz, xyz + 3 * c->n_nodes);
+    build_lists(c);
+    LMG_CUDA(c, cudaMemcpyAsync(c->d_xyz, xyz, sizeof(double) * 3 * c->n_nodes, cudaMemcpyHostToDevice, c->stream));
+    LMG_CUDA(c, dupload(c, c->d_aff, c->h_aff.data(), c->h_aff.size()));
+    LMG_CUDA(c, dupload(c, c->d_gen, c->h_gen.data(), c->h_gen.size()));
+  }
+  if (elem_coef) {
+    if (!c->d_coef) LMG_CUDA(c, dalloc(c->d_coef, (size_t)c->n_elem));
+    LMG_CUDA(c, cudaMemcpyAsync(c->d_coef, elem_coef, sizeof(double) * c->n_elem, cudaMemcpyHostToDevice, c->stream));
+  }
+  if (nodal_f) {
+    if (!c->d_f) LMG_CUDA(c, dalloc(c->d_f, (size_t)(c->n_nodes * c->n_vars)));
+    LMG_CUDA(c, cudaMemcpyAsync(c->d_f, nodal_f, sizeof(double) * c->n_nodes * c->n_vars, cudaMemcpyHostToDevice, c->stream));
+  }
+  return LMG_OK;
+}
+
+lmg_status lmg_assemble(lmg_ctx *c, int32_t precision, double *K, double *F, int32_t out_on_device) {
+  if (!c) return LMG_ERR_ARG;
+  if (!c->have_sparsity) return fail(c, LMG_ERR_STATE, "assemble: build the sparsity first");
+  if (!c->have_form) return fail(c, LMG_ERR_STATE, "assemble: set the form first");
+  if (precision != LMG_FP64 && precision != LMG_MIXED) return fail(c, LMG_ERR_ARG, "assemble: unknown precision");
+  if (precision == LMG_MIXED) return fail(c, LMG_ERR_UNSUPPORTED, "assemble: mixed form not built yet");
+  cudaSetDevice(c->device);
+  lmg_status st = reset_status(c);
+  if (st) return st;
+  ElemArgs a{};
+  a.npe = c->npe;
+  a.xyz = c->d_xyz;
+  a.conn = c->d_conn;
+  a.coef = c->d_coef;
+  a.nodal_f = c->d_f;
+  a.cmask = c->d_cmask;
+  a.nu = c->nu;
+  a.Ke = c->d_Ke;
+  a.Fe = c->d_Fe;
+  a.status = c->d_status;
+  a.bad_elem = c->d_bad;
+  a.fe = c->dfe;
+  const int grid = c->n_sm * 8;
+  cudaEvent_t e3[3] = {nullptr, nullptr, nullptr};
+  if (c->perflog) {
+    for (auto &e : e3) LMG_CUDA(c, cudaEventCreate(&e));
+    for (auto &e : e3) c->ev.push_back(e);
+    LMG_CUDA(c, cudaEventRecord(e3[0], c->stream));
+  }
+  if (!c->h_aff.empty()) {
+    a.n_list = (int64_t)c->h_aff.size();
+    a.list = c->d_aff;
+    launch_elements(c->form, c->tab.n, c->n_vars, true, a, grid, c->stream);
+    c->launches++;
+  }
+  if (!c->h_gen.empty()) {
+    a.n_list = (int64_t)c->h_gen.size();
+    a.list = c->d_gen;
+    launch_elements(c->form, c->tab.n, c->n_vars, false, a, grid, c->stream);
+    c->launches++;
+  }
+  if (c->perflog) LMG_CUDA(c, cudaEventRecord(e3[1], c->stream));
+  GatherArgs g{};
+  g.n_dofs = c->n_dofs;
+  g.bs = c->bs;
+  g.nb = c->nb;
+  g.brow_ptr = c->d_brow_ptr;
+  g.row_ptr = c->d_row_ptr;
+  g.bptr = c->d_bptr;
+  g.bcontrib = c->d_bcontrib;
+  g.fptr = c->d_fptr;
+  g.fcontrib = c->d_fcontrib;
+  g.Ke = c->d_Ke;
+  g.Ke32 = c->d_Ke32;
+  g.Fe = c->d_Fe;
+  g.K = c->d_K;
+  g.F = c->d_F;
+  launch_gather(g, false, c->stream);
+  c->launches++;
+  if (c->perflog) LMG_CUDA(c, cudaEventRecord(e3[2], c->stream));
+  LMG_CUDA(c, cudaGetLastError());
+  const cudaMemcpyKind kind = out_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+  if (K) LMG_CUDA(c, cudaMemcpyAsync(K, c->d_K, sizeof(double) * c->nnz, kind, c->stream));
+  if (F) LMG_CUDA(c, cudaMemcpyAsync(F, c->d_F, sizeof(double) * c->n_dofs, kind, c->stream));
+  // Device outputs stay asynchronous; lmg_synchronize reports their status.
+  if (out_on_device || (!K && !F)) return LMG_OK;
+  return check_status(c, "assemble");
+}
+
+lmg_status lmg_synchronize(lmg_ctx *c) {
+  if (!c) return LMG_ERR_ARG;
+  cudaSetDevice(c->device);
+  LMG_CUDA(c, cudaStreamSynchronize(c->stream));
+  return check_status(c, "assemble");
+}
+
+lmg_status lmg_result_device(lmg_ctx *c, double **K, double **F) {
+  if (!c) return LMG_ERR_ARG;
+  if (K) *K = c->d_K;
+  if (F) *F = c->d_F;
+  return LMG_OK;
+}
+
+lmg_status lmg_last_error(lmg_ctx *c, int64_t *elem_id, char *msg, int32_t msg_len) {
+  if (!c) return LMG_ERR_ARG;
+  if (elem_id) *elem_id = c->err_elem;
+  if (msg && msg_len > 0) {
+    std::strncpy(msg, c->err.c_str(), (size_t)msg_len - 1);
+    msg[msg_len - 1] = 0;
+  }
+  return LMG_OK;
+}
+
+lmg_status lmg_perflog_enable(lmg_ctx *c, int32_t on) {
+  if (!c) return LMG_ERR_ARG;
+  c->perflog = on != 0;
+  return LMG_OK;
+}
+
+lmg_status lmg_perflog_read(lmg_ctx *c, double *elements_ms, double *gather_ms, int64_t *calls) {
+  if (!c) return LMG_ERR_ARG;
+  cudaSetDevice(c->device);
+  LMG_CUDA(c, cudaStreamSynchronize(c->stream));
+  for (size_t i = 0; i + 2 < c->ev.size(); i += 3) {
+    float a = 0, b = 0;
+    LMG_CUDA(c, cudaEventElapsedTime(&a, c->ev[i], c->ev[i + 1]));
+    LMG_CUDA(c, cudaEventElapsedTime(&b, c->ev[i + 1], c->ev[i + 2]));
+    c->log_ms[0] += a;
+    c->log_ms[1] += b;
+    c->log_calls++;
+  }
+  for (auto e : c->ev) cudaEventDestroy(e);
+  c->ev.clear();
+  if (elements_ms) *elements_ms = c->log_ms[0];
+  if (gather_ms) *gather_ms = c->log_ms[1];
+  if (calls) *calls = c->log_calls;
+  c->log_ms[0] = c->log_ms[1] = 0.0;
+  c->log_calls = 0;
+  return LMG_OK;
+}
+
+lmg_status lmg_launch_count(lmg_ctx *c, int64_t *count) {
+  if (!c || !count) return LMG_ERR_ARG;
+  *count = c->launches;
+  return LMG_OK;
+}
+
+}  // extern "C"

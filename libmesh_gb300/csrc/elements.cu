@@ -1,0 +1,338 @@
+// Element kernels: per-element Jacobian, inverse and determinant in FP64 and
+// the weak-form contraction, written to a per-element block buffer that the
+// gather kernel reduces into CSR values.
+//
+// What the reference does per element (the user's assembly callback):
+//   FE::reinit -> FEMap::compute_affine_map | compute_single_point_map
+//     (src/fe/fe_map.C:1167-1245, 980-1078), map_dphi (src/fe/h1_fe_transformation.C:64-195),
+//   then Ke(i,j) += JxW dphi_i.dphi_j (introduction_ex4.C:467) or the
+//   elasticity form (systems_of_equations_ex6.C:222-230), then
+//   constrain_element_matrix_and_vector (src/base/dof_map_constraints.C:2439-2515).
+// Here two kernels cover that:
+//   * k_elem_affine: elements whose map is affine (Elem::has_affine_map).  The
+//     Jacobian is taken once at qp 0 as libMesh does; the quadrature sum is
+//     folded into reference tensors S^{mn}_{ab} = sum_q w_q dphi_a/dxi_m dphi_b/dxi_n,
+//     so Ke_ab = sum_mn A_mn S^{mn}_ab with an element tensor A built from
+//     detJ, J^-1 and the coefficients.  One warp takes 32 elements: lane = element
+//     for the geometry, lane = output block for the contraction.
+//   * k_elem_general: any element; the Jacobian, detJ and J^-1 at every qp,
+//     physical gradients per qp, and accumulation over qps (warp per element).
+// Dirichlet rows/columns are applied in the epilogue: a constrained local dof
+// gets a zero row and column with 1 on the diagonal and a zero load, which is
+// what C^T K C and C^T F give for an empty constraint row.
+#include <cuda_runtime.h>
+
+#include "assemble.cuh"
+#include "../../include/libmesh_gb300.h"
+
+namespace lmg {
+
+namespace {
+
+constexpr unsigned FULL = 0xffffffffu;
+
+// Jacobian at one point from the mapping shape derivatives gd [n_geo][3] and
+// element coordinates X [n_geo][3]; returns detJ and G[m][d] = dxi_m / dx_d.
+__device__ __forceinline__ double jacobian(const double *X, const double *gd, int n_geo,
+                                           double G[9]) {
+  double J[9];  // J[m*3+d] = d x_d / d xi_m
+#pragma unroll
+  for (int i = 0; i < 9; ++i) J[i] = 0.0;
+  for (int a = 0; a < n_geo; ++a) {
+    const double x = X[3 * a], y = X[3 * a + 1], z = X[3 * a + 2];
+#pragma unroll
+    for (int m = 0; m < 3; ++m) {
+      const double g = gd[3 * a + m];
+      J[3 * m + 0] += x * g;
+      J[3 * m + 1] += y * g;
+      J[3 * m + 2] += z * g;
+    }
+  }
+  const double xxi = J[0], yxi = J[1], zxi = J[2];
+  const double xet = J[3], yet = J[4], zet = J[5];
+  const double xze = J[6], yze = J[7], zze = J[8];
+  const double c0 = yet * zze - zet * yze, c1 = zet * xze - xet * zze, c2 = xet * yze - yet * xze;
+  const double det = xxi * c0 + yxi * c1 + zxi * c2;
+  const double inv = 1.0 / det;
+  G[0] = c0 * inv;
+  G[1] = c1 * inv;
+  G[2] = c2 * inv;
+  G[3] = (zxi * yze - yxi * zze) * inv;
+  G[4] = (xxi * zze - zxi * xze) * inv;
+  G[5] = (yxi * xze - xxi * yze) * inv;
+  G[6] = (yxi * zet - zxi * yet) * inv;
+  G[7] = (zxi * xet - xxi * zet) * inv;
+  G[8] = (xxi * yet - yxi * xet) * inv;
+  return det;
+}
+
+__device__ __forceinline__ void report_bad(const ElemArgs &a, int code, int64_t e) {
+  atomicCAS(a.status, 0, code);
+  atomicMin(a.bad_elem, (unsigned long long)e);
+}
+
+// Lamé constants of libMesh's elasticity_tensor with Young's modulus E.
+__device__ __forceinline__ void lame(double E, double nu, double &lam, double &mu) {
+  lam = (E * nu) / ((1. + nu) * (1. - 2. * nu));
+  mu = E / (2. * (1. + nu));
+}
+
+// Element tensor A of the affine path.
+//   POISSON:    A[mn]      = k detJ (G G^T)_mn
+//   ELASTICITY: A[ik][mn]  = detJ (lam G_mi G_nk + mu G_mk G_ni + mu d_ik (G G^T)_mn)
+template <int FORM>
+__device__ __forceinline__ void element_tensor(const double G[9], double det, double coef,
+                                               double nu, double *A) {
+  double GG[9];
+#pragma unroll
+  for (int m = 0; m < 3; ++m)
+#pragma unroll
+    for (int n = 0; n < 3; ++n)
+      GG[3 * m + n] = G[3 * m] * G[3 * n] + G[3 * m + 1] * G[3 * n + 1] + G[3 * m + 2] * G[3 * n + 2];
+  if (FORM == LMG_POISSON) {
+    const double s = coef * det;
+#pragma unroll
+    for (int i = 0; i < 9; ++i) A[i] = s * GG[i];
+  } else {
+    double lam, mu;
+    lame(coef, nu, lam, mu);
+    lam *= det;
+    mu *= det;
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int k = 0; k < 3; ++k)
+#pragma unroll
+        for (int m = 0; m < 3; ++m)
+#pragma unroll
+          for (int n = 0; n < 3; ++n) {
+            double v = lam * G[3 * m + i] * G[3 * n + k] + mu * G[3 * m + k] * G[3 * n + i];
+            if (i == k) v += mu * GG[3 * m + n];
+            A[(3 * i + k) * 9 + 3 * m + n] = v;
+          }
+  }
+}
+
+template <int FORM, int N, int NV>
+__global__ void __launch_bounds__(128) k_elem_affine(ElemArgs a) {
+  constexpr int NA = (FORM == LMG_POISSON) ? 9 : 81;
+  constexpr int NB = N * N;
+  constexpr int BPL = (NB + 31) / 32;
+  extern __shared__ double smem[];
+  double *sS = smem;                                   // [9][N][N]
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  double *sA = sS + 9 * NB + warp * 32 * NA;           // [32][NA]
+  uint64_t *sMask = reinterpret_cast<uint64_t *>(smem + 9 * NB + 4 * 32 * NA) + warp * 32;
+  for (int i = threadIdx.x; i < 9 * NB; i += blockDim.x) sS[i] = a.fe.S[i];
+  __syncthreads();
+
+  const int64_t n_tiles = (a.n_list + 31) / 32;
+  for (int64_t tile = (int64_t)blockIdx.x * 4 + warp; tile < n_tiles; tile += (int64_t)gridDim.x * 4) {
+    const int64_t li = tile * 32 + lane;
+    const int32_t e = (li < a.n_list) ? a.list[li] : -1;
+    if (e >= 0) {
+      double X[N * 3];
+      const int32_t *c = a.conn + (int64_t)e * a.npe;
+#pragma unroll
+      for (int g = 0; g < N; ++g) {
+        const double *p = a.xyz + 3 * (int64_t)c[g];
+        X[3 * g] = p[0];
+        X[3 * g + 1] = p[1];
+        X[3 * g + 2] = p[2];
+      }
+      double G[9];
+      const double det = jacobian(X, a.fe.gdphi, N, G);
+      if (!(det > 0.0)) report_bad(a, LMG_ERR_DEGENERATE, e);
+      const double coef = a.coef ? a.coef[e] : 1.0;
+      element_tensor<FORM>(G, det, coef, a.nu, sA + lane * NA);
+      const uint64_t mask = a.cmask[e];
+      sMask[lane] = mask;
+      // Load vector: Fe_a^i = detJ sum_b M_ab f_b^i (f interpolated with phi).
+      double *Fo = a.Fe + (int64_t)e * N * NV;
+      for (int ai = 0; ai < N; ++ai)
+        for (int v = 0; v < NV; ++v) {
+          double s = 0.0;
+          if (a.nodal_f)
+            for (int b = 0; b < N; ++b)
+              s += a.fe.M[ai * N + b] * a.nodal_f[(int64_t)c[b] * NV + v];
+          s *= det;
+          if ((mask >> (v * N + ai)) & 1ull) s = 0.0;
+          Fo[ai * NV + v] = s;
+        }
+    }
+    __syncwarp();
+    for (int t = 0; t < 32; ++t) {
+      const int32_t et = __shfl_sync(FULL, e, t);
+      if (et < 0) break;
+      const double *At = sA + t * NA;
+      const uint64_t mask = sMask[t];
+      double *Ko = a.Ke + (int64_t)et * NB * NV * NV;
+#pragma unroll
+      for (int k = 0; k < BPL; ++k) {
+        const int blk = lane + 32 * k;
+        if (blk < NB) {
+          const int ra = blk / N, cb = blk - ra * N;
+          double sv[9];
+#pragma unroll
+          for (int mn = 0; mn < 9; ++mn) sv[mn] = sS[mn * NB + blk];
+#pragma unroll
+          for (int ik = 0; ik < NV * NV; ++ik) {
+            const int i = ik / NV, kk = ik - i * NV;
+            double acc = 0.0;
+#pragma unroll
+            for (int mn = 0; mn < 9; ++mn) acc = fma(At[ik * 9 + mn], sv[mn], acc);
+            const int lr = i * N + ra, lc = kk * N + cb;
+            if (((mask >> lr) | (mask >> lc)) & 1ull) acc = (lr == lc) ? 1.0 : 0.0;
+            Ko[blk * NV * NV + ik] = acc;
+          }
+        }
+      }
+    }
+    __syncwarp();
+  }
+}
+
+template <int FORM, int N, int NV>
+__global__ void __launch_bounds__(128) k_elem_general(ElemArgs a) {
+  constexpr int NB = N * N;
+  constexpr int BPL = (NB + 31) / 32;
+  constexpr int MAXQ = 27;
+  __shared__ double sX[4][27 * 3];
+  __shared__ double sGeo[4][MAXQ][10];  // G (9) and JxW per qp
+  __shared__ double sGr[4][N * 3];      // physical gradients at the current qp
+  __shared__ double sF[4][N * NV];      // nodal load of the element
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int n_geo = a.fe.n_geo, Q = a.fe.q;
+  for (int64_t li = (int64_t)blockIdx.x * 4 + warp; li < a.n_list; li += (int64_t)gridDim.x * 4) {
+    const int32_t e = a.list[li];
+    const int32_t *c = a.conn + (int64_t)e * a.npe;
+    for (int i = lane; i < n_geo * 3; i += 32) sX[warp][i] = a.xyz[3 * (int64_t)c[i / 3] + i % 3];
+    for (int i = lane; i < N * NV; i += 32)
+      sF[warp][i] = a.nodal_f ? a.nodal_f[(int64_t)c[i / NV] * NV + i % NV] : 0.0;
+    __syncwarp();
+    const double coef = a.coef ? a.coef[e] : 1.0;
+    for (int q = lane; q < Q; q += 32) {
+      double G[9];
+      const double det = jacobian(sX[warp], a.fe.gdphi + (int64_t)q * n_geo * 3, n_geo, G);
+      if (!(det > 0.0)) report_bad(a, LMG_ERR_DEGENERATE, e);
+      for (int i = 0; i < 9; ++i) sGeo[warp][q][i] = G[i];
+      sGeo[warp][q][9] = det * a.fe.qw[q];
+    }
+    __syncwarp();
+    double lam = 0.0, mu = 0.0;
+    if (FORM == LMG_ELASTICITY) lame(coef, a.nu, lam, mu);
+    double acc[BPL][NV * NV];
+#pragma unroll
+    for (int k = 0; k < BPL; ++k)
+#pragma unroll
+      for (int ik = 0; ik < NV * NV; ++ik) acc[k][ik] = 0.0;
+    double facc[NV];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) facc[v] = 0.0;
+    for (int q = 0; q < Q; ++q) {
+      const double *Gq = sGeo[warp][q];
+      for (int i = lane; i < N * 3; i += 32) {
+        const int ai = i / 3, d = i - 3 * ai;
+        const double *r = a.fe.dphi + ((int64_t)q * N + ai) * 3;
+        sGr[warp][i] = r[0] * Gq[d] + r[1] * Gq[3 + d] + r[2] * Gq[6 + d];
+      }
+      __syncwarp();
+      const double jxw = Gq[9];
+#pragma unroll
+      for (int k = 0; k < BPL; ++k) {
+        const int blk = lane + 32 * k;
+        if (blk < NB) {
+          const int ra = blk / N, cb = blk - ra * N;
+          const double *ga = sGr[warp] + 3 * ra, *gb = sGr[warp] + 3 * cb;
+          const double dot = ga[0] * gb[0] + ga[1] * gb[1] + ga[2] * gb[2];
+          if (FORM == LMG_POISSON) {
+            acc[k][0] += jxw * coef * dot;
+          } else {
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+              for (int kk = 0; kk < 3; ++kk) {
+                double v = lam * ga[i] * gb[kk] + mu * ga[kk] * gb[i];
+                if (i == kk) v += mu * dot;
+                acc[k][3 * i + kk] += jxw * v;
+              }
+          }
+        }
+      }
+      if (lane < N) {  // load vector, lane = shape a
+        const double *ph = a.fe.phi + (int64_t)q * N;
+#pragma unroll
+        for (int v = 0; v < NV; ++v) {
+          double fq = 0.0;
+          for (int b = 0; b < N; ++b) fq += ph[b] * sF[warp][b * NV + v];
+          facc[v] += jxw * fq * ph[lane];
+        }
+      }
+      __syncwarp();
+    }
+    const uint64_t mask = a.cmask[e];
+    double *Ko = a.Ke + (int64_t)e * NB * NV * NV;
+#pragma unroll
+    for (int k = 0; k < BPL; ++k) {
+      const int blk = lane + 32 * k;
+      if (blk < NB) {
+        const int ra = blk / N, cb = blk - ra * N;
+#pragma unroll
+        for (int ik = 0; ik < NV * NV; ++ik) {
+          const int i = ik / NV, kk = ik - i * NV;
+          const int lr = i * N + ra, lc = kk * N + cb;
+          double v = acc[k][ik];
+          if (((mask >> lr) | (mask >> lc)) & 1ull) v = (lr == lc) ? 1.0 : 0.0;
+          Ko[blk * NV * NV + ik] = v;
+        }
+      }
+    }
+    if (lane < N) {
+#pragma unroll
+      for (int v = 0; v < NV; ++v) {
+        double s = facc[v];
+        if ((mask >> (v * N + lane)) & 1ull) s = 0.0;
+        a.Fe[((int64_t)e * N + lane) * NV + v] = s;
+      }
+    }
+    __syncwarp();
+  }
+}
+
+template <int FORM, int N, int NV>
+void launch_t(bool affine, const ElemArgs &a, int grid, cudaStream_t s) {
+  if (a.n_list <= 0) return;
+  if (affine) {
+    constexpr int NA = (FORM == LMG_POISSON) ? 9 : 81;
+    const size_t sm = sizeof(double) * (9 * N * N + 4 * 32 * NA) + sizeof(uint64_t) * 4 * 32;
+    cudaFuncSetAttribute(k_elem_affine<FORM, N, NV>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)sm);
+    const int64_t tiles = (a.n_list + 31) / 32;
+    const int64_t blocks = (tiles + 3) / 4;
+    k_elem_affine<FORM, N, NV><<<(int)(blocks < grid ? blocks : grid), 128, sm, s>>>(a);
+  } else {
+    const int64_t blocks = (a.n_list + 3) / 4;
+    k_elem_general<FORM, N, NV><<<(int)(blocks < grid ? blocks : grid), 128, 0, s>>>(a);
+  }
+}
+
+}  // namespace
+
+void launch_elements(int form, int n, int nv, bool affine, const ElemArgs &a, int grid,
+                     cudaStream_t s) {
+#define LMG_CASE(F, NN, V)                                   \
+  if (form == F && n == NN && nv == V) {                     \
+    launch_t<F, NN, V>(affine, a, grid, s);                  \
+    return;                                                  \
+  }
+  LMG_CASE(LMG_POISSON, 4, 1)
+  LMG_CASE(LMG_POISSON, 8, 1)
+  LMG_CASE(LMG_POISSON, 10, 1)
+  LMG_CASE(LMG_POISSON, 27, 1)
+  LMG_CASE(LMG_ELASTICITY, 4, 3)
+  LMG_CASE(LMG_ELASTICITY, 8, 3)
+  LMG_CASE(LMG_ELASTICITY, 10, 3)
+#undef LMG_CASE
+}
+
+}  // namespace lmg

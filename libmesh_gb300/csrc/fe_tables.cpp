@@ -1,0 +1,276 @@
+// Reference-element tables for the element kernels: QGauss points and weights,
+// LAGRANGE shape values and reference gradients at those points, and the
+// reference tensors used by the affine fast path.  Built once per
+// (element type, FE order, quadrature order) on the host and uploaded.
+//
+// Rules follow libMesh's QGauss (src/quadrature/quadrature_gauss_1D.C:30-80,
+// src/quadrature/quadrature_gauss_3D.C:30-226, src/quadrature/quadrature.C:283-305):
+// an order-p rule integrates degree-p polynomials exactly, hexes use the
+// tensor product with the first coordinate fastest, tets use the published
+// Zienkiewicz-Taylor (orders 1-3) and Keast (order 4, 11 points, one negative
+// weight) rules.  The 1D Gauss-Legendre nodes are computed here by Newton
+// iteration on P_n in long double.
+#include <cmath>
+
+#include "lmg_internal.h"
+
+namespace lmg {
+
+namespace {
+
+void gauss_legendre(int np, std::vector<double> &x, std::vector<double> &w) {
+  x.assign(np, 0.0);
+  w.assign(np, 0.0);
+  const long double pi = 3.141592653589793238462643383279502884L;
+  for (int i = 0; i < np; ++i) {
+    // i-th node from the left: cos(pi (np - i - 0.25) / (np + 0.5)) start.
+    long double z = cosl(pi * (np - i - 0.25L) / (np + 0.5L));
+    long double dp = 0;
+    for (int it = 0; it < 100; ++it) {
+      long double p0 = 1, p1 = z;
+      for (int k = 2; k <= np; ++k) {
+        long double p2 = ((2 * k - 1) * z * p1 - (k - 1) * p0) / k;
+        p0 = p1;
+        p1 = p2;
+      }
+      if (np == 1) { p1 = z; p0 = 1; }
+      dp = np * (z * p1 - p0) / (z * z - 1);
+      long double dz = p1 / dp;
+      z -= dz;
+      if (fabsl(dz) < 1e-30L) break;
+    }
+    long double p0 = 1, p1 = z;
+    for (int k = 2; k <= np; ++k) {
+      long double p2 = ((2 * k - 1) * z * p1 - (k - 1) * p0) / k;
+      p0 = p1;
+      p1 = p2;
+    }
+    dp = (np == 1) ? 1.0L : np * (z * p1 - p0) / (z * z - 1);
+    x[i] = (double)z;
+    w[i] = (double)(2.0L / ((1 - z * z) * dp * dp));
+  }
+  if (np % 2 == 1) x[np / 2] = 0.0;  // the middle node is exactly zero
+  for (int i = 0; i < np / 2; ++i) {  // exact symmetry, as libMesh stores it
+    x[np - 1 - i] = -x[i];
+    w[np - 1 - i] = w[i];
+  }
+}
+
+void tet_rule(int order, std::vector<double> &p, std::vector<double> &w) {
+  p.clear();
+  w.clear();
+  auto add = [&](double a, double b, double c, double wt) {
+    p.push_back(a); p.push_back(b); p.push_back(c); w.push_back(wt);
+  };
+  if (order <= 1) {
+    add(0.25, 0.25, 0.25, 1.0 / 6.0);
+  } else if (order == 2) {
+    const double b = 0.25 * (1.0 - std::sqrt(5.0) / 5.0), a = 1.0 - 3.0 * b;
+    add(a, b, b, 1.0 / 24); add(b, a, b, 1.0 / 24); add(b, b, a, 1.0 / 24); add(b, b, b, 1.0 / 24);
+  } else if (order == 3) {
+    add(0.25, 0.25, 0.25, -2.0 / 15.0);
+    add(0.5, 1.0 / 6, 1.0 / 6, 0.075); add(1.0 / 6, 0.5, 1.0 / 6, 0.075);
+    add(1.0 / 6, 1.0 / 6, 0.5, 0.075); add(1.0 / 6, 1.0 / 6, 1.0 / 6, 0.075);
+  } else {
+    // Keast (1986) degree-4 rule: centroid, a 4-orbit and a 6-orbit.
+    add(0.25, 0.25, 0.25, -74.0 / 5625.0);
+    const double a4 = 11.0 / 14.0, b4 = 1.0 / 14.0, w4 = 343.0 / 45000.0;
+    add(a4, b4, b4, w4); add(b4, a4, b4, w4); add(b4, b4, a4, w4); add(b4, b4, b4, w4);
+    const double s = std::sqrt(5.0 / 14.0);
+    const double a6 = 0.25 * (1.0 + s), b6 = 0.25 * (1.0 - s), w6 = 56.0 / 2250.0;
+    add(a6, a6, b6, w6); add(a6, b6, b6, w6); add(b6, b6, a6, w6);
+    add(b6, a6, b6, w6); add(b6, a6, a6, w6); add(a6, b6, a6, w6);
+  }
+}
+
+// Hex node -> 1D index tables (the node numbering of libMesh's HEX8 / HEX27).
+const int HEX8_I[3][8] = {{0, 1, 1, 0, 0, 1, 1, 0}, {0, 0, 1, 1, 0, 0, 1, 1}, {0, 0, 0, 0, 1, 1, 1, 1}};
+const int HEX27_I[3][27] = {
+    {0, 1, 1, 0, 0, 1, 1, 0, 2, 1, 2, 0, 0, 1, 1, 0, 2, 1, 2, 0, 2, 2, 1, 2, 0, 2, 2},
+    {0, 0, 1, 1, 0, 0, 1, 1, 0, 2, 1, 2, 0, 0, 1, 1, 0, 2, 1, 2, 2, 0, 2, 1, 2, 2, 2},
+    {0, 0, 0, 0, 1, 1, 1, 1, 0, 0, 0, 0, 2, 2, 2, 2, 1, 1, 1, 1, 0, 2, 2, 2, 2, 1, 2}};
+
+void l1d(int order, int i, double x, double &v, double &d) {
+  if (order == 1) {
+    v = (i == 0) ? 0.5 * (1.0 - x) : 0.5 * (1.0 + x);
+    d = (i == 0) ? -0.5 : 0.5;
+  } else {
+    if (i == 0) { v = 0.5 * x * (x - 1.0); d = x - 0.5; }
+    else if (i == 1) { v = 0.5 * x * (x + 1.0); d = x + 0.5; }
+    else { v = 1.0 - x * x; d = -2.0 * x; }
+  }
+}
+
+// Values and reference gradients of the n LAGRANGE shapes at point p.
+int lagrange_shapes(int type, int order, const double *p, double *v, double *g) {
+  if (type == LMG_HEX8 || type == LMG_HEX27) {
+    const int n = (order == 1) ? 8 : 27;
+    if (order == 2 && type != LMG_HEX27) return 0;
+    for (int a = 0; a < n; ++a) {
+      double s[3], ds[3];
+      for (int m = 0; m < 3; ++m) {
+        const int idx = (order == 1) ? HEX8_I[m][a] : HEX27_I[m][a];
+        l1d(order, idx, p[m], s[m], ds[m]);
+      }
+      v[a] = s[0] * s[1] * s[2];
+      g[3 * a + 0] = ds[0] * s[1] * s[2];
+      g[3 * a + 1] = s[0] * ds[1] * s[2];
+      g[3 * a + 2] = s[0] * s[1] * ds[2];
+    }
+    return n;
+  }
+  if (type == LMG_TET4 || type == LMG_TET10) {
+    const double z[4] = {1.0 - p[0] - p[1] - p[2], p[0], p[1], p[2]};
+    const double dz[4][3] = {{-1, -1, -1}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+    if (order == 1) {
+      for (int a = 0; a < 4; ++a) {
+        v[a] = z[a];
+        for (int m = 0; m < 3; ++m) g[3 * a + m] = dz[a][m];
+      }
+      return 4;
+    }
+    if (type != LMG_TET10) return 0;
+    static const int EV[6][2] = {{0, 1}, {1, 2}, {2, 0}, {0, 3}, {1, 3}, {2, 3}};
+    for (int a = 0; a < 4; ++a) {
+      v[a] = z[a] * (2.0 * z[a] - 1.0);
+      for (int m = 0; m < 3; ++m) g[3 * a + m] = (4.0 * z[a] - 1.0) * dz[a][m];
+    }
+    for (int k = 0; k < 6; ++k) {
+      const int i = EV[k][0], j = EV[k][1];
+      v[4 + k] = 4.0 * z[i] * z[j];
+      for (int m = 0; m < 3; ++m) g[3 * (4 + k) + m] = 4.0 * (z[i] * dz[j][m] + dz[i][m] * z[j]);
+    }
+    return 10;
+  }
+  return 0;
+}
+
+}  // namespace
+
+std::string build_fe_tables(FETables &t, int type, int fe_order, int q_order) {
+  t = FETables();
+  t.elem_type = type;
+  t.fe_order = fe_order;
+  t.q_order = q_order;
+  if (fe_order < 1 || fe_order > 2) return "fe_order must be FIRST or SECOND";
+  const bool hex = (type == LMG_HEX8 || type == LMG_HEX27);
+  const bool tet = (type == LMG_TET4 || type == LMG_TET10);
+  if (!hex && !tet) return "unsupported element type";
+  const int geo_order = (type == LMG_HEX27 || type == LMG_TET10) ? 2 : 1;
+  if (hex) {
+    std::vector<double> x, w;
+    gauss_legendre(q_order / 2 + 1, x, w);
+    const int np = (int)x.size();
+    for (int k = 0; k < np; ++k)
+      for (int j = 0; j < np; ++j)
+        for (int i = 0; i < np; ++i) {
+          t.qp.push_back(x[i]); t.qp.push_back(x[j]); t.qp.push_back(x[k]);
+          t.qw.push_back(w[i] * w[j] * w[k]);
+        }
+  } else {
+    if (q_order > 4) return "tet quadrature above FOURTH is not built";
+    tet_rule(q_order, t.qp, t.qw);
+  }
+  t.q = (int)t.qw.size();
+  double v[27], g[81];
+  t.n = lagrange_shapes(type, fe_order, &t.qp[0], v, g);
+  t.n_geo = lagrange_shapes(type, geo_order, &t.qp[0], v, g);
+  if (!t.n || !t.n_geo) return "unsupported element type / order";
+  t.phi.resize((size_t)t.q * t.n);
+  t.dphi.resize((size_t)t.q * t.n * 3);
+  t.gphi.resize((size_t)t.q * t.n_geo);
+  t.gdphi.resize((size_t)t.q * t.n_geo * 3);
+  for (int q = 0; q < t.q; ++q) {
+    lagrange_shapes(type, fe_order, &t.qp[3 * q], v, g);
+    for (int a = 0; a < t.n; ++a) {
+      t.phi[(size_t)q * t.n + a] = v[a];
+      for (int m = 0; m < 3; ++m) t.dphi[((size_t)q * t.n + a) * 3 + m] = g[3 * a + m];
+    }
+    lagrange_shapes(type, geo_order, &t.qp[3 * q], v, g);
+    for (int a = 0; a < t.n_geo; ++a) {
+      t.gphi[(size_t)q * t.n_geo + a] = v[a];
+      for (int m = 0; m < 3; ++m) t.gdphi[((size_t)q * t.n_geo + a) * 3 + m] = g[3 * a + m];
+    }
+  }
+  const int n = t.n;
+  t.S.assign((size_t)9 * n * n, 0.0);
+  t.M.assign((size_t)n * n, 0.0);
+  for (int q = 0; q < t.q; ++q)
+    for (int a = 0; a < n; ++a)
+      for (int b = 0; b < n; ++b) {
+        t.M[(size_t)a * n + b] += t.qw[q] * t.phi[(size_t)q * n + a] * t.phi[(size_t)q * n + b];
+        for (int m = 0; m < 3; ++m)
+          for (int mm = 0; mm < 3; ++mm)
+            t.S[(((size_t)(m * 3 + mm) * n) + a) * n + b] +=
+                t.qw[q] * t.dphi[((size_t)q * n + a) * 3 + m] * t.dphi[((size_t)q * n + b) * 3 + mm];
+      }
+  return "";
+}
+
+namespace {
+// libMesh relative_fuzzy_equals on 3-vectors (include/utils/fuzzy_equals.h:78-84):
+// l1(a - b) <= tol * (l1(a) + l1(b)), with affine_tol = TOLERANCE^2 = 1e-12.
+bool rfe(const double *a, const double *b) {
+  const double tol = 1e-6 * 1e-6;
+  double d = 0, na = 0, nb = 0;
+  for (int i = 0; i < 3; ++i) {
+    d += std::fabs(a[i] - b[i]);
+    na += std::fabs(a[i]);
+    nb += std::fabs(b[i]);
+  }
+  return d <= tol * (na + nb);
+}
+void sub(const double *P, int i, int j, double *o) {
+  for (int d = 0; d < 3; ++d) o[d] = P[3 * i + d] - P[3 * j + d];
+}
+}  // namespace
+
+bool elem_has_affine_map(int type, const double *P) {
+  double v[3], w[3];
+  switch (type) {
+    case LMG_TET4:
+      return true;
+    case LMG_TET10: {  // cell_tet10.C:143-172
+      static const int E[6][3] = {{1, 0, 4}, {2, 1, 5}, {2, 0, 6}, {3, 0, 7}, {3, 1, 8}, {3, 2, 9}};
+      for (int k = 0; k < 6; ++k) {
+        sub(P, E[k][0], E[k][1], v);
+        sub(P, E[k][2], E[k][1], w);
+        for (int d = 0; d < 3; ++d) w[d] *= 2;
+        if (!rfe(v, w)) return false;
+      }
+      return true;
+    }
+    case LMG_HEX8: {  // cell_hex8.C:121-135
+      sub(P, 1, 0, v);
+      sub(P, 2, 3, w); if (!rfe(v, w)) return false;
+      sub(P, 5, 4, w); if (!rfe(v, w)) return false;
+      sub(P, 6, 7, w); if (!rfe(v, w)) return false;
+      sub(P, 4, 0, v);
+      sub(P, 7, 3, w); return rfe(v, w);
+    }
+    case LMG_HEX27: {  // cell_hex27.C:125-170
+      sub(P, 1, 0, v);
+      sub(P, 2, 3, w); if (!rfe(v, w)) return false;
+      sub(P, 5, 4, w); if (!rfe(v, w)) return false;
+      sub(P, 6, 7, w); if (!rfe(v, w)) return false;
+      for (int d = 0; d < 3; ++d) v[d] /= 2;
+      static const int X[9][2] = {{8, 0}, {10, 3}, {16, 4}, {18, 7}, {20, 11},
+                                  {21, 12}, {23, 15}, {25, 19}, {26, 24}};
+      for (auto &p : X) { sub(P, p[0], p[1], w); if (!rfe(v, w)) return false; }
+      sub(P, 4, 0, v);
+      sub(P, 7, 3, w); if (!rfe(v, w)) return false;
+      for (int d = 0; d < 3; ++d) v[d] /= 2;
+      static const int Z[6][2] = {{12, 0}, {13, 1}, {14, 2}, {15, 3}, {22, 9}, {24, 11}};
+      for (auto &p : Z) { sub(P, p[0], p[1], w); if (!rfe(v, w)) return false; }
+      sub(P, 3, 0, v);
+      for (int d = 0; d < 3; ++d) v[d] /= 2;
+      static const int Y[4][2] = {{11, 0}, {9, 1}, {17, 5}, {19, 4}};
+      for (auto &p : Y) { sub(P, p[0], p[1], w); if (!rfe(v, w)) return false; }
+      return true;
+    }
+    default:
+      return false;
+  }
+}
+
+}  // namespace lmg

@@ -1,0 +1,192 @@
+// Host mirror of libMesh's DofMap setup: dof numbering, dof_indices,
+// Dirichlet constraint sets and the element-coupling sparsity graph.
+#include <algorithm>
+#include <atomic>
+#include <new>
+#include <thread>
+
+#include "lmg_internal.h"
+
+namespace lmg {
+
+// Block graph: row P holds every block Q that shares an element with P,
+// sorted ascending.  This is SparsityPattern::Build with DefaultCoupling(0)
+// and full variable coupling (src/base/sparsity_pattern.C:279-363): every row
+// of an element couples every column of the same element.
+void build_block_graph(int64_t n_elem, int nb, const int32_t *eb, int64_t n_blocks,
+                       std::vector<int64_t> &row_ptr, std::vector<int32_t> &cols, int n_threads) {
+  // block -> elements (CSR), elements listed once per block they touch
+  std::vector<int64_t> bptr((size_t)n_blocks + 1, 0);
+  for (int64_t i = 0; i < n_elem * nb; ++i) bptr[(size_t)eb[i] + 1]++;
+  for (int64_t b = 0; b < n_blocks; ++b) bptr[(size_t)b + 1] += bptr[(size_t)b];
+  std::vector<int32_t> belem((size_t)bptr[(size_t)n_blocks]);
+  {
+    std::vector<int64_t> cur(bptr.begin(), bptr.end() - 1);
+    for (int64_t e = 0; e < n_elem; ++e)
+      for (int a = 0; a < nb; ++a) belem[(size_t)cur[(size_t)eb[e * nb + a]]++] = (int32_t)e;
+  }
+  if (n_threads < 1) n_threads = 1;
+  std::vector<int64_t> deg((size_t)n_blocks, 0);
+  // pass 1: degrees; pass 2: fill.  Each pass sorts the candidate list of a row.
+  auto row_cols = [&](int64_t P, std::vector<int32_t> &buf) {
+    buf.clear();
+    for (int64_t k = bptr[(size_t)P]; k < bptr[(size_t)P + 1]; ++k) {
+      const int32_t *b = eb + (int64_t)belem[(size_t)k] * nb;
+      buf.insert(buf.end(), b, b + nb);
+    }
+    std::sort(buf.begin(), buf.end());
+    buf.erase(std::unique(buf.begin(), buf.end()), buf.end());
+  };
+  auto run = [&](auto &&fn) {
+    std::atomic<int64_t> next{0};
+    std::vector<std::thread> th;
+    for (int t = 0; t < n_threads; ++t)
+      th.emplace_back([&]() {
+        std::vector<int32_t> buf;
+        const int64_t chunk = 4096;
+        for (;;) {
+          int64_t s = next.fetch_add(chunk);
+          if (s >= n_blocks) break;
+          int64_t e = std::min(n_blocks, s + chunk);
+          for (int64_t P = s; P < e; ++P) fn(P, buf);
+        }
+      });
+    for (auto &t : th) t.join();
+  };
+  run([&](int64_t P, std::vector<int32_t> &buf) {
+    row_cols(P, buf);
+    deg[(size_t)P] = (int64_t)buf.size();
+  });
+  row_ptr.assign((size_t)n_blocks + 1, 0);
+  for (int64_t P = 0; P < n_blocks; ++P) row_ptr[(size_t)P + 1] = row_ptr[(size_t)P] + deg[(size_t)P];
+  cols.resize((size_t)row_ptr[(size_t)n_blocks]);
+  run([&](int64_t P, std::vector<int32_t> &buf) {
+    row_cols(P, buf);
+    std::copy(buf.begin(), buf.end(), cols.begin() + row_ptr[(size_t)P]);
+  });
+}
+
+void block_structure(int64_t n_elem, int npe, int nv, const int32_t *ed, int &bs, int &nb,
+                     std::vector<int32_t> &eb) {
+  const int nl = nv * npe;
+  bool ok = nv > 1;
+  for (int64_t e = 0; ok && e < n_elem; ++e) {
+    const int32_t *d = ed + e * nl;
+    for (int a = 0; ok && a < npe; ++a) {
+      if (d[a] % nv != 0) ok = false;
+      for (int v = 1; ok && v < nv; ++v) ok = (d[v * npe + a] == d[a] + v);
+    }
+  }
+  bs = ok ? nv : 1;
+  nb = ok ? npe : nl;
+  eb.resize((size_t)(n_elem * nb));
+  for (int64_t e = 0; e < n_elem; ++e)
+    for (int a = 0; a < nb; ++a) eb[(size_t)(e * nb + a)] = ed[e * nl + a] / bs;
+}
+
+}  // namespace lmg
+
+extern "C" {
+
+lmg_status lmg_host_sparsity(int64_t n_elem, int32_t npe, int32_t n_vars, int64_t n_dofs,
+                             const int32_t *elem_dofs, int64_t *nnz, int32_t *row_ptr, int32_t *col_idx) {
+  if (!elem_dofs || !nnz || n_elem <= 0 || npe <= 0 || n_vars <= 0 || n_dofs <= 0) return LMG_ERR_ARG;
+  try {
+    int bs = 1, nb = 0;
+    std::vector<int32_t> eb;
+    lmg::block_structure(n_elem, npe, n_vars, elem_dofs, bs, nb, eb);
+    std::vector<int64_t> brow;
+    std::vector<int32_t> bcol;
+    const unsigned hw = std::thread::hardware_concurrency();
+    lmg::build_block_graph(n_elem, nb, eb.data(), n_dofs / bs, brow, bcol, hw ? (int)hw : 4);
+    const int64_t total = (int64_t)bcol.size() * bs * bs;
+    if (total >= INT32_MAX) return LMG_ERR_UNSUPPORTED;
+    *nnz = total;
+    if (row_ptr && col_idx) {
+      int64_t o = 0;
+      for (int64_t r = 0; r < n_dofs; ++r) {
+        row_ptr[r] = (int32_t)o;
+        const int64_t P = r / bs;
+        for (int64_t j = brow[(size_t)P]; j < brow[(size_t)P + 1]; ++j)
+          for (int k = 0; k < bs; ++k) col_idx[o++] = bs * bcol[(size_t)j] + k;
+      }
+      row_ptr[n_dofs] = (int32_t)o;
+    }
+  } catch (const std::bad_alloc &) {
+    return LMG_ERR_OOM;
+  }
+  return LMG_OK;
+}
+
+lmg_status lmg_dofmap_distribute(int64_t n_nodes, int64_t n_elem, int32_t npe, const int32_t *conn,
+                                 int32_t n_vars, int64_t *n_dofs, int32_t *elem_dofs) {
+  if (!conn || !n_dofs || n_nodes < 0 || n_elem < 0 || npe <= 0 || n_vars <= 0) return LMG_ERR_ARG;
+  try {
+    // distribute_local_dofs_var_major (dof_map.C:1417-1537): one VariableGroup
+    // of n_vars LAGRANGE variables, one component per node; a node's dofs are
+    // vg_dof_base + var (DofObject::dof_number, include/base/dof_object.h:1029-1056).
+    std::vector<int64_t> base((size_t)n_nodes, -1);
+    int64_t next = 0;
+    for (int64_t e = 0; e < n_elem; ++e)
+      for (int a = 0; a < npe; ++a) {
+        const int32_t n = conn[e * npe + a];
+        if (n < 0 || n >= n_nodes) return LMG_ERR_BOUNDS;
+        if (base[(size_t)n] < 0) {
+          base[(size_t)n] = next;
+          next += n_vars;
+        }
+      }
+    // Nodes no element touches get numbered afterwards (dof_map.C:1515-1527).
+    for (int64_t n = 0; n < n_nodes; ++n)
+      if (base[(size_t)n] < 0) {
+        base[(size_t)n] = next;
+        next += n_vars;
+      }
+    if (next > INT32_MAX) return LMG_ERR_UNSUPPORTED;
+    *n_dofs = next;
+    if (elem_dofs) {
+      const int64_t nl = (int64_t)n_vars * npe;
+      for (int64_t e = 0; e < n_elem; ++e)
+        for (int v = 0; v < n_vars; ++v)
+          for (int a = 0; a < npe; ++a)
+            elem_dofs[e * nl + v * npe + a] = (int32_t)(base[(size_t)conn[e * npe + a]] + v);
+    }
+  } catch (const std::bad_alloc &) {
+    return LMG_ERR_OOM;
+  }
+  return LMG_OK;
+}
+
+lmg_status lmg_dirichlet_dofs(int64_t n_elem, int32_t elem_type, int32_t n_vars,
+                              const int32_t *elem_dofs, const int8_t *side_bid, const int32_t *bids,
+                              int32_t n_bids, const int32_t *vars, int32_t n_vars_bc,
+                              int64_t n_dofs, uint8_t *constrained) {
+  if (!elem_dofs || !side_bid || !constrained || (n_bids > 0 && !bids) ||
+      (n_vars_bc > 0 && !vars) || n_vars <= 0)
+    return LMG_ERR_ARG;
+  const int npe = lmg::nodes_per_elem(elem_type), ns = lmg::sides_per_elem(elem_type);
+  if (!npe) return LMG_ERR_UNSUPPORTED;
+  for (int i = 0; i < n_vars_bc; ++i)
+    if (vars[i] < 0 || vars[i] >= n_vars) return LMG_ERR_ARG;
+  std::fill(constrained, constrained + n_dofs, (uint8_t)0);
+  const int64_t nl = (int64_t)n_vars * npe;
+  int sn[9];
+  for (int64_t e = 0; e < n_elem; ++e)
+    for (int s = 0; s < ns; ++s) {
+      const int b = side_bid[e * ns + s];
+      if (b < 0) continue;
+      bool hit = false;
+      for (int i = 0; i < n_bids; ++i) hit |= (bids[i] == b);
+      if (!hit) continue;
+      const int k = lmg::side_nodes(elem_type, s, sn);
+      for (int i = 0; i < n_vars_bc; ++i)
+        for (int j = 0; j < k; ++j) {
+          const int32_t d = elem_dofs[e * nl + (int64_t)vars[i] * npe + sn[j]];
+          if (d < 0 || d >= n_dofs) return LMG_ERR_BOUNDS;
+          constrained[d] = 1;
+        }
+    }
+  return LMG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,700 @@
+// CPU oracle for the libMesh finite-element assembly path.
+//
+// TEST INFRASTRUCTURE ONLY.  This file restates, operation by operation and in
+// plain scalar C++, what libMesh does on the assembly path, so that the GPU
+// product can be checked against it.  Only tests/, __graft_entry__.smoke() and
+// the cpu_baseline / reference legs of bench.py may load it; the product
+// (libmesh_gb300) never links or calls it.
+//
+// The reference cannot be compiled here (its TIMPI / MetaPhysicL submodules are
+// empty and there is no MPI or PETSc), so this restatement is the oracle.  It
+// is pinned by the reference's own known-answer tests as far as they reach:
+// QGauss monomial exactness (tests/quadrature/quadrature_test.C), exact
+// reproduction of linear / quadratic fields and gradients by LAGRANGE shapes
+// (tests/fe/fe_test.h), build_cube counts (tests/mesh/mesh_generation_test.C)
+// and element volumes (tests/geom/volume_test.C).  No reference test or file
+// holds assembled K / F values.
+//
+// Build: oracle/build.py compiles it with -O2 -ffp-contract=off so that no
+// multiply-add is fused, as in libMesh's x86-64 default build.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <set>
+#include <thread>
+#include <vector>
+
+namespace {
+
+enum { TET4 = 8, TET10 = 9, HEX8 = 10, HEX27 = 12 };
+enum { POISSON = 0, ELASTICITY = 1 };
+
+// libMesh's _R literal: a long double literal narrowed to Real
+// (include/base/libmesh.h:283-286).
+#define R_(x) ((double)(x##L))
+
+struct Pt { double v[3]; };
+
+// ------------------------------------------------------------------ QGauss
+// QGauss::init_1D, src/quadrature/quadrature_gauss_1D.C:30-120.
+void qgauss_1d(int order, std::vector<double> &x, std::vector<double> &w) {
+  x.clear(); w.clear();
+  switch (order) {
+    case 0: case 1:
+      x = {0.}; w = {2.}; return;
+    case 2: case 3: {
+      double p0 = -std::sqrt(3.0) / 3;
+      x = {p0, -p0}; w = {1., 1.}; return;
+    }
+    case 4: case 5: {
+      double p0 = R_(-7.7459666924148337703585307995648e-01);
+      x = {p0, 0., -p0};
+      double w0 = 5.0 / 9, w1 = 8.0 / 9;
+      w = {w0, w1, w0}; return;
+    }
+    case 6: case 7: {
+      double p0 = R_(-8.6113631159405257522394648889281e-01), p1 = R_(-3.3998104358485626480266575910324e-01);
+      x = {p0, p1, -p1, -p0};
+      double w0 = R_(3.4785484513745385737306394922200e-01), w1 = R_(6.5214515486254614262693605077800e-01);
+      w = {w0, w1, w1, w0}; return;
+    }
+    default: {  // EIGHTH / NINTH
+      double p0 = R_(-9.0617984593866399279762687829939e-01), p1 = R_(-5.3846931010568309103631442070021e-01);
+      x = {p0, p1, 0., -p1, -p0};
+      double w0 = R_(2.3692688505618908751426404071992e-01), w1 = R_(4.7862867049936646804129151483564e-01),
+             w2 = R_(5.6888888888888888888888888888889e-01);
+      w = {w0, w1, w2, w1, w0}; return;
+    }
+  }
+}
+
+// QGauss::keast_rule, src/quadrature/quadrature_gauss.C:43-190.
+void keast_rule(const double rule[][4], int n_pts, std::vector<Pt> &P, std::vector<double> &W) {
+  for (int p = 0; p < n_pts; ++p) {
+    int type = 1;
+    if (rule[p][1] != 0.0) type = (rule[p][2] != 0.0) ? 12 : 4;
+    else if (rule[p][2] != 0.0) type = 6;
+    const double a = rule[p][0], wt = rule[p][3];
+    if (type == 1) { P.push_back({{a, a, a}}); W.push_back(wt); }
+    else if (type == 4) {
+      const double b = rule[p][1];
+      P.push_back({{a, b, b}}); P.push_back({{b, a, b}}); P.push_back({{b, b, a}}); P.push_back({{b, b, b}});
+      for (int j = 0; j < 4; ++j) W.push_back(wt);
+    } else if (type == 6) {
+      const double b = rule[p][2];
+      P.push_back({{a, a, b}}); P.push_back({{a, b, b}}); P.push_back({{b, b, a}});
+      P.push_back({{b, a, b}}); P.push_back({{b, a, a}}); P.push_back({{a, b, a}});
+      for (int j = 0; j < 6; ++j) W.push_back(wt);
+    }
+  }
+}
+
+// QGauss::init_3D, src/quadrature/quadrature_gauss_3D.C:30-226, and
+// QBase::tensor_product_hex, src/quadrature/quadrature.C:283-305.
+bool qgauss_3d(int type, int order, std::vector<Pt> &P, std::vector<double> &W) {
+  P.clear(); W.clear();
+  if (type == HEX8 || type == HEX27) {
+    std::vector<double> x, w;
+    qgauss_1d(order, x, w);
+    const int np = (int)x.size();
+    for (int k = 0; k < np; k++)
+      for (int j = 0; j < np; j++)
+        for (int i = 0; i < np; i++) {
+          P.push_back({{x[i], x[j], x[k]}});
+          W.push_back(w[i] * w[j] * w[k]);
+        }
+    return true;
+  }
+  if (type != TET4 && type != TET10) return false;
+  switch (order) {
+    case 0: case 1:
+      P.push_back({{.25, .25, .25}}); W.push_back(1.0 / 6); return true;
+    case 2: {
+      const double b = 0.25 * (1 - std::sqrt(5.0) / 5);
+      const double a = 1 - 3 * b;
+      P = {{{a, b, b}}, {{b, a, b}}, {{b, b, a}}, {{b, b, b}}};
+      const double w0 = 1.0 / 24;
+      W = {w0, w0, w0, w0}; return true;
+    }
+    case 3: {  // allow_rules_with_negative_weights defaults to true (quadrature.C:29)
+      P = {{{.25, .25, .25}}, {{.5, 1.0 / 6, 1.0 / 6}}, {{1.0 / 6, .5, 1.0 / 6}},
+           {{1.0 / 6, 1.0 / 6, .5}}, {{1.0 / 6, 1.0 / 6, 1.0 / 6}}};
+      W = {-2.0 / 15, .075, .075, .075, .075}; return true;
+    }
+    case 4: {
+      const double rule[3][4] = {
+          {R_(0.250000000000000000e+00), 0., 0., R_(-0.131555555555555556e-01)},
+          {R_(0.785714285714285714e+00), R_(0.714285714285714285e-01), 0., R_(0.762222222222222222e-02)},
+          {R_(0.399403576166799219e+00), 0., R_(0.100596423833200785e+00), R_(0.248888888888888889e-01)}};
+      keast_rule(rule, 3, P, W);
+      return true;
+    }
+    default:
+      return false;
+  }
+}
+
+// ------------------------------------------------------------------ shapes
+// include/fe/fe_lagrange_shape_1D.h
+double l1(int i, double xi) { return i == 0 ? .5 * (1. - xi) : .5 * (1. + xi); }
+double l1d(int i) { return i == 0 ? -.5 : .5; }
+double q1(int i, double xi) {
+  if (i == 0) return .5 * xi * (xi - 1.);
+  if (i == 1) return .5 * xi * (xi + 1);
+  return (1. - xi * xi);
+}
+double q1d(int i, double xi) {
+  if (i == 0) return xi - .5;
+  if (i == 1) return xi + .5;
+  return -2. * xi;
+}
+
+const unsigned H8_I0[] = {0, 1, 1, 0, 0, 1, 1, 0};
+const unsigned H8_I1[] = {0, 0, 1, 1, 0, 0, 1, 1};
+const unsigned H8_I2[] = {0, 0, 0, 0, 1, 1, 1, 1};
+const unsigned H27_I0[] = {0, 1, 1, 0, 0, 1, 1, 0, 2, 1, 2, 0, 0, 1, 1, 0, 2, 1, 2, 0, 2, 2, 1, 2, 0, 2, 2};
+const unsigned H27_I1[] = {0, 0, 1, 1, 0, 0, 1, 1, 0, 2, 1, 2, 0, 0, 1, 1, 0, 2, 1, 2, 2, 0, 2, 1, 2, 2, 2};
+const unsigned H27_I2[] = {0, 0, 0, 0, 1, 1, 1, 1, 0, 0, 0, 0, 2, 2, 2, 2, 1, 1, 1, 1, 0, 2, 2, 2, 2, 1, 2};
+
+// Number of LAGRANGE shapes of `order` on `type` (isoparametric cases only).
+int n_shapes(int type, int order) {
+  if (type == HEX8 || type == HEX27) return order == 1 ? 8 : (type == HEX27 ? 27 : 0);
+  if (type == TET4 || type == TET10) return order == 1 ? 4 : (type == TET10 ? 10 : 0);
+  return 0;
+}
+
+// fe_lagrange_3D_shape for TET4/TET10 (src/fe/fe_lagrange_shape_3D.C:710-740, 957-1010).
+double tet_shape(int order, int i, const Pt &p) {
+  const double zeta1 = p.v[0], zeta2 = p.v[1], zeta3 = p.v[2];
+  const double zeta0 = 1. - zeta1 - zeta2 - zeta3;
+  if (order == 1) {
+    const double z[4] = {zeta0, zeta1, zeta2, zeta3};
+    return z[i];
+  }
+  switch (i) {
+    case 0: return zeta0 * (2. * zeta0 - 1.);
+    case 1: return zeta1 * (2. * zeta1 - 1.);
+    case 2: return zeta2 * (2. * zeta2 - 1.);
+    case 3: return zeta3 * (2. * zeta3 - 1.);
+    case 4: return 4. * zeta0 * zeta1;
+    case 5: return 4. * zeta1 * zeta2;
+    case 6: return 4. * zeta2 * zeta0;
+    case 7: return 4. * zeta0 * zeta3;
+    case 8: return 4. * zeta1 * zeta3;
+    default: return 4. * zeta2 * zeta3;
+  }
+}
+
+// fe_lagrange_3D_shape_deriv for TET4/TET10 (src/fe/fe_lagrange_shape_3D.C:1543-1638, 2175-2330).
+double tet_shape_deriv(int order, int i, int j, const Pt &p) {
+  const double dz[4][3] = {{-1., -1., -1.}, {1., 0., 0.}, {0., 1., 0.}, {0., 0., 1.}};
+  if (order == 1) return dz[i][j];
+  const double zeta1 = p.v[0], zeta2 = p.v[1], zeta3 = p.v[2];
+  const double zeta0 = 1. - zeta1 - zeta2 - zeta3;
+  const double z[4] = {zeta0, zeta1, zeta2, zeta3};
+  if (i < 4) return (4. * z[i] - 1.) * dz[i][j];
+  static const int E[6][2] = {{0, 1}, {1, 2}, {0, 2}, {0, 3}, {1, 3}, {2, 3}};
+  const int a = E[i - 4][0], b = E[i - 4][1];
+  return 4. * (z[a] * dz[b][j] + dz[a][j] * z[b]);
+}
+
+// FE<3,LAGRANGE>::all_shapes / all_shape_derivs at a list of points
+// (hex tensor fast path, fe_lagrange_shape_3D.C:72-416; tets by scalar calls).
+// phi[i][p], d[c][i][p].
+void all_shapes(int type, int order, const std::vector<Pt> &pts, std::vector<std::vector<double>> &phi,
+                std::vector<std::vector<double>> d[3]) {
+  const int n = n_shapes(type, order), np = (int)pts.size();
+  phi.assign(n, std::vector<double>(np));
+  for (int c = 0; c < 3; ++c) d[c].assign(n, std::vector<double>(np));
+  const bool hex = (type == HEX8 || type == HEX27);
+  for (int q = 0; q < np; ++q) {
+    if (hex) {
+      const double xi = pts[q].v[0], eta = pts[q].v[1], zeta = pts[q].v[2];
+      const unsigned *i0 = order == 1 ? H8_I0 : H27_I0, *i1 = order == 1 ? H8_I1 : H27_I1,
+                     *i2 = order == 1 ? H8_I2 : H27_I2;
+      double s[3][3], ds[3][3];
+      for (int k = 0; k < (order == 1 ? 2 : 3); ++k) {
+        const double c3[3] = {xi, eta, zeta};
+        for (int m = 0; m < 3; ++m) {
+          s[m][k] = order == 1 ? l1(k, c3[m]) : q1(k, c3[m]);
+          ds[m][k] = order == 1 ? l1d(k) : q1d(k, c3[m]);
+        }
+      }
+      for (int i = 0; i < n; ++i) {
+        phi[i][q] = s[0][i0[i]] * s[1][i1[i]] * s[2][i2[i]];
+        d[0][i][q] = ds[0][i0[i]] * s[1][i1[i]] * s[2][i2[i]];
+        d[1][i][q] = s[0][i0[i]] * ds[1][i1[i]] * s[2][i2[i]];
+        d[2][i][q] = s[0][i0[i]] * s[1][i1[i]] * ds[2][i2[i]];
+      }
+    } else {
+      for (int i = 0; i < n; ++i) {
+        phi[i][q] = tet_shape(order, i, pts[q]);
+        for (int c = 0; c < 3; ++c) d[c][i][q] = tet_shape_deriv(order, i, c, pts[q]);
+      }
+    }
+  }
+}
+
+}  // namespace
+
+namespace {
+
+// ------------------------------------------------------------------ affine test
+// relative_fuzzy_equals (include/utils/fuzzy_equals.h:78-84) with affine_tol = TOLERANCE^2.
+bool rfe(const Pt &a, const Pt &b) {
+  const double tol = 1.e-6 * 1.e-6;
+  double d = 0, la = 0, lb = 0;
+  for (int i = 0; i < 3; ++i) d += std::abs(a.v[i] - b.v[i]);
+  for (int i = 0; i < 3; ++i) la += std::abs(a.v[i]);
+  for (int i = 0; i < 3; ++i) lb += std::abs(b.v[i]);
+  return d <= tol * (la + lb);
+}
+Pt sub(const Pt &a, const Pt &b) { return {{a.v[0] - b.v[0], a.v[1] - b.v[1], a.v[2] - b.v[2]}}; }
+Pt scl(const Pt &a, double s) { return {{a.v[0] * s, a.v[1] * s, a.v[2] * s}}; }
+Pt dvd(const Pt &a, double s) { return {{a.v[0] / s, a.v[1] / s, a.v[2] / s}}; }
+
+// Elem::has_affine_map: cell_hex8.C:121, cell_hex27.C:125, cell_tet4.h:136, cell_tet10.C:143.
+bool has_affine_map(int type, const std::vector<Pt> &p) {
+  if (type == TET4) return true;
+  if (type == TET10) {
+    const int E[6][3] = {{1, 0, 4}, {2, 1, 5}, {2, 0, 6}, {3, 0, 7}, {3, 1, 8}, {3, 2, 9}};
+    for (auto &e : E)
+      if (!rfe(sub(p[e[0]], p[e[1]]), scl(sub(p[e[2]], p[e[1]]), 2))) return false;
+    return true;
+  }
+  Pt v = sub(p[1], p[0]);
+  if (!rfe(v, sub(p[2], p[3])) || !rfe(v, sub(p[5], p[4])) || !rfe(v, sub(p[6], p[7]))) return false;
+  if (type == HEX27) {
+    v = dvd(v, 2);
+    const int X[9][2] = {{8, 0}, {10, 3}, {16, 4}, {18, 7}, {20, 11}, {21, 12}, {23, 15}, {25, 19}, {26, 24}};
+    for (auto &x : X) if (!rfe(v, sub(p[x[0]], p[x[1]]))) return false;
+  }
+  v = sub(p[4], p[0]);
+  if (!rfe(v, sub(p[7], p[3]))) return false;
+  if (type == HEX27) {
+    v = dvd(v, 2);
+    const int Z[6][2] = {{12, 0}, {13, 1}, {14, 2}, {15, 3}, {22, 9}, {24, 11}};
+    for (auto &z : Z) if (!rfe(v, sub(p[z[0]], p[z[1]]))) return false;
+    v = dvd(sub(p[3], p[0]), 2);
+    const int Y[4][2] = {{11, 0}, {9, 1}, {17, 5}, {19, 4}};
+    for (auto &y : Y) if (!rfe(v, sub(p[y[0]], p[y[1]]))) return false;
+  }
+  return true;
+}
+
+// ------------------------------------------------------------------ FE object
+// FE<3,LAGRANGE>::reinit (src/fe/fe.C:197-368) with its FEMap
+// (src/fe/fe_map.C:109-444, 448-1078, 1167-1374) and H1FETransformation::map_dphi
+// (src/fe/h1_fe_transformation.C:64-195).  Shape tables are built once per
+// element type (the reference caches them while the type does not change).
+struct OracleFE {
+  int type = 0, order = 0, n = 0, n_geo = 0, nq = 0;
+  std::vector<Pt> qp;
+  std::vector<double> qw;
+  std::vector<std::vector<double>> phi, dref[3];      // FE shapes
+  std::vector<std::vector<double>> phi_map, dmap[3];  // mapping shapes (default order)
+  // per-element results
+  std::vector<double> JxW, jac, G[9];                 // G[3*m+d] = dxi_m/dx_d
+  std::vector<std::vector<Pt>> dphi;                  // dphi[i][q]
+
+  bool init(int type_, int order_, int q_order) {
+    type = type_; order = order_;
+    if (!qgauss_3d(type, q_order, qp, qw)) return false;
+    nq = (int)qp.size();
+    n = n_shapes(type, order);
+    const int geo_order = (type == HEX27 || type == TET10) ? 2 : 1;
+    n_geo = n_shapes(type, geo_order);
+    if (!n || !n_geo) return false;
+    all_shapes(type, order, qp, phi, dref);
+    all_shapes(type, geo_order, qp, phi_map, dmap);
+    JxW.assign(nq, 0); jac.assign(nq, 0);
+    for (auto &g : G) g.assign(nq, 0);
+    dphi.assign(n, std::vector<Pt>(nq));
+    return true;
+  }
+
+  // compute_single_point_map, 3-D branch (fe_map.C:980-1078).  Returns false
+  // when jac <= jacobian_tolerance (0), i.e. libMesh would throw DegenerateMap.
+  bool single_point_map(const std::vector<Pt> &X, int p) {
+    double dxi[3] = {0, 0, 0}, deta[3] = {0, 0, 0}, dzeta[3] = {0, 0, 0};
+    for (int i = 0; i < n_geo; ++i)
+      for (int c = 0; c < 3; ++c) {
+        dxi[c] += dmap[0][i][p] * X[i].v[c];
+        deta[c] += dmap[1][i][p] * X[i].v[c];
+        dzeta[c] += dmap[2][i][p] * X[i].v[c];
+      }
+    const double dx_dxi = dxi[0], dy_dxi = dxi[1], dz_dxi = dxi[2];
+    const double dx_deta = deta[0], dy_deta = deta[1], dz_deta = deta[2];
+    const double dx_dzeta = dzeta[0], dy_dzeta = dzeta[1], dz_dzeta = dzeta[2];
+    jac[p] = (dx_dxi * (dy_deta * dz_dzeta - dz_deta * dy_dzeta) +
+              dy_dxi * (dz_deta * dx_dzeta - dx_deta * dz_dzeta) +
+              dz_dxi * (dx_deta * dy_dzeta - dy_deta * dx_dzeta));
+    const bool ok = jac[p] > 0.0;
+    JxW[p] = jac[p] * qw[p];
+    const double inv_jac = 1. / jac[p];
+    G[0][p] = (dy_deta * dz_dzeta - dz_deta * dy_dzeta) * inv_jac;
+    G[1][p] = (dz_deta * dx_dzeta - dx_deta * dz_dzeta) * inv_jac;
+    G[2][p] = (dx_deta * dy_dzeta - dy_deta * dx_dzeta) * inv_jac;
+    G[3][p] = (dz_dxi * dy_dzeta - dy_dxi * dz_dzeta) * inv_jac;
+    G[4][p] = (dx_dxi * dz_dzeta - dz_dxi * dx_dzeta) * inv_jac;
+    G[5][p] = (dy_dxi * dx_dzeta - dx_dxi * dy_dzeta) * inv_jac;
+    G[6][p] = (dy_dxi * dz_deta - dz_dxi * dy_deta) * inv_jac;
+    G[7][p] = (dz_dxi * dx_deta - dx_dxi * dz_deta) * inv_jac;
+    G[8][p] = (dx_dxi * dy_deta - dy_dxi * dx_deta) * inv_jac;
+    return ok;
+  }
+
+  bool reinit(const std::vector<Pt> &X) {
+    bool ok = true;
+    if (has_affine_map(type, X)) {  // compute_affine_map, fe_map.C:1167-1245
+      ok = single_point_map(X, 0);
+      for (int p = 1; p < nq; ++p) {
+        for (int k = 0; k < 9; ++k) G[k][p] = G[k][0];
+        jac[p] = jac[0];
+        JxW[p] = JxW[0] / qw[0] * qw[p];
+      }
+    } else {
+      for (int p = 0; p < nq; ++p) ok = single_point_map(X, p) && ok;
+    }
+    // map_dphi: dphi/dx = dphi/dxi dxi/dx + dphi/deta deta/dx + dphi/dzeta dzeta/dx
+    for (int i = 0; i < n; ++i)
+      for (int p = 0; p < nq; ++p)
+        for (int d = 0; d < 3; ++d)
+          dphi[i][p].v[d] = (dref[0][i][p] * G[0 + d][p] + dref[1][i][p] * G[3 + d][p] +
+                             dref[2][i][p] * G[6 + d][p]);
+    return ok;
+  }
+};
+
+double dot(const Pt &a, const Pt &b) { return (a.v[0] * b.v[0] + a.v[1] * b.v[1] + a.v[2] * b.v[2]); }
+
+// ------------------------------------------------------------------ dense algebra
+struct Dense {
+  int m = 0, n = 0;
+  std::vector<double> v;  // row-major, include/numerics/dense_matrix.h:969-977
+  void resize(int m_, int n_) { m = m_; n = n_; v.assign((size_t)m * n, 0.0); }
+  double &operator()(int i, int j) { return v[(size_t)i * n + j]; }
+  double operator()(int i, int j) const { return v[(size_t)i * n + j]; }
+};
+
+// DenseMatrix::_left_multiply_transpose (include/numerics/dense_matrix_impl.h:109-168), this <- A^T this.
+void left_multiply_transpose(Dense &self, const Dense &A) {
+  Dense B = self;
+  self.resize(A.n, B.n);
+  for (int i = 0; i < A.n; i++)
+    for (int k = 0; k < A.m; k++)
+      if (A(k, i) != 0.)
+        for (int j = 0; j < self.n; j++) self(i, j) += A(k, i) * B(k, j);
+}
+// DenseMatrix::right_multiply -> DenseMatrixBase::multiply (dense_matrix_base_impl.h:46-68), this <- this M3.
+void right_multiply(Dense &self, const Dense &M3) {
+  Dense M2 = self;
+  self.resize(M2.m, M3.n);
+  for (int k = 0; k < M2.n; k++)
+    for (int j = 0; j < self.n; j++)
+      if (M3(k, j) != 0.)
+        for (int i = 0; i < M2.m; i++) self(i, j) += M2(i, k) * M3(k, j);
+}
+
+}  // namespace
+
+namespace {
+
+// ------------------------------------------------------------------ element assembly
+struct Problem {
+  int form, type, fe_order, q_order, npe, n_vars, nl;
+  int64_t n_nodes, n_elem, n_dofs;
+  const double *xyz;
+  const int32_t *conn, *elem_dofs;
+  const uint8_t *constrained;
+  const double *coef, *nodal_f;
+  double nu;
+  const int32_t *row_ptr, *col;
+};
+
+// Lamé form of the elasticity tensor (systems_of_equations_ex6.C:120-150) with Young's modulus E.
+double elasticity_tensor(double E, double nu, unsigned i, unsigned j, unsigned k, unsigned l) {
+  auto kd = [](unsigned a, unsigned b) { return a == b ? 1. : 0.; };
+  const double lambda_1 = (E * nu) / ((1. + nu) * (1. - 2. * nu));
+  const double lambda_2 = E / (2. * (1. + nu));
+  return lambda_1 * kd(i, j) * kd(k, l) + lambda_2 * (kd(i, k) * kd(j, l) + kd(i, l) * kd(j, k));
+}
+
+// One element: reinit, weak form, constrain_element_matrix_and_vector.
+// Returns false on a degenerate map.
+bool element_matrix(const Problem &P, OracleFE &fe, int64_t e, Dense &Ke, std::vector<double> &Fe,
+                    std::vector<int32_t> &dofs) {
+  std::vector<Pt> X(P.npe);
+  for (int a = 0; a < P.npe; ++a)
+    for (int d = 0; d < 3; ++d) X[a].v[d] = P.xyz[3 * (int64_t)P.conn[e * P.npe + a] + d];
+  const bool ok = fe.reinit(X);
+  const int n = fe.n, nl = P.nl;
+  dofs.assign(P.elem_dofs + e * nl, P.elem_dofs + (e + 1) * nl);
+  Ke.resize(nl, nl);
+  Fe.assign(nl, 0.0);
+  const double coef = P.coef ? P.coef[e] : 1.0;
+  std::vector<double> f(n * P.n_vars, 0.0);
+  if (P.nodal_f)
+    for (int a = 0; a < n; ++a)
+      for (int v = 0; v < P.n_vars; ++v) f[a * P.n_vars + v] = P.nodal_f[(int64_t)P.conn[e * P.npe + a] * P.n_vars + v];
+  if (P.form == POISSON) {
+    // introduction_ex4.C:464-467 and 536 with nodal f interpolated by phi.
+    for (int qp = 0; qp < fe.nq; qp++)
+      for (int i = 0; i != n; i++)
+        for (int j = 0; j != n; j++)
+          Ke(i, j) += (coef * fe.JxW[qp]) * dot(fe.dphi[i][qp], fe.dphi[j][qp]);
+    for (int qp = 0; qp < fe.nq; qp++) {
+      double fxy = 0.0;
+      for (int j = 0; j < n; ++j) fxy += fe.phi[j][qp] * f[j];
+      for (int i = 0; i != n; i++) Fe[i] += fe.JxW[qp] * fxy * fe.phi[i][qp];
+    }
+  } else {
+    // systems_of_equations_ex6.C:214-236: Ke_var[i][k](dof_i,dof_j) += JxW C_ijkl dphi_j(l) dphi_i(j).
+    for (int qp = 0; qp < fe.nq; qp++) {
+      for (int dof_i = 0; dof_i < n; dof_i++)
+        for (int dof_j = 0; dof_j < n; dof_j++)
+          for (unsigned i = 0; i < 3; i++)
+            for (unsigned j = 0; j < 3; j++)
+              for (unsigned k = 0; k < 3; k++)
+                for (unsigned l = 0; l < 3; l++)
+                  Ke(i * n + dof_i, k * n + dof_j) += fe.JxW[qp] * elasticity_tensor(coef, P.nu, i, j, k, l) *
+                                                      fe.dphi[dof_j][qp].v[l] * fe.dphi[dof_i][qp].v[j];
+      double f_vec[3] = {0, 0, 0};
+      for (int i = 0; i < 3; ++i)
+        for (int b = 0; b < n; ++b) f_vec[i] += fe.phi[b][qp] * f[b * 3 + i];
+      for (int dof_i = 0; dof_i < n; dof_i++)
+        for (int i = 0; i < 3; i++) Fe[i * n + dof_i] += fe.JxW[qp] * (f_vec[i] * fe.phi[dof_i][qp]);
+    }
+  }
+  // DofMap::constrain_element_matrix_and_vector (dof_map_constraints.C:2439-2515)
+  // with build_constraint_matrix (:3433-3540).  Dirichlet rows are empty, so
+  // no dof is appended and C is square.
+  bool any = false;
+  for (int i = 0; i < nl; ++i) any |= P.constrained[dofs[i]] != 0;
+  if (any) {
+    Dense C;
+    C.resize(nl, nl);
+    for (int i = 0; i < nl; ++i)
+      if (!P.constrained[dofs[i]]) C(i, i) = 1.;
+    left_multiply_transpose(Ke, C);
+    right_multiply(Ke, C);
+    for (int i = 0; i < nl; ++i)
+      if (P.constrained[dofs[i]]) {
+        for (int j = 0; j < nl; ++j) Ke(i, j) = 0.;
+        Ke(i, i) = 1.;
+      }
+    std::vector<double> old = Fe;
+    for (int i = 0; i < nl; i++) {  // DenseMatrix::vector_mult_transpose
+      Fe[i] = 0.;
+      for (int j = 0; j < nl; j++) Fe[i] += C(j, i) * old[j];
+    }
+  }
+  return ok;
+}
+
+// PetscMatrix::add_matrix (MatSetValues ADD_VALUES, petsc_matrix.C:735-755) into a
+// preallocated AIJ pattern; a missing entry is an error (MAT_NEW_NONZERO_ALLOCATION_ERR).
+bool add_matrix(const Problem &P, const Dense &Ke, const std::vector<int32_t> &dofs, double *K) {
+  for (int i = 0; i < Ke.m; ++i) {
+    const int32_t r = dofs[i];
+    const int32_t *b = P.col + P.row_ptr[r], *en = P.col + P.row_ptr[r + 1];
+    for (int j = 0; j < Ke.n; ++j) {
+      const int32_t *it = std::lower_bound(b, en, dofs[j]);
+      if (it == en || *it != dofs[j]) return false;
+      K[it - P.col] += Ke(i, j);
+    }
+  }
+  return true;
+}
+
+// SparsityPattern::Build::handle_vi_vj (sparsity_pattern.C:152-275): merge the
+// sorted element dofs into each sorted row.
+void merge_row(std::vector<int32_t> &row, const std::vector<int32_t> &add) {
+  std::vector<int32_t> out;
+  out.reserve(row.size() + add.size());
+  std::set_union(row.begin(), row.end(), add.begin(), add.end(), std::back_inserter(out));
+  row.swap(out);
+}
+
+}  // namespace
+
+extern "C" {
+
+int orc_qgauss(int type, int order, double *pts, double *w, int cap) {
+  std::vector<Pt> P;
+  std::vector<double> W;
+  if (!qgauss_3d(type, order, P, W)) return -1;
+  const int n = (int)W.size();
+  for (int q = 0; q < n && q < cap; ++q) {
+    for (int d = 0; d < 3; ++d) pts[3 * q + d] = P[q].v[d];
+    w[q] = W[q];
+  }
+  return n;
+}
+
+// phi [n][np], dphi [3][n][np]
+int orc_shapes(int type, int order, int np, const double *pts, double *phi, double *dphi) {
+  std::vector<Pt> P(np);
+  for (int q = 0; q < np; ++q)
+    for (int d = 0; d < 3; ++d) P[q].v[d] = pts[3 * q + d];
+  std::vector<std::vector<double>> ph, dr[3];
+  const int n = n_shapes(type, order);
+  if (!n) return -1;
+  all_shapes(type, order, P, ph, dr);
+  for (int i = 0; i < n; ++i)
+    for (int q = 0; q < np; ++q) {
+      phi[i * np + q] = ph[i][q];
+      for (int c = 0; c < 3; ++c) dphi[(c * n + i) * np + q] = dr[c][i][q];
+    }
+  return n;
+}
+
+int orc_has_affine_map(int type, const double *X) {
+  const int n = (type == TET4) ? 4 : (type == TET10) ? 10 : (type == HEX8) ? 8 : 27;
+  std::vector<Pt> p(n);
+  for (int a = 0; a < n; ++a)
+    for (int d = 0; d < 3; ++d) p[a].v[d] = X[3 * a + d];
+  return has_affine_map(type, p) ? 1 : 0;
+}
+
+// DofMap::distribute_local_dofs_var_major (dof_map.C:1417-1537) and dof_indices.
+int orc_distribute_dofs(int64_t n_nodes, int64_t n_elem, int npe, const int32_t *conn, int n_vars,
+                        int32_t *elem_dofs, int64_t *n_dofs) {
+  std::vector<int64_t> base(n_nodes, -1);
+  int64_t next_free_dof = 0;
+  for (int64_t e = 0; e < n_elem; ++e)
+    for (int n = 0; n < npe; ++n) {
+      const int32_t node = conn[e * npe + n];
+      if (base[node] == -1) {
+        base[node] = next_free_dof;
+        next_free_dof += n_vars * 1;
+      }
+    }
+  for (int64_t node = 0; node < n_nodes; ++node)
+    if (base[node] == -1) {
+      base[node] = next_free_dof;
+      next_free_dof += n_vars;
+    }
+  *n_dofs = next_free_dof;
+  const int nl = n_vars * npe;
+  for (int64_t e = 0; e < n_elem; ++e)
+    for (int v = 0; v < n_vars; ++v)
+      for (int n = 0; n < npe; ++n)
+        elem_dofs[e * nl + v * npe + n] = (int32_t)(base[conn[e * npe + n]] + v * 1 + 0);
+  return 0;
+}
+
+// Dofs a homogeneous DirichletBoundary constrains on the given side ids
+// (ConstrainDirichlet, dof_map_constraints.C:257-1560: LAGRANGE dofs of the side's nodes).
+int orc_dirichlet(int64_t n_elem, int type, int n_vars, const int32_t *elem_dofs, const int8_t *side_bid,
+                  const int32_t *bids, int n_bids, const int32_t *vars, int n_bc_vars, uint8_t *constrained) {
+  static const int H8[6][4] = {{0, 3, 2, 1}, {0, 1, 5, 4}, {1, 2, 6, 5}, {2, 3, 7, 6}, {3, 0, 4, 7}, {4, 5, 6, 7}};
+  static const int H27[6][9] = {{0, 3, 2, 1, 11, 10, 9, 8, 20}, {0, 1, 5, 4, 8, 13, 16, 12, 21},
+                                {1, 2, 6, 5, 9, 14, 17, 13, 22}, {2, 3, 7, 6, 10, 15, 18, 14, 23},
+                                {3, 0, 4, 7, 11, 12, 19, 15, 24}, {4, 5, 6, 7, 16, 17, 18, 19, 25}};
+  static const int T4[4][3] = {{0, 2, 1}, {0, 1, 3}, {1, 2, 3}, {2, 0, 3}};
+  static const int T10[4][6] = {{0, 2, 1, 6, 5, 4}, {0, 1, 3, 4, 8, 7}, {1, 2, 3, 5, 9, 8}, {2, 0, 3, 6, 7, 9}};
+  const int npe = (type == TET4) ? 4 : (type == TET10) ? 10 : (type == HEX8) ? 8 : 27;
+  const int ns = (type == TET4 || type == TET10) ? 4 : 6;
+  const int nl = n_vars * npe;
+  for (int64_t e = 0; e < n_elem; ++e)
+    for (int s = 0; s < ns; ++s) {
+      const int b = side_bid[e * ns + s];
+      if (b < 0 || std::find(bids, bids + n_bids, b) == bids + n_bids) continue;
+      std::vector<int> sn;
+      if (type == HEX8) sn.assign(H8[s], H8[s] + 4);
+      else if (type == HEX27) sn.assign(H27[s], H27[s] + 9);
+      else if (type == TET4) sn.assign(T4[s], T4[s] + 3);
+      else sn.assign(T10[s], T10[s] + 6);
+      for (int iv = 0; iv < n_bc_vars; ++iv)
+        for (int a : sn) constrained[elem_dofs[e * nl + vars[iv] * npe + a]] = 1;
+    }
+  return 0;
+}
+
+// DofMap::compute_sparsity for a single rank: row_ptr [n_dofs+1], col [nnz].
+// Call with row_ptr/col NULL to get nnz only.
+int orc_sparsity(int64_t n_dofs, int64_t n_elem, int nl, const int32_t *elem_dofs, int64_t *nnz,
+                 int32_t *row_ptr, int32_t *col) {
+  std::vector<std::vector<int32_t>> rows(n_dofs);
+  std::vector<int32_t> ed;
+  for (int64_t e = 0; e < n_elem; ++e) {
+    ed.assign(elem_dofs + e * nl, elem_dofs + (e + 1) * nl);
+    std::sort(ed.begin(), ed.end());
+    ed.erase(std::unique(ed.begin(), ed.end()), ed.end());
+    for (int32_t r : ed) merge_row(rows[r], ed);
+  }
+  int64_t total = 0;
+  for (auto &r : rows) total += (int64_t)r.size();
+  *nnz = total;
+  if (row_ptr && col) {
+    int64_t o = 0;
+    for (int64_t r = 0; r < n_dofs; ++r) {
+      row_ptr[r] = (int32_t)o;
+      for (int32_t c : rows[r]) col[o++] = c;
+    }
+    row_ptr[n_dofs] = (int32_t)o;
+  }
+  return 0;
+}
+
+// Assembly over elements [e_begin, e_end) into K (CSR values) and F, both
+// zeroed here first.  n_threads > 1 splits the range into contiguous chunks,
+// each thread builds element matrices and inserts under one mutex, as
+// FEMSystem::assembly does (src/systems/fem_system.C:940-944, 362-369).
+// Returns 0, 4 (degenerate element, *bad_elem set) or 6 (entry outside the pattern).
+int orc_assemble(int form, int type, int fe_order, int q_order, int64_t n_nodes, const double *xyz,
+                 int64_t n_elem, const int32_t *conn, int n_vars, const int32_t *elem_dofs, int64_t n_dofs,
+                 const uint8_t *constrained, const double *coef, const double *nodal_f, double nu,
+                 const int32_t *row_ptr, const int32_t *col, double *K, double *F, int n_threads,
+                 int64_t e_begin, int64_t e_end, int64_t *bad_elem, double *loop_seconds) {
+  Problem P{};
+  P.form = form; P.type = type; P.fe_order = fe_order; P.q_order = q_order;
+  P.npe = n_shapes(type, (type == HEX27 || type == TET10) ? 2 : 1);
+  P.n_vars = n_vars; P.nl = n_vars * P.npe;
+  P.n_nodes = n_nodes; P.n_elem = n_elem; P.n_dofs = n_dofs;
+  P.xyz = xyz; P.conn = conn; P.elem_dofs = elem_dofs; P.constrained = constrained;
+  P.coef = coef; P.nodal_f = nodal_f; P.nu = nu; P.row_ptr = row_ptr; P.col = col;
+  if (n_shapes(type, fe_order) != P.npe) return 8;
+  std::fill(K, K + row_ptr[n_dofs], 0.0);
+  std::fill(F, F + n_dofs, 0.0);
+  if (e_end > n_elem) e_end = n_elem;
+  if (n_threads < 1) n_threads = 1;
+  std::mutex mtx;
+  int status = 0;
+  int64_t first_bad = -1;
+  auto work = [&](int64_t b, int64_t en) {
+    OracleFE fe;
+    fe.init(type, fe_order, q_order);
+    Dense Ke;
+    std::vector<double> Fe;
+    std::vector<int32_t> dofs;
+    for (int64_t e = b; e < en; ++e) {
+      const bool ok = element_matrix(P, fe, e, Ke, Fe, dofs);
+      std::lock_guard<std::mutex> lk(mtx);
+      if (!ok && status == 0) { status = 4; first_bad = e; }
+      if (!add_matrix(P, Ke, dofs, K) && status == 0) status = 6;
+      for (int i = 0; i < P.nl; ++i) F[dofs[i]] += Fe[i];  // PetscVector::add_vector
+    }
+  };
+  const auto t0 = std::chrono::steady_clock::now();
+  if (n_threads == 1) {
+    work(e_begin, e_end);
+  } else {
+    std::vector<std::thread> th;
+    const int64_t n = e_end - e_begin;
+    for (int t = 0; t < n_threads; ++t)
+      th.emplace_back(work, e_begin + n * t / n_threads, e_begin + n * (t + 1) / n_threads);
+    for (auto &t : th) t.join();
+  }
+  if (loop_seconds)
+    *loop_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  if (bad_elem) *bad_elem = first_bad;
+  return status;
+}
+
+}  // extern "C"

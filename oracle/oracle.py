@@ -1,0 +1,110 @@
+"""ctypes front end of the CPU oracle (oracle.cpp).  Test infrastructure only:
+tests/, __graft_entry__.smoke() and bench.py's CPU legs use it as the checker."""
+import ctypes as C
+import os
+import sys
+
+import numpy as np
+
+sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+import build as _build  # noqa: E402
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        _lib = C.CDLL(_build.build())
+        v, i32, i64, f64 = C.c_void_p, C.c_int32, C.c_int64, C.c_double
+        _lib.orc_qgauss.argtypes = [i32, i32, v, v, i32]
+        _lib.orc_shapes.argtypes = [i32, i32, i32, v, v, v]
+        _lib.orc_has_affine_map.argtypes = [i32, v]
+        _lib.orc_distribute_dofs.argtypes = [i64, i64, i32, v, i32, v, C.POINTER(i64)]
+        _lib.orc_dirichlet.argtypes = [i64, i32, i32, v, v, v, i32, v, i32, v]
+        _lib.orc_sparsity.argtypes = [i64, i64, i32, v, C.POINTER(i64), v, v]
+        _lib.orc_assemble.argtypes = [i32, i32, i32, i32, i64, v, i64, v, i32, v, i64, v, v, v, f64,
+                                      v, v, v, v, i32, i64, i64, C.POINTER(i64), C.POINTER(f64)]
+        for f in (_lib.orc_qgauss, _lib.orc_shapes, _lib.orc_has_affine_map, _lib.orc_distribute_dofs,
+                  _lib.orc_dirichlet, _lib.orc_sparsity, _lib.orc_assemble):
+            f.restype = C.c_int32
+    return _lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def qgauss(elem_type, order):
+    pts = np.zeros((1000, 3))
+    w = np.zeros(1000)
+    n = lib().orc_qgauss(elem_type, order, _p(pts), _p(w), 1000)
+    assert n > 0
+    return pts[:n].copy(), w[:n].copy()
+
+
+def shapes(elem_type, order, pts):
+    pts = np.ascontiguousarray(pts, np.float64)
+    np_ = pts.shape[0]
+    phi = np.zeros((64, np_))
+    dphi = np.zeros((3, 64, np_))
+    n = lib().orc_shapes(elem_type, order, np_, _p(pts), _p(phi), _p(dphi.reshape(-1)))
+    assert n > 0
+    dphi = dphi.reshape(-1)[:3 * n * np_].reshape(3, n, np_)
+    return phi.reshape(-1)[:n * np_].reshape(n, np_).copy(), dphi.copy()
+
+
+def has_affine_map(elem_type, X):
+    return bool(lib().orc_has_affine_map(elem_type, _p(np.ascontiguousarray(X, np.float64))))
+
+
+def distribute_dofs(n_nodes, conn, n_vars):
+    conn = np.ascontiguousarray(conn, np.int32)
+    ed = np.zeros((conn.shape[0], n_vars * conn.shape[1]), np.int32)
+    nd = C.c_int64()
+    lib().orc_distribute_dofs(n_nodes, conn.shape[0], conn.shape[1], _p(conn), n_vars, _p(ed), C.byref(nd))
+    return ed, nd.value
+
+
+def dirichlet(elem_type, n_vars, elem_dofs, side_bid, bids, variables, n_dofs):
+    bids = np.ascontiguousarray(bids, np.int32)
+    variables = np.ascontiguousarray(variables, np.int32)
+    c = np.zeros(n_dofs, np.uint8)
+    lib().orc_dirichlet(elem_dofs.shape[0], elem_type, n_vars, _p(np.ascontiguousarray(elem_dofs)),
+                        _p(np.ascontiguousarray(side_bid, np.int8)), _p(bids), len(bids), _p(variables),
+                        len(variables), _p(c))
+    return c
+
+
+def sparsity(n_dofs, elem_dofs):
+    ed = np.ascontiguousarray(elem_dofs, np.int32)
+    nnz = C.c_int64()
+    lib().orc_sparsity(n_dofs, ed.shape[0], ed.shape[1], _p(ed), C.byref(nnz), None, None)
+    rp = np.zeros(n_dofs + 1, np.int32)
+    col = np.zeros(nnz.value, np.int32)
+    lib().orc_sparsity(n_dofs, ed.shape[0], ed.shape[1], _p(ed), C.byref(nnz), _p(rp), _p(col))
+    return rp, col
+
+
+def assemble(form, elem_type, fe_order, q_order, xyz, conn, n_vars, elem_dofs, n_dofs, constrained,
+             row_ptr, col, coef=None, nodal_f=None, nu=0.3, n_threads=1, e_range=None, timing=None):
+    """Returns (K values, F, status, first bad element); timing (a dict) gets
+    the wall time of the element loop under "seconds"."""
+    xyz = np.ascontiguousarray(xyz, np.float64)
+    conn = np.ascontiguousarray(conn, np.int32)
+    ed = np.ascontiguousarray(elem_dofs, np.int32)
+    cons = np.ascontiguousarray(constrained, np.uint8)
+    coef = None if coef is None else np.ascontiguousarray(coef, np.float64)
+    nodal_f = None if nodal_f is None else np.ascontiguousarray(nodal_f, np.float64)
+    K = np.zeros(int(row_ptr[-1]))
+    F = np.zeros(n_dofs)
+    b, e = (0, conn.shape[0]) if e_range is None else e_range
+    bad = C.c_int64(-1)
+    secs = C.c_double(0)
+    st = lib().orc_assemble(form, elem_type, fe_order, q_order, xyz.shape[0], _p(xyz), conn.shape[0],
+                            _p(conn), n_vars, _p(ed), n_dofs, _p(cons), _p(coef), _p(nodal_f), nu,
+                            _p(np.ascontiguousarray(row_ptr, np.int32)), _p(np.ascontiguousarray(col, np.int32)),
+                            _p(K), _p(F), n_threads, b, e, C.byref(bad), C.byref(secs))
+    if timing is not None:
+        timing["seconds"] = secs.value
+    return K, F, st, bad.value
