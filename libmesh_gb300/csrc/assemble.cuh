@@ -54,6 +54,8 @@ struct GatherArgs {
   double *F;
 };
 
+// Whether an element kernel is instantiated for (form, shapes per variable, variables).
+bool elements_built(int form, int n, int nv);
 void launch_elements(int form, int n, int nv, bool affine, const ElemArgs &a, int grid,
                      cudaStream_t s);
 void launch_gather(const GatherArgs &g, bool mixed, cudaStream_t s);

@@ -516,6 +516,9 @@ lmg_status lmg_form_set(lmg_ctx *c, int32_t form, int32_t fe_order, int32_t q_or
   if (!err.empty()) return fail(c, LMG_ERR_UNSUPPORTED, "form_set: " + err);
   if (t.n != c->npe || t.n_geo != c->npe)
     return fail(c, LMG_ERR_UNSUPPORTED, "form_set: only isoparametric LAGRANGE elements are built");
+  if (t.q > 27) return fail(c, LMG_ERR_UNSUPPORTED, "form_set: more than 27 quadrature points");
+  if (!elements_built(form, t.n, c->n_vars))
+    return fail(c, LMG_ERR_UNSUPPORTED, "form_set: no element kernel for this form / element");
   c->tab = t;
   c->form = form;
   c->fe_order = fe_order;

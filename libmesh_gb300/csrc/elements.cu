@@ -318,6 +318,11 @@ void launch_t(bool affine, const ElemArgs &a, int grid, cudaStream_t s) {
 
 }  // namespace
 
+bool elements_built(int form, int n, int nv) {
+  return (form == LMG_POISSON && nv == 1 && (n == 4 || n == 8 || n == 10 || n == 27)) ||
+         (form == LMG_ELASTICITY && nv == 3 && (n == 4 || n == 8 || n == 10));
+}
+
 void launch_elements(int form, int n, int nv, bool affine, const ElemArgs &a, int grid,
                      cudaStream_t s) {
 #define LMG_CASE(F, NN, V)                                   \
