@@ -49,11 +49,18 @@ def build_problem(n=N_CUBE):
 
 
 def algorithmic(mesh, dm, nnz):
-    """Unique bytes and reference-form flops of one assembly (FMA = 2)."""
+    """Unique bytes of one assembly, and flops per element (FMA = 2) of the
+    reference's B^T D B form and of the affine reference-tensor form the FP64
+    element kernel executes."""
     n_geo, n, q = 10, 10, 11
     B = 24 * mesh.n_nodes + 4 * mesh.n_elem * n_geo + 8 * dm.n_dofs + 8 * mesh.n_elem + 8 * nnz + 8 * dm.n_dofs
-    per_elem = q * (2 * (6 * 6 * 3 * n + 3 * n * 3 * n * 6) + 18 * n) + q * (18 * n_geo + 60)
-    return B, per_elem * mesh.n_elem
+    ref_form = q * (2 * (6 * 6 * 3 * n + 3 * n * 3 * n * 6) + 18 * n) + q * (18 * n_geo + 60)
+    blocks = n * (n + 1) // 2                      # diagonal + strictly upper 3x3 blocks
+    ours = (2 * blocks * 9 * 9                     # K^{ik}_{ab} = sum_mn A^{ik}_{mn} S^{mn}_{ab}
+            + 2 * 3 * n * n                        # Fe = detJ M f
+            + 2 * 81 * 3 + 2 * 27                  # element tensor A (81 entries) and G G^T
+            + 2 * n_geo * 9 + 60)                  # Jacobian at qp 0, det, inverse
+    return B, ref_form, ours
 
 
 class Clocks:
@@ -157,6 +164,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
+    ap.add_argument("--n", type=int, default=N_CUBE, help="cube divisions (48 = the headline mesh)")
+    ap.add_argument("--no-mixed", action="store_true", help="skip timing the mixed form beside FP64")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
@@ -174,7 +183,7 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl")
     prec = lm.FP64 if args.precision == "fp64" else lm.MIXED
-    mesh, dm, E, f = build_problem()
+    mesh, dm, E, f = build_problem(args.n)
     asm = lm.GpuAssembly(lm.ELASTICITY, 2, 4, elem_coef=E, nodal_f=f, nu=0.3, device=local)
     asm.init(mesh, dm)
     stream = torch.cuda.current_stream()
@@ -206,6 +215,30 @@ def main():
         ms = float(t.item())
     value = world * mesh.n_elem / (ms * 1e-3) / 1e6
 
+    # the other form, timed the same way on the same inputs
+    other = None
+    if not args.no_mixed and prec == lm.FP64:
+        asm.assemble_device(lm.MIXED)
+        asm.synchronize()
+        ev0.record(stream)
+        for _ in range(args.steps):
+            asm.assemble_device(lm.MIXED)
+        ev1.record(stream)
+        ev1.synchronize()
+        asm.synchronize()
+        ms32 = ev0.elapsed_time(ev1) / args.steps
+        K32 = torch.empty(asm.nnz, dtype=torch.float64, device="cuda")
+        K64 = torch.empty(asm.nnz, dtype=torch.float64, device="cuda")
+        Fd = torch.empty(dm.n_dofs, dtype=torch.float64, device="cuda")
+        asm.assemble_device(lm.MIXED, K32.data_ptr(), Fd.data_ptr())
+        asm.assemble_device(lm.FP64, K64.data_ptr(), Fd.data_ptr())
+        asm.synchronize()
+        krel = float(torch.linalg.norm(K32 - K64) / torch.linalg.norm(K64))
+        del K32, K64, Fd
+        other = {"form": "mixed (FP32 contraction, FP64 Jacobian/diagonal/accumulation)",
+                 "value": world * mesh.n_elem / (ms32 * 1e-3) / 1e6, "unit": "Melem/s", "ms_per_step": ms32,
+                 "speedup_vs_fp64": ms / ms32, "k_rel_frobenius_vs_fp64": krel}
+
     # per-stage times (PerfLog events) for the roofline
     asm.perflog_enable(True)
     for _ in range(5):
@@ -236,17 +269,20 @@ def main():
         e2e_s = float(t.item())
     e2e = world * mesh.n_elem / e2e_s / 1e6
 
-    B, flops = algorithmic(mesh, dm, asm.nnz)
+    B, ref_flops, our_flops = algorithmic(mesh, dm, asm.nnz)
     hbm, hbm_src = peaks()
     fp64 = lm.probe_fp64(local)
     if el_ms >= ga_ms:
-        dom = {"kernel": "k_elem_affine<ELASTICITY,10,3>", "bound": "fp64", "unit": "TFLOP/s",
-               "achieved": flops / (el_ms * 1e-3) / 1e12, "peak": fp64,
-               "peak_source": "measured FP64 DFMA probe (lmg_probe_fp64) in this run"}
+        dom = {"kernel": "k_elem_affine<ELASTICITY,10,3,double>", "bound": "fp64", "unit": "TFLOP/s",
+               "achieved": our_flops * mesh.n_elem / (el_ms * 1e-3) / 1e12, "peak": fp64,
+               "peak_source": "measured FP64 DFMA probe (lmg_probe_fp64) in this run",
+               "flops_per_elem": our_flops, "reference_form_flops_per_elem": ref_flops}
     else:
-        dom = {"kernel": "k_gather<double>", "bound": "hbm", "unit": "GB/s",
-               "achieved": (8 * asm.nnz + 8 * dm.n_dofs) / (ga_ms * 1e-3) / 1e9, "peak": hbm,
-               "peak_source": hbm_src}
+        no = 45
+        gbytes = (8 * asm.nnz + 8 * dm.n_dofs + 8 * mesh.n_elem * (10 * 9 + no * 9) + 8 * mesh.n_elem * 30)
+        dom = {"kernel": "k_gather<double,3>", "bound": "hbm", "unit": "GB/s",
+               "achieved": gbytes / (ga_ms * 1e-3) / 1e9, "peak": hbm, "peak_source": hbm_src,
+               "bytes_per_launch": gbytes}
     dom["frac"] = dom["achieved"] / dom["peak"]
     dom["traffic"] = None
     dom["stages_ms"] = {"elements": el_ms, "insertion": ga_ms}
@@ -267,14 +303,15 @@ def main():
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64" if prec == lm.FP64 else "f32+f64",
             "data": "synthetic (seeded mesh jitter, E_e, f)",
-            "config": {"workload": "elasticity TET10 build_cube 48^3 x6 tets, QGauss FOURTH",
+            "config": {"workload": "elasticity TET10 build_cube %d^3 x6 tets, QGauss FOURTH" % args.n,
                        "n_elem": mesh.n_elem, "n_dofs": dm.n_dofs, "nnz": asm.nnz,
                        "precision": args.precision, "l2": "inputs larger than L2 (4.8 GB element buffer)",
                        "parallelism": "replica per GPU"},
             "mdofs_per_s": value * dm.n_dofs / mesh.n_elem,
             "e2e": {"value": e2e, "unit": "Melem/s", "h2d_bytes_per_step": 8 * (mesh.n_elem + 3 * mesh.n_nodes),
                     "d2h_bytes_per_step": 8 * (asm.nnz + dm.n_dofs)},
-            "gpu_launches": launches, "clocks": clk, "roofline": dom, "cpu_baseline": cpu}))
+            "gpu_launches": launches, "clocks": clk, "roofline": dom, "cpu_baseline": cpu,
+            "mixed": other}))
     if dist:
         dist.destroy_process_group()
 

@@ -167,6 +167,13 @@ lmg_status lmg_result_device(lmg_ctx *ctx, double **K, double **F);
  * the context's stream; lmg_synchronize waits for it and returns its status. */
 lmg_status lmg_synchronize(lmg_ctx *ctx);
 
+/* Jacobi-preconditioned CG on the last assembled K (LinearImplicitSystem::solve
+ * with KSPCG, src/systems/linear_implicit_system.C:122-165): solves K x = rhs
+ * (host array; NULL = the last assembled F) until ||r|| <= rtol ||rhs|| or maxit
+ * iterations; x is a host array of n_dofs. */
+lmg_status lmg_cg_solve(lmg_ctx *ctx, const double *rhs, double *x, double rtol, int32_t maxit,
+                        int32_t *iters, double *relres);
+
 /* First failing element of the last call (-1 if none) and a message. */
 lmg_status lmg_last_error(lmg_ctx *ctx, int64_t *elem_id, char *msg, int32_t msg_len);
 

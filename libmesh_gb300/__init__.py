@@ -160,6 +160,14 @@ class GpuAssembly:
     def set_stream(self, stream_ptr):
         self._ok(lib().lmg_context_set_stream(self.ctx, C.c_void_p(stream_ptr)))
 
+    def solve(self, rhs=None, rtol=1e-10, maxit=20000):
+        """CG on the last assembled system; returns (x, iterations, relative residual)."""
+        x = np.empty(self.dof_map.n_dofs, np.float64)
+        it, rr = C.c_int32(), C.c_double()
+        b = None if rhs is None else np.ascontiguousarray(rhs, np.float64)
+        self._ok(lib().lmg_cg_solve(self.ctx, ptr(b), ptr(x), float(rtol), int(maxit), C.byref(it), C.byref(rr)))
+        return x, it.value, rr.value
+
     def perflog_enable(self, on=True):
         self._ok(lib().lmg_perflog_enable(self.ctx, 1 if on else 0))
 

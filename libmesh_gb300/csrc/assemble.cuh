@@ -28,9 +28,13 @@ struct ElemArgs {
   const double *nodal_f;      // [n_nodes][nv] or null (=0)
   const uint64_t *cmask;      // [n_elem] constrained local dofs, bit v*n + a
   double nu;                  // Poisson ratio (elasticity)
-  double *Ke;                 // [n_elem][n][n][nv][nv]
+  // Symmetric element matrices are stored as nv x nv blocks: the n diagonal
+  // blocks in FP64 and the n(n-1)/2 strictly upper blocks (a < b, row-major
+  // over a then b) in FP64 (drop-in) or FP32 (mixed form).
+  double *Kdiag;              // [n_elem][n][nv][nv]
+  double *Koff;               // [n_elem][n(n-1)/2][nv][nv] (FP64) or null
+  float *Koff32;              // same layout in FP32 (mixed) or null
   double *Fe;                 // [n_elem][n][nv]
-  float *Ke32;                // mixed form: FP32 element blocks (same layout) or null
   int *status;                // [0] error code
   unsigned long long *bad_elem;  // first failing element id
   DevFE fe;
@@ -43,12 +47,18 @@ struct GatherArgs {
   int nb;                     // blocks per element
   const int64_t *brow_ptr;    // [n_blocks+1]
   const int32_t *row_ptr;     // [n_dofs+1]
+  const int32_t *bcol;        // [nnzb]
   const int32_t *bptr;        // [nnzb+1] contributions per block slot
-  const int32_t *bcontrib;    // (e*nb + a)*nb + b, ascending per slot
+  // Per slot, ascending in element: diagonal slots hold e*nb + a (a Kdiag
+  // block); off-diagonal slots hold 2*(e*no + o) + t, o the strictly upper
+  // block of the element pair and t = 1 when the slot takes its transpose.
+  const int32_t *bcontrib;
+  int no;                     // strictly upper blocks per element
   const int32_t *fptr;        // [n_blocks+1]
   const int32_t *fcontrib;    // e*nb + a, ascending per block row
-  const double *Ke;
-  const float *Ke32;
+  const double *Kdiag;
+  const double *Koff;
+  const float *Koff32;
   const double *Fe;
   double *K;
   double *F;
@@ -56,8 +66,12 @@ struct GatherArgs {
 
 // Whether an element kernel is instantiated for (form, shapes per variable, variables).
 bool elements_built(int form, int n, int nv);
-void launch_elements(int form, int n, int nv, bool affine, const ElemArgs &a, int grid,
+void launch_elements(int form, int n, int nv, bool affine, bool mixed, const ElemArgs &a, int grid,
                      cudaStream_t s);
+bool gather_built(int bs);
+// PCG (Jacobi) on a CSR matrix; returns 0 on success, 7 out of memory, 2 CUDA error.
+int cg_solve(int64_t n, const int32_t *rp, const int32_t *col, const double *val, const double *b, double *x,
+             double rtol, int maxit, cudaStream_t s, int n_sm, int *iters, double *relres, int64_t *launches);
 void launch_gather(const GatherArgs &g, bool mixed, cudaStream_t s);
 
 }  // namespace lmg

@@ -55,8 +55,8 @@ struct lmg_ctx {
   DevFE dfe{};
   double *d_coef = nullptr, *d_f = nullptr;
   // work and result buffers
-  double *d_Ke = nullptr, *d_Fe = nullptr, *d_K = nullptr, *d_F = nullptr;
-  float *d_Ke32 = nullptr;
+  double *d_Kdiag = nullptr, *d_Koff = nullptr, *d_Fe = nullptr, *d_K = nullptr, *d_F = nullptr;
+  float *d_Koff32 = nullptr;
   int *d_status = nullptr;
   unsigned long long *d_bad = nullptr;
   // PerfLog-style stage timing (CUDA events on the context stream)
@@ -176,6 +176,28 @@ __global__ void k_segsort(int64_t n_seg, const int32_t *ptr, int32_t *v) {
   }
 }
 
+// Re-encodes every matrix contribution (e*nb + a)*nb + b of a slot into the
+// symmetric element storage: diagonal pairs -> e*nb + a (Kdiag block), other
+// pairs -> 2*(e*no + o) + t with o the strictly upper block of {a, b} and
+// t = 1 for a > b (the slot reads the transpose).  Element order is kept.
+__global__ void k_encode(int64_t n, int nb, int32_t *v) {
+  const int no = nb * (nb - 1) / 2;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t x = v[i];
+    const int64_t e = x / ((int64_t)nb * nb);
+    const int ab = (int)(x - e * nb * nb);
+    const int a = ab / nb, b = ab - a * nb;
+    if (a == b) {
+      v[i] = (int32_t)(e * nb + a);
+    } else {
+      const int lo = a < b ? a : b, hi = a < b ? b : a;
+      const int o = lo * nb - lo * (lo + 1) / 2 + (hi - lo - 1);
+      v[i] = (int32_t)(2 * (e * no + o) + (a > b ? 1 : 0));
+    }
+  }
+}
+
 // Exclusive scan helpers: block-local scan, then scan of block sums.
 constexpr int SCAN_T = 1024;
 __global__ void k_scan_local(int64_t n, const int32_t *in, int32_t *out, int32_t *bsum) {
@@ -282,6 +304,7 @@ lmg_status build_plan(lmg_ctx *c) {
   const int nb = c->nb;
   const int64_t npair = c->n_elem * nb * nb, nrow = c->n_elem * nb;
   if (npair >= INT32_MAX) return fail(c, LMG_ERR_UNSUPPORTED, "mesh too large for 32-bit plan");
+  if (!gather_built(c->bs)) return fail(c, LMG_ERR_UNSUPPORTED, "no insertion kernel for this block size");
   int32_t *slot = nullptr, *cnt = nullptr, *cur = nullptr;
   LMG_CUDA(c, dalloc(slot, (size_t)npair));
   LMG_CUDA(c, dalloc(cnt, (size_t)std::max(c->nnzb, c->n_blocks)));
@@ -301,7 +324,8 @@ lmg_status build_plan(lmg_ctx *c) {
   LMG_CUDA(c, cudaMemsetAsync(cur, 0, sizeof(int32_t) * c->nnzb, c->stream));
   k_fill<<<grid_for(c, npair, 256), 256, 0, c->stream>>>(npair, slot, c->d_bptr, cur, c->d_bcontrib);
   k_segsort<<<grid_for(c, c->nnzb, 256), 256, 0, c->stream>>>(c->nnzb, c->d_bptr, c->d_bcontrib);
-  c->launches += 2;
+  k_encode<<<grid_for(c, npair, 256), 256, 0, c->stream>>>(npair, nb, c->d_bcontrib);
+  c->launches += 3;
   // vector plan
   LMG_CUDA(c, cudaMemsetAsync(cnt, 0, sizeof(int32_t) * c->n_blocks, c->stream));
   k_count_rows<<<grid_for(c, nrow, 256), 256, 0, c->stream>>>(nrow, c->d_eb, cnt);
@@ -379,8 +403,8 @@ lmg_status lmg_context_destroy(lmg_ctx *c) {
   dfree(c->d_xyz); dfree(c->d_conn); dfree(c->d_aff); dfree(c->d_gen); dfree(c->d_eb);
   dfree(c->d_cmask); dfree(c->d_brow_ptr); dfree(c->d_bcol); dfree(c->d_row_ptr); dfree(c->d_col);
   dfree(c->d_bptr); dfree(c->d_bcontrib); dfree(c->d_fptr); dfree(c->d_fcontrib); dfree(c->d_tab);
-  dfree(c->d_coef); dfree(c->d_f); dfree(c->d_Ke); dfree(c->d_Fe); dfree(c->d_K); dfree(c->d_F);
-  dfree(c->d_Ke32); dfree(c->d_status); dfree(c->d_bad);
+  dfree(c->d_coef); dfree(c->d_f); dfree(c->d_Kdiag); dfree(c->d_Koff); dfree(c->d_Fe); dfree(c->d_K);
+  dfree(c->d_F); dfree(c->d_Koff32); dfree(c->d_status); dfree(c->d_bad);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
   delete c;
   return LMG_OK;
@@ -477,7 +501,10 @@ lmg_status lmg_sparsity_build(lmg_ctx *c, int64_t *nnz) {
   if (st) return st;
   LMG_CUDA(c, dalloc(c->d_K, (size_t)c->nnz));
   LMG_CUDA(c, dalloc(c->d_F, (size_t)c->n_dofs));
-  LMG_CUDA(c, dalloc(c->d_Ke, (size_t)(c->n_elem * c->nl * c->nl)));
+  const size_t b2 = (size_t)c->bs * c->bs, no = (size_t)c->nb * (c->nb - 1) / 2;
+  LMG_CUDA(c, dalloc(c->d_Kdiag, (size_t)c->n_elem * c->nb * b2));
+  LMG_CUDA(c, dalloc(c->d_Koff, (size_t)c->n_elem * no * b2));
+  dfree(c->d_Koff32);  // allocated on the first mixed assembly
   LMG_CUDA(c, dalloc(c->d_Fe, (size_t)(c->n_elem * c->nl)));
   c->have_sparsity = true;
   if (nnz) *nnz = c->nnz;
@@ -517,6 +544,8 @@ lmg_status lmg_form_set(lmg_ctx *c, int32_t form, int32_t fe_order, int32_t q_or
   if (t.n != c->npe || t.n_geo != c->npe)
     return fail(c, LMG_ERR_UNSUPPORTED, "form_set: only isoparametric LAGRANGE elements are built");
   if (t.q > 27) return fail(c, LMG_ERR_UNSUPPORTED, "form_set: more than 27 quadrature points");
+  if (c->bs != c->n_vars)
+    return fail(c, LMG_ERR_UNSUPPORTED, "form_set: variables must be node-interleaved (one VariableGroup)");
   if (!elements_built(form, t.n, c->n_vars))
     return fail(c, LMG_ERR_UNSUPPORTED, "form_set: no element kernel for this form / element");
   c->tab = t;
@@ -575,8 +604,10 @@ lmg_status lmg_assemble(lmg_ctx *c, int32_t precision, double *K, double *F, int
   if (!c->have_sparsity) return fail(c, LMG_ERR_STATE, "assemble: build the sparsity first");
   if (!c->have_form) return fail(c, LMG_ERR_STATE, "assemble: set the form first");
   if (precision != LMG_FP64 && precision != LMG_MIXED) return fail(c, LMG_ERR_ARG, "assemble: unknown precision");
-  if (precision == LMG_MIXED) return fail(c, LMG_ERR_UNSUPPORTED, "assemble: mixed form not built yet");
   cudaSetDevice(c->device);
+  const bool mixed = precision == LMG_MIXED;
+  if (mixed && !c->d_Koff32)
+    LMG_CUDA(c, dalloc(c->d_Koff32, (size_t)c->n_elem * c->nb * (c->nb - 1) / 2 * c->bs * c->bs));
   lmg_status st = reset_status(c);
   if (st) return st;
   ElemArgs a{};
@@ -587,7 +618,9 @@ lmg_status lmg_assemble(lmg_ctx *c, int32_t precision, double *K, double *F, int
   a.nodal_f = c->d_f;
   a.cmask = c->d_cmask;
   a.nu = c->nu;
-  a.Ke = c->d_Ke;
+  a.Kdiag = c->d_Kdiag;
+  a.Koff = c->d_Koff;
+  a.Koff32 = c->d_Koff32;
   a.Fe = c->d_Fe;
   a.status = c->d_status;
   a.bad_elem = c->d_bad;
@@ -602,13 +635,13 @@ lmg_status lmg_assemble(lmg_ctx *c, int32_t precision, double *K, double *F, int
   if (!c->h_aff.empty()) {
     a.n_list = (int64_t)c->h_aff.size();
     a.list = c->d_aff;
-    launch_elements(c->form, c->tab.n, c->n_vars, true, a, grid, c->stream);
+    launch_elements(c->form, c->tab.n, c->n_vars, true, mixed, a, grid, c->stream);
     c->launches++;
   }
   if (!c->h_gen.empty()) {
     a.n_list = (int64_t)c->h_gen.size();
     a.list = c->d_gen;
-    launch_elements(c->form, c->tab.n, c->n_vars, false, a, grid, c->stream);
+    launch_elements(c->form, c->tab.n, c->n_vars, false, mixed, a, grid, c->stream);
     c->launches++;
   }
   if (c->perflog) LMG_CUDA(c, cudaEventRecord(e3[1], c->stream));
@@ -618,16 +651,19 @@ lmg_status lmg_assemble(lmg_ctx *c, int32_t precision, double *K, double *F, int
   g.nb = c->nb;
   g.brow_ptr = c->d_brow_ptr;
   g.row_ptr = c->d_row_ptr;
+  g.bcol = c->d_bcol;
   g.bptr = c->d_bptr;
   g.bcontrib = c->d_bcontrib;
+  g.no = c->nb * (c->nb - 1) / 2;
   g.fptr = c->d_fptr;
   g.fcontrib = c->d_fcontrib;
-  g.Ke = c->d_Ke;
-  g.Ke32 = c->d_Ke32;
+  g.Kdiag = c->d_Kdiag;
+  g.Koff = c->d_Koff;
+  g.Koff32 = c->d_Koff32;
   g.Fe = c->d_Fe;
   g.K = c->d_K;
   g.F = c->d_F;
-  launch_gather(g, false, c->stream);
+  launch_gather(g, mixed, c->stream);
   c->launches++;
   if (c->perflog) LMG_CUDA(c, cudaEventRecord(e3[2], c->stream));
   LMG_CUDA(c, cudaGetLastError());
@@ -660,6 +696,32 @@ lmg_status lmg_last_error(lmg_ctx *c, int64_t *elem_id, char *msg, int32_t msg_l
     std::strncpy(msg, c->err.c_str(), (size_t)msg_len - 1);
     msg[msg_len - 1] = 0;
   }
+  return LMG_OK;
+}
+
+lmg_status lmg_cg_solve(lmg_ctx *c, const double *rhs, double *x, double rtol, int32_t maxit,
+                        int32_t *iters, double *relres) {
+  if (!c || !x || rtol <= 0 || maxit <= 0) return fail(c, LMG_ERR_ARG, "cg_solve: bad argument");
+  if (!c->have_sparsity) return fail(c, LMG_ERR_STATE, "cg_solve: assemble first");
+  cudaSetDevice(c->device);
+  double *b = c->d_F, *dx = nullptr, *db = nullptr;
+  LMG_CUDA(c, dalloc(dx, (size_t)c->n_dofs));
+  if (rhs) {
+    LMG_CUDA(c, dupload(c, db, rhs, (size_t)c->n_dofs));
+    b = db;
+  }
+  int it = 0;
+  double rr = 0.0;
+  const int st = cg_solve(c->n_dofs, c->d_row_ptr, c->d_col, c->d_K, b, dx, rtol, maxit, c->stream, c->n_sm,
+                          &it, &rr, &c->launches);
+  if (st == 0)
+    LMG_CUDA(c, cudaMemcpyAsync(x, dx, sizeof(double) * c->n_dofs, cudaMemcpyDeviceToHost, c->stream));
+  LMG_CUDA(c, cudaStreamSynchronize(c->stream));
+  dfree(dx);
+  dfree(db);
+  if (st) return fail(c, st == 7 ? LMG_ERR_OOM : LMG_ERR_CUDA, "cg_solve: device failure");
+  if (iters) *iters = it;
+  if (relres) *relres = rr;
   return LMG_OK;
 }
 

@@ -20,6 +20,14 @@
 // Dirichlet rows/columns are applied in the epilogue: a constrained local dof
 // gets a zero row and column with 1 on the diagonal and a zero load, which is
 // what C^T K C and C^T F give for an empty constraint row.
+//
+// Both forms are symmetric (K^{ik}_{ab} = K^{ki}_{ba}), so only the n diagonal
+// blocks and the n(n-1)/2 strictly upper blocks are computed and stored; the
+// gather reads a lower block as the transpose of its upper partner.
+// The mixed form (T = float) contracts in FP32 and then rebuilds each diagonal
+// block in FP64 as minus the sum of the stored off-diagonal blocks of its block
+// row, so every rigid translation stays exactly in the kernel of the element
+// matrix (sum_b dphi_b = 0 makes that identity exact in real arithmetic).
 #include <cuda_runtime.h>
 
 #include "assemble.cuh"
@@ -113,17 +121,80 @@ __device__ __forceinline__ void element_tensor(const double G[9], double det, do
   }
 }
 
-template <int FORM, int N, int NV>
+// Strictly upper block index o of (a, b), a < b, and its inverse.
+__host__ __device__ constexpr int off_index(int N, int a, int b) { return a * N - a * (a + 1) / 2 + (b - a - 1); }
+
+template <int N>
+__device__ __forceinline__ void build_pairs(uint16_t *pair) {
+  for (int o = threadIdx.x; o < N * (N - 1) / 2; o += blockDim.x) {
+    int a = 0, rem = o;
+    while (rem >= N - 1 - a) { rem -= N - 1 - a; ++a; }
+    pair[o] = (uint16_t)((a << 8) | (a + 1 + rem));
+  }
+}
+
+// Dirichlet epilogue of one entry (local rows lr, lc).
+__device__ __forceinline__ double masked(double v, uint64_t mask, int lr, int lc) {
+  if (((mask >> lr) | (mask >> lc)) & 1ull) return (lr == lc) ? 1.0 : 0.0;
+  return v;
+}
+
+// Mixed form: diagonal blocks as minus the FP64 sum of the stored FP32
+// off-diagonal blocks of the block row (read from the per-warp stage).
+template <int N, int NV>
+__device__ __forceinline__ void diag_from_rows(const float *stage, uint64_t mask, int lane, double *Kd) {
+  constexpr int B2 = NV * NV;
+  for (int a = lane; a < N; a += 32) {
+    double d[B2];
+#pragma unroll
+    for (int ik = 0; ik < B2; ++ik) d[ik] = 0.0;
+    for (int b = 0; b < N; ++b) {
+      if (b == a) continue;
+      const float *blk = stage + (a < b ? off_index(N, a, b) : off_index(N, b, a)) * B2;
+#pragma unroll
+      for (int i = 0; i < NV; ++i)
+#pragma unroll
+        for (int k = 0; k < NV; ++k) d[i * NV + k] -= (double)(a < b ? blk[i * NV + k] : blk[k * NV + i]);
+    }
+#pragma unroll
+    for (int i = 0; i < NV; ++i)
+#pragma unroll
+      for (int k = 0; k < NV; ++k) Kd[a * B2 + i * NV + k] = masked(d[i * NV + k], mask, i * N + a, k * N + a);
+  }
+}
+
+// Byte offsets of the affine kernel's dynamic shared memory (4 warps per CTA).
+__host__ __device__ constexpr size_t al16(size_t x) { return (x + 15) & ~(size_t)15; }
+template <int FORM, int N, int NV, typename T>
+struct AffineSmem {
+  static constexpr int NA = (FORM == LMG_POISSON) ? 9 : 81;
+  static constexpr int NO = N * (N - 1) / 2;
+  static constexpr bool MIXED = sizeof(T) == 4;
+  static constexpr size_t S = 0;
+  static constexpr size_t A = S + al16(sizeof(T) * 9 * N * N);
+  static constexpr size_t MASK = A + al16(sizeof(T) * 4 * 32 * NA);
+  static constexpr size_t PAIR = MASK + al16(sizeof(uint64_t) * 4 * 32);
+  static constexpr size_t STAGE = PAIR + al16(sizeof(uint16_t) * (NO > 0 ? NO : 1));
+  static constexpr size_t BYTES = STAGE + al16(MIXED ? sizeof(float) * 4 * NO * NV * NV : 0);
+};
+
+template <int FORM, int N, int NV, typename T>
 __global__ void __launch_bounds__(128) k_elem_affine(ElemArgs a) {
+  constexpr bool MIXED = sizeof(T) == 4;
   constexpr int NA = (FORM == LMG_POISSON) ? 9 : 81;
-  constexpr int NB = N * N;
-  constexpr int BPL = (NB + 31) / 32;
-  extern __shared__ double smem[];
-  double *sS = smem;                                   // [9][N][N]
+  constexpr int NB = N * N, NO = N * (N - 1) / 2, B2 = NV * NV;
+  constexpr int NWORK = MIXED ? NO : N + NO;  // blocks computed by the contraction
+  constexpr int BPL = (NWORK + 31) / 32;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  using L = AffineSmem<FORM, N, NV, T>;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  double *sA = sS + 9 * NB + warp * 32 * NA;           // [32][NA]
-  uint64_t *sMask = reinterpret_cast<uint64_t *>(smem + 9 * NB + 4 * 32 * NA) + warp * 32;
-  for (int i = threadIdx.x; i < 9 * NB; i += blockDim.x) sS[i] = a.fe.S[i];
+  T *sS = reinterpret_cast<T *>(smem_raw + L::S);                       // [9][N][N]
+  T *sA = reinterpret_cast<T *>(smem_raw + L::A) + warp * 32 * NA;      // [32][NA]
+  uint64_t *sMask = reinterpret_cast<uint64_t *>(smem_raw + L::MASK) + warp * 32;
+  uint16_t *sPair = reinterpret_cast<uint16_t *>(smem_raw + L::PAIR);   // [NO]
+  float *sStage = reinterpret_cast<float *>(smem_raw + L::STAGE) + warp * (MIXED ? NO * B2 : 0);
+  for (int i = threadIdx.x; i < 9 * NB; i += blockDim.x) sS[i] = (T)a.fe.S[i];
+  build_pairs<N>(sPair);
   __syncthreads();
 
   const int64_t n_tiles = (a.n_list + 31) / 32;
@@ -144,17 +215,19 @@ __global__ void __launch_bounds__(128) k_elem_affine(ElemArgs a) {
       const double det = jacobian(X, a.fe.gdphi, N, G);
       if (!(det > 0.0)) report_bad(a, LMG_ERR_DEGENERATE, e);
       const double coef = a.coef ? a.coef[e] : 1.0;
-      element_tensor<FORM>(G, det, coef, a.nu, sA + lane * NA);
+      double A[NA];
+      element_tensor<FORM>(G, det, coef, a.nu, A);
+#pragma unroll
+      for (int i = 0; i < NA; ++i) sA[lane * NA + i] = (T)A[i];
       const uint64_t mask = a.cmask[e];
       sMask[lane] = mask;
-      // Load vector: Fe_a^i = detJ sum_b M_ab f_b^i (f interpolated with phi).
+      // Load vector: Fe_a^i = detJ sum_b M_ab f_b^i (f interpolated with phi), FP64.
       double *Fo = a.Fe + (int64_t)e * N * NV;
       for (int ai = 0; ai < N; ++ai)
         for (int v = 0; v < NV; ++v) {
           double s = 0.0;
           if (a.nodal_f)
-            for (int b = 0; b < N; ++b)
-              s += a.fe.M[ai * N + b] * a.nodal_f[(int64_t)c[b] * NV + v];
+            for (int b = 0; b < N; ++b) s += a.fe.M[ai * N + b] * a.nodal_f[(int64_t)c[b] * NV + v];
           s *= det;
           if ((mask >> (v * N + ai)) & 1ull) s = 0.0;
           Fo[ai * NV + v] = s;
@@ -164,56 +237,71 @@ __global__ void __launch_bounds__(128) k_elem_affine(ElemArgs a) {
     for (int t = 0; t < 32; ++t) {
       const int32_t et = __shfl_sync(FULL, e, t);
       if (et < 0) break;
-      const double *At = sA + t * NA;
+      const T *At = sA + t * NA;
       const uint64_t mask = sMask[t];
-      double *Ko = a.Ke + (int64_t)et * NB * NV * NV;
 #pragma unroll
       for (int k = 0; k < BPL; ++k) {
-        const int blk = lane + 32 * k;
-        if (blk < NB) {
-          const int ra = blk / N, cb = blk - ra * N;
-          double sv[9];
+        const int w = lane + 32 * k;
+        if (w < NWORK) {
+          int ra, cb, o;
+          if (!MIXED && w < N) { ra = cb = w; o = -1; }
+          else { o = MIXED ? w : w - N; ra = sPair[o] >> 8; cb = sPair[o] & 0xff; }
+          const int blk = ra * N + cb;
+          T sv[9];
 #pragma unroll
           for (int mn = 0; mn < 9; ++mn) sv[mn] = sS[mn * NB + blk];
 #pragma unroll
-          for (int ik = 0; ik < NV * NV; ++ik) {
+          for (int ik = 0; ik < B2; ++ik) {
             const int i = ik / NV, kk = ik - i * NV;
-            double acc = 0.0;
+            T acc = 0;
 #pragma unroll
             for (int mn = 0; mn < 9; ++mn) acc = fma(At[ik * 9 + mn], sv[mn], acc);
             const int lr = i * N + ra, lc = kk * N + cb;
-            if (((mask >> lr) | (mask >> lc)) & 1ull) acc = (lr == lc) ? 1.0 : 0.0;
-            Ko[blk * NV * NV + ik] = acc;
+            if (o < 0) {
+              a.Kdiag[((int64_t)et * N + ra) * B2 + ik] = masked((double)acc, mask, lr, lc);
+            } else if (MIXED) {
+              sStage[o * B2 + ik] = (float)acc;
+              a.Koff32[((int64_t)et * NO + o) * B2 + ik] = (float)masked((double)acc, mask, lr, lc);
+            } else {
+              a.Koff[((int64_t)et * NO + o) * B2 + ik] = masked((double)acc, mask, lr, lc);
+            }
           }
         }
+      }
+      if (MIXED) {
+        __syncwarp();
+        diag_from_rows<N, NV>(sStage, mask, lane, a.Kdiag + (int64_t)et * N * B2);
+        __syncwarp();
       }
     }
     __syncwarp();
   }
 }
 
-template <int FORM, int N, int NV>
+template <int FORM, int N, int NV, typename T>
 __global__ void __launch_bounds__(128) k_elem_general(ElemArgs a) {
-  constexpr int NB = N * N;
+  constexpr bool MIXED = sizeof(T) == 4;
+  constexpr int NB = N * N, NO = N * (N - 1) / 2, B2 = NV * NV;
   constexpr int BPL = (NB + 31) / 32;
   constexpr int MAXQ = 27;
-  __shared__ double sX[4][27 * 3];
+  __shared__ double sX[4][N * 3];
   __shared__ double sGeo[4][MAXQ][10];  // G (9) and JxW per qp
   __shared__ double sGr[4][N * 3];      // physical gradients at the current qp
   __shared__ double sF[4][N * NV];      // nodal load of the element
+  __shared__ float sStage[4][MIXED ? NO * B2 : 1];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int n_geo = a.fe.n_geo, Q = a.fe.q;
+  const int Q = a.fe.q;
   for (int64_t li = (int64_t)blockIdx.x * 4 + warp; li < a.n_list; li += (int64_t)gridDim.x * 4) {
     const int32_t e = a.list[li];
     const int32_t *c = a.conn + (int64_t)e * a.npe;
-    for (int i = lane; i < n_geo * 3; i += 32) sX[warp][i] = a.xyz[3 * (int64_t)c[i / 3] + i % 3];
+    for (int i = lane; i < N * 3; i += 32) sX[warp][i] = a.xyz[3 * (int64_t)c[i / 3] + i % 3];
     for (int i = lane; i < N * NV; i += 32)
       sF[warp][i] = a.nodal_f ? a.nodal_f[(int64_t)c[i / NV] * NV + i % NV] : 0.0;
     __syncwarp();
     const double coef = a.coef ? a.coef[e] : 1.0;
     for (int q = lane; q < Q; q += 32) {
       double G[9];
-      const double det = jacobian(sX[warp], a.fe.gdphi + (int64_t)q * n_geo * 3, n_geo, G);
+      const double det = jacobian(sX[warp], a.fe.gdphi + (int64_t)q * N * 3, N, G);
       if (!(det > 0.0)) report_bad(a, LMG_ERR_DEGENERATE, e);
       for (int i = 0; i < 9; ++i) sGeo[warp][q][i] = G[i];
       sGeo[warp][q][9] = det * a.fe.qw[q];
@@ -221,11 +309,11 @@ __global__ void __launch_bounds__(128) k_elem_general(ElemArgs a) {
     __syncwarp();
     double lam = 0.0, mu = 0.0;
     if (FORM == LMG_ELASTICITY) lame(coef, a.nu, lam, mu);
-    double acc[BPL][NV * NV];
+    T acc[BPL][B2];
 #pragma unroll
     for (int k = 0; k < BPL; ++k)
 #pragma unroll
-      for (int ik = 0; ik < NV * NV; ++ik) acc[k][ik] = 0.0;
+      for (int ik = 0; ik < B2; ++ik) acc[k][ik] = 0;
     double facc[NV];
 #pragma unroll
     for (int v = 0; v < NV; ++v) facc[v] = 0.0;
@@ -237,55 +325,71 @@ __global__ void __launch_bounds__(128) k_elem_general(ElemArgs a) {
         sGr[warp][i] = r[0] * Gq[d] + r[1] * Gq[3 + d] + r[2] * Gq[6 + d];
       }
       __syncwarp();
-      const double jxw = Gq[9];
+      const T jxw = (T)Gq[9];
 #pragma unroll
       for (int k = 0; k < BPL; ++k) {
         const int blk = lane + 32 * k;
         if (blk < NB) {
           const int ra = blk / N, cb = blk - ra * N;
-          const double *ga = sGr[warp] + 3 * ra, *gb = sGr[warp] + 3 * cb;
-          const double dot = ga[0] * gb[0] + ga[1] * gb[1] + ga[2] * gb[2];
-          if (FORM == LMG_POISSON) {
-            acc[k][0] += jxw * coef * dot;
-          } else {
+          if (ra <= cb) {
+            T ga[3], gb[3];
 #pragma unroll
-            for (int i = 0; i < 3; ++i)
+            for (int d = 0; d < 3; ++d) { ga[d] = (T)sGr[warp][3 * ra + d]; gb[d] = (T)sGr[warp][3 * cb + d]; }
+            const T dot = ga[0] * gb[0] + ga[1] * gb[1] + ga[2] * gb[2];
+            if (FORM == LMG_POISSON) {
+              acc[k][0] += jxw * (T)coef * dot;
+            } else {
 #pragma unroll
-              for (int kk = 0; kk < 3; ++kk) {
-                double v = lam * ga[i] * gb[kk] + mu * ga[kk] * gb[i];
-                if (i == kk) v += mu * dot;
-                acc[k][3 * i + kk] += jxw * v;
-              }
+              for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int kk = 0; kk < 3; ++kk) {
+                  T v = (T)lam * ga[i] * gb[kk] + (T)mu * ga[kk] * gb[i];
+                  if (i == kk) v += (T)mu * dot;
+                  acc[k][3 * i + kk] += jxw * v;
+                }
+            }
           }
         }
       }
-      if (lane < N) {  // load vector, lane = shape a
+      if (lane < N) {  // load vector, lane = shape a (FP64)
         const double *ph = a.fe.phi + (int64_t)q * N;
 #pragma unroll
         for (int v = 0; v < NV; ++v) {
           double fq = 0.0;
           for (int b = 0; b < N; ++b) fq += ph[b] * sF[warp][b * NV + v];
-          facc[v] += jxw * fq * ph[lane];
+          facc[v] += Gq[9] * fq * ph[lane];
         }
       }
       __syncwarp();
     }
     const uint64_t mask = a.cmask[e];
-    double *Ko = a.Ke + (int64_t)e * NB * NV * NV;
 #pragma unroll
     for (int k = 0; k < BPL; ++k) {
       const int blk = lane + 32 * k;
       if (blk < NB) {
         const int ra = blk / N, cb = blk - ra * N;
+        if (ra > cb || (MIXED && ra == cb)) continue;
 #pragma unroll
-        for (int ik = 0; ik < NV * NV; ++ik) {
+        for (int ik = 0; ik < B2; ++ik) {
           const int i = ik / NV, kk = ik - i * NV;
-          const int lr = i * N + ra, lc = kk * N + cb;
-          double v = acc[k][ik];
-          if (((mask >> lr) | (mask >> lc)) & 1ull) v = (lr == lc) ? 1.0 : 0.0;
-          Ko[blk * NV * NV + ik] = v;
+          const double v = masked((double)acc[k][ik], mask, i * N + ra, kk * N + cb);
+          if (ra == cb) {
+            a.Kdiag[((int64_t)e * N + ra) * B2 + ik] = v;
+          } else {
+            const int o = off_index(N, ra, cb);
+            if (MIXED) {
+              sStage[warp][o * B2 + ik] = (float)acc[k][ik];
+              a.Koff32[((int64_t)e * NO + o) * B2 + ik] = (float)v;
+            } else {
+              a.Koff[((int64_t)e * NO + o) * B2 + ik] = v;
+            }
+          }
         }
       }
+    }
+    if (MIXED) {
+      __syncwarp();
+      diag_from_rows<N, NV>(sStage[warp], mask, lane, a.Kdiag + (int64_t)e * N * B2);
     }
     if (lane < N) {
 #pragma unroll
@@ -299,20 +403,18 @@ __global__ void __launch_bounds__(128) k_elem_general(ElemArgs a) {
   }
 }
 
-template <int FORM, int N, int NV>
+template <int FORM, int N, int NV, typename T>
 void launch_t(bool affine, const ElemArgs &a, int grid, cudaStream_t s) {
   if (a.n_list <= 0) return;
   if (affine) {
-    constexpr int NA = (FORM == LMG_POISSON) ? 9 : 81;
-    const size_t sm = sizeof(double) * (9 * N * N + 4 * 32 * NA) + sizeof(uint64_t) * 4 * 32;
-    cudaFuncSetAttribute(k_elem_affine<FORM, N, NV>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)sm);
+    const size_t sm = AffineSmem<FORM, N, NV, T>::BYTES;
+    cudaFuncSetAttribute(k_elem_affine<FORM, N, NV, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     const int64_t tiles = (a.n_list + 31) / 32;
     const int64_t blocks = (tiles + 3) / 4;
-    k_elem_affine<FORM, N, NV><<<(int)(blocks < grid ? blocks : grid), 128, sm, s>>>(a);
+    k_elem_affine<FORM, N, NV, T><<<(int)(blocks < grid ? blocks : grid), 128, sm, s>>>(a);
   } else {
     const int64_t blocks = (a.n_list + 3) / 4;
-    k_elem_general<FORM, N, NV><<<(int)(blocks < grid ? blocks : grid), 128, 0, s>>>(a);
+    k_elem_general<FORM, N, NV, T><<<(int)(blocks < grid ? blocks : grid), 128, 0, s>>>(a);
   }
 }
 
@@ -323,12 +425,13 @@ bool elements_built(int form, int n, int nv) {
          (form == LMG_ELASTICITY && nv == 3 && (n == 4 || n == 8 || n == 10));
 }
 
-void launch_elements(int form, int n, int nv, bool affine, const ElemArgs &a, int grid,
+void launch_elements(int form, int n, int nv, bool affine, bool mixed, const ElemArgs &a, int grid,
                      cudaStream_t s) {
-#define LMG_CASE(F, NN, V)                                   \
-  if (form == F && n == NN && nv == V) {                     \
-    launch_t<F, NN, V>(affine, a, grid, s);                  \
-    return;                                                  \
+#define LMG_CASE(F, NN, V)                                                      \
+  if (form == F && n == NN && nv == V) {                                        \
+    if (mixed) launch_t<F, NN, V, float>(affine, a, grid, s);                   \
+    else launch_t<F, NN, V, double>(affine, a, grid, s);                        \
+    return;                                                                     \
   }
   LMG_CASE(LMG_POISSON, 4, 1)
   LMG_CASE(LMG_POISSON, 8, 1)
