@@ -60,6 +60,7 @@ struct GatherArgs {
   const double *Koff;
   const float *Koff32;
   const double *Fe;
+  const uint8_t *constrained; // [n_dofs] (mixed form applies the Dirichlet rows here)
   double *K;
   double *F;
 };

@@ -40,6 +40,7 @@ struct lmg_ctx {
   // constraints
   std::vector<uint8_t> h_constrained;
   uint64_t *d_cmask = nullptr;
+  uint8_t *d_cons = nullptr;
   // sparsity and plan
   bool have_sparsity = false;
   int64_t nnz = 0, nnzb = 0;
@@ -362,6 +363,9 @@ lmg_status upload_cmask(lmg_ctx *c) {
       for (int l = 0; l < c->nl; ++l)
         if (c->h_constrained[(size_t)c->h_elem_dofs[(size_t)(e * c->nl + l)]]) m[(size_t)e] |= 1ull << l;
   LMG_CUDA(c, dupload(c, c->d_cmask, m.data(), m.size()));
+  std::vector<uint8_t> cons = c->h_constrained;
+  cons.resize((size_t)c->n_dofs, 0);
+  LMG_CUDA(c, dupload(c, c->d_cons, cons.data(), cons.size()));
   LMG_CUDA(c, cudaStreamSynchronize(c->stream));
   return LMG_OK;
 }
@@ -401,7 +405,7 @@ lmg_status lmg_context_destroy(lmg_ctx *c) {
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
   dfree(c->d_xyz); dfree(c->d_conn); dfree(c->d_aff); dfree(c->d_gen); dfree(c->d_eb);
-  dfree(c->d_cmask); dfree(c->d_brow_ptr); dfree(c->d_bcol); dfree(c->d_row_ptr); dfree(c->d_col);
+  dfree(c->d_cmask); dfree(c->d_cons); dfree(c->d_brow_ptr); dfree(c->d_bcol); dfree(c->d_row_ptr); dfree(c->d_col);
   dfree(c->d_bptr); dfree(c->d_bcontrib); dfree(c->d_fptr); dfree(c->d_fcontrib); dfree(c->d_tab);
   dfree(c->d_coef); dfree(c->d_f); dfree(c->d_Kdiag); dfree(c->d_Koff); dfree(c->d_Fe); dfree(c->d_K);
   dfree(c->d_F); dfree(c->d_Koff32); dfree(c->d_status); dfree(c->d_bad);
@@ -661,6 +665,7 @@ lmg_status lmg_assemble(lmg_ctx *c, int32_t precision, double *K, double *F, int
   g.Koff = c->d_Koff;
   g.Koff32 = c->d_Koff32;
   g.Fe = c->d_Fe;
+  g.constrained = c->d_cons;
   g.K = c->d_K;
   g.F = c->d_F;
   launch_gather(g, mixed, c->stream);

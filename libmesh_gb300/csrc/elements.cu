@@ -24,10 +24,12 @@
 // Both forms are symmetric (K^{ik}_{ab} = K^{ki}_{ba}), so only the n diagonal
 // blocks and the n(n-1)/2 strictly upper blocks are computed and stored; the
 // gather reads a lower block as the transpose of its upper partner.
-// The mixed form (T = float) contracts in FP32 and then rebuilds each diagonal
-// block in FP64 as minus the sum of the stored off-diagonal blocks of its block
-// row, so every rigid translation stays exactly in the kernel of the element
-// matrix (sum_b dphi_b = 0 makes that identity exact in real arithmetic).
+// The mixed form (T = float) contracts only the off-diagonal blocks, in FP32,
+// and stores them without the Dirichlet epilogue; the insertion kernel applies
+// the constraints and rebuilds every diagonal block of the global matrix as
+// minus the (double-float accumulated) sum of its row's off-diagonal blocks.
+// That identity is exact in real arithmetic because sum_b dphi_b = 0, and
+// enforcing it keeps every rigid translation in the kernel of K.
 #include <cuda_runtime.h>
 
 #include "assemble.cuh"
@@ -139,43 +141,17 @@ __device__ __forceinline__ double masked(double v, uint64_t mask, int lr, int lc
   return v;
 }
 
-// Mixed form: diagonal blocks as minus the FP64 sum of the stored FP32
-// off-diagonal blocks of the block row (read from the per-warp stage).
-template <int N, int NV>
-__device__ __forceinline__ void diag_from_rows(const float *stage, uint64_t mask, int lane, double *Kd) {
-  constexpr int B2 = NV * NV;
-  for (int a = lane; a < N; a += 32) {
-    double d[B2];
-#pragma unroll
-    for (int ik = 0; ik < B2; ++ik) d[ik] = 0.0;
-    for (int b = 0; b < N; ++b) {
-      if (b == a) continue;
-      const float *blk = stage + (a < b ? off_index(N, a, b) : off_index(N, b, a)) * B2;
-#pragma unroll
-      for (int i = 0; i < NV; ++i)
-#pragma unroll
-        for (int k = 0; k < NV; ++k) d[i * NV + k] -= (double)(a < b ? blk[i * NV + k] : blk[k * NV + i]);
-    }
-#pragma unroll
-    for (int i = 0; i < NV; ++i)
-#pragma unroll
-      for (int k = 0; k < NV; ++k) Kd[a * B2 + i * NV + k] = masked(d[i * NV + k], mask, i * N + a, k * N + a);
-  }
-}
-
 // Byte offsets of the affine kernel's dynamic shared memory (4 warps per CTA).
 __host__ __device__ constexpr size_t al16(size_t x) { return (x + 15) & ~(size_t)15; }
 template <int FORM, int N, int NV, typename T>
 struct AffineSmem {
   static constexpr int NA = (FORM == LMG_POISSON) ? 9 : 81;
   static constexpr int NO = N * (N - 1) / 2;
-  static constexpr bool MIXED = sizeof(T) == 4;
   static constexpr size_t S = 0;
   static constexpr size_t A = S + al16(sizeof(T) * 9 * N * N);
   static constexpr size_t MASK = A + al16(sizeof(T) * 4 * 32 * NA);
   static constexpr size_t PAIR = MASK + al16(sizeof(uint64_t) * 4 * 32);
-  static constexpr size_t STAGE = PAIR + al16(sizeof(uint16_t) * (NO > 0 ? NO : 1));
-  static constexpr size_t BYTES = STAGE + al16(MIXED ? sizeof(float) * 4 * NO * NV * NV : 0);
+  static constexpr size_t BYTES = PAIR + al16(sizeof(uint16_t) * (NO > 0 ? NO : 1));
 };
 
 template <int FORM, int N, int NV, typename T>
@@ -192,7 +168,6 @@ __global__ void __launch_bounds__(128) k_elem_affine(ElemArgs a) {
   T *sA = reinterpret_cast<T *>(smem_raw + L::A) + warp * 32 * NA;      // [32][NA]
   uint64_t *sMask = reinterpret_cast<uint64_t *>(smem_raw + L::MASK) + warp * 32;
   uint16_t *sPair = reinterpret_cast<uint16_t *>(smem_raw + L::PAIR);   // [NO]
-  float *sStage = reinterpret_cast<float *>(smem_raw + L::STAGE) + warp * (MIXED ? NO * B2 : 0);
   for (int i = threadIdx.x; i < 9 * NB; i += blockDim.x) sS[i] = (T)a.fe.S[i];
   build_pairs<N>(sPair);
   __syncthreads();
@@ -260,18 +235,12 @@ __global__ void __launch_bounds__(128) k_elem_affine(ElemArgs a) {
             if (o < 0) {
               a.Kdiag[((int64_t)et * N + ra) * B2 + ik] = masked((double)acc, mask, lr, lc);
             } else if (MIXED) {
-              sStage[o * B2 + ik] = (float)acc;
-              a.Koff32[((int64_t)et * NO + o) * B2 + ik] = (float)masked((double)acc, mask, lr, lc);
+              a.Koff32[((int64_t)et * NO + o) * B2 + ik] = (float)acc;
             } else {
               a.Koff[((int64_t)et * NO + o) * B2 + ik] = masked((double)acc, mask, lr, lc);
             }
           }
         }
-      }
-      if (MIXED) {
-        __syncwarp();
-        diag_from_rows<N, NV>(sStage, mask, lane, a.Kdiag + (int64_t)et * N * B2);
-        __syncwarp();
       }
     }
     __syncwarp();
@@ -288,7 +257,6 @@ __global__ void __launch_bounds__(128) k_elem_general(ElemArgs a) {
   __shared__ double sGeo[4][MAXQ][10];  // G (9) and JxW per qp
   __shared__ double sGr[4][N * 3];      // physical gradients at the current qp
   __shared__ double sF[4][N * NV];      // nodal load of the element
-  __shared__ float sStage[4][MIXED ? NO * B2 : 1];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int Q = a.fe.q;
   for (int64_t li = (int64_t)blockIdx.x * 4 + warp; li < a.n_list; li += (int64_t)gridDim.x * 4) {
@@ -375,21 +343,13 @@ __global__ void __launch_bounds__(128) k_elem_general(ElemArgs a) {
           const double v = masked((double)acc[k][ik], mask, i * N + ra, kk * N + cb);
           if (ra == cb) {
             a.Kdiag[((int64_t)e * N + ra) * B2 + ik] = v;
+          } else if (MIXED) {
+            a.Koff32[((int64_t)e * NO + off_index(N, ra, cb)) * B2 + ik] = (float)acc[k][ik];
           } else {
-            const int o = off_index(N, ra, cb);
-            if (MIXED) {
-              sStage[warp][o * B2 + ik] = (float)acc[k][ik];
-              a.Koff32[((int64_t)e * NO + o) * B2 + ik] = (float)v;
-            } else {
-              a.Koff[((int64_t)e * NO + o) * B2 + ik] = v;
-            }
+            a.Koff[((int64_t)e * NO + off_index(N, ra, cb)) * B2 + ik] = v;
           }
         }
       }
-    }
-    if (MIXED) {
-      __syncwarp();
-      diag_from_rows<N, NV>(sStage[warp], mask, lane, a.Kdiag + (int64_t)e * N * B2);
     }
     if (lane < N) {
 #pragma unroll

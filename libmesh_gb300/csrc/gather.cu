@@ -70,6 +70,117 @@ __global__ void __launch_bounds__(256) k_gather(GatherArgs g, const TO *Koff) {
   }
 }
 
+// ---- mixed form: double-float (pair of FP32) accumulation on the FP32 pipe.
+// two_sum / fast_two_sum are Knuth's and Dekker's exact-error additions; the
+// __fadd_rn intrinsics keep the compiler from contracting or reassociating them.
+struct DF { float hi, lo; };
+__device__ __forceinline__ DF two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+  return {s, e};
+}
+__device__ __forceinline__ DF df_add(DF x, DF y) {
+  DF s = two_sum(x.hi, y.hi);
+  const float lo = __fadd_rn(s.lo, __fadd_rn(x.lo, y.lo));
+  const float hi = __fadd_rn(s.hi, lo);
+  return {hi, __fsub_rn(lo, __fsub_rn(hi, s.hi))};
+}
+__device__ __forceinline__ DF df_add1(DF x, float y) {
+  DF s = two_sum(x.hi, y);
+  const float lo = __fadd_rn(s.lo, x.lo);
+  const float hi = __fadd_rn(s.hi, lo);
+  return {hi, __fsub_rn(lo, __fsub_rn(hi, s.hi))};
+}
+// Exact float -> double by moving the bits (keeps the FP64 pipe free); zero,
+// subnormal, inf and NaN take the hardware conversion.
+__device__ __forceinline__ double f2d(float f) {
+  const uint32_t u = __float_as_uint(f);
+  const uint32_t e = (u >> 23) & 0xffu;
+  if (e == 0u || e == 0xffu) return (u & 0x7fffffffu) == 0u ? __longlong_as_double((long long)(u & 0x80000000u) << 32) : (double)f;
+  const uint64_t bits = ((uint64_t)(u & 0x80000000u) << 32) | ((uint64_t)(e + 896u) << 52) |
+                        ((uint64_t)(u & 0x7fffffu) << 29);
+  return __longlong_as_double((long long)bits);
+}
+
+// Mixed insertion, warp per block row P.  Off-diagonal entries: contributions
+// summed in double-float, rounded to FP32, masked by the Dirichlet rows and
+// columns.  Diagonal blocks: minus the double-float sum of the row's stored
+// (unmasked) off-diagonal entries, so K t = 0 holds to FP64 roundoff for every
+// rigid translation t on unconstrained rows; a constrained dof gets the
+// reference's value (one 1 per element touching it).
+template <int BS>
+__global__ void __launch_bounds__(256) k_gather_mixed(GatherArgs g) {
+  constexpr int B2 = BS * BS;
+  const int lane = threadIdx.x & 31;
+  const int64_t n_brows = g.n_dofs / BS;
+  for (int64_t P = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; P < n_brows;
+       P += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+    const int64_t rb = g.brow_ptr[P];
+    const int deg = (int)(g.brow_ptr[P + 1] - rb);
+    const int total = deg * B2;
+    int32_t rowp[BS];
+    bool rc[BS];
+#pragma unroll
+    for (int i = 0; i < BS; ++i) {
+      rowp[i] = g.row_ptr[BS * P + i];
+      rc[i] = g.constrained[BS * P + i] != 0;
+    }
+    DF acc[B2];
+#pragma unroll
+    for (int r = 0; r < B2; ++r) acc[r] = {0.f, 0.f};
+    int jdiag = -1;
+    for (int m = lane; m < total; m += 32) {
+      const int jj = m / B2, rem = m - jj * B2;
+      const int i = rem / BS, k = rem - i * BS;
+      const int64_t j = rb + jj;
+      const int32_t Q = g.bcol[j];
+      if (Q == (int32_t)P) { jdiag = jj; continue; }
+      const int tr = k * BS + i;
+      DF s = {0.f, 0.f};
+      for (int32_t c = g.bptr[j]; c < g.bptr[j + 1]; ++c) {
+        const int32_t x = g.bcontrib[c];
+        s = df_add1(s, g.Koff32[(int64_t)(x >> 1) * B2 + ((x & 1) ? tr : rem)]);
+      }
+      const float kv = __fadd_rn(s.hi, s.lo);  // the stored entry, rounded to FP32
+#pragma unroll
+      for (int r = 0; r < B2; ++r)
+        if (r == rem) acc[r] = df_add1(acc[r], kv);
+      const bool masked = rc[i] || g.constrained[(int64_t)BS * Q + k] != 0;
+      g.K[rowp[i] + jj * BS + k] = masked ? 0.0 : f2d(kv);
+    }
+    // warp reduction of the row sums (fixed butterfly order: deterministic)
+#pragma unroll
+    for (int r = 0; r < B2; ++r)
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        DF y;
+        y.hi = __shfl_xor_sync(0xffffffffu, acc[r].hi, o);
+        y.lo = __shfl_xor_sync(0xffffffffu, acc[r].lo, o);
+        acc[r] = (lane & o) ? df_add(y, acc[r]) : df_add(acc[r], y);
+      }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) jdiag = max(jdiag, __shfl_xor_sync(0xffffffffu, jdiag, o));
+    if (lane < B2 && jdiag >= 0) {
+      const int i = lane / BS, k = lane - i * BS;
+      double v = 0.0;
+#pragma unroll
+      for (int r = 0; r < B2; ++r)
+        if (r == lane) v = -(f2d(acc[r].hi) + f2d(acc[r].lo));
+      if (rc[i] || rc[k]) {
+        const int64_t j = rb + jdiag;
+        v = (i == k) ? (double)(g.bptr[j + 1] - g.bptr[j]) : 0.0;
+      }
+      g.K[rowp[i] + jdiag * BS + k] = v;
+    }
+    if (lane < BS) {
+      double s = 0.0;
+      for (int32_t c = g.fptr[P]; c < g.fptr[P + 1]; ++c) s += g.Fe[(int64_t)g.fcontrib[c] * BS + lane];
+      g.F[BS * P + lane] = s;
+    }
+  }
+}
+
 template <typename TO>
 void launch_bs(const GatherArgs &g, const TO *Koff, cudaStream_t s, int blocks) {
   switch (g.bs) {
@@ -92,8 +203,12 @@ void launch_gather(const GatherArgs &g, bool mixed, cudaStream_t s) {
   const int64_t cap = (int64_t)n_sm * 16;
   if (blocks > cap) blocks = cap;
   if (blocks < 1) blocks = 1;
-  if (mixed) launch_bs<float>(g, g.Koff32, s, (int)blocks);
-  else launch_bs<double>(g, g.Koff, s, (int)blocks);
+  if (mixed) {
+    if (g.bs == 1) k_gather_mixed<1><<<(int)blocks, 256, 0, s>>>(g);
+    else if (g.bs == 3) k_gather_mixed<3><<<(int)blocks, 256, 0, s>>>(g);
+  } else {
+    launch_bs<double>(g, g.Koff, s, (int)blocks);
+  }
 }
 
 }  // namespace lmg
