@@ -29,11 +29,13 @@ struct ElemArgs {
   const uint64_t *cmask;      // [n_elem] constrained local dofs, bit v*n + a
   double nu;                  // Poisson ratio (elasticity)
   // Symmetric element matrices are stored as nv x nv blocks: the n diagonal
-  // blocks in FP64 and the n(n-1)/2 strictly upper blocks (a < b, row-major
-  // over a then b) in FP64 (drop-in) or FP32 (mixed form).
-  double *Kdiag;              // [n_elem][n][nv][nv]
-  double *Koff;               // [n_elem][n(n-1)/2][nv][nv] (FP64) or null
-  float *Koff32;              // same layout in FP32 (mixed) or null
+  // blocks and the n(n-1)/2 strictly upper blocks (a < b, row-major over a
+  // then b).  The FP64 drop-in stores every entry as a double-float pair
+  // (hi + lo, 48-bit significand); the mixed form stores only the off-diagonal
+  // blocks, in FP32.
+  float2 *Kdiag2;             // [n_elem][n][nv][nv]          (FP64 drop-in)
+  float2 *Koff2;              // [n_elem][n(n-1)/2][nv][nv]   (FP64 drop-in)
+  float *Koff32;              // [n_elem][n(n-1)/2][nv][nv]   (mixed)
   double *Fe;                 // [n_elem][n][nv]
   int *status;                // [0] error code
   unsigned long long *bad_elem;  // first failing element id
@@ -56,8 +58,8 @@ struct GatherArgs {
   int no;                     // strictly upper blocks per element
   const int32_t *fptr;        // [n_blocks+1]
   const int32_t *fcontrib;    // e*nb + a, ascending per block row
-  const double *Kdiag;
-  const double *Koff;
+  const float2 *Kdiag2;
+  const float2 *Koff2;
   const float *Koff32;
   const double *Fe;
   const uint8_t *constrained; // [n_dofs] (mixed form applies the Dirichlet rows here)

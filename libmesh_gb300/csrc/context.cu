@@ -56,7 +56,8 @@ struct lmg_ctx {
   DevFE dfe{};
   double *d_coef = nullptr, *d_f = nullptr;
   // work and result buffers
-  double *d_Kdiag = nullptr, *d_Koff = nullptr, *d_Fe = nullptr, *d_K = nullptr, *d_F = nullptr;
+  float2 *d_Kdiag2 = nullptr, *d_Koff2 = nullptr;
+  double *d_Fe = nullptr, *d_K = nullptr, *d_F = nullptr;
   float *d_Koff32 = nullptr;
   int *d_status = nullptr;
   unsigned long long *d_bad = nullptr;
@@ -407,7 +408,7 @@ lmg_status lmg_context_destroy(lmg_ctx *c) {
   dfree(c->d_xyz); dfree(c->d_conn); dfree(c->d_aff); dfree(c->d_gen); dfree(c->d_eb);
   dfree(c->d_cmask); dfree(c->d_cons); dfree(c->d_brow_ptr); dfree(c->d_bcol); dfree(c->d_row_ptr); dfree(c->d_col);
   dfree(c->d_bptr); dfree(c->d_bcontrib); dfree(c->d_fptr); dfree(c->d_fcontrib); dfree(c->d_tab);
-  dfree(c->d_coef); dfree(c->d_f); dfree(c->d_Kdiag); dfree(c->d_Koff); dfree(c->d_Fe); dfree(c->d_K);
+  dfree(c->d_coef); dfree(c->d_f); dfree(c->d_Kdiag2); dfree(c->d_Koff2); dfree(c->d_Fe); dfree(c->d_K);
   dfree(c->d_F); dfree(c->d_Koff32); dfree(c->d_status); dfree(c->d_bad);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
   delete c;
@@ -506,8 +507,8 @@ lmg_status lmg_sparsity_build(lmg_ctx *c, int64_t *nnz) {
   LMG_CUDA(c, dalloc(c->d_K, (size_t)c->nnz));
   LMG_CUDA(c, dalloc(c->d_F, (size_t)c->n_dofs));
   const size_t b2 = (size_t)c->bs * c->bs, no = (size_t)c->nb * (c->nb - 1) / 2;
-  LMG_CUDA(c, dalloc(c->d_Kdiag, (size_t)c->n_elem * c->nb * b2));
-  LMG_CUDA(c, dalloc(c->d_Koff, (size_t)c->n_elem * no * b2));
+  LMG_CUDA(c, dalloc(c->d_Kdiag2, (size_t)c->n_elem * c->nb * b2));
+  LMG_CUDA(c, dalloc(c->d_Koff2, (size_t)c->n_elem * no * b2));
   dfree(c->d_Koff32);  // allocated on the first mixed assembly
   LMG_CUDA(c, dalloc(c->d_Fe, (size_t)(c->n_elem * c->nl)));
   c->have_sparsity = true;
@@ -622,8 +623,8 @@ lmg_status lmg_assemble(lmg_ctx *c, int32_t precision, double *K, double *F, int
   a.nodal_f = c->d_f;
   a.cmask = c->d_cmask;
   a.nu = c->nu;
-  a.Kdiag = c->d_Kdiag;
-  a.Koff = c->d_Koff;
+  a.Kdiag2 = c->d_Kdiag2;
+  a.Koff2 = c->d_Koff2;
   a.Koff32 = c->d_Koff32;
   a.Fe = c->d_Fe;
   a.status = c->d_status;
@@ -661,8 +662,8 @@ lmg_status lmg_assemble(lmg_ctx *c, int32_t precision, double *K, double *F, int
   g.no = c->nb * (c->nb - 1) / 2;
   g.fptr = c->d_fptr;
   g.fcontrib = c->d_fcontrib;
-  g.Kdiag = c->d_Kdiag;
-  g.Koff = c->d_Koff;
+  g.Kdiag2 = c->d_Kdiag2;
+  g.Koff2 = c->d_Koff2;
   g.Koff32 = c->d_Koff32;
   g.Fe = c->d_Fe;
   g.constrained = c->d_cons;

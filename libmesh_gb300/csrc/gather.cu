@@ -12,17 +12,23 @@
 // Lanes walk the bs*bs values of consecutive block slots, so the bs*bs values of
 // one stored element block are read by bs*bs neighbouring lanes (one contiguous
 // chunk); each lane loads its contribution indices four at a time before
-// summing, to keep several independent loads in flight.
+// summing, to keep several independent loads in flight.  Sums run in
+// double-float (df.cuh) on the FP32 pipe; GB300's FP64 pipe would otherwise
+// bound this memory-streaming kernel.
 #include <cuda_runtime.h>
 
 #include "assemble.cuh"
+#include "df.cuh"
 
 namespace lmg {
 
 namespace {
 
-template <typename TO, int BS>
-__global__ void __launch_bounds__(256) k_gather(GatherArgs g, const TO *Koff) {
+// FP64 drop-in insertion, warp per block row P: each value is the sum, in
+// element order, of the double-float element entries that land on it; the sum
+// runs in double-float and is rounded once to FP64.
+template <int BS>
+__global__ void __launch_bounds__(256) k_gather(GatherArgs g) {
   constexpr int B2 = BS * BS;
   const int lane = threadIdx.x & 31;
   const int64_t n_brows = g.n_dofs / BS;
@@ -39,28 +45,32 @@ __global__ void __launch_bounds__(256) k_gather(GatherArgs g, const TO *Koff) {
       const int i = rem / BS, k = rem - i * BS;
       const int64_t j = rb + jj;
       const int32_t c0 = g.bptr[j], c1 = g.bptr[j + 1];
-      double s = 0.0;
+      DF s = {0.f, 0.f};
       if (g.bcol[j] == (int32_t)P) {
-        for (int32_t c = c0; c < c1; ++c) s += g.Kdiag[(int64_t)g.bcontrib[c] * B2 + rem];
+        for (int32_t c = c0; c < c1; ++c) {
+          const float2 v = g.Kdiag2[(int64_t)g.bcontrib[c] * B2 + rem];
+          s = df_add(s, DF{v.x, v.y});
+        }
       } else {
         const int tr = k * BS + i;
         int32_t c = c0;
         for (; c + 4 <= c1; c += 4) {
           int32_t x[4];
-          double v[4];
+          float2 v[4];
 #pragma unroll
           for (int u = 0; u < 4; ++u) x[u] = g.bcontrib[c + u];
 #pragma unroll
-          for (int u = 0; u < 4; ++u) v[u] = (double)Koff[(int64_t)(x[u] >> 1) * B2 + ((x[u] & 1) ? tr : rem)];
+          for (int u = 0; u < 4; ++u) v[u] = g.Koff2[(int64_t)(x[u] >> 1) * B2 + ((x[u] & 1) ? tr : rem)];
 #pragma unroll
-          for (int u = 0; u < 4; ++u) s += v[u];
+          for (int u = 0; u < 4; ++u) s = df_add(s, DF{v[u].x, v[u].y});
         }
         for (; c < c1; ++c) {
           const int32_t x = g.bcontrib[c];
-          s += (double)Koff[(int64_t)(x >> 1) * B2 + ((x & 1) ? tr : rem)];
+          const float2 v = g.Koff2[(int64_t)(x >> 1) * B2 + ((x & 1) ? tr : rem)];
+          s = df_add(s, DF{v.x, v.y});
         }
       }
-      g.K[rowp[i] + jj * BS + k] = s;
+      g.K[rowp[i] + jj * BS + k] = df_to_double(s);
     }
     if (lane < BS) {
       double s = 0.0;
@@ -68,39 +78,6 @@ __global__ void __launch_bounds__(256) k_gather(GatherArgs g, const TO *Koff) {
       g.F[BS * P + lane] = s;
     }
   }
-}
-
-// ---- mixed form: double-float (pair of FP32) accumulation on the FP32 pipe.
-// two_sum / fast_two_sum are Knuth's and Dekker's exact-error additions; the
-// __fadd_rn intrinsics keep the compiler from contracting or reassociating them.
-struct DF { float hi, lo; };
-__device__ __forceinline__ DF two_sum(float a, float b) {
-  const float s = __fadd_rn(a, b);
-  const float bb = __fsub_rn(s, a);
-  const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
-  return {s, e};
-}
-__device__ __forceinline__ DF df_add(DF x, DF y) {
-  DF s = two_sum(x.hi, y.hi);
-  const float lo = __fadd_rn(s.lo, __fadd_rn(x.lo, y.lo));
-  const float hi = __fadd_rn(s.hi, lo);
-  return {hi, __fsub_rn(lo, __fsub_rn(hi, s.hi))};
-}
-__device__ __forceinline__ DF df_add1(DF x, float y) {
-  DF s = two_sum(x.hi, y);
-  const float lo = __fadd_rn(s.lo, x.lo);
-  const float hi = __fadd_rn(s.hi, lo);
-  return {hi, __fsub_rn(lo, __fsub_rn(hi, s.hi))};
-}
-// Exact float -> double by moving the bits (keeps the FP64 pipe free); zero,
-// subnormal, inf and NaN take the hardware conversion.
-__device__ __forceinline__ double f2d(float f) {
-  const uint32_t u = __float_as_uint(f);
-  const uint32_t e = (u >> 23) & 0xffu;
-  if (e == 0u || e == 0xffu) return (u & 0x7fffffffu) == 0u ? __longlong_as_double((long long)(u & 0x80000000u) << 32) : (double)f;
-  const uint64_t bits = ((uint64_t)(u & 0x80000000u) << 32) | ((uint64_t)(e + 896u) << 52) |
-                        ((uint64_t)(u & 0x7fffffu) << 29);
-  return __longlong_as_double((long long)bits);
 }
 
 // Mixed insertion, warp per block row P.  Off-diagonal entries: contributions
@@ -181,15 +158,6 @@ __global__ void __launch_bounds__(256) k_gather_mixed(GatherArgs g) {
   }
 }
 
-template <typename TO>
-void launch_bs(const GatherArgs &g, const TO *Koff, cudaStream_t s, int blocks) {
-  switch (g.bs) {
-    case 1: k_gather<TO, 1><<<blocks, 256, 0, s>>>(g, Koff); break;
-    case 3: k_gather<TO, 3><<<blocks, 256, 0, s>>>(g, Koff); break;
-    default: break;
-  }
-}
-
 }  // namespace
 
 bool gather_built(int bs) { return bs == 1 || bs == 3; }
@@ -207,7 +175,8 @@ void launch_gather(const GatherArgs &g, bool mixed, cudaStream_t s) {
     if (g.bs == 1) k_gather_mixed<1><<<(int)blocks, 256, 0, s>>>(g);
     else if (g.bs == 3) k_gather_mixed<3><<<(int)blocks, 256, 0, s>>>(g);
   } else {
-    launch_bs<double>(g, g.Koff, s, (int)blocks);
+    if (g.bs == 1) k_gather<1><<<(int)blocks, 256, 0, s>>>(g);
+    else if (g.bs == 3) k_gather<3><<<(int)blocks, 256, 0, s>>>(g);
   }
 }
 
