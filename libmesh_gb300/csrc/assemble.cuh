@@ -26,6 +26,7 @@ struct ElemArgs {
   const int32_t *conn;        // [n_elem][npe]
   const double *coef;         // [n_elem] or null (=1)
   const double *nodal_f;      // [n_nodes][nv] or null (=0)
+  const float2 *nodal_f2;     // the same as double-float pairs, or null
   const uint64_t *cmask;      // [n_elem] constrained local dofs, bit v*n + a
   double nu;                  // Poisson ratio (elasticity)
   // Symmetric element matrices are stored as nv x nv blocks: the n diagonal
@@ -36,7 +37,7 @@ struct ElemArgs {
   float2 *Kdiag2;             // [n_elem][n][nv][nv]          (FP64 drop-in)
   float2 *Koff2;              // [n_elem][n(n-1)/2][nv][nv]   (FP64 drop-in)
   float *Koff32;              // [n_elem][n(n-1)/2][nv][nv]   (mixed)
-  double *Fe;                 // [n_elem][n][nv]
+  float2 *Fe2;                // [n_elem][n][nv] load vector, double-float pairs
   int *status;                // [0] error code
   unsigned long long *bad_elem;  // first failing element id
   DevFE fe;
@@ -61,7 +62,7 @@ struct GatherArgs {
   const float2 *Kdiag2;
   const float2 *Koff2;
   const float *Koff32;
-  const double *Fe;
+  const float2 *Fe2;
   const uint8_t *constrained; // [n_dofs] (mixed form applies the Dirichlet rows here)
   double *K;
   double *F;

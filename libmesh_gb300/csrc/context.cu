@@ -55,9 +55,11 @@ struct lmg_ctx {
   double *d_tab = nullptr;
   DevFE dfe{};
   double *d_coef = nullptr, *d_f = nullptr;
+  float2 *d_f2 = nullptr;  // nodal load as double-float pairs
   // work and result buffers
   float2 *d_Kdiag2 = nullptr, *d_Koff2 = nullptr;
-  double *d_Fe = nullptr, *d_K = nullptr, *d_F = nullptr;
+  float2 *d_Fe2 = nullptr;
+  double *d_K = nullptr, *d_F = nullptr;
   float *d_Koff32 = nullptr;
   int *d_status = nullptr;
   unsigned long long *d_bad = nullptr;
@@ -197,6 +199,14 @@ __global__ void k_encode(int64_t n, int nb, int32_t *v) {
       const int o = lo * nb - lo * (lo + 1) / 2 + (hi - lo - 1);
       v[i] = (int32_t)(2 * (e * no + o) + (a > b ? 1 : 0));
     }
+  }
+}
+
+// Nodal load split into double-float pairs (read by the affine element kernels).
+__global__ void k_split(int64_t n, const double *x, float2 *y) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float hi = (float)x[i];
+    y[i] = make_float2(hi, (float)(x[i] - (double)hi));
   }
 }
 
@@ -408,7 +418,7 @@ lmg_status lmg_context_destroy(lmg_ctx *c) {
   dfree(c->d_xyz); dfree(c->d_conn); dfree(c->d_aff); dfree(c->d_gen); dfree(c->d_eb);
   dfree(c->d_cmask); dfree(c->d_cons); dfree(c->d_brow_ptr); dfree(c->d_bcol); dfree(c->d_row_ptr); dfree(c->d_col);
   dfree(c->d_bptr); dfree(c->d_bcontrib); dfree(c->d_fptr); dfree(c->d_fcontrib); dfree(c->d_tab);
-  dfree(c->d_coef); dfree(c->d_f); dfree(c->d_Kdiag2); dfree(c->d_Koff2); dfree(c->d_Fe); dfree(c->d_K);
+  dfree(c->d_coef); dfree(c->d_f); dfree(c->d_f2); dfree(c->d_Kdiag2); dfree(c->d_Koff2); dfree(c->d_Fe2); dfree(c->d_K);
   dfree(c->d_F); dfree(c->d_Koff32); dfree(c->d_status); dfree(c->d_bad);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
   delete c;
@@ -510,7 +520,7 @@ lmg_status lmg_sparsity_build(lmg_ctx *c, int64_t *nnz) {
   LMG_CUDA(c, dalloc(c->d_Kdiag2, (size_t)c->n_elem * c->nb * b2));
   LMG_CUDA(c, dalloc(c->d_Koff2, (size_t)c->n_elem * no * b2));
   dfree(c->d_Koff32);  // allocated on the first mixed assembly
-  LMG_CUDA(c, dalloc(c->d_Fe, (size_t)(c->n_elem * c->nl)));
+  LMG_CUDA(c, dalloc(c->d_Fe2, (size_t)(c->n_elem * c->nl)));
   c->have_sparsity = true;
   if (nnz) *nnz = c->nnz;
   return LMG_OK;
@@ -575,7 +585,13 @@ lmg_status lmg_form_set(lmg_ctx *c, int32_t form, int32_t fe_order, int32_t q_or
   dfree(c->d_coef);
   dfree(c->d_f);
   if (elem_coef) LMG_CUDA(c, dupload(c, c->d_coef, elem_coef, (size_t)c->n_elem));
-  if (nodal_f) LMG_CUDA(c, dupload(c, c->d_f, nodal_f, (size_t)(c->n_nodes * c->n_vars)));
+  dfree(c->d_f2);
+  if (nodal_f) {
+    LMG_CUDA(c, dupload(c, c->d_f, nodal_f, (size_t)(c->n_nodes * c->n_vars)));
+    LMG_CUDA(c, dalloc(c->d_f2, (size_t)(c->n_nodes * c->n_vars)));
+    k_split<<<grid_for(c, c->n_nodes * c->n_vars, 256), 256, 0, c->stream>>>(c->n_nodes * c->n_vars, c->d_f, c->d_f2);
+    c->launches++;
+  }
   LMG_CUDA(c, cudaStreamSynchronize(c->stream));
   c->have_form = true;
   return LMG_OK;
@@ -599,7 +615,10 @@ lmg_status lmg_inputs_update(lmg_ctx *c, const double *xyz, const double *elem_c
   }
   if (nodal_f) {
     if (!c->d_f) LMG_CUDA(c, dalloc(c->d_f, (size_t)(c->n_nodes * c->n_vars)));
+    if (!c->d_f2) LMG_CUDA(c, dalloc(c->d_f2, (size_t)(c->n_nodes * c->n_vars)));
     LMG_CUDA(c, cudaMemcpyAsync(c->d_f, nodal_f, sizeof(double) * c->n_nodes * c->n_vars, cudaMemcpyHostToDevice, c->stream));
+    k_split<<<grid_for(c, c->n_nodes * c->n_vars, 256), 256, 0, c->stream>>>(c->n_nodes * c->n_vars, c->d_f, c->d_f2);
+    c->launches++;
   }
   return LMG_OK;
 }
@@ -621,12 +640,13 @@ lmg_status lmg_assemble(lmg_ctx *c, int32_t precision, double *K, double *F, int
   a.conn = c->d_conn;
   a.coef = c->d_coef;
   a.nodal_f = c->d_f;
+  a.nodal_f2 = c->d_f2;
   a.cmask = c->d_cmask;
   a.nu = c->nu;
   a.Kdiag2 = c->d_Kdiag2;
   a.Koff2 = c->d_Koff2;
   a.Koff32 = c->d_Koff32;
-  a.Fe = c->d_Fe;
+  a.Fe2 = c->d_Fe2;
   a.status = c->d_status;
   a.bad_elem = c->d_bad;
   a.fe = c->dfe;
@@ -665,7 +685,7 @@ lmg_status lmg_assemble(lmg_ctx *c, int32_t precision, double *K, double *F, int
   g.Kdiag2 = c->d_Kdiag2;
   g.Koff2 = c->d_Koff2;
   g.Koff32 = c->d_Koff32;
-  g.Fe = c->d_Fe;
+  g.Fe2 = c->d_Fe2;
   g.constrained = c->d_cons;
   g.K = c->d_K;
   g.F = c->d_F;

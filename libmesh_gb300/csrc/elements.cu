@@ -94,42 +94,6 @@ __device__ __forceinline__ void lame(double E, double nu, double &lam, double &m
   mu = E / (2. * (1. + nu));
 }
 
-// Element tensor A of the affine path.
-//   POISSON:    A[mn]      = k detJ (G G^T)_mn
-//   ELASTICITY: A[ik][mn]  = detJ (lam G_mi G_nk + mu G_mk G_ni + mu d_ik (G G^T)_mn)
-template <int FORM>
-__device__ __forceinline__ void element_tensor(const double G[9], double det, double coef,
-                                               double nu, double *A) {
-  double GG[9];
-#pragma unroll
-  for (int m = 0; m < 3; ++m)
-#pragma unroll
-    for (int n = 0; n < 3; ++n)
-      GG[3 * m + n] = G[3 * m] * G[3 * n] + G[3 * m + 1] * G[3 * n + 1] + G[3 * m + 2] * G[3 * n + 2];
-  if (FORM == LMG_POISSON) {
-    const double s = coef * det;
-#pragma unroll
-    for (int i = 0; i < 9; ++i) A[i] = s * GG[i];
-  } else {
-    double lam, mu;
-    lame(coef, nu, lam, mu);
-    lam *= det;
-    mu *= det;
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-#pragma unroll
-      for (int k = 0; k < 3; ++k)
-#pragma unroll
-        for (int m = 0; m < 3; ++m)
-#pragma unroll
-          for (int n = 0; n < 3; ++n) {
-            double v = lam * G[3 * m + i] * G[3 * n + k] + mu * G[3 * m + k] * G[3 * n + i];
-            if (i == k) v += mu * GG[3 * m + n];
-            A[(3 * i + k) * 9 + 3 * m + n] = v;
-          }
-  }
-}
-
 // Strictly upper block index o of (a, b), a < b, and its inverse.
 __host__ __device__ constexpr int off_index(int N, int a, int b) { return a * N - a * (a + 1) / 2 + (b - a - 1); }
 
@@ -148,39 +112,66 @@ __device__ __forceinline__ double masked(double v, uint64_t mask, int lr, int lc
   return v;
 }
 
+// Arithmetic of the affine contraction: T = float2 is a double-float pair
+// (FP64 drop-in, df.cuh), T = float plain FP32 (mixed form).
+template <typename T> struct Ar;
+template <> struct Ar<float> {
+  using V = float;
+  static __device__ __forceinline__ V zero() { return 0.f; }
+  static __device__ __forceinline__ V from(double x) { return (float)x; }
+  static __device__ __forceinline__ V ld(float x) { return x; }
+  static __device__ __forceinline__ V fma(V acc, V a, V b) { return fmaf(a, b, acc); }
+  static __device__ __forceinline__ V norm(V x) { return x; }
+};
+template <> struct Ar<float2> {
+  using V = DF;
+  static __device__ __forceinline__ V zero() { return {0.f, 0.f}; }
+  static __device__ __forceinline__ V from(double x) { return df_split(x); }
+  static __device__ __forceinline__ V ld(float2 x) { return {x.x, x.y}; }
+  static __device__ __forceinline__ V fma(V acc, V a, V b) { return df_fma_lazy(acc, a, b); }
+  static __device__ __forceinline__ V norm(V x) { return df_norm(x); }
+};
+__device__ __forceinline__ void st(float &o, float v) { o = v; }
+__device__ __forceinline__ void st(float2 &o, DF v) { o = make_float2(v.hi, v.lo); }
+
+// Per-element operands of the affine contraction, in T:
+//   POISSON:    A_mn = k detJ (G G^T)_mn                    (9)
+//   ELASTICITY: G_mn, lam detJ, mu detJ                     (11)
+template <int FORM> struct Geo { static constexpr int NG = (FORM == LMG_POISSON) ? 9 : 11; };
+
 // Byte offsets of the affine kernel's dynamic shared memory (4 warps per CTA).
 __host__ __device__ constexpr size_t al16(size_t x) { return (x + 15) & ~(size_t)15; }
 template <int FORM, int N, int NV, typename T>
 struct AffineSmem {
-  static constexpr int NA = (FORM == LMG_POISSON) ? 9 : 81;
+  static constexpr int NG = Geo<FORM>::NG;
   static constexpr int NO = N * (N - 1) / 2;
-  static constexpr size_t S = 0;
-  static constexpr size_t A = S + al16(sizeof(T) * 9 * N * N);
-  static constexpr size_t MASK = A + al16(sizeof(T) * 4 * 32 * NA);
+  static constexpr size_t S = 0;                                        // [9][N][N] T
+  static constexpr size_t M = S + al16(sizeof(T) * 9 * N * N);          // [N][N] float2
+  static constexpr size_t G = M + al16(sizeof(float2) * N * N);         // [4][32][NG] T
+  static constexpr size_t MASK = G + al16(sizeof(T) * 4 * 32 * NG);     // [4][32] u64
   static constexpr size_t PAIR = MASK + al16(sizeof(uint64_t) * 4 * 32);
   static constexpr size_t BYTES = PAIR + al16(sizeof(uint16_t) * (NO > 0 ? NO : 1));
 };
 
-// Storage conversions of the affine kernel's operands: T = float2 holds a
-// double-float pair (FP64 drop-in), T = float a plain FP32 value (mixed form).
-__device__ __forceinline__ void to_op(double x, float2 &o) { const DF d = df_split(x); o = make_float2(d.hi, d.lo); }
-__device__ __forceinline__ void to_op(double x, float &o) { o = (float)x; }
-
 template <int FORM, int N, int NV, typename T>
 __global__ void __launch_bounds__(128) k_elem_affine(ElemArgs a) {
+  using R = Ar<T>;
+  using V = typename R::V;
   constexpr bool MIXED = sizeof(T) == 4;
-  constexpr int NA = (FORM == LMG_POISSON) ? 9 : 81;
+  constexpr int NG = Geo<FORM>::NG;
   constexpr int NB = N * N, NO = N * (N - 1) / 2, B2 = NV * NV;
   constexpr int NWORK = MIXED ? NO : N + NO;  // blocks computed by the contraction
   constexpr int BPL = (NWORK + 31) / 32;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   using L = AffineSmem<FORM, N, NV, T>;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  T *sS = reinterpret_cast<T *>(smem_raw + L::S);                       // [9][N][N]
-  T *sA = reinterpret_cast<T *>(smem_raw + L::A) + warp * 32 * NA;      // [32][NA]
+  T *sS = reinterpret_cast<T *>(smem_raw + L::S);
+  float2 *sM = reinterpret_cast<float2 *>(smem_raw + L::M);
+  T *sG = reinterpret_cast<T *>(smem_raw + L::G) + warp * 32 * NG;
   uint64_t *sMask = reinterpret_cast<uint64_t *>(smem_raw + L::MASK) + warp * 32;
-  uint16_t *sPair = reinterpret_cast<uint16_t *>(smem_raw + L::PAIR);   // [NO]
-  for (int i = threadIdx.x; i < 9 * NB; i += blockDim.x) to_op(a.fe.S[i], sS[i]);
+  uint16_t *sPair = reinterpret_cast<uint16_t *>(smem_raw + L::PAIR);
+  for (int i = threadIdx.x; i < 9 * NB; i += blockDim.x) st(sS[i], R::from(a.fe.S[i]));
+  for (int i = threadIdx.x; i < NB; i += blockDim.x) st(sM[i], df_split(a.fe.M[i]));
   build_pairs<N>(sPair);
   __syncthreads();
 
@@ -188,43 +179,65 @@ __global__ void __launch_bounds__(128) k_elem_affine(ElemArgs a) {
   for (int64_t tile = (int64_t)blockIdx.x * 4 + warp; tile < n_tiles; tile += (int64_t)gridDim.x * 4) {
     const int64_t li = tile * 32 + lane;
     const int32_t e = (li < a.n_list) ? a.list[li] : -1;
-    if (e >= 0) {
-      double X[N * 3];
+    if (e >= 0) {  // lane = element: FP64 geometry at qp 0 (compute_affine_map)
       const int32_t *c = a.conn + (int64_t)e * a.npe;
-#pragma unroll
-      for (int g = 0; g < N; ++g) {
-        const double *p = a.xyz + 3 * (int64_t)c[g];
-        X[3 * g] = p[0];
-        X[3 * g + 1] = p[1];
-        X[3 * g + 2] = p[2];
-      }
       double G[9];
-      const double det = jacobian(X, a.fe.gdphi, N, G);
+      double det;
+      {
+        double X[N * 3];
+#pragma unroll
+        for (int g = 0; g < N; ++g) {
+          const double *p = a.xyz + 3 * (int64_t)c[g];
+          X[3 * g] = p[0];
+          X[3 * g + 1] = p[1];
+          X[3 * g + 2] = p[2];
+        }
+        det = jacobian(X, a.fe.gdphi, N, G);
+      }
       if (!(det > 0.0)) report_bad(a, LMG_ERR_DEGENERATE, e);
       const double coef = a.coef ? a.coef[e] : 1.0;
-      double A[NA];
-      element_tensor<FORM>(G, det, coef, a.nu, A);
+      T *g = sG + lane * NG;
+      if (FORM == LMG_POISSON) {
+        const double s = coef * det;
 #pragma unroll
-      for (int i = 0; i < NA; ++i) to_op(A[i], sA[lane * NA + i]);
+        for (int m = 0; m < 3; ++m)
+#pragma unroll
+          for (int n = 0; n < 3; ++n)
+            st(g[3 * m + n], R::from(s * (G[3 * m] * G[3 * n] + G[3 * m + 1] * G[3 * n + 1] + G[3 * m + 2] * G[3 * n + 2])));
+      } else {
+        double lam, mu;
+        lame(coef, a.nu, lam, mu);
+#pragma unroll
+        for (int i = 0; i < 9; ++i) st(g[i], R::from(G[i]));
+        st(g[9], R::from(lam * det));
+        st(g[10], R::from(mu * det));
+      }
       const uint64_t mask = a.cmask[e];
       sMask[lane] = mask;
-      // Load vector: Fe_a^i = detJ sum_b M_ab f_b^i (f interpolated with phi), FP64.
-      double *Fo = a.Fe + (int64_t)e * N * NV;
+      // Load vector Fe_a^i = detJ sum_b M_ab f_b^i in double-float (both forms).
+      float2 *Fo = a.Fe2 + (int64_t)e * N * NV;
+      const DF dd = df_split(det);
       for (int ai = 0; ai < N; ++ai)
+#pragma unroll
         for (int v = 0; v < NV; ++v) {
-          double s = 0.0;
-          if (a.nodal_f)
-            for (int b = 0; b < N; ++b) s += a.fe.M[ai * N + b] * a.nodal_f[(int64_t)c[b] * NV + v];
-          s *= det;
-          if ((mask >> (v * N + ai)) & 1ull) s = 0.0;
-          Fo[ai * NV + v] = s;
+          DF s = {0.f, 0.f};
+          if (a.nodal_f2)
+            for (int b = 0; b < N; ++b) {
+              const float2 fb = a.nodal_f2[(int64_t)c[b] * NV + v], mb = sM[ai * N + b];
+              s = df_fma_lazy(s, DF{mb.x, mb.y}, DF{fb.x, fb.y});
+            }
+          s = df_norm(df_fma_lazy(DF{0.f, 0.f}, df_norm(s), dd));
+          Fo[ai * NV + v] = ((mask >> (v * N + ai)) & 1ull) ? make_float2(0.f, 0.f) : make_float2(s.hi, s.lo);
         }
     }
     __syncwarp();
-    for (int t = 0; t < 32; ++t) {
+    for (int t = 0; t < 32; ++t) {  // lane = output block
       const int32_t et = __shfl_sync(FULL, e, t);
       if (et < 0) break;
-      const T *At = sA + t * NA;
+      const T *gt = sG + t * NG;
+      V gv[NG];
+#pragma unroll
+      for (int i = 0; i < NG; ++i) gv[i] = R::ld(gt[i]);
       const uint64_t mask = sMask[t];
 #pragma unroll
       for (int k = 0; k < BPL; ++k) {
@@ -234,30 +247,62 @@ __global__ void __launch_bounds__(128) k_elem_affine(ElemArgs a) {
           if (!MIXED && w < N) { ra = cb = w; o = -1; }
           else { o = MIXED ? w : w - N; ra = sPair[o] >> 8; cb = sPair[o] & 0xff; }
           const int blk = ra * N + cb;
-          T sv[9];
+          V sv[9];
 #pragma unroll
-          for (int mn = 0; mn < 9; ++mn) sv[mn] = sS[mn * NB + blk];
+          for (int mn = 0; mn < 9; ++mn) sv[mn] = R::ld(sS[mn * NB + blk]);
+          V out[B2];
+          if (FORM == LMG_POISSON) {
+            V acc = R::zero();
+#pragma unroll
+            for (int mn = 0; mn < 9; ++mn) acc = R::fma(acc, gv[mn], sv[mn]);
+            out[0] = R::norm(acc);
+          } else {
+            // P = G^T S_ab G (T = S_ab G, then G^T T); K^{ik} = lam' P^{ik} + mu' P^{ki} + d_ik mu' tr P
+            V Tm[9];
+#pragma unroll
+            for (int m = 0; m < 3; ++m)
+#pragma unroll
+              for (int kk = 0; kk < 3; ++kk) {
+                V acc = R::zero();
+#pragma unroll
+                for (int n = 0; n < 3; ++n) acc = R::fma(acc, sv[3 * m + n], gv[3 * n + kk]);
+                Tm[3 * m + kk] = R::norm(acc);
+              }
+            V Pm[9];
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+              for (int kk = 0; kk < 3; ++kk) {
+                V acc = R::zero();
+#pragma unroll
+                for (int m = 0; m < 3; ++m) acc = R::fma(acc, gv[3 * m + i], Tm[3 * m + kk]);
+                Pm[3 * i + kk] = R::norm(acc);
+              }
+            V tr = R::zero();
+#pragma unroll
+            for (int i = 0; i < 3; ++i) tr = R::fma(tr, Pm[4 * i], R::from(1.0));
+            tr = R::norm(tr);
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+              for (int kk = 0; kk < 3; ++kk) {
+                V acc = R::fma(R::zero(), gv[9], Pm[3 * i + kk]);
+                acc = R::fma(acc, gv[10], Pm[3 * kk + i]);
+                if (i == kk) acc = R::fma(acc, gv[10], tr);
+                out[3 * i + kk] = R::norm(acc);
+              }
+          }
 #pragma unroll
           for (int ik = 0; ik < B2; ++ik) {
             const int i = ik / NV, kk = ik - i * NV;
             const int lr = i * N + ra, lc = kk * N + cb;
             if constexpr (MIXED) {
-              float acc = 0.f;
-#pragma unroll
-              for (int mn = 0; mn < 9; ++mn) acc = fmaf(At[ik * 9 + mn], sv[mn], acc);
-              a.Koff32[((int64_t)et * NO + o) * B2 + ik] = acc;
+              a.Koff32[((int64_t)et * NO + o) * B2 + ik] = out[ik];
             } else {
-              DF acc = {0.f, 0.f};
-#pragma unroll
-              for (int mn = 0; mn < 9; ++mn) {
-                const float2 av = At[ik * 9 + mn], bv = sv[mn];
-                acc = df_fma_lazy(acc, DF{av.x, av.y}, DF{bv.x, bv.y});
-              }
-              acc = df_norm(acc);
-              float2 out = make_float2(acc.hi, acc.lo);
-              if (((mask >> lr) | (mask >> lc)) & 1ull) out = make_float2(lr == lc ? 1.f : 0.f, 0.f);
-              if (o < 0) a.Kdiag2[((int64_t)et * N + ra) * B2 + ik] = out;
-              else a.Koff2[((int64_t)et * NO + o) * B2 + ik] = out;
+              float2 v = make_float2(out[ik].hi, out[ik].lo);
+              if (((mask >> lr) | (mask >> lc)) & 1ull) v = make_float2(lr == lc ? 1.f : 0.f, 0.f);
+              if (o < 0) a.Kdiag2[((int64_t)et * N + ra) * B2 + ik] = v;
+              else a.Koff2[((int64_t)et * NO + o) * B2 + ik] = v;
             }
           }
         }
@@ -373,9 +418,8 @@ __global__ void __launch_bounds__(128) k_elem_general(ElemArgs a) {
     if (lane < N) {
 #pragma unroll
       for (int v = 0; v < NV; ++v) {
-        double s = facc[v];
-        if ((mask >> (v * N + lane)) & 1ull) s = 0.0;
-        a.Fe[((int64_t)e * N + lane) * NV + v] = s;
+        const DF s = df_split(((mask >> (v * N + lane)) & 1ull) ? 0.0 : facc[v]);
+        a.Fe2[((int64_t)e * N + lane) * NV + v] = make_float2(s.hi, s.lo);
       }
     }
     __syncwarp();

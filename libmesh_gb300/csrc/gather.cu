@@ -24,6 +24,41 @@ namespace lmg {
 
 namespace {
 
+// Load vector of block row P: the element entries that land on each of its bs
+// dofs, summed in double-float by a fixed butterfly over the warp (lane l takes
+// contributions l, l+32, ... in element order), rounded once to FP64.
+template <int BS>
+__device__ __forceinline__ void row_load(const GatherArgs &g, int64_t P, int lane) {
+  const int32_t f0 = g.fptr[P], f1 = g.fptr[P + 1];
+  DF s[BS];
+#pragma unroll
+  for (int i = 0; i < BS; ++i) s[i] = {0.f, 0.f};
+  for (int32_t c = f0 + lane; c < f1; c += 32) {
+    const int64_t base = (int64_t)g.fcontrib[c] * BS;
+#pragma unroll
+    for (int i = 0; i < BS; ++i) {
+      const float2 v = g.Fe2[base + i];
+      s[i] = df_add(s[i], DF{v.x, v.y});
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < BS; ++i)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      DF y;
+      y.hi = __shfl_xor_sync(0xffffffffu, s[i].hi, o);
+      y.lo = __shfl_xor_sync(0xffffffffu, s[i].lo, o);
+      s[i] = (lane & o) ? df_add(y, s[i]) : df_add(s[i], y);
+    }
+  if (lane < BS) {
+    DF r = s[0];
+#pragma unroll
+    for (int i = 1; i < BS; ++i)
+      if (lane == i) r = s[i];
+    g.F[BS * P + lane] = df_to_double(r);
+  }
+}
+
 // FP64 drop-in insertion, warp per block row P: each value is the sum, in
 // element order, of the double-float element entries that land on it; the sum
 // runs in double-float and is rounded once to FP64.
@@ -53,30 +88,23 @@ __global__ void __launch_bounds__(256) k_gather(GatherArgs g) {
         }
       } else {
         const int tr = k * BS + i;
-        int32_t c = c0;
-        for (; c + 4 <= c1; c += 4) {
+        for (int32_t c = c0; c < c1; c += 4) {  // four predicated loads in flight
           int32_t x[4];
           float2 v[4];
 #pragma unroll
-          for (int u = 0; u < 4; ++u) x[u] = g.bcontrib[c + u];
+          for (int u = 0; u < 4; ++u) x[u] = (c + u < c1) ? __ldg(g.bcontrib + c + u) : -1;
 #pragma unroll
-          for (int u = 0; u < 4; ++u) v[u] = g.Koff2[(int64_t)(x[u] >> 1) * B2 + ((x[u] & 1) ? tr : rem)];
+          for (int u = 0; u < 4; ++u)
+            v[u] = (x[u] >= 0) ? __ldg(g.Koff2 + (int64_t)(x[u] >> 1) * B2 + ((x[u] & 1) ? tr : rem))
+                               : make_float2(0.f, 0.f);
 #pragma unroll
-          for (int u = 0; u < 4; ++u) s = df_add(s, DF{v[u].x, v[u].y});
-        }
-        for (; c < c1; ++c) {
-          const int32_t x = g.bcontrib[c];
-          const float2 v = g.Koff2[(int64_t)(x >> 1) * B2 + ((x & 1) ? tr : rem)];
-          s = df_add(s, DF{v.x, v.y});
+          for (int u = 0; u < 4; ++u)
+            if (x[u] >= 0) s = df_add(s, DF{v[u].x, v[u].y});
         }
       }
       g.K[rowp[i] + jj * BS + k] = df_to_double(s);
     }
-    if (lane < BS) {
-      double s = 0.0;
-      for (int32_t c = g.fptr[P]; c < g.fptr[P + 1]; ++c) s += g.Fe[(int64_t)g.fcontrib[c] * BS + lane];
-      g.F[BS * P + lane] = s;
-    }
+    row_load<BS>(g, P, lane);
   }
 }
 
@@ -150,11 +178,7 @@ __global__ void __launch_bounds__(256) k_gather_mixed(GatherArgs g) {
       }
       g.K[rowp[i] + jdiag * BS + k] = v;
     }
-    if (lane < BS) {
-      double s = 0.0;
-      for (int32_t c = g.fptr[P]; c < g.fptr[P + 1]; ++c) s += g.Fe[(int64_t)g.fcontrib[c] * BS + lane];
-      g.F[BS * P + lane] = s;
-    }
+    row_load<BS>(g, P, lane);
   }
 }
 
