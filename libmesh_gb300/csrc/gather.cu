@@ -59,124 +59,122 @@ __device__ __forceinline__ void row_load(const GatherArgs &g, int64_t P, int lan
   }
 }
 
-// FP64 drop-in insertion, warp per block row P: each value is the sum, in
-// element order, of the double-float element entries that land on it; the sum
-// runs in double-float and is rounded once to FP64.
+// Contributions of one block slot to one entry, summed in double-float in
+// element order; four predicated loads in flight per step.
+template <int B2, typename TV>
+__device__ __forceinline__ DF slot_sum(const GatherArgs &g, const TV *Kb, int32_t c0, int32_t c1, int rem, int tr,
+                                       bool coded) {
+  DF s = {0.f, 0.f};
+  for (int32_t c = c0; c < c1; c += 4) {
+    int32_t x[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) x[u] = (c + u < c1) ? __ldg(g.bcontrib + c + u) : -1;
+    TV v[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      int64_t idx = 0;
+      if (x[u] >= 0) idx = coded ? (int64_t)(x[u] >> 1) * B2 + ((x[u] & 1) ? tr : rem) : (int64_t)x[u] * B2 + rem;
+      v[u] = (x[u] >= 0) ? __ldg(Kb + idx) : TV{};
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+      if (x[u] >= 0) {
+        if constexpr (sizeof(TV) == 8) s = df_add(s, DF{((const float2 &)v[u]).x, ((const float2 &)v[u]).y});
+        else s = df_add1(s, (const float &)v[u]);
+      }
+  }
+  return s;
+}
+
+// FP64 drop-in insertion, warp per block row P.  Lane l < (32/B2)*B2 owns entry
+// rem = l % B2 of the slots jj = l / B2 + (32/B2) t, so the B2 values of one
+// stored element block are read by B2 neighbouring lanes as one chunk.  Each
+// value is the sum, in element order, of the double-float element entries that
+// land on it, rounded once to FP64.
 template <int BS>
 __global__ void __launch_bounds__(256) k_gather(GatherArgs g) {
-  constexpr int B2 = BS * BS;
+  constexpr int B2 = BS * BS, SPL = 32 / B2;
   const int lane = threadIdx.x & 31;
+  const int js = lane / B2, rem = lane - js * B2;
+  const bool act = lane < SPL * B2;
+  const int i = rem / BS, k = rem - i * BS, tr = k * BS + i;
   const int64_t n_brows = g.n_dofs / BS;
   for (int64_t P = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; P < n_brows;
        P += ((int64_t)gridDim.x * blockDim.x) >> 5) {
     const int64_t rb = g.brow_ptr[P];
     const int deg = (int)(g.brow_ptr[P + 1] - rb);
-    const int total = deg * B2;
-    int32_t rowp[BS];
-#pragma unroll
-    for (int i = 0; i < BS; ++i) rowp[i] = g.row_ptr[BS * P + i];
-    for (int m = lane; m < total; m += 32) {
-      const int jj = m / B2, rem = m - jj * B2;
-      const int i = rem / BS, k = rem - i * BS;
+    const int32_t rowp = act ? g.row_ptr[BS * P + i] : 0;
+    for (int jj = js; act && jj < deg; jj += SPL) {
       const int64_t j = rb + jj;
       const int32_t c0 = g.bptr[j], c1 = g.bptr[j + 1];
-      DF s = {0.f, 0.f};
-      if (g.bcol[j] == (int32_t)P) {
-        for (int32_t c = c0; c < c1; ++c) {
-          const float2 v = g.Kdiag2[(int64_t)g.bcontrib[c] * B2 + rem];
-          s = df_add(s, DF{v.x, v.y});
-        }
-      } else {
-        const int tr = k * BS + i;
-        for (int32_t c = c0; c < c1; c += 4) {  // four predicated loads in flight
-          int32_t x[4];
-          float2 v[4];
-#pragma unroll
-          for (int u = 0; u < 4; ++u) x[u] = (c + u < c1) ? __ldg(g.bcontrib + c + u) : -1;
-#pragma unroll
-          for (int u = 0; u < 4; ++u)
-            v[u] = (x[u] >= 0) ? __ldg(g.Koff2 + (int64_t)(x[u] >> 1) * B2 + ((x[u] & 1) ? tr : rem))
-                               : make_float2(0.f, 0.f);
-#pragma unroll
-          for (int u = 0; u < 4; ++u)
-            if (x[u] >= 0) s = df_add(s, DF{v[u].x, v[u].y});
-        }
-      }
-      g.K[rowp[i] + jj * BS + k] = df_to_double(s);
+      const bool diag = g.bcol[j] == (int32_t)P;
+      const DF s = diag ? slot_sum<B2>(g, g.Kdiag2, c0, c1, rem, rem, false)
+                        : slot_sum<B2>(g, g.Koff2, c0, c1, rem, tr, true);
+      g.K[rowp + jj * BS + k] = df_to_double(s);
     }
     row_load<BS>(g, P, lane);
   }
 }
 
-// Mixed insertion, warp per block row P.  Off-diagonal entries: contributions
-// summed in double-float, rounded to FP32, masked by the Dirichlet rows and
-// columns.  Diagonal blocks: minus the double-float sum of the row's stored
-// (unmasked) off-diagonal entries, so K t = 0 holds to FP64 roundoff for every
-// rigid translation t on unconstrained rows; a constrained dof gets the
-// reference's value (one 1 per element touching it).
+// Mixed insertion, warp per block row P, same lane layout.  Off-diagonal
+// entries: contributions summed in double-float, rounded to FP32, masked by the
+// Dirichlet rows and columns.  Diagonal blocks: minus the double-float sum of
+// the row's stored (unmasked) off-diagonal entries, so K t = 0 holds to FP64
+// roundoff for every rigid translation t on unconstrained rows; a constrained
+// dof gets the reference's value (one 1 per element touching it).
 template <int BS>
 __global__ void __launch_bounds__(256) k_gather_mixed(GatherArgs g) {
-  constexpr int B2 = BS * BS;
+  constexpr int B2 = BS * BS, SPL = 32 / B2;
   const int lane = threadIdx.x & 31;
+  const int js = lane / B2, rem = lane - js * B2;
+  const bool act = lane < SPL * B2;
+  const int i = rem / BS, k = rem - i * BS, tr = k * BS + i;
   const int64_t n_brows = g.n_dofs / BS;
   for (int64_t P = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; P < n_brows;
        P += ((int64_t)gridDim.x * blockDim.x) >> 5) {
     const int64_t rb = g.brow_ptr[P];
     const int deg = (int)(g.brow_ptr[P + 1] - rb);
-    const int total = deg * B2;
-    int32_t rowp[BS];
-    bool rc[BS];
-#pragma unroll
-    for (int i = 0; i < BS; ++i) {
-      rowp[i] = g.row_ptr[BS * P + i];
-      rc[i] = g.constrained[BS * P + i] != 0;
-    }
-    DF acc[B2];
-#pragma unroll
-    for (int r = 0; r < B2; ++r) acc[r] = {0.f, 0.f};
+    const int32_t rowp = act ? g.row_ptr[BS * P + i] : 0;
+    const bool rc = act && g.constrained[BS * P + i] != 0;
+    DF acc = {0.f, 0.f};
     int jdiag = -1;
-    for (int m = lane; m < total; m += 32) {
-      const int jj = m / B2, rem = m - jj * B2;
-      const int i = rem / BS, k = rem - i * BS;
+    for (int jj = js; act && jj < deg; jj += SPL) {
       const int64_t j = rb + jj;
       const int32_t Q = g.bcol[j];
       if (Q == (int32_t)P) { jdiag = jj; continue; }
-      const int tr = k * BS + i;
-      DF s = {0.f, 0.f};
-      for (int32_t c = g.bptr[j]; c < g.bptr[j + 1]; ++c) {
-        const int32_t x = g.bcontrib[c];
-        s = df_add1(s, g.Koff32[(int64_t)(x >> 1) * B2 + ((x & 1) ? tr : rem)]);
-      }
+      const DF s = slot_sum<B2>(g, g.Koff32, g.bptr[j], g.bptr[j + 1], rem, tr, true);
       const float kv = __fadd_rn(s.hi, s.lo);  // the stored entry, rounded to FP32
-#pragma unroll
-      for (int r = 0; r < B2; ++r)
-        if (r == rem) acc[r] = df_add1(acc[r], kv);
-      const bool masked = rc[i] || g.constrained[(int64_t)BS * Q + k] != 0;
-      g.K[rowp[i] + jj * BS + k] = masked ? 0.0 : f2d(kv);
+      acc = df_add1(acc, kv);
+      const bool masked = rc || g.constrained[(int64_t)BS * Q + k] != 0;
+      g.K[rowp + jj * BS + k] = masked ? 0.0 : f2d(kv);
     }
-    // warp reduction of the row sums (fixed butterfly order: deterministic)
-#pragma unroll
-    for (int r = 0; r < B2; ++r)
+    // row sums: lanes rem, rem + B2, ... hold partial sums of the same entry
+    if constexpr (B2 == 1) {
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) {
         DF y;
-        y.hi = __shfl_xor_sync(0xffffffffu, acc[r].hi, o);
-        y.lo = __shfl_xor_sync(0xffffffffu, acc[r].lo, o);
-        acc[r] = (lane & o) ? df_add(y, acc[r]) : df_add(acc[r], y);
+        y.hi = __shfl_xor_sync(0xffffffffu, acc.hi, o);
+        y.lo = __shfl_xor_sync(0xffffffffu, acc.lo, o);
+        acc = (lane & o) ? df_add(y, acc) : df_add(acc, y);
       }
+    } else {
+#pragma unroll
+      for (int t = 1; t < SPL; ++t) {
+        DF y;
+        y.hi = __shfl_sync(0xffffffffu, acc.hi, (lane + t * B2) & 31);
+        y.lo = __shfl_sync(0xffffffffu, acc.lo, (lane + t * B2) & 31);
+        if (lane < B2) acc = df_add(acc, y);
+      }
+    }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) jdiag = max(jdiag, __shfl_xor_sync(0xffffffffu, jdiag, o));
     if (lane < B2 && jdiag >= 0) {
-      const int i = lane / BS, k = lane - i * BS;
-      double v = 0.0;
-#pragma unroll
-      for (int r = 0; r < B2; ++r)
-        if (r == lane) v = -(f2d(acc[r].hi) + f2d(acc[r].lo));
-      if (rc[i] || rc[k]) {
+      double v = -(f2d(acc.hi) + f2d(acc.lo));
+      if (rc || g.constrained[BS * P + k] != 0) {
         const int64_t j = rb + jdiag;
         v = (i == k) ? (double)(g.bptr[j + 1] - g.bptr[j]) : 0.0;
       }
-      g.K[rowp[i] + jdiag * BS + k] = v;
+      g.K[rowp + jdiag * BS + k] = v;
     }
     row_load<BS>(g, P, lane);
   }
