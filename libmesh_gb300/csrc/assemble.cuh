@@ -29,16 +29,14 @@ struct ElemArgs {
   const float2 *nodal_f2;     // the same as double-float pairs, or null
   const uint64_t *cmask;      // [n_elem] constrained local dofs, bit v*n + a
   double nu;                  // Poisson ratio (elasticity)
-  // Element blocks go straight to their place in the slot-major contribution
-  // buffer: dest[(e*n + a)*n + b] is the rank of element block (a, b) among the
-  // contributions of its CSR block slot (slots in CSR order, contributions in
-  // element order).  Only the diagonal and upper blocks are computed; each
-  // upper block is written as computed to slot (a, b) and transposed to (b, a).
-  // The FP64 drop-in stores double-float pairs (48-bit significand); the mixed
-  // form stores FP32 off-diagonal blocks only.
-  const int32_t *dest;        // [n_elem][n][n]
-  float2 *C2;                 // [n_contrib][nv][nv]  (FP64 drop-in)
-  float *C32;                 // [n_contrib][nv][nv]  (mixed; diagonal slots unused)
+  // Symmetric element matrices are stored as nv x nv blocks: the n diagonal
+  // blocks and the n(n-1)/2 strictly upper blocks (a < b, row-major over a
+  // then b).  The FP64 drop-in stores every entry as a double-float pair
+  // (hi + lo, 48-bit significand); the mixed form stores only the off-diagonal
+  // blocks, in FP32.
+  float2 *Kdiag2;             // [n_elem][n][nv][nv]          (FP64 drop-in)
+  float2 *Koff2;              // [n_elem][n(n-1)/2][nv][nv]   (FP64 drop-in)
+  float *Koff32;              // [n_elem][n(n-1)/2][nv][nv]   (mixed)
   float2 *Fe2;                // [n_elem][n][nv] load vector, double-float pairs
   int *status;                // [0] error code
   unsigned long long *bad_elem;  // first failing element id
@@ -53,11 +51,17 @@ struct GatherArgs {
   const int64_t *brow_ptr;    // [n_blocks+1]
   const int32_t *row_ptr;     // [n_dofs+1]
   const int32_t *bcol;        // [nnzb]
-  const int32_t *bptr;        // [nnzb+1] contribution range of each block slot
+  const int32_t *bptr;        // [nnzb+1] contributions per block slot
+  // Per slot, ascending in element: diagonal slots hold e*nb + a (a Kdiag
+  // block); off-diagonal slots hold 2*(e*no + o) + t, o the strictly upper
+  // block of the element pair and t = 1 when the slot takes its transpose.
+  const int32_t *bcontrib;
+  int no;                     // strictly upper blocks per element
   const int32_t *fptr;        // [n_blocks+1]
   const int32_t *fcontrib;    // e*nb + a, ascending per block row
-  const float2 *C2;
-  const float *C32;
+  const float2 *Kdiag2;
+  const float2 *Koff2;
+  const float *Koff32;
   const float2 *Fe2;
   const uint8_t *constrained; // [n_dofs] (mixed form applies the Dirichlet rows here)
   double *K;

@@ -57,11 +57,10 @@ struct lmg_ctx {
   double *d_coef = nullptr, *d_f = nullptr;
   float2 *d_f2 = nullptr;  // nodal load as double-float pairs
   // work and result buffers
-  int32_t *d_dest = nullptr;   // element block pair -> contribution rank
-  float2 *d_C2 = nullptr;      // slot-major contributions (FP64 drop-in)
+  float2 *d_Kdiag2 = nullptr, *d_Koff2 = nullptr;
   float2 *d_Fe2 = nullptr;
   double *d_K = nullptr, *d_F = nullptr;
-  float *d_C32 = nullptr;      // slot-major contributions (mixed)
+  float *d_Koff32 = nullptr;
   int *d_status = nullptr;
   unsigned long long *d_bad = nullptr;
   // PerfLog-style stage timing (CUDA events on the context stream)
@@ -181,11 +180,26 @@ __global__ void k_segsort(int64_t n_seg, const int32_t *ptr, int32_t *v) {
   }
 }
 
-// Inverts the per-slot contribution lists: dest[(e*nb + a)*nb + b] = rank of
-// element block (a, b) in the slot-major contribution buffer.
-__global__ void k_dest(int64_t n, const int32_t *contrib, int32_t *dest) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    dest[contrib[i]] = (int32_t)i;
+// Re-encodes every matrix contribution (e*nb + a)*nb + b of a slot into the
+// symmetric element storage: diagonal pairs -> e*nb + a (Kdiag block), other
+// pairs -> 2*(e*no + o) + t with o the strictly upper block of {a, b} and
+// t = 1 for a > b (the slot reads the transpose).  Element order is kept.
+__global__ void k_encode(int64_t n, int nb, int32_t *v) {
+  const int no = nb * (nb - 1) / 2;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t x = v[i];
+    const int64_t e = x / ((int64_t)nb * nb);
+    const int ab = (int)(x - e * nb * nb);
+    const int a = ab / nb, b = ab - a * nb;
+    if (a == b) {
+      v[i] = (int32_t)(e * nb + a);
+    } else {
+      const int lo = a < b ? a : b, hi = a < b ? b : a;
+      const int o = lo * nb - lo * (lo + 1) / 2 + (hi - lo - 1);
+      v[i] = (int32_t)(2 * (e * no + o) + (a > b ? 1 : 0));
+    }
+  }
 }
 
 // Nodal load split into double-float pairs (read by the affine element kernels).
@@ -322,8 +336,7 @@ lmg_status build_plan(lmg_ctx *c) {
   LMG_CUDA(c, cudaMemsetAsync(cur, 0, sizeof(int32_t) * c->nnzb, c->stream));
   k_fill<<<grid_for(c, npair, 256), 256, 0, c->stream>>>(npair, slot, c->d_bptr, cur, c->d_bcontrib);
   k_segsort<<<grid_for(c, c->nnzb, 256), 256, 0, c->stream>>>(c->nnzb, c->d_bptr, c->d_bcontrib);
-  LMG_CUDA(c, dalloc(c->d_dest, (size_t)npair));
-  k_dest<<<grid_for(c, npair, 256), 256, 0, c->stream>>>(npair, c->d_bcontrib, c->d_dest);
+  k_encode<<<grid_for(c, npair, 256), 256, 0, c->stream>>>(npair, nb, c->d_bcontrib);
   c->launches += 3;
   // vector plan
   LMG_CUDA(c, cudaMemsetAsync(cnt, 0, sizeof(int32_t) * c->n_blocks, c->stream));
@@ -339,7 +352,6 @@ lmg_status build_plan(lmg_ctx *c) {
   dfree(slot);
   dfree(cnt);
   dfree(cur);
-  dfree(c->d_bcontrib);  // the contribution lists now live in dest
   return check_status(c, "sparsity plan");
 }
 
@@ -406,8 +418,8 @@ lmg_status lmg_context_destroy(lmg_ctx *c) {
   dfree(c->d_xyz); dfree(c->d_conn); dfree(c->d_aff); dfree(c->d_gen); dfree(c->d_eb);
   dfree(c->d_cmask); dfree(c->d_cons); dfree(c->d_brow_ptr); dfree(c->d_bcol); dfree(c->d_row_ptr); dfree(c->d_col);
   dfree(c->d_bptr); dfree(c->d_bcontrib); dfree(c->d_fptr); dfree(c->d_fcontrib); dfree(c->d_tab);
-  dfree(c->d_coef); dfree(c->d_f); dfree(c->d_f2); dfree(c->d_dest); dfree(c->d_C2); dfree(c->d_Fe2); dfree(c->d_K);
-  dfree(c->d_F); dfree(c->d_C32); dfree(c->d_status); dfree(c->d_bad);
+  dfree(c->d_coef); dfree(c->d_f); dfree(c->d_f2); dfree(c->d_Kdiag2); dfree(c->d_Koff2); dfree(c->d_Fe2); dfree(c->d_K);
+  dfree(c->d_F); dfree(c->d_Koff32); dfree(c->d_status); dfree(c->d_bad);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
   delete c;
   return LMG_OK;
@@ -504,9 +516,10 @@ lmg_status lmg_sparsity_build(lmg_ctx *c, int64_t *nnz) {
   if (st) return st;
   LMG_CUDA(c, dalloc(c->d_K, (size_t)c->nnz));
   LMG_CUDA(c, dalloc(c->d_F, (size_t)c->n_dofs));
-  const size_t b2 = (size_t)c->bs * c->bs;
-  LMG_CUDA(c, dalloc(c->d_C2, (size_t)c->n_elem * c->nb * c->nb * b2));
-  dfree(c->d_C32);  // allocated on the first mixed assembly
+  const size_t b2 = (size_t)c->bs * c->bs, no = (size_t)c->nb * (c->nb - 1) / 2;
+  LMG_CUDA(c, dalloc(c->d_Kdiag2, (size_t)c->n_elem * c->nb * b2));
+  LMG_CUDA(c, dalloc(c->d_Koff2, (size_t)c->n_elem * no * b2));
+  dfree(c->d_Koff32);  // allocated on the first mixed assembly
   LMG_CUDA(c, dalloc(c->d_Fe2, (size_t)(c->n_elem * c->nl)));
   c->have_sparsity = true;
   if (nnz) *nnz = c->nnz;
@@ -617,8 +630,8 @@ lmg_status lmg_assemble(lmg_ctx *c, int32_t precision, double *K, double *F, int
   if (precision != LMG_FP64 && precision != LMG_MIXED) return fail(c, LMG_ERR_ARG, "assemble: unknown precision");
   cudaSetDevice(c->device);
   const bool mixed = precision == LMG_MIXED;
-  if (mixed && !c->d_C32)
-    LMG_CUDA(c, dalloc(c->d_C32, (size_t)c->n_elem * c->nb * c->nb * c->bs * c->bs));
+  if (mixed && !c->d_Koff32)
+    LMG_CUDA(c, dalloc(c->d_Koff32, (size_t)c->n_elem * c->nb * (c->nb - 1) / 2 * c->bs * c->bs));
   lmg_status st = reset_status(c);
   if (st) return st;
   ElemArgs a{};
@@ -630,9 +643,9 @@ lmg_status lmg_assemble(lmg_ctx *c, int32_t precision, double *K, double *F, int
   a.nodal_f2 = c->d_f2;
   a.cmask = c->d_cmask;
   a.nu = c->nu;
-  a.dest = c->d_dest;
-  a.C2 = c->d_C2;
-  a.C32 = c->d_C32;
+  a.Kdiag2 = c->d_Kdiag2;
+  a.Koff2 = c->d_Koff2;
+  a.Koff32 = c->d_Koff32;
   a.Fe2 = c->d_Fe2;
   a.status = c->d_status;
   a.bad_elem = c->d_bad;
@@ -665,10 +678,13 @@ lmg_status lmg_assemble(lmg_ctx *c, int32_t precision, double *K, double *F, int
   g.row_ptr = c->d_row_ptr;
   g.bcol = c->d_bcol;
   g.bptr = c->d_bptr;
+  g.bcontrib = c->d_bcontrib;
+  g.no = c->nb * (c->nb - 1) / 2;
   g.fptr = c->d_fptr;
   g.fcontrib = c->d_fcontrib;
-  g.C2 = c->d_C2;
-  g.C32 = c->d_C32;
+  g.Kdiag2 = c->d_Kdiag2;
+  g.Koff2 = c->d_Koff2;
+  g.Koff32 = c->d_Koff32;
   g.Fe2 = c->d_Fe2;
   g.constrained = c->d_cons;
   g.K = c->d_K;

@@ -292,20 +292,17 @@ __global__ void __launch_bounds__(128) k_elem_affine(ElemArgs a) {
                 out[3 * i + kk] = R::norm(acc);
               }
           }
-          const int64_t d_up = (int64_t)a.dest[((int64_t)et * N + ra) * N + cb] * B2;
-          const int64_t d_lo = (ra != cb) ? (int64_t)a.dest[((int64_t)et * N + cb) * N + ra] * B2 : -1;
 #pragma unroll
           for (int ik = 0; ik < B2; ++ik) {
             const int i = ik / NV, kk = ik - i * NV;
             const int lr = i * N + ra, lc = kk * N + cb;
             if constexpr (MIXED) {
-              a.C32[d_up + ik] = out[ik];
-              a.C32[d_lo + kk * NV + i] = out[ik];
+              a.Koff32[((int64_t)et * NO + o) * B2 + ik] = out[ik];
             } else {
               float2 v = make_float2(out[ik].hi, out[ik].lo);
               if (((mask >> lr) | (mask >> lc)) & 1ull) v = make_float2(lr == lc ? 1.f : 0.f, 0.f);
-              a.C2[d_up + ik] = v;
-              if (d_lo >= 0) a.C2[d_lo + kk * NV + i] = v;
+              if (o < 0) a.Kdiag2[((int64_t)et * N + ra) * B2 + ik] = v;
+              else a.Koff2[((int64_t)et * NO + o) * B2 + ik] = v;
             }
           }
         }
@@ -408,15 +405,12 @@ __global__ void __launch_bounds__(128) k_elem_general(ElemArgs a) {
 #pragma unroll
         for (int ik = 0; ik < B2; ++ik) {
           const int i = ik / NV, kk = ik - i * NV;
-          const int64_t d_up = (int64_t)a.dest[((int64_t)e * N + ra) * N + cb] * B2;
-          const int64_t d_lo = (ra != cb) ? (int64_t)a.dest[((int64_t)e * N + cb) * N + ra] * B2 : -1;
           if (MIXED) {
-            a.C32[d_up + ik] = (float)acc[k][ik];
-            a.C32[d_lo + kk * NV + i] = (float)acc[k][ik];
+            a.Koff32[((int64_t)e * NO + off_index(N, ra, cb)) * B2 + ik] = (float)acc[k][ik];
           } else {
             const DF v = df_split(masked((double)acc[k][ik], mask, i * N + ra, kk * N + cb));
-            a.C2[d_up + ik] = make_float2(v.hi, v.lo);
-            if (d_lo >= 0) a.C2[d_lo + kk * NV + i] = make_float2(v.hi, v.lo);
+            if (ra == cb) a.Kdiag2[((int64_t)e * N + ra) * B2 + ik] = make_float2(v.hi, v.lo);
+            else a.Koff2[((int64_t)e * NO + off_index(N, ra, cb)) * B2 + ik] = make_float2(v.hi, v.lo);
           }
         }
       }

@@ -59,35 +59,36 @@ __device__ __forceinline__ void row_load(const GatherArgs &g, int64_t P, int lan
   }
 }
 
-// Contributions of one block slot to one entry: a contiguous run of the
-// slot-major buffer, summed in double-float in element order.
+// Contributions of one block slot to one entry, summed in double-float in
+// element order; four predicated loads in flight per step.
 template <int B2, typename TV>
-__device__ __forceinline__ DF slot_sum(const TV *C, int32_t c0, int32_t c1, int rem) {
+__device__ __forceinline__ DF slot_sum(const GatherArgs &g, const TV *Kb, int32_t c0, int32_t c1, int rem, int tr,
+                                       bool coded) {
   DF s = {0.f, 0.f};
-  const TV *p = C + (int64_t)c0 * B2 + rem;
-  int32_t n = c1 - c0;
-  for (; n >= 4; n -= 4, p += 4 * B2) {
+  for (int32_t c = c0; c < c1; c += 4) {
+    int32_t x[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) x[u] = (c + u < c1) ? __ldg(g.bcontrib + c + u) : -1;
     TV v[4];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) v[u] = __ldg(p + u * B2);
-#pragma unroll
     for (int u = 0; u < 4; ++u) {
-      if constexpr (sizeof(TV) == 8) s = df_add(s, DF{((const float2 &)v[u]).x, ((const float2 &)v[u]).y});
-      else s = df_add1(s, (const float &)v[u]);
+      int64_t idx = 0;
+      if (x[u] >= 0) idx = coded ? (int64_t)(x[u] >> 1) * B2 + ((x[u] & 1) ? tr : rem) : (int64_t)x[u] * B2 + rem;
+      v[u] = (x[u] >= 0) ? __ldg(Kb + idx) : TV{};
     }
-  }
-  for (; n > 0; --n, p += B2) {
-    const TV v = __ldg(p);
-    if constexpr (sizeof(TV) == 8) s = df_add(s, DF{((const float2 &)v).x, ((const float2 &)v).y});
-    else s = df_add1(s, (const float &)v);
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+      if (x[u] >= 0) {
+        if constexpr (sizeof(TV) == 8) s = df_add(s, DF{((const float2 &)v[u]).x, ((const float2 &)v[u]).y});
+        else s = df_add1(s, (const float &)v[u]);
+      }
   }
   return s;
 }
 
 // FP64 drop-in insertion, warp per block row P.  Lane l < (32/B2)*B2 owns entry
-// rem = l % B2 of the slots jj = l / B2 + (32/B2) t; the B2 values of one
-// contribution are read by B2 neighbouring lanes as one chunk, and a block
-// row's contributions form one contiguous run of the buffer.  Each
+// rem = l % B2 of the slots jj = l / B2 + (32/B2) t, so the B2 values of one
+// stored element block are read by B2 neighbouring lanes as one chunk.  Each
 // value is the sum, in element order, of the double-float element entries that
 // land on it, rounded once to FP64.
 template <int BS>
@@ -96,7 +97,7 @@ __global__ void __launch_bounds__(256) k_gather(GatherArgs g) {
   const int lane = threadIdx.x & 31;
   const int js = lane / B2, rem = lane - js * B2;
   const bool act = lane < SPL * B2;
-  const int i = rem / BS, k = rem - i * BS;
+  const int i = rem / BS, k = rem - i * BS, tr = k * BS + i;
   const int64_t n_brows = g.n_dofs / BS;
   for (int64_t P = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; P < n_brows;
        P += ((int64_t)gridDim.x * blockDim.x) >> 5) {
@@ -105,7 +106,10 @@ __global__ void __launch_bounds__(256) k_gather(GatherArgs g) {
     const int32_t rowp = act ? g.row_ptr[BS * P + i] : 0;
     for (int jj = js; act && jj < deg; jj += SPL) {
       const int64_t j = rb + jj;
-      const DF s = slot_sum<B2>(g.C2, g.bptr[j], g.bptr[j + 1], rem);
+      const int32_t c0 = g.bptr[j], c1 = g.bptr[j + 1];
+      const bool diag = g.bcol[j] == (int32_t)P;
+      const DF s = diag ? slot_sum<B2>(g, g.Kdiag2, c0, c1, rem, rem, false)
+                        : slot_sum<B2>(g, g.Koff2, c0, c1, rem, tr, true);
       g.K[rowp + jj * BS + k] = df_to_double(s);
     }
     row_load<BS>(g, P, lane);
@@ -124,7 +128,7 @@ __global__ void __launch_bounds__(256) k_gather_mixed(GatherArgs g) {
   const int lane = threadIdx.x & 31;
   const int js = lane / B2, rem = lane - js * B2;
   const bool act = lane < SPL * B2;
-  const int i = rem / BS, k = rem - i * BS;
+  const int i = rem / BS, k = rem - i * BS, tr = k * BS + i;
   const int64_t n_brows = g.n_dofs / BS;
   for (int64_t P = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; P < n_brows;
        P += ((int64_t)gridDim.x * blockDim.x) >> 5) {
@@ -138,7 +142,7 @@ __global__ void __launch_bounds__(256) k_gather_mixed(GatherArgs g) {
       const int64_t j = rb + jj;
       const int32_t Q = g.bcol[j];
       if (Q == (int32_t)P) { jdiag = jj; continue; }
-      const DF s = slot_sum<B2>(g.C32, g.bptr[j], g.bptr[j + 1], rem);
+      const DF s = slot_sum<B2>(g, g.Koff32, g.bptr[j], g.bptr[j + 1], rem, tr, true);
       const float kv = __fadd_rn(s.hi, s.lo);  // the stored entry, rounded to FP32
       acc = df_add1(acc, kv);
       const bool masked = rc || g.constrained[(int64_t)BS * Q + k] != 0;
