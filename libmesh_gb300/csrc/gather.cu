@@ -62,12 +62,13 @@ __device__ __forceinline__ void row_load(const GatherArgs &g, int64_t P, int lan
 // Contributions of one block slot to one entry, summed in double-float in
 // element order; four predicated loads in flight per step.
 template <int B2, typename TV>
-__device__ __forceinline__ DF slot_sum(const int32_t *codes, int32_t n, const TV *Kb, int rem, int tr, bool coded) {
+__device__ __forceinline__ DF slot_sum(const GatherArgs &g, const TV *Kb, int32_t c0, int32_t c1, int rem, int tr,
+                                       bool coded) {
   DF s = {0.f, 0.f};
-  for (int32_t c = 0; c < n; c += 4) {
+  for (int32_t c = c0; c < c1; c += 4) {
     int32_t x[4];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) x[u] = (c + u < n) ? codes[c + u] : -1;
+    for (int u = 0; u < 4; ++u) x[u] = (c + u < c1) ? __ldg(g.bcontrib + c + u) : -1;
     TV v[4];
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
@@ -85,29 +86,6 @@ __device__ __forceinline__ DF slot_sum(const int32_t *codes, int32_t n, const TV
   return s;
 }
 
-// A warp stages the slot offsets and contribution codes of its block row in
-// shared memory with coalesced loads (both are contiguous in CSR order), so
-// each lane's element-block loads issue without a dependent global load first.
-constexpr int STAGE_SLOTS = 160, STAGE_CODES = 640, GATHER_WARPS = 8;
-struct RowStage {
-  int32_t ptr[STAGE_SLOTS + 1];
-  int32_t code[STAGE_CODES];
-};
-
-// Returns true when the row fits the stage (else callers read global memory).
-__device__ __forceinline__ bool stage_row(const GatherArgs &g, int64_t rb, int deg, RowStage &st, int lane,
-                                          int32_t &base) {
-  base = g.bptr[rb];
-  const int32_t n = g.bptr[rb + deg] - base;
-  const bool fits = deg <= STAGE_SLOTS && n <= STAGE_CODES;
-  if (fits) {
-    for (int t = lane; t <= deg; t += 32) st.ptr[t] = g.bptr[rb + t] - base;
-    for (int t = lane; t < n; t += 32) st.code[t] = g.bcontrib[base + t];
-  }
-  __syncwarp();
-  return fits;
-}
-
 // FP64 drop-in insertion, warp per block row P.  Lane l < (32/B2)*B2 owns entry
 // rem = l % B2 of the slots jj = l / B2 + (32/B2) t, so the B2 values of one
 // stored element block are read by B2 neighbouring lanes as one chunk.  Each
@@ -121,26 +99,20 @@ __global__ void __launch_bounds__(256) k_gather(GatherArgs g) {
   const bool act = lane < SPL * B2;
   const int i = rem / BS, k = rem - i * BS, tr = k * BS + i;
   const int64_t n_brows = g.n_dofs / BS;
-  __shared__ RowStage stages[GATHER_WARPS];
-  RowStage &st = stages[threadIdx.x >> 5];
   for (int64_t P = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; P < n_brows;
        P += ((int64_t)gridDim.x * blockDim.x) >> 5) {
     const int64_t rb = g.brow_ptr[P];
     const int deg = (int)(g.brow_ptr[P + 1] - rb);
     const int32_t rowp = act ? g.row_ptr[BS * P + i] : 0;
-    int32_t base;
-    const bool staged = stage_row(g, rb, deg, st, lane, base);
     for (int jj = js; act && jj < deg; jj += SPL) {
       const int64_t j = rb + jj;
-      const int32_t c0 = staged ? st.ptr[jj] : g.bptr[j] - base, c1 = staged ? st.ptr[jj + 1] : g.bptr[j + 1] - base;
-      const int32_t *codes = staged ? st.code + c0 : g.bcontrib + base + c0;
+      const int32_t c0 = g.bptr[j], c1 = g.bptr[j + 1];
       const bool diag = g.bcol[j] == (int32_t)P;
-      const DF s = diag ? slot_sum<B2>(codes, c1 - c0, g.Kdiag2, rem, rem, false)
-                        : slot_sum<B2>(codes, c1 - c0, g.Koff2, rem, tr, true);
+      const DF s = diag ? slot_sum<B2>(g, g.Kdiag2, c0, c1, rem, rem, false)
+                        : slot_sum<B2>(g, g.Koff2, c0, c1, rem, tr, true);
       g.K[rowp + jj * BS + k] = df_to_double(s);
     }
     row_load<BS>(g, P, lane);
-    __syncwarp();
   }
 }
 
@@ -158,25 +130,19 @@ __global__ void __launch_bounds__(256) k_gather_mixed(GatherArgs g) {
   const bool act = lane < SPL * B2;
   const int i = rem / BS, k = rem - i * BS, tr = k * BS + i;
   const int64_t n_brows = g.n_dofs / BS;
-  __shared__ RowStage stages[GATHER_WARPS];
-  RowStage &st = stages[threadIdx.x >> 5];
   for (int64_t P = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; P < n_brows;
        P += ((int64_t)gridDim.x * blockDim.x) >> 5) {
     const int64_t rb = g.brow_ptr[P];
     const int deg = (int)(g.brow_ptr[P + 1] - rb);
     const int32_t rowp = act ? g.row_ptr[BS * P + i] : 0;
     const bool rc = act && g.constrained[BS * P + i] != 0;
-    int32_t base;
-    const bool staged = stage_row(g, rb, deg, st, lane, base);
     DF acc = {0.f, 0.f};
     int jdiag = -1;
     for (int jj = js; act && jj < deg; jj += SPL) {
       const int64_t j = rb + jj;
       const int32_t Q = g.bcol[j];
       if (Q == (int32_t)P) { jdiag = jj; continue; }
-      const int32_t c0 = staged ? st.ptr[jj] : g.bptr[j] - base, c1 = staged ? st.ptr[jj + 1] : g.bptr[j + 1] - base;
-      const int32_t *codes = staged ? st.code + c0 : g.bcontrib + base + c0;
-      const DF s = slot_sum<B2>(codes, c1 - c0, g.Koff32, rem, tr, true);
+      const DF s = slot_sum<B2>(g, g.Koff32, g.bptr[j], g.bptr[j + 1], rem, tr, true);
       const float kv = __fadd_rn(s.hi, s.lo);  // the stored entry, rounded to FP32
       acc = df_add1(acc, kv);
       const bool masked = rc || g.constrained[(int64_t)BS * Q + k] != 0;
@@ -211,7 +177,6 @@ __global__ void __launch_bounds__(256) k_gather_mixed(GatherArgs g) {
       g.K[rowp + jdiag * BS + k] = v;
     }
     row_load<BS>(g, P, lane);
-    __syncwarp();
   }
 }
 
