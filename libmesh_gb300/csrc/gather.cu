@@ -88,7 +88,10 @@ __device__ __forceinline__ DF slot_sum(const GatherArgs &g, const TV *Kb, int32_
 
 // FP64 drop-in insertion, warp per block row P.  Lane l < (32/B2)*B2 owns entry
 // rem = l % B2 of the slots jj = l / B2 + (32/B2) t, so the B2 values of one
-// stored element block are read by B2 neighbouring lanes as one chunk.  Each
+// stored element block are read by B2 neighbouring lanes as one chunk.  Both
+// forms are symmetric and their sums run over the same element blocks in the
+// same order, so K_QP = K_PQ^T bit for bit: a row computes its diagonal and
+// upper slots and writes each upper value into the transposed slot as well.  Each
 // value is the sum, in element order, of the double-float element entries that
 // land on it, rounded once to FP64.
 template <int BS>
@@ -106,11 +109,18 @@ __global__ void __launch_bounds__(256) k_gather(GatherArgs g) {
     const int32_t rowp = act ? g.row_ptr[BS * P + i] : 0;
     for (int jj = js; act && jj < deg; jj += SPL) {
       const int64_t j = rb + jj;
+      const int32_t Q = g.bcol[j];
+      if (Q < (int32_t)P) continue;  // written by block row Q as a transpose
       const int32_t c0 = g.bptr[j], c1 = g.bptr[j + 1];
-      const bool diag = g.bcol[j] == (int32_t)P;
+      const bool diag = Q == (int32_t)P;
       const DF s = diag ? slot_sum<B2>(g, g.Kdiag2, c0, c1, rem, rem, false)
                         : slot_sum<B2>(g, g.Koff2, c0, c1, rem, tr, true);
-      g.K[rowp + jj * BS + k] = df_to_double(s);
+      const double v = df_to_double(s);
+      g.K[rowp + jj * BS + k] = v;
+      if (!diag) {  // K is symmetric entry by entry: K_QP^{ki} = K_PQ^{ik}
+        const int32_t jt = g.tslot[j];
+        g.K[g.row_ptr[(int64_t)BS * Q + k] + (int64_t)(jt - g.brow_ptr[Q]) * BS + i] = v;
+      }
     }
     row_load<BS>(g, P, lane);
   }
