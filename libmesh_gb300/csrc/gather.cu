@@ -107,10 +107,15 @@ __global__ void __launch_bounds__(256) k_gather(GatherArgs g) {
     const int64_t rb = g.brow_ptr[P];
     const int deg = (int)(g.brow_ptr[P + 1] - rb);
     const int32_t rowp = act ? g.row_ptr[BS * P + i] : 0;
-    for (int jj = js; act && jj < deg; jj += SPL) {
+    // the diagonal and upper slots are the suffix of the sorted block row
+    int lo = 0, hi = deg;
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if (g.bcol[rb + mid] < (int32_t)P) lo = mid + 1; else hi = mid;
+    }
+    for (int jj = lo + js; act && jj < deg; jj += SPL) {
       const int64_t j = rb + jj;
       const int32_t Q = g.bcol[j];
-      if (Q < (int32_t)P) continue;  // written by block row Q as a transpose
       const int32_t c0 = g.bptr[j], c1 = g.bptr[j + 1];
       const bool diag = Q == (int32_t)P;
       const DF s = diag ? slot_sum<B2>(g, g.Kdiag2, c0, c1, rem, rem, false)
