@@ -86,73 +86,45 @@ __device__ __forceinline__ DF slot_sum(const GatherArgs &g, const TV *Kb, int32_
   return s;
 }
 
-// FP64 drop-in insertion, warp per block row P, lane per block slot: a lane
-// loads each contributing element block once (its bs*bs values are contiguous)
-// and accumulates all bs*bs entries, so index loads and address arithmetic are
-// shared by the whole block.  Both forms are symmetric and every sum runs over
-// the same element blocks in the same order, so K_QP = K_PQ^T bit for bit: a
-// row computes its diagonal and upper slots and also writes each upper block
-// transposed into slot (Q, P).  Each value is the sum, in element order, of the
-// double-float element entries that land on it, rounded once to FP64.
+// FP64 drop-in insertion, warp per block row P.  Lane l < (32/B2)*B2 owns entry
+// rem = l % B2 of the slots jj = l / B2 + (32/B2) t, so the B2 values of one
+// stored element block are read by B2 neighbouring lanes as one chunk.  Both
+// forms are symmetric and their sums run over the same element blocks in the
+// same order, so K_QP = K_PQ^T bit for bit: a row computes its diagonal and
+// upper slots and writes each upper value into the transposed slot as well.  Each
+// value is the sum, in element order, of the double-float element entries that
+// land on it, rounded once to FP64.
 template <int BS>
 __global__ void __launch_bounds__(256) k_gather(GatherArgs g) {
-  constexpr int B2 = BS * BS;
+  constexpr int B2 = BS * BS, SPL = 32 / B2;
   const int lane = threadIdx.x & 31;
+  const int js = lane / B2, rem = lane - js * B2;
+  const bool act = lane < SPL * B2;
+  const int i = rem / BS, k = rem - i * BS, tr = k * BS + i;
   const int64_t n_brows = g.n_dofs / BS;
   for (int64_t P = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; P < n_brows;
        P += ((int64_t)gridDim.x * blockDim.x) >> 5) {
     const int64_t rb = g.brow_ptr[P];
     const int deg = (int)(g.brow_ptr[P + 1] - rb);
+    const int32_t rowp = act ? g.row_ptr[BS * P + i] : 0;
     // the diagonal and upper slots are the suffix of the sorted block row
     int lo = 0, hi = deg;
     while (lo < hi) {
       const int mid = (lo + hi) >> 1;
       if (g.bcol[rb + mid] < (int32_t)P) lo = mid + 1; else hi = mid;
     }
-    for (int jj = lo + lane; jj < deg; jj += 32) {
+    for (int jj = lo + js; act && jj < deg; jj += SPL) {
       const int64_t j = rb + jj;
       const int32_t Q = g.bcol[j];
       const int32_t c0 = g.bptr[j], c1 = g.bptr[j + 1];
       const bool diag = Q == (int32_t)P;
-      DF s[B2];
-#pragma unroll
-      for (int r = 0; r < B2; ++r) s[r] = {0.f, 0.f};
-      for (int32_t c = c0; c < c1; ++c) {
-        const int32_t x = __ldg(g.bcontrib + c);
-        if (diag) {
-          const float2 *blk = g.Kdiag2 + (int64_t)x * B2;
-#pragma unroll
-          for (int r = 0; r < B2; ++r) {
-            const float2 v = __ldg(blk + r);
-            s[r] = df_add(s[r], DF{v.x, v.y});
-          }
-        } else {
-          const float2 *blk = g.Koff2 + (int64_t)(x >> 1) * B2;
-          const bool t = x & 1;
-#pragma unroll
-          for (int i = 0; i < BS; ++i)
-#pragma unroll
-            for (int k = 0; k < BS; ++k) {
-              const float2 v = __ldg(blk + (t ? k * BS + i : i * BS + k));
-              s[i * BS + k] = df_add(s[i * BS + k], DF{v.x, v.y});
-            }
-        }
-      }
-      const int64_t jt = diag ? 0 : g.tslot[j];
-#pragma unroll
-      for (int i = 0; i < BS; ++i) {
-        double *row = g.K + g.row_ptr[BS * P + i] + (int64_t)jj * BS;
-#pragma unroll
-        for (int k = 0; k < BS; ++k) row[k] = df_to_double(s[i * BS + k]);
-      }
-      if (!diag) {  // K_QP^{ki} = K_PQ^{ik}
-        const int64_t off = (jt - g.brow_ptr[Q]) * BS;
-#pragma unroll
-        for (int k = 0; k < BS; ++k) {
-          double *row = g.K + g.row_ptr[(int64_t)BS * Q + k] + off;
-#pragma unroll
-          for (int i = 0; i < BS; ++i) row[i] = df_to_double(s[i * BS + k]);
-        }
+      const DF s = diag ? slot_sum<B2>(g, g.Kdiag2, c0, c1, rem, rem, false)
+                        : slot_sum<B2>(g, g.Koff2, c0, c1, rem, tr, true);
+      const double v = df_to_double(s);
+      g.K[rowp + jj * BS + k] = v;
+      if (!diag) {  // K is symmetric entry by entry: K_QP^{ki} = K_PQ^{ik}
+        const int32_t jt = g.tslot[j];
+        g.K[g.row_ptr[(int64_t)BS * Q + k] + (int64_t)(jt - g.brow_ptr[Q]) * BS + i] = v;
       }
     }
     row_load<BS>(g, P, lane);
