@@ -174,6 +174,18 @@ lmg_status lmg_synchronize(lmg_ctx *ctx);
 lmg_status lmg_cg_solve(lmg_ctx *ctx, const double *rhs, double *x, double rtol, int32_t maxit,
                         int32_t *iters, double *relres);
 
+/* Adjoint sensitivities (ImplicitSystem::adjoint_qoi_parameter_sensitivity,
+ * src/systems/implicit_system.C:517-623, with the element coefficients of the
+ * form as parameters; ParameterVector, src/systems/parameter_vector.C:28-132).
+ * lmg_qoi_region_load: q[n_dofs] = derivative of the QoI "integral of the
+ * solution over the marked elements" (in_region[n_elem] 0/1), the right-hand
+ * side of the adjoint solve K^T z = q (lmg_cg_solve with rhs = q; K is
+ * symmetric).  lmg_vjp_coef: dq/dcoef_e = -z_e^T (dK_e/dcoef_e) u_e for every
+ * element, exact (K is linear in each coefficient and F does not depend on it),
+ * geometry recomputed per quadrature point.  u, z, q, dq_dcoef are host arrays. */
+lmg_status lmg_qoi_region_load(lmg_ctx *ctx, const uint8_t *in_region, double *q);
+lmg_status lmg_vjp_coef(lmg_ctx *ctx, const double *u, const double *z, double *dq_dcoef);
+
 /* First failing element of the last call (-1 if none) and a message. */
 lmg_status lmg_last_error(lmg_ctx *ctx, int64_t *elem_id, char *msg, int32_t msg_len);
 

@@ -168,6 +168,19 @@ class GpuAssembly:
         self._ok(lib().lmg_cg_solve(self.ctx, ptr(b), ptr(x), float(rtol), int(maxit), C.byref(it), C.byref(rr)))
         return x, it.value, rr.value
 
+    def qoi_region_load(self, in_region):
+        """dq/du of q(u) = integral of u over the marked elements."""
+        q = np.empty(self.dof_map.n_dofs, np.float64)
+        self._ok(lib().lmg_qoi_region_load(self.ctx, ptr(np.ascontiguousarray(in_region, np.uint8)), ptr(q)))
+        return q
+
+    def vjp_coef(self, u, z):
+        """dq/dcoef_e = -z_e^T dK_e/dcoef_e u_e for every element."""
+        g = np.empty(self.mesh.n_elem, np.float64)
+        self._ok(lib().lmg_vjp_coef(self.ctx, ptr(np.ascontiguousarray(u, np.float64)),
+                                    ptr(np.ascontiguousarray(z, np.float64)), ptr(g)))
+        return g
+
     def perflog_enable(self, on=True):
         self._ok(lib().lmg_perflog_enable(self.ctx, 1 if on else 0))
 
@@ -227,6 +240,18 @@ class LinearImplicitSystem:
         K, F = self.assembly.assemble(precision)
         self.matrix, self.rhs = K, F
         return K, F
+
+    def adjoint_qoi_parameter_sensitivity(self, in_region, rtol=1e-12, maxit=50000):
+        """q(u) = integral of u over the marked elements; returns (q, dq/dcoef_e for
+        every element) from one primal and one adjoint solve and one VJP pass
+        (ImplicitSystem::adjoint_qoi_parameter_sensitivity with the element
+        coefficients as the ParameterVector)."""
+        a = self.assembly
+        a.assemble()
+        u, _, _ = a.solve(rtol=rtol, maxit=maxit)
+        qv = a.qoi_region_load(in_region)
+        z, _, _ = a.solve(rhs=qv, rtol=rtol, maxit=maxit)
+        return float(qv @ u), a.vjp_coef(u, z)
 
     def matrix_csr(self):
         import scipy.sparse as sp

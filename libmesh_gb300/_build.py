@@ -12,7 +12,7 @@ OUT = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT, "liblmg.so")
 
 CXX_SOURCES = ["host_mesh.cpp", "host_mesh_tri.cpp", "host_dofmap.cpp", "fe_tables.cpp"]
-CU_SOURCES = ["elements.cu", "gather.cu", "context.cu", "cg.cu", "probe.cu"]
+CU_SOURCES = ["elements.cu", "gather.cu", "context.cu", "cg.cu", "vjp.cu", "probe.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -69,6 +69,25 @@ struct GatherArgs {
   double *F;
 };
 
+// Adjoint sensitivity and QoI load arguments.
+struct VjpArgs {
+  int64_t n_elem;
+  const double *xyz;
+  const int32_t *conn;        // [n_elem][n]
+  const int32_t *eb;          // [n_elem][n] block (node) of each local node
+  const double *u, *z;        // [n_dofs] primal and adjoint solutions
+  const uint8_t *region;      // [n_elem] QoI element set
+  const uint64_t *cmask;      // [n_elem] constrained local dofs (their QoI load is zero)
+  double nu;
+  double *out;                // [n_elem] dq/dp_e
+  float2 *Fe2;                // [n_elem][n][nv] load of the QoI set
+  int *status;
+  unsigned long long *bad_elem;
+  DevFE fe;
+};
+bool launch_vjp(int form, int n, int nv, bool region, const VjpArgs &v, int grid, cudaStream_t s);
+void launch_gather_f(const GatherArgs &g, cudaStream_t s);
+
 // Whether an element kernel is instantiated for (form, shapes per variable, variables).
 bool elements_built(int form, int n, int nv);
 void launch_elements(int form, int n, int nv, bool affine, bool mixed, const ElemArgs &a, int grid,

@@ -748,6 +748,78 @@ lmg_status lmg_last_error(lmg_ctx *c, int64_t *elem_id, char *msg, int32_t msg_l
   return LMG_OK;
 }
 
+namespace {
+VjpArgs vjp_args(lmg_ctx *c) {
+  VjpArgs v{};
+  v.n_elem = c->n_elem;
+  v.xyz = c->d_xyz;
+  v.conn = c->d_conn;
+  v.eb = c->d_eb;
+  v.nu = c->nu;
+  v.status = c->d_status;
+  v.bad_elem = c->d_bad;
+  v.cmask = c->d_cmask;
+  v.fe = c->dfe;
+  return v;
+}
+}  // namespace
+
+lmg_status lmg_qoi_region_load(lmg_ctx *c, const uint8_t *in_region, double *q) {
+  if (!c || !in_region || !q) return fail(c, LMG_ERR_ARG, "qoi_region_load: bad argument");
+  if (!c->have_sparsity || !c->have_form) return fail(c, LMG_ERR_STATE, "qoi_region_load: set up the system first");
+  cudaSetDevice(c->device);
+  uint8_t *d_reg = nullptr;
+  LMG_CUDA(c, dupload(c, d_reg, in_region, (size_t)c->n_elem));
+  lmg_status st = reset_status(c);
+  if (st) return st;
+  VjpArgs v = vjp_args(c);
+  v.region = d_reg;
+  v.Fe2 = c->d_Fe2;
+  launch_vjp(c->form, c->tab.n, c->n_vars, true, v, c->n_sm * 8, c->stream);
+  GatherArgs g{};
+  g.n_dofs = c->n_dofs;
+  g.bs = c->bs;
+  g.fptr = c->d_fptr;
+  g.fcontrib = c->d_fcontrib;
+  g.Fe2 = c->d_Fe2;
+  double *d_q = nullptr;
+  LMG_CUDA(c, dalloc(d_q, (size_t)c->n_dofs));
+  g.F = d_q;
+  launch_gather_f(g, c->stream);
+  c->launches += 2;
+  LMG_CUDA(c, cudaGetLastError());
+  LMG_CUDA(c, cudaMemcpyAsync(q, d_q, sizeof(double) * c->n_dofs, cudaMemcpyDeviceToHost, c->stream));
+  st = check_status(c, "qoi_region_load");
+  dfree(d_reg);
+  dfree(d_q);
+  return st;
+}
+
+lmg_status lmg_vjp_coef(lmg_ctx *c, const double *u, const double *z, double *dq_dcoef) {
+  if (!c || !u || !z || !dq_dcoef) return fail(c, LMG_ERR_ARG, "vjp_coef: bad argument");
+  if (!c->have_sparsity || !c->have_form) return fail(c, LMG_ERR_STATE, "vjp_coef: set up the system first");
+  cudaSetDevice(c->device);
+  double *du = nullptr, *dz = nullptr, *dout = nullptr;
+  LMG_CUDA(c, dupload(c, du, u, (size_t)c->n_dofs));
+  LMG_CUDA(c, dupload(c, dz, z, (size_t)c->n_dofs));
+  LMG_CUDA(c, dalloc(dout, (size_t)c->n_elem));
+  lmg_status st = reset_status(c);
+  if (st) return st;
+  VjpArgs v = vjp_args(c);
+  v.u = du;
+  v.z = dz;
+  v.out = dout;
+  launch_vjp(c->form, c->tab.n, c->n_vars, false, v, c->n_sm * 8, c->stream);
+  c->launches++;
+  LMG_CUDA(c, cudaGetLastError());
+  LMG_CUDA(c, cudaMemcpyAsync(dq_dcoef, dout, sizeof(double) * c->n_elem, cudaMemcpyDeviceToHost, c->stream));
+  st = check_status(c, "vjp_coef");
+  dfree(du);
+  dfree(dz);
+  dfree(dout);
+  return st;
+}
+
 lmg_status lmg_cg_solve(lmg_ctx *c, const double *rhs, double *x, double rtol, int32_t maxit,
                         int32_t *iters, double *relres) {
   if (!c || !x || rtol <= 0 || maxit <= 0) return fail(c, LMG_ERR_ARG, "cg_solve: bad argument");

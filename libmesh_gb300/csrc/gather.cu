@@ -195,7 +195,28 @@ __global__ void __launch_bounds__(256) k_gather_mixed(GatherArgs g) {
   }
 }
 
+// Load vector only (QoI derivative): warp per block row, F from the element loads.
+template <int BS>
+__global__ void __launch_bounds__(256) k_gather_f(GatherArgs g) {
+  const int lane = threadIdx.x & 31;
+  const int64_t n_brows = g.n_dofs / BS;
+  for (int64_t P = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; P < n_brows;
+       P += ((int64_t)gridDim.x * blockDim.x) >> 5)
+    row_load<BS>(g, P, lane);
+}
+
 }  // namespace
+
+void launch_gather_f(const GatherArgs &g, cudaStream_t s) {
+  int dev = 0, n_sm = 152;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
+  int64_t blocks = (g.n_dofs / g.bs + 7) / 8;
+  if (blocks > (int64_t)n_sm * 16) blocks = (int64_t)n_sm * 16;
+  if (blocks < 1) blocks = 1;
+  if (g.bs == 1) k_gather_f<1><<<(int)blocks, 256, 0, s>>>(g);
+  else if (g.bs == 3) k_gather_f<3><<<(int)blocks, 256, 0, s>>>(g);
+}
 
 bool gather_built(int bs) { return bs == 1 || bs == 3; }
 

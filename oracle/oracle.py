@@ -108,3 +108,46 @@ def assemble(form, elem_type, fe_order, q_order, xyz, conn, n_vars, elem_dofs, n
     if timing is not None:
         timing["seconds"] = secs.value
     return K, F, st, bad.value
+
+
+def adjoint_qoi_parameter_sensitivity(form, elem_type, fe_order, q_order, xyz, conn, n_vars, elem_dofs, n_dofs,
+                                      constrained, row_ptr, col, coef, nodal_f, in_region, params, nu=0.3):
+    """Restatement of ImplicitSystem::adjoint_qoi_parameter_sensitivity
+    (src/systems/implicit_system.C:474-623) for q(u) = integral of u over the
+    marked elements and the element coefficients listed in `params`:
+    u from K u = F; z from K^T z = dq/du (constrained dofs held at zero);
+    for each parameter p: delta = 1e-6 max(|p|, 1e-3), the residual R = K u - F
+    assembled at p - delta and p + delta, -dR/dp = (R(p-d) - R(p+d)) / (2 d),
+    dq/dp = (q(p+d) - q(p-d)) / (2 d) (zero here: q does not depend on p),
+    sensitivity = dq/dp + (-dR/dp) . z.  Small meshes only (two full
+    assemblies per parameter).  Returns (q, sensitivities)."""
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as spla
+    n = n_dofs
+    K, F, st, _ = assemble(form, elem_type, fe_order, q_order, xyz, conn, n_vars, elem_dofs, n_dofs, constrained,
+                           row_ptr, col, coef=coef, nodal_f=nodal_f, nu=nu)
+    assert st == 0
+    A = sp.csc_matrix(sp.csr_matrix((K, col, row_ptr), shape=(n, n)))
+    u = spla.spsolve(A, F)
+    sel = np.nonzero(np.asarray(in_region) != 0)[0]
+    ones = np.ones((xyz.shape[0], n_vars))
+    _, qv, st, _ = assemble(form, elem_type, fe_order, q_order, xyz, conn[sel], n_vars, elem_dofs[sel], n_dofs,
+                            np.zeros(n_dofs, np.uint8), row_ptr, col, coef=coef[sel], nodal_f=ones, nu=nu)
+    assert st == 0
+    qv[np.asarray(constrained) != 0] = 0.0
+    z = spla.spsolve(A.T.tocsc(), qv)
+    sens = []
+    for j in params:
+        old = coef[j]
+        d = 1e-6 * max(abs(old), 1e-3)
+        cm, cp = coef.copy(), coef.copy()
+        cm[j], cp[j] = old - d, old + d
+        Km, Fm, _, _ = assemble(form, elem_type, fe_order, q_order, xyz, conn, n_vars, elem_dofs, n_dofs, constrained,
+                                row_ptr, col, coef=cm, nodal_f=nodal_f, nu=nu)
+        Kp, Fp, _, _ = assemble(form, elem_type, fe_order, q_order, xyz, conn, n_vars, elem_dofs, n_dofs, constrained,
+                                row_ptr, col, coef=cp, nodal_f=nodal_f, nu=nu)
+        Rm = sp.csr_matrix((Km, col, row_ptr), shape=(n, n)) @ u - Fm
+        Rp = sp.csr_matrix((Kp, col, row_ptr), shape=(n, n)) @ u - Fp
+        neg = (Rm - Rp) / (2 * d)
+        sens.append(0.0 + neg @ z)
+    return float(qv @ u), np.array(sens)
