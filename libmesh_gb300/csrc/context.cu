@@ -333,7 +333,7 @@ void detect_blocks(lmg_ctx *c) {
 lmg_status build_plan(lmg_ctx *c) {
   const int nb = c->nb;
   const int64_t npair = c->n_elem * nb * nb, nrow = c->n_elem * nb;
-  if (npair >= INT32_MAX) return fail(c, LMG_ERR_UNSUPPORTED, "mesh too large for 32-bit plan");
+  if (npair * c->bs * c->bs >= INT32_MAX) return fail(c, LMG_ERR_UNSUPPORTED, "mesh too large for 32-bit plan");
   if (!gather_built(c->bs)) return fail(c, LMG_ERR_UNSUPPORTED, "no insertion kernel for this block size");
   int32_t *slot = nullptr, *cnt = nullptr, *cur = nullptr;
   LMG_CUDA(c, dalloc(slot, (size_t)npair));

@@ -132,7 +132,7 @@ __global__ void __launch_bounds__(256) k_gather(GatherArgs g) {
 }
 
 // Mixed insertion, warp per block row P, same lane layout.  Off-diagonal
-// entries: contributions summed in double-float, rounded to FP32, masked by the
+// entries: FP32 contributions summed in FP32 in element order, masked by the
 // Dirichlet rows and columns.  Diagonal blocks: minus the double-float sum of
 // the row's stored (unmasked) off-diagonal entries, so K t = 0 holds to FP64
 // roundoff for every rigid translation t on unconstrained rows; a constrained
@@ -157,9 +157,22 @@ __global__ void __launch_bounds__(256) k_gather_mixed(GatherArgs g) {
       const int64_t j = rb + jj;
       const int32_t Q = g.bcol[j];
       if (Q == (int32_t)P) { jdiag = jj; continue; }
-      const DF s = slot_sum<B2>(g, g.Koff32, g.bptr[j], g.bptr[j + 1], rem, tr, true);
-      const float kv = __fadd_rn(s.hi, s.lo);  // the stored entry, rounded to FP32
-      acc = df_add1(acc, kv);
+      // FP32 sum of the FP32 contributions, in element order (32-bit offsets:
+      // the plan guarantees n_contributions * bs^2 < 2^31)
+      const int32_t c0 = g.bptr[j], c1 = g.bptr[j + 1];
+      float kv = 0.f;
+      for (int32_t c = c0; c < c1; c += 4) {
+        float v[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int32_t x = (c + u < c1) ? __ldg(g.bcontrib + c + u) : -1;
+          v[u] = (x >= 0) ? __ldg(g.Koff32 + (x >> 1) * B2 + ((x & 1) ? tr : rem)) : 0.f;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+          if (c + u < c1) kv = __fadd_rn(kv, v[u]);
+      }
+      acc = df_add1(acc, kv);  // row sums stay double-float over the stored entries
       const bool masked = rc || g.constrained[(int64_t)BS * Q + k] != 0;
       g.K[rowp + jj * BS + k] = masked ? 0.0 : f2d(kv);
     }
