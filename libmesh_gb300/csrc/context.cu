@@ -672,7 +672,7 @@ lmg_status lmg_assemble(lmg_ctx *c, int32_t precision, double *K, double *F, int
   a.status = c->d_status;
   a.bad_elem = c->d_bad;
   a.fe = c->dfe;
-  const int grid = c->n_sm * 8;
+  const int grid = c->n_sm * 32;  // grid-stride: enough CTAs to fill every SM
   cudaEvent_t e3[3] = {nullptr, nullptr, nullptr};
   if (c->perflog) {
     for (auto &e : e3) LMG_CUDA(c, cudaEventCreate(&e));
