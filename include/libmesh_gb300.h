@@ -174,6 +174,33 @@ lmg_status lmg_synchronize(lmg_ctx *ctx);
 lmg_status lmg_cg_solve(lmg_ctx *ctx, const double *rhs, double *x, double rtol, int32_t maxit,
                         int32_t *iters, double *relres);
 
+/* lmg_cg_solve_noalloc — no counterpart in libMesh.  The solve of lmg_cg_solve
+ * for callers that cannot allocate device memory: a solver plug-in run from
+ * inside another library's solve (a PETSc shell preconditioner, say) whose
+ * device memory that library owns and pools, or a service that fixes its
+ * device footprint at start-up.  cudaMalloc and cudaFree also synchronize the
+ * whole device and stall the caller's other streams.  lmg_cg_solve allocates
+ * its work vectors on every call; this variant allocates nothing (no cudaMalloc,
+ * no cudaFree, no allocating library routine).  It runs the same kernels in the
+ * same reduction order, so it returns the same iterates, on caller-owned device
+ * arrays: row_ptr[n_dofs + 1], col_idx, val (the CSR of lmg_sparsity_copy /
+ * lmg_assemble), rhs[n_dofs], x[n_dofs] (output).  Its work vectors live in one
+ * fixed device array inside the library, 5 x LMG_CG_NOALLOC_MAX_DOFS doubles
+ * (20 MiB); n_dofs above LMG_CG_NOALLOC_MAX_DOFS returns LMG_ERR_ARG and says
+ * so in msg.  The first call on each device looks up that array's address on
+ * the current device (cudaGetSymbolAddress): make that first call before any
+ * stream capture.  Every call on a device shares the one array, so calls whose
+ * work overlaps on the GPU (other streams, other host threads) race and give
+ * wrong results: serialize them.  The scalar slots are cleared at the start of
+ * every call; every other word is written before it is read.  stream is a
+ * cudaStream_t (NULL = the legacy default stream); the call returns once the
+ * solve has finished on it.  msg (may be NULL) receives the error text. */
+#define LMG_CG_NOALLOC_MAX_DOFS 524288
+lmg_status lmg_cg_solve_noalloc(int64_t n_dofs, const int32_t *row_ptr, const int32_t *col_idx,
+                                const double *val, const double *rhs, double *x, double rtol,
+                                int32_t maxit, void *stream, int32_t *iters, double *relres,
+                                char *msg, int32_t msg_len);
+
 /* Adjoint sensitivities (ImplicitSystem::adjoint_qoi_parameter_sensitivity,
  * src/systems/implicit_system.C:517-623, with the element coefficients of the
  * form as parameters; ParameterVector, src/systems/parameter_vector.C:28-132).

@@ -18,6 +18,8 @@ TET4, TET10, HEX8, HEX27, PRISM6 = 8, 9, 10, 12, 13
 # forms and precisions
 POISSON, ELASTICITY = 0, 1
 FP64, MIXED = 0, 1
+# work-space limit of lmg_cg_solve_noalloc
+CG_NOALLOC_MAX_DOFS = 524288
 
 _p = C.c_void_p
 _i32, _i64, _u64, _f64 = C.c_int32, C.c_int64, C.c_uint64, C.c_double
@@ -47,6 +49,7 @@ SIGNATURES = {
     "lmg_synchronize": [_p],
     "lmg_last_error": [_p, _pi64, C.c_char_p, _i32],
     "lmg_cg_solve": [_p, _p, _p, _f64, _i32, _pi32, _pf64],
+    "lmg_cg_solve_noalloc": [_i64, _p, _p, _p, _p, _p, _f64, _i32, _p, _pi32, _pf64, C.c_char_p, _i32],
     "lmg_qoi_region_load": [_p, _p, _p],
     "lmg_vjp_coef": [_p, _p, _p, _p],
     "lmg_perflog_enable": [_p, _i32],

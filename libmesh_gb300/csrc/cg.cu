@@ -9,9 +9,12 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <cstdio>
+#include <mutex>
 #include <vector>
 
 #include "assemble.cuh"
+#include "../../include/libmesh_gb300.h"
 
 namespace lmg {
 
@@ -178,3 +181,111 @@ int cg_solve(int64_t n, const int32_t *rp, const int32_t *col, const double *val
 }
 
 }  // namespace lmg
+
+// ---------------------------------------------------------------------------
+// lmg_cg_solve_noalloc: the solve above on caller-owned device arrays, with
+// its work vectors in one fixed device array of this file instead of memory
+// from cudaMalloc.  Same kernels, same launch shapes, same reduction order,
+// so the iterates equal lmg_cg_solve's.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr int64_t NA_DOFS = LMG_CG_NOALLOC_MAX_DOFS;
+constexpr int NA_DEVICES = 64;
+
+// r, z, p, q, dinv (NA_DOFS each), the reduction partials (2 RBLK), the scalar slots (8).
+// Shared by every call on a device.
+static __device__ __align__(256) double g_cg_scratch[5 * NA_DOFS + 2 * lmg::RBLK + 8];
+
+std::mutex g_na_mutex;
+double *g_na_base[NA_DEVICES] = {};
+int g_na_sm[NA_DEVICES] = {};
+
+lmg_status na_fail(char *msg, int32_t len, lmg_status code, const char *text) {
+  if (msg && len > 0) std::snprintf(msg, (size_t)len, "%s", text);
+  return code;
+}
+
+// Once per device, with that device current: the array's device address.
+cudaError_t na_setup(int dev, double **base, int *n_sm) {
+  std::lock_guard<std::mutex> lock(g_na_mutex);
+  if (!g_na_base[dev]) {
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_cg_scratch);
+    if (e != cudaSuccess) return e;
+    int sm = 0;
+    e = cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    g_na_sm[dev] = sm;
+    g_na_base[dev] = static_cast<double *>(p);
+  }
+  *base = g_na_base[dev];
+  *n_sm = g_na_sm[dev];
+  return cudaSuccess;
+}
+
+}  // namespace
+
+extern "C" lmg_status lmg_cg_solve_noalloc(int64_t n, const int32_t *rp, const int32_t *col, const double *val,
+                                           const double *b, double *x, double rtol, int32_t maxit, void *stream,
+                                           int32_t *iters, double *relres, char *msg, int32_t msg_len) {
+  using namespace lmg;
+  na_fail(msg, msg_len, LMG_OK, "");
+  if (n <= 0 || !rp || !col || !val || !b || !x || !(rtol > 0.0) || maxit <= 0)
+    return na_fail(msg, msg_len, LMG_ERR_ARG, "cg_solve_noalloc: bad argument");
+  if (n > NA_DOFS) {
+    char t[160];
+    std::snprintf(t, sizeof t, "cg_solve_noalloc: n_dofs = %lld exceeds the fixed work space of %lld dofs",
+                  (long long)n, (long long)NA_DOFS);
+    return na_fail(msg, msg_len, LMG_ERR_ARG, t);
+  }
+  int dev = 0, n_sm = 0;
+  double *base = nullptr;
+  if (cudaGetDevice(&dev) != cudaSuccess) return na_fail(msg, msg_len, LMG_ERR_CUDA, "cg_solve_noalloc: no device");
+  if (dev >= NA_DEVICES) return na_fail(msg, msg_len, LMG_ERR_ARG, "cg_solve_noalloc: device ordinal too large");
+  if (na_setup(dev, &base, &n_sm) != cudaSuccess)
+    return na_fail(msg, msg_len, LMG_ERR_CUDA, "cg_solve_noalloc: cudaGetSymbolAddress of the work space failed");
+  double *r = base, *z = base + NA_DOFS, *p = base + 2 * NA_DOFS, *q = base + 3 * NA_DOFS,
+         *dinv = base + 4 * NA_DOFS, *partial = base + 5 * NA_DOFS, *sc = partial + 2 * RBLK;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  // The scalar slots start every call at zero; every other word is written before it is read.
+  if (cudaMemsetAsync(sc, 0, sizeof(double) * 8, s) != cudaSuccess)
+    return na_fail(msg, msg_len, LMG_ERR_CUDA, "cg_solve_noalloc: clearing the scalar slots failed");
+  const int g1 = n_sm * 8, gs = n_sm * 16;
+  const int nblk = (int)std::min<int64_t>(RBLK, (n + RT - 1) / RT);
+  k_diag_inv<<<g1, 256, 0, s>>>(n, rp, col, val, dinv);
+  k_init<<<g1, 256, 0, s>>>(n, b, x, r, z, p, dinv);
+  k_dot2<<<nblk, RT, 0, s>>>(n, r, z, r, r, partial);
+  k_dot2_final<<<1, RT, 0, s>>>(nblk, partial, sc);  // sc[0] = rz, sc[1] = rr
+  double h[2] = {0.0, 0.0};
+  if (cudaMemcpyAsync(h, sc, sizeof(double) * 2, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess)
+    return na_fail(msg, msg_len, LMG_ERR_CUDA, "cg_solve_noalloc: device failure");
+  const double bnorm = std::sqrt(h[1]);
+  double rn = bnorm;
+  int it = 0;
+  if (bnorm > 0.0) {
+    for (it = 0; it < maxit; ++it) {
+      k_spmv<<<gs, 256, 0, s>>>(n, rp, col, val, p, q);
+      k_dot2<<<nblk, RT, 0, s>>>(n, p, q, nullptr, nullptr, partial);
+      k_dot2_final<<<1, RT, 0, s>>>(nblk, partial, sc + 2);  // sc[2] = pq
+      k_update_xr<<<g1, 256, 0, s>>>(n, sc, x, r, z, p, q, dinv);
+      k_dot2<<<nblk, RT, 0, s>>>(n, r, z, r, r, partial);
+      k_dot2_final<<<1, RT, 0, s>>>(nblk, partial, sc + 3);  // sc[3] = rz_new, sc[4] = rr
+      k_update_p<<<g1, 256, 0, s>>>(n, sc, p, z);
+      k_copy2<<<1, 1, 0, s>>>(sc, sc + 3);                   // rz <- rz_new
+      if ((it + 1) % 16 == 0 || it + 1 == maxit) {
+        if (cudaMemcpyAsync(h, sc + 4, sizeof(double), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+            cudaStreamSynchronize(s) != cudaSuccess)
+          return na_fail(msg, msg_len, LMG_ERR_CUDA, "cg_solve_noalloc: device failure");
+        rn = std::sqrt(h[0]);
+        if (!(rn > rtol * bnorm)) { ++it; break; }
+      }
+    }
+  }
+  if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(s) != cudaSuccess)
+    return na_fail(msg, msg_len, LMG_ERR_CUDA, "cg_solve_noalloc: device failure");
+  if (iters) *iters = it;
+  if (relres) *relres = bnorm > 0.0 ? rn / bnorm : 0.0;
+  return LMG_OK;
+}
