@@ -58,8 +58,11 @@ enum { LMG_TET4 = 8, LMG_TET10 = 9, LMG_HEX8 = 10, LMG_HEX27 = 12, LMG_PRISM6 = 
  *   LMG_POISSON    Ke += k_e JxW dphi_i.dphi_j, Fe += JxW f phi_i
  *                  (examples/introduction/introduction_ex4/introduction_ex4.C:467,536)
  *   LMG_ELASTICITY Ke_var[i][k] += JxW C_ijkl(E_e, nu) dphi_b(l) dphi_a(j), Fe_var[i] += JxW f_i phi_a
- *                  (examples/systems_of_equations/systems_of_equations_ex6/systems_of_equations_ex6.C:136-230) */
-enum { LMG_POISSON = 0, LMG_ELASTICITY = 1 };
+ *                  (examples/systems_of_equations/systems_of_equations_ex6/systems_of_equations_ex6.C:136-230)
+ *   LMG_ADVDIFF    Ke += JxW [(b . dphi_j) phi_i + kappa k_e dphi_i.dphi_j], Fe += JxW f phi_i, the
+ *                  steady Galerkin convection-diffusion of examples/adaptivity/adaptivity_ex2/adaptivity_ex2.C:660-690
+ *                  with b = curl of psi = sum_m a_m sin(k_m . x + phase_m) */
+enum { LMG_POISSON = 0, LMG_ELASTICITY = 1, LMG_ADVDIFF = 2 };
 
 /* Arithmetic of the element contraction.  LMG_FP64 is the drop-in (matches
  * libMesh to 1e-13 per entry).  LMG_MIXED keeps Jacobians, the global
@@ -116,6 +119,45 @@ lmg_status lmg_host_sparsity(int64_t n_elem, int32_t npe, int32_t n_vars, int64_
                              const int32_t *elem_dofs, int64_t *nnz, int32_t *row_ptr,
                              int32_t *col_idx);
 
+/* h-refinement of an unjittered HEX8 / HEX27 build_cube mesh
+ * (MeshRefinement::refine_and_coarsen_elements, src/mesh/mesh_refinement.C:482-786;
+ * Elem::refine, src/geom/elem_refinement.C:87-150): `cycles` rounds, each
+ * flagging floor(fraction * n_active) distinct active elements drawn from a
+ * splitmix64 stream seeded with `seed`, then flagging every coarser face
+ * neighbor of a flagged element until the level-one rule holds, then refining
+ * (children appended in parent id order, new nodes by the embedding matrices,
+ * nodes renumbered first-touch over all elements as
+ * ReplicatedMesh::renumber_nodes_and_elements does).  Afterwards the mesh
+ * holds the active elements in id order (lmg_mesh_info / lmg_mesh_copy). */
+lmg_status lmg_mesh_refine(lmg_mesh *m, int32_t cycles, double fraction, uint64_t seed);
+/* The refinement tree: every element ever created (all_conn [n_all][npe],
+ * parent id or -1, level) and the ids of the active elements (active_ids
+ * [n_elem], the rows of lmg_mesh_copy's conn).  NULL arrays are skipped. */
+lmg_status lmg_mesh_tree(const lmg_mesh *m, int64_t *n_all, int32_t *all_conn, int32_t *parent,
+                         int8_t *level, int32_t *active_ids);
+
+/* DofMap::create_dof_constraints + process_constraints for LAGRANGE variables
+ * on the active mesh (src/base/dof_map_constraints.C:1736-1895, 4341-4490):
+ * hanging-node rows (lagrange_compute_constraints, src/fe/fe_lagrange.C:867-1063:
+ * coefficient = parent-side shape at the hanging node, kept when
+ * 1e-5 < |c| < 0.999), then empty rows for the dofs flagged in dirichlet[n_dofs]
+ * that are still free (AddPrimalConstraint), then chains substituted until
+ * every row refers to free dofs.  Output: constrained[n_dofs] 0/1 and the rows
+ * as CSR over all dofs: cons_ptr[n_dofs+1], cons_col / cons_val ascending per
+ * row.  Call with cons_col = cons_val = NULL to get cons_ptr only (the size is
+ * cons_ptr[n_dofs]); cap is the capacity of cons_col / cons_val. */
+lmg_status lmg_constraint_rows(const lmg_mesh *m, int32_t n_vars, const int32_t *elem_dofs,
+                               int64_t n_dofs, const uint8_t *dirichlet, uint8_t *constrained,
+                               int64_t *cons_ptr, int32_t *cons_col, double *cons_val, int64_t cap);
+
+/* DofMap::compute_sparsity with constraints (find_connected_dofs,
+ * src/base/dof_map.C:2915-2970): every element couples the union of its dofs
+ * and of the dofs that constrain them.  elem_dofs [n_elem][dofs_per_elem]. */
+lmg_status lmg_host_sparsity_constrained(int64_t n_elem, int32_t dofs_per_elem, int64_t n_dofs,
+                                         const int32_t *elem_dofs, const int64_t *cons_ptr,
+                                         const int32_t *cons_col, int64_t *nnz, int32_t *row_ptr,
+                                         int32_t *col_idx);
+
 /* ------------------------------------------------------------------------- */
 /* Device context: the assembly drop-in.                                     */
 /* ------------------------------------------------------------------------- */
@@ -140,13 +182,27 @@ lmg_status lmg_dofmap_upload(lmg_ctx *ctx, int32_t n_vars, int64_t n_dofs,
  * Dirichlet), as DofMap::_dof_constraints holds them. constrained[n_dofs]. */
 lmg_status lmg_constraints_upload(lmg_ctx *ctx, const uint8_t *constrained);
 
+/* Constraint rows with coefficients (hanging nodes; DofMap::_dof_constraints
+ * after process_constraints, e.g. from lmg_constraint_rows): constrained[n_dofs]
+ * and the rows as CSR over all dofs, cons_ptr[n_dofs+1], cons_col / cons_val
+ * ascending per row, empty rows for Dirichlet dofs; every row must refer to
+ * free dofs only.  The assembly then applies constrain_element_matrix_and_vector
+ * in full (C^T K C on the element's dofs plus its constraining dofs,
+ * asymmetric constraint rows; src/base/dof_map_constraints.C:2439-2515,
+ * 3433-3540) and lmg_sparsity_build adds the constraint couplings
+ * (find_connected_dofs).  That path takes one variable, affine elements and
+ * LMG_FP64; lmg_constraints_upload drops the rows again. */
+lmg_status lmg_constraint_rows_upload(lmg_ctx *ctx, const uint8_t *constrained, const int64_t *cons_ptr,
+                                      const int32_t *cons_col, const double *cons_val);
+
 /* DofMap::compute_sparsity: PETSc-AIJ CSR (sorted column indices per row). */
 lmg_status lmg_sparsity_build(lmg_ctx *ctx, int64_t *nnz);
 lmg_status lmg_sparsity_copy(lmg_ctx *ctx, int32_t *row_ptr, int32_t *col_idx);
 
 /* Weak form and its data.  fe_order: 1 FIRST / 2 SECOND LAGRANGE.
  * q_order: QGauss order (libMesh Order value).  params: POISSON none;
- * ELASTICITY {nu}.  elem_coef[n_elem]: k_e (POISSON) or E_e (ELASTICITY),
+ * ELASTICITY {nu}; ADVDIFF {kappa, n_modes, then per mode a[3], k[3], phase}
+ * (one variable, affine elements, LMG_FP64).  elem_coef[n_elem]: k_e (POISSON) or E_e (ELASTICITY),
  * NULL = 1.  nodal_f[n_nodes][n_vars]: load interpolated with phi, NULL = 0. */
 lmg_status lmg_form_set(lmg_ctx *ctx, int32_t form, int32_t fe_order, int32_t q_order,
                         const double *params, int32_t n_params,

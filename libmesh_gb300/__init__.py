@@ -14,13 +14,13 @@ import ctypes as C
 import numpy as np
 
 from . import _capi
-from ._capi import (ELASTICITY, FP64, HEX8, HEX27, MIXED, POISSON, PRISM6, TET4, TET10,
+from ._capi import (ADVDIFF, ELASTICITY, FP64, HEX8, HEX27, MIXED, POISSON, PRISM6, TET4, TET10,
                     DegenerateMap, LmgError, check, lib, ptr)
 
 FIRST, SECOND, THIRD, FOURTH, FIFTH = 1, 2, 3, 4, 5
 
 __all__ = ["Mesh", "DofMap", "GpuAssembly", "LinearImplicitSystem", "DegenerateMap", "LmgError",
-           "HEX8", "HEX27", "TET4", "TET10", "PRISM6", "POISSON", "ELASTICITY", "FP64", "MIXED",
+           "HEX8", "HEX27", "TET4", "TET10", "PRISM6", "POISSON", "ELASTICITY", "ADVDIFF", "FP64", "MIXED",
            "FIRST", "SECOND", "THIRD", "FOURTH", "FIFTH"]
 
 
@@ -42,22 +42,67 @@ class Mesh:
     def n_elem(self):
         return self.conn.shape[0]
 
+    _handle = None
+
+    @staticmethod
+    def _arrays(h):
+        L = lib()
+        nn, ne = C.c_int64(), C.c_int64()
+        et, npe, ns = C.c_int32(), C.c_int32(), C.c_int32()
+        check(L.lmg_mesh_info(h, C.byref(nn), C.byref(ne), C.byref(et), C.byref(npe), C.byref(ns)))
+        xyz = np.empty((nn.value, 3), np.float64)
+        conn = np.empty((ne.value, npe.value), np.int32)
+        sb = np.empty((ne.value, ns.value), np.int8)
+        check(L.lmg_mesh_copy(h, ptr(xyz), ptr(conn), ptr(sb)))
+        return xyz, conn, et.value, sb
+
     @classmethod
     def build_cube(cls, nx, ny, nz, elem_type=HEX8, jitter=0.0, seed=0):
         L = lib()
         h = C.c_void_p()
         check(L.lmg_mesh_cube(nx, ny, nz, elem_type, float(jitter), int(seed), C.byref(h)))
         try:
-            nn, ne = C.c_int64(), C.c_int64()
-            et, npe, ns = C.c_int32(), C.c_int32(), C.c_int32()
-            check(L.lmg_mesh_info(h, C.byref(nn), C.byref(ne), C.byref(et), C.byref(npe), C.byref(ns)))
-            xyz = np.empty((nn.value, 3), np.float64)
-            conn = np.empty((ne.value, npe.value), np.int32)
-            sb = np.empty((ne.value, ns.value), np.int8)
-            check(L.lmg_mesh_copy(h, ptr(xyz), ptr(conn), ptr(sb)))
+            xyz, conn, et, sb = cls._arrays(h)
         finally:
             L.lmg_mesh_free(h)
-        return cls(xyz, conn, et.value, sb)
+        return cls(xyz, conn, et, sb)
+
+    @classmethod
+    def build_refined_cube(cls, n, elem_type, cycles, fraction, seed):
+        """build_cube(n,n,n) followed by `cycles` rounds of random h-refinement
+        (MeshRefinement with the level-one rule); the mesh keeps its native
+        refinement tree for the hanging-node constraints."""
+        L = lib()
+        h = C.c_void_p()
+        check(L.lmg_mesh_cube(n, n, n, elem_type, 0.0, 0, C.byref(h)))
+        try:
+            check(L.lmg_mesh_refine(h, int(cycles), float(fraction), int(seed)))
+            xyz, conn, et, sb = cls._arrays(h)
+        except Exception:
+            L.lmg_mesh_free(h)
+            raise
+        m = cls(xyz, conn, et, sb)
+        m._handle = h
+        return m
+
+    def tree(self):
+        """(all_conn, parent, level, active_ids) of the refinement tree."""
+        assert self._handle is not None
+        L = lib()
+        n = C.c_int64()
+        check(L.lmg_mesh_tree(self._handle, C.byref(n), None, None, None, None))
+        npe = self.conn.shape[1]
+        all_conn = np.empty((n.value, npe), np.int32)
+        parent = np.empty(n.value, np.int32)
+        level = np.empty(n.value, np.int8)
+        act = np.empty(self.n_elem, np.int32)
+        check(L.lmg_mesh_tree(self._handle, C.byref(n), ptr(all_conn), ptr(parent), ptr(level), ptr(act)))
+        return all_conn, parent, level, act
+
+    def __del__(self):
+        if self._handle is not None:
+            lib().lmg_mesh_free(self._handle)
+            self._handle = None
 
 
 class DofMap:
@@ -96,13 +141,45 @@ class DofMap:
     def is_constrained_dof(self, d):
         return bool(self.constrained[d])
 
+    cons_ptr = cons_col = cons_val = None
+
+    def create_dof_constraints(self):
+        """DofMap::create_dof_constraints + process_constraints: hanging-node
+        rows of a refined mesh, then empty rows for the Dirichlet dofs still
+        free, chains substituted.  Sets constrained and the rows (CSR over all
+        dofs: cons_ptr, cons_col, cons_val)."""
+        L = lib()
+        h = self.mesh._handle
+        owned = h is None
+        if owned:  # an unrefined mesh has no hanging nodes: rebuild a handle-free result
+            self.cons_ptr = np.zeros(self.n_dofs + 1, np.int64)
+            self.cons_ptr[1:] = 0
+            self.cons_col = np.zeros(0, np.int32)
+            self.cons_val = np.zeros(0, np.float64)
+            return
+        dirichlet = self.constrained.copy()
+        cons = np.zeros(self.n_dofs, np.uint8)
+        cp = np.zeros(self.n_dofs + 1, np.int64)
+        check(L.lmg_constraint_rows(h, self.n_vars, ptr(self.elem_dofs), self.n_dofs, ptr(dirichlet), ptr(cons),
+                                    ptr(cp), None, None, 0))
+        total = int(cp[-1])
+        col = np.zeros(max(total, 1), np.int32)
+        val = np.zeros(max(total, 1), np.float64)
+        check(L.lmg_constraint_rows(h, self.n_vars, ptr(self.elem_dofs), self.n_dofs, ptr(dirichlet), ptr(cons),
+                                    ptr(cp), ptr(col), ptr(val), total))
+        self.constrained = cons
+        self.cons_ptr, self.cons_col, self.cons_val = cp, col[:total], val[:total]
+
 
 class GpuAssembly:
     """System::Assembly replacement: one device context per system holding the
     mesh, dof map, constraints, sparsity, scatter plan and form data."""
 
-    def __init__(self, form, fe_order, q_order, elem_coef=None, nodal_f=None, nu=0.3, device=0):
+    def __init__(self, form, fe_order, q_order, elem_coef=None, nodal_f=None, nu=0.3, device=0, params=None):
+        """params: the form's parameter list when it has more than nu (ADVDIFF:
+        {kappa, n_modes, then per mode a[3], k[3], phase})."""
         self.form, self.fe_order, self.q_order = int(form), int(fe_order), int(q_order)
+        self.params = None if params is None else np.ascontiguousarray(params, np.float64)
         self.elem_coef = None if elem_coef is None else np.ascontiguousarray(elem_coef, np.float64)
         self.nodal_f = None if nodal_f is None else np.ascontiguousarray(nodal_f, np.float64)
         self.nu = float(nu)
@@ -123,12 +200,16 @@ class GpuAssembly:
         self._ok(L.lmg_mesh_upload(self.ctx, mesh.n_nodes, ptr(mesh.xyz), mesh.n_elem, mesh.elem_type,
                                    ptr(mesh.conn)))
         self._ok(L.lmg_dofmap_upload(self.ctx, dof_map.n_vars, dof_map.n_dofs, ptr(dof_map.elem_dofs)))
-        self._ok(L.lmg_constraints_upload(self.ctx, ptr(dof_map.constrained)))
+        if dof_map.cons_ptr is not None and len(dof_map.cons_col):
+            self._ok(L.lmg_constraint_rows_upload(self.ctx, ptr(dof_map.constrained), ptr(dof_map.cons_ptr),
+                                                  ptr(dof_map.cons_col), ptr(dof_map.cons_val)))
+        else:
+            self._ok(L.lmg_constraints_upload(self.ctx, ptr(dof_map.constrained)))
         nnz = C.c_int64()
         self._ok(L.lmg_sparsity_build(self.ctx, C.byref(nnz)))
         self.nnz = nnz.value
-        params = np.array([self.nu], np.float64)
-        self._ok(L.lmg_form_set(self.ctx, self.form, self.fe_order, self.q_order, ptr(params), 1,
+        params = np.array([self.nu], np.float64) if self.params is None else self.params
+        self._ok(L.lmg_form_set(self.ctx, self.form, self.fe_order, self.q_order, ptr(params), len(params),
                                 ptr(self.elem_coef), ptr(self.nodal_f)))
 
     def sparsity(self):

@@ -16,7 +16,7 @@ STATUS_NAMES = {0: "OK", 1: "ERR_ARG", 2: "ERR_CUDA", 3: "ERR_STATE", 4: "ERR_DE
 # element types (libMesh ElemType values)
 TET4, TET10, HEX8, HEX27, PRISM6 = 8, 9, 10, 12, 13
 # forms and precisions
-POISSON, ELASTICITY = 0, 1
+POISSON, ELASTICITY, ADVDIFF = 0, 1, 2
 FP64, MIXED = 0, 1
 # work-space limit of lmg_cg_solve_noalloc
 CG_NOALLOC_MAX_DOFS = 524288
@@ -34,12 +34,17 @@ SIGNATURES = {
     "lmg_dofmap_distribute": [_i64, _i64, _i32, _p, _i32, _pi64, _p],
     "lmg_dirichlet_dofs": [_i64, _i32, _i32, _p, _p, _p, _i32, _p, _i32, _i64, _p],
     "lmg_host_sparsity": [_i64, _i32, _i32, _i64, _p, _pi64, _p, _p],
+    "lmg_mesh_refine": [_p, _i32, _f64, _u64],
+    "lmg_mesh_tree": [_p, _pi64, _p, _p, _p, _p],
+    "lmg_constraint_rows": [_p, _i32, _p, _i64, _p, _p, _p, _p, _p, _i64],
+    "lmg_host_sparsity_constrained": [_i64, _i32, _i64, _p, _p, _p, _pi64, _p, _p],
     "lmg_context_create": [C.POINTER(_p), _i32],
     "lmg_context_destroy": [_p],
     "lmg_context_set_stream": [_p, _p],
     "lmg_mesh_upload": [_p, _i64, _p, _i64, _i32, _p],
     "lmg_dofmap_upload": [_p, _i32, _i64, _p],
     "lmg_constraints_upload": [_p, _p],
+    "lmg_constraint_rows_upload": [_p, _p, _p, _p, _p],
     "lmg_sparsity_build": [_p, _pi64],
     "lmg_sparsity_copy": [_p, _p, _p],
     "lmg_form_set": [_p, _i32, _i32, _i32, _p, _i32, _p, _p],

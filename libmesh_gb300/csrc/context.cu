@@ -10,104 +10,12 @@
 #include <thread>
 #include <vector>
 
-#include "assemble.cuh"
-#include "lmg_internal.h"
+#include "context_internal.cuh"
+#include "general.cuh"
 
 using namespace lmg;
 
-struct lmg_ctx {
-  int device = 0;
-  cudaStream_t stream = nullptr;
-  bool own_stream = false;
-  int n_sm = 152;
-  int64_t launches = 0;
-  std::string err;
-  int64_t err_elem = -1;
-  // mesh
-  int elem_type = 0, npe = 0;
-  int64_t n_nodes = 0, n_elem = 0;
-  std::vector<double> h_xyz;
-  std::vector<int32_t> h_conn;
-  double *d_xyz = nullptr;
-  int32_t *d_conn = nullptr;
-  std::vector<int32_t> h_aff, h_gen;  // affine / general element lists
-  int32_t *d_aff = nullptr, *d_gen = nullptr;
-  // dofmap
-  int n_vars = 0, nl = 0, bs = 1, nb = 0;
-  int64_t n_dofs = 0, n_blocks = 0;
-  std::vector<int32_t> h_elem_dofs, h_eb;
-  int32_t *d_eb = nullptr;
-  // constraints
-  std::vector<uint8_t> h_constrained;
-  uint64_t *d_cmask = nullptr;
-  uint8_t *d_cons = nullptr;
-  // sparsity and plan
-  bool have_sparsity = false;
-  int64_t nnz = 0, nnzb = 0;
-  int64_t *d_brow_ptr = nullptr;
-  int32_t *d_bcol = nullptr, *d_row_ptr = nullptr, *d_col = nullptr, *d_tslot = nullptr;
-  int32_t *d_bptr = nullptr, *d_bcontrib = nullptr, *d_fptr = nullptr, *d_fcontrib = nullptr;
-  // form
-  bool have_form = false;
-  int form = 0, fe_order = 0, q_order = 0;
-  double nu = 0.3;
-  FETables tab;
-  double *d_tab = nullptr;
-  DevFE dfe{};
-  double *d_coef = nullptr, *d_f = nullptr;
-  float2 *d_f2 = nullptr;  // nodal load as double-float pairs
-  // work and result buffers
-  float2 *d_Kdiag2 = nullptr, *d_Koff2 = nullptr;
-  float2 *d_Fe2 = nullptr;
-  double *d_K = nullptr, *d_F = nullptr;
-  float *d_Koff32 = nullptr;
-  int *d_status = nullptr;
-  unsigned long long *d_bad = nullptr;
-  // PerfLog-style stage timing (CUDA events on the context stream)
-  bool perflog = false;
-  std::vector<cudaEvent_t> ev;       // 3 per logged assemble call
-  double log_ms[2] = {0.0, 0.0};     // element kernels, gather
-  int64_t log_calls = 0;
-};
-
 namespace {
-
-template <typename T>
-void dfree(T *&p) {
-  if (p) cudaFree((void *)p);
-  p = nullptr;
-}
-
-lmg_status fail(lmg_ctx *c, lmg_status code, const std::string &msg, int64_t elem = -1) {
-  if (c) {
-    c->err = msg;
-    c->err_elem = elem;
-  }
-  return code;
-}
-
-#define LMG_CUDA(ctx, call)                                                        \
-  do {                                                                             \
-    cudaError_t e_ = (call);                                                       \
-    if (e_ != cudaSuccess)                                                         \
-      return fail(ctx, e_ == cudaErrorMemoryAllocation ? LMG_ERR_OOM : LMG_ERR_CUDA, \
-                  std::string(#call) + ": " + cudaGetErrorString(e_));             \
-  } while (0)
-
-template <typename T>
-cudaError_t dalloc(T *&p, size_t n) {
-  dfree(p);
-  if (n == 0) n = 1;
-  return cudaMalloc((void **)&p, n * sizeof(T));
-}
-
-template <typename T>
-cudaError_t dupload(lmg_ctx *c, T *&p, const T *h, size_t n) {
-  cudaError_t e = dalloc(p, n);
-  if (e != cudaSuccess) return e;
-  if (n) e = cudaMemcpyAsync(p, h, n * sizeof(T), cudaMemcpyHostToDevice, c->stream);
-  return e;
-}
 
 // ---------------------------------------------------------------- kernels
 __global__ void k_expand_cols(int64_t n_dofs, int bs, const int64_t *brow_ptr, const int32_t *bcol,
@@ -438,6 +346,8 @@ lmg_status lmg_context_destroy(lmg_ctx *c) {
   dfree(c->d_bptr); dfree(c->d_bcontrib); dfree(c->d_fptr); dfree(c->d_fcontrib); dfree(c->d_tab);
   dfree(c->d_coef); dfree(c->d_f); dfree(c->d_f2); dfree(c->d_Kdiag2); dfree(c->d_Koff2); dfree(c->d_Fe2); dfree(c->d_K);
   dfree(c->d_F); dfree(c->d_Koff32); dfree(c->d_status); dfree(c->d_bad);
+  general_free(c);
+  dfree(c->d_D6); dfree(c->d_modes);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
   delete c;
   return LMG_OK;
@@ -494,7 +404,12 @@ lmg_status lmg_dofmap_upload(lmg_ctx *c, int32_t n_vars, int64_t n_dofs, const i
   detect_blocks(c);
   LMG_CUDA(c, dupload(c, c->d_eb, c->h_eb.data(), c->h_eb.size()));
   c->h_constrained.clear();
+  c->h_cons_ptr.clear();
+  c->h_cons_col.clear();
+  c->h_cons_val.clear();
+  c->has_rows = false;
   c->have_sparsity = false;
+  c->gen_plan = false;
   return upload_cmask(c);
 }
 
@@ -503,6 +418,12 @@ lmg_status lmg_constraints_upload(lmg_ctx *c, const uint8_t *constrained) {
   if (!c->n_dofs) return fail(c, LMG_ERR_STATE, "constraints_upload: upload the dofmap first");
   cudaSetDevice(c->device);
   c->h_constrained.assign(constrained, constrained + c->n_dofs);
+  if (c->has_rows) c->have_sparsity = false;  // the pattern loses the constraint couplings
+  c->h_cons_ptr.clear();
+  c->h_cons_col.clear();
+  c->h_cons_val.clear();
+  c->has_rows = false;
+  c->gen_plan = false;
   return upload_cmask(c);
 }
 
@@ -510,6 +431,17 @@ lmg_status lmg_sparsity_build(lmg_ctx *c, int64_t *nnz) {
   if (!c) return LMG_ERR_ARG;
   if (!c->n_dofs) return fail(c, LMG_ERR_STATE, "sparsity_build: upload the dofmap first");
   cudaSetDevice(c->device);
+  c->gen_plan = false;
+  c->h_row_ptr.clear();
+  c->h_col.clear();
+  c->general = c->has_rows || (c->have_form && c->form == LMG_ADVDIFF);
+  if (c->general) {  // constraint rows with coefficients: find_connected_dofs pattern
+    lmg_status st = general_sparsity(c);
+    if (st) return st;
+    c->have_sparsity = true;
+    if (nnz) *nnz = c->nnz;
+    return LMG_OK;
+  }
   std::vector<int64_t> brow;
   std::vector<int32_t> bcol;
   const unsigned hw = std::thread::hardware_concurrency();
@@ -571,9 +503,17 @@ lmg_status lmg_form_set(lmg_ctx *c, int32_t form, int32_t fe_order, int32_t q_or
                         const double *nodal_f) {
   if (!c) return LMG_ERR_ARG;
   if (!c->n_dofs) return fail(c, LMG_ERR_STATE, "form_set: upload the dofmap first");
-  if (form != LMG_POISSON && form != LMG_ELASTICITY) return fail(c, LMG_ERR_ARG, "form_set: unknown form");
-  if ((form == LMG_POISSON && c->n_vars != 1) || (form == LMG_ELASTICITY && c->n_vars != 3))
+  if (form != LMG_POISSON && form != LMG_ELASTICITY && form != LMG_ADVDIFF)
+    return fail(c, LMG_ERR_ARG, "form_set: unknown form");
+  if ((form != LMG_ELASTICITY && c->n_vars != 1) || (form == LMG_ELASTICITY && c->n_vars != 3))
     return fail(c, LMG_ERR_ARG, "form_set: variable count does not match the form");
+  int n_modes = 0;
+  if (form == LMG_ADVDIFF) {
+    if (!params || n_params < 2) return fail(c, LMG_ERR_ARG, "form_set: ADVDIFF needs {kappa, n_modes, modes}");
+    n_modes = (int)params[1];
+    if (n_modes < 0 || n_modes > GEN_MAX_MODES || n_params != 2 + 7 * n_modes)
+      return fail(c, LMG_ERR_ARG, "form_set: ADVDIFF parameter count does not match n_modes");
+  }
   cudaSetDevice(c->device);
   FETables t;
   std::string err = build_fe_tables(t, c->elem_type, fe_order, q_order);
@@ -581,10 +521,37 @@ lmg_status lmg_form_set(lmg_ctx *c, int32_t form, int32_t fe_order, int32_t q_or
   if (t.n != c->npe || t.n_geo != c->npe)
     return fail(c, LMG_ERR_UNSUPPORTED, "form_set: only isoparametric LAGRANGE elements are built");
   if (t.q > 27) return fail(c, LMG_ERR_UNSUPPORTED, "form_set: more than 27 quadrature points");
-  if (c->bs != c->n_vars)
-    return fail(c, LMG_ERR_UNSUPPORTED, "form_set: variables must be node-interleaved (one VariableGroup)");
-  if (!elements_built(form, t.n, c->n_vars))
-    return fail(c, LMG_ERR_UNSUPPORTED, "form_set: no element kernel for this form / element");
+  const bool general = c->has_rows || form == LMG_ADVDIFF;
+  if (general) {
+    if (!gen_elements_built(form, t.n, t.q))
+      return fail(c, LMG_ERR_UNSUPPORTED, "form_set: no general-path kernel for this form / element / rule");
+    if (!c->h_gen.empty())
+      return fail(c, LMG_ERR_UNSUPPORTED, "form_set: the constrained / convection path takes affine elements only");
+  } else {
+    if (c->bs != c->n_vars)
+      return fail(c, LMG_ERR_UNSUPPORTED, "form_set: variables must be node-interleaved (one VariableGroup)");
+    if (!elements_built(form, t.n, c->n_vars))
+      return fail(c, LMG_ERR_UNSUPPORTED, "form_set: no element kernel for this form / element");
+  }
+  if (c->n_vars == 1) {  // symmetrized reference tensors of the general path
+    const int n = t.n;
+    std::vector<double> D((size_t)6 * n * n);
+    auto S = [&](int m, int k, int a, int b) { return t.S[(((size_t)(3 * m + k) * n) + a) * n + b]; };
+    const int pm[6][2] = {{0, 0}, {1, 1}, {2, 2}, {0, 1}, {0, 2}, {1, 2}};
+    for (int k = 0; k < 6; ++k)
+      for (int a = 0; a < n; ++a)
+        for (int b = 0; b < n; ++b) {
+          const int m0 = pm[k][0], m1 = pm[k][1];
+          D[((size_t)k * n + a) * n + b] = (m0 == m1) ? S(m0, m0, a, b) : S(m0, m1, a, b) + S(m1, m0, a, b);
+        }
+    LMG_CUDA(c, dupload(c, c->d_D6, D.data(), D.size()));
+  }
+  c->kappa = form == LMG_ADVDIFF ? params[0] : 0.0;
+  c->n_modes = n_modes;
+  dfree(c->d_modes);
+  if (n_modes) LMG_CUDA(c, dupload(c, c->d_modes, params + 2, (size_t)(7 * n_modes)));
+  if (general != c->general) c->gen_plan = false;
+  c->general = general;
   c->tab = t;
   c->form = form;
   c->fe_order = fe_order;
@@ -651,6 +618,32 @@ lmg_status lmg_assemble(lmg_ctx *c, int32_t precision, double *K, double *F, int
   if (!c->have_form) return fail(c, LMG_ERR_STATE, "assemble: set the form first");
   if (precision != LMG_FP64 && precision != LMG_MIXED) return fail(c, LMG_ERR_ARG, "assemble: unknown precision");
   cudaSetDevice(c->device);
+  if (c->general) {
+    if (precision != LMG_FP64)
+      return fail(c, LMG_ERR_UNSUPPORTED, "assemble: the constrained / convection path computes in FP64 only");
+    if (!c->gen_plan) {
+      lmg_status st = general_plan(c);
+      if (st) return st;
+    }
+    lmg_status st = reset_status(c);
+    if (st) return st;
+    cudaEvent_t e3[3] = {nullptr, nullptr, nullptr};
+    if (c->perflog) {
+      for (auto &e : e3) LMG_CUDA(c, cudaEventCreate(&e));
+      for (auto &e : e3) c->ev.push_back(e);
+      LMG_CUDA(c, cudaEventRecord(e3[0], c->stream));
+    }
+    general_assemble(c);
+    if (c->perflog) LMG_CUDA(c, cudaEventRecord(e3[1], c->stream));
+    general_gather(c);
+    if (c->perflog) LMG_CUDA(c, cudaEventRecord(e3[2], c->stream));
+    LMG_CUDA(c, cudaGetLastError());
+    const cudaMemcpyKind kind = out_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    if (K) LMG_CUDA(c, cudaMemcpyAsync(K, c->d_K, sizeof(double) * c->nnz, kind, c->stream));
+    if (F) LMG_CUDA(c, cudaMemcpyAsync(F, c->d_F, sizeof(double) * c->n_dofs, kind, c->stream));
+    if (out_on_device || (!K && !F)) return LMG_OK;
+    return check_status(c, "assemble");
+  }
   const bool mixed = precision == LMG_MIXED;
   if (mixed && !c->d_Koff32)
     LMG_CUDA(c, dalloc(c->d_Koff32, (size_t)c->n_elem * c->nb * (c->nb - 1) / 2 * c->bs * c->bs));
@@ -765,6 +758,8 @@ VjpArgs vjp_args(lmg_ctx *c) {
 }  // namespace
 
 lmg_status lmg_qoi_region_load(lmg_ctx *c, const uint8_t *in_region, double *q) {
+  if (c && c->general)
+    return fail(c, LMG_ERR_UNSUPPORTED, "adjoint sensitivities are built for the unconstrained symmetric forms");
   if (!c || !in_region || !q) return fail(c, LMG_ERR_ARG, "qoi_region_load: bad argument");
   if (!c->have_sparsity || !c->have_form) return fail(c, LMG_ERR_STATE, "qoi_region_load: set up the system first");
   cudaSetDevice(c->device);
@@ -796,6 +791,8 @@ lmg_status lmg_qoi_region_load(lmg_ctx *c, const uint8_t *in_region, double *q) 
 }
 
 lmg_status lmg_vjp_coef(lmg_ctx *c, const double *u, const double *z, double *dq_dcoef) {
+  if (c && c->general)
+    return fail(c, LMG_ERR_UNSUPPORTED, "adjoint sensitivities are built for the unconstrained symmetric forms");
   if (!c || !u || !z || !dq_dcoef) return fail(c, LMG_ERR_ARG, "vjp_coef: bad argument");
   if (!c->have_sparsity || !c->have_form) return fail(c, LMG_ERR_STATE, "vjp_coef: set up the system first");
   cudaSetDevice(c->device);

@@ -1,0 +1,135 @@
+// Internal state of the device context (shared by context.cu and
+// context_general.cu).  Not part of the C ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "assemble.cuh"
+#include "lmg_internal.h"
+
+struct lmg_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  int n_sm = 152;
+  int64_t launches = 0;
+  std::string err;
+  int64_t err_elem = -1;
+  // mesh
+  int elem_type = 0, npe = 0;
+  int64_t n_nodes = 0, n_elem = 0;
+  std::vector<double> h_xyz;
+  std::vector<int32_t> h_conn;
+  double *d_xyz = nullptr;
+  int32_t *d_conn = nullptr;
+  std::vector<int32_t> h_aff, h_gen;  // affine / general element lists
+  int32_t *d_aff = nullptr, *d_gen = nullptr;
+  // dofmap
+  int n_vars = 0, nl = 0, bs = 1, nb = 0;
+  int64_t n_dofs = 0, n_blocks = 0;
+  std::vector<int32_t> h_elem_dofs, h_eb;
+  int32_t *d_eb = nullptr;
+  // constraints
+  std::vector<uint8_t> h_constrained;
+  uint64_t *d_cmask = nullptr;
+  uint8_t *d_cons = nullptr;
+  // sparsity and plan
+  bool have_sparsity = false;
+  int64_t nnz = 0, nnzb = 0;
+  int64_t *d_brow_ptr = nullptr;
+  int32_t *d_bcol = nullptr, *d_row_ptr = nullptr, *d_col = nullptr, *d_tslot = nullptr;
+  int32_t *d_bptr = nullptr, *d_bcontrib = nullptr, *d_fptr = nullptr, *d_fcontrib = nullptr;
+  // form
+  bool have_form = false;
+  int form = 0, fe_order = 0, q_order = 0;
+  double nu = 0.3;
+  lmg::FETables tab;
+  double *d_tab = nullptr;
+  lmg::DevFE dfe{};
+  double *d_coef = nullptr, *d_f = nullptr;
+  float2 *d_f2 = nullptr;  // nodal load as double-float pairs
+  // work and result buffers
+  float2 *d_Kdiag2 = nullptr, *d_Koff2 = nullptr;
+  float2 *d_Fe2 = nullptr;
+  double *d_K = nullptr, *d_F = nullptr;
+  float *d_Koff32 = nullptr;
+  int *d_status = nullptr;
+  unsigned long long *d_bad = nullptr;
+  // general path (general.cu): constraint rows with coefficients or a
+  // nonsymmetric form; full element matrices, C^T K C, slot gather
+  std::vector<int64_t> h_cons_ptr;   // [n_dofs+1] constraint rows (empty: none uploaded)
+  std::vector<int32_t> h_cons_col;
+  std::vector<double> h_cons_val;
+  bool has_rows = false;             // some row has coefficients
+  bool general = false;              // assembly runs through general.cu
+  bool gen_plan = false;
+  std::vector<int32_t> h_row_ptr, h_col;  // host copy of the CSR pattern
+  double kappa = 0.0;
+  int n_modes = 0;
+  double *d_D6 = nullptr, *d_modes = nullptr, *d_Ebuf = nullptr, *d_Fbuf = nullptr;
+  int64_t *d_cptr = nullptr, *d_gfptr = nullptr;
+  uint32_t *d_coff = nullptr, *d_gfoff = nullptr;
+  int64_t n_cons_elem = 0;
+  int32_t *d_celem = nullptr, *d_cne = nullptr, *d_ccp = nullptr;
+  int64_t *d_ckout = nullptr, *d_cfout = nullptr, *d_cbase = nullptr, *d_cebase = nullptr;
+  uint8_t *d_cci = nullptr;
+  double *d_ccv = nullptr;
+  uint64_t *d_crow = nullptr;
+  // PerfLog-style stage timing (CUDA events on the context stream)
+  bool perflog = false;
+  std::vector<cudaEvent_t> ev;       // 3 per logged assemble call
+  double log_ms[2] = {0.0, 0.0};     // element kernels, gather
+  int64_t log_calls = 0;
+};
+
+namespace lmg {
+
+
+template <typename T>
+inline void dfree(T *&p) {
+  if (p) cudaFree((void *)p);
+  p = nullptr;
+}
+
+inline lmg_status fail(lmg_ctx *c, lmg_status code, const std::string &msg, int64_t elem = -1) {
+  if (c) {
+    c->err = msg;
+    c->err_elem = elem;
+  }
+  return code;
+}
+
+#define LMG_CUDA(ctx, call)                                                        \
+  do {                                                                             \
+    cudaError_t e_ = (call);                                                       \
+    if (e_ != cudaSuccess)                                                         \
+      return fail(ctx, e_ == cudaErrorMemoryAllocation ? LMG_ERR_OOM : LMG_ERR_CUDA, \
+                  std::string(#call) + ": " + cudaGetErrorString(e_));             \
+  } while (0)
+
+template <typename T>
+inline cudaError_t dalloc(T *&p, size_t n) {
+  dfree(p);
+  if (n == 0) n = 1;
+  return cudaMalloc((void **)&p, n * sizeof(T));
+}
+
+template <typename T>
+inline cudaError_t dupload(lmg_ctx *c, T *&p, const T *h, size_t n) {
+  cudaError_t e = dalloc(p, n);
+  if (e != cudaSuccess) return e;
+  if (n) e = cudaMemcpyAsync(p, h, n * sizeof(T), cudaMemcpyHostToDevice, c->stream);
+  return e;
+}
+
+// general.cu path (context_general.cu)
+lmg_status general_sparsity(lmg_ctx *c);   // CSR with the constraint couplings
+lmg_status general_plan(lmg_ctx *c);       // constraint columns, slot plan, buffers
+lmg_status general_assemble(lmg_ctx *c);   // element and constraint kernels
+void general_gather(lmg_ctx *c);           // slot gather into K and F
+void general_free(lmg_ctx *c);             // plan and work buffers
+
+}  // namespace lmg

@@ -1,0 +1,295 @@
+// General scalar assembly path: full (nonsymmetric) element matrices, the
+// constraint product C^T K C for elements that touch constrained dofs, and a
+// deterministic gather into the CSR values.  Used for the convection-diffusion
+// form and for systems with constraint rows (hanging nodes).
+//
+//   element loop, FEBase::reinit, weak form     adaptivity_ex2.C:580-690 (steady part),
+//                                                introduction_ex4.C:440-540
+//   DofMap::constrain_element_matrix_and_vector  src/base/dof_map_constraints.C:2439-2515
+//   DofMap::build_constraint_matrix              src/base/dof_map_constraints.C:3433-3540
+//   SparseMatrix::add_matrix / add_vector        src/numerics/petsc_matrix.C:735-755
+//
+// Element kernel: one warp per element, lane b computes column b of Ke.
+// Affine elements only: the diffusion block is the reference-tensor
+// contraction K_ab = sum_k A_k D^k_ab (D = symmetrized sum_q w dphi_m dphi_n
+// tables), the convection block C_ab = sum_q phi_a(q) sum_m beta_m(q) dphi_m,b(q)
+// with beta_m(q) = w_q detJ (dxi_m/dx . b(x_q)).  All FP64.
+//
+// Constraint kernel: one CTA per constrained element.  K' = C^T K C over the
+// element's dofs followed by its constraining dofs (sorted), with C given by
+// its columns (row index, coefficient) in ascending row order, evaluated in
+// the reference's order: L_pj = sum_i C_ip K_ij, K'_pq = sum_j L_pj C_jq.
+// Constrained rows become e_i^T with -c_ij at their constraining dofs; F' = C^T F.
+#include <cuda_runtime.h>
+
+#include "general.cuh"
+#include "../../include/libmesh_gb300.h"
+
+namespace lmg {
+
+namespace {
+
+constexpr int WARPS = 8;
+
+__device__ __forceinline__ double warp_allsum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+template <int FORM, int N, int Q>
+__global__ void __launch_bounds__(WARPS * 32) k_elem_full(GenElemArgs a) {
+  extern __shared__ double sm[];
+  double *sphi = sm;                  // [Q][N]
+  double *sdphi = sphi + Q * N;       // [Q][N][3]
+  double *sD = sdphi + Q * N * 3;     // [6][N][N]
+  double *sqw = sD + 6 * N * N;       // [Q]
+  double *sgd = sqw + Q;              // [N][3] mapping derivatives at qp 0
+  double *smode = sgd + N * 3;        // [7 * n_modes]
+  double *wbase = smode + 7 * a.n_modes;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  double *sX = wbase + warp * (N * 3 + N + 4 * Q);  // [N][3]
+  double *sf = sX + N * 3;                            // [N]
+  double *sbeta = sf + N;                             // [Q][3]
+  double *sfq = sbeta + 3 * Q;                        // [Q]
+  for (int i = threadIdx.x; i < Q * N; i += blockDim.x) sphi[i] = a.fe.phi[i];
+  for (int i = threadIdx.x; i < Q * N * 3; i += blockDim.x) sdphi[i] = a.fe.dphi[i];
+  for (int i = threadIdx.x; i < 6 * N * N; i += blockDim.x) sD[i] = a.D6[i];
+  for (int i = threadIdx.x; i < Q; i += blockDim.x) sqw[i] = a.fe.qw[i];
+  for (int i = threadIdx.x; i < N * 3; i += blockDim.x) sgd[i] = a.fe.gdphi[i];
+  for (int i = threadIdx.x; i < 7 * a.n_modes; i += blockDim.x) smode[i] = a.modes[i];
+  __syncthreads();
+  const int64_t stride = (int64_t)gridDim.x * WARPS;
+  for (int64_t e = (int64_t)blockIdx.x * WARPS + warp; e < a.n_elem; e += stride) {
+    // geometry and nodal load of this element
+    double jp[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) jp[i] = 0.0;
+    if (lane < N) {
+      const int64_t nd = a.conn[e * N + lane];
+      const double x = a.xyz[3 * nd], y = a.xyz[3 * nd + 1], z = a.xyz[3 * nd + 2];
+      sX[3 * lane] = x;
+      sX[3 * lane + 1] = y;
+      sX[3 * lane + 2] = z;
+      sf[lane] = a.nodal_f ? a.nodal_f[nd] : 0.0;
+#pragma unroll
+      for (int m = 0; m < 3; ++m) {
+        const double g = sgd[3 * lane + m];
+        jp[3 * m + 0] = x * g;
+        jp[3 * m + 1] = y * g;
+        jp[3 * m + 2] = z * g;
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < 9; ++i) jp[i] = warp_allsum(jp[i]);
+    // jp[m*3+d] = d x_d / d xi_m; G[3m+d] = d xi_m / d x_d (fe_map.C:1046-1068)
+    const double c0 = jp[4] * jp[8] - jp[5] * jp[7], c1 = jp[5] * jp[6] - jp[3] * jp[8],
+                 c2 = jp[3] * jp[7] - jp[4] * jp[6];
+    const double det = jp[0] * c0 + jp[1] * c1 + jp[2] * c2;
+    const double inv = 1.0 / det;
+    double G[9];
+    G[0] = c0 * inv;
+    G[1] = c1 * inv;
+    G[2] = c2 * inv;
+    G[3] = (jp[2] * jp[7] - jp[1] * jp[8]) * inv;
+    G[4] = (jp[0] * jp[8] - jp[2] * jp[6]) * inv;
+    G[5] = (jp[1] * jp[6] - jp[0] * jp[7]) * inv;
+    G[6] = (jp[1] * jp[5] - jp[2] * jp[4]) * inv;
+    G[7] = (jp[2] * jp[3] - jp[0] * jp[5]) * inv;
+    G[8] = (jp[0] * jp[4] - jp[1] * jp[3]) * inv;
+    if (lane == 0 && !(det > 0.0)) {
+      atomicCAS(a.status, 0, LMG_ERR_DEGENERATE);
+      atomicMin(a.bad_elem, (unsigned long long)e);
+    }
+    const double coef = a.coef ? a.coef[e] : 1.0;
+    const double kap = (FORM == LMG_ADVDIFF ? a.kappa * coef : coef) * det;
+    double A[6];
+    A[0] = kap * (G[0] * G[0] + G[1] * G[1] + G[2] * G[2]);
+    A[1] = kap * (G[3] * G[3] + G[4] * G[4] + G[5] * G[5]);
+    A[2] = kap * (G[6] * G[6] + G[7] * G[7] + G[8] * G[8]);
+    A[3] = kap * (G[0] * G[3] + G[1] * G[4] + G[2] * G[5]);
+    A[4] = kap * (G[0] * G[6] + G[1] * G[7] + G[2] * G[8]);
+    A[5] = kap * (G[3] * G[6] + G[4] * G[7] + G[5] * G[8]);
+    __syncwarp();
+    // per quadrature point: transport coefficients and the load
+    if (lane < Q) {
+      const int q = lane;
+      double xq[3] = {0.0, 0.0, 0.0}, fx = 0.0;
+      for (int c = 0; c < N; ++c) {
+        const double s = sphi[q * N + c];  // isoparametric: mapping shapes = FE shapes
+        xq[0] += s * sX[3 * c];
+        xq[1] += s * sX[3 * c + 1];
+        xq[2] += s * sX[3 * c + 2];
+        fx += s * sf[c];
+      }
+      const double jxw = det * sqw[q];
+      sfq[q] = jxw * fx;
+      if (FORM == LMG_ADVDIFF) {
+        double b[3] = {0.0, 0.0, 0.0};
+        for (int m = 0; m < a.n_modes; ++m) {
+          const double *md = smode + 7 * m;
+          const double cs = cos(md[3] * xq[0] + md[4] * xq[1] + md[5] * xq[2] + md[6]);
+          b[0] += cs * (md[4] * md[2] - md[5] * md[1]);
+          b[1] += cs * (md[5] * md[0] - md[3] * md[2]);
+          b[2] += cs * (md[3] * md[1] - md[4] * md[0]);
+        }
+#pragma unroll
+        for (int m = 0; m < 3; ++m)
+          sbeta[3 * q + m] = jxw * (G[3 * m] * b[0] + G[3 * m + 1] * b[1] + G[3 * m + 2] * b[2]);
+      }
+    }
+    __syncwarp();
+    if (lane < N) {
+      const int b = lane;
+      double P[Q];
+      if (FORM == LMG_ADVDIFF) {
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+          const double *d = sdphi + (q * N + b) * 3;
+          P[q] = sbeta[3 * q] * d[0] + sbeta[3 * q + 1] * d[1] + sbeta[3 * q + 2] * d[2];
+        }
+      }
+      double *Ke = a.Kraw + e * (N * N);
+      for (int r = 0; r < N; ++r) {
+        double k = A[0] * sD[r * N + b];
+#pragma unroll
+        for (int t = 1; t < 6; ++t) k += A[t] * sD[(t * N + r) * N + b];
+        if (FORM == LMG_ADVDIFF) {
+#pragma unroll
+          for (int q = 0; q < Q; ++q) k += sphi[q * N + r] * P[q];
+        }
+        Ke[r * N + b] = k;
+      }
+      double fe = 0.0;
+#pragma unroll
+      for (int q = 0; q < Q; ++q) fe += sfq[q] * sphi[q * N + b];
+      a.Fraw[e * N + b] = fe;
+    }
+    __syncwarp();
+  }
+}
+
+template <int FORM, int N, int Q>
+void launch_full(const GenElemArgs &a, int n_sm, cudaStream_t s) {
+  const size_t smem = sizeof(double) * ((size_t)Q * N * 4 + 6 * N * N + Q + N * 3 + 7 * a.n_modes +
+                                        (size_t)WARPS * (N * 3 + N + 4 * Q));
+  static size_t attr = 0;  // largest dynamic shared memory granted so far
+  if (smem > attr) {
+    cudaFuncSetAttribute(k_elem_full<FORM, N, Q>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    attr = smem;
+  }
+  const int64_t need = (a.n_elem + WARPS - 1) / WARPS;
+  const int grid = (int)(need < (int64_t)n_sm * 8 ? need : (int64_t)n_sm * 8);
+  if (grid > 0) k_elem_full<FORM, N, Q><<<grid, WARPS * 32, smem, s>>>(a);
+}
+
+__global__ void __launch_bounds__(128) k_constrain(ConsArgs c) {
+  __shared__ double sK[GEN_MAX_N * GEN_MAX_N];
+  __shared__ double sF[GEN_MAX_N];
+  __shared__ int32_t scp[GEN_MAX_NE + 1];
+  __shared__ uint8_t sci[GEN_MAX_ENTRIES];
+  __shared__ double scv[GEN_MAX_ENTRIES];
+  const int N = c.N;
+  for (int64_t k = blockIdx.x; k < c.n_cons; k += gridDim.x) {
+    const int64_t e = c.elem[k];
+    const int ne = c.ne[k];
+    const int64_t cb = c.cbase[k], eb = c.ebase[k];
+    const uint64_t rows = c.rowmask[k];
+    __syncthreads();
+    for (int i = threadIdx.x; i < N * N; i += blockDim.x) sK[i] = c.Kraw[e * N * N + i];
+    for (int i = threadIdx.x; i < N; i += blockDim.x) sF[i] = c.Fraw[e * N + i];
+    for (int i = threadIdx.x; i <= ne; i += blockDim.x) scp[i] = c.ccp[cb + i];
+    __syncthreads();
+    const int n_ent = scp[ne];
+    for (int i = threadIdx.x; i < n_ent; i += blockDim.x) {
+      sci[i] = c.ci[eb + i];
+      scv[i] = c.cv[eb + i];
+    }
+    __syncthreads();
+    double *out = c.Ebuf + c.kout[k];
+    for (int idx = threadIdx.x; idx < ne * ne; idx += blockDim.x) {
+      const int p = idx / ne, q = idx - p * ne;
+      double v = 0.0;
+      if (p < N && ((rows >> p) & 1ull)) {
+        if (p == q) {
+          v = 1.0;
+        } else {
+          for (int t = scp[q]; t < scp[q + 1]; ++t)
+            if (sci[t] == p) v = -scv[t];
+        }
+      } else {
+        for (int t = scp[q]; t < scp[q + 1]; ++t) {
+          const int j = sci[t];
+          double l = 0.0;
+          for (int u = scp[p]; u < scp[p + 1]; ++u) l += scv[u] * sK[sci[u] * N + j];
+          v += l * scv[t];
+        }
+      }
+      out[idx] = v;
+    }
+    double *fo = c.Fbuf + c.fout[k];
+    for (int p = threadIdx.x; p < ne; p += blockDim.x) {
+      double v = 0.0;
+      for (int u = scp[p]; u < scp[p + 1]; ++u) v += scv[u] * sF[sci[u]];
+      fo[p] = v;
+    }
+  }
+}
+
+// K[s] = sum of the slot's contributions in element order; F likewise per dof.
+__global__ void k_gather_full(int64_t nnz, const int64_t *__restrict__ cptr, const uint32_t *__restrict__ coff,
+                              const double *__restrict__ E, double *__restrict__ K, int64_t n_dofs,
+                              const int64_t *__restrict__ fptr, const uint32_t *__restrict__ foff,
+                              const double *__restrict__ Fb, double *__restrict__ F) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < nnz + n_dofs; s += stride) {
+    if (s < nnz) {
+      double v = 0.0;
+      for (int64_t t = cptr[s]; t < cptr[s + 1]; ++t) v += E[coff[t]];
+      K[s] = v;
+    } else {
+      const int64_t d = s - nnz;
+      double v = 0.0;
+      for (int64_t t = fptr[d]; t < fptr[d + 1]; ++t) v += Fb[foff[t]];
+      F[d] = v;
+    }
+  }
+}
+
+}  // namespace
+
+bool gen_elements_built(int form, int n, int q) {
+  if (form != LMG_POISSON && form != LMG_ADVDIFF) return false;
+  return (n == 8 || n == 27) && (q == 8 || q == 27);
+}
+
+void launch_gen_elements(int form, int n, int q, const GenElemArgs &a, int n_sm, cudaStream_t s) {
+#define LMG_G(F, NN, QQ) \
+  if (form == F && n == NN && q == QQ) return launch_full<F, NN, QQ>(a, n_sm, s);
+  LMG_G(LMG_POISSON, 8, 8)
+  LMG_G(LMG_POISSON, 8, 27)
+  LMG_G(LMG_POISSON, 27, 8)
+  LMG_G(LMG_POISSON, 27, 27)
+  LMG_G(LMG_ADVDIFF, 8, 8)
+  LMG_G(LMG_ADVDIFF, 8, 27)
+  LMG_G(LMG_ADVDIFF, 27, 8)
+  LMG_G(LMG_ADVDIFF, 27, 27)
+#undef LMG_G
+}
+
+void launch_constrain(const ConsArgs &c, int n_sm, cudaStream_t s) {
+  if (c.n_cons <= 0) return;
+  const int64_t g = c.n_cons < (int64_t)n_sm * 16 ? c.n_cons : (int64_t)n_sm * 16;
+  k_constrain<<<(int)g, 128, 0, s>>>(c);
+}
+
+void launch_gather_full(int64_t nnz, const int64_t *cptr, const uint32_t *coff, const double *E, double *K,
+                        int64_t n_dofs, const int64_t *fptr, const uint32_t *foff, const double *Fb, double *F,
+                        int n_sm, cudaStream_t s) {
+  const int64_t items = nnz + n_dofs;
+  const int64_t blocks = (items + 255) / 256;
+  const int g = (int)(blocks < (int64_t)n_sm * 16 ? blocks : (int64_t)n_sm * 16);
+  k_gather_full<<<g, 256, 0, s>>>(nnz, cptr, coff, E, K, n_dofs, fptr, foff, Fb, F);
+}
+
+}  // namespace lmg

@@ -1,0 +1,60 @@
+// Declarations of the general scalar assembly path (general.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+
+#include "assemble.cuh"
+
+namespace lmg {
+
+constexpr int GEN_MAX_N = 27;          // dofs per element
+constexpr int GEN_MAX_NE = 128;        // dofs of a constrained element incl. constraining dofs
+constexpr int GEN_MAX_ENTRIES = 2048;  // nonzeros of one element's constraint matrix
+constexpr int GEN_MAX_MODES = 64;      // transport-velocity modes
+
+struct GenElemArgs {
+  int64_t n_elem;
+  const double *xyz;          // [n_nodes][3]
+  const int32_t *conn;        // [n_elem][N]
+  const double *coef;         // [n_elem] or null (=1)
+  const double *nodal_f;      // [n_nodes] or null (=0)
+  const double *D6;           // [6][N][N]: S00, S11, S22, S01+S10, S02+S20, S12+S21
+  double kappa;               // convection-diffusion diffusivity
+  int n_modes;
+  const double *modes;        // [n_modes][7]: a[3], k[3], phase
+  double *Kraw;               // [n_elem][N][N]
+  double *Fraw;               // [n_elem][N]
+  int *status;
+  unsigned long long *bad_elem;
+  DevFE fe;
+};
+
+// Constrained elements: column lists of each element's constraint matrix.
+struct ConsArgs {
+  int64_t n_cons;
+  int N;
+  const int32_t *elem;        // [n_cons] element id
+  const int32_t *ne;          // [n_cons] dofs after enlargement
+  const int64_t *kout;        // [n_cons] offset of the ne x ne result in Ebuf
+  const int64_t *fout;        // [n_cons] offset of the ne result in Fbuf
+  const int64_t *cbase;       // [n_cons] start of the element's ne+1 column pointers in ccp
+  const int32_t *ccp;         // column pointers, relative to the element's entries
+  const int64_t *ebase;       // [n_cons] start of the element's entries in ci / cv
+  const uint8_t *ci;          // row index of each entry
+  const double *cv;           // coefficient of each entry
+  const uint64_t *rowmask;    // [n_cons] constrained local rows
+  const double *Kraw;
+  const double *Fraw;
+  double *Ebuf;
+  double *Fbuf;
+};
+
+bool gen_elements_built(int form, int n, int q);
+void launch_gen_elements(int form, int n, int q, const GenElemArgs &a, int n_sm, cudaStream_t s);
+void launch_constrain(const ConsArgs &c, int n_sm, cudaStream_t s);
+void launch_gather_full(int64_t nnz, const int64_t *cptr, const uint32_t *coff, const double *E, double *K,
+                        int64_t n_dofs, const int64_t *fptr, const uint32_t *foff, const double *Fb, double *F,
+                        int n_sm, cudaStream_t s);
+
+}  // namespace lmg

@@ -66,6 +66,90 @@ void build_block_graph(int64_t n_elem, int nb, const int32_t *eb, int64_t n_bloc
   });
 }
 
+// Element lists of varying length (eptr [n_elem+1], elist): the same row-wise
+// union as build_block_graph.
+static void build_var_graph(int64_t n_elem, const std::vector<int64_t> &eptr, const std::vector<int32_t> &elist,
+                            int64_t n_rows, std::vector<int64_t> &row_ptr, std::vector<int32_t> &cols,
+                            int n_threads) {
+  std::vector<int64_t> rptr((size_t)n_rows + 1, 0);
+  for (int32_t r : elist) rptr[(size_t)r + 1]++;
+  for (int64_t r = 0; r < n_rows; ++r) rptr[(size_t)r + 1] += rptr[(size_t)r];
+  std::vector<int32_t> relem((size_t)rptr[(size_t)n_rows]);
+  {
+    std::vector<int64_t> cur(rptr.begin(), rptr.end() - 1);
+    for (int64_t e = 0; e < n_elem; ++e)
+      for (int64_t k = eptr[(size_t)e]; k < eptr[(size_t)e + 1]; ++k)
+        relem[(size_t)cur[(size_t)elist[(size_t)k]]++] = (int32_t)e;
+  }
+  if (n_threads < 1) n_threads = 1;
+  std::vector<int64_t> deg((size_t)n_rows, 0);
+  auto row_cols = [&](int64_t r, std::vector<int32_t> &buf) {
+    buf.clear();
+    for (int64_t k = rptr[(size_t)r]; k < rptr[(size_t)r + 1]; ++k) {
+      const int64_t e = relem[(size_t)k];
+      buf.insert(buf.end(), elist.begin() + eptr[(size_t)e], elist.begin() + eptr[(size_t)e + 1]);
+    }
+    std::sort(buf.begin(), buf.end());
+    buf.erase(std::unique(buf.begin(), buf.end()), buf.end());
+  };
+  auto run = [&](auto &&fn) {
+    std::atomic<int64_t> next{0};
+    std::vector<std::thread> th;
+    for (int t = 0; t < n_threads; ++t)
+      th.emplace_back([&]() {
+        std::vector<int32_t> buf;
+        for (;;) {
+          const int64_t s0 = next.fetch_add(4096);
+          if (s0 >= n_rows) break;
+          const int64_t s1 = std::min(n_rows, s0 + 4096);
+          for (int64_t r = s0; r < s1; ++r) fn(r, buf);
+        }
+      });
+    for (auto &t : th) t.join();
+  };
+  run([&](int64_t r, std::vector<int32_t> &buf) {
+    row_cols(r, buf);
+    deg[(size_t)r] = (int64_t)buf.size();
+  });
+  row_ptr.assign((size_t)n_rows + 1, 0);
+  for (int64_t r = 0; r < n_rows; ++r) row_ptr[(size_t)r + 1] = row_ptr[(size_t)r] + deg[(size_t)r];
+  cols.resize((size_t)row_ptr[(size_t)n_rows]);
+  run([&](int64_t r, std::vector<int32_t> &buf) {
+    row_cols(r, buf);
+    std::copy(buf.begin(), buf.end(), cols.begin() + row_ptr[(size_t)r]);
+  });
+}
+
+void build_constrained_graph(int64_t n_elem, int nl, const int32_t *ed, int64_t n_dofs, const int64_t *cons_ptr,
+                             const int32_t *cons_col, std::vector<int64_t> &row_ptr, std::vector<int32_t> &cols,
+                             int n_threads) {
+  // find_connected_dofs: close each element's dof set under "constrained by"
+  std::vector<int64_t> eptr((size_t)n_elem + 1, 0);
+  std::vector<int32_t> elist;
+  elist.reserve((size_t)(n_elem * nl));
+  std::vector<int32_t> set, add;
+  for (int64_t e = 0; e < n_elem; ++e) {
+    set.assign(ed + e * nl, ed + (e + 1) * nl);
+    std::sort(set.begin(), set.end());
+    set.erase(std::unique(set.begin(), set.end()), set.end());
+    for (bool done = false; !done;) {
+      add.clear();
+      for (int32_t d : set)
+        for (int64_t k = cons_ptr[d]; k < cons_ptr[d + 1]; ++k)
+          if (!std::binary_search(set.begin(), set.end(), cons_col[k])) add.push_back(cons_col[k]);
+      done = add.empty();
+      if (!done) {
+        set.insert(set.end(), add.begin(), add.end());
+        std::sort(set.begin(), set.end());
+        set.erase(std::unique(set.begin(), set.end()), set.end());
+      }
+    }
+    elist.insert(elist.end(), set.begin(), set.end());
+    eptr[(size_t)e + 1] = (int64_t)elist.size();
+  }
+  build_var_graph(n_elem, eptr, elist, n_dofs, row_ptr, cols, n_threads);
+}
+
 void block_structure(int64_t n_elem, int npe, int nv, const int32_t *ed, int &bs, int &nb,
                      std::vector<int32_t> &eb) {
   const int nl = nv * npe;
@@ -87,6 +171,33 @@ void block_structure(int64_t n_elem, int npe, int nv, const int32_t *ed, int &bs
 }  // namespace lmg
 
 extern "C" {
+
+lmg_status lmg_host_sparsity_constrained(int64_t n_elem, int32_t dofs_per_elem, int64_t n_dofs,
+                                         const int32_t *elem_dofs, const int64_t *cons_ptr,
+                                         const int32_t *cons_col, int64_t *nnz, int32_t *row_ptr,
+                                         int32_t *col_idx) {
+  if (!elem_dofs || !nnz || !cons_ptr || n_elem <= 0 || dofs_per_elem <= 0 || n_dofs <= 0) return LMG_ERR_ARG;
+  for (int64_t i = 0; i < n_elem * dofs_per_elem; ++i)
+    if (elem_dofs[i] < 0 || elem_dofs[i] >= n_dofs) return LMG_ERR_BOUNDS;
+  for (int64_t k = 0; k < cons_ptr[n_dofs]; ++k)
+    if (!cons_col || cons_col[k] < 0 || cons_col[k] >= n_dofs) return LMG_ERR_BOUNDS;
+  try {
+    std::vector<int64_t> rp;
+    std::vector<int32_t> cols;
+    const unsigned hw = std::thread::hardware_concurrency();
+    lmg::build_constrained_graph(n_elem, dofs_per_elem, elem_dofs, n_dofs, cons_ptr, cons_col, rp, cols,
+                                 hw ? (int)hw : 4);
+    if ((int64_t)cols.size() >= INT32_MAX) return LMG_ERR_UNSUPPORTED;
+    *nnz = (int64_t)cols.size();
+    if (row_ptr && col_idx) {
+      for (int64_t r = 0; r <= n_dofs; ++r) row_ptr[r] = (int32_t)rp[(size_t)r];
+      std::copy(cols.begin(), cols.end(), col_idx);
+    }
+  } catch (const std::bad_alloc &) {
+    return LMG_ERR_OOM;
+  }
+  return LMG_OK;
+}
 
 lmg_status lmg_host_sparsity(int64_t n_elem, int32_t npe, int32_t n_vars, int64_t n_dofs,
                              const int32_t *elem_dofs, int64_t *nnz, int32_t *row_ptr, int32_t *col_idx) {

@@ -195,10 +195,6 @@ std::string all_second_order_tet4(HostMesh &m) {
 
 }  // namespace lmg
 
-struct lmg_mesh {
-  lmg::HostMesh m;
-};
-
 extern "C" {
 
 lmg_status lmg_mesh_cube(int32_t nx, int32_t ny, int32_t nz, int32_t elem_type, double jitter,
@@ -213,6 +209,11 @@ lmg_status lmg_mesh_cube(int32_t nx, int32_t ny, int32_t nz, int32_t elem_type, 
     const int base = tets ? LMG_HEX8 : elem_type;
     std::string err = lmg::build_cube_hex(mesh->m, nx, ny, nz, base);
     if (err.empty()) lmg::jitter_interior(mesh->m, jitter, nx, ny, nz, seed);
+    if (err.empty() && !tets && jitter == 0.0) {  // unjittered hex cube: lattice for refinement
+      mesh->m.cube[0] = nx;
+      mesh->m.cube[1] = ny;
+      mesh->m.cube[2] = nz;
+    }
     if (err.empty() && tets) err = lmg::all_tri_hex8(mesh->m);
     if (err.empty() && elem_type == LMG_TET10) err = lmg::all_second_order_tet4(mesh->m);
     if (!err.empty()) {

@@ -19,6 +19,26 @@ int vertices_per_elem(int elem_type);
 int side_nodes(int elem_type, int s, int *out);
 
 // ---------------------------------------------------------------- mesh
+// Refinement tree of a structured hex cube (host_amr.cpp).  Every element
+// ever created keeps its id (children are appended, as MeshRefinement::add_elem
+// does); node and element corners live on an integer lattice whose level-0
+// element edge is AMR_S0, so coincident nodes are found exactly.
+constexpr int64_t AMR_S0 = 1024;
+constexpr int AMR_MAX_LEVEL = 8;
+struct AmrTree {
+  bool on = false;
+  int nx = 0, ny = 0, nz = 0;
+  std::vector<int32_t> conn;          // [n_all][npe], current node ids
+  std::vector<int32_t> parent;        // -1 on level 0
+  std::vector<int32_t> first_child;   // -1 while active
+  std::vector<int8_t> level;
+  std::vector<int64_t> origin;        // [n_all][3] lattice position of vertex 0
+  std::vector<int8_t> side_bid;       // [n_all][6]
+  std::vector<int64_t> node_lat;      // [n_nodes][3]
+  std::vector<int32_t> active;        // active element ids, id order
+  int64_t n_all() const { return (int64_t)parent.size(); }
+};
+
 struct HostMesh {
   int elem_type = 0;
   int npe = 0;           // nodes per element
@@ -26,6 +46,8 @@ struct HostMesh {
   std::vector<double> xyz;      // [n_nodes][3]
   std::vector<int32_t> conn;    // [n_elem][npe]
   std::vector<int8_t> side_bid; // [n_elem][nsides], -1 = interior
+  int cube[3] = {0, 0, 0};      // build_cube grid of an unjittered hex cube (else 0)
+  AmrTree amr;                  // refinement tree once lmg_mesh_refine ran
   int64_t n_nodes() const { return (int64_t)xyz.size() / 3; }
   int64_t n_elem() const { return npe ? (int64_t)conn.size() / npe : 0; }
 };
@@ -36,6 +58,24 @@ void renumber_nodes_first_touch(HostMesh &m);
 void jitter_interior(HostMesh &m, double amp, int nx, int ny, int nz, uint64_t seed);
 std::string all_tri_hex8(HostMesh &m);
 std::string all_second_order_tet4(HostMesh &m);
+
+// AMR (host_amr.cpp).  amr_refine runs `cycles` rounds of: flag
+// floor(fraction * n_active) random active elements, enforce the level-one
+// rule across faces, refine; HostMesh::conn / side_bid then hold the active
+// elements in id order.
+std::string amr_refine(HostMesh &m, int cycles, double fraction, uint64_t seed);
+// Constraint rows of the dofs of hanging nodes (lagrange_compute_constraints)
+// for LAGRANGE variables on the active mesh, then empty rows for the dofs in
+// `dirichlet` that are still free, then chain expansion (process_constraints).
+// rows: dof -> (dof -> coefficient), both ascending.
+struct ConstraintRows {
+  std::vector<int32_t> dofs;                 // constrained dofs, ascending
+  std::vector<int64_t> ptr;                  // [dofs.size() + 1]
+  std::vector<int32_t> col;
+  std::vector<double> val;
+};
+std::string amr_constraint_rows(const HostMesh &m, int n_vars, const int32_t *elem_dofs, int64_t n_dofs,
+                                const uint8_t *dirichlet, ConstraintRows &out);
 
 // ---------------------------------------------------------------- rng
 // splitmix64; u01 maps the top 53 bits to [0,1).
@@ -81,8 +121,20 @@ bool elem_has_affine_map(int elem_type, const double *pts /* [npe][3] */);
 // layout holds, else bs = 1 and nb = n_vars*npe (every dof is a block).
 void block_structure(int64_t n_elem, int npe, int n_vars, const int32_t *elem_dofs, int &bs, int &nb,
                      std::vector<int32_t> &elem_blocks);
+// Sparsity of a constrained system (DofMap::compute_sparsity with
+// find_connected_dofs): every element couples the sorted union of its dofs and,
+// transitively, the dofs that constrain them.  cons_ptr [n_dofs+1] / cons_col
+// give each dof's constraint row (empty for free and Dirichlet dofs).
+void build_constrained_graph(int64_t n_elem, int nl, const int32_t *elem_dofs, int64_t n_dofs,
+                             const int64_t *cons_ptr, const int32_t *cons_col,
+                             std::vector<int64_t> &row_ptr, std::vector<int32_t> &cols, int n_threads);
 void build_block_graph(int64_t n_elem, int nb_per_elem, const int32_t *elem_blocks,
                        int64_t n_blocks, std::vector<int64_t> &row_ptr,
                        std::vector<int32_t> &cols, int n_threads);
 
 }  // namespace lmg
+
+// The opaque mesh handle of the C ABI.
+struct lmg_mesh {
+  lmg::HostMesh m;
+};

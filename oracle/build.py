@@ -1,6 +1,6 @@
-"""Build recipe for the CPU oracle (test infrastructure): oracle/oracle.cpp ->
-oracle/_build/liboracle.so, compiled with -ffp-contract=off so that no
-multiply-add is fused."""
+"""Build recipe for the CPU oracle (test infrastructure): oracle/oracle.cpp and
+oracle/oracle_constraints.cpp -> oracle/_build/liboracle.so, compiled with
+-ffp-contract=off so that no multiply-add is fused."""
 import os
 import subprocess
 
@@ -9,13 +9,13 @@ LIB = os.path.join(HERE, "_build", "liboracle.so")
 
 
 def build(force=False):
-    src = os.path.join(HERE, "oracle.cpp")
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(src):
+    srcs = [os.path.join(HERE, f) for f in ("oracle.cpp", "oracle_constraints.cpp")]
+    if not force and os.path.exists(LIB) and all(os.path.getmtime(LIB) >= os.path.getmtime(s) for s in srcs):
         return LIB
     os.makedirs(os.path.dirname(LIB), exist_ok=True)
     tmp = LIB + ".tmp"
     cmd = ["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared",
-           "-pthread", src, "-o", tmp]
+           "-pthread"] + srcs + ["-o", tmp]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("oracle build failed:\n" + r.stdout + r.stderr)

@@ -405,6 +405,8 @@ void right_multiply(Dense &self, const Dense &M3) {
 namespace {
 
 // ------------------------------------------------------------------ element assembly
+const int ADVDIFF = 2;
+
 struct Problem {
   int form, type, fe_order, q_order, npe, n_vars, nl;
   int64_t n_nodes, n_elem, n_dofs;
@@ -414,7 +416,69 @@ struct Problem {
   const double *coef, *nodal_f;
   double nu;
   const int32_t *row_ptr, *col;
+  // constraint rows (NULL: every constrained dof has an empty row)
+  const int64_t *cons_ptr;
+  const int32_t *cons_col;
+  const double *cons_val;
+  // ADVDIFF: {kappa, n_modes, then per mode a[3], k[3], phase}
+  const double *params;
+  int n_params;
 };
+
+// Constraint row of dof d as (dof, coefficient) pairs in ascending dof order
+// (DofConstraintRow is a std::map).
+void constraint_row(const Problem &P, int32_t d, std::vector<std::pair<int32_t, double>> &row) {
+  row.clear();
+  if (!P.cons_ptr) return;
+  for (int64_t k = P.cons_ptr[d]; k < P.cons_ptr[d + 1]; ++k) row.emplace_back(P.cons_col[k], P.cons_val[k]);
+}
+
+// DofMap::build_constraint_matrix (src/base/dof_map_constraints.C:3433-3540).
+void build_constraint_matrix(const Problem &P, Dense &C, std::vector<int32_t> &elem_dofs, bool called_recursively) {
+  std::set<int32_t> dof_set;
+  bool we_have_constraints = false;
+  std::vector<std::pair<int32_t, double>> row;
+  for (const auto &dof : elem_dofs)
+    if (P.constrained[dof]) {
+      we_have_constraints = true;
+      constraint_row(P, dof, row);
+      for (const auto &item : row) dof_set.insert(item.first);
+    }
+  if (!we_have_constraints) return;
+  for (const auto &dof : elem_dofs) dof_set.erase(dof);
+  if (!dof_set.empty() || !called_recursively) {
+    const int old_size = (int)elem_dofs.size();
+    elem_dofs.insert(elem_dofs.end(), dof_set.begin(), dof_set.end());
+    C.resize(old_size, (int)elem_dofs.size());
+    for (int i = 0; i != old_size; i++)
+      if (P.constrained[elem_dofs[i]]) {
+        constraint_row(P, elem_dofs[i], row);
+        for (const auto &item : row)
+          for (int j = 0, n_elem_dofs = (int)elem_dofs.size(); j != n_elem_dofs; j++)
+            if (elem_dofs[j] == item.first) C(i, j) = item.second;
+      } else {
+        C(i, i) = 1.;
+      }
+    Dense Cnew;
+    build_constraint_matrix(P, Cnew, elem_dofs, true);
+    if ((C.n == Cnew.m) && (Cnew.n == (int)elem_dofs.size())) right_multiply(C, Cnew);
+  }
+}
+
+// Transport velocity b = curl psi of psi = sum_m a_m sin(k_m . x + phase_m):
+// b = sum_m cos(k_m . x + phase_m) (k_m x a_m).
+void velocity(const Problem &P, const Pt &x, double b[3]) {
+  b[0] = b[1] = b[2] = 0.;
+  const int nm = P.n_params > 1 ? (int)P.params[1] : 0;
+  for (int m = 0; m < nm; ++m) {
+    const double *md = P.params + 2 + 7 * m;
+    const double *a = md, *k = md + 3;
+    const double c = std::cos(k[0] * x.v[0] + k[1] * x.v[1] + k[2] * x.v[2] + md[6]);
+    b[0] += c * (k[1] * a[2] - k[2] * a[1]);
+    b[1] += c * (k[2] * a[0] - k[0] * a[2]);
+    b[2] += c * (k[0] * a[1] - k[1] * a[0]);
+  }
+}
 
 // Lamé form of the elasticity tensor (systems_of_equations_ex6.C:120-150) with Young's modulus E.
 double elasticity_tensor(double E, double nu, unsigned i, unsigned j, unsigned k, unsigned l) {
@@ -441,7 +505,29 @@ bool element_matrix(const Problem &P, OracleFE &fe, int64_t e, Dense &Ke, std::v
   if (P.nodal_f)
     for (int a = 0; a < n; ++a)
       for (int v = 0; v < P.n_vars; ++v) f[a * P.n_vars + v] = P.nodal_f[(int64_t)P.conn[e * P.npe + a] * P.n_vars + v];
-  if (P.form == POISSON) {
+  if (P.form == ADVDIFF) {
+    // Steady Galerkin convection-diffusion (adaptivity_ex2.C:660-690 without
+    // the time terms): Ke(i,j) += JxW [(b . dphi_j) phi_i + kappa_e dphi_i . dphi_j],
+    // Fe(i) += JxW f phi_i, with kappa_e = kappa * coef_e and b at the mapped point.
+    const double kappa = P.params[0] * coef;
+    for (int qp = 0; qp < fe.nq; qp++) {
+      Pt xq = {{0., 0., 0.}};
+      for (int a = 0; a < fe.n_geo; ++a)
+        for (int d = 0; d < 3; ++d) xq.v[d] += fe.phi_map[a][qp] * X[a].v[d];
+      double bv[3];
+      velocity(P, xq, bv);
+      const Pt b = {{bv[0], bv[1], bv[2]}};
+      for (int i = 0; i != n; i++)
+        for (int j = 0; j != n; j++)
+          Ke(i, j) += fe.JxW[qp] * (dot(b, fe.dphi[j][qp]) * fe.phi[i][qp] +
+                                    kappa * dot(fe.dphi[i][qp], fe.dphi[j][qp]));
+    }
+    for (int qp = 0; qp < fe.nq; qp++) {
+      double fxy = 0.0;
+      for (int j = 0; j < n; ++j) fxy += fe.phi[j][qp] * f[j];
+      for (int i = 0; i != n; i++) Fe[i] += fe.JxW[qp] * fxy * fe.phi[i][qp];
+    }
+  } else if (P.form == POISSON) {
     // introduction_ex4.C:464-467 and 536 with nodal f interpolated by phi.
     for (int qp = 0; qp < fe.nq; qp++)
       for (int i = 0; i != n; i++)
@@ -471,27 +557,26 @@ bool element_matrix(const Problem &P, OracleFE &fe, int64_t e, Dense &Ke, std::v
     }
   }
   // DofMap::constrain_element_matrix_and_vector (dof_map_constraints.C:2439-2515)
-  // with build_constraint_matrix (:3433-3540).  Dirichlet rows are empty, so
-  // no dof is appended and C is square.
-  bool any = false;
-  for (int i = 0; i < nl; ++i) any |= P.constrained[dofs[i]] != 0;
-  if (any) {
-    Dense C;
-    C.resize(nl, nl);
-    for (int i = 0; i < nl; ++i)
-      if (!P.constrained[dofs[i]]) C(i, i) = 1.;
+  // with asymmetric constraint rows (the default, include/base/dof_map.h:1351-1354).
+  Dense C;
+  build_constraint_matrix(P, C, dofs, false);
+  if ((C.m == Ke.m) && (C.n == (int)dofs.size())) {
     left_multiply_transpose(Ke, C);
     right_multiply(Ke, C);
-    for (int i = 0; i < nl; ++i)
+    std::vector<std::pair<int32_t, double>> row;
+    for (int i = 0, n_elem_dofs = (int)dofs.size(); i != n_elem_dofs; i++)
       if (P.constrained[dofs[i]]) {
-        for (int j = 0; j < nl; ++j) Ke(i, j) = 0.;
+        for (int j = 0; j < Ke.n; ++j) Ke(i, j) = 0.;
         Ke(i, i) = 1.;
+        constraint_row(P, dofs[i], row);
+        for (const auto &item : row)
+          for (int j = 0; j != n_elem_dofs; j++)
+            if (dofs[j] == item.first) Ke(i, j) = -item.second;
       }
-    std::vector<double> old = Fe;
-    for (int i = 0; i < nl; i++) {  // DenseMatrix::vector_mult_transpose
-      Fe[i] = 0.;
-      for (int j = 0; j < nl; j++) Fe[i] += C(j, i) * old[j];
-    }
+    std::vector<double> old_rhs = Fe;
+    Fe.assign(C.n, 0.);
+    for (int i = 0; i < C.n; i++)  // DenseMatrix::vector_mult_transpose
+      for (int j = 0; j < C.m; j++) Fe[i] += C(j, i) * old_rhs[j];
   }
   return ok;
 }
@@ -647,12 +732,37 @@ int orc_sparsity(int64_t n_dofs, int64_t n_elem, int nl, const int32_t *elem_dof
 // each thread builds element matrices and inserts under one mutex, as
 // FEMSystem::assembly does (src/systems/fem_system.C:940-944, 362-369).
 // Returns 0, 4 (degenerate element, *bad_elem set) or 6 (entry outside the pattern).
+// orc_assemble2 adds the constraint rows (cons_ptr [n_dofs+1], cons_col,
+// cons_val; NULL = empty rows) and the form parameters (ADVDIFF).
+int orc_assemble2(int form, int type, int fe_order, int q_order, int64_t n_nodes, const double *xyz,
+                  int64_t n_elem, const int32_t *conn, int n_vars, const int32_t *elem_dofs, int64_t n_dofs,
+                  const uint8_t *constrained, const double *coef, const double *nodal_f, double nu,
+                  const int32_t *row_ptr, const int32_t *col, double *K, double *F, int n_threads,
+                  int64_t e_begin, int64_t e_end, int64_t *bad_elem, double *loop_seconds,
+                  const int64_t *cons_ptr, const int32_t *cons_col, const double *cons_val,
+                  const double *params, int n_params);
+
 int orc_assemble(int form, int type, int fe_order, int q_order, int64_t n_nodes, const double *xyz,
                  int64_t n_elem, const int32_t *conn, int n_vars, const int32_t *elem_dofs, int64_t n_dofs,
                  const uint8_t *constrained, const double *coef, const double *nodal_f, double nu,
                  const int32_t *row_ptr, const int32_t *col, double *K, double *F, int n_threads,
                  int64_t e_begin, int64_t e_end, int64_t *bad_elem, double *loop_seconds) {
+  return orc_assemble2(form, type, fe_order, q_order, n_nodes, xyz, n_elem, conn, n_vars, elem_dofs, n_dofs,
+                       constrained, coef, nodal_f, nu, row_ptr, col, K, F, n_threads, e_begin, e_end, bad_elem,
+                       loop_seconds, nullptr, nullptr, nullptr, nullptr, 0);
+}
+
+int orc_assemble2(int form, int type, int fe_order, int q_order, int64_t n_nodes, const double *xyz,
+                  int64_t n_elem, const int32_t *conn, int n_vars, const int32_t *elem_dofs, int64_t n_dofs,
+                  const uint8_t *constrained, const double *coef, const double *nodal_f, double nu,
+                  const int32_t *row_ptr, const int32_t *col, double *K, double *F, int n_threads,
+                  int64_t e_begin, int64_t e_end, int64_t *bad_elem, double *loop_seconds,
+                  const int64_t *cons_ptr, const int32_t *cons_col, const double *cons_val,
+                  const double *params, int n_params) {
   Problem P{};
+  P.cons_ptr = cons_ptr; P.cons_col = cons_col; P.cons_val = cons_val;
+  P.params = params; P.n_params = n_params;
+  if (form == ADVDIFF && n_params < 2) return 1;
   P.form = form; P.type = type; P.fe_order = fe_order; P.q_order = q_order;
   P.npe = n_shapes(type, (type == HEX27 || type == TET10) ? 2 : 1);
   P.n_vars = n_vars; P.nl = n_vars * P.npe;
@@ -678,7 +788,7 @@ int orc_assemble(int form, int type, int fe_order, int q_order, int64_t n_nodes,
       std::lock_guard<std::mutex> lk(mtx);
       if (!ok && status == 0) { status = 4; first_bad = e; }
       if (!add_matrix(P, Ke, dofs, K) && status == 0) status = 6;
-      for (int i = 0; i < P.nl; ++i) F[dofs[i]] += Fe[i];  // PetscVector::add_vector
+      for (size_t i = 0; i < dofs.size(); ++i) F[dofs[i]] += Fe[i];  // PetscVector::add_vector
     }
   };
   const auto t0 = std::chrono::steady_clock::now();

@@ -25,8 +25,13 @@ def lib():
         _lib.orc_sparsity.argtypes = [i64, i64, i32, v, C.POINTER(i64), v, v]
         _lib.orc_assemble.argtypes = [i32, i32, i32, i32, i64, v, i64, v, i32, v, i64, v, v, v, f64,
                                       v, v, v, v, i32, i64, i64, C.POINTER(i64), C.POINTER(f64)]
+        _lib.orc_assemble2.argtypes = _lib.orc_assemble.argtypes + [v, v, v, v, i32]
+        _lib.orc_constraint_rows.argtypes = [i32, i64, v, i64, v, v, v, i64, v, i32, v, i64, v, v, v, v, v, i64]
+        _lib.orc_constraint_rows.restype = i64
+        _lib.orc_sparsity_constrained.argtypes = [i64, i64, i32, v, v, v, C.POINTER(i64), v, v]
         for f in (_lib.orc_qgauss, _lib.orc_shapes, _lib.orc_has_affine_map, _lib.orc_distribute_dofs,
-                  _lib.orc_dirichlet, _lib.orc_sparsity, _lib.orc_assemble):
+                  _lib.orc_dirichlet, _lib.orc_sparsity, _lib.orc_assemble, _lib.orc_assemble2,
+                  _lib.orc_sparsity_constrained):
             f.restype = C.c_int32
     return _lib
 
@@ -86,10 +91,50 @@ def sparsity(n_dofs, elem_dofs):
     return rp, col
 
 
+ADVDIFF = 2
+
+
+def constraint_rows(elem_type, xyz, all_conn, parent, level, active_ids, n_vars, elem_dofs, n_dofs, dirichlet):
+    """Hanging-node rows + Dirichlet rows + process_constraints on a refined
+    hex mesh.  Returns (constrained, cons_ptr, cons_col, cons_val)."""
+    xyz = np.ascontiguousarray(xyz, np.float64)
+    all_conn = np.ascontiguousarray(all_conn, np.int32)
+    parent = np.ascontiguousarray(parent, np.int32)
+    level = np.ascontiguousarray(level, np.int8)
+    act = np.ascontiguousarray(active_ids, np.int32)
+    ed = np.ascontiguousarray(elem_dofs, np.int32)
+    dr = None if dirichlet is None else np.ascontiguousarray(dirichlet, np.uint8)
+    cons = np.zeros(n_dofs, np.uint8)
+    ptr_ = np.zeros(n_dofs + 1, np.int64)
+    args = (elem_type, xyz.shape[0], _p(xyz), all_conn.shape[0], _p(all_conn), _p(parent), _p(level),
+            act.shape[0], _p(act), n_vars, _p(ed), n_dofs, _p(dr), _p(cons), _p(ptr_))
+    total = lib().orc_constraint_rows(*args, None, None, 0)
+    col = np.zeros(max(total, 1), np.int32)
+    val = np.zeros(max(total, 1), np.float64)
+    assert lib().orc_constraint_rows(*args, _p(col), _p(val), total) == total
+    return cons, ptr_, col[:total], val[:total]
+
+
+def sparsity_constrained(n_dofs, elem_dofs, cons_ptr, cons_col):
+    ed = np.ascontiguousarray(elem_dofs, np.int32)
+    cp = np.ascontiguousarray(cons_ptr, np.int64)
+    cc = np.ascontiguousarray(cons_col, np.int32)
+    nnz = C.c_int64()
+    lib().orc_sparsity_constrained(n_dofs, ed.shape[0], ed.shape[1], _p(ed), _p(cp), _p(cc), C.byref(nnz), None, None)
+    rp = np.zeros(n_dofs + 1, np.int32)
+    col = np.zeros(nnz.value, np.int32)
+    lib().orc_sparsity_constrained(n_dofs, ed.shape[0], ed.shape[1], _p(ed), _p(cp), _p(cc), C.byref(nnz), _p(rp),
+                                   _p(col))
+    return rp, col
+
+
 def assemble(form, elem_type, fe_order, q_order, xyz, conn, n_vars, elem_dofs, n_dofs, constrained,
-             row_ptr, col, coef=None, nodal_f=None, nu=0.3, n_threads=1, e_range=None, timing=None):
+             row_ptr, col, coef=None, nodal_f=None, nu=0.3, n_threads=1, e_range=None, timing=None,
+             cons_rows=None, params=None):
     """Returns (K values, F, status, first bad element); timing (a dict) gets
-    the wall time of the element loop under "seconds"."""
+    the wall time of the element loop under "seconds".  cons_rows =
+    (cons_ptr, cons_col, cons_val) gives the constraint rows (default: empty
+    rows); params the form parameters (ADVDIFF)."""
     xyz = np.ascontiguousarray(xyz, np.float64)
     conn = np.ascontiguousarray(conn, np.int32)
     ed = np.ascontiguousarray(elem_dofs, np.int32)
@@ -101,10 +146,15 @@ def assemble(form, elem_type, fe_order, q_order, xyz, conn, n_vars, elem_dofs, n
     b, e = (0, conn.shape[0]) if e_range is None else e_range
     bad = C.c_int64(-1)
     secs = C.c_double(0)
-    st = lib().orc_assemble(form, elem_type, fe_order, q_order, xyz.shape[0], _p(xyz), conn.shape[0],
-                            _p(conn), n_vars, _p(ed), n_dofs, _p(cons), _p(coef), _p(nodal_f), nu,
-                            _p(np.ascontiguousarray(row_ptr, np.int32)), _p(np.ascontiguousarray(col, np.int32)),
-                            _p(K), _p(F), n_threads, b, e, C.byref(bad), C.byref(secs))
+    cr = (None, None, None) if cons_rows is None else (np.ascontiguousarray(cons_rows[0], np.int64),
+                                                         np.ascontiguousarray(cons_rows[1], np.int32),
+                                                         np.ascontiguousarray(cons_rows[2], np.float64))
+    pr = None if params is None else np.ascontiguousarray(params, np.float64)
+    st = lib().orc_assemble2(form, elem_type, fe_order, q_order, xyz.shape[0], _p(xyz), conn.shape[0],
+                             _p(conn), n_vars, _p(ed), n_dofs, _p(cons), _p(coef), _p(nodal_f), nu,
+                             _p(np.ascontiguousarray(row_ptr, np.int32)), _p(np.ascontiguousarray(col, np.int32)),
+                             _p(K), _p(F), n_threads, b, e, C.byref(bad), C.byref(secs),
+                             _p(cr[0]), _p(cr[1]), _p(cr[2]), _p(pr), 0 if pr is None else len(pr))
     if timing is not None:
         timing["seconds"] = secs.value
     return K, F, st, bad.value
