@@ -156,6 +156,87 @@ def run_reference(args, rank):
         "e2e": {"value": v, "unit": "Melem/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
 
 
+def cd_params(seed=3, n_modes=8, kappa=1e-2):
+    """Convection-diffusion data: kappa and the modes of the streamfunction
+    psi = sum_m a_m sin(k_m . x + phase_m), b = curl psi (divergence-free)."""
+    rng = np.random.default_rng(seed)
+    p = [kappa, n_modes]
+    for _ in range(n_modes):
+        p += list(rng.uniform(-1, 1, 3)) + list(2 * np.pi * rng.uniform(-1.5, 1.5, 3)) + [rng.uniform(0, 2 * np.pi)]
+    return np.array(p)
+
+
+def run_amr(args, local):
+    """Secondary workload: steady convection-diffusion, SECOND LAGRANGE HEX27,
+    QGauss FIFTH, on build_cube(n^3, HEX27) after 3 cycles of refining 20% of
+    the active elements (level-one rule), hanging-node and Dirichlet
+    constraints applied through C^T K C.  Same JSON keys as the headline."""
+    import torch
+    import libmesh_gb300 as lm
+    torch.cuda.set_device(local)
+    t0 = time.perf_counter()
+    n = 24 if args.n == N_CUBE else args.n      # build_cube 24^3 HEX27 unless --n is given
+    mesh = lm.Mesh.build_refined_cube(n, lm.HEX27, 3, 0.2, 2)
+    dm = lm.DofMap(mesh, 1)
+    dm.add_dirichlet_boundary([0, 1, 2, 3, 4, 5], [0])
+    dm.create_dof_constraints()
+    rng = np.random.default_rng(2)
+    k = np.exp(rng.normal(0.0, 0.5, mesh.n_elem))
+    f = rng.uniform(-1.0, 1.0, (mesh.n_nodes, 1))
+    asm = lm.GpuAssembly(lm.ADVDIFF, 2, 5, elem_coef=k, nodal_f=f, params=cd_params(), device=local)
+    asm.init(mesh, dm)
+    stream = torch.cuda.current_stream()
+    asm.set_stream(stream.cuda_stream)
+    asm.assemble_device(lm.FP64)        # builds the slot plan
+    asm.synchronize()
+    setup_s = time.perf_counter() - t0
+    for _ in range(max(3, args.warmup)):
+        asm.assemble_device(lm.FP64)
+    asm.synchronize()
+    clocks = Clocks(local)
+    clocks.start()
+    torch.cuda.synchronize()
+    l0 = asm.launch_count()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        asm.assemble_device(lm.FP64)
+    ev1.record(stream)
+    ev1.synchronize()
+    asm.synchronize()
+    ms = ev0.elapsed_time(ev1) / args.steps
+    launches = asm.launch_count() - l0
+    clk = clocks.stop()
+    asm.perflog_enable(True)
+    for _ in range(5):
+        asm.assemble_device(lm.FP64)
+    el_ms, ga_ms, calls = asm.perflog_read()
+    asm.perflog_enable(False)
+    Kh = torch.empty(asm.nnz, dtype=torch.float64, pin_memory=True)
+    Fh = torch.empty(dm.n_dofs, dtype=torch.float64, pin_memory=True)
+    kh = torch.from_numpy(k).pin_memory()
+    t1 = time.perf_counter()
+    n_e2e = max(3, min(args.steps, 5))
+    for _ in range(n_e2e):
+        asm.update_inputs(elem_coef=kh.numpy())
+        asm.assemble_into(Kh.data_ptr(), Fh.data_ptr(), lm.FP64)
+    e2e_s = (time.perf_counter() - t1) / n_e2e
+    asm.close()
+    n_cons = int(dm.constrained[dm.elem_dofs].any(1).sum())
+    print(json.dumps({
+        "metric": METRIC, "value": mesh.n_elem / (ms * 1e-3) / 1e6, "unit": "Melem/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded refinement, k_e, f, b)",
+        "config": {"workload": "convection-diffusion HEX27 build_cube %d^3, 3 cycles x 20%% h-refinement, "
+                               "QGauss FIFTH, hanging-node + Dirichlet constraints" % n,
+                   "n_elem": mesh.n_elem, "n_dofs": dm.n_dofs, "nnz": asm.nnz, "constrained_elements": n_cons,
+                   "setup_s": setup_s, "l2": "inputs larger than L2"},
+        "e2e": {"value": mesh.n_elem / e2e_s / 1e6, "unit": "Melem/s", "h2d_bytes_per_step": 8 * mesh.n_elem,
+                "d2h_bytes_per_step": 8 * (asm.nnz + dm.n_dofs)},
+        "gpu_launches": launches, "clocks": clk,
+        "stages_ms": {"elements_and_constraints": el_ms / calls, "insertion": ga_ms / calls}}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -166,12 +247,18 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
     ap.add_argument("--n", type=int, default=N_CUBE, help="cube divisions (48 = the headline mesh)")
     ap.add_argument("--no-mixed", action="store_true", help="skip timing the mixed form beside FP64")
+    ap.add_argument("--workload", default="elasticity", choices=["elasticity", "amr-cd"],
+                    help="elasticity = the headline; amr-cd = refined HEX27 convection-diffusion")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
     local = int(os.environ.get("LOCAL_RANK", 0))
     if args.impl == "reference":
         return run_reference(args, rank)
+    if args.workload == "amr-cd":
+        from libmesh_gb300 import _build
+        _build.build()
+        return run_amr(args, local)
 
     import torch
     import libmesh_gb300 as lm

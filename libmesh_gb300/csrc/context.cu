@@ -544,6 +544,24 @@ lmg_status lmg_form_set(lmg_ctx *c, int32_t form, int32_t fe_order, int32_t q_or
           const int m0 = pm[k][0], m1 = pm[k][1];
           D[((size_t)k * n + a) * n + b] = (m0 == m1) ? S(m0, m0, a, b) : S(m0, m1, a, b) + S(m1, m0, a, b);
         }
+    // 1-D shapes at the 1-D Gauss points of a tensor hex rule: L1[i][q1]
+    if (general && (c->elem_type == LMG_HEX8 || c->elem_type == LMG_HEX27)) {
+      const int q1n = (t.q == 8) ? 2 : 3, n1 = (n == 8) ? 2 : 3;
+      bool tensor = q1n * q1n * q1n == t.q;
+      for (int q = 0; q < t.q && tensor; ++q) {
+        const int id[3] = {q % q1n, (q / q1n) % q1n, q / (q1n * q1n)};
+        for (int d = 0; d < 3; ++d) tensor = tensor && t.qp[3 * q + d] == t.qp[3 * id[d]];
+      }
+      if (!tensor) return fail(c, LMG_ERR_UNSUPPORTED, "form_set: the convection kernel needs a tensor Gauss rule");
+      for (int i = 0; i < n1; ++i)
+        for (int q1 = 0; q1 < q1n; ++q1) {
+          const double x = t.qp[3 * q1];
+          double v;
+          if (n1 == 2) v = i == 0 ? .5 * (1. - x) : .5 * (1. + x);
+          else v = i == 0 ? .5 * x * (x - 1.) : (i == 1 ? .5 * x * (x + 1.) : (1. - x) * (1. + x));
+          D.push_back(v);
+        }
+    }
     LMG_CUDA(c, dupload(c, c->d_D6, D.data(), D.size()));
   }
   c->kappa = form == LMG_ADVDIFF ? params[0] : 0.0;

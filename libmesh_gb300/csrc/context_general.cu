@@ -104,6 +104,7 @@ lmg_status general_plan(lmg_ctx *c) {
   int64_t kr = E * (int64_t)N * N, fr = E * (int64_t)N;  // enlarged regions start after the raw ones
   std::vector<int32_t> dofs;
   std::vector<std::vector<std::pair<int, double>>> col;
+  int max_ne = 0, max_ent = 0;
   for (int64_t e = 0; e < E; ++e) {
     const int32_t *ed = &c->h_elem_dofs[(size_t)(e * N)];
     bool any = false;
@@ -148,6 +149,8 @@ lmg_status general_plan(lmg_ctx *c) {
       int n_ent = 0;
       for (auto &cl : col) n_ent += (int)cl.size();
       if (n_ent > GEN_MAX_ENTRIES) return fail(c, LMG_ERR_UNSUPPORTED, "constraint matrix too large", e);
+      max_ne = std::max(max_ne, ne);
+      max_ent = std::max(max_ent, n_ent);
       celem.push_back((int32_t)e);
       cne.push_back(ne);
       ckout.push_back(kr);
@@ -230,6 +233,8 @@ lmg_status general_plan(lmg_ctx *c) {
       foff[(size_t)t] = (uint32_t)(fbase[(size_t)ie[(size_t)t]] + ip[(size_t)t]);
   general_free(c);
   c->n_cons_elem = (int64_t)celem.size();
+  c->cons_max_ne = max_ne;
+  c->cons_max_ent = max_ent;
   LMG_CUDA(c, dupload(c, c->d_cptr, cptr.data(), cptr.size()));
   LMG_CUDA(c, dupload(c, c->d_coff, coff.data(), coff.size()));
   LMG_CUDA(c, dupload(c, c->d_gfptr, iptr.data(), iptr.size()));
@@ -273,6 +278,8 @@ lmg_status general_assemble(lmg_ctx *c) {
     ConsArgs k{};
     k.n_cons = c->n_cons_elem;
     k.N = c->nl;
+    k.max_ne = c->cons_max_ne;
+    k.max_ent = c->cons_max_ent;
     k.elem = c->d_celem;
     k.ne = c->d_cne;
     k.kout = c->d_ckout;

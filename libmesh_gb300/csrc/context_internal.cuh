@@ -73,6 +73,7 @@ struct lmg_ctx {
   int64_t *d_cptr = nullptr, *d_gfptr = nullptr;
   uint32_t *d_coff = nullptr, *d_gfoff = nullptr;
   int64_t n_cons_elem = 0;
+  int cons_max_ne = 0, cons_max_ent = 0;
   int32_t *d_celem = nullptr, *d_cne = nullptr, *d_ccp = nullptr;
   int64_t *d_ckout = nullptr, *d_cfout = nullptr, *d_cbase = nullptr, *d_cebase = nullptr;
   uint8_t *d_cci = nullptr;

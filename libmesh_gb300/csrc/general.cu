@@ -10,10 +10,12 @@
 //   SparseMatrix::add_matrix / add_vector        src/numerics/petsc_matrix.C:735-755
 //
 // Element kernel: one warp per element, lane b computes column b of Ke.
-// Affine elements only: the diffusion block is the reference-tensor
+// Affine hexahedra only: the diffusion block is the reference-tensor
 // contraction K_ab = sum_k A_k D^k_ab (D = symmetrized sum_q w dphi_m dphi_n
 // tables), the convection block C_ab = sum_q phi_a(q) sum_m beta_m(q) dphi_m,b(q)
-// with beta_m(q) = w_q detJ (dxi_m/dx . b(x_q)).  All FP64.
+// with beta_m(q) = w_q detJ (dxi_m/dx . b(x_q)), summed over q by sum
+// factorization (phi_a(q) is a product of 1-D shapes on the tensor Gauss
+// rule).  All FP64.
 //
 // Constraint kernel: one CTA per constrained element.  K' = C^T K C over the
 // element's dofs followed by its constraining dofs (sorted), with C given by
@@ -37,8 +39,68 @@ __device__ __forceinline__ double warp_allsum(double v) {
   return v;
 }
 
+// Tensor indices of a hex node in the 1-D Lagrange bases (0 at -1, 1 at +1,
+// 2 at 0), packed as i + 3 j + 9 k: HEX27 node order of cell_hex27.C, HEX8
+// node order of cell_hex8.C.
+__host__ __device__ constexpr int hex_tensor(int n, int a) {
+  if (n == 8) {
+    switch (a) {
+      case 0: return 0;  case 1: return 1;  case 2: return 4;  case 3: return 3;
+      case 4: return 9;  case 5: return 10; case 6: return 13; default: return 12;
+    }
+  }
+  switch (a) {
+    case 0: return 0;   case 1: return 1;   case 2: return 4;   case 3: return 3;   case 4: return 9;
+    case 5: return 10;  case 6: return 13;  case 7: return 12;  case 8: return 2;   case 9: return 7;
+    case 10: return 5;  case 11: return 6;  case 12: return 18; case 13: return 19; case 14: return 22;
+    case 15: return 21; case 16: return 11; case 17: return 16; case 18: return 14; case 19: return 15;
+    case 20: return 8;  case 21: return 20; case 22: return 25; case 23: return 23; case 24: return 24;
+    case 25: return 17; default: return 26;
+  }
+}
+
+// C_rb = sum_q phi_r(q) P(q) for the tensor-product element: phi_r(q) =
+// L_i(x_q1) L_j(x_q2) L_k(x_q3), q = q1 + Q1 (q2 + Q1 q3); three 1-D passes.
+template <int N1, int Q1>
+__device__ __forceinline__ void tensor_contract(const double *L1, const double *P, double *Cc) {
+  double T1[N1 * Q1 * Q1];
+#pragma unroll
+  for (int i = 0; i < N1; ++i)
+#pragma unroll
+    for (int r = 0; r < Q1 * Q1; ++r) {
+      double t = 0.0;
+#pragma unroll
+      for (int q1 = 0; q1 < Q1; ++q1) t += L1[i * Q1 + q1] * P[q1 + Q1 * r];
+      T1[i * Q1 * Q1 + r] = t;
+    }
+  double T2[N1 * N1 * Q1];
+#pragma unroll
+  for (int i = 0; i < N1; ++i)
+#pragma unroll
+    for (int j = 0; j < N1; ++j)
+#pragma unroll
+      for (int q3 = 0; q3 < Q1; ++q3) {
+        double t = 0.0;
+#pragma unroll
+        for (int q2 = 0; q2 < Q1; ++q2) t += L1[j * Q1 + q2] * T1[i * Q1 * Q1 + q2 + Q1 * q3];
+        T2[(i * N1 + j) * Q1 + q3] = t;
+      }
+#pragma unroll
+  for (int i = 0; i < N1; ++i)
+#pragma unroll
+    for (int j = 0; j < N1; ++j)
+#pragma unroll
+      for (int k = 0; k < N1; ++k) {
+        double t = 0.0;
+#pragma unroll
+        for (int q3 = 0; q3 < Q1; ++q3) t += L1[k * Q1 + q3] * T2[(i * N1 + j) * Q1 + q3];
+        Cc[i + 3 * j + 9 * k] = t;
+      }
+}
+
 template <int FORM, int N, int Q>
 __global__ void __launch_bounds__(WARPS * 32) k_elem_full(GenElemArgs a) {
+  constexpr int N1 = (N == 8) ? 2 : 3, Q1 = (Q == 8) ? 2 : 3;
   extern __shared__ double sm[];
   double *sphi = sm;                  // [Q][N]
   double *sdphi = sphi + Q * N;       // [Q][N][3]
@@ -58,6 +120,8 @@ __global__ void __launch_bounds__(WARPS * 32) k_elem_full(GenElemArgs a) {
   for (int i = threadIdx.x; i < Q; i += blockDim.x) sqw[i] = a.fe.qw[i];
   for (int i = threadIdx.x; i < N * 3; i += blockDim.x) sgd[i] = a.fe.gdphi[i];
   for (int i = threadIdx.x; i < 7 * a.n_modes; i += blockDim.x) smode[i] = a.modes[i];
+  __shared__ double sL1[9];
+  for (int i = threadIdx.x; i < N1 * Q1; i += blockDim.x) sL1[i] = a.D6[6 * N * N + i];
   __syncthreads();
   const int64_t stride = (int64_t)gridDim.x * WARPS;
   for (int64_t e = (int64_t)blockIdx.x * WARPS + warp; e < a.n_elem; e += stride) {
@@ -149,15 +213,20 @@ __global__ void __launch_bounds__(WARPS * 32) k_elem_full(GenElemArgs a) {
           P[q] = sbeta[3 * q] * d[0] + sbeta[3 * q + 1] * d[1] + sbeta[3 * q + 2] * d[2];
         }
       }
+      double Cc[27];
+      if (FORM == LMG_ADVDIFF) {
+        double L1[N1 * Q1];
+#pragma unroll
+        for (int i = 0; i < N1 * Q1; ++i) L1[i] = sL1[i];
+        tensor_contract<N1, Q1>(L1, P, Cc);
+      }
       double *Ke = a.Kraw + e * (N * N);
+#pragma unroll
       for (int r = 0; r < N; ++r) {
         double k = A[0] * sD[r * N + b];
 #pragma unroll
         for (int t = 1; t < 6; ++t) k += A[t] * sD[(t * N + r) * N + b];
-        if (FORM == LMG_ADVDIFF) {
-#pragma unroll
-          for (int q = 0; q < Q; ++q) k += sphi[q * N + r] * P[q];
-        }
+        if (FORM == LMG_ADVDIFF) k += Cc[hex_tensor(N, r)];
         Ke[r * N + b] = k;
       }
       double fe = 0.0;
@@ -183,13 +252,17 @@ void launch_full(const GenElemArgs &a, int n_sm, cudaStream_t s) {
   if (grid > 0) k_elem_full<FORM, N, Q><<<grid, WARPS * 32, smem, s>>>(a);
 }
 
+// Dynamic shared memory: K [N][N], F [N], L = C^T K [max_ne][N], coefficients
+// [max_ent], column pointers [max_ne + 1], row indices [max_ent].
 __global__ void __launch_bounds__(128) k_constrain(ConsArgs c) {
-  __shared__ double sK[GEN_MAX_N * GEN_MAX_N];
-  __shared__ double sF[GEN_MAX_N];
-  __shared__ int32_t scp[GEN_MAX_NE + 1];
-  __shared__ uint8_t sci[GEN_MAX_ENTRIES];
-  __shared__ double scv[GEN_MAX_ENTRIES];
+  extern __shared__ double csm[];
   const int N = c.N;
+  double *sK = csm;
+  double *sF = sK + N * N;
+  double *sL = sF + N;
+  double *scv = sL + c.max_ne * N;
+  int32_t *scp = reinterpret_cast<int32_t *>(scv + c.max_ent);
+  uint8_t *sci = reinterpret_cast<uint8_t *>(scp + c.max_ne + 1);
   for (int64_t k = blockIdx.x; k < c.n_cons; k += gridDim.x) {
     const int64_t e = c.elem[k];
     const int ne = c.ne[k];
@@ -206,6 +279,15 @@ __global__ void __launch_bounds__(128) k_constrain(ConsArgs c) {
       scv[i] = c.cv[eb + i];
     }
     __syncthreads();
+    // L_pj = sum_i C_ip K_ij (rows of constrained local dofs are replaced below)
+    for (int idx = threadIdx.x; idx < ne * N; idx += blockDim.x) {
+      const int p = idx / N, j = idx - p * N;
+      double l = 0.0;
+      if (!(p < N && ((rows >> p) & 1ull)))
+        for (int u = scp[p]; u < scp[p + 1]; ++u) l += scv[u] * sK[sci[u] * N + j];
+      sL[idx] = l;
+    }
+    __syncthreads();
     double *out = c.Ebuf + c.kout[k];
     for (int idx = threadIdx.x; idx < ne * ne; idx += blockDim.x) {
       const int p = idx / ne, q = idx - p * ne;
@@ -218,12 +300,8 @@ __global__ void __launch_bounds__(128) k_constrain(ConsArgs c) {
             if (sci[t] == p) v = -scv[t];
         }
       } else {
-        for (int t = scp[q]; t < scp[q + 1]; ++t) {
-          const int j = sci[t];
-          double l = 0.0;
-          for (int u = scp[p]; u < scp[p + 1]; ++u) l += scv[u] * sK[sci[u] * N + j];
-          v += l * scv[t];
-        }
+        const double *lp = sL + p * N;
+        for (int t = scp[q]; t < scp[q + 1]; ++t) v += lp[sci[t]] * scv[t];
       }
       out[idx] = v;
     }
@@ -280,7 +358,14 @@ void launch_gen_elements(int form, int n, int q, const GenElemArgs &a, int n_sm,
 void launch_constrain(const ConsArgs &c, int n_sm, cudaStream_t s) {
   if (c.n_cons <= 0) return;
   const int64_t g = c.n_cons < (int64_t)n_sm * 16 ? c.n_cons : (int64_t)n_sm * 16;
-  k_constrain<<<(int)g, 128, 0, s>>>(c);
+  const size_t smem = sizeof(double) * ((size_t)c.N * c.N + c.N + (size_t)c.max_ne * c.N + c.max_ent) +
+                      sizeof(int32_t) * (c.max_ne + 1) + c.max_ent;
+  static size_t attr = 0;
+  if (smem > attr) {
+    cudaFuncSetAttribute(k_constrain, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    attr = smem;
+  }
+  k_constrain<<<(int)g, 128, smem, s>>>(c);
 }
 
 void launch_gather_full(int64_t nnz, const int64_t *cptr, const uint32_t *coff, const double *E, double *K,

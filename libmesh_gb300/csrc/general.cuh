@@ -34,6 +34,8 @@ struct GenElemArgs {
 struct ConsArgs {
   int64_t n_cons;
   int N;
+  int max_ne;                 // largest ne over the constrained elements
+  int max_ent;                // largest entry count over the constrained elements
   const int32_t *elem;        // [n_cons] element id
   const int32_t *ne;          // [n_cons] dofs after enlargement
   const int64_t *kout;        // [n_cons] offset of the ne x ne result in Ebuf
