@@ -552,6 +552,8 @@ lmg_status lmg_form_set(lmg_ctx *c, int32_t form, int32_t fe_order, int32_t q_or
         const int id[3] = {q % q1n, (q / q1n) % q1n, q / (q1n * q1n)};
         for (int d = 0; d < 3; ++d) tensor = tensor && t.qp[3 * q + d] == t.qp[3 * id[d]];
       }
+      // symmetric 1-D points: -g, +g (two) or -g, 0, +g (three)
+      tensor = tensor && t.qp[0] == -t.qp[3 * (q1n - 1)] && t.qp[0] < 0.0 && (q1n == 2 || t.qp[3] == 0.0);
       if (!tensor) return fail(c, LMG_ERR_UNSUPPORTED, "form_set: the convection kernel needs a tensor Gauss rule");
       for (int i = 0; i < n1; ++i)
         for (int q1 = 0; q1 < q1n; ++q1) {
@@ -561,6 +563,7 @@ lmg_status lmg_form_set(lmg_ctx *c, int32_t form, int32_t fe_order, int32_t q_or
           else v = i == 0 ? .5 * x * (x - 1.) : (i == 1 ? .5 * x * (x + 1.) : (1. - x) * (1. + x));
           D.push_back(v);
         }
+      D.push_back(t.qp[3 * (q1n - 1)]);  // outer 1-D Gauss point
     }
     LMG_CUDA(c, dupload(c, c->d_D6, D.data(), D.size()));
   }

@@ -110,10 +110,11 @@ __global__ void __launch_bounds__(WARPS * 32) k_elem_full(GenElemArgs a) {
   double *smode = sgd + N * 3;        // [7 * n_modes]
   double *wbase = smode + 7 * a.n_modes;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  double *sX = wbase + warp * (N * 3 + N + 4 * Q);  // [N][3]
+  double *sX = wbase + warp * (N * 3 + N + 4 * Q + 8 * a.n_modes);  // [N][3]
   double *sf = sX + N * 3;                            // [N]
   double *sbeta = sf + N;                             // [Q][3]
   double *sfq = sbeta + 3 * Q;                        // [Q]
+  double *sE = sfq + Q;                               // [n_modes][4] (cos, sin)
   for (int i = threadIdx.x; i < Q * N; i += blockDim.x) sphi[i] = a.fe.phi[i];
   for (int i = threadIdx.x; i < Q * N * 3; i += blockDim.x) sdphi[i] = a.fe.dphi[i];
   for (int i = threadIdx.x; i < 6 * N * N; i += blockDim.x) sD[i] = a.D6[i];
@@ -122,6 +123,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_elem_full(GenElemArgs a) {
   for (int i = threadIdx.x; i < 7 * a.n_modes; i += blockDim.x) smode[i] = a.modes[i];
   __shared__ double sL1[9];
   for (int i = threadIdx.x; i < N1 * Q1; i += blockDim.x) sL1[i] = a.D6[6 * N * N + i];
+  const double gp = a.D6[6 * N * N + N1 * Q1];  // outer 1-D Gauss point (+gp, -gp, and 0 when Q1 = 3)
   __syncthreads();
   const int64_t stride = (int64_t)gridDim.x * WARPS;
   for (int64_t e = (int64_t)blockIdx.x * WARPS + warp; e < a.n_elem; e += stride) {
@@ -175,6 +177,28 @@ __global__ void __launch_bounds__(WARPS * 32) k_elem_full(GenElemArgs a) {
     A[4] = kap * (G[0] * G[6] + G[1] * G[7] + G[2] * G[8]);
     A[5] = kap * (G[3] * G[6] + G[4] * G[7] + G[5] * G[8]);
     __syncwarp();
+    if (FORM == LMG_ADVDIFF) {
+      // exp(i (k.x + phase)) at the element centre and exp(i gp k.dx/dxi_m):
+      // the phase is affine in xi, so every Gauss point's value is a product
+      // of these (angle addition) -- four sincos per mode, one per lane.
+      const double xc[3] = {0.5 * (sX[0] + sX[18]), 0.5 * (sX[1] + sX[19]), 0.5 * (sX[2] + sX[20])};
+      for (int t = lane; t < 4 * a.n_modes; t += 32) {
+        const double *md = smode + 7 * (t >> 2);
+        const int w = t & 3;
+        double ang;
+        if (w == 0) {
+          ang = md[3] * xc[0] + md[4] * xc[1] + md[5] * xc[2] + md[6];
+        } else {
+          const int m = w - 1;
+          ang = gp * (md[3] * jp[3 * m] + md[4] * jp[3 * m + 1] + md[5] * jp[3 * m + 2]);
+        }
+        double sn, cs;
+        sincos(ang, &sn, &cs);
+        sE[2 * t] = cs;
+        sE[2 * t + 1] = sn;
+      }
+      __syncwarp();
+    }
     // per quadrature point: transport coefficients and the load
     if (lane < Q) {
       const int q = lane;
@@ -190,9 +214,21 @@ __global__ void __launch_bounds__(WARPS * 32) k_elem_full(GenElemArgs a) {
       sfq[q] = jxw * fx;
       if (FORM == LMG_ADVDIFF) {
         double b[3] = {0.0, 0.0, 0.0};
+        // offset of this point along each reference axis: -1, 0 or +1 times gp
+        const int qi[3] = {q % Q1, (q / Q1) % Q1, q / (Q1 * Q1)};
         for (int m = 0; m < a.n_modes; ++m) {
           const double *md = smode + 7 * m;
-          const double cs = cos(md[3] * xq[0] + md[4] * xq[1] + md[5] * xq[2] + md[6]);
+          const double *E = sE + 8 * m;
+          double re = E[0], im = E[1];
+#pragma unroll
+          for (int d = 0; d < 3; ++d) {
+            if (Q1 == 3 && qi[d] == 1) continue;
+            const double c = E[2 * (d + 1)], sn = qi[d] == 0 ? -E[2 * (d + 1) + 1] : E[2 * (d + 1) + 1];
+            const double r2 = re * c - im * sn;
+            im = re * sn + im * c;
+            re = r2;
+          }
+          const double cs = re;
           b[0] += cs * (md[4] * md[2] - md[5] * md[1]);
           b[1] += cs * (md[5] * md[0] - md[3] * md[2]);
           b[2] += cs * (md[3] * md[1] - md[4] * md[0]);
@@ -241,7 +277,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_elem_full(GenElemArgs a) {
 template <int FORM, int N, int Q>
 void launch_full(const GenElemArgs &a, int n_sm, cudaStream_t s) {
   const size_t smem = sizeof(double) * ((size_t)Q * N * 4 + 6 * N * N + Q + N * 3 + 7 * a.n_modes +
-                                        (size_t)WARPS * (N * 3 + N + 4 * Q));
+                                        (size_t)WARPS * (N * 3 + N + 4 * Q + 8 * a.n_modes));
   static size_t attr = 0;  // largest dynamic shared memory granted so far
   if (smem > attr) {
     cudaFuncSetAttribute(k_elem_full<FORM, N, Q>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
