@@ -199,7 +199,13 @@ lmg_status lmg_constraint_rows_upload(lmg_ctx *ctx, const uint8_t *constrained, 
 lmg_status lmg_sparsity_build(lmg_ctx *ctx, int64_t *nnz);
 lmg_status lmg_sparsity_copy(lmg_ctx *ctx, int32_t *row_ptr, int32_t *col_idx);
 
-/* Weak form and its data.  fe_order: 1 FIRST / 2 SECOND LAGRANGE.
+/* FE family flag OR'ed into fe_order (libMesh FEType{order, family}):
+ * LMG_HIERARCHIC selects HIERARCHIC (FIRST on HEX8, SECOND on HEX27; shapes of
+ * src/fe/fe_hierarchic_shape_3D.C, derivatives by central differences as
+ * FE<3,HIERARCHIC>::shape_deriv takes them).  Without it the family is LAGRANGE. */
+enum { LMG_HIERARCHIC = 0x100 };
+
+/* Weak form and its data.  fe_order: 1 FIRST / 2 SECOND LAGRANGE (| LMG_HIERARCHIC).
  * q_order: QGauss order (libMesh Order value).  params: POISSON none;
  * ELASTICITY {nu}; ADVDIFF {kappa, n_modes, then per mode a[3], k[3], phase}
  * (one variable, affine elements, LMG_FP64).  elem_coef[n_elem]: k_e (POISSON) or E_e (ELASTICITY),

@@ -14,13 +14,13 @@ import ctypes as C
 import numpy as np
 
 from . import _capi
-from ._capi import (ADVDIFF, ELASTICITY, FP64, HEX8, HEX27, MIXED, POISSON, PRISM6, TET4, TET10,
+from ._capi import (ADVDIFF, ELASTICITY, FP64, HEX8, HEX27, HIERARCHIC, MIXED, POISSON, PRISM6, TET4, TET10,
                     DegenerateMap, LmgError, check, lib, ptr)
 
 FIRST, SECOND, THIRD, FOURTH, FIFTH = 1, 2, 3, 4, 5
 
 __all__ = ["Mesh", "DofMap", "GpuAssembly", "LinearImplicitSystem", "DegenerateMap", "LmgError",
-           "HEX8", "HEX27", "TET4", "TET10", "PRISM6", "POISSON", "ELASTICITY", "ADVDIFF", "FP64", "MIXED",
+           "HEX8", "HEX27", "TET4", "TET10", "PRISM6", "POISSON", "ELASTICITY", "ADVDIFF", "FP64", "MIXED", "HIERARCHIC",
            "FIRST", "SECOND", "THIRD", "FOURTH", "FIFTH"]
 
 

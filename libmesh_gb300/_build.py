@@ -50,12 +50,15 @@ def build(verbose=False, force=False):
     for s in CXX_SOURCES:
         o = os.path.join(OUT, "obj", s + ".o")
         objs.append(o)
-        jobs.append(["g++", "-std=c++17", "-O3", "-fPIC", "-pthread", "-Wall", "-c",
+        # -ffp-contract=off: host tables (central-difference derivatives, refined
+        # coordinates, constraint rows) round identically on x86-64 and aarch64,
+        # where g++ would otherwise fuse multiply-adds
+        jobs.append(["g++", "-std=c++17", "-O3", "-ffp-contract=off", "-fPIC", "-pthread", "-Wall", "-c",
                      os.path.join(SRC, s), "-o", o])
     for s in CU_SOURCES:
         o = os.path.join(OUT, "obj", s + ".o")
         objs.append(o)
-        jobs.append([nvcc, "-std=c++17", "-O3", *ARCH, "-lineinfo", "-Xcompiler", "-fPIC",
+        jobs.append([nvcc, "-std=c++17", "-O3", *ARCH, "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off",
                      "--expt-relaxed-constexpr", "-c", os.path.join(SRC, s), "-o", o])
     with ThreadPoolExecutor(max_workers=max(2, min(8, os.cpu_count() or 2))) as ex:
         logs = list(ex.map(_run, jobs))

@@ -18,6 +18,8 @@ TET4, TET10, HEX8, HEX27, PRISM6 = 8, 9, 10, 12, 13
 # forms and precisions
 POISSON, ELASTICITY, ADVDIFF = 0, 1, 2
 FP64, MIXED = 0, 1
+# FE family flag OR'ed into fe_order
+HIERARCHIC = 0x100
 # work-space limit of lmg_cg_solve_noalloc
 CG_NOALLOC_MAX_DOFS = 524288
 

@@ -13,6 +13,7 @@ struct DevFE {
   const double *phi;    // [q][n]
   const double *dphi;   // [q][n][3]
   const double *gdphi;  // [q][n_geo][3]
+  const double *gphi;   // [q][n_geo] mapping shapes
   const double *S;      // [9][n][n]
   const double *M;      // [n][n]
 };

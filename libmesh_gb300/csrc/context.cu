@@ -515,8 +515,10 @@ lmg_status lmg_form_set(lmg_ctx *c, int32_t form, int32_t fe_order, int32_t q_or
       return fail(c, LMG_ERR_ARG, "form_set: ADVDIFF parameter count does not match n_modes");
   }
   cudaSetDevice(c->device);
+  const int family = (fe_order & LMG_HIERARCHIC) ? 1 : 0;
+  fe_order &= 0xff;
   FETables t;
-  std::string err = build_fe_tables(t, c->elem_type, fe_order, q_order);
+  std::string err = build_fe_tables(t, c->elem_type, fe_order, q_order, family);
   if (!err.empty()) return fail(c, LMG_ERR_UNSUPPORTED, "form_set: " + err);
   if (t.n != c->npe || t.n_geo != c->npe)
     return fail(c, LMG_ERR_UNSUPPORTED, "form_set: only isoparametric LAGRANGE elements are built");
@@ -560,6 +562,7 @@ lmg_status lmg_form_set(lmg_ctx *c, int32_t form, int32_t fe_order, int32_t q_or
           const double x = t.qp[3 * q1];
           double v;
           if (n1 == 2) v = i == 0 ? .5 * (1. - x) : .5 * (1. + x);
+          else if (family == 1) v = i == 0 ? .5 * (1. - x) : (i == 1 ? .5 * (1. + x) : (x * x - 1.) / 2.);
           else v = i == 0 ? .5 * x * (x - 1.) : (i == 1 ? .5 * x * (x + 1.) : (1. - x) * (1. + x));
           D.push_back(v);
         }
@@ -581,7 +584,7 @@ lmg_status lmg_form_set(lmg_ctx *c, int32_t form, int32_t fe_order, int32_t q_or
   std::vector<double> buf;
   auto put = [&](const std::vector<double> &v) { size_t o = buf.size(); buf.insert(buf.end(), v.begin(), v.end()); return o; };
   const size_t oqw = put(t.qw), ophi = put(t.phi), odphi = put(t.dphi), ogd = put(t.gdphi),
-               oS = put(t.S), oM = put(t.M);
+               oS = put(t.S), oM = put(t.M), ogp = put(t.gphi);
   LMG_CUDA(c, dupload(c, c->d_tab, buf.data(), buf.size()));
   c->dfe.n = t.n;
   c->dfe.q = t.q;
@@ -592,6 +595,7 @@ lmg_status lmg_form_set(lmg_ctx *c, int32_t form, int32_t fe_order, int32_t q_or
   c->dfe.gdphi = c->d_tab + ogd;
   c->dfe.S = c->d_tab + oS;
   c->dfe.M = c->d_tab + oM;
+  c->dfe.gphi = c->d_tab + ogp;
   dfree(c->d_coef);
   dfree(c->d_f);
   if (elem_coef) LMG_CUDA(c, dupload(c, c->d_coef, elem_coef, (size_t)c->n_elem));

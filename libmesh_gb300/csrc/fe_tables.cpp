@@ -145,14 +145,60 @@ int lagrange_shapes(int type, int order, const double *p, double *v, double *g) 
   return 0;
 }
 
+// fe_hierarchic_1D_shape (src/fe/fe_hierarchic_shape_1D.C:430-498): linear
+// end functions, then (xi^i - 1)/i! (even i) and (xi^i - xi)/i! (odd i).
+double hier1d(int i, double xi) {
+  switch (i) {
+    case 0: return .5 * (1. - xi);
+    case 1: return .5 * (1. + xi);
+    case 2: return (xi * xi - 1.) / 2.;
+    default: return (xi * xi * xi - xi) / 6.;
+  }
+}
+
+// HIERARCHIC hex shapes for p <= 2 (fe_hierarchic_shape_3D.C:2249-2290 with
+// cube_indices, :166-760): the tensor index of dof i is the HEX27 node index
+// table (vertices, one edge dof per edge, one dof per face, one interior dof),
+// and the bases are even in every coordinate, so the edge / face orientation
+// flips of cube_indices leave them unchanged.  Value = (s0 s1) s2;
+// derivative = (shape(p + eps e_j) - shape(p - eps e_j)) / 2. / eps with
+// eps = 1e-6 (fe_fdm_deriv, src/fe/fe.C:794-811, 929-944).
+int hierarchic_shapes(int type, int order, const double *p, double *v, double *g) {
+  if (!((type == LMG_HEX8 && order == 1) || (type == LMG_HEX27 && order == 2))) return 0;
+  const int n = (order == 1) ? 8 : 27;
+  auto shape = [&](int a, const double *x) {
+    const int i0 = (order == 1) ? HEX8_I[0][a] : HEX27_I[0][a], i1 = (order == 1) ? HEX8_I[1][a] : HEX27_I[1][a],
+              i2 = (order == 1) ? HEX8_I[2][a] : HEX27_I[2][a];
+    return hier1d(i0, x[0]) * hier1d(i1, x[1]) * hier1d(i2, x[2]);
+  };
+  const double eps = 1.e-6;
+  for (int a = 0; a < n; ++a) {
+    v[a] = shape(a, p);
+    for (int j = 0; j < 3; ++j) {
+      double pp[3] = {p[0], p[1], p[2]}, pm[3] = {p[0], p[1], p[2]};
+      pp[j] += eps;
+      pm[j] -= eps;
+      g[3 * a + j] = (shape(a, pp) - shape(a, pm)) / 2. / eps;
+    }
+  }
+  return n;
+}
+
 }  // namespace
 
-std::string build_fe_tables(FETables &t, int type, int fe_order, int q_order) {
+std::string build_fe_tables(FETables &t, int type, int fe_order, int q_order, int family) {
   t = FETables();
   t.elem_type = type;
   t.fe_order = fe_order;
   t.q_order = q_order;
+  t.family = family;
   if (fe_order < 1 || fe_order > 2) return "fe_order must be FIRST or SECOND";
+  if (family != 0 && family != 1) return "unknown FE family";
+  if (family == 1 && !((type == LMG_HEX8 && fe_order == 1) || (type == LMG_HEX27 && fe_order == 2)))
+    return "HIERARCHIC is built for FIRST on HEX8 and SECOND on HEX27";
+  auto fe_shapes = [&](const double *p, double *v, double *g) {
+    return family == 1 ? hierarchic_shapes(type, fe_order, p, v, g) : lagrange_shapes(type, fe_order, p, v, g);
+  };
   const bool hex = (type == LMG_HEX8 || type == LMG_HEX27);
   const bool tet = (type == LMG_TET4 || type == LMG_TET10);
   if (!hex && !tet) return "unsupported element type";
@@ -173,7 +219,7 @@ std::string build_fe_tables(FETables &t, int type, int fe_order, int q_order) {
   }
   t.q = (int)t.qw.size();
   double v[27], g[81];
-  t.n = lagrange_shapes(type, fe_order, &t.qp[0], v, g);
+  t.n = fe_shapes(&t.qp[0], v, g);
   t.n_geo = lagrange_shapes(type, geo_order, &t.qp[0], v, g);
   if (!t.n || !t.n_geo) return "unsupported element type / order";
   t.phi.resize((size_t)t.q * t.n);
@@ -181,7 +227,7 @@ std::string build_fe_tables(FETables &t, int type, int fe_order, int q_order) {
   t.gphi.resize((size_t)t.q * t.n_geo);
   t.gdphi.resize((size_t)t.q * t.n_geo * 3);
   for (int q = 0; q < t.q; ++q) {
-    lagrange_shapes(type, fe_order, &t.qp[3 * q], v, g);
+    fe_shapes(&t.qp[3 * q], v, g);
     for (int a = 0; a < t.n; ++a) {
       t.phi[(size_t)q * t.n + a] = v[a];
       for (int m = 0; m < 3; ++m) t.dphi[((size_t)q * t.n + a) * 3 + m] = g[3 * a + m];

@@ -107,7 +107,8 @@ __global__ void __launch_bounds__(WARPS * 32) k_elem_full(GenElemArgs a) {
   double *sD = sdphi + Q * N * 3;     // [6][N][N]
   double *sqw = sD + 6 * N * N;       // [Q]
   double *sgd = sqw + Q;              // [N][3] mapping derivatives at qp 0
-  double *smode = sgd + N * 3;        // [7 * n_modes]
+  double *sgp = sgd + N * 3;          // [Q][N] mapping shapes (isoparametric geometry)
+  double *smode = sgp + Q * N;        // [7 * n_modes]
   double *wbase = smode + 7 * a.n_modes;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   double *sX = wbase + warp * (N * 3 + N + 4 * Q + 8 * a.n_modes);  // [N][3]
@@ -120,6 +121,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_elem_full(GenElemArgs a) {
   for (int i = threadIdx.x; i < 6 * N * N; i += blockDim.x) sD[i] = a.D6[i];
   for (int i = threadIdx.x; i < Q; i += blockDim.x) sqw[i] = a.fe.qw[i];
   for (int i = threadIdx.x; i < N * 3; i += blockDim.x) sgd[i] = a.fe.gdphi[i];
+  for (int i = threadIdx.x; i < Q * N; i += blockDim.x) sgp[i] = a.fe.gphi[i];
   for (int i = threadIdx.x; i < 7 * a.n_modes; i += blockDim.x) smode[i] = a.modes[i];
   __shared__ double sL1[9];
   for (int i = threadIdx.x; i < N1 * Q1; i += blockDim.x) sL1[i] = a.D6[6 * N * N + i];
@@ -204,11 +206,11 @@ __global__ void __launch_bounds__(WARPS * 32) k_elem_full(GenElemArgs a) {
       const int q = lane;
       double xq[3] = {0.0, 0.0, 0.0}, fx = 0.0;
       for (int c = 0; c < N; ++c) {
-        const double s = sphi[q * N + c];  // isoparametric: mapping shapes = FE shapes
-        xq[0] += s * sX[3 * c];
-        xq[1] += s * sX[3 * c + 1];
-        xq[2] += s * sX[3 * c + 2];
-        fx += s * sf[c];
+        const double g = sgp[q * N + c], s = sphi[q * N + c];
+        xq[0] += g * sX[3 * c];
+        xq[1] += g * sX[3 * c + 1];
+        xq[2] += g * sX[3 * c + 2];
+        fx += s * sf[c];   // the load is interpolated with the FE shapes
       }
       const double jxw = det * sqw[q];
       sfq[q] = jxw * fx;
@@ -276,7 +278,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_elem_full(GenElemArgs a) {
 
 template <int FORM, int N, int Q>
 void launch_full(const GenElemArgs &a, int n_sm, cudaStream_t s) {
-  const size_t smem = sizeof(double) * ((size_t)Q * N * 4 + 6 * N * N + Q + N * 3 + 7 * a.n_modes +
+  const size_t smem = sizeof(double) * ((size_t)Q * N * 5 + 6 * N * N + Q + N * 3 + 7 * a.n_modes +
                                         (size_t)WARPS * (N * 3 + N + 4 * Q + 8 * a.n_modes));
   static size_t attr = 0;  // largest dynamic shared memory granted so far
   if (smem > attr) {

@@ -95,6 +95,7 @@ struct SplitMix64 {
 // Reference-element data for one (element type, FE order, quadrature order).
 struct FETables {
   int elem_type = 0, fe_order = 0, q_order = 0;
+  int family = 0;  // 0 LAGRANGE, 1 HIERARCHIC
   int n = 0;       // shape functions
   int q = 0;       // quadrature points
   int n_geo = 0;   // mapping shape functions (element default order)
@@ -107,7 +108,9 @@ struct FETables {
   std::vector<double> S;         // [3][3][n][n]: sum_q w dphi_a/dxi_m dphi_b/dxi_n
   std::vector<double> M;         // [n][n]: sum_q w phi_a phi_b
 };
-std::string build_fe_tables(FETables &t, int elem_type, int fe_order, int q_order);
+// family 1 (HIERARCHIC, hexahedra, p <= 2): products of the 1-D hierarchic
+// shapes, reference derivatives by libMesh's central differences (eps = 1e-6).
+std::string build_fe_tables(FETables &t, int elem_type, int fe_order, int q_order, int family = 0);
 
 // libMesh Elem::has_affine_map for one element (cell_hex8.C:121, cell_hex27.C:125,
 // cell_tet4 always, cell_tet10.C:143).

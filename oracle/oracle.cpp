@@ -239,6 +239,73 @@ void all_shapes(int type, int order, const std::vector<Pt> &pts, std::vector<std
   }
 }
 
+// ------------------------------------------------------------------ HIERARCHIC
+// fe_hierarchic_1D_shape (src/fe/fe_hierarchic_shape_1D.C:430-498).
+double hier_1d(unsigned i, double xi) {
+  double returnval = 1.;
+  switch (i) {
+    case 0: returnval = .5 * (1. - xi); break;
+    case 1: returnval = .5 * (1. + xi); break;
+    case 2: returnval = (xi * xi - 1.) / 2.; break;
+    case 3: returnval = (xi * xi * xi - xi) / 6.; break;
+    default: {
+      double denominator = 1.;
+      for (unsigned n = 1; n <= i; ++n) {
+        returnval *= xi;
+        denominator *= n;
+      }
+      returnval = (i % 2) ? (returnval - xi) / denominator : (returnval - 1.) / denominator;
+    }
+  }
+  return returnval;
+}
+
+// cube_indices (fe_hierarchic_shape_3D.C:166-760) for totalorder <= 2: vertex
+// dofs 0-7, edge dofs 8-19 (e = 1 per edge), face dofs 20-25, interior 26.
+// The edge / face flips it applies negate or swap arguments of even 1-D
+// functions at this order, which leaves every value unchanged, so they are
+// not restated.
+void cube_indices_p2(unsigned i, unsigned &i0, unsigned &i1, unsigned &i2) {
+  static const unsigned V[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0},
+                                   {0, 0, 1}, {1, 0, 1}, {1, 1, 1}, {0, 1, 1}};
+  static const unsigned EF[19][3] = {  // i = 8 .. 26
+      {2, 0, 0}, {1, 2, 0}, {2, 1, 0}, {0, 2, 0}, {0, 0, 2}, {1, 0, 2}, {1, 1, 2}, {0, 1, 2}, {2, 0, 1},
+      {1, 2, 1}, {2, 1, 1}, {0, 2, 1}, {2, 2, 0}, {2, 0, 2}, {1, 2, 2}, {2, 1, 2}, {0, 2, 2}, {2, 2, 1},
+      {2, 2, 2}};
+  const unsigned *t = i < 8 ? V[i] : EF[i - 8];
+  i0 = t[0];
+  i1 = t[1];
+  i2 = t[2];
+}
+
+// FE<3,HIERARCHIC>::shape on a hex: (s0 * s1) * s2.
+double hier_hex_shape(unsigned i, const Pt &p) {
+  unsigned i0, i1, i2;
+  cube_indices_p2(i, i0, i1, i2);
+  return hier_1d(i0, p.v[0]) * hier_1d(i1, p.v[1]) * hier_1d(i2, p.v[2]);
+}
+
+// fe_fdm_deriv (src/fe/fe.C:794-811, 929-944): central difference, eps = 1e-6.
+double hier_hex_deriv(unsigned i, unsigned j, const Pt &p) {
+  const double eps = 1.e-6;
+  Pt pp = p, pm = p;
+  pp.v[j] += eps;
+  pm.v[j] -= eps;
+  return (hier_hex_shape(i, pp) - hier_hex_shape(i, pm)) / 2. / eps;
+}
+
+void all_shapes_hierarchic(int order, const std::vector<Pt> &pts, std::vector<std::vector<double>> &phi,
+                           std::vector<std::vector<double>> d[3]) {
+  const unsigned n = (order + 1) * (order + 1) * (order + 1), np = (unsigned)pts.size();
+  phi.assign(n, std::vector<double>(np));
+  for (int c = 0; c < 3; ++c) d[c].assign(n, std::vector<double>(np));
+  for (unsigned q = 0; q < np; ++q)
+    for (unsigned i = 0; i < n; ++i) {
+      phi[i][q] = hier_hex_shape(i, pts[q]);
+      for (unsigned c = 0; c < 3; ++c) d[c][i][q] = hier_hex_deriv(i, c, pts[q]);
+    }
+}
+
 }  // namespace
 
 namespace {
@@ -301,7 +368,9 @@ struct OracleFE {
   std::vector<double> JxW, jac, G[9];                 // G[3*m+d] = dxi_m/dx_d
   std::vector<std::vector<Pt>> dphi;                  // dphi[i][q]
 
-  bool init(int type_, int order_, int q_order) {
+  int family = 0;  // 0 LAGRANGE, 1 HIERARCHIC (hex, order <= 2)
+  bool init(int type_, int order_, int q_order, int family_ = 0) {
+    family = family_;
     type = type_; order = order_;
     if (!qgauss_3d(type, q_order, qp, qw)) return false;
     nq = (int)qp.size();
@@ -309,7 +378,8 @@ struct OracleFE {
     const int geo_order = (type == HEX27 || type == TET10) ? 2 : 1;
     n_geo = n_shapes(type, geo_order);
     if (!n || !n_geo) return false;
-    all_shapes(type, order, qp, phi, dref);
+    if (family == 1) all_shapes_hierarchic(order, qp, phi, dref);
+    else all_shapes(type, order, qp, phi, dref);
     all_shapes(type, geo_order, qp, phi_map, dmap);
     JxW.assign(nq, 0); jac.assign(nq, 0);
     for (auto &g : G) g.assign(nq, 0);
@@ -627,9 +697,16 @@ int orc_shapes(int type, int order, int np, const double *pts, double *phi, doub
   for (int q = 0; q < np; ++q)
     for (int d = 0; d < 3; ++d) P[q].v[d] = pts[3 * q + d];
   std::vector<std::vector<double>> ph, dr[3];
+  const int family = (order & 0x100) ? 1 : 0;  // HIERARCHIC flag
+  order &= 0xff;
   const int n = n_shapes(type, order);
   if (!n) return -1;
-  all_shapes(type, order, P, ph, dr);
+  if (family == 1) {
+    if (!((type == HEX8 && order == 1) || (type == HEX27 && order == 2))) return -1;
+    all_shapes_hierarchic(order, P, ph, dr);
+  } else {
+    all_shapes(type, order, P, ph, dr);
+  }
   for (int i = 0; i < n; ++i)
     for (int q = 0; q < np; ++q) {
       phi[i * np + q] = ph[i][q];
@@ -760,6 +837,9 @@ int orc_assemble2(int form, int type, int fe_order, int q_order, int64_t n_nodes
                   const int64_t *cons_ptr, const int32_t *cons_col, const double *cons_val,
                   const double *params, int n_params) {
   Problem P{};
+  const int family = (fe_order & 0x100) ? 1 : 0;  // HIERARCHIC flag (FEType family)
+  fe_order &= 0xff;
+  if (family == 1 && !((type == HEX8 && fe_order == 1) || (type == HEX27 && fe_order == 2))) return 8;
   P.cons_ptr = cons_ptr; P.cons_col = cons_col; P.cons_val = cons_val;
   P.params = params; P.n_params = n_params;
   if (form == ADVDIFF && n_params < 2) return 1;
@@ -779,7 +859,7 @@ int orc_assemble2(int form, int type, int fe_order, int q_order, int64_t n_nodes
   int64_t first_bad = -1;
   auto work = [&](int64_t b, int64_t en) {
     OracleFE fe;
-    fe.init(type, fe_order, q_order);
+    fe.init(type, fe_order, q_order, family);
     Dense Ke;
     std::vector<double> Fe;
     std::vector<int32_t> dofs;

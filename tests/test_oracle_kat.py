@@ -109,3 +109,29 @@ def test_oracle_volume_through_load(et, nv, form, fo, qo):
     for v in range(nv):
         sel = dm.elem_dofs[:, v * mesh.conn.shape[1]:(v + 1) * mesh.conn.shape[1]]
         assert abs(F[np.unique(sel)].sum() - 1.0) < 1e-13
+
+
+@pytest.mark.parametrize("et,order", [(10, 1), (12, 2)])
+def test_hierarchic_shapes_span_the_lagrange_space(et, order):
+    """HIERARCHIC hex shapes of order p lie in Q_p (fe_hierarchic_test.C checks
+    reproduction of polynomial fields): each equals the LAGRANGE interpolant of
+    its nodal values, and its central-difference derivative (eps = 1e-6) equals
+    the interpolant's exact derivative to the difference error."""
+    rng = np.random.default_rng(0)
+    nodes = orc.shapes(et, order, np.zeros((1, 3)))[0].shape[0]
+    lag_nodes = {10: np.array([[-1, -1, -1], [1, -1, -1], [1, 1, -1], [-1, 1, -1], [-1, -1, 1], [1, -1, 1], [1, 1, 1],
+                               [-1, 1, 1]], float)}
+    if et == 12:
+        off = [[0, 0, 0], [2, 0, 0], [2, 2, 0], [0, 2, 0], [0, 0, 2], [2, 0, 2], [2, 2, 2], [0, 2, 2], [1, 0, 0],
+               [2, 1, 0], [1, 2, 0], [0, 1, 0], [0, 0, 1], [2, 0, 1], [2, 2, 1], [0, 2, 1], [1, 0, 2], [2, 1, 2],
+               [1, 2, 2], [0, 1, 2], [1, 1, 0], [1, 0, 1], [2, 1, 1], [1, 2, 1], [0, 1, 1], [1, 1, 2], [1, 1, 1]]
+        lag_nodes[12] = np.array(off, float) - 1.0
+    X = lag_nodes[et]
+    pts = rng.uniform(-1, 1, (20, 3))
+    hv, hd = orc.shapes(et, order | 0x100, pts)
+    hn, _ = orc.shapes(et, order | 0x100, X)          # hierarchic values at the Lagrange nodes
+    lv, ld = orc.shapes(et, order, pts)
+    assert hv.shape[0] == nodes
+    np.testing.assert_allclose(hv, hn @ lv, atol=1e-14)
+    for c in range(3):
+        np.testing.assert_allclose(hd[c], hn @ ld[c], atol=1e-9)
