@@ -237,6 +237,103 @@ def run_amr(args, local):
         "stages_ms": {"elements_and_constraints": el_ms / calls, "insertion": ga_ms / calls}}))
 
 
+def batch_members(n_meshes, seed=3, lo=1e3, hi=5e4):
+    """Meshes with log-uniform element counts in [lo, hi], cycling through
+    HIERARCHIC FIRST HEX8 Poisson, HIERARCHIC SECOND HEX27 Poisson, LAGRANGE
+    TET10 elasticity and LAGRANGE HEX27 convection-diffusion."""
+    import libmesh_gb300 as lm
+    rng = np.random.default_rng(seed)
+    sizes = np.exp(rng.uniform(np.log(lo), np.log(hi), n_meshes))
+    out = []
+    for i, s in enumerate(sizes):
+        kind = i % 4
+        per_hex = 6 if kind == 2 else 1
+        n = max(2, int(round((s / per_hex) ** (1.0 / 3.0))))
+        et = [lm.HEX8, lm.HEX27, lm.TET10, lm.HEX27][kind]
+        mesh = lm.Mesh.build_cube(n, n, n, et, jitter=0.2 if kind == 2 else 0.0, seed=i + 1)
+        nv = 3 if kind == 2 else 1
+        dm = lm.DofMap(mesh, nv)
+        dm.add_dirichlet_boundary([4] if kind == 2 else [0, 1, 2, 3, 4, 5], list(range(nv)))
+        k = np.exp(rng.normal(0.0, 0.5, mesh.n_elem))
+        f = rng.uniform(-1.0, 1.0, (mesh.n_nodes, nv))
+        if kind == 0:
+            a = lm.GpuAssembly(lm.POISSON, 1 | lm.HIERARCHIC, 3, elem_coef=k, nodal_f=f)
+        elif kind == 1:
+            a = lm.GpuAssembly(lm.POISSON, 2 | lm.HIERARCHIC, 5, elem_coef=k, nodal_f=f)
+        elif kind == 2:
+            a = lm.GpuAssembly(lm.ELASTICITY, 2, 4, elem_coef=k, nodal_f=f)
+        else:
+            a = lm.GpuAssembly(lm.ADVDIFF, 2, 5, elem_coef=k, nodal_f=f, params=cd_params())
+        a.init(mesh, dm)
+        out.append((a, mesh.n_elem))
+    return out
+
+
+def run_batch(args, local):
+    """Secondary workload: many independent systems of mixed element types,
+    forms and FE families, assembled (a) one after another through the C ABI
+    and (b) as one tuned CUDA graph (lmg_batch_*)."""
+    import torch
+    import libmesh_gb300 as lm
+    torch.cuda.set_device(local)
+    n_meshes = args.meshes
+    t0 = time.perf_counter()
+    mem = batch_members(n_meshes)
+    setup_s = time.perf_counter() - t0
+    total = sum(e for _, e in mem)
+    # (a) one after another, default grids
+    for a, _ in mem:
+        a.assemble_device(lm.FP64)
+    for a, _ in mem:
+        a.synchronize()
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    for _ in range(args.steps):
+        for a, _ in mem:
+            a.assemble_device(lm.FP64)
+        for a, _ in mem:
+            a.synchronize()
+    seq_ms = (time.perf_counter() - t1) * 1e3 / args.steps
+    # (b) one graph, tuned grids
+    b = lm.Batch(local)
+    for a, _ in mem:
+        b.add(a)
+    t2 = time.perf_counter()
+    b.tune(lm.FP64, reps=2)
+    tune_s = time.perf_counter() - t2
+    for _ in range(max(3, args.warmup)):
+        b.assemble(lm.FP64)
+    b.synchronize()
+    sptr, launches, grids = b.info()
+    stream = torch.cuda.ExternalStream(sptr)
+    clocks = Clocks(local)
+    clocks.start()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        b.assemble(lm.FP64)
+    ev1.record(stream)
+    ev1.synchronize()
+    b.synchronize()
+    ms = ev0.elapsed_time(ev1) / args.steps
+    clk = clocks.stop()
+    b.close()
+    for a, _ in mem:
+        a.close()
+    print(json.dumps({
+        "metric": METRIC, "value": total / (ms * 1e-3) / 1e6, "unit": "Melem/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic (seeded sizes, jitter, coefficients, loads)",
+        "config": {"workload": "batch of %d systems, element counts log-uniform in [1e3, 5e4]: HIERARCHIC HEX8 p1 "
+                               "Poisson, HIERARCHIC HEX27 p2 Poisson, TET10 elasticity, HEX27 convection-diffusion"
+                               % n_meshes, "total_elements": total, "setup_s": setup_s, "tune_s": tune_s},
+        "sequential": {"ms_per_step": seq_ms, "value": total / (seq_ms * 1e-3) / 1e6, "unit": "Melem/s",
+                       "how": "lmg_assemble per system on its own stream, host loop, default grids"},
+        "graph_speedup": seq_ms / ms, "gpu_launches": launches * args.steps, "launches_per_replay": launches,
+        "tuned_ctas_per_sm": {str(g): int((grids == g).sum()) for g in sorted(set(grids.tolist()))},
+        "clocks": clk}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -247,18 +344,20 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
     ap.add_argument("--n", type=int, default=N_CUBE, help="cube divisions (48 = the headline mesh)")
     ap.add_argument("--no-mixed", action="store_true", help="skip timing the mixed form beside FP64")
-    ap.add_argument("--workload", default="elasticity", choices=["elasticity", "amr-cd"],
-                    help="elasticity = the headline; amr-cd = refined HEX27 convection-diffusion")
+    ap.add_argument("--workload", default="elasticity", choices=["elasticity", "amr-cd", "batch"],
+                    help="elasticity = the headline; amr-cd = refined HEX27 convection-diffusion; "
+                         "batch = many mixed systems as one CUDA graph")
+    ap.add_argument("--meshes", type=int, default=64, help="systems in the batch workload")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
     local = int(os.environ.get("LOCAL_RANK", 0))
     if args.impl == "reference":
         return run_reference(args, rank)
-    if args.workload == "amr-cd":
+    if args.workload in ("amr-cd", "batch"):
         from libmesh_gb300 import _build
         _build.build()
-        return run_amr(args, local)
+        return run_amr(args, local) if args.workload == "amr-cd" else run_batch(args, local)
 
     import torch
     import libmesh_gb300 as lm

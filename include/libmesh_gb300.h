@@ -224,6 +224,9 @@ lmg_status lmg_inputs_update(lmg_ctx *ctx, const double *xyz, const double *elem
 lmg_status lmg_assemble(lmg_ctx *ctx, int32_t precision, double *K, double *F,
                         int32_t out_on_device);
 lmg_status lmg_result_device(lmg_ctx *ctx, double **K, double **F);
+/* Copy the last assembled K and F from the context's device buffers to host
+ * arrays (either may be NULL), waiting for the context's stream. */
+lmg_status lmg_result_copy(lmg_ctx *ctx, double *K, double *F);
 
 /* With device (or no) outputs lmg_assemble returns once the work is queued on
  * the context's stream; lmg_synchronize waits for it and returns its status. */
@@ -285,6 +288,39 @@ lmg_status lmg_last_error(lmg_ctx *ctx, int64_t *elem_id, char *msg, int32_t msg
  * and the number of logged calls, and resets the totals. */
 lmg_status lmg_perflog_enable(lmg_ctx *ctx, int32_t on);
 lmg_status lmg_perflog_read(lmg_ctx *ctx, double *elements_ms, double *gather_ms, int64_t *calls);
+
+/* Element-kernel grid of this context in CTAs per SM (0 = default 32); the
+ * batch autotuner sets it. */
+lmg_status lmg_context_set_grid(lmg_ctx *ctx, int32_t ctas_per_sm);
+
+/* ------------------------------------------------------------------------- */
+/* Batched assembly of many systems as one CUDA graph.                       */
+/* ------------------------------------------------------------------------- */
+/* libMesh assembles each System with its own System::assemble call
+ * (src/systems/system.C:554-561).  A batch holds any number of set-up contexts
+ * (each its own mesh, element type, form and FE family) on one stream:
+ * lmg_batch_add moves a context onto the batch stream (its sparsity and form
+ * must be set); lmg_batch_tune times each context's element kernel at
+ * {2, 4, 8, 16, 32} CTAs per SM (reps assemblies each) and keeps the fastest;
+ * lmg_batch_assemble assembles every context into its own device K and F
+ * (lmg_result_device): the first call per precision runs each context once
+ * eagerly, then captures all of them into one CUDA graph, and every call
+ * launches that graph and returns without waiting.  lmg_batch_synchronize
+ * waits and reports the first failing context.  Changing a context's inputs
+ * with lmg_inputs_update between replays is allowed (same buffers); changing
+ * its mesh, dof map, constraints, sparsity or form requires a new batch.
+ * lmg_batch_destroy gives every context a stream of its own again. */
+typedef struct lmg_batch lmg_batch;
+lmg_status lmg_batch_create(lmg_batch **batch, int32_t device);
+lmg_status lmg_batch_destroy(lmg_batch *batch);
+lmg_status lmg_batch_add(lmg_batch *batch, lmg_ctx *ctx);
+lmg_status lmg_batch_tune(lmg_batch *batch, int32_t precision, int32_t reps);
+lmg_status lmg_batch_assemble(lmg_batch *batch, int32_t precision);
+lmg_status lmg_batch_synchronize(lmg_batch *batch, int64_t *first_failed);
+/* The batch stream, kernels per graph replay, and the tuned CTAs per SM of
+ * the first n contexts (any pointer may be NULL). */
+lmg_status lmg_batch_info(lmg_batch *batch, void **stream, int64_t *launches_per_replay,
+                          int32_t *ctas_per_sm, int32_t n);
 
 /* Number of kernels this context has launched since creation. */
 lmg_status lmg_launch_count(lmg_ctx *ctx, int64_t *count);

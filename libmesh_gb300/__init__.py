@@ -19,7 +19,7 @@ from ._capi import (ADVDIFF, ELASTICITY, FP64, HEX8, HEX27, HIERARCHIC, MIXED, P
 
 FIRST, SECOND, THIRD, FOURTH, FIFTH = 1, 2, 3, 4, 5
 
-__all__ = ["Mesh", "DofMap", "GpuAssembly", "LinearImplicitSystem", "DegenerateMap", "LmgError",
+__all__ = ["Mesh", "DofMap", "GpuAssembly", "Batch", "LinearImplicitSystem", "DegenerateMap", "LmgError",
            "HEX8", "HEX27", "TET4", "TET10", "PRISM6", "POISSON", "ELASTICITY", "ADVDIFF", "FP64", "MIXED", "HIERARCHIC",
            "FIRST", "SECOND", "THIRD", "FOURTH", "FIFTH"]
 
@@ -276,6 +276,16 @@ class GpuAssembly:
         self._ok(lib().lmg_assemble(self.ctx, precision, C.c_void_p(K_ptr), C.c_void_p(F_ptr),
                                     1 if on_device else 0))
 
+    def result(self):
+        """(K, F) of the last assembly, copied from the device."""
+        K = np.empty(self.nnz, np.float64)
+        F = np.empty(self.dof_map.n_dofs, np.float64)
+        self._ok(lib().lmg_result_copy(self.ctx, ptr(K), ptr(F)))
+        return K, F
+
+    def set_grid(self, ctas_per_sm):
+        self._ok(lib().lmg_context_set_grid(self.ctx, int(ctas_per_sm)))
+
     def launch_count(self):
         n = C.c_int64()
         self._ok(lib().lmg_launch_count(self.ctx, C.byref(n)))
@@ -338,3 +348,39 @@ class LinearImplicitSystem:
         import scipy.sparse as sp
         n = self.dof_map.n_dofs
         return sp.csr_matrix((self.matrix, self.col_idx, self.row_ptr), shape=(n, n))
+
+
+class Batch:
+    """Many set-up GpuAssembly objects assembled as one CUDA graph
+    (lmg_batch_*): add, tune, then assemble / synchronize repeatedly."""
+
+    def __init__(self, device=0):
+        h = C.c_void_p()
+        check(lib().lmg_batch_create(C.byref(h), device))
+        self.h = h
+        self.members = []
+
+    def add(self, assembly):
+        check(lib().lmg_batch_add(self.h, assembly.ctx))
+        self.members.append(assembly)
+
+    def tune(self, precision=FP64, reps=3):
+        check(lib().lmg_batch_tune(self.h, precision, reps))
+
+    def assemble(self, precision=FP64):
+        check(lib().lmg_batch_assemble(self.h, precision))
+
+    def synchronize(self):
+        bad = C.c_int64(-1)
+        check(lib().lmg_batch_synchronize(self.h, C.byref(bad)))
+
+    def info(self):
+        s, l = C.c_void_p(), C.c_int64()
+        g = np.zeros(len(self.members), np.int32)
+        check(lib().lmg_batch_info(self.h, C.byref(s), C.byref(l), ptr(g), len(self.members)))
+        return s.value, l.value, g
+
+    def close(self):
+        if self.h is not None:
+            lib().lmg_batch_destroy(self.h)
+            self.h = None

@@ -12,8 +12,8 @@ OUT = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT, "liblmg.so")
 
 CXX_SOURCES = ["host_mesh.cpp", "host_mesh_tri.cpp", "host_dofmap.cpp", "host_amr.cpp", "fe_tables.cpp"]
-CU_SOURCES = ["elements.cu", "gather.cu", "context.cu", "context_general.cu", "general.cu", "cg.cu", "vjp.cu",
-              "probe.cu"]
+CU_SOURCES = ["elements.cu", "gather.cu", "context.cu", "context_general.cu", "general.cu", "batch.cu", "cg.cu",
+              "vjp.cu", "probe.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

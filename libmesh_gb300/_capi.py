@@ -54,6 +54,7 @@ SIGNATURES = {
     "lmg_assemble": [_p, _i32, _p, _p, _i32],
     "lmg_result_device": [_p, C.POINTER(_p), C.POINTER(_p)],
     "lmg_synchronize": [_p],
+    "lmg_result_copy": [_p, _p, _p],
     "lmg_last_error": [_p, _pi64, C.c_char_p, _i32],
     "lmg_cg_solve": [_p, _p, _p, _f64, _i32, _pi32, _pf64],
     "lmg_cg_solve_noalloc": [_i64, _p, _p, _p, _p, _p, _f64, _i32, _p, _pi32, _pf64, C.c_char_p, _i32],
@@ -62,6 +63,14 @@ SIGNATURES = {
     "lmg_perflog_enable": [_p, _i32],
     "lmg_perflog_read": [_p, _pf64, _pf64, _pi64],
     "lmg_launch_count": [_p, _pi64],
+    "lmg_context_set_grid": [_p, _i32],
+    "lmg_batch_create": [C.POINTER(_p), _i32],
+    "lmg_batch_destroy": [_p],
+    "lmg_batch_add": [_p, _p],
+    "lmg_batch_tune": [_p, _i32, _i32],
+    "lmg_batch_assemble": [_p, _i32],
+    "lmg_batch_synchronize": [_p, _pi64],
+    "lmg_batch_info": [_p, C.POINTER(_p), _pi64, _p, _i32],
     "lmg_probe_fp64": [_i32, _pf64],
 }
 

@@ -1,0 +1,216 @@
+// Batched assembly: many independent systems (meshes, forms, element types)
+// assembled as one CUDA graph on one stream.  libMesh assembles each system
+// through its own System::assemble call (src/systems/system.C:554-561); a
+// batch replays the kernels of all of them with one graph launch, after an
+// autotuner has picked each system's element-kernel grid.
+//
+// Life cycle: lmg_batch_add moves a fully set-up context (sparsity, form) onto
+// the batch stream; lmg_batch_tune times a few grid sizes per context;
+// lmg_batch_assemble warms every context up once (lazy plans, buffers), then
+// captures their assemblies into a graph per precision and replays it.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "context_internal.cuh"
+
+struct lmg_batch {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::vector<lmg_ctx *> ctx;
+  cudaGraphExec_t exec[2] = {nullptr, nullptr};  // per precision
+  cudaGraph_t graph[2] = {nullptr, nullptr};
+  bool warm[2] = {false, false};
+  int64_t launches = 0;    // kernels in one replay
+  std::string err;
+};
+
+namespace {
+
+void drop_graphs(lmg_batch *b) {
+  for (int p = 0; p < 2; ++p) {
+    if (b->exec[p]) cudaGraphExecDestroy(b->exec[p]);
+    if (b->graph[p]) cudaGraphDestroy(b->graph[p]);
+    b->exec[p] = nullptr;
+    b->graph[p] = nullptr;
+  }
+}
+
+lmg_status bfail(lmg_batch *b, lmg_status code, const std::string &msg) {
+  if (b) b->err = msg;
+  return code;
+}
+
+// Assemble every context once on the batch stream with outputs kept on the
+// device, then check each context's status.
+lmg_status run_all(lmg_batch *b, int precision) {
+  for (lmg_ctx *c : b->ctx) {
+    const lmg_status st = lmg_assemble(c, precision, nullptr, nullptr, 1);
+    if (st) return bfail(b, st, "batch: assemble failed: " + c->err);
+  }
+  for (lmg_ctx *c : b->ctx) {
+    const lmg_status st = lmg_synchronize(c);
+    if (st) return bfail(b, st, "batch: " + c->err);
+  }
+  return LMG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+lmg_status lmg_batch_create(lmg_batch **out, int32_t device) {
+  if (!out) return LMG_ERR_ARG;
+  *out = nullptr;
+  lmg_batch *b = new (std::nothrow) lmg_batch;
+  if (!b) return LMG_ERR_OOM;
+  b->device = device;
+  if (cudaSetDevice(device) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete b;
+    return LMG_ERR_CUDA;
+  }
+  *out = b;
+  return LMG_OK;
+}
+
+lmg_status lmg_batch_destroy(lmg_batch *b) {
+  if (!b) return LMG_OK;
+  cudaSetDevice(b->device);
+  cudaStreamSynchronize(b->stream);
+  drop_graphs(b);
+  // the contexts stay valid; they keep running on the batch stream's handle
+  // only while the batch lives, so give each its own stream back
+  for (lmg_ctx *c : b->ctx) {
+    cudaStream_t s = nullptr;
+    if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) == cudaSuccess) {
+      c->stream = s;
+      c->own_stream = true;
+    }
+  }
+  cudaStreamDestroy(b->stream);
+  delete b;
+  return LMG_OK;
+}
+
+lmg_status lmg_batch_add(lmg_batch *b, lmg_ctx *c) {
+  if (!b || !c) return bfail(b, LMG_ERR_ARG, "batch_add: bad argument");
+  if (c->device != b->device) return bfail(b, LMG_ERR_ARG, "batch_add: context on another device");
+  if (!c->have_sparsity || !c->have_form) return bfail(b, LMG_ERR_STATE, "batch_add: build sparsity and form first");
+  if (std::find(b->ctx.begin(), b->ctx.end(), c) != b->ctx.end()) return LMG_OK;
+  const lmg_status st = lmg_context_set_stream(c, (void *)b->stream);
+  if (st) return bfail(b, st, "batch_add: " + c->err);
+  c->perflog = false;
+  b->ctx.push_back(c);
+  drop_graphs(b);
+  b->warm[0] = b->warm[1] = false;
+  return LMG_OK;
+}
+
+lmg_status lmg_batch_tune(lmg_batch *b, int32_t precision, int32_t reps) {
+  if (!b || (precision != LMG_FP64 && precision != LMG_MIXED)) return bfail(b, LMG_ERR_ARG, "batch_tune: bad argument");
+  cudaSetDevice(b->device);
+  if (reps <= 0) reps = 3;
+  lmg_status st = run_all(b, precision);  // lazy plans and buffers before any timing
+  if (st) return st;
+  static const int cand[] = {2, 4, 8, 16, 32};
+  cudaEvent_t e0, e1;
+  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
+    return bfail(b, LMG_ERR_CUDA, "batch_tune: event creation failed");
+  for (lmg_ctx *c : b->ctx) {
+    float best = 1e30f;
+    int best_c = c->ctas_per_sm;
+    for (int k : cand) {
+      c->ctas_per_sm = k;
+      st = lmg_assemble(c, precision, nullptr, nullptr, 1);
+      if (st) break;
+      cudaEventRecord(e0, b->stream);
+      for (int r = 0; r < reps && !st; ++r) st = lmg_assemble(c, precision, nullptr, nullptr, 1);
+      cudaEventRecord(e1, b->stream);
+      if (st || cudaEventSynchronize(e1) != cudaSuccess) break;
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (ms < best) {
+        best = ms;
+        best_c = k;
+      }
+    }
+    c->ctas_per_sm = best_c;
+    if (st) break;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (st) return bfail(b, st, "batch_tune: assemble failed");
+  drop_graphs(b);
+  return LMG_OK;
+}
+
+lmg_status lmg_batch_assemble(lmg_batch *b, int32_t precision) {
+  if (!b || (precision != LMG_FP64 && precision != LMG_MIXED)) return bfail(b, LMG_ERR_ARG, "batch_assemble: bad argument");
+  if (b->ctx.empty()) return bfail(b, LMG_ERR_STATE, "batch_assemble: no contexts");
+  cudaSetDevice(b->device);
+  const int p = precision == LMG_MIXED ? 1 : 0;
+  if (!b->exec[p]) {
+    if (!b->warm[p]) {
+      const lmg_status st = run_all(b, precision);
+      if (st) return st;
+      b->warm[p] = true;
+    }
+    int64_t l0 = 0, l1 = 0;
+    for (lmg_ctx *c : b->ctx) l0 += c->launches;
+    if (cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+      return bfail(b, LMG_ERR_CUDA, "batch_assemble: stream capture failed to start");
+    lmg_status st = LMG_OK;
+    for (lmg_ctx *c : b->ctx) {
+      st = lmg_assemble(c, precision, nullptr, nullptr, 1);
+      if (st) break;
+    }
+    cudaGraph_t g = nullptr;
+    const cudaError_t ce = cudaStreamEndCapture(b->stream, &g);
+    if (st || ce != cudaSuccess || !g) {
+      if (g) cudaGraphDestroy(g);
+      return bfail(b, st ? st : LMG_ERR_CUDA, "batch_assemble: capture failed");
+    }
+    for (lmg_ctx *c : b->ctx) l1 += c->launches;
+    b->launches = l1 - l0;
+    b->graph[p] = g;
+    if (cudaGraphInstantiate(&b->exec[p], g, 0) != cudaSuccess) {
+      drop_graphs(b);
+      return bfail(b, LMG_ERR_CUDA, "batch_assemble: graph instantiation failed");
+    }
+  }
+  if (cudaGraphLaunch(b->exec[p], b->stream) != cudaSuccess)
+    return bfail(b, LMG_ERR_CUDA, "batch_assemble: graph launch failed");
+  for (lmg_ctx *c : b->ctx) c->launches += b->launches / (int64_t)b->ctx.size();
+  return LMG_OK;
+}
+
+lmg_status lmg_batch_synchronize(lmg_batch *b, int64_t *first_failed) {
+  if (!b) return LMG_ERR_ARG;
+  if (first_failed) *first_failed = -1;
+  cudaSetDevice(b->device);
+  if (cudaStreamSynchronize(b->stream) != cudaSuccess) return bfail(b, LMG_ERR_CUDA, "batch: device failure");
+  for (size_t i = 0; i < b->ctx.size(); ++i) {
+    const lmg_status st = lmg_synchronize(b->ctx[i]);
+    if (st) {
+      if (first_failed) *first_failed = (int64_t)i;
+      return bfail(b, st, "batch: context " + std::to_string(i) + ": " + b->ctx[i]->err);
+    }
+  }
+  return LMG_OK;
+}
+
+lmg_status lmg_batch_info(lmg_batch *b, void **stream, int64_t *launches_per_replay, int32_t *ctas_per_sm,
+                          int32_t n) {
+  if (!b) return LMG_ERR_ARG;
+  if (stream) *stream = (void *)b->stream;
+  if (launches_per_replay) *launches_per_replay = b->launches;
+  if (ctas_per_sm)
+    for (int32_t i = 0; i < n && i < (int32_t)b->ctx.size(); ++i) ctas_per_sm[i] = b->ctx[(size_t)i]->ctas_per_sm;
+  return LMG_OK;
+}
+
+}  // extern "C"

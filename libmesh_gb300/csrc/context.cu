@@ -690,7 +690,7 @@ lmg_status lmg_assemble(lmg_ctx *c, int32_t precision, double *K, double *F, int
   a.status = c->d_status;
   a.bad_elem = c->d_bad;
   a.fe = c->dfe;
-  const int grid = c->n_sm * 32;  // grid-stride: enough CTAs to fill every SM
+  const int grid = c->n_sm * c->ctas_per_sm;  // grid-stride over the element lists
   cudaEvent_t e3[3] = {nullptr, nullptr, nullptr};
   if (c->perflog) {
     for (auto &e : e3) LMG_CUDA(c, cudaEventCreate(&e));
@@ -754,6 +754,15 @@ lmg_status lmg_result_device(lmg_ctx *c, double **K, double **F) {
   if (K) *K = c->d_K;
   if (F) *F = c->d_F;
   return LMG_OK;
+}
+
+lmg_status lmg_result_copy(lmg_ctx *c, double *K, double *F) {
+  if (!c) return LMG_ERR_ARG;
+  if (!c->have_sparsity) return fail(c, LMG_ERR_STATE, "result_copy: nothing assembled");
+  cudaSetDevice(c->device);
+  if (K) LMG_CUDA(c, cudaMemcpyAsync(K, c->d_K, sizeof(double) * c->nnz, cudaMemcpyDeviceToHost, c->stream));
+  if (F) LMG_CUDA(c, cudaMemcpyAsync(F, c->d_F, sizeof(double) * c->n_dofs, cudaMemcpyDeviceToHost, c->stream));
+  return check_status(c, "result_copy");
 }
 
 lmg_status lmg_last_error(lmg_ctx *c, int64_t *elem_id, char *msg, int32_t msg_len) {
@@ -893,6 +902,12 @@ lmg_status lmg_perflog_read(lmg_ctx *c, double *elements_ms, double *gather_ms, 
   if (calls) *calls = c->log_calls;
   c->log_ms[0] = c->log_ms[1] = 0.0;
   c->log_calls = 0;
+  return LMG_OK;
+}
+
+lmg_status lmg_context_set_grid(lmg_ctx *c, int32_t ctas_per_sm) {
+  if (!c || ctas_per_sm < 0 || ctas_per_sm > 64) return fail(c, LMG_ERR_ARG, "set_grid: 0 (default) .. 64");
+  c->ctas_per_sm = ctas_per_sm ? ctas_per_sm : 32;
   return LMG_OK;
 }
 

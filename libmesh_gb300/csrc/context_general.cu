@@ -272,7 +272,7 @@ lmg_status general_assemble(lmg_ctx *c) {
   a.status = c->d_status;
   a.bad_elem = c->d_bad;
   a.fe = c->dfe;
-  launch_gen_elements(c->form, c->tab.n, c->tab.q, a, c->n_sm, c->stream);
+  launch_gen_elements(c->form, c->tab.n, c->tab.q, a, c->n_sm * c->ctas_per_sm / 4, c->stream);
   c->launches++;
   if (c->n_cons_elem) {
     ConsArgs k{};

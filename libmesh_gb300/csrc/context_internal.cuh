@@ -15,6 +15,7 @@ struct lmg_ctx {
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   int n_sm = 152;
+  int ctas_per_sm = 32;  // element-kernel grid (grid-stride), set by the batch autotuner
   int64_t launches = 0;
   std::string err;
   int64_t err_elem = -1;

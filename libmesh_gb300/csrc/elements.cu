@@ -432,7 +432,11 @@ void launch_t(bool affine, const ElemArgs &a, int grid, cudaStream_t s) {
   if (affine) {
     using TA = typename std::conditional<sizeof(T) == 4, float, float2>::type;
     const size_t sm = AffineSmem<FORM, N, NV, TA>::BYTES;
-    cudaFuncSetAttribute(k_elem_affine<FORM, N, NV, TA>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    static bool attr = false;  // set once, before any stream capture of this launch
+    if (!attr) {
+      cudaFuncSetAttribute(k_elem_affine<FORM, N, NV, TA>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+      attr = true;
+    }
     const int64_t tiles = (a.n_list + 31) / 32;
     const int64_t blocks = (tiles + 3) / 4;
     k_elem_affine<FORM, N, NV, TA><<<(int)(blocks < grid ? blocks : grid), 128, sm, s>>>(a);

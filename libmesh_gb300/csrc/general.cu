@@ -277,7 +277,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_elem_full(GenElemArgs a) {
 }
 
 template <int FORM, int N, int Q>
-void launch_full(const GenElemArgs &a, int n_sm, cudaStream_t s) {
+void launch_full(const GenElemArgs &a, int max_ctas, cudaStream_t s) {
   const size_t smem = sizeof(double) * ((size_t)Q * N * 5 + 6 * N * N + Q + N * 3 + 7 * a.n_modes +
                                         (size_t)WARPS * (N * 3 + N + 4 * Q + 8 * a.n_modes));
   static size_t attr = 0;  // largest dynamic shared memory granted so far
@@ -286,7 +286,7 @@ void launch_full(const GenElemArgs &a, int n_sm, cudaStream_t s) {
     attr = smem;
   }
   const int64_t need = (a.n_elem + WARPS - 1) / WARPS;
-  const int grid = (int)(need < (int64_t)n_sm * 8 ? need : (int64_t)n_sm * 8);
+  const int grid = (int)(need < (int64_t)max_ctas ? need : (int64_t)max_ctas);
   if (grid > 0) k_elem_full<FORM, N, Q><<<grid, WARPS * 32, smem, s>>>(a);
 }
 
@@ -379,9 +379,9 @@ bool gen_elements_built(int form, int n, int q) {
   return (n == 8 || n == 27) && (q == 8 || q == 27);
 }
 
-void launch_gen_elements(int form, int n, int q, const GenElemArgs &a, int n_sm, cudaStream_t s) {
+void launch_gen_elements(int form, int n, int q, const GenElemArgs &a, int max_ctas, cudaStream_t s) {
 #define LMG_G(F, NN, QQ) \
-  if (form == F && n == NN && q == QQ) return launch_full<F, NN, QQ>(a, n_sm, s);
+  if (form == F && n == NN && q == QQ) return launch_full<F, NN, QQ>(a, max_ctas, s);
   LMG_G(LMG_POISSON, 8, 8)
   LMG_G(LMG_POISSON, 8, 27)
   LMG_G(LMG_POISSON, 27, 8)

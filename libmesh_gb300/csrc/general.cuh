@@ -53,7 +53,8 @@ struct ConsArgs {
 };
 
 bool gen_elements_built(int form, int n, int q);
-void launch_gen_elements(int form, int n, int q, const GenElemArgs &a, int n_sm, cudaStream_t s);
+// max_ctas: grid cap of the grid-stride element loop
+void launch_gen_elements(int form, int n, int q, const GenElemArgs &a, int max_ctas, cudaStream_t s);
 void launch_constrain(const ConsArgs &c, int n_sm, cudaStream_t s);
 void launch_gather_full(int64_t nnz, const int64_t *cptr, const uint32_t *coff, const double *E, double *K,
                         int64_t n_dofs, const int64_t *fptr, const uint32_t *foff, const double *Fb, double *F,
