@@ -298,18 +298,20 @@ lmg_status lmg_context_set_grid(lmg_ctx *ctx, int32_t ctas_per_sm);
 /* ------------------------------------------------------------------------- */
 /* libMesh assembles each System with its own System::assemble call
  * (src/systems/system.C:554-561).  A batch holds any number of set-up contexts
- * (each its own mesh, element type, form and FE family) on one stream:
- * lmg_batch_add moves a context onto the batch stream (its sparsity and form
- * must be set); lmg_batch_tune times each context's element kernel at
+ * (each its own mesh, element type, form and FE family):
+ * lmg_batch_add registers a context (its sparsity and form must be set; it
+ * keeps its own stream); lmg_batch_tune times each context's element kernel at
  * {2, 4, 8, 16, 32} CTAs per SM (reps assemblies each) and keeps the fastest;
  * lmg_batch_assemble assembles every context into its own device K and F
  * (lmg_result_device): the first call per precision runs each context once
- * eagerly, then captures all of them into one CUDA graph, and every call
- * launches that graph and returns without waiting.  lmg_batch_synchronize
- * waits and reports the first failing context.  Changing a context's inputs
- * with lmg_inputs_update between replays is allowed (same buffers); changing
- * its mesh, dof map, constraints, sparsity or form requires a new batch.
- * lmg_batch_destroy gives every context a stream of its own again. */
+ * eagerly, then captures all of them into one CUDA graph (one branch per
+ * context, forked from and joined into the batch stream), and every call
+ * launches that graph on the batch stream and returns without waiting.
+ * lmg_batch_synchronize waits and reports the first failing context.
+ * Changing a context's inputs with lmg_inputs_update between replays is
+ * allowed (same buffers; synchronize first); changing its mesh, dof map,
+ * constraints, sparsity or form, or its stream, requires a new batch.  Do not
+ * call a member's own entry points while a replay is in flight. */
 typedef struct lmg_batch lmg_batch;
 lmg_status lmg_batch_create(lmg_batch **batch, int32_t device);
 lmg_status lmg_batch_destroy(lmg_batch *batch);

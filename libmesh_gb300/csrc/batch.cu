@@ -1,13 +1,16 @@
 // Batched assembly: many independent systems (meshes, forms, element types)
-// assembled as one CUDA graph on one stream.  libMesh assembles each system
+// assembled as one CUDA graph.  libMesh assembles each system
 // through its own System::assemble call (src/systems/system.C:554-561); a
 // batch replays the kernels of all of them with one graph launch, after an
 // autotuner has picked each system's element-kernel grid.
 //
-// Life cycle: lmg_batch_add moves a fully set-up context (sparsity, form) onto
-// the batch stream; lmg_batch_tune times a few grid sizes per context;
-// lmg_batch_assemble warms every context up once (lazy plans, buffers), then
-// captures their assemblies into a graph per precision and replays it.
+// Life cycle: lmg_batch_add registers a fully set-up context (sparsity,
+// form); lmg_batch_tune times a few grid sizes per context; lmg_batch_assemble
+// warms every context up once (lazy plans, buffers), then captures their
+// assemblies into a graph per precision and replays it.  The capture forks
+// from the batch stream into every context's own stream and joins back, so
+// the graph holds one independent branch per system and small systems run
+// side by side.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -21,6 +24,8 @@ struct lmg_batch {
   int device = 0;
   cudaStream_t stream = nullptr;
   std::vector<lmg_ctx *> ctx;
+  std::vector<cudaEvent_t> join;                  // one per context, capture-time joins
+  cudaEvent_t fork = nullptr;
   cudaGraphExec_t exec[2] = {nullptr, nullptr};  // per precision
   cudaGraph_t graph[2] = {nullptr, nullptr};
   bool warm[2] = {false, false};
@@ -44,7 +49,7 @@ lmg_status bfail(lmg_batch *b, lmg_status code, const std::string &msg) {
   return code;
 }
 
-// Assemble every context once on the batch stream with outputs kept on the
+// Assemble every context once on its own stream with outputs kept on the
 // device, then check each context's status.
 lmg_status run_all(lmg_batch *b, int precision) {
   for (lmg_ctx *c : b->ctx) {
@@ -73,6 +78,11 @@ lmg_status lmg_batch_create(lmg_batch **out, int32_t device) {
     delete b;
     return LMG_ERR_CUDA;
   }
+  if (cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess) {
+    cudaStreamDestroy(b->stream);
+    delete b;
+    return LMG_ERR_CUDA;
+  }
   *out = b;
   return LMG_OK;
 }
@@ -81,16 +91,10 @@ lmg_status lmg_batch_destroy(lmg_batch *b) {
   if (!b) return LMG_OK;
   cudaSetDevice(b->device);
   cudaStreamSynchronize(b->stream);
+  for (lmg_ctx *c : b->ctx) cudaStreamSynchronize(c->stream);
   drop_graphs(b);
-  // the contexts stay valid; they keep running on the batch stream's handle
-  // only while the batch lives, so give each its own stream back
-  for (lmg_ctx *c : b->ctx) {
-    cudaStream_t s = nullptr;
-    if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) == cudaSuccess) {
-      c->stream = s;
-      c->own_stream = true;
-    }
-  }
+  for (cudaEvent_t e : b->join) cudaEventDestroy(e);
+  cudaEventDestroy(b->fork);
   cudaStreamDestroy(b->stream);
   delete b;
   return LMG_OK;
@@ -101,10 +105,13 @@ lmg_status lmg_batch_add(lmg_batch *b, lmg_ctx *c) {
   if (c->device != b->device) return bfail(b, LMG_ERR_ARG, "batch_add: context on another device");
   if (!c->have_sparsity || !c->have_form) return bfail(b, LMG_ERR_STATE, "batch_add: build sparsity and form first");
   if (std::find(b->ctx.begin(), b->ctx.end(), c) != b->ctx.end()) return LMG_OK;
-  const lmg_status st = lmg_context_set_stream(c, (void *)b->stream);
-  if (st) return bfail(b, st, "batch_add: " + c->err);
+  cudaSetDevice(b->device);
+  cudaEvent_t e = nullptr;
+  if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess)
+    return bfail(b, LMG_ERR_CUDA, "batch_add: event creation failed");
   c->perflog = false;
   b->ctx.push_back(c);
+  b->join.push_back(e);
   drop_graphs(b);
   b->warm[0] = b->warm[1] = false;
   return LMG_OK;
@@ -127,9 +134,9 @@ lmg_status lmg_batch_tune(lmg_batch *b, int32_t precision, int32_t reps) {
       c->ctas_per_sm = k;
       st = lmg_assemble(c, precision, nullptr, nullptr, 1);
       if (st) break;
-      cudaEventRecord(e0, b->stream);
+      cudaEventRecord(e0, c->stream);
       for (int r = 0; r < reps && !st; ++r) st = lmg_assemble(c, precision, nullptr, nullptr, 1);
-      cudaEventRecord(e1, b->stream);
+      cudaEventRecord(e1, c->stream);
       if (st || cudaEventSynchronize(e1) != cudaSuccess) break;
       float ms = 0.f;
       cudaEventElapsedTime(&ms, e0, e1);
@@ -164,10 +171,17 @@ lmg_status lmg_batch_assemble(lmg_batch *b, int32_t precision) {
     if (cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
       return bfail(b, LMG_ERR_CUDA, "batch_assemble: stream capture failed to start");
     lmg_status st = LMG_OK;
-    for (lmg_ctx *c : b->ctx) {
+    cudaError_t fe = cudaEventRecord(b->fork, b->stream);
+    for (size_t i = 0; i < b->ctx.size() && !st && fe == cudaSuccess; ++i) {
+      lmg_ctx *c = b->ctx[i];
+      fe = cudaStreamWaitEvent(c->stream, b->fork, 0);   // the context's stream joins the capture
+      if (fe != cudaSuccess) break;
       st = lmg_assemble(c, precision, nullptr, nullptr, 1);
       if (st) break;
+      fe = cudaEventRecord(b->join[i], c->stream);
+      if (fe == cudaSuccess) fe = cudaStreamWaitEvent(b->stream, b->join[i], 0);
     }
+    if (fe != cudaSuccess && !st) st = LMG_ERR_CUDA;
     cudaGraph_t g = nullptr;
     const cudaError_t ce = cudaStreamEndCapture(b->stream, &g);
     if (st || ce != cudaSuccess || !g) {
