@@ -88,12 +88,14 @@ __device__ __forceinline__ DF slot_sum(const GatherArgs &g, const TV *Kb, int32_
 
 // FP64 drop-in insertion, warp per block row P.  Lane l < (32/B2)*B2 owns entry
 // rem = l % B2 of the slots jj = l / B2 + (32/B2) t, so the B2 values of one
-// stored element block are read by B2 neighbouring lanes as one chunk.  Both
-// forms are symmetric and their sums run over the same element blocks in the
-// same order, so K_QP = K_PQ^T bit for bit: a row computes its diagonal and
-// upper slots and writes each upper value into the transposed slot as well.  Each
-// value is the sum, in element order, of the double-float element entries that
-// land on it, rounded once to FP64.
+// stored element block are read by B2 neighbouring lanes as one chunk.  Every
+// slot of the row is summed (a lower slot reads the stored upper element block
+// transposed), so each row of K is written contiguously: writing the upper
+// values into their transposed slots instead scatters 8-byte stores over other
+// rows and measured slower.  Both forms are symmetric and a slot and its
+// transpose sum the same entries in the same element order, so K_QP = K_PQ^T bit
+// for bit.  Each value is the sum, in element order, of the double-float
+// element entries that land on it, rounded once to FP64.
 template <int BS>
 __global__ void __launch_bounds__(256) k_gather(GatherArgs g) {
   constexpr int B2 = BS * BS, SPL = 32 / B2;
@@ -107,25 +109,14 @@ __global__ void __launch_bounds__(256) k_gather(GatherArgs g) {
     const int64_t rb = g.brow_ptr[P];
     const int deg = (int)(g.brow_ptr[P + 1] - rb);
     const int32_t rowp = act ? g.row_ptr[BS * P + i] : 0;
-    // the diagonal and upper slots are the suffix of the sorted block row
-    int lo = 0, hi = deg;
-    while (lo < hi) {
-      const int mid = (lo + hi) >> 1;
-      if (g.bcol[rb + mid] < (int32_t)P) lo = mid + 1; else hi = mid;
-    }
-    for (int jj = lo + js; act && jj < deg; jj += SPL) {
+    for (int jj = js; act && jj < deg; jj += SPL) {
       const int64_t j = rb + jj;
       const int32_t Q = g.bcol[j];
       const int32_t c0 = g.bptr[j], c1 = g.bptr[j + 1];
       const bool diag = Q == (int32_t)P;
       const DF s = diag ? slot_sum<B2>(g, g.Kdiag2, c0, c1, rem, rem, false)
                         : slot_sum<B2>(g, g.Koff2, c0, c1, rem, tr, true);
-      const double v = df_to_double(s);
-      g.K[rowp + jj * BS + k] = v;
-      if (!diag) {  // K is symmetric entry by entry: K_QP^{ki} = K_PQ^{ik}
-        const int32_t jt = g.tslot[j];
-        g.K[g.row_ptr[(int64_t)BS * Q + k] + (int64_t)(jt - g.brow_ptr[Q]) * BS + i] = v;
-      }
+      g.K[rowp + jj * BS + k] = df_to_double(s);
     }
     row_load<BS>(g, P, lane);
   }
