@@ -52,7 +52,6 @@ struct GatherArgs {
   const int64_t *brow_ptr;    // [n_blocks+1]
   const int32_t *row_ptr;     // [n_dofs+1]
   const int32_t *bcol;        // [nnzb]
-  const int32_t *tslot;       // [nnzb] block slot of the transposed pair (Q,P)
   const int32_t *bptr;        // [nnzb+1] contributions per block slot
   // Per slot, ascending in element: diagonal slots hold e*nb + a (a Kdiag
   // block); off-diagonal slots hold 2*(e*no + o) + t, o the strictly upper

@@ -57,24 +57,6 @@ __global__ void k_slots(int64_t n_elem, int nb, const int32_t *eb, const int64_t
   }
 }
 
-// Block slot of the transposed pair: for slot j = (P, Q), the position of P in
-// block row Q (the pattern is structurally symmetric).
-__global__ void k_tslot(int64_t n_blocks, const int64_t *brow_ptr, const int32_t *bcol, int32_t *tslot) {
-  const int lane = threadIdx.x & 31;
-  for (int64_t P = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; P < n_blocks;
-       P += ((int64_t)gridDim.x * blockDim.x) >> 5) {
-    for (int64_t j = brow_ptr[P] + lane; j < brow_ptr[P + 1]; j += 32) {
-      const int32_t Q = bcol[j];
-      int64_t lo = brow_ptr[Q], hi = brow_ptr[Q + 1];
-      while (lo < hi) {
-        const int64_t mid = (lo + hi) >> 1;
-        if (bcol[mid] < (int32_t)P) lo = mid + 1; else hi = mid;
-      }
-      tslot[j] = (int32_t)lo;
-    }
-  }
-}
-
 __global__ void k_count_rows(int64_t n, const int32_t *eb, int32_t *cnt) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x)
@@ -342,7 +324,7 @@ lmg_status lmg_context_destroy(lmg_ctx *c) {
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
   dfree(c->d_xyz); dfree(c->d_conn); dfree(c->d_aff); dfree(c->d_gen); dfree(c->d_eb);
-  dfree(c->d_cmask); dfree(c->d_cons); dfree(c->d_brow_ptr); dfree(c->d_bcol); dfree(c->d_tslot); dfree(c->d_row_ptr); dfree(c->d_col);
+  dfree(c->d_cmask); dfree(c->d_cons); dfree(c->d_brow_ptr); dfree(c->d_bcol); dfree(c->d_row_ptr); dfree(c->d_col);
   dfree(c->d_bptr); dfree(c->d_bcontrib); dfree(c->d_fptr); dfree(c->d_fcontrib); dfree(c->d_tab);
   dfree(c->d_coef); dfree(c->d_f); dfree(c->d_f2); dfree(c->d_Kdiag2); dfree(c->d_Koff2); dfree(c->d_Fe2); dfree(c->d_K);
   dfree(c->d_F); dfree(c->d_Koff32); dfree(c->d_status); dfree(c->d_bad);
@@ -461,10 +443,6 @@ lmg_status lmg_sparsity_build(lmg_ctx *c, int64_t *nnz) {
   LMG_CUDA(c, dalloc(c->d_col, (size_t)c->nnz));
   k_expand_cols<<<grid_for(c, c->n_dofs * 32, 256), 256, 0, c->stream>>>(
       c->n_dofs, c->bs, c->d_brow_ptr, c->d_bcol, c->d_row_ptr, c->d_col);
-  c->launches++;
-  LMG_CUDA(c, dalloc(c->d_tslot, (size_t)c->nnzb));
-  k_tslot<<<grid_for(c, c->n_blocks * 32, 256), 256, 0, c->stream>>>(c->n_blocks, c->d_brow_ptr, c->d_bcol,
-                                                                       c->d_tslot);
   c->launches++;
   lmg_status st = build_plan(c);
   if (st) return st;
@@ -717,7 +695,6 @@ lmg_status lmg_assemble(lmg_ctx *c, int32_t precision, double *K, double *F, int
   g.brow_ptr = c->d_brow_ptr;
   g.row_ptr = c->d_row_ptr;
   g.bcol = c->d_bcol;
-  g.tslot = c->d_tslot;
   g.bptr = c->d_bptr;
   g.bcontrib = c->d_bcontrib;
   g.no = c->nb * (c->nb - 1) / 2;

@@ -41,7 +41,7 @@ struct lmg_ctx {
   bool have_sparsity = false;
   int64_t nnz = 0, nnzb = 0;
   int64_t *d_brow_ptr = nullptr;
-  int32_t *d_bcol = nullptr, *d_row_ptr = nullptr, *d_col = nullptr, *d_tslot = nullptr;
+  int32_t *d_bcol = nullptr, *d_row_ptr = nullptr, *d_col = nullptr;
   int32_t *d_bptr = nullptr, *d_bcontrib = nullptr, *d_fptr = nullptr, *d_fcontrib = nullptr;
   // form
   bool have_form = false;
