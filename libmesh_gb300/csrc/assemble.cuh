@@ -44,6 +44,23 @@ struct ElemArgs {
   DevFE fe;
 };
 
+// Fused mixed assembly (element contraction and insertion in one row kernel).
+struct FusedArgs {
+  ElemArgs el;                // geometry, coefficients, loads, mask, status; list = elements
+  float *geo;                 // [n_elem][NG] per-element FP32 operands of the contraction
+  int64_t n_brows;
+  const int64_t *brow_ptr;    // [n_brows+1]
+  const int32_t *bcol;        // [nnzb]
+  const int32_t *row_ptr;     // [n_dofs+1]
+  const int32_t *fptr;        // [n_brows+1] incidences of each block row
+  const int32_t *fcontrib;    // e*N + a, ascending (element order)
+  const uint8_t *relslot;     // [n_elem][N][N] slot of block (a, b) inside block row of a
+  const uint8_t *constrained; // [n_dofs]
+  int max_deg;                // largest block-row degree
+  double *K;
+  double *F;
+};
+
 // Scatter plan: gather-by-slot segmented reduction into CSR values.
 struct GatherArgs {
   int64_t n_dofs;
@@ -89,6 +106,9 @@ bool launch_vjp(int form, int n, int nv, bool region, const VjpArgs &v, int grid
 void launch_gather_f(const GatherArgs &g, cudaStream_t s);
 
 // Whether an element kernel is instantiated for (form, shapes per variable, variables).
+bool fused_built(int form, int n, int nv);
+// k_geo then k_rows_mixed; returns false if no kernel is built for the case.
+bool launch_fused_mixed(int form, int n, int nv, const FusedArgs &f, int grid, cudaStream_t s);
 bool elements_built(int form, int n, int nv);
 void launch_elements(int form, int n, int nv, bool affine, bool mixed, const ElemArgs &a, int grid,
                      cudaStream_t s);

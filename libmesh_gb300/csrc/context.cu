@@ -57,6 +57,17 @@ __global__ void k_slots(int64_t n_elem, int nb, const int32_t *eb, const int64_t
   }
 }
 
+// Slot of block (a, b) relative to the start of block row eb[e][a] (fits a
+// byte when every block row has at most 255 slots).
+__global__ void k_relslot(int64_t npair, int nb, const int32_t *eb, const int64_t *brow_ptr, const int32_t *slot,
+                          uint8_t *rel) {
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < npair;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t ea = idx / nb;  // e * nb + a
+    rel[idx] = (uint8_t)(slot[idx] - brow_ptr[eb[ea]]);
+  }
+}
+
 __global__ void k_count_rows(int64_t n, const int32_t *eb, int32_t *cnt) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x)
@@ -246,6 +257,13 @@ lmg_status build_plan(lmg_ctx *c) {
   k_segsort<<<grid_for(c, c->nnzb, 256), 256, 0, c->stream>>>(c->nnzb, c->d_bptr, c->d_bcontrib);
   k_encode<<<grid_for(c, npair, 256), 256, 0, c->stream>>>(npair, nb, c->d_bcontrib);
   c->launches += 3;
+  dfree(c->d_relslot);
+  if (c->max_bdeg <= 255) {  // the fused mixed form addresses slots with one byte
+    LMG_CUDA(c, dalloc(c->d_relslot, (size_t)npair));
+    k_relslot<<<grid_for(c, npair, 256), 256, 0, c->stream>>>(npair, nb, c->d_eb, c->d_brow_ptr, slot,
+                                                              c->d_relslot);
+    c->launches++;
+  }
   // vector plan
   LMG_CUDA(c, cudaMemsetAsync(cnt, 0, sizeof(int32_t) * c->n_blocks, c->stream));
   k_count_rows<<<grid_for(c, nrow, 256), 256, 0, c->stream>>>(nrow, c->d_eb, cnt);
@@ -328,6 +346,7 @@ lmg_status lmg_context_destroy(lmg_ctx *c) {
   dfree(c->d_bptr); dfree(c->d_bcontrib); dfree(c->d_fptr); dfree(c->d_fcontrib); dfree(c->d_tab);
   dfree(c->d_coef); dfree(c->d_f); dfree(c->d_f2); dfree(c->d_Kdiag2); dfree(c->d_Koff2); dfree(c->d_Fe2); dfree(c->d_K);
   dfree(c->d_F); dfree(c->d_Koff32); dfree(c->d_status); dfree(c->d_bad);
+  dfree(c->d_relslot); dfree(c->d_geo);
   general_free(c);
   dfree(c->d_D6); dfree(c->d_modes);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
@@ -430,6 +449,8 @@ lmg_status lmg_sparsity_build(lmg_ctx *c, int64_t *nnz) {
   build_block_graph(c->n_elem, c->nb, c->h_eb.data(), c->n_blocks, brow, bcol, hw ? (int)hw : 4);
   c->nnzb = (int64_t)bcol.size();
   c->nnz = c->nnzb * c->bs * c->bs;
+  c->max_bdeg = 0;
+  for (size_t P = 0; P + 1 < brow.size(); ++P) c->max_bdeg = std::max(c->max_bdeg, (int)(brow[P + 1] - brow[P]));
   if (c->nnz >= INT32_MAX) return fail(c, LMG_ERR_UNSUPPORTED, "nnz exceeds 32-bit CSR");
   std::vector<int32_t> row_ptr((size_t)c->n_dofs + 1);
   row_ptr[0] = 0;
@@ -648,8 +669,11 @@ lmg_status lmg_assemble(lmg_ctx *c, int32_t precision, double *K, double *F, int
     return check_status(c, "assemble");
   }
   const bool mixed = precision == LMG_MIXED;
-  if (mixed && !c->d_Koff32)
+  const bool fused = mixed && c->h_gen.empty() && c->d_relslot && fused_built(c->form, c->tab.n, c->n_vars);
+  if (mixed && !fused && !c->d_Koff32)
     LMG_CUDA(c, dalloc(c->d_Koff32, (size_t)c->n_elem * c->nb * (c->nb - 1) / 2 * c->bs * c->bs));
+  if (fused && !c->d_geo)
+    LMG_CUDA(c, dalloc(c->d_geo, (size_t)c->n_elem * (c->form == LMG_POISSON ? 9 : 11)));
   lmg_status st = reset_status(c);
   if (st) return st;
   ElemArgs a{};
@@ -674,6 +698,36 @@ lmg_status lmg_assemble(lmg_ctx *c, int32_t precision, double *K, double *F, int
     for (auto &e : e3) LMG_CUDA(c, cudaEventCreate(&e));
     for (auto &e : e3) c->ev.push_back(e);
     LMG_CUDA(c, cudaEventRecord(e3[0], c->stream));
+  }
+  if (fused) {  // mixed form, one row kernel: no element-block buffer
+    FusedArgs f{};
+    f.el = a;
+    f.el.n_list = (int64_t)c->h_aff.size();
+    f.el.list = c->d_aff;
+    f.geo = c->d_geo;
+    f.n_brows = c->n_blocks;
+    f.brow_ptr = c->d_brow_ptr;
+    f.bcol = c->d_bcol;
+    f.row_ptr = c->d_row_ptr;
+    f.fptr = c->d_fptr;
+    f.fcontrib = c->d_fcontrib;
+    f.relslot = c->d_relslot;
+    f.constrained = c->d_cons;
+    f.max_deg = c->max_bdeg;
+    f.K = c->d_K;
+    f.F = c->d_F;
+    launch_fused_mixed(c->form, c->tab.n, c->n_vars, f, grid, c->stream);
+    c->launches += 2;
+    if (c->perflog) {
+      LMG_CUDA(c, cudaEventRecord(e3[1], c->stream));
+      LMG_CUDA(c, cudaEventRecord(e3[2], c->stream));
+    }
+    LMG_CUDA(c, cudaGetLastError());
+    const cudaMemcpyKind kind = out_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    if (K) LMG_CUDA(c, cudaMemcpyAsync(K, c->d_K, sizeof(double) * c->nnz, kind, c->stream));
+    if (F) LMG_CUDA(c, cudaMemcpyAsync(F, c->d_F, sizeof(double) * c->n_dofs, kind, c->stream));
+    if (out_on_device || (!K && !F)) return LMG_OK;
+    return check_status(c, "assemble");
   }
   if (!c->h_aff.empty()) {
     a.n_list = (int64_t)c->h_aff.size();

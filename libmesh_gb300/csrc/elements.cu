@@ -40,6 +40,7 @@
 
 #include "assemble.cuh"
 #include "df.cuh"
+#include "row_load.cuh"
 #include "../../include/libmesh_gb300.h"
 
 namespace lmg {
@@ -138,6 +139,59 @@ __device__ __forceinline__ void st(float2 &o, DF v) { o = make_float2(v.hi, v.lo
 //   POISSON:    A_mn = k detJ (G G^T)_mn                    (9)
 //   ELASTICITY: G_mn, lam detJ, mu detJ                     (11)
 template <int FORM> struct Geo { static constexpr int NG = (FORM == LMG_POISSON) ? 9 : 11; };
+
+// One element block from the per-element operands gv (Geo<FORM>::NG values)
+// and the reference tensors sv = S^{mn}_{ab} (9 values) of the block (a, b):
+//   POISSON    K_ab = sum_mn A_mn S^{mn}_ab
+//   ELASTICITY K^{ik}_ab = lam' P^{ik} + mu' P^{ki} + d_ik mu' tr P, P = G^T S_ab G.
+// Shared by the element kernel and the fused row kernel so that both produce
+// the same bits.
+template <int FORM, typename R>
+__device__ __forceinline__ void contract_block(const typename R::V *gv, const typename R::V *sv,
+                                               typename R::V *out) {
+  using V = typename R::V;
+  if (FORM == LMG_POISSON) {
+    V acc = R::zero();
+#pragma unroll
+    for (int mn = 0; mn < 9; ++mn) acc = R::fma(acc, gv[mn], sv[mn]);
+    out[0] = R::norm(acc);
+  } else {
+    // P = G^T S_ab G (T = S_ab G, then G^T T); K^{ik} = lam' P^{ik} + mu' P^{ki} + d_ik mu' tr P
+    V Tm[9];
+#pragma unroll
+    for (int m = 0; m < 3; ++m)
+#pragma unroll
+      for (int kk = 0; kk < 3; ++kk) {
+        V acc = R::zero();
+#pragma unroll
+        for (int n = 0; n < 3; ++n) acc = R::fma(acc, sv[3 * m + n], gv[3 * n + kk]);
+        Tm[3 * m + kk] = R::norm(acc);
+      }
+    V Pm[9];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int kk = 0; kk < 3; ++kk) {
+        V acc = R::zero();
+#pragma unroll
+        for (int m = 0; m < 3; ++m) acc = R::fma(acc, gv[3 * m + i], Tm[3 * m + kk]);
+        Pm[3 * i + kk] = R::norm(acc);
+      }
+    V tr = R::zero();
+#pragma unroll
+    for (int i = 0; i < 3; ++i) tr = R::fma(tr, Pm[4 * i], R::from(1.0));
+    tr = R::norm(tr);
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int kk = 0; kk < 3; ++kk) {
+        V acc = R::fma(R::zero(), gv[9], Pm[3 * i + kk]);
+        acc = R::fma(acc, gv[10], Pm[3 * kk + i]);
+        if (i == kk) acc = R::fma(acc, gv[10], tr);
+        out[3 * i + kk] = R::norm(acc);
+      }
+  }
+}
 
 // Byte offsets of the affine kernel's dynamic shared memory (4 warps per CTA).
 __host__ __device__ constexpr size_t al16(size_t x) { return (x + 15) & ~(size_t)15; }
@@ -251,47 +305,7 @@ __global__ void __launch_bounds__(128) k_elem_affine(ElemArgs a) {
 #pragma unroll
           for (int mn = 0; mn < 9; ++mn) sv[mn] = R::ld(sS[mn * NB + blk]);
           V out[B2];
-          if (FORM == LMG_POISSON) {
-            V acc = R::zero();
-#pragma unroll
-            for (int mn = 0; mn < 9; ++mn) acc = R::fma(acc, gv[mn], sv[mn]);
-            out[0] = R::norm(acc);
-          } else {
-            // P = G^T S_ab G (T = S_ab G, then G^T T); K^{ik} = lam' P^{ik} + mu' P^{ki} + d_ik mu' tr P
-            V Tm[9];
-#pragma unroll
-            for (int m = 0; m < 3; ++m)
-#pragma unroll
-              for (int kk = 0; kk < 3; ++kk) {
-                V acc = R::zero();
-#pragma unroll
-                for (int n = 0; n < 3; ++n) acc = R::fma(acc, sv[3 * m + n], gv[3 * n + kk]);
-                Tm[3 * m + kk] = R::norm(acc);
-              }
-            V Pm[9];
-#pragma unroll
-            for (int i = 0; i < 3; ++i)
-#pragma unroll
-              for (int kk = 0; kk < 3; ++kk) {
-                V acc = R::zero();
-#pragma unroll
-                for (int m = 0; m < 3; ++m) acc = R::fma(acc, gv[3 * m + i], Tm[3 * m + kk]);
-                Pm[3 * i + kk] = R::norm(acc);
-              }
-            V tr = R::zero();
-#pragma unroll
-            for (int i = 0; i < 3; ++i) tr = R::fma(tr, Pm[4 * i], R::from(1.0));
-            tr = R::norm(tr);
-#pragma unroll
-            for (int i = 0; i < 3; ++i)
-#pragma unroll
-              for (int kk = 0; kk < 3; ++kk) {
-                V acc = R::fma(R::zero(), gv[9], Pm[3 * i + kk]);
-                acc = R::fma(acc, gv[10], Pm[3 * kk + i]);
-                if (i == kk) acc = R::fma(acc, gv[10], tr);
-                out[3 * i + kk] = R::norm(acc);
-              }
-          }
+          contract_block<FORM, R>(gv, sv, out);
 #pragma unroll
           for (int ik = 0; ik < B2; ++ik) {
             const int i = ik / NV, kk = ik - i * NV;
@@ -446,11 +460,223 @@ void launch_t(bool affine, const ElemArgs &a, int grid, cudaStream_t s) {
   }
 }
 
+
+// ---------------------------------------------------------------- fused mixed form
+// The mixed form without the element-block buffer: k_geo stores each element's
+// FP32 operands (the values the element kernel keeps in shared memory) and its
+// double-float load vector; k_rows_mixed then runs one warp per block row P,
+// walks the elements touching P in element order (the load-vector plan lists
+// them), recomputes the element blocks of P's row with contract_block, and adds
+// them in FP32 into a shared-memory row, as the insertion would sum the stored
+// blocks.  The epilogue is the mixed insertion's: Dirichlet masking and the
+// diagonal rebuilt from double-float row sums.  Same bits as element kernel +
+// mixed insertion, without writing and re-reading the blocks.
+template <int FORM, int N, int NV>
+__global__ void __launch_bounds__(128) k_geo(FusedArgs f) {
+  using R = Ar<float>;
+  constexpr int NG = Geo<FORM>::NG;
+  const ElemArgs &a = f.el;
+  __shared__ float2 sM[N * N];  // the mass matrix as double-float pairs, split once per CTA
+  for (int i = threadIdx.x; i < N * N; i += blockDim.x) {
+    const DF d = df_split(a.fe.M[i]);
+    sM[i] = make_float2(d.hi, d.lo);
+  }
+  __syncthreads();
+  for (int64_t li = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; li < a.n_list;
+       li += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t e = a.list[li];
+    const int32_t *c = a.conn + (int64_t)e * a.npe;
+    double G[9], det;
+    {
+      double X[N * 3];
+#pragma unroll
+      for (int g = 0; g < N; ++g) {
+        const double *p = a.xyz + 3 * (int64_t)c[g];
+        X[3 * g] = p[0];
+        X[3 * g + 1] = p[1];
+        X[3 * g + 2] = p[2];
+      }
+      det = jacobian(X, a.fe.gdphi, N, G);
+    }
+    if (!(det > 0.0)) report_bad(a, LMG_ERR_DEGENERATE, e);
+    const double coef = a.coef ? a.coef[e] : 1.0;
+    float *g = f.geo + (int64_t)e * NG;
+    if (FORM == LMG_POISSON) {
+      const double sc = coef * det;
+#pragma unroll
+      for (int m = 0; m < 3; ++m)
+#pragma unroll
+        for (int n = 0; n < 3; ++n)
+          g[3 * m + n] = R::from(sc * (G[3 * m] * G[3 * n] + G[3 * m + 1] * G[3 * n + 1] + G[3 * m + 2] * G[3 * n + 2]));
+    } else {
+      double lam, mu;
+      lame(coef, a.nu, lam, mu);
+#pragma unroll
+      for (int i = 0; i < 9; ++i) g[i] = R::from(G[i]);
+      g[9] = R::from(lam * det);
+      g[10] = R::from(mu * det);
+    }
+    // load vector, as the element kernel computes it
+    const uint64_t mask = a.cmask[e];
+    float2 *Fo = a.Fe2 + (int64_t)e * N * NV;
+    const DF dd = df_split(det);
+    for (int ai = 0; ai < N; ++ai)
+#pragma unroll
+      for (int v = 0; v < NV; ++v) {
+        DF s = {0.f, 0.f};
+        if (a.nodal_f2)
+          for (int b = 0; b < N; ++b) {
+            const float2 fb = a.nodal_f2[(int64_t)c[b] * NV + v], mb = sM[ai * N + b];
+            s = df_fma_lazy(s, DF{mb.x, mb.y}, DF{fb.x, fb.y});
+          }
+        s = df_norm(df_fma_lazy(DF{0.f, 0.f}, df_norm(s), dd));
+        Fo[ai * NV + v] = ((mask >> (v * N + ai)) & 1ull) ? make_float2(0.f, 0.f) : make_float2(s.hi, s.lo);
+      }
+  }
+}
+
+template <int FORM, int N, int NV>
+__global__ void __launch_bounds__(256) k_rows_mixed(FusedArgs f) {
+  using R = Ar<float>;
+  constexpr int NG = Geo<FORM>::NG, B2 = NV * NV, NPASS = 32 / N, SPL = 32 / B2;
+  extern __shared__ float fsm[];
+  float *sS = fsm;  // [9][N*N]
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  float *acc = sS + 9 * N * N + (int64_t)warp * f.max_deg * B2;
+  for (int i = threadIdx.x; i < 9 * N * N; i += blockDim.x) sS[i] = R::from(f.el.fe.S[i]);
+  __syncthreads();
+  const int wi = lane / N, bl = lane - wi * N;  // incidence slot and local column node of this lane
+  const int js = lane / B2, rem = lane - js * B2;
+  const bool act = lane < SPL * B2;
+  const int i = rem / NV, k = rem - i * NV;
+  for (int64_t P = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; P < f.n_brows;
+       P += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+    const int64_t rb = f.brow_ptr[P];
+    const int deg = (int)(f.brow_ptr[P + 1] - rb);
+    const int32_t t0 = f.fptr[P], t1 = f.fptr[P + 1];
+    __syncwarp();
+    for (int x = lane; x < deg * B2; x += 32) acc[x] = 0.f;
+    __syncwarp();
+    for (int32_t tg = t0; tg < t1; tg += NPASS) {
+      const int32_t t = tg + wi;
+      const bool valid = lane < NPASS * N && t < t1;
+      const int32_t code = valid ? f.fcontrib[t] : 0;
+      const int32_t e = code / N, ae = code - e * N;
+      const bool work = valid && bl != ae;
+      float out[B2];
+      int rel = 0;
+      if (work) {
+        float gv[NG];
+#pragma unroll
+        for (int q = 0; q < NG; ++q) gv[q] = f.geo[(int64_t)e * NG + q];
+        const int ra = ae < bl ? ae : bl, cb = ae < bl ? bl : ae;
+        float sv[9];
+#pragma unroll
+        for (int mn = 0; mn < 9; ++mn) sv[mn] = sS[mn * N * N + ra * N + cb];
+        contract_block<FORM, R>(gv, sv, out);
+        if (NV > 1 && bl < ae) {  // the stored block is (b, a): take its transpose
+#pragma unroll
+          for (int p = 0; p < NV; ++p)
+#pragma unroll
+            for (int q = p + 1; q < NV; ++q) {
+              const float tmp = out[p * NV + q];
+              out[p * NV + q] = out[q * NV + p];
+              out[q * NV + p] = tmp;
+            }
+        }
+        rel = f.relslot[(int64_t)code * N + bl];
+      }
+      // element order: the incidences of this pass add one after the other
+#pragma unroll
+      for (int w = 0; w < NPASS; ++w) {
+        if (work && wi == w)
+#pragma unroll
+          for (int ik = 0; ik < B2; ++ik) acc[rel * B2 + ik] = __fadd_rn(acc[rel * B2 + ik], out[ik]);
+        __syncwarp();
+      }
+    }
+    // epilogue of the mixed insertion, reading the row from shared memory
+    const int32_t rowp = act ? f.row_ptr[NV * P + i] : 0;
+    const bool rc = act && f.constrained[NV * P + i] != 0;
+    DF racc = {0.f, 0.f};
+    int jdiag = -1;
+    for (int jj = js; act && jj < deg; jj += SPL) {
+      const int32_t Q = f.bcol[rb + jj];
+      if (Q == (int32_t)P) { jdiag = jj; continue; }
+      const float kv = acc[jj * B2 + rem];
+      racc = df_add1(racc, kv);
+      const bool msk = rc || f.constrained[(int64_t)NV * Q + k] != 0;
+      f.K[rowp + jj * NV + k] = msk ? 0.0 : f2d(kv);
+    }
+    if constexpr (B2 == 1) {
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        DF y;
+        y.hi = __shfl_xor_sync(0xffffffffu, racc.hi, o);
+        y.lo = __shfl_xor_sync(0xffffffffu, racc.lo, o);
+        racc = (lane & o) ? df_add(y, racc) : df_add(racc, y);
+      }
+    } else {
+#pragma unroll
+      for (int t = 1; t < SPL; ++t) {
+        DF y;
+        y.hi = __shfl_sync(0xffffffffu, racc.hi, (lane + t * B2) & 31);
+        y.lo = __shfl_sync(0xffffffffu, racc.lo, (lane + t * B2) & 31);
+        if (lane < B2) racc = df_add(racc, y);
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) jdiag = max(jdiag, __shfl_xor_sync(0xffffffffu, jdiag, o));
+    if (lane < B2 && jdiag >= 0) {
+      double v = -(f2d(racc.hi) + f2d(racc.lo));
+      if (rc || f.constrained[NV * P + k] != 0) v = (i == k) ? (double)(t1 - t0) : 0.0;
+      f.K[rowp + jdiag * NV + k] = v;
+    }
+    row_load_f<NV>(f.fptr, f.fcontrib, f.el.Fe2, f.F, P, lane);
+  }
+}
+
+template <int FORM, int N, int NV>
+void launch_fused_t(const FusedArgs &f, int grid, cudaStream_t s) {
+  const int64_t gb = (f.el.n_list + 127) / 128;
+  if (gb > 0) k_geo<FORM, N, NV><<<(int)(gb < grid ? gb : grid), 128, 0, s>>>(f);
+  const size_t smem = sizeof(float) * (9 * N * N + (size_t)8 * f.max_deg * NV * NV);
+  static size_t attr = 0;
+  if (smem > attr) {
+    cudaFuncSetAttribute(k_rows_mixed<FORM, N, NV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    attr = smem;
+  }
+  const int64_t rb = (f.n_brows + 7) / 8;
+  if (rb > 0) k_rows_mixed<FORM, N, NV><<<(int)(rb < grid ? rb : grid), 256, smem, s>>>(f);
+}
+
 }  // namespace
 
 bool elements_built(int form, int n, int nv) {
   return (form == LMG_POISSON && nv == 1 && (n == 4 || n == 8 || n == 10 || n == 27)) ||
          (form == LMG_ELASTICITY && nv == 3 && (n == 4 || n == 8 || n == 10));
+}
+
+bool fused_built(int form, int n, int nv) {
+  return (form == LMG_POISSON && nv == 1 && (n == 4 || n == 8 || n == 10 || n == 27)) ||
+         (form == LMG_ELASTICITY && nv == 3 && (n == 4 || n == 8 || n == 10));
+}
+
+bool launch_fused_mixed(int form, int n, int nv, const FusedArgs &f, int grid, cudaStream_t s) {
+#define LMG_F(F, NN, V)                   \
+  if (form == F && n == NN && nv == V) {  \
+    launch_fused_t<F, NN, V>(f, grid, s); \
+    return true;                          \
+  }
+  LMG_F(LMG_POISSON, 4, 1)
+  LMG_F(LMG_POISSON, 8, 1)
+  LMG_F(LMG_POISSON, 10, 1)
+  LMG_F(LMG_POISSON, 27, 1)
+  LMG_F(LMG_ELASTICITY, 4, 3)
+  LMG_F(LMG_ELASTICITY, 8, 3)
+  LMG_F(LMG_ELASTICITY, 10, 3)
+#undef LMG_F
+  return false;
 }
 
 void launch_elements(int form, int n, int nv, bool affine, bool mixed, const ElemArgs &a, int grid,

@@ -19,44 +19,15 @@
 
 #include "assemble.cuh"
 #include "df.cuh"
+#include "row_load.cuh"
 
 namespace lmg {
 
 namespace {
 
-// Load vector of block row P: the element entries that land on each of its bs
-// dofs, summed in double-float by a fixed butterfly over the warp (lane l takes
-// contributions l, l+32, ... in element order), rounded once to FP64.
 template <int BS>
 __device__ __forceinline__ void row_load(const GatherArgs &g, int64_t P, int lane) {
-  const int32_t f0 = g.fptr[P], f1 = g.fptr[P + 1];
-  DF s[BS];
-#pragma unroll
-  for (int i = 0; i < BS; ++i) s[i] = {0.f, 0.f};
-  for (int32_t c = f0 + lane; c < f1; c += 32) {
-    const int64_t base = (int64_t)g.fcontrib[c] * BS;
-#pragma unroll
-    for (int i = 0; i < BS; ++i) {
-      const float2 v = g.Fe2[base + i];
-      s[i] = df_add(s[i], DF{v.x, v.y});
-    }
-  }
-#pragma unroll
-  for (int i = 0; i < BS; ++i)
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      DF y;
-      y.hi = __shfl_xor_sync(0xffffffffu, s[i].hi, o);
-      y.lo = __shfl_xor_sync(0xffffffffu, s[i].lo, o);
-      s[i] = (lane & o) ? df_add(y, s[i]) : df_add(s[i], y);
-    }
-  if (lane < BS) {
-    DF r = s[0];
-#pragma unroll
-    for (int i = 1; i < BS; ++i)
-      if (lane == i) r = s[i];
-    g.F[BS * P + lane] = df_to_double(r);
-  }
+  row_load_f<BS>(g.fptr, g.fcontrib, g.Fe2, g.F, P, lane);
 }
 
 // Contributions of one block slot to one entry, summed in double-float in
