@@ -375,6 +375,9 @@ def run_adjoint(args, local):
         g = asm.vjp_coef(u, z)
         vj.append(time.perf_counter() - t0)
     t["vjp_s"] = float(np.median(vj))
+    t0 = time.perf_counter()
+    gx = asm.vjp_xyz(u, z, region)
+    t["vjp_xyz_s"] = time.perf_counter() - t0
     asm.close()
     total = sum(t.values())
     print(json.dumps({
@@ -386,7 +389,7 @@ def run_adjoint(args, local):
                                % n, "n_elem": mesh.n_elem, "n_dofs": dm.n_dofs, "nnz": asm.nnz,
                    "cg_iterations": [it_u, it_z], "relres": [rr_u, rr_z]},
         "stages_s": t, "vjp_melem_per_s": mesh.n_elem / t["vjp_s"] / 1e6,
-        "q": float(qv @ u), "grad_norm": float(np.linalg.norm(g)),
+        "q": float(qv @ u), "grad_norm": float(np.linalg.norm(g)), "coord_grad_norm": float(np.linalg.norm(gx)),
         "e2e_note": "host timers around the public calls; u, z, q and the gradient cross the host boundary"}))
 
 

@@ -277,6 +277,13 @@ lmg_status lmg_cg_solve_noalloc(int64_t n_dofs, const int32_t *row_ptr, const in
  * geometry recomputed per quadrature point.  u, z, q, dq_dcoef are host arrays. */
 lmg_status lmg_qoi_region_load(lmg_ctx *ctx, const uint8_t *in_region, double *q);
 lmg_status lmg_vjp_coef(lmg_ctx *ctx, const double *u, const double *z, double *dq_dcoef);
+/* Node-coordinate sensitivities of the same QoI (Poisson form; the reference's
+ * ParameterVector over node coordinates): dq/dx = dq/dx|_u - z^T d(K u - F)/dx
+ * for every node, by reverse mode through detJ and J^{-1} at every quadrature
+ * point.  in_region[n_elem] marks the QoI elements (NULL: no explicit term);
+ * dq_dxyz [n_nodes][3]; all arrays on the host. */
+lmg_status lmg_vjp_xyz(lmg_ctx *ctx, const double *u, const double *z, const uint8_t *in_region,
+                       double *dq_dxyz);
 
 /* First failing element of the last call (-1 if none) and a message. */
 lmg_status lmg_last_error(lmg_ctx *ctx, int64_t *elem_id, char *msg, int32_t msg_len);

@@ -262,6 +262,14 @@ class GpuAssembly:
                                     ptr(np.ascontiguousarray(z, np.float64)), ptr(g)))
         return g
 
+    def vjp_xyz(self, u, z, in_region=None):
+        """dq/dx for every node coordinate (Poisson form): [n_nodes, 3]."""
+        g = np.empty((self.mesh.n_nodes, 3), np.float64)
+        reg = None if in_region is None else np.ascontiguousarray(in_region, np.uint8)
+        self._ok(lib().lmg_vjp_xyz(self.ctx, ptr(np.ascontiguousarray(u, np.float64)),
+                                   ptr(np.ascontiguousarray(z, np.float64)), ptr(reg), ptr(g)))
+        return g
+
     def perflog_enable(self, on=True):
         self._ok(lib().lmg_perflog_enable(self.ctx, 1 if on else 0))
 

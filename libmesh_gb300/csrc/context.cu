@@ -882,6 +882,50 @@ lmg_status lmg_vjp_coef(lmg_ctx *c, const double *u, const double *z, double *dq
   return st;
 }
 
+lmg_status lmg_vjp_xyz(lmg_ctx *c, const double *u, const double *z, const uint8_t *in_region, double *dq_dxyz) {
+  if (!c || !u || !z || !dq_dxyz) return fail(c, LMG_ERR_ARG, "vjp_xyz: bad argument");
+  if (c->general || c->form != LMG_POISSON || c->n_vars != 1)
+    return fail(c, LMG_ERR_UNSUPPORTED, "vjp_xyz: built for the Poisson form");
+  if (!c->have_sparsity || !c->have_form) return fail(c, LMG_ERR_STATE, "vjp_xyz: set up the system first");
+  cudaSetDevice(c->device);
+  double *du = nullptr, *dz = nullptr, *dx = nullptr, *drow = nullptr;
+  uint8_t *dreg = nullptr;
+  LMG_CUDA(c, dupload(c, du, u, (size_t)c->n_dofs));
+  LMG_CUDA(c, dupload(c, dz, z, (size_t)c->n_dofs));
+  if (in_region) LMG_CUDA(c, dupload(c, dreg, in_region, (size_t)c->n_elem));
+  LMG_CUDA(c, dalloc(dx, (size_t)c->n_elem * c->npe * 3));
+  LMG_CUDA(c, dalloc(drow, (size_t)c->n_blocks * 3));
+  lmg_status st = reset_status(c);
+  if (st) return st;
+  VjpArgs v = vjp_args(c);
+  v.u = du;
+  v.z = dz;
+  v.region = dreg;
+  v.coef = c->d_coef;
+  v.nodal_f = c->d_f;
+  v.xout = dx;
+  v.n_rows = c->n_blocks;
+  v.fptr = c->d_fptr;
+  v.fcontrib = c->d_fcontrib;
+  v.row_out = drow;
+  if (!launch_vjp_xyz(c->tab.n, v, c->n_sm * 8, c->stream))
+    return fail(c, LMG_ERR_UNSUPPORTED, "vjp_xyz: element not built");
+  c->launches += 2;
+  LMG_CUDA(c, cudaGetLastError());
+  std::vector<double> row((size_t)c->n_blocks * 3);
+  LMG_CUDA(c, cudaMemcpyAsync(row.data(), drow, sizeof(double) * row.size(), cudaMemcpyDeviceToHost, c->stream));
+  st = check_status(c, "vjp_xyz");
+  dfree(du); dfree(dz); dfree(dreg); dfree(dx); dfree(drow);
+  if (st) return st;
+  std::fill(dq_dxyz, dq_dxyz + 3 * c->n_nodes, 0.0);
+  for (int64_t e = 0; e < c->n_elem; ++e)  // node of every dof (one variable)
+    for (int a = 0; a < c->npe; ++a) {
+      const int64_t node = c->h_conn[(size_t)(e * c->npe + a)], dof = c->h_elem_dofs[(size_t)(e * c->nl + a)];
+      for (int d = 0; d < 3; ++d) dq_dxyz[3 * node + d] = row[(size_t)(3 * dof + d)];
+    }
+  return LMG_OK;
+}
+
 lmg_status lmg_cg_solve(lmg_ctx *c, const double *rhs, double *x, double rtol, int32_t maxit,
                         int32_t *iters, double *relres) {
   if (!c || !x || rtol <= 0 || maxit <= 0) return fail(c, LMG_ERR_ARG, "cg_solve: bad argument");

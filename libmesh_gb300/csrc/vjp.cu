@@ -161,6 +161,104 @@ __global__ void k_region_fe(VjpArgs v) {
   }
 }
 
+// Coordinate sensitivities, Poisson form (introduction_ex4.C:464-536 weak form):
+// with r = K(X) u - F(X) and q(u, X) = integral of u over the marked elements,
+//   dq/dX = dq/dX|_u - z^T dr/dX,
+// per element and quadrature point in reverse mode through detJ and J^{-1}
+// (J_en = dx_e/dxi_n, G = J^{-1}, v = grad u, w = grad z, hats = G applied again):
+//   d(detJ)/dJ_en          = detJ G_ne
+//   d(detJ w.v)/dJ_en      = detJ (G_ne w.v - v_e w^_n - w_e v^_n)
+// and dJ_en/dX_ae = dphi_map_a/dxi_n.  Every quadrature point takes its own
+// Jacobian, which is what central differences of the reference's assembly see
+// (a perturbed affine element is no longer affine).
+template <int N>
+__global__ void k_vjp_xyz(VjpArgs v) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < v.n_elem;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    double X[N * 3], U[N], Z[N], Fn[N], dX[N * 3];
+    const int32_t *c = v.conn + e * N;
+#pragma unroll
+    for (int a = 0; a < N; ++a) {
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        X[3 * a + d] = v.xyz[3 * (int64_t)c[a] + d];
+        dX[3 * a + d] = 0.0;
+      }
+      const int64_t dof = v.eb[e * N + a];
+      U[a] = v.u[dof];
+      Z[a] = v.z[dof];
+      Fn[a] = v.nodal_f ? v.nodal_f[c[a]] : 0.0;
+    }
+    const double k = v.coef ? v.coef[e] : 1.0;
+    const bool in_q = v.region && v.region[e];
+    bool bad = false;
+    for (int q = 0; q < v.fe.q; ++q) {
+      const double *gd = v.fe.gdphi + (int64_t)q * N * 3;
+      double G[9];
+      const double det = jac_inv(X, gd, N, G);
+      bad |= !(det > 0.0);
+      const double *dp = v.fe.dphi + (int64_t)q * N * 3, *ph = v.fe.phi + (int64_t)q * N;
+      double gu[3] = {0, 0, 0}, gz[3] = {0, 0, 0}, uq = 0.0, zq = 0.0, fq = 0.0;
+#pragma unroll
+      for (int a = 0; a < N; ++a) {
+#pragma unroll
+        for (int m = 0; m < 3; ++m) {
+          gu[m] += dp[3 * a + m] * U[a];
+          gz[m] += dp[3 * a + m] * Z[a];
+        }
+        uq += ph[a] * U[a];
+        zq += ph[a] * Z[a];
+        fq += ph[a] * Fn[a];
+      }
+      double vv[3], ww[3];
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        vv[d] = G[d] * gu[0] + G[3 + d] * gu[1] + G[6 + d] * gu[2];
+        ww[d] = G[d] * gz[0] + G[3 + d] * gz[1] + G[6 + d] * gz[2];
+      }
+      double vh[3], wh[3];
+#pragma unroll
+      for (int n = 0; n < 3; ++n) {
+        vh[n] = G[3 * n] * vv[0] + G[3 * n + 1] * vv[1] + G[3 * n + 2] * vv[2];
+        wh[n] = G[3 * n] * ww[0] + G[3 * n + 1] * ww[1] + G[3 * n + 2] * ww[2];
+      }
+      const double jw = det * v.fe.qw[q];
+      const double dot = vv[0] * ww[0] + vv[1] * ww[1] + vv[2] * ww[2];
+      // d/dJ of  (in_q ? jw uq : 0) - (k jw w.v - jw f z)
+      const double scal = (in_q ? jw * uq : 0.0) - k * jw * dot + jw * fq * zq;
+#pragma unroll
+      for (int ee = 0; ee < 3; ++ee)
+#pragma unroll
+        for (int n = 0; n < 3; ++n) {
+          const double cj = G[3 * n + ee] * scal + k * jw * (vv[ee] * wh[n] + ww[ee] * vh[n]);
+#pragma unroll
+          for (int a = 0; a < N; ++a) dX[3 * a + ee] += cj * gd[3 * a + n];
+        }
+    }
+    if (bad) {
+      atomicCAS(v.status, 0, LMG_ERR_DEGENERATE);
+      atomicMin(v.bad_elem, (unsigned long long)e);
+    }
+#pragma unroll
+    for (int i = 0; i < N * 3; ++i) v.xout[e * N * 3 + i] = dX[i];
+  }
+}
+
+// Per-dof sums of the element node contributions, in element order.
+__global__ void k_gather_xyz(VjpArgs v) {
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < v.n_rows;
+       r += (int64_t)gridDim.x * blockDim.x) {
+    double s[3] = {0.0, 0.0, 0.0};
+    for (int32_t t = v.fptr[r]; t < v.fptr[r + 1]; ++t) {
+      const int64_t code = v.fcontrib[t];
+#pragma unroll
+      for (int d = 0; d < 3; ++d) s[d] += v.xout[code * 3 + d];
+    }
+#pragma unroll
+    for (int d = 0; d < 3; ++d) v.row_out[r * 3 + d] = s[d];
+  }
+}
+
 template <int FORM, int N, int NV>
 void launch_v(bool region, const VjpArgs &v, int grid, cudaStream_t s) {
   const int64_t blocks = (v.n_elem + 127) / 128;
@@ -170,6 +268,19 @@ void launch_v(bool region, const VjpArgs &v, int grid, cudaStream_t s) {
 }
 
 }  // namespace
+
+bool launch_vjp_xyz(int n, const VjpArgs &v, int grid, cudaStream_t s) {
+  const int64_t blocks = (v.n_elem + 127) / 128;
+  const int g = (int)(blocks < grid ? blocks : grid);
+  if (n == 4) k_vjp_xyz<4><<<g, 128, 0, s>>>(v);
+  else if (n == 8) k_vjp_xyz<8><<<g, 128, 0, s>>>(v);
+  else if (n == 10) k_vjp_xyz<10><<<g, 128, 0, s>>>(v);
+  else if (n == 27) k_vjp_xyz<27><<<g, 128, 0, s>>>(v);
+  else return false;
+  const int64_t rb = (v.n_rows + 255) / 256;
+  k_gather_xyz<<<(int)(rb < grid ? rb : grid), 256, 0, s>>>(v);
+  return true;
+}
 
 bool launch_vjp(int form, int n, int nv, bool region, const VjpArgs &v, int grid, cudaStream_t s) {
 #define LMG_V(F, NN, V)                          \
