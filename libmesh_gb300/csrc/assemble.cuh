@@ -48,7 +48,8 @@ struct ElemArgs {
 struct FusedArgs {
   ElemArgs el;                // geometry, coefficients, loads, mask, status; list = elements
   float *geo;                 // [n_elem][NG] per-element FP32 operands of the contraction
-  int64_t n_brows;
+  int64_t n_brows;            // block rows [row_begin, n_brows) are assembled
+  int64_t row_begin;
   const int64_t *brow_ptr;    // [n_brows+1]
   const int32_t *bcol;        // [nnzb]
   const int32_t *row_ptr;     // [n_dofs+1]
@@ -64,6 +65,7 @@ struct FusedArgs {
 // Scatter plan: gather-by-slot segmented reduction into CSR values.
 struct GatherArgs {
   int64_t n_dofs;
+  int64_t row_begin, row_end; // block rows to insert (row_end 0 = all)
   int bs;                     // dofs per block (node-interleaved variables)
   int nb;                     // blocks per element
   const int64_t *brow_ptr;    // [n_blocks+1]
@@ -116,8 +118,9 @@ void launch_gather_f(const GatherArgs &g, cudaStream_t s);
 
 // Whether an element kernel is instantiated for (form, shapes per variable, variables).
 bool fused_built(int form, int n, int nv);
-// k_geo then k_rows_mixed; returns false if no kernel is built for the case.
-bool launch_fused_mixed(int form, int n, int nv, const FusedArgs &f, int grid, cudaStream_t s);
+// k_geo (when geo) then k_rows_mixed over f's rows (when rows); false if no kernel is built.
+bool launch_fused_mixed(int form, int n, int nv, const FusedArgs &f, int grid, cudaStream_t s, bool geo = true,
+                        bool rows = true);
 bool elements_built(int form, int n, int nv);
 void launch_elements(int form, int n, int nv, bool affine, bool mixed, const ElemArgs &a, int grid,
                      cudaStream_t s);

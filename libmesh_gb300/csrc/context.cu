@@ -281,6 +281,39 @@ lmg_status build_plan(lmg_ctx *c) {
   return check_status(c, "sparsity plan");
 }
 
+// Insertion in row chunks with the device-to-host copy of K overlapped: chunk
+// ch is inserted on the context stream, then copied on a second stream while
+// the next chunk is inserted.  launch_rows(P0, P1) enqueues the insertion of
+// block rows [P0, P1) on the context stream.
+constexpr int OUT_CHUNKS = 8;
+template <typename Launch>
+lmg_status rows_with_copy(lmg_ctx *c, double *K, Launch &&launch_rows) {
+  if (!c->copy_stream) LMG_CUDA(c, cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+  while ((int)c->chunk_ev.size() < OUT_CHUNKS) {
+    cudaEvent_t e;
+    LMG_CUDA(c, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    c->chunk_ev.push_back(e);
+  }
+  const int64_t nb = c->n_blocks;
+  for (int ch = 0; ch < OUT_CHUNKS; ++ch) {
+    const int64_t P0 = nb * ch / OUT_CHUNKS, P1 = nb * (ch + 1) / OUT_CHUNKS;
+    if (P1 <= P0) continue;
+    launch_rows(P0, P1);
+    LMG_CUDA(c, cudaEventRecord(c->chunk_ev[ch], c->stream));
+    LMG_CUDA(c, cudaStreamWaitEvent(c->copy_stream, c->chunk_ev[ch], 0));
+    const int64_t k0 = c->h_rowptr_blk[(size_t)(c->bs * P0)], k1 = c->h_rowptr_blk[(size_t)(c->bs * P1)];
+    LMG_CUDA(c, cudaMemcpyAsync(K + k0, c->d_K + k0, sizeof(double) * (k1 - k0), cudaMemcpyDeviceToHost,
+                                c->copy_stream));
+  }
+  return LMG_OK;
+}
+
+// Host outputs of a large system take the chunked path.
+bool chunked_output(const lmg_ctx *c, const double *K, int32_t out_on_device) {
+  return K && !out_on_device && c->nnz * (int64_t)sizeof(double) > ((int64_t)64 << 20) &&
+         (int64_t)c->h_rowptr_blk.size() == c->n_dofs + 1;
+}
+
 void build_lists(lmg_ctx *c) {
   c->h_aff.clear();
   c->h_gen.clear();
@@ -349,6 +382,8 @@ lmg_status lmg_context_destroy(lmg_ctx *c) {
   dfree(c->d_relslot); dfree(c->d_geo);
   general_free(c);
   dfree(c->d_D6); dfree(c->d_modes);
+  for (cudaEvent_t e : c->chunk_ev) cudaEventDestroy(e);
+  if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
   delete c;
   return LMG_OK;
@@ -461,6 +496,7 @@ lmg_status lmg_sparsity_build(lmg_ctx *c, int64_t *nnz) {
   LMG_CUDA(c, dupload(c, c->d_brow_ptr, brow.data(), brow.size()));
   LMG_CUDA(c, dupload(c, c->d_bcol, bcol.data(), bcol.size()));
   LMG_CUDA(c, dupload(c, c->d_row_ptr, row_ptr.data(), row_ptr.size()));
+  c->h_rowptr_blk = row_ptr;
   LMG_CUDA(c, dalloc(c->d_col, (size_t)c->nnz));
   k_expand_cols<<<grid_for(c, c->n_dofs * 32, 256), 256, 0, c->stream>>>(
       c->n_dofs, c->bs, c->d_brow_ptr, c->d_bcol, c->d_row_ptr, c->d_col);
@@ -716,16 +752,28 @@ lmg_status lmg_assemble(lmg_ctx *c, int32_t precision, double *K, double *F, int
     f.max_deg = c->max_bdeg;
     f.K = c->d_K;
     f.F = c->d_F;
-    launch_fused_mixed(c->form, c->tab.n, c->n_vars, f, grid, c->stream);
+    const bool chunked = chunked_output(c, K, out_on_device);
+    launch_fused_mixed(c->form, c->tab.n, c->n_vars, f, grid, c->stream, true, !chunked);
     c->launches += 2;
+    if (chunked) {
+      lmg_status cs = rows_with_copy(c, K, [&](int64_t P0, int64_t P1) {
+        FusedArgs fc = f;
+        fc.row_begin = P0;
+        fc.n_brows = P1;
+        launch_fused_mixed(c->form, c->tab.n, c->n_vars, fc, grid, c->stream, false, true);
+        c->launches++;
+      });
+      if (cs) return cs;
+    }
     if (c->perflog) {
       LMG_CUDA(c, cudaEventRecord(e3[1], c->stream));
       LMG_CUDA(c, cudaEventRecord(e3[2], c->stream));
     }
     LMG_CUDA(c, cudaGetLastError());
     const cudaMemcpyKind kind = out_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
-    if (K) LMG_CUDA(c, cudaMemcpyAsync(K, c->d_K, sizeof(double) * c->nnz, kind, c->stream));
+    if (K && !chunked) LMG_CUDA(c, cudaMemcpyAsync(K, c->d_K, sizeof(double) * c->nnz, kind, c->stream));
     if (F) LMG_CUDA(c, cudaMemcpyAsync(F, c->d_F, sizeof(double) * c->n_dofs, kind, c->stream));
+    if (chunked) LMG_CUDA(c, cudaStreamSynchronize(c->copy_stream));
     if (out_on_device || (!K && !F)) return LMG_OK;
     return check_status(c, "assemble");
   }
@@ -761,13 +809,26 @@ lmg_status lmg_assemble(lmg_ctx *c, int32_t precision, double *K, double *F, int
   g.constrained = c->d_cons;
   g.K = c->d_K;
   g.F = c->d_F;
-  launch_gather(g, mixed, c->stream);
-  c->launches++;
+  const bool chunked = chunked_output(c, K, out_on_device);
+  if (chunked) {
+    lmg_status cs = rows_with_copy(c, K, [&](int64_t P0, int64_t P1) {
+      GatherArgs gc = g;
+      gc.row_begin = P0;
+      gc.row_end = P1;
+      launch_gather(gc, mixed, c->stream);
+      c->launches++;
+    });
+    if (cs) return cs;
+  } else {
+    launch_gather(g, mixed, c->stream);
+    c->launches++;
+  }
   if (c->perflog) LMG_CUDA(c, cudaEventRecord(e3[2], c->stream));
   LMG_CUDA(c, cudaGetLastError());
   const cudaMemcpyKind kind = out_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
-  if (K) LMG_CUDA(c, cudaMemcpyAsync(K, c->d_K, sizeof(double) * c->nnz, kind, c->stream));
+  if (K && !chunked) LMG_CUDA(c, cudaMemcpyAsync(K, c->d_K, sizeof(double) * c->nnz, kind, c->stream));
   if (F) LMG_CUDA(c, cudaMemcpyAsync(F, c->d_F, sizeof(double) * c->n_dofs, kind, c->stream));
+  if (chunked) LMG_CUDA(c, cudaStreamSynchronize(c->copy_stream));
   // Device outputs stay asynchronous; lmg_synchronize reports their status.
   if (out_on_device || (!K && !F)) return LMG_OK;
   return check_status(c, "assemble");

@@ -43,6 +43,9 @@ struct lmg_ctx {
   int64_t *d_brow_ptr = nullptr;
   int32_t *d_bcol = nullptr, *d_row_ptr = nullptr, *d_col = nullptr;
   int32_t *d_bptr = nullptr, *d_bcontrib = nullptr, *d_fptr = nullptr, *d_fcontrib = nullptr;
+  std::vector<int32_t> h_rowptr_blk;      // host copy of row_ptr (block path), for chunked output copies
+  cudaStream_t copy_stream = nullptr;     // device-to-host copies overlapped with the insertion
+  std::vector<cudaEvent_t> chunk_ev;
   uint8_t *d_relslot = nullptr;  // [E][nb][nb] slot of block (a, b) in block row of a (fused mixed form)
   int max_bdeg = 0;              // largest block-row degree
   float *d_geo = nullptr;        // [E][NG] per-element operands (fused mixed form)

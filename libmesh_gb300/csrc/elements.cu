@@ -549,7 +549,7 @@ __global__ void __launch_bounds__(256) k_rows_mixed(FusedArgs f) {
   const int js = lane / B2, rem = lane - js * B2;
   const bool act = lane < SPL * B2;
   const int i = rem / NV, k = rem - i * NV;
-  for (int64_t P = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; P < f.n_brows;
+  for (int64_t P = f.row_begin + (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5); P < f.n_brows;
        P += ((int64_t)gridDim.x * blockDim.x) >> 5) {
     const int64_t rb = f.brow_ptr[P];
     const int deg = (int)(f.brow_ptr[P + 1] - rb);
@@ -637,16 +637,17 @@ __global__ void __launch_bounds__(256) k_rows_mixed(FusedArgs f) {
 }
 
 template <int FORM, int N, int NV>
-void launch_fused_t(const FusedArgs &f, int grid, cudaStream_t s) {
+void launch_fused_t(const FusedArgs &f, int grid, cudaStream_t s, bool geo, bool rows) {
   const int64_t gb = (f.el.n_list + 127) / 128;
-  if (gb > 0) k_geo<FORM, N, NV><<<(int)(gb < grid ? gb : grid), 128, 0, s>>>(f);
+  if (geo && gb > 0) k_geo<FORM, N, NV><<<(int)(gb < grid ? gb : grid), 128, 0, s>>>(f);
+  if (!rows) return;
   const size_t smem = sizeof(float) * (9 * N * N + (size_t)8 * f.max_deg * NV * NV);
   static size_t attr = 0;
   if (smem > attr) {
     cudaFuncSetAttribute(k_rows_mixed<FORM, N, NV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     attr = smem;
   }
-  const int64_t rb = (f.n_brows + 7) / 8;
+  const int64_t rb = (f.n_brows - f.row_begin + 7) / 8;
   if (rb > 0) k_rows_mixed<FORM, N, NV><<<(int)(rb < grid ? rb : grid), 256, smem, s>>>(f);
 }
 
@@ -662,11 +663,12 @@ bool fused_built(int form, int n, int nv) {
          (form == LMG_ELASTICITY && nv == 3 && (n == 4 || n == 8 || n == 10));
 }
 
-bool launch_fused_mixed(int form, int n, int nv, const FusedArgs &f, int grid, cudaStream_t s) {
-#define LMG_F(F, NN, V)                   \
-  if (form == F && n == NN && nv == V) {  \
-    launch_fused_t<F, NN, V>(f, grid, s); \
-    return true;                          \
+bool launch_fused_mixed(int form, int n, int nv, const FusedArgs &f, int grid, cudaStream_t s, bool geo,
+                        bool rows) {
+#define LMG_F(F, NN, V)                               \
+  if (form == F && n == NN && nv == V) {              \
+    launch_fused_t<F, NN, V>(f, grid, s, geo, rows);  \
+    return true;                                      \
   }
   LMG_F(LMG_POISSON, 4, 1)
   LMG_F(LMG_POISSON, 8, 1)

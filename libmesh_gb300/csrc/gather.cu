@@ -74,8 +74,7 @@ __global__ void __launch_bounds__(256) k_gather(GatherArgs g) {
   const int js = lane / B2, rem = lane - js * B2;
   const bool act = lane < SPL * B2;
   const int i = rem / BS, k = rem - i * BS, tr = k * BS + i;
-  const int64_t n_brows = g.n_dofs / BS;
-  for (int64_t P = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; P < n_brows;
+  for (int64_t P = g.row_begin + (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5); P < g.row_end;
        P += ((int64_t)gridDim.x * blockDim.x) >> 5) {
     const int64_t rb = g.brow_ptr[P];
     const int deg = (int)(g.brow_ptr[P + 1] - rb);
@@ -106,8 +105,7 @@ __global__ void __launch_bounds__(256) k_gather_mixed(GatherArgs g) {
   const int js = lane / B2, rem = lane - js * B2;
   const bool act = lane < SPL * B2;
   const int i = rem / BS, k = rem - i * BS, tr = k * BS + i;
-  const int64_t n_brows = g.n_dofs / BS;
-  for (int64_t P = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; P < n_brows;
+  for (int64_t P = g.row_begin + (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5); P < g.row_end;
        P += ((int64_t)gridDim.x * blockDim.x) >> 5) {
     const int64_t rb = g.brow_ptr[P];
     const int deg = (int)(g.brow_ptr[P + 1] - rb);
@@ -174,15 +172,16 @@ __global__ void __launch_bounds__(256) k_gather_mixed(GatherArgs g) {
 template <int BS>
 __global__ void __launch_bounds__(256) k_gather_f(GatherArgs g) {
   const int lane = threadIdx.x & 31;
-  const int64_t n_brows = g.n_dofs / BS;
-  for (int64_t P = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; P < n_brows;
+  for (int64_t P = g.row_begin + (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5); P < g.row_end;
        P += ((int64_t)gridDim.x * blockDim.x) >> 5)
     row_load<BS>(g, P, lane);
 }
 
 }  // namespace
 
-void launch_gather_f(const GatherArgs &g, cudaStream_t s) {
+void launch_gather_f(const GatherArgs &g0, cudaStream_t s) {
+  GatherArgs g = g0;
+  if (g.row_end == 0) g.row_end = g.n_dofs / g.bs;
   int dev = 0, n_sm = 152;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
@@ -195,11 +194,13 @@ void launch_gather_f(const GatherArgs &g, cudaStream_t s) {
 
 bool gather_built(int bs) { return bs == 1 || bs == 3; }
 
-void launch_gather(const GatherArgs &g, bool mixed, cudaStream_t s) {
+void launch_gather(const GatherArgs &g0, bool mixed, cudaStream_t s) {
+  GatherArgs g = g0;
+  if (g.row_end == 0) g.row_end = g.n_dofs / g.bs;
   int dev = 0, n_sm = 152;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
-  const int64_t warps = g.n_dofs / g.bs;
+  const int64_t warps = g.row_end - g.row_begin;
   int64_t blocks = (warps + 7) / 8;
   const int64_t cap = (int64_t)n_sm * 16;
   if (blocks > cap) blocks = cap;

@@ -162,3 +162,23 @@ def test_c2_full_size_properties():
 def test_c2_medium_parity():
     mesh, dm, k, f = make_problem(10, lm.TET10, 3, lm.ELASTICITY, jitter=0.2, seed=1)
     check_parity(mesh, dm, lm.ELASTICITY, 2, 4, k, f)
+
+
+@pytest.mark.parametrize("precision", [lm.FP64, lm.MIXED])
+def test_chunked_host_output_equals_device_output(precision):
+    """Host outputs above 64 MB are inserted in row chunks, each copied to the
+    host while the next is inserted; the result equals the device-resident
+    assembly (one insertion launch, one copy afterwards) bit for bit."""
+    mesh, dm, k, f = make_problem(20, lm.TET10, 3, lm.ELASTICITY, jitter=0.2, seed=5)
+    asm, rp, col = gpu_system(mesh, dm, lm.ELASTICITY, 2, 4, k, f)
+    assert asm.nnz * 8 > 64 << 20
+    n0 = asm.launch_count()
+    asm.assemble_device(precision)
+    asm.synchronize()
+    n1 = asm.launch_count()
+    Kd, Fd = asm.result()
+    K, F = asm.assemble(precision)
+    n2 = asm.launch_count()
+    assert n2 - n1 > n1 - n0                  # the insertion ran in several launches
+    assert np.array_equal(K, Kd) and np.array_equal(F, Fd)
+    asm.close()
