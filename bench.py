@@ -513,6 +513,16 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_s = float(t.item())
     e2e = world * mesh.n_elem / e2e_s / 1e6
+    # the device-to-host link alone: one plain copy of K's size into the same pinned buffer
+    Kd = torch.empty(asm.nnz, dtype=torch.float64, device=local)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for r in range(3):
+        ev0.record()
+        Kh.copy_(Kd, non_blocking=True)
+        ev1.record()
+        ev1.synchronize()
+    link_gbs = 8 * asm.nnz / (ev0.elapsed_time(ev1) * 1e-3) / 1e9
+    del Kd
 
     B, ref_flops, our_flops = algorithmic(mesh, dm, asm.nnz)
     hbm, hbm_src = peaks()
@@ -559,7 +569,8 @@ def main():
                        "parallelism": "replica per GPU"},
             "mdofs_per_s": value * dm.n_dofs / mesh.n_elem,
             "e2e": {"value": e2e, "unit": "Melem/s", "h2d_bytes_per_step": 8 * (mesh.n_elem + 3 * mesh.n_nodes),
-                    "d2h_bytes_per_step": 8 * (asm.nnz + dm.n_dofs)},
+                    "d2h_bytes_per_step": 8 * (asm.nnz + dm.n_dofs), "d2h_link_gbs": link_gbs,
+                    "copy_floor_melem_s": mesh.n_elem / (8 * (asm.nnz + dm.n_dofs) / (link_gbs * 1e9)) / 1e6},
             "gpu_launches": launches, "clocks": clk, "roofline": dom, "cpu_baseline": cpu,
             "mixed": other}))
     if dist:
