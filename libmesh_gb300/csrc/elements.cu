@@ -654,13 +654,13 @@ void launch_fused_t(const FusedArgs &f, int grid, cudaStream_t s, bool geo, bool
 }  // namespace
 
 bool elements_built(int form, int n, int nv) {
-  return (form == LMG_POISSON && nv == 1 && (n == 4 || n == 8 || n == 10 || n == 27)) ||
-         (form == LMG_ELASTICITY && nv == 3 && (n == 4 || n == 8 || n == 10));
+  return (form == LMG_POISSON && nv == 1 && (n == 4 || n == 6 || n == 8 || n == 10 || n == 27)) ||
+         (form == LMG_ELASTICITY && nv == 3 && (n == 4 || n == 6 || n == 8 || n == 10));
 }
 
 bool fused_built(int form, int n, int nv) {
-  return (form == LMG_POISSON && nv == 1 && (n == 4 || n == 8 || n == 10 || n == 27)) ||
-         (form == LMG_ELASTICITY && nv == 3 && (n == 4 || n == 8 || n == 10));
+  return (form == LMG_POISSON && nv == 1 && (n == 4 || n == 6 || n == 8 || n == 10 || n == 27)) ||
+         (form == LMG_ELASTICITY && nv == 3 && (n == 4 || n == 6 || n == 8 || n == 10));
 }
 
 bool launch_fused_mixed(int form, int n, int nv, const FusedArgs &f, int grid, cudaStream_t s, bool geo,
@@ -671,10 +671,12 @@ bool launch_fused_mixed(int form, int n, int nv, const FusedArgs &f, int grid, c
     return true;                                      \
   }
   LMG_F(LMG_POISSON, 4, 1)
+  LMG_F(LMG_POISSON, 6, 1)
   LMG_F(LMG_POISSON, 8, 1)
   LMG_F(LMG_POISSON, 10, 1)
   LMG_F(LMG_POISSON, 27, 1)
   LMG_F(LMG_ELASTICITY, 4, 3)
+  LMG_F(LMG_ELASTICITY, 6, 3)
   LMG_F(LMG_ELASTICITY, 8, 3)
   LMG_F(LMG_ELASTICITY, 10, 3)
 #undef LMG_F
@@ -690,10 +692,12 @@ void launch_elements(int form, int n, int nv, bool affine, bool mixed, const Ele
     return;                                                                     \
   }
   LMG_CASE(LMG_POISSON, 4, 1)
+  LMG_CASE(LMG_POISSON, 6, 1)
   LMG_CASE(LMG_POISSON, 8, 1)
   LMG_CASE(LMG_POISSON, 10, 1)
   LMG_CASE(LMG_POISSON, 27, 1)
   LMG_CASE(LMG_ELASTICITY, 4, 3)
+  LMG_CASE(LMG_ELASTICITY, 6, 3)
   LMG_CASE(LMG_ELASTICITY, 8, 3)
   LMG_CASE(LMG_ELASTICITY, 10, 3)
 #undef LMG_CASE

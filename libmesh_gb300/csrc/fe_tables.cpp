@@ -72,14 +72,53 @@ void tet_rule(int order, std::vector<double> &p, std::vector<double> &w) {
     add(0.5, 1.0 / 6, 1.0 / 6, 0.075); add(1.0 / 6, 0.5, 1.0 / 6, 0.075);
     add(1.0 / 6, 1.0 / 6, 0.5, 0.075); add(1.0 / 6, 1.0 / 6, 1.0 / 6, 0.075);
   } else {
-    // Keast (1986) degree-4 rule: centroid, a 4-orbit and a 6-orbit.
-    add(0.25, 0.25, 0.25, -74.0 / 5625.0);
-    const double a4 = 11.0 / 14.0, b4 = 1.0 / 14.0, w4 = 343.0 / 45000.0;
+    // Keast (1986) degree-4 rule: centroid, a 4-orbit and a 6-orbit, with the
+    // 18-digit values libMesh tabulates (quadrature_gauss_3D.C:198-226), so
+    // that difference quotients of shapes at these points agree bit for bit.
+    add(0.25, 0.25, 0.25, -0.131555555555555556e-01);
+    const double a4 = 0.785714285714285714e+00, b4 = 0.714285714285714285e-01, w4 = 0.762222222222222222e-02;
     add(a4, b4, b4, w4); add(b4, a4, b4, w4); add(b4, b4, a4, w4); add(b4, b4, b4, w4);
-    const double s = std::sqrt(5.0 / 14.0);
-    const double a6 = 0.25 * (1.0 + s), b6 = 0.25 * (1.0 - s), w6 = 56.0 / 2250.0;
+    const double a6 = 0.399403576166799219e+00, b6 = 0.100596423833200785e+00, w6 = 0.248888888888888889e-01;
     add(a6, a6, b6, w6); add(a6, b6, b6, w6); add(b6, b6, a6, w6);
     add(b6, a6, b6, w6); add(b6, a6, a6, w6); add(a6, b6, a6, w6);
+  }
+}
+
+// Triangle QGauss rules on the reference triangle (0,0), (1,0), (0,1), as
+// libMesh tabulates them (src/quadrature/quadrature_gauss_2D.C:73-260): the
+// centroid (FIRST), the three interior points (SECOND), the 4-point conical
+// product rule (THIRD), the published Dunavant rule of degree 4 (6 points) and
+// the degree-5 rule (7 points), expanded from their orbits in the same point
+// order.  The
+// literal values are kept so that a point's difference quotients agree bit for
+// bit with the reference's.
+void tri_rule(int order, std::vector<double> &p, std::vector<double> &w) {
+  p.clear();
+  w.clear();
+  auto add = [&](double a, double b, double wt) { p.push_back(a); p.push_back(b); w.push_back(wt); };
+  // Dunavant orbit expansion: a 1-orbit at the centroid, a 3-orbit (a, a, 1-2a)
+  // in the order (a, a), (a, 1-2a), (1-2a, a).
+  auto orbit = [&](double a, double wt) {
+    add(a, a, wt);
+    add(a, 1.0 - 2.0 * a, wt);
+    add(1.0 - 2.0 * a, a, wt);
+  };
+  if (order <= 1) {
+    add(1.0 / 3, 1.0 / 3, 0.5);
+  } else if (order == 2) {
+    add(2.0 / 3, 1.0 / 6, 1.0 / 6); add(1.0 / 6, 2.0 / 3, 1.0 / 6); add(1.0 / 6, 1.0 / 6, 1.0 / 6);
+  } else if (order == 3) {
+    add(1.5505102572168219018027159252941e-01, 1.7855872826361642311703513337422e-01, 1.5902069087198858469718450103758e-01);
+    add(6.4494897427831780981972840747059e-01, 7.5031110222608118177475598324603e-02, 9.0979309128011415302815498962418e-02);
+    add(1.5505102572168219018027159252941e-01, 6.6639024601470138670269327409637e-01, 1.5902069087198858469718450103758e-01);
+    add(6.4494897427831780981972840747059e-01, 2.8001991549907407200279599420481e-01, 9.0979309128011415302815498962418e-02);
+  } else if (order == 4) {
+    orbit(4.4594849091596488631832925388305e-01, 1.1169079483900573284750350421656e-01);
+    orbit(9.1576213509770743459571463402202e-02, 5.4975871827660933819163162450105e-02);
+  } else {  // degree 5 (Walkington): centroid and two 3-orbits given in closed form
+    add(1.0 / 3, 1.0 / 3, 9.0 / 80);
+    orbit(2.0 / 7 + std::sqrt(15.0) / 21, 31.0 / 480 + std::sqrt(15.0) / 2400);
+    orbit(2.0 / 7 - std::sqrt(15.0) / 21, 31.0 / 480 - std::sqrt(15.0) / 2400);
   }
 }
 
@@ -118,6 +157,22 @@ int lagrange_shapes(int type, int order, const double *p, double *v, double *g) 
       g[3 * a + 2] = s[0] * s[1] * ds[2];
     }
     return n;
+  }
+  if (type == LMG_PRISM6) {
+    // fe_lagrange_shape_3D.C PRISM6: TRI3 shape (1 - xi - eta, xi, eta) times
+    // the 1-D linear shape in zeta; nodes 0-2 at zeta = -1, 3-5 at zeta = +1.
+    if (order != 1) return 0;
+    const double t[3] = {1. - p[0] - p[1], p[0], p[1]};
+    const double dt[3][2] = {{-1., -1.}, {1., 0.}, {0., 1.}};
+    for (int a = 0; a < 6; ++a) {
+      const int i1 = a % 3, i0 = a / 3;
+      const double l = i0 == 0 ? .5 * (1. - p[2]) : .5 * (1. + p[2]), dl = i0 == 0 ? -.5 : .5;
+      v[a] = t[i1] * l;
+      g[3 * a + 0] = dt[i1][0] * l;
+      g[3 * a + 1] = dt[i1][1] * l;
+      g[3 * a + 2] = t[i1] * dl;
+    }
+    return 6;
   }
   if (type == LMG_TET4 || type == LMG_TET10) {
     const double z[4] = {1.0 - p[0] - p[1] - p[2], p[0], p[1], p[2]};
@@ -163,10 +218,40 @@ double hier1d(int i, double xi) {
 // flips of cube_indices leave them unchanged.  Value = (s0 s1) s2;
 // derivative = (shape(p + eps e_j) - shape(p - eps e_j)) / 2. / eps with
 // eps = 1e-6 (fe_fdm_deriv, src/fe/fe.C:794-811, 929-944).
+//
+// Tets (TET4 FIRST, TET10 SECOND): barycentric vertex functions and, per edge
+// (v0, v1) of the TET4 edge list, c^2 * hier1d(2, (z1 - z0) / c) with
+// c = z0 + z1 ((z1 - z0)^2 / 2 where c is exactly 0); std::pow as the
+// reference evaluates it, so the difference quotients match bit for bit.
+double hier_tet(int a, const double *x) {
+  const double zeta[4] = {1 - x[0] - x[1] - x[2], x[0], x[1], x[2]};
+  if (a < 4) return zeta[a];
+  static const int EN[6][2] = {{0, 1}, {1, 2}, {0, 2}, {0, 3}, {1, 3}, {2, 3}};
+  const unsigned k = 2;
+  const double c = zeta[EN[a - 4][0]] + zeta[EN[a - 4][1]], num = zeta[EN[a - 4][1]] - zeta[EN[a - 4][0]];
+  if (c == 0.) return std::pow(num, k) / 2u;
+  const double flip = 1;
+  return flip * std::pow(c, k) * hier1d(2, num / c);
+}
+
+//
+// PRISM6 FIRST (prism_indices vertices): TRI vertex function times the 1-D
+// end function, the same products as LAGRANGE; derivatives by the same
+// difference quotient.
+double hier_prism6(int a, const double *x) {
+  const double t[3] = {1. - x[0] - x[1], x[0], x[1]};
+  const int i01 = a % 3, i2 = a / 3;
+  return t[i01] * (i2 == 0 ? .5 * (1. - x[2]) : .5 * (1. + x[2]));
+}
+
 int hierarchic_shapes(int type, int order, const double *p, double *v, double *g) {
-  if (!((type == LMG_HEX8 && order == 1) || (type == LMG_HEX27 && order == 2))) return 0;
-  const int n = (order == 1) ? 8 : 27;
+  const bool tet = (type == LMG_TET4 && order == 1) || (type == LMG_TET10 && order == 2);
+  const bool prism = type == LMG_PRISM6 && order == 1;
+  if (!((type == LMG_HEX8 && order == 1) || (type == LMG_HEX27 && order == 2) || tet || prism)) return 0;
+  const int n = prism ? 6 : tet ? (order == 1 ? 4 : 10) : (order == 1) ? 8 : 27;
   auto shape = [&](int a, const double *x) {
+    if (prism) return hier_prism6(a, x);
+    if (tet) return hier_tet(a, x);
     const int i0 = (order == 1) ? HEX8_I[0][a] : HEX27_I[0][a], i1 = (order == 1) ? HEX8_I[1][a] : HEX27_I[1][a],
               i2 = (order == 1) ? HEX8_I[2][a] : HEX27_I[2][a];
     return hier1d(i0, x[0]) * hier1d(i1, x[1]) * hier1d(i2, x[2]);
@@ -194,14 +279,17 @@ std::string build_fe_tables(FETables &t, int type, int fe_order, int q_order, in
   t.family = family;
   if (fe_order < 1 || fe_order > 2) return "fe_order must be FIRST or SECOND";
   if (family != 0 && family != 1) return "unknown FE family";
-  if (family == 1 && !((type == LMG_HEX8 && fe_order == 1) || (type == LMG_HEX27 && fe_order == 2)))
-    return "HIERARCHIC is built for FIRST on HEX8 and SECOND on HEX27";
+  if (family == 1 && !((type == LMG_HEX8 && fe_order == 1) || (type == LMG_HEX27 && fe_order == 2) ||
+                       (type == LMG_TET4 && fe_order == 1) || (type == LMG_TET10 && fe_order == 2) ||
+                       (type == LMG_PRISM6 && fe_order == 1)))
+    return "HIERARCHIC is built for FIRST on HEX8 / TET4 / PRISM6 and SECOND on HEX27 / TET10";
   auto fe_shapes = [&](const double *p, double *v, double *g) {
     return family == 1 ? hierarchic_shapes(type, fe_order, p, v, g) : lagrange_shapes(type, fe_order, p, v, g);
   };
   const bool hex = (type == LMG_HEX8 || type == LMG_HEX27);
   const bool tet = (type == LMG_TET4 || type == LMG_TET10);
-  if (!hex && !tet) return "unsupported element type";
+  const bool prism = type == LMG_PRISM6;
+  if (!hex && !tet && !prism) return "unsupported element type";
   const int geo_order = (type == LMG_HEX27 || type == LMG_TET10) ? 2 : 1;
   if (hex) {
     std::vector<double> x, w;
@@ -213,6 +301,18 @@ std::string build_fe_tables(FETables &t, int type, int fe_order, int q_order, in
           t.qp.push_back(x[i]); t.qp.push_back(x[j]); t.qp.push_back(x[k]);
           t.qw.push_back(w[i] * w[j] * w[k]);
         }
+  } else if (prism) {
+    // tensor_product_prism (quadrature.C:310-331): triangle point fastest,
+    // then the 1-D Gauss point in zeta.
+    if (q_order > 5) return "prism quadrature above FIFTH is not built";
+    std::vector<double> x, w, tp, tw;
+    gauss_legendre(q_order / 2 + 1, x, w);
+    tri_rule(q_order, tp, tw);
+    for (size_t j = 0; j < x.size(); ++j)
+      for (size_t i = 0; i < tw.size(); ++i) {
+        t.qp.push_back(tp[2 * i]); t.qp.push_back(tp[2 * i + 1]); t.qp.push_back(x[j]);
+        t.qw.push_back(tw[i] * w[j]);
+      }
   } else {
     if (q_order > 4) return "tet quadrature above FOURTH is not built";
     tet_rule(q_order, t.qp, t.qw);
@@ -274,6 +374,11 @@ void sub(const double *P, int i, int j, double *o) {
 bool elem_has_affine_map(int type, const double *P) {
   double v[3], w[3];
   switch (type) {
+    case LMG_PRISM6: {  // cell_prism6.C:199-207: the three z edges are parallel translates
+      sub(P, 3, 0, v);
+      sub(P, 4, 1, w); if (!rfe(v, w)) return false;
+      sub(P, 5, 2, w); return rfe(v, w);
+    }
     case LMG_TET4:
       return true;
     case LMG_TET10: {  // cell_tet10.C:143-172

@@ -34,6 +34,8 @@ static const int HEX27_SIDES[6][9] = {{0, 3, 2, 1, 11, 10, 9, 8, 20},
 static const int TET4_SIDES[4][3] = {{0, 2, 1}, {0, 1, 3}, {1, 2, 3}, {2, 0, 3}};
 static const int TET10_SIDES[4][6] = {
     {0, 2, 1, 6, 5, 4}, {0, 1, 3, 4, 8, 7}, {1, 2, 3, 5, 9, 8}, {2, 0, 3, 6, 7, 9}};
+// PRISM6 sides (cell_prism6.C side_nodes_map): two triangles, three quads.
+static const int PRISM6_SIDES[5][4] = {{0, 2, 1, -1}, {0, 1, 4, 3}, {1, 2, 5, 4}, {2, 0, 3, 5}, {3, 4, 5, -1}};
 // Vertices adjacent to TET10 mid-edge nodes 4..9 (cell_tet10.C _second_order_adjacent_vertices).
 static const int TET10_EDGE_VERTS[6][2] = {{0, 1}, {1, 2}, {0, 2}, {0, 3}, {1, 3}, {2, 3}};
 
@@ -43,6 +45,7 @@ int nodes_per_elem(int t) {
     case LMG_TET10: return 10;
     case LMG_HEX8: return 8;
     case LMG_HEX27: return 27;
+    case LMG_PRISM6: return 6;
     default: return 0;
   }
 }
@@ -50,6 +53,7 @@ int sides_per_elem(int t) {
   switch (t) {
     case LMG_TET4: case LMG_TET10: return 4;
     case LMG_HEX8: case LMG_HEX27: return 6;
+    case LMG_PRISM6: return 5;
     default: return 0;
   }
 }
@@ -57,6 +61,7 @@ int vertices_per_elem(int t) {
   switch (t) {
     case LMG_TET4: case LMG_TET10: return 4;
     case LMG_HEX8: case LMG_HEX27: return 8;
+    case LMG_PRISM6: return 6;
     default: return 0;
   }
 }
@@ -66,6 +71,11 @@ int side_nodes(int t, int s, int *out) {
     case LMG_HEX27: for (int i = 0; i < 9; ++i) out[i] = HEX27_SIDES[s][i]; return 9;
     case LMG_TET4: for (int i = 0; i < 3; ++i) out[i] = TET4_SIDES[s][i]; return 3;
     case LMG_TET10: for (int i = 0; i < 6; ++i) out[i] = TET10_SIDES[s][i]; return 6;
+    case LMG_PRISM6: {
+      const int k = (s == 0 || s == 4) ? 3 : 4;
+      for (int i = 0; i < k; ++i) out[i] = PRISM6_SIDES[s][i];
+      return k;
+    }
     default: return 0;
   }
 }
@@ -77,9 +87,67 @@ static inline int64_t grid_idx(int64_t gx, int64_t gy, int64_t i, int64_t j, int
   return i + gx * (j + k * gy);
 }
 
+// PRISM6 build_cube (mesh_generation.C:1501-1545): the HEX8 node grid, two
+// prisms per grid cell split along the (i+1, j) - (i, j+1) diagonal, in
+// k, j, i cell order; side ids on the triangles (0 bottom, 5 top) and on the
+// quads that lie on the cube faces.
+static std::string build_cube_prism6(HostMesh &m, int nx, int ny, int nz) {
+  const int64_t gx = (int64_t)nx + 1, gy = (int64_t)ny + 1, gz = (int64_t)nz + 1;
+  m.elem_type = LMG_PRISM6;
+  m.npe = 6;
+  m.nsides = 5;
+  m.xyz.resize((size_t)(gx * gy * gz) * 3);
+  for (int64_t k = 0; k < gz; ++k)
+    for (int64_t j = 0; j < gy; ++j)
+      for (int64_t i = 0; i < gx; ++i) {
+        const int64_t id = grid_idx(gx, gy, i, j, k);
+        m.xyz[3 * id + 0] = (double)i / (double)nx * (1.0 - 0.0) + 0.0;
+        m.xyz[3 * id + 1] = (double)j / (double)ny * (1.0 - 0.0) + 0.0;
+        m.xyz[3 * id + 2] = (double)k / (double)nz * (1.0 - 0.0) + 0.0;
+      }
+  const int64_t E = 2 * (int64_t)nx * ny * nz;
+  m.conn.resize((size_t)(E * 6));
+  m.side_bid.assign((size_t)(E * 5), (int8_t)-1);
+  int64_t e = 0;
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        int32_t *c = &m.conn[(size_t)(e * 6)];
+        int8_t *sb = &m.side_bid[(size_t)(e * 5)];
+        c[0] = (int32_t)grid_idx(gx, gy, i, j, k);
+        c[1] = (int32_t)grid_idx(gx, gy, i + 1, j, k);
+        c[2] = (int32_t)grid_idx(gx, gy, i, j + 1, k);
+        c[3] = (int32_t)grid_idx(gx, gy, i, j, k + 1);
+        c[4] = (int32_t)grid_idx(gx, gy, i + 1, j, k + 1);
+        c[5] = (int32_t)grid_idx(gx, gy, i, j + 1, k + 1);
+        if (i == 0) sb[3] = 4;
+        if (j == 0) sb[1] = 1;
+        if (k == 0) sb[0] = 0;
+        if (k == nz - 1) sb[4] = 5;
+        ++e;
+        c = &m.conn[(size_t)(e * 6)];
+        sb = &m.side_bid[(size_t)(e * 5)];
+        c[0] = (int32_t)grid_idx(gx, gy, i + 1, j, k);
+        c[1] = (int32_t)grid_idx(gx, gy, i + 1, j + 1, k);
+        c[2] = (int32_t)grid_idx(gx, gy, i, j + 1, k);
+        c[3] = (int32_t)grid_idx(gx, gy, i + 1, j, k + 1);
+        c[4] = (int32_t)grid_idx(gx, gy, i + 1, j + 1, k + 1);
+        c[5] = (int32_t)grid_idx(gx, gy, i, j + 1, k + 1);
+        if (i == nx - 1) sb[1] = 2;
+        if (j == ny - 1) sb[2] = 3;
+        if (k == 0) sb[0] = 0;
+        if (k == nz - 1) sb[4] = 5;
+        ++e;
+      }
+  renumber_nodes_first_touch(m);
+  return "";
+}
+
 std::string build_cube_hex(HostMesh &m, int nx, int ny, int nz, int type) {
   if (nx <= 0 || ny <= 0 || nz <= 0) return "build_cube: nx, ny, nz must be positive";
-  if (type != LMG_HEX8 && type != LMG_HEX27) return "build_cube: type must be HEX8 or HEX27";
+  if (type != LMG_HEX8 && type != LMG_HEX27 && type != LMG_PRISM6)
+    return "build_cube: type must be HEX8, HEX27 or PRISM6";
+  if (type == LMG_PRISM6) return build_cube_prism6(m, nx, ny, nz);
   const int f = (type == LMG_HEX8) ? 1 : 2;  // grid refinement factor
   const int64_t gx = (int64_t)f * nx + 1, gy = (int64_t)f * ny + 1, gz = (int64_t)f * nz + 1;
   m.elem_type = type;

@@ -209,7 +209,7 @@ lmg_status lmg_mesh_cube(int32_t nx, int32_t ny, int32_t nz, int32_t elem_type, 
     const int base = tets ? LMG_HEX8 : elem_type;
     std::string err = lmg::build_cube_hex(mesh->m, nx, ny, nz, base);
     if (err.empty()) lmg::jitter_interior(mesh->m, jitter, nx, ny, nz, seed);
-    if (err.empty() && !tets && jitter == 0.0) {  // unjittered hex cube: lattice for refinement
+    if (err.empty() && !tets && elem_type != LMG_PRISM6 && jitter == 0.0) {  // unjittered hex cube: lattice for refinement
       mesh->m.cube[0] = nx;
       mesh->m.cube[1] = ny;
       mesh->m.cube[2] = nz;
@@ -218,8 +218,9 @@ lmg_status lmg_mesh_cube(int32_t nx, int32_t ny, int32_t nz, int32_t elem_type, 
     if (err.empty() && elem_type == LMG_TET10) err = lmg::all_second_order_tet4(mesh->m);
     if (!err.empty()) {
       delete mesh;
-      return (elem_type == LMG_HEX8 || elem_type == LMG_HEX27 || tets) ? LMG_ERR_ARG
-                                                                       : LMG_ERR_UNSUPPORTED;
+      return (elem_type == LMG_HEX8 || elem_type == LMG_HEX27 || elem_type == LMG_PRISM6 || tets)
+                 ? LMG_ERR_ARG
+                 : LMG_ERR_UNSUPPORTED;
     }
   } catch (const std::bad_alloc &) {
     delete mesh;

@@ -273,6 +273,7 @@ bool launch_vjp_xyz(int n, const VjpArgs &v, int grid, cudaStream_t s) {
   const int64_t blocks = (v.n_elem + 127) / 128;
   const int g = (int)(blocks < grid ? blocks : grid);
   if (n == 4) k_vjp_xyz<4><<<g, 128, 0, s>>>(v);
+  else if (n == 6) k_vjp_xyz<6><<<g, 128, 0, s>>>(v);
   else if (n == 8) k_vjp_xyz<8><<<g, 128, 0, s>>>(v);
   else if (n == 10) k_vjp_xyz<10><<<g, 128, 0, s>>>(v);
   else if (n == 27) k_vjp_xyz<27><<<g, 128, 0, s>>>(v);
@@ -289,10 +290,12 @@ bool launch_vjp(int form, int n, int nv, bool region, const VjpArgs &v, int grid
     return true;                                 \
   }
   LMG_V(LMG_POISSON, 4, 1)
+  LMG_V(LMG_POISSON, 6, 1)
   LMG_V(LMG_POISSON, 8, 1)
   LMG_V(LMG_POISSON, 10, 1)
   LMG_V(LMG_POISSON, 27, 1)
   LMG_V(LMG_ELASTICITY, 4, 3)
+  LMG_V(LMG_ELASTICITY, 6, 3)
   LMG_V(LMG_ELASTICITY, 8, 3)
   LMG_V(LMG_ELASTICITY, 10, 3)
 #undef LMG_V

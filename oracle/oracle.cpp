@@ -30,7 +30,7 @@
 
 namespace {
 
-enum { TET4 = 8, TET10 = 9, HEX8 = 10, HEX27 = 12 };
+enum { TET4 = 8, TET10 = 9, HEX8 = 10, HEX27 = 12, PRISM6 = 13 };
 enum { POISSON = 0, ELASTICITY = 1 };
 
 // libMesh's _R literal: a long double literal narrowed to Real
@@ -95,8 +95,54 @@ void keast_rule(const double rule[][4], int n_pts, std::vector<Pt> &P, std::vect
 
 // QGauss::init_3D, src/quadrature/quadrature_gauss_3D.C:30-226, and
 // QBase::tensor_product_hex, src/quadrature/quadrature.C:283-305.
+// QGauss::init_2D for TRI3, orders CONSTANT-FIFTH (src/quadrature/quadrature_gauss_2D.C:73-262),
+// with dunavant_rule2's orbit expansion (src/quadrature/quadrature_gauss.C:195-260):
+// a 3-orbit of a gives (a, a), (a, 1-2a), (1-2a, a).
+void qgauss_tri(int order, std::vector<double> &x, std::vector<double> &y, std::vector<double> &w) {
+  x.clear(); y.clear(); w.clear();
+  auto pt = [&](double a, double b, double wt) { x.push_back(a); y.push_back(b); w.push_back(wt); };
+  auto orbit3 = [&](double a, double wt) { pt(a, a, wt); pt(a, 1 - 2 * a, wt); pt(1 - 2 * a, a, wt); };
+  switch (order) {
+    case 0: case 1:
+      pt(1.0 / 3, 1.0 / 3, 0.5); return;
+    case 2:
+      pt(2.0 / 3, 1.0 / 6, 1.0 / 6); pt(1.0 / 6, 2.0 / 3, 1.0 / 6); pt(1.0 / 6, 1.0 / 6, 1.0 / 6); return;
+    case 3:
+      pt(R_(1.5505102572168219018027159252941e-01), R_(1.7855872826361642311703513337422e-01),
+         R_(1.5902069087198858469718450103758e-01));
+      pt(R_(6.4494897427831780981972840747059e-01), R_(7.5031110222608118177475598324603e-02),
+         R_(9.0979309128011415302815498962418e-02));
+      pt(R_(1.5505102572168219018027159252941e-01), R_(6.6639024601470138670269327409637e-01),
+         R_(1.5902069087198858469718450103758e-01));
+      pt(R_(6.4494897427831780981972840747059e-01), R_(2.8001991549907407200279599420481e-01),
+         R_(9.0979309128011415302815498962418e-02));
+      return;
+    case 4:
+      orbit3(R_(4.4594849091596488631832925388305199e-01), R_(1.1169079483900573284750350421656140e-01));
+      orbit3(R_(9.1576213509770743459571463402201508e-02), R_(5.4975871827660933819163162450105264e-02));
+      return;
+    default:  // FIFTH
+      pt(1.0 / 3, 1.0 / 3, 9.0 / 80);
+      orbit3(2.0 / 7 + std::sqrt(15.0) / 21, 31.0 / 480 + std::sqrt(15.0) / 2400);
+      orbit3(2.0 / 7 - std::sqrt(15.0) / 21, 31.0 / 480 - std::sqrt(15.0) / 2400);
+      return;
+  }
+}
+
 bool qgauss_3d(int type, int order, std::vector<Pt> &P, std::vector<double> &W) {
   P.clear(); W.clear();
+  if (type == PRISM6) {  // quadrature_gauss_3D.C:507-525, tensor_product_prism (quadrature.C:310-331)
+    if (order > 5) return false;
+    std::vector<double> z, wz, tx, ty, tw;
+    qgauss_1d(order, z, wz);
+    qgauss_tri(order, tx, ty, tw);
+    for (size_t j = 0; j < z.size(); j++)
+      for (size_t i = 0; i < tw.size(); i++) {
+        P.push_back({{tx[i], ty[i], z[j]}});
+        W.push_back(tw[i] * wz[j]);
+      }
+    return true;
+  }
   if (type == HEX8 || type == HEX27) {
     std::vector<double> x, w;
     qgauss_1d(order, x, w);
@@ -162,6 +208,7 @@ const unsigned H27_I2[] = {0, 0, 0, 0, 1, 1, 1, 1, 0, 0, 0, 0, 2, 2, 2, 2, 1, 1,
 
 // Number of LAGRANGE shapes of `order` on `type` (isoparametric cases only).
 int n_shapes(int type, int order) {
+  if (type == PRISM6) return order == 1 ? 6 : 0;
   if (type == HEX8 || type == HEX27) return order == 1 ? 8 : (type == HEX27 ? 27 : 0);
   if (type == TET4 || type == TET10) return order == 1 ? 4 : (type == TET10 ? 10 : 0);
   return 0;
@@ -202,6 +249,26 @@ double tet_shape_deriv(int order, int i, int j, const Pt &p) {
   return 4. * (z[a] * dz[b][j] + dz[a][j] * z[b]);
 }
 
+// fe_lagrange_3D_shape(_deriv) for PRISM6 (fe_lagrange_shape_3D.C:742-762, 1639-1676):
+// FE<2,LAGRANGE>::shape(TRI3, FIRST) = (1 - xi - eta, xi, eta) times the 1-D
+// linear shape in zeta, i0 = {0,0,0,1,1,1}, i1 = {0,1,2,0,1,2}.
+double tri3_shape(int i, double xi, double eta) {
+  return i == 0 ? 1. - xi - eta : (i == 1 ? xi : eta);
+}
+double tri3_deriv(int i, int j) {
+  static const double d[3][2] = {{-1., -1.}, {1., 0.}, {0., 1.}};
+  return d[i][j];
+}
+double prism6_shape(int i, const Pt &p) {
+  static const int i0[] = {0, 0, 0, 1, 1, 1}, i1[] = {0, 1, 2, 0, 1, 2};
+  return tri3_shape(i1[i], p.v[0], p.v[1]) * l1(i0[i], p.v[2]);
+}
+double prism6_deriv(int i, int j, const Pt &p) {
+  static const int i0[] = {0, 0, 0, 1, 1, 1}, i1[] = {0, 1, 2, 0, 1, 2};
+  if (j < 2) return tri3_deriv(i1[i], j) * l1(i0[i], p.v[2]);
+  return tri3_shape(i1[i], p.v[0], p.v[1]) * l1d(i0[i]);
+}
+
 // FE<3,LAGRANGE>::all_shapes / all_shape_derivs at a list of points
 // (hex tensor fast path, fe_lagrange_shape_3D.C:72-416; tets by scalar calls).
 // phi[i][p], d[c][i][p].
@@ -229,6 +296,11 @@ void all_shapes(int type, int order, const std::vector<Pt> &pts, std::vector<std
         d[0][i][q] = ds[0][i0[i]] * s[1][i1[i]] * s[2][i2[i]];
         d[1][i][q] = s[0][i0[i]] * ds[1][i1[i]] * s[2][i2[i]];
         d[2][i][q] = s[0][i0[i]] * s[1][i1[i]] * ds[2][i2[i]];
+      }
+    } else if (type == PRISM6) {
+      for (int i = 0; i < n; ++i) {
+        phi[i][q] = prism6_shape(i, pts[q]);
+        for (int c = 0; c < 3; ++c) d[c][i][q] = prism6_deriv(i, c, pts[q]);
       }
     } else {
       for (int i = 0; i < n; ++i) {
@@ -285,6 +357,140 @@ double hier_hex_shape(unsigned i, const Pt &p) {
   return hier_1d(i0, p.v[0]) * hier_1d(i1, p.v[1]) * hier_1d(i2, p.v[2]);
 }
 
+// ---------------------------------------------------------- HIERARCHIC p = 3
+// cube_indices for totalorder 3 on a HEX27 (fe_hierarchic_shape_3D.C:166-760):
+// e = 2 dofs per edge, e^2 = 4 per face, e^3 = 8 interior.  Edge dofs reflect
+// their coordinate when Elem::positive_edge_orientation (elem.C:3634-3640,
+// lexicographic Point >) says so; face dofs swap / reflect the two in-face
+// coordinates by the face's minimum vertex (get_min_point) and
+// Elem::positive_face_orientation (elem.C:3642-3661).  Interior dofs use
+// cube_number_column / row / page; face dofs square_number_row / column
+// (number_lookups.C), restated for the entries this order reaches.
+bool pt_less(const Pt &a, const Pt &b) {  // TypeVector::operator< (type_vector.C:66-76)
+  for (int i = 0; i < 3; i++) {
+    if (a.v[i] < b.v[i]) return true;
+    if (a.v[i] > b.v[i]) return false;
+  }
+  return false;
+}
+bool pt_eq(const Pt &a, const Pt &b) { return a.v[0] == b.v[0] && a.v[1] == b.v[1] && a.v[2] == b.v[2]; }
+
+const unsigned HEX_EDGE[12][2] = {{0, 1}, {1, 2}, {2, 3}, {0, 3}, {0, 4}, {1, 5},
+                                  {2, 6}, {3, 7}, {4, 5}, {5, 6}, {6, 7}, {4, 7}};
+const unsigned HEX_SIDE4[6][4] = {{0, 3, 2, 1}, {0, 1, 5, 4}, {1, 2, 6, 5}, {2, 3, 7, 6}, {3, 0, 4, 7}, {4, 5, 6, 7}};
+
+bool positive_edge_orientation(const std::vector<Pt> &X, unsigned i) {
+  return pt_less(X[HEX_EDGE[i][1]], X[HEX_EDGE[i][0]]);
+}
+bool positive_face_orientation(const std::vector<Pt> &X, unsigned i) {
+  const unsigned *nodes = HEX_SIDE4[i];
+  const unsigned N = 4;
+  unsigned v = 0;
+  for (unsigned k = 1; k < N; ++k)
+    if (pt_less(X[nodes[k]], X[nodes[v]])) v = k;  // std::min_element: first minimum
+  return pt_less(X[nodes[(v - 1 + N) % N]], X[nodes[(v + 1) % N]]);
+}
+Pt min_point(const std::vector<Pt> &X, unsigned a, unsigned b, unsigned c, unsigned d) {
+  auto mn = [](const Pt &p, const Pt &q) { return pt_less(q, p) ? q : p; };  // std::min
+  return mn(mn(X[a], X[b]), mn(X[c], X[d]));
+}
+
+void cube_indices_p3(const std::vector<Pt> &X, unsigned i, double &xi, double &eta, double &zeta, unsigned &i0,
+                     unsigned &i1, unsigned &i2) {
+  static const unsigned SQ_ROW[4] = {0, 1, 1, 0}, SQ_COL[4] = {0, 0, 1, 1};
+  static const unsigned CB_COL[8] = {0, 0, 1, 1, 0, 1, 1, 0}, CB_ROW[8] = {0, 1, 1, 0, 1, 1, 0, 0},
+                        CB_PAGE[8] = {0, 0, 0, 0, 1, 1, 1, 1};
+  static const unsigned V[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0},
+                                   {0, 0, 1}, {1, 0, 1}, {1, 1, 1}, {0, 1, 1}};
+  const unsigned e = 2;
+  const double xs = xi, es = eta, zs = zeta;
+  if (i < 8) {
+    i0 = V[i][0]; i1 = V[i][1]; i2 = V[i][2];
+    return;
+  }
+  if (i < 8 + 12 * e) {  // edges: the varying index and its direction, then the flip rule
+    const unsigned ed = (i - 8) / e, k = i - ed * e - 6;
+    static const int DIR[12] = {0, 1, 0, 1, 2, 2, 2, 2, 0, 1, 0, 1};
+    static const unsigned FIX[12][2] = {{0, 0}, {1, 0}, {1, 0}, {0, 0}, {0, 0}, {1, 0},
+                                        {1, 1}, {0, 1}, {0, 1}, {1, 1}, {1, 1}, {0, 1}};
+    const bool pos = positive_edge_orientation(X, ed);
+    const bool flip = (ed == 2 || ed == 10) ? !pos : pos;
+    const int d = DIR[ed];
+    if (d == 0) { i0 = k; i1 = FIX[ed][0]; i2 = FIX[ed][1]; if (flip) xi = -xs; }
+    else if (d == 1) { i0 = FIX[ed][0]; i1 = k; i2 = FIX[ed][1]; if (flip) eta = -es; }
+    else { i0 = FIX[ed][0]; i1 = FIX[ed][1]; i2 = k; if (flip) zeta = -zs; }
+    return;
+  }
+  if (i < 8 + 12 * e + 6 * e * e) {
+    const unsigned f = (i - 8 - 12 * e) / (e * e), basisnum = i - 8 - 12 * e - f * e * e;
+    const unsigned r = SQ_ROW[basisnum] + 2, c = SQ_COL[basisnum] + 2;
+    // Per face: its in-face coordinates (A, B), the vertices the cases test
+    // against get_min_point in their order, whether the orientation test is
+    // negated, and the remap of each case (o = orientation test true / false):
+    // ID (A, B), SW (B, A), TA (-B, A), TB (A, -B), NG (-A, -B), NS (-B, -A),
+    // TC (B, -A), TD (-A, B) -- the eight cases of every face as written there.
+    enum { ID, SW, TA, TB, NG, NS, TC, TD };
+    static const unsigned TESTV[6][4] = {{0, 3, 2, 1}, {0, 1, 5, 4}, {1, 2, 6, 5},
+                                         {3, 7, 6, 2}, {0, 4, 7, 3}, {4, 5, 6, 7}};
+    static const unsigned GMP[6][4] = {{1, 2, 0, 3}, {0, 1, 5, 4}, {1, 2, 6, 5},
+                                       {2, 3, 7, 6}, {3, 0, 4, 7}, {4, 5, 6, 7}};
+    static const bool NEG[6] = {false, true, true, false, false, true};
+    static const int CASE[6][4][2] = {{{ID, SW}, {TA, TB}, {NG, NS}, {TC, TD}},
+                                      {{ID, SW}, {TC, TD}, {NG, NS}, {TD, TB}},
+                                      {{ID, SW}, {TC, TD}, {NG, NS}, {TA, TB}},
+                                      {{ID, SW}, {TA, TB}, {NG, NS}, {TC, TD}},
+                                      {{ID, SW}, {TA, TB}, {NG, NS}, {TC, TD}},
+                                      {{ID, SW}, {TC, TD}, {NG, NS}, {TA, ID}}};
+    double *A, *B;
+    double As, Bs;
+    switch (f) {
+      case 0: i0 = r; i1 = c; i2 = 0; A = &xi; B = &eta; As = xs; Bs = es; break;
+      case 1: i0 = r; i1 = 0; i2 = c; A = &xi; B = &zeta; As = xs; Bs = zs; break;
+      case 2: i0 = 1; i1 = r; i2 = c; A = &eta; B = &zeta; As = es; Bs = zs; break;
+      case 3: i0 = r; i1 = 1; i2 = c; A = &xi; B = &zeta; As = xs; Bs = zs; break;
+      case 4: i0 = 0; i1 = r; i2 = c; A = &eta; B = &zeta; As = es; Bs = zs; break;
+      default: i0 = r; i1 = c; i2 = 1; A = &xi; B = &eta; As = xs; Bs = es; break;
+    }
+    const Pt m = min_point(X, GMP[f][0], GMP[f][1], GMP[f][2], GMP[f][3]);
+    const bool o = NEG[f] ? !positive_face_orientation(X, f) : positive_face_orientation(X, f);
+    for (int t = 0; t < 4; ++t) {
+      if (!pt_eq(X[TESTV[f][t]], m)) continue;
+      switch (CASE[f][t][o ? 0 : 1]) {
+        case ID: *A = As; *B = Bs; break;
+        case SW: *A = Bs; *B = As; break;
+        case TA: *A = -Bs; *B = As; break;
+        case TB: *A = As; *B = -Bs; break;
+        case NG: *A = -As; *B = -Bs; break;
+        case NS: *A = -Bs; *B = -As; break;
+        case TC: *A = Bs; *B = -As; break;
+        default: *A = -As; *B = Bs; break;
+      }
+      break;
+    }
+    return;
+  }
+  const unsigned basisnum = i - 8 - 12 * e - 6 * e * e;
+  i0 = CB_COL[basisnum] + 2;
+  i1 = CB_ROW[basisnum] + 2;
+  i2 = CB_PAGE[basisnum] + 2;
+}
+
+// FE<3,HIERARCHIC>::shape at totalorder 3 on one element: cube_indices, then
+// (s0 * s1) * s2 at the remapped coordinates.
+double hier_hex3_shape(const std::vector<Pt> &X, unsigned i, const Pt &p) {
+  double xi = p.v[0], eta = p.v[1], zeta = p.v[2];
+  unsigned i0, i1, i2;
+  cube_indices_p3(X, i, xi, eta, zeta, i0, i1, i2);
+  return hier_1d(i0, xi) * hier_1d(i1, eta) * hier_1d(i2, zeta);
+}
+double hier_hex3_deriv(const std::vector<Pt> &X, unsigned i, unsigned j, const Pt &p) {
+  const double eps = 1.e-6;
+  Pt pp = p, pm = p;
+  pp.v[j] += eps;
+  pm.v[j] -= eps;
+  return (hier_hex3_shape(X, i, pp) - hier_hex3_shape(X, i, pm)) / 2. / eps;
+}
+
 // fe_fdm_deriv (src/fe/fe.C:794-811, 929-944): central difference, eps = 1e-6.
 double hier_hex_deriv(unsigned i, unsigned j, const Pt &p) {
   const double eps = 1.e-6;
@@ -294,15 +500,73 @@ double hier_hex_deriv(unsigned i, unsigned j, const Pt &p) {
   return (hier_hex_shape(i, pp) - hier_hex_shape(i, pm)) / 2. / eps;
 }
 
-void all_shapes_hierarchic(int order, const std::vector<Pt> &pts, std::vector<std::vector<double>> &phi,
+// FE<3,HIERARCHIC>::shape on a tet, totalorder <= 2 (fe_hierarchic_shape_3D.C,
+// TET4/TET10/TET14 branch): vertex dofs are the barycentric coordinates; edge
+// dof of edge k (Tet4::edge_nodes_map, cell_tet4.C:46-54) is
+// crossval^2 * hier_1d(2, (z1 - z0) / crossval) with crossval = z0 + z1, or
+// (z1 - z0)^2 / 2 when crossval is exactly 0.  The odd-order edge flip does
+// not arise at this order.
+double hier_tet_shape(unsigned i, const Pt &p) {
+  const double zeta[4] = {1 - p.v[0] - p.v[1] - p.v[2], p.v[0], p.v[1], p.v[2]};
+  if (i < 4) return zeta[i];
+  static const unsigned EN[6][2] = {{0, 1}, {1, 2}, {0, 2}, {0, 3}, {1, 3}, {2, 3}};
+  const unsigned edge_num = i - 4, basisorder = 2;
+  const double crossval = zeta[EN[edge_num][0]] + zeta[EN[edge_num][1]];
+  const double edgenumerator = zeta[EN[edge_num][1]] - zeta[EN[edge_num][0]];
+  if (crossval == 0.) {
+    unsigned basisfactorial = 1;
+    for (unsigned n = 2; n <= basisorder; ++n) basisfactorial *= n;
+    return std::pow(edgenumerator, basisorder) / basisfactorial;
+  }
+  const double edgeval = edgenumerator / crossval;
+  const double crossfunc = std::pow(crossval, basisorder);
+  const double flip = 1;
+  return flip * crossfunc * hier_1d(basisorder, edgeval);
+}
+
+// FE<3,HIERARCHIC>::shape on a PRISM6, totalorder 1 (prism_indices vertices,
+// fe_hierarchic_shape_3D.C:764-810): the TRI vertex function (zeta0 =
+// 1 - xi - eta, xi, eta; fe_hierarchic_shape_2D.C:969-983) times the 1-D
+// end function in zeta.
+double hier_prism_shape(unsigned i, const Pt &p) {
+  const unsigned i01 = i % 3, i2 = i / 3;
+  const double zeta1 = p.v[0], zeta2 = p.v[1], zeta0 = 1. - zeta1 - zeta2;
+  const double t = i01 == 0 ? zeta0 : (i01 == 1 ? zeta1 : zeta2);
+  return t * hier_1d(i2, p.v[2]);
+}
+
+double hier_shape(int type, unsigned i, const Pt &p) {
+  if (type == PRISM6) return hier_prism_shape(i, p);
+  return (type == TET4 || type == TET10) ? hier_tet_shape(i, p) : hier_hex_shape(i, p);
+}
+
+double hier_deriv(int type, unsigned i, unsigned j, const Pt &p) {
+  if (type == HEX8 || type == HEX27) return hier_hex_deriv(i, j, p);
+  const double eps = 1.e-6;
+  Pt pp = p, pm = p;
+  pp.v[j] += eps;
+  pm.v[j] -= eps;
+  return (hier_shape(type, i, pp) - hier_shape(type, i, pm)) / 2. / eps;
+}
+
+bool hierarchic_built(int type, int order) {
+  return (type == HEX8 && order == 1) || (type == HEX27 && order == 2) || (type == TET4 && order == 1) ||
+         (type == TET10 && order == 2) || (type == PRISM6 && order == 1);
+}
+
+void all_shapes_hierarchic(int type, int order, const std::vector<Pt> &pts, std::vector<std::vector<double>> &phi,
                            std::vector<std::vector<double>> d[3]) {
-  const unsigned n = (order + 1) * (order + 1) * (order + 1), np = (unsigned)pts.size();
+  const bool tet = (type == TET4 || type == TET10);
+  const unsigned n = type == PRISM6 ? (order + 1) * (order + 1) * (order + 2) / 2
+                     : tet      ? (order + 1) * (order + 2) * (order + 3) / 6
+                                : (order + 1) * (order + 1) * (order + 1);
+  const unsigned np = (unsigned)pts.size();
   phi.assign(n, std::vector<double>(np));
   for (int c = 0; c < 3; ++c) d[c].assign(n, std::vector<double>(np));
   for (unsigned q = 0; q < np; ++q)
     for (unsigned i = 0; i < n; ++i) {
-      phi[i][q] = hier_hex_shape(i, pts[q]);
-      for (unsigned c = 0; c < 3; ++c) d[c][i][q] = hier_hex_deriv(i, c, pts[q]);
+      phi[i][q] = hier_shape(type, i, pts[q]);
+      for (unsigned c = 0; c < 3; ++c) d[c][i][q] = hier_deriv(type, i, c, pts[q]);
     }
 }
 
@@ -327,6 +591,10 @@ Pt dvd(const Pt &a, double s) { return {{a.v[0] / s, a.v[1] / s, a.v[2] / s}}; }
 // Elem::has_affine_map: cell_hex8.C:121, cell_hex27.C:125, cell_tet4.h:136, cell_tet10.C:143.
 bool has_affine_map(int type, const std::vector<Pt> &p) {
   if (type == TET4) return true;
+  if (type == PRISM6) {  // cell_prism6.C:199-207
+    const Pt v = sub(p[3], p[0]);
+    return rfe(v, sub(p[4], p[1])) && rfe(v, sub(p[5], p[2]));
+  }
   if (type == TET10) {
     const int E[6][3] = {{1, 0, 4}, {2, 1, 5}, {2, 0, 6}, {3, 0, 7}, {3, 1, 8}, {3, 2, 9}};
     for (auto &e : E)
@@ -368,17 +636,21 @@ struct OracleFE {
   std::vector<double> JxW, jac, G[9];                 // G[3*m+d] = dxi_m/dx_d
   std::vector<std::vector<Pt>> dphi;                  // dphi[i][q]
 
-  int family = 0;  // 0 LAGRANGE, 1 HIERARCHIC (hex, order <= 2)
+  int family = 0;  // 0 LAGRANGE, 1 HIERARCHIC (order <= 2)
   bool init(int type_, int order_, int q_order, int family_ = 0) {
     family = family_;
     type = type_; order = order_;
     if (!qgauss_3d(type, q_order, qp, qw)) return false;
     nq = (int)qp.size();
-    n = n_shapes(type, order);
+    const bool p3 = family == 1 && order == 3 && type == HEX27;
+    n = p3 ? 64 : n_shapes(type, order);
     const int geo_order = (type == HEX27 || type == TET10) ? 2 : 1;
     n_geo = n_shapes(type, geo_order);
     if (!n || !n_geo) return false;
-    if (family == 1) all_shapes_hierarchic(order, qp, phi, dref);
+    if (p3) {  // element-dependent: filled by orient() per element
+      phi.assign(n, std::vector<double>(nq));
+      for (int c = 0; c < 3; ++c) dref[c].assign(n, std::vector<double>(nq));
+    } else if (family == 1) all_shapes_hierarchic(type, order, qp, phi, dref);
     else all_shapes(type, order, qp, phi, dref);
     all_shapes(type, geo_order, qp, phi_map, dmap);
     JxW.assign(nq, 0); jac.assign(nq, 0);
@@ -416,6 +688,18 @@ struct OracleFE {
     G[7][p] = (dz_dxi * dx_deta - dx_dxi * dz_deta) * inv_jac;
     G[8][p] = (dx_dxi * dy_deta - dy_dxi * dx_deta) * inv_jac;
     return ok;
+  }
+
+  // HIERARCHIC cubic shapes depend on the element's edge and face orientation:
+  // recomputed for every element (fe.C:174-192 re-inits when the cached
+  // element does not match).
+  void orient(const std::vector<Pt> &X) {
+    if (!(family == 1 && order == 3)) return;
+    for (int q = 0; q < nq; ++q)
+      for (int i = 0; i < n; ++i) {
+        phi[i][q] = hier_hex3_shape(X, i, qp[q]);
+        for (int c = 0; c < 3; ++c) dref[c][i][q] = hier_hex3_deriv(X, i, c, qp[q]);
+      }
   }
 
   bool reinit(const std::vector<Pt> &X) {
@@ -565,6 +849,7 @@ bool element_matrix(const Problem &P, OracleFE &fe, int64_t e, Dense &Ke, std::v
   std::vector<Pt> X(P.npe);
   for (int a = 0; a < P.npe; ++a)
     for (int d = 0; d < 3; ++d) X[a].v[d] = P.xyz[3 * (int64_t)P.conn[e * P.npe + a] + d];
+  fe.orient(X);
   const bool ok = fe.reinit(X);
   const int n = fe.n, nl = P.nl;
   dofs.assign(P.elem_dofs + e * nl, P.elem_dofs + (e + 1) * nl);
@@ -572,9 +857,16 @@ bool element_matrix(const Problem &P, OracleFE &fe, int64_t e, Dense &Ke, std::v
   Fe.assign(nl, 0.0);
   const double coef = P.coef ? P.coef[e] : 1.0;
   std::vector<double> f(n * P.n_vars, 0.0);
-  if (P.nodal_f)
+  if (P.nodal_f && n == P.npe)
     for (int a = 0; a < n; ++a)
       for (int v = 0; v < P.n_vars; ++v) f[a * P.n_vars + v] = P.nodal_f[(int64_t)P.conn[e * P.npe + a] * P.n_vars + v];
+  // More shapes than nodes (HIERARCHIC cubic on HEX27): the nodal load is
+  // interpolated by the mapping basis, f(x_q) = sum_g phi_map_g(q) f_g.
+  const bool geo_load = n != P.npe;
+  std::vector<double> fq(fe.nq, 0.0);
+  if (P.nodal_f && geo_load)
+    for (int qp = 0; qp < fe.nq; qp++)
+      for (int g = 0; g < fe.n_geo; ++g) fq[qp] += fe.phi_map[g][qp] * P.nodal_f[(int64_t)P.conn[e * P.npe + g]];
   if (P.form == ADVDIFF) {
     // Steady Galerkin convection-diffusion (adaptivity_ex2.C:660-690 without
     // the time terms): Ke(i,j) += JxW [(b . dphi_j) phi_i + kappa_e dphi_i . dphi_j],
@@ -595,6 +887,7 @@ bool element_matrix(const Problem &P, OracleFE &fe, int64_t e, Dense &Ke, std::v
     for (int qp = 0; qp < fe.nq; qp++) {
       double fxy = 0.0;
       for (int j = 0; j < n; ++j) fxy += fe.phi[j][qp] * f[j];
+      if (geo_load) fxy = fq[qp];
       for (int i = 0; i != n; i++) Fe[i] += fe.JxW[qp] * fxy * fe.phi[i][qp];
     }
   } else if (P.form == POISSON) {
@@ -606,6 +899,7 @@ bool element_matrix(const Problem &P, OracleFE &fe, int64_t e, Dense &Ke, std::v
     for (int qp = 0; qp < fe.nq; qp++) {
       double fxy = 0.0;
       for (int j = 0; j < n; ++j) fxy += fe.phi[j][qp] * f[j];
+      if (geo_load) fxy = fq[qp];
       for (int i = 0; i != n; i++) Fe[i] += fe.JxW[qp] * fxy * fe.phi[i][qp];
     }
   } else {
@@ -702,8 +996,8 @@ int orc_shapes(int type, int order, int np, const double *pts, double *phi, doub
   const int n = n_shapes(type, order);
   if (!n) return -1;
   if (family == 1) {
-    if (!((type == HEX8 && order == 1) || (type == HEX27 && order == 2))) return -1;
-    all_shapes_hierarchic(order, P, ph, dr);
+    if (!hierarchic_built(type, order)) return -1;
+    all_shapes_hierarchic(type, order, P, ph, dr);
   } else {
     all_shapes(type, order, P, ph, dr);
   }
@@ -715,8 +1009,25 @@ int orc_shapes(int type, int order, int np, const double *pts, double *phi, doub
   return n;
 }
 
+// The 64 cubic HIERARCHIC shapes of one HEX27 element (its 27 node
+// coordinates X) and their difference-quotient derivatives: phi [64][np],
+// dphi [3][64][np].
+int orc_shapes_hier3(const double *X27, int np, const double *pts, double *phi, double *dphi) {
+  std::vector<Pt> X(27);
+  for (int a = 0; a < 27; ++a)
+    for (int d = 0; d < 3; ++d) X[a].v[d] = X27[3 * a + d];
+  for (int q = 0; q < np; ++q) {
+    const Pt p = {{pts[3 * q], pts[3 * q + 1], pts[3 * q + 2]}};
+    for (int i = 0; i < 64; ++i) {
+      phi[i * np + q] = hier_hex3_shape(X, i, p);
+      for (int c = 0; c < 3; ++c) dphi[(c * 64 + i) * np + q] = hier_hex3_deriv(X, i, c, p);
+    }
+  }
+  return 64;
+}
+
 int orc_has_affine_map(int type, const double *X) {
-  const int n = (type == TET4) ? 4 : (type == TET10) ? 10 : (type == HEX8) ? 8 : 27;
+  const int n = (type == TET4) ? 4 : (type == TET10) ? 10 : (type == HEX8) ? 8 : (type == PRISM6) ? 6 : 27;
   std::vector<Pt> p(n);
   for (int a = 0; a < n; ++a)
     for (int d = 0; d < 3; ++d) p[a].v[d] = X[3 * a + d];
@@ -750,6 +1061,68 @@ int orc_distribute_dofs(int64_t n_nodes, int64_t n_elem, int npe, const int32_t 
   return 0;
 }
 
+// FEType{THIRD, HIERARCHIC} on HEX27, one variable: HIERARCHIC_n_dofs_at_node
+// (fe_hierarchic.C:236-290) gives vertices 1, edge nodes o-1 = 2, face nodes
+// (o-1)^2 = 4 and the centre node 0 dofs; the (o-1)^3 = 8 interior dofs belong
+// to the element (n_dofs_per_elem).  distribute_local_dofs_var_major numbers,
+// per element in order, the not yet numbered nodes, then the element's own
+// dofs.  dof_indices (dof_map.h:2619-2760) lists each node's dofs, non-vertex
+// nodes in reverse (extra_hanging_dofs is true for HIERARCHIC), then the
+// element dofs.
+static int hier3_node_dofs(int n) { return n < 8 ? 1 : (n < 20 ? 2 : (n < 26 ? 4 : 0)); }
+
+int orc_distribute_dofs_hier3(int64_t n_nodes, int64_t n_elem, const int32_t *conn, int32_t *elem_dofs,
+                              int64_t *n_dofs) {
+  std::vector<int64_t> base(n_nodes, -1), ebase(n_elem);
+  int64_t next_free_dof = 0;
+  for (int64_t e = 0; e < n_elem; ++e) {
+    for (int n = 0; n < 27; ++n) {
+      const int32_t node = conn[e * 27 + n];
+      if (hier3_node_dofs(n) > 0 && base[node] == -1) {
+        base[node] = next_free_dof;
+        next_free_dof += hier3_node_dofs(n);
+      }
+    }
+    ebase[e] = next_free_dof;
+    next_free_dof += 8;
+  }
+  *n_dofs = next_free_dof;
+  for (int64_t e = 0; e < n_elem; ++e) {
+    int32_t *d = elem_dofs + e * 64;
+    int k = 0;
+    for (int n = 0; n < 27; ++n) {
+      const int nc = hier3_node_dofs(n);
+      const int64_t b = base[conn[e * 27 + n]];
+      if (n < 8) {
+        for (int i = 0; i < nc; ++i) d[k++] = (int32_t)(b + i);
+      } else {
+        for (int i = nc - 1; i >= 0; --i) d[k++] = (int32_t)(b + i);
+      }
+    }
+    for (int i = 0; i < 8; ++i) d[k++] = (int32_t)(ebase[e] + i);
+  }
+  return 0;
+}
+
+// Homogeneous Dirichlet for the cubic HIERARCHIC hex: every dof on a node of
+// a boundary side (vertex, edge and face dofs) has an empty row.
+int orc_dirichlet_hier3(int64_t n_elem, const int32_t *elem_dofs, const int8_t *side_bid, const int32_t *bids,
+                        int n_bids, uint8_t *constrained) {
+  static const int H27[6][9] = {{0, 3, 2, 1, 11, 10, 9, 8, 20}, {0, 1, 5, 4, 8, 13, 16, 12, 21},
+                                {1, 2, 6, 5, 9, 14, 17, 13, 22}, {2, 3, 7, 6, 10, 15, 18, 14, 23},
+                                {3, 0, 4, 7, 11, 12, 19, 15, 24}, {4, 5, 6, 7, 16, 17, 18, 19, 25}};
+  int first[27];
+  for (int n = 0, k = 0; n < 27; ++n) { first[n] = k; k += hier3_node_dofs(n); }
+  for (int64_t e = 0; e < n_elem; ++e)
+    for (int s = 0; s < 6; ++s) {
+      const int b = side_bid[e * 6 + s];
+      if (b < 0 || std::find(bids, bids + n_bids, b) == bids + n_bids) continue;
+      for (int a : H27[s])
+        for (int i = 0; i < hier3_node_dofs(a); ++i) constrained[elem_dofs[e * 64 + first[a] + i]] = 1;
+    }
+  return 0;
+}
+
 // Dofs a homogeneous DirichletBoundary constrains on the given side ids
 // (ConstrainDirichlet, dof_map_constraints.C:257-1560: LAGRANGE dofs of the side's nodes).
 int orc_dirichlet(int64_t n_elem, int type, int n_vars, const int32_t *elem_dofs, const int8_t *side_bid,
@@ -760,8 +1133,9 @@ int orc_dirichlet(int64_t n_elem, int type, int n_vars, const int32_t *elem_dofs
                                 {3, 0, 4, 7, 11, 12, 19, 15, 24}, {4, 5, 6, 7, 16, 17, 18, 19, 25}};
   static const int T4[4][3] = {{0, 2, 1}, {0, 1, 3}, {1, 2, 3}, {2, 0, 3}};
   static const int T10[4][6] = {{0, 2, 1, 6, 5, 4}, {0, 1, 3, 4, 8, 7}, {1, 2, 3, 5, 9, 8}, {2, 0, 3, 6, 7, 9}};
-  const int npe = (type == TET4) ? 4 : (type == TET10) ? 10 : (type == HEX8) ? 8 : 27;
-  const int ns = (type == TET4 || type == TET10) ? 4 : 6;
+  static const int P6[5][4] = {{0, 2, 1, -1}, {0, 1, 4, 3}, {1, 2, 5, 4}, {2, 0, 3, 5}, {3, 4, 5, -1}};
+  const int npe = (type == TET4) ? 4 : (type == TET10) ? 10 : (type == HEX8) ? 8 : (type == PRISM6) ? 6 : 27;
+  const int ns = (type == TET4 || type == TET10) ? 4 : (type == PRISM6) ? 5 : 6;
   const int nl = n_vars * npe;
   for (int64_t e = 0; e < n_elem; ++e)
     for (int s = 0; s < ns; ++s) {
@@ -771,6 +1145,7 @@ int orc_dirichlet(int64_t n_elem, int type, int n_vars, const int32_t *elem_dofs
       if (type == HEX8) sn.assign(H8[s], H8[s] + 4);
       else if (type == HEX27) sn.assign(H27[s], H27[s] + 9);
       else if (type == TET4) sn.assign(T4[s], T4[s] + 3);
+      else if (type == PRISM6) sn.assign(P6[s], P6[s] + ((s == 0 || s == 4) ? 3 : 4));
       else sn.assign(T10[s], T10[s] + 6);
       for (int iv = 0; iv < n_bc_vars; ++iv)
         for (int a : sn) constrained[elem_dofs[e * nl + vars[iv] * npe + a]] = 1;
@@ -839,17 +1214,19 @@ int orc_assemble2(int form, int type, int fe_order, int q_order, int64_t n_nodes
   Problem P{};
   const int family = (fe_order & 0x100) ? 1 : 0;  // HIERARCHIC flag (FEType family)
   fe_order &= 0xff;
-  if (family == 1 && !((type == HEX8 && fe_order == 1) || (type == HEX27 && fe_order == 2))) return 8;
+  const bool p3 = family == 1 && fe_order == 3 && type == HEX27;
+  if (family == 1 && !hierarchic_built(type, fe_order) && !p3) return 8;
+  if (p3 && (n_vars != 1 || form == ELASTICITY)) return 8;
   P.cons_ptr = cons_ptr; P.cons_col = cons_col; P.cons_val = cons_val;
   P.params = params; P.n_params = n_params;
   if (form == ADVDIFF && n_params < 2) return 1;
   P.form = form; P.type = type; P.fe_order = fe_order; P.q_order = q_order;
   P.npe = n_shapes(type, (type == HEX27 || type == TET10) ? 2 : 1);
-  P.n_vars = n_vars; P.nl = n_vars * P.npe;
+  P.n_vars = n_vars; P.nl = n_vars * (p3 ? 64 : P.npe);
   P.n_nodes = n_nodes; P.n_elem = n_elem; P.n_dofs = n_dofs;
   P.xyz = xyz; P.conn = conn; P.elem_dofs = elem_dofs; P.constrained = constrained;
   P.coef = coef; P.nodal_f = nodal_f; P.nu = nu; P.row_ptr = row_ptr; P.col = col;
-  if (n_shapes(type, fe_order) != P.npe) return 8;
+  if (!p3 && n_shapes(type, fe_order) != P.npe) return 8;
   std::fill(K, K + row_ptr[n_dofs], 0.0);
   std::fill(F, F + n_dofs, 0.0);
   if (e_end > n_elem) e_end = n_elem;

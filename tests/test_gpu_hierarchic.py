@@ -1,4 +1,4 @@
-"""HIERARCHIC hex elements (FEType{FIRST/SECOND, HIERARCHIC}) on the GPU:
+"""HIERARCHIC hex, tet and prism elements (FEType{FIRST/SECOND, HIERARCHIC}) on the GPU:
 FP64 drop-in Poisson on the symmetric block path and convection-diffusion on
 the general path, against the oracle's restatement of
 fe_hierarchic_3D_shape / cube_indices / fe_fdm_deriv.
@@ -38,7 +38,9 @@ def problem(n, et, jitter=0.0, seed=3):
 
 
 @pytest.mark.parametrize("et,fo,qo,n,jit", [(lm.HEX8, 1, 3, 6, 0.0), (lm.HEX8, 1, 3, 5, 0.2),
-                                           (lm.HEX27, 2, 5, 4, 0.0)])
+                                           (lm.HEX27, 2, 5, 4, 0.0), (lm.TET4, 1, 2, 4, 0.2),
+                                           (lm.TET10, 2, 4, 3, 0.0), (lm.TET10, 2, 4, 3, 0.2),
+                                           (lm.PRISM6, 1, 3, 4, 0.0), (lm.PRISM6, 1, 3, 3, 0.2)])
 def test_hierarchic_poisson_matches_oracle(et, fo, qo, n, jit):
     m, dm, k, f = problem(n, et, jit)
     check(lm.POISSON, m, dm, k, f, fo, qo)

@@ -58,7 +58,8 @@ def test_poisson_hex8_nonaffine():
 
 
 @pytest.mark.parametrize("et,fo,qo,n,jit", [(lm.HEX27, 2, 5, 3, 0.0), (lm.TET4, 1, 2, 4, 0.2),
-                                            (lm.TET10, 2, 4, 3, 0.2), (lm.TET10, 2, 3, 2, 0.0)])
+                                            (lm.TET10, 2, 4, 3, 0.2), (lm.TET10, 2, 3, 2, 0.0),
+                                            (lm.PRISM6, 1, 3, 4, 0.0), (lm.PRISM6, 1, 5, 3, 0.2)])
 def test_poisson_other_elements(et, fo, qo, n, jit):
     mesh, dm, k, f = make_problem(n, et, 1, lm.POISSON, jitter=jit)
     check_parity(mesh, dm, lm.POISSON, fo, qo, k, f)
@@ -89,6 +90,16 @@ def test_elasticity_hex8_and_tet4():
     check_parity(mesh, dm, lm.ELASTICITY, 1, 2, k, f, nu=0.25)
     mesh, dm, k, f = make_problem(3, lm.TET4, 3, lm.ELASTICITY, jitter=0.2)
     check_parity(mesh, dm, lm.ELASTICITY, 1, 2, k, f)
+
+
+@pytest.mark.parametrize("jit", [0.0, 0.2])
+def test_elasticity_prism6(jit):
+    """PRISM6 (build_cube, two prisms per cell): affine when unjittered, the
+    per-quadrature-point map once interior nodes move."""
+    mesh, dm, k, f = make_problem(3, lm.PRISM6, 3, lm.ELASTICITY, jitter=jit)
+    aff = sum(orc.has_affine_map(lm.PRISM6, x) for x in mesh.xyz[mesh.conn])
+    assert (aff == mesh.n_elem) == (jit == 0.0)
+    check_parity(mesh, dm, lm.ELASTICITY, 1, 3, k, f)
 
 
 def test_repeat_is_bitwise_deterministic():

@@ -10,7 +10,7 @@ import oracle as orc
 from libmesh_gb300._capi import lib, ptr
 
 CASES = [(lm.HEX8, 1, 4), (lm.HEX27, 1, 3), (lm.TET4, 1, 3), (lm.TET10, 3, 3), (lm.TET10, 1, 2),
-         (lm.HEX8, 3, 3)]
+         (lm.HEX8, 3, 3), (lm.PRISM6, 1, 3), (lm.PRISM6, 3, 2)]
 
 
 def host_sparsity(dm):
