@@ -112,6 +112,28 @@ lmg_status lmg_dirichlet_dofs(int64_t n_elem, int32_t elem_type, int32_t n_vars,
                               const int32_t *vars, int32_t n_vars_bc,
                               int64_t n_dofs, uint8_t *constrained);
 
+/* Dofs per element of FEType fe_order (| LMG_HIERARCHIC) on elem_type for
+ * n_vars variables: n_vars * nodes for the nodal cases, 64 for
+ * FEType{THIRD, HIERARCHIC} on HEX27 (HIERARCHIC_n_dofs, src/fe/fe_hierarchic.C:94-141). */
+lmg_status lmg_fe_dofs_per_elem(int32_t elem_type, int32_t fe_order, int32_t n_vars, int32_t *n);
+
+/* DofMap::distribute_dofs + dof_indices for an FEType: the nodal cases as
+ * lmg_dofmap_distribute; FEType{THIRD, HIERARCHIC} on HEX27 (one variable)
+ * with HIERARCHIC_n_dofs_at_node's per-node counts (vertex 1, edge node 2,
+ * face node 4, centre 0) and 8 element-interior dofs, numbered per element
+ * nodes-then-element (src/base/dof_map.C:1417-1537), non-vertex node dofs
+ * listed last to first (include/base/dof_map.h:2685-2712).
+ * elem_dofs [n_elem][lmg_fe_dofs_per_elem]. */
+lmg_status lmg_dofmap_distribute_fe(int64_t n_nodes, int64_t n_elem, int32_t elem_type, const int32_t *conn,
+                                    int32_t n_vars, int32_t fe_order, int64_t *n_dofs, int32_t *elem_dofs);
+
+/* lmg_dirichlet_dofs for an FEType: for FEType{THIRD, HIERARCHIC} every dof
+ * of every node of a matching side (vertex, edge and face dofs). */
+lmg_status lmg_dirichlet_dofs_fe(int64_t n_elem, int32_t elem_type, int32_t fe_order, int32_t n_vars,
+                                 const int32_t *elem_dofs, const int8_t *side_bid, const int32_t *bids,
+                                 int32_t n_bids, const int32_t *vars, int32_t n_vars_bc, int64_t n_dofs,
+                                 uint8_t *constrained);
+
 /* DofMap::compute_sparsity on the host (the same pattern lmg_sparsity_build
  * puts on the device): PETSc-AIJ CSR with sorted columns, full coupling of the
  * dofs of each element.  Call with row_ptr = col_idx = NULL to get nnz. */
@@ -178,6 +200,14 @@ lmg_status lmg_mesh_upload(lmg_ctx *ctx, int64_t n_nodes, const double *xyz,
 lmg_status lmg_dofmap_upload(lmg_ctx *ctx, int32_t n_vars, int64_t n_dofs,
                              const int32_t *elem_dofs);
 
+/* dof_indices output for an FEType whose dofs are not one per node and
+ * variable: elem_dofs[e][0 .. lmg_fe_dofs_per_elem) as
+ * lmg_dofmap_distribute_fe lists them.  FEType{THIRD, HIERARCHIC} on HEX27
+ * (one variable, affine elements, POISSON, LMG_FP64) assembles on the
+ * general path: full element matrices, constraint product, slot gather. */
+lmg_status lmg_dofmap_upload_fe(lmg_ctx *ctx, int32_t n_vars, int32_t fe_order, int64_t n_dofs,
+                                const int32_t *elem_dofs);
+
 /* Constrained dofs with empty constraint rows and zero values (homogeneous
  * Dirichlet), as DofMap::_dof_constraints holds them. constrained[n_dofs]. */
 lmg_status lmg_constraints_upload(lmg_ctx *ctx, const uint8_t *constrained);
@@ -200,9 +230,10 @@ lmg_status lmg_sparsity_build(lmg_ctx *ctx, int64_t *nnz);
 lmg_status lmg_sparsity_copy(lmg_ctx *ctx, int32_t *row_ptr, int32_t *col_idx);
 
 /* FE family flag OR'ed into fe_order (libMesh FEType{order, family}):
- * LMG_HIERARCHIC selects HIERARCHIC (FIRST on HEX8, SECOND on HEX27; shapes of
- * src/fe/fe_hierarchic_shape_3D.C, derivatives by central differences as
- * FE<3,HIERARCHIC>::shape_deriv takes them).  Without it the family is LAGRANGE. */
+ * LMG_HIERARCHIC selects HIERARCHIC (FIRST on HEX8 / TET4 / PRISM6, SECOND on
+ * HEX27 / TET10, THIRD on HEX27; shapes of src/fe/fe_hierarchic_shape_3D.C with
+ * cube_indices' edge and face orientation, derivatives by central differences
+ * as FE<3,HIERARCHIC>::shape_deriv takes them).  Without it the family is LAGRANGE. */
 enum { LMG_HIERARCHIC = 0x100 };
 
 /* Weak form and its data.  fe_order: 1 FIRST / 2 SECOND LAGRANGE (| LMG_HIERARCHIC).

@@ -106,17 +106,24 @@ class Mesh:
 
 
 class DofMap:
-    """Var-major first-touch numbering of n_vars LAGRANGE variables (one
-    VariableGroup); elem_dofs[e] is DofMap::dof_indices(elem)."""
+    """Var-major first-touch numbering of n_vars variables (one VariableGroup);
+    elem_dofs[e] is DofMap::dof_indices(elem).  fe_order (| HIERARCHIC) picks
+    the FEType whose dofs are numbered: nodal types give one dof per node and
+    variable; 3 | HIERARCHIC on HEX27 gives 64 dofs per element."""
 
-    def __init__(self, mesh, n_vars=1):
+    def __init__(self, mesh, n_vars=1, fe_order=None):
         self.mesh = mesh
         self.n_vars = int(n_vars)
-        npe = mesh.conn.shape[1]
-        self.elem_dofs = np.empty((mesh.n_elem, self.n_vars * npe), np.int32)
+        self.fe_order = 0 if fe_order is None else int(fe_order)
+        n = C.c_int32()
+        if self.fe_order:
+            check(lib().lmg_fe_dofs_per_elem(mesh.elem_type, self.fe_order, self.n_vars, C.byref(n)))
+        else:
+            n.value = self.n_vars * mesh.conn.shape[1]
+        self.elem_dofs = np.empty((mesh.n_elem, n.value), np.int32)
         nd = C.c_int64()
-        check(lib().lmg_dofmap_distribute(mesh.n_nodes, mesh.n_elem, npe, ptr(mesh.conn), self.n_vars,
-                                          C.byref(nd), ptr(self.elem_dofs)))
+        check(lib().lmg_dofmap_distribute_fe(mesh.n_nodes, mesh.n_elem, mesh.elem_type, ptr(mesh.conn),
+                                             self.n_vars, self.fe_order, C.byref(nd), ptr(self.elem_dofs)))
         self.n_dofs = nd.value
         self.constrained = np.zeros(self.n_dofs, np.uint8)
 
@@ -132,9 +139,9 @@ class DofMap:
         bids = np.ascontiguousarray(bids, np.int32)
         variables = np.ascontiguousarray(variables, np.int32)
         c = np.zeros(self.n_dofs, np.uint8)
-        check(lib().lmg_dirichlet_dofs(self.mesh.n_elem, self.mesh.elem_type, self.n_vars,
-                                       ptr(self.elem_dofs), ptr(self.mesh.side_bid), ptr(bids),
-                                       len(bids), ptr(variables), len(variables), self.n_dofs, ptr(c)))
+        check(lib().lmg_dirichlet_dofs_fe(self.mesh.n_elem, self.mesh.elem_type, self.fe_order, self.n_vars,
+                                          ptr(self.elem_dofs), ptr(self.mesh.side_bid), ptr(bids),
+                                          len(bids), ptr(variables), len(variables), self.n_dofs, ptr(c)))
         self.constrained |= c
         return c
 
@@ -199,7 +206,8 @@ class GpuAssembly:
         self.mesh, self.dof_map = mesh, dof_map
         self._ok(L.lmg_mesh_upload(self.ctx, mesh.n_nodes, ptr(mesh.xyz), mesh.n_elem, mesh.elem_type,
                                    ptr(mesh.conn)))
-        self._ok(L.lmg_dofmap_upload(self.ctx, dof_map.n_vars, dof_map.n_dofs, ptr(dof_map.elem_dofs)))
+        self._ok(L.lmg_dofmap_upload_fe(self.ctx, dof_map.n_vars, getattr(dof_map, "fe_order", 0), dof_map.n_dofs,
+                                        ptr(dof_map.elem_dofs)))
         if dof_map.cons_ptr is not None and len(dof_map.cons_col):
             self._ok(L.lmg_constraint_rows_upload(self.ctx, ptr(dof_map.constrained), ptr(dof_map.cons_ptr),
                                                   ptr(dof_map.cons_col), ptr(dof_map.cons_val)))

@@ -35,6 +35,9 @@ SIGNATURES = {
     "lmg_mesh_free": [_p],
     "lmg_dofmap_distribute": [_i64, _i64, _i32, _p, _i32, _pi64, _p],
     "lmg_dirichlet_dofs": [_i64, _i32, _i32, _p, _p, _p, _i32, _p, _i32, _i64, _p],
+    "lmg_fe_dofs_per_elem": [_i32, _i32, _i32, _pi32],
+    "lmg_dofmap_distribute_fe": [_i64, _i64, _i32, _p, _i32, _i32, _pi64, _p],
+    "lmg_dirichlet_dofs_fe": [_i64, _i32, _i32, _i32, _p, _p, _p, _i32, _p, _i32, _i64, _p],
     "lmg_host_sparsity": [_i64, _i32, _i32, _i64, _p, _pi64, _p, _p],
     "lmg_mesh_refine": [_p, _i32, _f64, _u64],
     "lmg_mesh_tree": [_p, _pi64, _p, _p, _p, _p],
@@ -45,6 +48,7 @@ SIGNATURES = {
     "lmg_context_set_stream": [_p, _p],
     "lmg_mesh_upload": [_p, _i64, _p, _i64, _i32, _p],
     "lmg_dofmap_upload": [_p, _i32, _i64, _p],
+    "lmg_dofmap_upload_fe": [_p, _i32, _i32, _i64, _p],
     "lmg_constraints_upload": [_p, _p],
     "lmg_constraint_rows_upload": [_p, _p, _p, _p, _p],
     "lmg_sparsity_build": [_p, _pi64],

@@ -381,6 +381,7 @@ lmg_status lmg_context_destroy(lmg_ctx *c) {
   dfree(c->d_F); dfree(c->d_Koff32); dfree(c->d_status); dfree(c->d_bad);
   dfree(c->d_relslot); dfree(c->d_geo);
   general_free(c);
+  hier3_free(c);
   dfree(c->d_D6); dfree(c->d_modes);
   for (cudaEvent_t e : c->chunk_ev) cudaEventDestroy(e);
   if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
@@ -436,6 +437,7 @@ lmg_status lmg_dofmap_upload(lmg_ctx *c, int32_t n_vars, int64_t n_dofs, const i
   c->n_vars = n_vars;
   c->nl = nl;
   c->n_dofs = n_dofs;
+  c->hier3 = false;
   c->h_elem_dofs.assign(elem_dofs, elem_dofs + c->n_elem * nl);
   detect_blocks(c);
   LMG_CUDA(c, dupload(c, c->d_eb, c->h_eb.data(), c->h_eb.size()));
@@ -445,6 +447,36 @@ lmg_status lmg_dofmap_upload(lmg_ctx *c, int32_t n_vars, int64_t n_dofs, const i
   c->h_cons_val.clear();
   c->has_rows = false;
   c->have_sparsity = false;
+  c->gen_plan = false;
+  return upload_cmask(c);
+}
+
+lmg_status lmg_dofmap_upload_fe(lmg_ctx *c, int32_t n_vars, int32_t fe_order, int64_t n_dofs,
+                                const int32_t *elem_dofs) {
+  if (fe_order != (3 | LMG_HIERARCHIC)) return lmg_dofmap_upload(c, n_vars, n_dofs, elem_dofs);
+  if (!c || !elem_dofs || n_vars != 1 || n_dofs <= 0) return fail(c, LMG_ERR_ARG, "dofmap_upload: bad argument");
+  if (!c->n_elem) return fail(c, LMG_ERR_STATE, "dofmap_upload: upload the mesh first");
+  if (c->elem_type != LMG_HEX27) return fail(c, LMG_ERR_UNSUPPORTED, "dofmap_upload: THIRD HIERARCHIC needs HEX27");
+  const int nl = 64;
+  for (int64_t i = 0; i < c->n_elem * nl; ++i)
+    if (elem_dofs[i] < 0 || elem_dofs[i] >= n_dofs) return fail(c, LMG_ERR_BOUNDS, "dof id out of range", i / nl);
+  cudaSetDevice(c->device);
+  c->n_vars = 1;
+  c->nl = nl;
+  c->n_dofs = n_dofs;
+  c->hier3 = true;
+  c->h_elem_dofs.assign(elem_dofs, elem_dofs + c->n_elem * nl);
+  c->bs = 1;  // no block structure: the general path assembles these systems
+  c->nb = nl;
+  c->n_blocks = n_dofs;
+  c->h_eb.clear();
+  c->h_constrained.clear();
+  c->h_cons_ptr.clear();
+  c->h_cons_col.clear();
+  c->h_cons_val.clear();
+  c->has_rows = false;
+  c->have_sparsity = false;
+  c->have_form = false;
   c->gen_plan = false;
   return upload_cmask(c);
 }
@@ -470,7 +502,7 @@ lmg_status lmg_sparsity_build(lmg_ctx *c, int64_t *nnz) {
   c->gen_plan = false;
   c->h_row_ptr.clear();
   c->h_col.clear();
-  c->general = c->has_rows || (c->have_form && c->form == LMG_ADVDIFF);
+  c->general = c->has_rows || c->hier3 || (c->have_form && c->form == LMG_ADVDIFF);
   if (c->general) {  // constraint rows with coefficients: find_connected_dofs pattern
     lmg_status st = general_sparsity(c);
     if (st) return st;
@@ -550,6 +582,9 @@ lmg_status lmg_form_set(lmg_ctx *c, int32_t form, int32_t fe_order, int32_t q_or
       return fail(c, LMG_ERR_ARG, "form_set: ADVDIFF parameter count does not match n_modes");
   }
   cudaSetDevice(c->device);
+  if (c->hier3 != (fe_order == (3 | LMG_HIERARCHIC)))
+    return fail(c, LMG_ERR_STATE, "form_set: the dof lists were uploaded for another FE type");
+  if (c->hier3) return hier3_form_set(c, form, q_order, elem_coef, nodal_f);
   const int family = (fe_order & LMG_HIERARCHIC) ? 1 : 0;
   fe_order &= 0xff;
   FETables t;

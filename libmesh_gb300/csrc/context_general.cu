@@ -74,7 +74,7 @@ lmg_status general_sparsity(lmg_ctx *c) {
 lmg_status general_plan(lmg_ctx *c) {
   const int N = c->nl;
   const int64_t E = c->n_elem;
-  if (c->n_vars != 1 || N > GEN_MAX_N)
+  if (c->n_vars != 1 || (N > GEN_MAX_N && !(c->hier3 && N == 64)))
     return fail(c, LMG_ERR_UNSUPPORTED, "general path: one variable and at most 27 dofs per element");
   if (c->h_row_ptr.empty()) {  // pattern built by the block path: bring it to the host
     c->h_row_ptr.resize((size_t)c->n_dofs + 1);
@@ -272,7 +272,8 @@ lmg_status general_assemble(lmg_ctx *c) {
   a.status = c->d_status;
   a.bad_elem = c->d_bad;
   a.fe = c->dfe;
-  launch_gen_elements(c->form, c->tab.n, c->tab.q, a, c->n_sm * c->ctas_per_sm / 4, c->stream);
+  if (c->hier3) launch_hier3(c);
+  else launch_gen_elements(c->form, c->tab.n, c->tab.q, a, c->n_sm * c->ctas_per_sm / 4, c->stream);
   c->launches++;
   if (c->n_cons_elem) {
     ConsArgs k{};

@@ -86,6 +86,11 @@ struct lmg_ctx {
   uint8_t *d_cci = nullptr;
   double *d_ccv = nullptr;
   uint64_t *d_crow = nullptr;
+  // cubic HIERARCHIC hexes (hier3.cu): dof lists of 64 per element, general path
+  bool hier3 = false;
+  uint16_t *d_h3var = nullptr;       // [n_elem][64] shape variant
+  double *d_h3D = nullptr, *d_h3M = nullptr, *d_h3gd = nullptr;
+  int h3V = 0;
   // PerfLog-style stage timing (CUDA events on the context stream)
   bool perflog = false;
   std::vector<cudaEvent_t> ev;       // 3 per logged assemble call
@@ -138,6 +143,11 @@ lmg_status general_sparsity(lmg_ctx *c);   // CSR with the constraint couplings
 lmg_status general_plan(lmg_ctx *c);       // constraint columns, slot plan, buffers
 lmg_status general_assemble(lmg_ctx *c);   // element and constraint kernels
 void general_gather(lmg_ctx *c);           // slot gather into K and F
+// hier3.cu
+void hier3_free(lmg_ctx *c);
+lmg_status hier3_form_set(lmg_ctx *c, int32_t form, int32_t q_order, const double *elem_coef,
+                          const double *nodal_f);
+void launch_hier3(lmg_ctx *c);
 void general_free(lmg_ctx *c);             // plan and work buffers
 
 }  // namespace lmg

@@ -49,6 +49,24 @@ void gauss_legendre(int np, std::vector<double> &x, std::vector<double> &w) {
     x[i] = (double)z;
     w[i] = (double)(2.0L / ((1 - z * z) * dp * dp));
   }
+  // 3-5 points: the 32-digit values libMesh tabulates (quadrature_gauss_1D.C:30-120),
+  // so that difference quotients taken at these points match bit for bit.
+  if (np == 3) {
+    x[0] = -7.7459666924148337703585307995648e-01;
+    w[0] = 5.0 / 9;
+    w[1] = 8.0 / 9;
+  } else if (np == 4) {
+    x[0] = -8.6113631159405257522394648889281e-01;
+    x[1] = -3.3998104358485626480266575910324e-01;
+    w[0] = 3.4785484513745385737306394922200e-01;
+    w[1] = 6.5214515486254614262693605077800e-01;
+  } else if (np == 5) {
+    x[0] = -9.0617984593866399279762687829939e-01;
+    x[1] = -5.3846931010568309103631442070021e-01;
+    w[0] = 2.3692688505618908751426404071992e-01;
+    w[1] = 4.7862867049936646804129151483564e-01;
+    w[2] = 5.6888888888888888888888888888889e-01;
+  }
   if (np % 2 == 1) x[np / 2] = 0.0;  // the middle node is exactly zero
   for (int i = 0; i < np / 2; ++i) {  // exact symmetry, as libMesh stores it
     x[np - 1 - i] = -x[i];

@@ -1,0 +1,217 @@
+// Tables of the cubic HIERARCHIC hex (FEType{THIRD, HIERARCHIC} on HEX27).
+//
+// libMesh evaluates shape i of an element as
+//   phi_i(xi) = h(i0, c0) * h(i1, c1) * h(i2, c2),  c_s = +-xi_{src(s)}
+// where cube_indices (src/fe/fe_hierarchic_shape_3D.C:166-760) picks the 1-D
+// indices (i0, i1, i2) and, from the element's edge and face orientation,
+// which reference coordinate feeds each slot and with which sign; the
+// derivatives are central differences with eps = 1e-6 (fe_fdm_deriv,
+// src/fe/fe.C:794-811, 929-944).  Every element thus uses shapes drawn from
+// a small set of "variants" (i0, i1, i2, slot sources, slot signs).  The
+// host finds each element's 64 variants, tabulates every variant that occurs
+// -- evaluated in the same order, so the difference quotients are the
+// reference's bit for bit -- and the affine reference tensors over variant
+// pairs,
+//   D_k[v][w] = sum_q w_q dphi_v^m(q) dphi_w^n(q)   (k = the six m <= n pairs,
+//                                                     off-diagonal pairs summed)
+//   M[v][g]   = sum_q w_q phi_v(q) phi^geo_g(q)     (load through the HEX27 map basis)
+// so that the device forms K_ij = sum_k A_k D_k[var_i][var_j] per element.
+#include <cmath>
+#include <unordered_map>
+
+#include "lmg_internal.h"
+
+namespace lmg {
+
+namespace {
+
+struct P3 { double v[3]; };
+
+bool pt_less(const double *a, const double *b) {  // TypeVector::operator<
+  for (int i = 0; i < 3; i++) {
+    if (a[i] < b[i]) return true;
+    if (a[i] > b[i]) return false;
+  }
+  return false;
+}
+bool pt_eq(const double *a, const double *b) { return a[0] == b[0] && a[1] == b[1] && a[2] == b[2]; }
+
+const int EDGE[12][2] = {{0, 1}, {1, 2}, {2, 3}, {0, 3}, {0, 4}, {1, 5}, {2, 6}, {3, 7}, {4, 5}, {5, 6}, {6, 7}, {4, 7}};
+const int SIDE4[6][4] = {{0, 3, 2, 1}, {0, 1, 5, 4}, {1, 2, 6, 5}, {2, 3, 7, 6}, {3, 0, 4, 7}, {4, 5, 6, 7}};
+
+// Signature of one shape: 1-D indices per slot, source coordinate per slot,
+// negation per slot.
+struct Sig {
+  int idx[3];
+  int src[3];
+  int neg[3];
+  uint32_t key() const {
+    uint32_t k = 0;
+    for (int s = 0; s < 3; ++s) k |= (uint32_t)idx[s] << (2 * s) | (uint32_t)src[s] << (6 + 2 * s) |
+                                     (uint32_t)neg[s] << (12 + s);
+    return k;
+  }
+};
+
+// cube_indices at totalorder 3 for the element with vertex coordinates X[8][3].
+Sig cube_sig(const double (*X)[3], int i) {
+  Sig g = {{0, 0, 0}, {0, 1, 2}, {0, 0, 0}};
+  static const int V[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0}, {0, 0, 1}, {1, 0, 1}, {1, 1, 1}, {0, 1, 1}};
+  if (i < 8) {
+    for (int s = 0; s < 3; ++s) g.idx[s] = V[i][s];
+    return g;
+  }
+  if (i < 32) {  // two dofs per edge; the edge's own coordinate flips by orientation
+    static const int DIR[12] = {0, 1, 0, 1, 2, 2, 2, 2, 0, 1, 0, 1};
+    static const int FIX[12][2] = {{0, 0}, {1, 0}, {1, 0}, {0, 0}, {0, 0}, {1, 0},
+                                   {1, 1}, {0, 1}, {0, 1}, {1, 1}, {1, 1}, {0, 1}};
+    const int ed = (i - 8) / 2, k = i - 2 * ed - 6, d = DIR[ed];
+    const bool pos = pt_less(X[EDGE[ed][1]], X[EDGE[ed][0]]);  // Elem::positive_edge_orientation
+    const bool flip = (ed == 2 || ed == 10) ? !pos : pos;
+    for (int s = 0, f = 0; s < 3; ++s) g.idx[s] = (s == d) ? k : FIX[ed][f++];
+    g.neg[d] = flip ? 1 : 0;
+    return g;
+  }
+  if (i < 56) {  // four dofs per face: in-face coordinates swapped / reflected by the face case
+    static const int SQ_ROW[4] = {0, 1, 1, 0}, SQ_COL[4] = {0, 0, 1, 1};
+    static const int AX[6][2] = {{0, 1}, {0, 2}, {1, 2}, {0, 2}, {1, 2}, {0, 1}};  // slots A, B
+    static const int FIXED[6][2] = {{2, 0}, {1, 0}, {0, 1}, {1, 1}, {0, 0}, {2, 1}};  // slot, index
+    static const int TESTV[6][4] = {{0, 3, 2, 1}, {0, 1, 5, 4}, {1, 2, 6, 5}, {3, 7, 6, 2}, {0, 4, 7, 3}, {4, 5, 6, 7}};
+    static const int GMP[6][4] = {{1, 2, 0, 3}, {0, 1, 5, 4}, {1, 2, 6, 5}, {2, 3, 7, 6}, {3, 0, 4, 7}, {4, 5, 6, 7}};
+    static const bool NEG[6] = {false, true, true, false, false, true};
+    // (A source, A negated, B source, B negated) with 0 = A, 1 = B
+    enum { ID, SW, TA, TB, NG, NS, TC, TD };
+    static const int MAP[8][4] = {{0, 0, 1, 0}, {1, 0, 0, 0}, {1, 1, 0, 0}, {0, 0, 1, 1},
+                                  {0, 1, 1, 1}, {1, 1, 0, 1}, {1, 0, 0, 1}, {0, 1, 1, 0}};
+    static const int CASE[6][4][2] = {{{ID, SW}, {TA, TB}, {NG, NS}, {TC, TD}},
+                                      {{ID, SW}, {TC, TD}, {NG, NS}, {TD, TB}},
+                                      {{ID, SW}, {TC, TD}, {NG, NS}, {TA, TB}},
+                                      {{ID, SW}, {TA, TB}, {NG, NS}, {TC, TD}},
+                                      {{ID, SW}, {TA, TB}, {NG, NS}, {TC, TD}},
+                                      {{ID, SW}, {TC, TD}, {NG, NS}, {TA, ID}}};
+    const int f = (i - 32) / 4, b = i - 32 - 4 * f;
+    const int sa = AX[f][0], sb = AX[f][1];
+    g.idx[sa] = SQ_ROW[b] + 2;
+    g.idx[sb] = SQ_COL[b] + 2;
+    g.idx[FIXED[f][0]] = FIXED[f][1];
+    // get_min_point and positive_face_orientation (elem.C:3642-3661)
+    const double *m = X[GMP[f][0]];
+    for (int t = 1; t < 4; ++t)
+      if (pt_less(X[GMP[f][t]], m)) m = X[GMP[f][t]];
+    int v = 0;
+    for (int t = 1; t < 4; ++t)
+      if (pt_less(X[SIDE4[f][t]], X[SIDE4[f][v]])) v = t;
+    const bool pos = pt_less(X[SIDE4[f][(v + 3) % 4]], X[SIDE4[f][(v + 1) % 4]]);
+    const bool o = NEG[f] ? !pos : pos;
+    for (int t = 0; t < 4; ++t) {
+      if (!pt_eq(X[TESTV[f][t]], m)) continue;
+      const int *mp = MAP[CASE[f][t][o ? 0 : 1]];
+      const int slot[2] = {sa, sb};
+      g.src[sa] = slot[mp[0]];
+      g.neg[sa] = mp[1];
+      g.src[sb] = slot[mp[2]];
+      g.neg[sb] = mp[3];
+      break;
+    }
+    return g;
+  }
+  static const int CB_COL[8] = {0, 0, 1, 1, 0, 1, 1, 0}, CB_ROW[8] = {0, 1, 1, 0, 1, 1, 0, 0},
+                   CB_PAGE[8] = {0, 0, 0, 0, 1, 1, 1, 1};
+  const int b = i - 56;
+  g.idx[0] = CB_COL[b] + 2;
+  g.idx[1] = CB_ROW[b] + 2;
+  g.idx[2] = CB_PAGE[b] + 2;
+  return g;
+}
+
+// fe_hierarchic_1D_shape for i <= 3 (src/fe/fe_hierarchic_shape_1D.C:430-498).
+double h1(int i, double x) {
+  switch (i) {
+    case 0: return .5 * (1. - x);
+    case 1: return .5 * (1. + x);
+    case 2: return (x * x - 1.) / 2.;
+    default: return (x * x * x - x) / 6.;
+  }
+}
+
+double sig_value(const Sig &g, const double *p) {
+  double c[3];
+  for (int s = 0; s < 3; ++s) c[s] = g.neg[s] ? -p[g.src[s]] : p[g.src[s]];
+  return h1(g.idx[0], c[0]) * h1(g.idx[1], c[1]) * h1(g.idx[2], c[2]);
+}
+
+}  // namespace
+
+std::string build_hier3_tables(Hier3Tables &h, int q_order, int64_t n_elem, const double *xyz, const int32_t *conn) {
+  h = Hier3Tables();
+  FETables geo;
+  std::string err = build_fe_tables(geo, LMG_HEX27, 2, q_order, 0);  // QGauss and the HEX27 map basis
+  if (!err.empty()) return err;
+  h.q = geo.q;
+  h.gd0.assign(geo.gdphi.begin(), geo.gdphi.begin() + 27 * 3);
+  std::unordered_map<uint32_t, int> id;
+  std::vector<Sig> vars;
+  h.var.resize((size_t)n_elem * 64);
+  double X[8][3];
+  for (int64_t e = 0; e < n_elem; ++e) {
+    for (int a = 0; a < 8; ++a)
+      for (int d = 0; d < 3; ++d) X[a][d] = xyz[3 * (int64_t)conn[e * 27 + a] + d];
+    for (int i = 0; i < 64; ++i) {
+      const Sig g = cube_sig(X, i);
+      auto it = id.find(g.key());
+      int v;
+      if (it == id.end()) {
+        v = (int)vars.size();
+        id.emplace(g.key(), v);
+        vars.push_back(g);
+      } else {
+        v = it->second;
+      }
+      h.var[(size_t)e * 64 + i] = (uint16_t)v;
+    }
+  }
+  const int V = (int)vars.size(), Q = geo.q;
+  if (V > 65535) return "too many shape variants";
+  h.V = V;
+  // variant values and difference-quotient derivatives at the quadrature points
+  std::vector<double> phi((size_t)V * Q), dphi((size_t)V * Q * 3);
+  const double eps = 1.e-6;
+  for (int v = 0; v < V; ++v)
+    for (int q = 0; q < Q; ++q) {
+      const double *p = &geo.qp[3 * (size_t)q];
+      phi[(size_t)v * Q + q] = sig_value(vars[(size_t)v], p);
+      for (int j = 0; j < 3; ++j) {
+        double pp[3] = {p[0], p[1], p[2]}, pm[3] = {p[0], p[1], p[2]};
+        pp[j] += eps;
+        pm[j] -= eps;
+        dphi[((size_t)v * Q + q) * 3 + j] =
+            (sig_value(vars[(size_t)v], pp) - sig_value(vars[(size_t)v], pm)) / 2. / eps;
+      }
+    }
+  const int pm[6][2] = {{0, 0}, {1, 1}, {2, 2}, {0, 1}, {0, 2}, {1, 2}};
+  h.D.assign((size_t)V * V * 6, 0.0);
+  for (int v = 0; v < V; ++v)
+    for (int w = 0; w < V; ++w) {
+      double S[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+      for (int q = 0; q < Q; ++q) {
+        const double *a = &dphi[((size_t)v * Q + q) * 3], *b = &dphi[((size_t)w * Q + q) * 3];
+        for (int m = 0; m < 3; ++m)
+          for (int n = 0; n < 3; ++n) S[m][n] += geo.qw[(size_t)q] * a[m] * b[n];
+      }
+      double *o = &h.D[((size_t)v * V + w) * 6];
+      for (int k = 0; k < 6; ++k) {
+        const int m0 = pm[k][0], m1 = pm[k][1];
+        o[k] = (m0 == m1) ? S[m0][m0] : S[m0][m1] + S[m1][m0];
+      }
+    }
+  h.M.assign((size_t)V * 27, 0.0);
+  for (int v = 0; v < V; ++v)
+    for (int g = 0; g < 27; ++g) {
+      double s = 0.0;
+      for (int q = 0; q < Q; ++q) s += geo.qw[(size_t)q] * phi[(size_t)v * Q + q] * geo.gphi[(size_t)q * 27 + g];
+      h.M[(size_t)v * 27 + g] = s;
+    }
+  return "";
+}
+
+}  // namespace lmg

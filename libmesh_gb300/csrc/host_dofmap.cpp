@@ -268,6 +268,101 @@ lmg_status lmg_dofmap_distribute(int64_t n_nodes, int64_t n_elem, int32_t npe, c
   return LMG_OK;
 }
 
+// FEType{THIRD, HIERARCHIC} on HEX27 (HIERARCHIC_n_dofs_at_node,
+// fe_hierarchic.C:236-290): a vertex carries 1 dof, an edge node 2, a face
+// node 4, the centre node none; the 8 interior dofs belong to the element.
+// distribute_local_dofs_var_major numbers, per element, the nodes not yet
+// numbered and then the element's dofs; dof_indices lists a non-vertex node's
+// dofs last to first (extra_hanging_dofs, dof_map.h:2685-2712).
+static int hier3_node_dofs(int a) { return a < 8 ? 1 : (a < 20 ? 2 : (a < 26 ? 4 : 0)); }
+
+lmg_status lmg_fe_dofs_per_elem(int32_t elem_type, int32_t fe_order, int32_t n_vars, int32_t *n) {
+  if (!n || n_vars <= 0) return LMG_ERR_ARG;
+  if (fe_order == (3 | LMG_HIERARCHIC)) {
+    if (elem_type != LMG_HEX27 || n_vars != 1) return LMG_ERR_UNSUPPORTED;
+    *n = 64;
+    return LMG_OK;
+  }
+  const int npe = lmg::nodes_per_elem(elem_type);
+  if (!npe) return LMG_ERR_UNSUPPORTED;
+  *n = n_vars * npe;
+  return LMG_OK;
+}
+
+lmg_status lmg_dofmap_distribute_fe(int64_t n_nodes, int64_t n_elem, int32_t elem_type, const int32_t *conn,
+                                    int32_t n_vars, int32_t fe_order, int64_t *n_dofs, int32_t *elem_dofs) {
+  if (fe_order != (3 | LMG_HIERARCHIC))
+    return lmg_dofmap_distribute(n_nodes, n_elem, lmg::nodes_per_elem(elem_type), conn, n_vars, n_dofs, elem_dofs);
+  if (!conn || !n_dofs || n_nodes < 0 || n_elem < 0) return LMG_ERR_ARG;
+  if (elem_type != LMG_HEX27 || n_vars != 1) return LMG_ERR_UNSUPPORTED;
+  try {
+    std::vector<int64_t> base((size_t)n_nodes, -1), ebase((size_t)n_elem);
+    int64_t next = 0;
+    for (int64_t e = 0; e < n_elem; ++e) {
+      for (int a = 0; a < 27; ++a) {
+        const int32_t n = conn[e * 27 + a];
+        if (n < 0 || n >= n_nodes) return LMG_ERR_BOUNDS;
+        if (hier3_node_dofs(a) && base[(size_t)n] < 0) {
+          base[(size_t)n] = next;
+          next += hier3_node_dofs(a);
+        }
+      }
+      ebase[(size_t)e] = next;
+      next += 8;
+    }
+    if (next > INT32_MAX) return LMG_ERR_UNSUPPORTED;
+    *n_dofs = next;
+    if (elem_dofs)
+      for (int64_t e = 0; e < n_elem; ++e) {
+        int32_t *d = elem_dofs + e * 64;
+        for (int a = 0; a < 27; ++a) {
+          const int c = hier3_node_dofs(a);
+          const int64_t b = base[(size_t)conn[e * 27 + a]];
+          for (int i = 0; i < c; ++i) *d++ = (int32_t)(b + (a < 8 ? i : c - 1 - i));
+        }
+        for (int i = 0; i < 8; ++i) *d++ = (int32_t)(ebase[(size_t)e] + i);
+      }
+  } catch (const std::bad_alloc &) {
+    return LMG_ERR_OOM;
+  }
+  return LMG_OK;
+}
+
+lmg_status lmg_dirichlet_dofs_fe(int64_t n_elem, int32_t elem_type, int32_t fe_order, int32_t n_vars,
+                                 const int32_t *elem_dofs, const int8_t *side_bid, const int32_t *bids,
+                                 int32_t n_bids, const int32_t *vars, int32_t n_vars_bc, int64_t n_dofs,
+                                 uint8_t *constrained) {
+  if (fe_order != (3 | LMG_HIERARCHIC))
+    return lmg_dirichlet_dofs(n_elem, elem_type, n_vars, elem_dofs, side_bid, bids, n_bids, vars, n_vars_bc,
+                              n_dofs, constrained);
+  if (!elem_dofs || !side_bid || !constrained || (n_bids > 0 && !bids)) return LMG_ERR_ARG;
+  if (elem_type != LMG_HEX27 || n_vars != 1) return LMG_ERR_UNSUPPORTED;
+  std::fill(constrained, constrained + n_dofs, (uint8_t)0);
+  if (n_vars_bc == 0) return LMG_OK;
+  int first[27];
+  for (int a = 0, k = 0; a < 27; ++a) {
+    first[a] = k;
+    k += hier3_node_dofs(a);
+  }
+  int sn[9];
+  for (int64_t e = 0; e < n_elem; ++e)
+    for (int s = 0; s < 6; ++s) {
+      const int b = side_bid[e * 6 + s];
+      if (b < 0) continue;
+      bool hit = false;
+      for (int i = 0; i < n_bids; ++i) hit |= (bids[i] == b);
+      if (!hit) continue;
+      const int k = lmg::side_nodes(LMG_HEX27, s, sn);
+      for (int j = 0; j < k; ++j)
+        for (int i = 0; i < hier3_node_dofs(sn[j]); ++i) {
+          const int32_t d = elem_dofs[e * 64 + first[sn[j]] + i];
+          if (d < 0 || d >= n_dofs) return LMG_ERR_BOUNDS;
+          constrained[d] = 1;
+        }
+    }
+  return LMG_OK;
+}
+
 lmg_status lmg_dirichlet_dofs(int64_t n_elem, int32_t elem_type, int32_t n_vars,
                               const int32_t *elem_dofs, const int8_t *side_bid, const int32_t *bids,
                               int32_t n_bids, const int32_t *vars, int32_t n_vars_bc,

@@ -112,6 +112,18 @@ struct FETables {
 // shapes, reference derivatives by libMesh's central differences (eps = 1e-6).
 std::string build_fe_tables(FETables &t, int elem_type, int fe_order, int q_order, int family = 0);
 
+// Cubic HIERARCHIC hex tables (hier3_tables.cpp): each element's 64 shape
+// variants and the tables over the variants that occur.
+struct Hier3Tables {
+  int V = 0;                     // variants
+  int q = 0;                     // quadrature points
+  std::vector<uint16_t> var;     // [n_elem][64] variant of each shape
+  std::vector<double> D;         // [V][V][6] affine reference tensors
+  std::vector<double> M;         // [V][27]   sum_q w phi_v phi^geo_g
+  std::vector<double> gd0;       // [27][3]   HEX27 map derivatives at qp 0
+};
+std::string build_hier3_tables(Hier3Tables &h, int q_order, int64_t n_elem, const double *xyz, const int32_t *conn);
+
 // libMesh Elem::has_affine_map for one element (cell_hex8.C:121, cell_hex27.C:125,
 // cell_tet4 always, cell_tet10.C:143).
 bool elem_has_affine_map(int elem_type, const double *pts /* [npe][3] */);

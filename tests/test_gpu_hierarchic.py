@@ -67,3 +67,31 @@ def test_hierarchic_differs_from_lagrange_but_shares_the_pattern():
     (rp1, c1), K1 = out[1]
     assert np.array_equal(rp0, rp1) and np.array_equal(c0, c1)
     assert np.abs(K0 - K1).max() > 1e-3
+
+
+@pytest.mark.parametrize("rotate,qo,n", [(False, 7, 3), (True, 7, 3), (True, 6, 2)])
+def test_hierarchic_cubic_hex_matches_oracle(rotate, qo, n):
+    """FEType{THIRD, HIERARCHIC} on HEX27 (64 dofs per element): per-element
+    shape variants from cube_indices' edge / face orientation, elements with
+    randomly rotated local node order, homogeneous Dirichlet on every side."""
+    from test_hier3_oracle import rotated_cube
+    m = rotated_cube(n, 21) if rotate else lm.Mesh.build_cube(n, n, n, lm.HEX27)
+    dm = lm.DofMap(m, 1, fe_order=3 | lm.HIERARCHIC)
+    dm.add_dirichlet_boundary([0, 1, 2, 3, 4, 5], [0])
+    rng = np.random.default_rng(8)
+    k = np.exp(rng.normal(0, 0.5, m.n_elem))
+    f = rng.uniform(-1, 1, (m.n_nodes, 1))
+    asm = lm.GpuAssembly(lm.POISSON, 3 | lm.HIERARCHIC, qo, elem_coef=k, nodal_f=f)
+    asm.init(m, dm)
+    rp, ci = asm.sparsity()
+    K, F = asm.assemble()
+    asm.close()
+    rpo, cio = orc.sparsity(dm.n_dofs, dm.elem_dofs)
+    assert np.array_equal(rp, rpo) and np.array_equal(ci, cio)
+    Kr, Fr, st, _ = orc.assemble(lm.POISSON, m.elem_type, 3 | 0x100, qo, m.xyz, m.conn, 1, dm.elem_dofs, dm.n_dofs,
+                                 dm.constrained, rp, ci, coef=k, nodal_f=f)
+    assert st == 0
+    tol = k_tolerance(Kr, rp)
+    assert np.all(np.abs(K - Kr) <= tol), np.max(np.abs(K - Kr) / np.maximum(tol, 1e-300))
+    ftol = 1e-13 * np.abs(Fr).max()
+    assert np.all(np.abs(F - Fr) <= np.maximum(1e-13 * np.abs(Fr), ftol))

@@ -111,3 +111,17 @@ def test_bad_arguments_are_errors():
     nd = C.c_int64()
     ed = np.empty((1, 8), np.int32)
     assert lib().lmg_dofmap_distribute(8, 1, 8, ptr(conn), 1, C.byref(nd), ptr(ed)) == 5
+
+
+@pytest.mark.parametrize("rotate", [False, True])
+def test_hier3_dofs_and_dirichlet_match_oracle(rotate):
+    """FEType{THIRD, HIERARCHIC} on HEX27: per-node dof counts, element dofs,
+    reversed non-vertex dofs, and the Dirichlet set, against the oracle."""
+    from test_hier3_oracle import rotated_cube
+    m = rotated_cube(3, 11) if rotate else lm.Mesh.build_cube(3, 3, 3, lm.HEX27)
+    dm = lm.DofMap(m, 1, fe_order=3 | lm.HIERARCHIC)
+    ed, nd = orc.distribute_dofs_hier3(m.n_nodes, m.conn)
+    assert nd == dm.n_dofs and np.array_equal(ed, dm.elem_dofs)
+    for bids in ([0, 1, 2, 3, 4, 5], [2], [0, 5]):
+        c = lm.DofMap(m, 1, fe_order=3 | lm.HIERARCHIC).add_dirichlet_boundary(bids, [0])
+        assert np.array_equal(c, orc.dirichlet_hier3(ed, m.side_bid, bids, nd))
