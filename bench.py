@@ -237,33 +237,34 @@ def run_amr(args, local):
         "stages_ms": {"elements_and_constraints": el_ms / calls, "insertion": ga_ms / calls}}))
 
 
+BATCH_KINDS = [  # (element, HIERARCHIC order, QGauss order, elements per grid cell)
+    (10, 1, 3, 1),   # HEX8   FIRST
+    (12, 2, 5, 1),   # HEX27  SECOND
+    (12, 3, 7, 1),   # HEX27  THIRD
+    (8, 1, 2, 6),    # TET4   FIRST
+    (9, 2, 4, 6),    # TET10  SECOND
+    (13, 1, 3, 2),   # PRISM6 FIRST
+]
+
+
 def batch_members(n_meshes, seed=3, lo=1e3, hi=5e4):
-    """Meshes with log-uniform element counts in [lo, hi], cycling through
-    HIERARCHIC FIRST HEX8 Poisson, HIERARCHIC SECOND HEX27 Poisson, LAGRANGE
-    TET10 elasticity and LAGRANGE HEX27 convection-diffusion."""
+    """The config-4 mix, scaled: meshes with log-uniform element counts in
+    [lo, hi], cycling through HIERARCHIC hexes (p = 1, 2, 3), tets (p = 1, 2)
+    and prisms (p = 1), Poisson with k_e ~ U[0.1, 10], Dirichlet on every side."""
     import libmesh_gb300 as lm
     rng = np.random.default_rng(seed)
     sizes = np.exp(rng.uniform(np.log(lo), np.log(hi), n_meshes))
     out = []
     for i, s in enumerate(sizes):
-        kind = i % 4
-        per_hex = 6 if kind == 2 else 1
-        n = max(2, int(round((s / per_hex) ** (1.0 / 3.0))))
-        et = [lm.HEX8, lm.HEX27, lm.TET10, lm.HEX27][kind]
-        mesh = lm.Mesh.build_cube(n, n, n, et, jitter=0.2 if kind == 2 else 0.0, seed=i + 1)
-        nv = 3 if kind == 2 else 1
-        dm = lm.DofMap(mesh, nv)
-        dm.add_dirichlet_boundary([4] if kind == 2 else [0, 1, 2, 3, 4, 5], list(range(nv)))
-        k = np.exp(rng.normal(0.0, 0.5, mesh.n_elem))
-        f = rng.uniform(-1.0, 1.0, (mesh.n_nodes, nv))
-        if kind == 0:
-            a = lm.GpuAssembly(lm.POISSON, 1 | lm.HIERARCHIC, 3, elem_coef=k, nodal_f=f)
-        elif kind == 1:
-            a = lm.GpuAssembly(lm.POISSON, 2 | lm.HIERARCHIC, 5, elem_coef=k, nodal_f=f)
-        elif kind == 2:
-            a = lm.GpuAssembly(lm.ELASTICITY, 2, 4, elem_coef=k, nodal_f=f)
-        else:
-            a = lm.GpuAssembly(lm.ADVDIFF, 2, 5, elem_coef=k, nodal_f=f, params=cd_params())
+        et, p, qo, per_cell = BATCH_KINDS[i % len(BATCH_KINDS)]
+        n = max(2, int(round((s / per_cell) ** (1.0 / 3.0))))
+        mesh = lm.Mesh.build_cube(n, n, n, et)
+        fo = p | lm.HIERARCHIC
+        dm = lm.DofMap(mesh, 1, fe_order=fo)
+        dm.add_dirichlet_boundary([0, 1, 2, 3, 4, 5], [0])
+        k = rng.uniform(0.1, 10.0, mesh.n_elem)
+        f = rng.uniform(-1.0, 1.0, (mesh.n_nodes, 1))
+        a = lm.GpuAssembly(lm.POISSON, fo, qo, elem_coef=k, nodal_f=f)
         a.init(mesh, dm)
         out.append((a, mesh.n_elem))
     return out
@@ -318,15 +319,18 @@ def run_batch(args, local):
     ms = ev0.elapsed_time(ev1) / args.steps
     clk = clocks.stop()
     b.close()
+    n_dofs_total = sum(a.dof_map.n_dofs for a, _ in mem)
     for a, _ in mem:
         a.close()
     print(json.dumps({
         "metric": METRIC, "value": total / (ms * 1e-3) / 1e6, "unit": "Melem/s", "n_gpus": 1, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64", "data": "synthetic (seeded sizes, jitter, coefficients, loads)",
-        "config": {"workload": "batch of %d systems, element counts log-uniform in [1e3, 5e4]: HIERARCHIC HEX8 p1 "
-                               "Poisson, HIERARCHIC HEX27 p2 Poisson, TET10 elasticity, HEX27 convection-diffusion"
-                               % n_meshes, "total_elements": total, "setup_s": setup_s, "tune_s": tune_s},
+        "dtype": "f64", "data": "synthetic (seeded sizes, coefficients, loads)",
+        "config": {"workload": "batch of %d systems (config-4 mix, scaled), element counts log-uniform in "
+                               "[1e3, 5e4]: HIERARCHIC Poisson on HEX8 p1, HEX27 p2, HEX27 p3, TET4 p1, TET10 p2, "
+                               "PRISM6 p1, k_e ~ U[0.1, 10]" % n_meshes,
+                   "total_elements": total, "total_dofs": n_dofs_total,
+                   "setup_s": setup_s, "tune_s": tune_s},
         "sequential": {"ms_per_step": seq_ms, "value": total / (seq_ms * 1e-3) / 1e6, "unit": "Melem/s",
                        "how": "lmg_assemble per system on its own stream, host loop, default grids"},
         "graph_speedup": seq_ms / ms, "gpu_launches": launches * args.steps, "launches_per_replay": launches,

@@ -99,6 +99,14 @@ __global__ void k_segsort(int64_t n_seg, const int32_t *ptr, int32_t *v) {
   }
 }
 
+// Last element contributing to block row P (contributions e*nb + a sorted
+// ascending); -1 for a row no element touches.
+__global__ void k_row_last(int64_t n_rows, int nb, const int32_t *ptr, const int32_t *contrib, int32_t *last) {
+  for (int64_t P = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; P < n_rows;
+       P += (int64_t)gridDim.x * blockDim.x)
+    last[P] = ptr[P + 1] > ptr[P] ? contrib[ptr[P + 1] - 1] / nb : -1;
+}
+
 // Re-encodes every matrix contribution (e*nb + a)*nb + b of a slot into the
 // symmetric element storage: diagonal pairs -> e*nb + a (Kdiag block), other
 // pairs -> 2*(e*no + o) + t with o the strictly upper block of {a, b} and
@@ -273,30 +281,47 @@ lmg_status build_plan(lmg_ctx *c) {
   k_fill<<<grid_for(c, nrow, 256), 256, 0, c->stream>>>(nrow, c->d_eb, c->d_fptr, cur, c->d_fcontrib);
   k_segsort<<<grid_for(c, c->n_blocks, 256), 256, 0, c->stream>>>(c->n_blocks, c->d_fptr,
                                                                   c->d_fcontrib);
-  c->launches += 2;
+  // last contributing element of every block row (the pipelined host output
+  // inserts a row once every element before it has run)
+  k_row_last<<<grid_for(c, c->n_blocks, 256), 256, 0, c->stream>>>(c->n_blocks, nb, c->d_fptr, c->d_fcontrib, cur);
+  c->launches += 3;
+  c->h_row_pmax.resize((size_t)c->n_blocks);
+  LMG_CUDA(c, cudaMemcpyAsync(c->h_row_pmax.data(), cur, sizeof(int32_t) * c->n_blocks, cudaMemcpyDeviceToHost,
+                              c->stream));
   LMG_CUDA(c, cudaStreamSynchronize(c->stream));
+  for (size_t P = 1; P < c->h_row_pmax.size(); ++P)  // prefix maximum
+    c->h_row_pmax[P] = std::max(c->h_row_pmax[P], c->h_row_pmax[P - 1]);
   dfree(slot);
   dfree(cnt);
   dfree(cur);
   return check_status(c, "sparsity plan");
 }
 
-// Insertion in row chunks with the device-to-host copy of K overlapped: chunk
-// ch is inserted on the context stream, then copied on a second stream while
-// the next chunk is inserted.  launch_rows(P0, P1) enqueues the insertion of
-// block rows [P0, P1) on the context stream.
+// Host output of K pipelined with the assembly: the elements run in
+// OUT_CHUNKS ranges of element ids; after range ch the block rows whose
+// contributing elements all lie in ranges <= ch (a prefix of the rows, from
+// the prefix maximum of each row's last element) are inserted on the context
+// stream and copied on a second stream while the next range runs.
+// launch_elems(E0, E1) enqueues the element work of elements [E0, E1);
+// launch_rows(P0, P1) the insertion of block rows [P0, P1).
 constexpr int OUT_CHUNKS = 8;
-template <typename Launch>
-lmg_status rows_with_copy(lmg_ctx *c, double *K, Launch &&launch_rows) {
+template <typename LaunchElems, typename LaunchRows>
+lmg_status pipelined_copy(lmg_ctx *c, double *K, LaunchElems &&launch_elems, LaunchRows &&launch_rows) {
   if (!c->copy_stream) LMG_CUDA(c, cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
   while ((int)c->chunk_ev.size() < OUT_CHUNKS) {
     cudaEvent_t e;
     LMG_CUDA(c, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     c->chunk_ev.push_back(e);
   }
-  const int64_t nb = c->n_blocks;
+  const int64_t nb = c->n_blocks, E = c->n_elem;
+  int64_t P0 = 0;
   for (int ch = 0; ch < OUT_CHUNKS; ++ch) {
-    const int64_t P0 = nb * ch / OUT_CHUNKS, P1 = nb * (ch + 1) / OUT_CHUNKS;
+    const int64_t E0 = E * ch / OUT_CHUNKS, E1 = E * (ch + 1) / OUT_CHUNKS;
+    if (E1 > E0) launch_elems(E0, E1);
+    const int64_t P1 = (ch == OUT_CHUNKS - 1)
+                           ? nb
+                           : (int64_t)(std::lower_bound(c->h_row_pmax.begin(), c->h_row_pmax.end(), (int32_t)E1) -
+                                       c->h_row_pmax.begin());
     if (P1 <= P0) continue;
     launch_rows(P0, P1);
     LMG_CUDA(c, cudaEventRecord(c->chunk_ev[ch], c->stream));
@@ -304,14 +329,22 @@ lmg_status rows_with_copy(lmg_ctx *c, double *K, Launch &&launch_rows) {
     const int64_t k0 = c->h_rowptr_blk[(size_t)(c->bs * P0)], k1 = c->h_rowptr_blk[(size_t)(c->bs * P1)];
     LMG_CUDA(c, cudaMemcpyAsync(K + k0, c->d_K + k0, sizeof(double) * (k1 - k0), cudaMemcpyDeviceToHost,
                                 c->copy_stream));
+    P0 = P1;
   }
   return LMG_OK;
+}
+
+// The slice of an ascending element list that falls in [E0, E1).
+inline void list_slice(const std::vector<int32_t> &h, int64_t E0, int64_t E1, int64_t &off, int64_t &cnt) {
+  const auto b = std::lower_bound(h.begin(), h.end(), (int32_t)E0), e = std::lower_bound(h.begin(), h.end(), (int32_t)E1);
+  off = b - h.begin();
+  cnt = e - b;
 }
 
 // Host outputs of a large system take the chunked path.
 bool chunked_output(const lmg_ctx *c, const double *K, int32_t out_on_device) {
   return K && !out_on_device && c->nnz * (int64_t)sizeof(double) > ((int64_t)64 << 20) &&
-         (int64_t)c->h_rowptr_blk.size() == c->n_dofs + 1;
+         (int64_t)c->h_rowptr_blk.size() == c->n_dofs + 1 && (int64_t)c->h_row_pmax.size() == c->n_blocks;
 }
 
 void build_lists(lmg_ctx *c) {
@@ -788,17 +821,30 @@ lmg_status lmg_assemble(lmg_ctx *c, int32_t precision, double *K, double *F, int
     f.K = c->d_K;
     f.F = c->d_F;
     const bool chunked = chunked_output(c, K, out_on_device);
-    launch_fused_mixed(c->form, c->tab.n, c->n_vars, f, grid, c->stream, true, !chunked);
-    c->launches += 2;
     if (chunked) {
-      lmg_status cs = rows_with_copy(c, K, [&](int64_t P0, int64_t P1) {
-        FusedArgs fc = f;
-        fc.row_begin = P0;
-        fc.n_brows = P1;
-        launch_fused_mixed(c->form, c->tab.n, c->n_vars, fc, grid, c->stream, false, true);
-        c->launches++;
-      });
+      lmg_status cs = pipelined_copy(
+          c, K,
+          [&](int64_t E0, int64_t E1) {
+            int64_t off, cnt;
+            list_slice(c->h_aff, E0, E1, off, cnt);
+            if (cnt == 0) return;
+            FusedArgs fg = f;
+            fg.el.list = c->d_aff + off;
+            fg.el.n_list = cnt;
+            launch_fused_mixed(c->form, c->tab.n, c->n_vars, fg, grid, c->stream, true, false);
+            c->launches++;
+          },
+          [&](int64_t P0, int64_t P1) {
+            FusedArgs fc = f;
+            fc.row_begin = P0;
+            fc.n_brows = P1;
+            launch_fused_mixed(c->form, c->tab.n, c->n_vars, fc, grid, c->stream, false, true);
+            c->launches++;
+          });
       if (cs) return cs;
+    } else {
+      launch_fused_mixed(c->form, c->tab.n, c->n_vars, f, grid, c->stream, true, true);
+      c->launches += 2;
     }
     if (c->perflog) {
       LMG_CUDA(c, cudaEventRecord(e3[1], c->stream));
@@ -812,18 +858,28 @@ lmg_status lmg_assemble(lmg_ctx *c, int32_t precision, double *K, double *F, int
     if (out_on_device || (!K && !F)) return LMG_OK;
     return check_status(c, "assemble");
   }
-  if (!c->h_aff.empty()) {
-    a.n_list = (int64_t)c->h_aff.size();
-    a.list = c->d_aff;
-    launch_elements(c->form, c->tab.n, c->n_vars, true, mixed, a, grid, c->stream);
-    c->launches++;
-  }
-  if (!c->h_gen.empty()) {
-    a.n_list = (int64_t)c->h_gen.size();
-    a.list = c->d_gen;
-    launch_elements(c->form, c->tab.n, c->n_vars, false, mixed, a, grid, c->stream);
-    c->launches++;
-  }
+  // element kernels over the elements [E0, E1) of both lists
+  auto run_elements = [&](int64_t E0, int64_t E1) {
+    int64_t off, cnt;
+    list_slice(c->h_aff, E0, E1, off, cnt);
+    if (cnt) {
+      ElemArgs aa = a;
+      aa.n_list = cnt;
+      aa.list = c->d_aff + off;
+      launch_elements(c->form, c->tab.n, c->n_vars, true, mixed, aa, grid, c->stream);
+      c->launches++;
+    }
+    list_slice(c->h_gen, E0, E1, off, cnt);
+    if (cnt) {
+      ElemArgs aa = a;
+      aa.n_list = cnt;
+      aa.list = c->d_gen + off;
+      launch_elements(c->form, c->tab.n, c->n_vars, false, mixed, aa, grid, c->stream);
+      c->launches++;
+    }
+  };
+  const bool chunked = chunked_output(c, K, out_on_device);
+  if (!chunked) run_elements(0, c->n_elem);
   if (c->perflog) LMG_CUDA(c, cudaEventRecord(e3[1], c->stream));
   GatherArgs g{};
   g.n_dofs = c->n_dofs;
@@ -844,9 +900,8 @@ lmg_status lmg_assemble(lmg_ctx *c, int32_t precision, double *K, double *F, int
   g.constrained = c->d_cons;
   g.K = c->d_K;
   g.F = c->d_F;
-  const bool chunked = chunked_output(c, K, out_on_device);
   if (chunked) {
-    lmg_status cs = rows_with_copy(c, K, [&](int64_t P0, int64_t P1) {
+    lmg_status cs = pipelined_copy(c, K, run_elements, [&](int64_t P0, int64_t P1) {
       GatherArgs gc = g;
       gc.row_begin = P0;
       gc.row_end = P1;

@@ -90,7 +90,8 @@ lmg_status general_plan(lmg_ctx *c) {
     b = have_rows ? c->h_cons_ptr[(size_t)d] : 0;
     e = have_rows ? c->h_cons_ptr[(size_t)d + 1] : 0;
   };
-  const uint8_t *cons = c->h_constrained.empty() ? nullptr : c->h_constrained.data();
+  // the cubic hex kernel masks homogeneous Dirichlet rows itself
+  const uint8_t *cons = (c->h_constrained.empty() || hier3_masks(c)) ? nullptr : c->h_constrained.data();
   // per element: output dof list, its length and where its matrix / vector sit
   std::vector<int64_t> lptr((size_t)E + 1, 0);
   std::vector<int32_t> ldofs;
@@ -302,8 +303,12 @@ lmg_status general_assemble(lmg_ctx *c) {
 }
 
 void general_gather(lmg_ctx *c) {
-  launch_gather_full(c->nnz, c->d_cptr, c->d_coff, c->d_Ebuf, c->d_K, c->n_dofs, c->d_gfptr, c->d_gfoff, c->d_Fbuf,
-                     c->d_F, c->n_sm, c->stream);
+  if (hier3_masks(c))  // cubic hexes write double-float element matrices
+    launch_gather_full_df(c->nnz, c->d_cptr, c->d_coff, reinterpret_cast<const float2 *>(c->d_Ebuf), c->d_K,
+                          c->n_dofs, c->d_gfptr, c->d_gfoff, c->d_Fbuf, c->d_F, c->n_sm, c->stream);
+  else
+    launch_gather_full(c->nnz, c->d_cptr, c->d_coff, c->d_Ebuf, c->d_K, c->n_dofs, c->d_gfptr, c->d_gfoff,
+                       c->d_Fbuf, c->d_F, c->n_sm, c->stream);
   c->launches++;
 }
 

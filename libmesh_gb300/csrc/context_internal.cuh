@@ -44,6 +44,7 @@ struct lmg_ctx {
   int32_t *d_bcol = nullptr, *d_row_ptr = nullptr, *d_col = nullptr;
   int32_t *d_bptr = nullptr, *d_bcontrib = nullptr, *d_fptr = nullptr, *d_fcontrib = nullptr;
   std::vector<int32_t> h_rowptr_blk;      // host copy of row_ptr (block path), for chunked output copies
+  std::vector<int32_t> h_row_pmax;        // prefix maximum of each block row's last contributing element
   cudaStream_t copy_stream = nullptr;     // device-to-host copies overlapped with the insertion
   std::vector<cudaEvent_t> chunk_ev;
   uint8_t *d_relslot = nullptr;  // [E][nb][nb] slot of block (a, b) in block row of a (fused mixed form)
@@ -88,9 +89,11 @@ struct lmg_ctx {
   uint64_t *d_crow = nullptr;
   // cubic HIERARCHIC hexes (hier3.cu): dof lists of 64 per element, general path
   bool hier3 = false;
-  uint16_t *d_h3var = nullptr;       // [n_elem][64] shape variant
-  double *d_h3D = nullptr, *d_h3M = nullptr, *d_h3gd = nullptr;
-  int h3V = 0;
+  int32_t *d_h3batch = nullptr, *d_h3order = nullptr;  // element batches of one orientation pattern
+  float2 *d_h3D = nullptr;           // per-pattern reference tensors, double-float pairs
+  double *d_h3M = nullptr, *d_h3gd = nullptr;
+  int64_t h3_nbatch = 0;
+  int h3_patterns = 0;
   // PerfLog-style stage timing (CUDA events on the context stream)
   bool perflog = false;
   std::vector<cudaEvent_t> ev;       // 3 per logged assemble call
@@ -148,6 +151,7 @@ void hier3_free(lmg_ctx *c);
 lmg_status hier3_form_set(lmg_ctx *c, int32_t form, int32_t q_order, const double *elem_coef,
                           const double *nodal_f);
 void launch_hier3(lmg_ctx *c);
+bool hier3_masks(const lmg_ctx *c);  // Dirichlet rows applied by the element kernel
 void general_free(lmg_ctx *c);             // plan and work buffers
 
 }  // namespace lmg

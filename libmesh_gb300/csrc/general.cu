@@ -24,6 +24,7 @@
 // Constrained rows become e_i^T with -c_ij at their constraining dofs; F' = C^T F.
 #include <cuda_runtime.h>
 
+#include "df.cuh"
 #include "general.cuh"
 #include "../../include/libmesh_gb300.h"
 
@@ -372,6 +373,31 @@ __global__ void k_gather_full(int64_t nnz, const int64_t *__restrict__ cptr, con
   }
 }
 
+// The same gather over element matrices stored as double-float pairs: the
+// contributions of a slot are summed in double-float arithmetic on the FP32
+// pipe and rounded to FP64 once per entry.
+__global__ void k_gather_full_df(int64_t nnz, const int64_t *__restrict__ cptr, const uint32_t *__restrict__ coff,
+                                 const float2 *__restrict__ E, double *__restrict__ K, int64_t n_dofs,
+                                 const int64_t *__restrict__ fptr, const uint32_t *__restrict__ foff,
+                                 const double *__restrict__ Fb, double *__restrict__ F) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < nnz + n_dofs; s += stride) {
+    if (s < nnz) {
+      DF v = {0.f, 0.f};
+      for (int64_t t = cptr[s]; t < cptr[s + 1]; ++t) {
+        const float2 x = E[coff[t]];
+        v = df_add(v, DF{x.x, x.y});
+      }
+      K[s] = df_to_double(v);
+    } else {
+      const int64_t d = s - nnz;
+      double v = 0.0;
+      for (int64_t t = fptr[d]; t < fptr[d + 1]; ++t) v += Fb[foff[t]];
+      F[d] = v;
+    }
+  }
+}
+
 }  // namespace
 
 bool gen_elements_built(int form, int n, int q) {
@@ -413,6 +439,15 @@ void launch_gather_full(int64_t nnz, const int64_t *cptr, const uint32_t *coff, 
   const int64_t blocks = (items + 255) / 256;
   const int g = (int)(blocks < (int64_t)n_sm * 16 ? blocks : (int64_t)n_sm * 16);
   k_gather_full<<<g, 256, 0, s>>>(nnz, cptr, coff, E, K, n_dofs, fptr, foff, Fb, F);
+}
+
+void launch_gather_full_df(int64_t nnz, const int64_t *cptr, const uint32_t *coff, const float2 *E, double *K,
+                           int64_t n_dofs, const int64_t *fptr, const uint32_t *foff, const double *Fb, double *F,
+                           int n_sm, cudaStream_t s) {
+  const int64_t items = nnz + n_dofs;
+  const int64_t blocks = (items + 255) / 256;
+  const int g = (int)(blocks < (int64_t)n_sm * 16 ? blocks : (int64_t)n_sm * 16);
+  k_gather_full_df<<<g, 256, 0, s>>>(nnz, cptr, coff, E, K, n_dofs, fptr, foff, Fb, F);
 }
 
 }  // namespace lmg

@@ -59,5 +59,9 @@ void launch_constrain(const ConsArgs &c, int n_sm, cudaStream_t s);
 void launch_gather_full(int64_t nnz, const int64_t *cptr, const uint32_t *coff, const double *E, double *K,
                         int64_t n_dofs, const int64_t *fptr, const uint32_t *foff, const double *Fb, double *F,
                         int n_sm, cudaStream_t s);
+// element matrices as double-float pairs (cubic hexes without constraint rows)
+void launch_gather_full_df(int64_t nnz, const int64_t *cptr, const uint32_t *coff, const float2 *E, double *K,
+                           int64_t n_dofs, const int64_t *fptr, const uint32_t *foff, const double *Fb, double *F,
+                           int n_sm, cudaStream_t s);
 
 }  // namespace lmg

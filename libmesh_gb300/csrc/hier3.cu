@@ -7,127 +7,166 @@
 //
 // Each element's 64 shapes are variants of the tensor hierarchic basis (which
 // reference coordinate feeds each 1-D factor and with which sign follows from
-// the element's edge and face orientation).  The host tabulates, over the
-// variants that occur, D_k[v][w] (affine reference tensors) and M[v][g]
-// (shape x HEX27 map basis); the kernel forms, per affine element,
-//   K_ij = sum_k A_k D_k[var_i][var_j],  A = coef detJ (G G^T) (6 entries),
-//   F_i  = detJ sum_g M[var_i][g] f_g,
-// and writes the full 64 x 64 matrix into the general path's element buffer,
-// where the constraint kernel and the slot gather take over.  One CTA per
-// element at a time (grid-stride); 256 threads cover the 4096 entries with
-// coalesced stores; the variant tables stay in L2.
+// the element's edge and face orientation).  The host tabulates the affine
+// reference tensors per orientation pattern (the element's 64 variants) in
+// the element's own shape order, D_k[i][j], and the load table M[i][g]
+// (shape x HEX27 map basis), and groups the elements by pattern into batches
+// of at most eight.  Per batch one CTA forms, for its elements,
+//   K_ij = sum_k A_k D_k[i][j],  A = coef detJ (G G^T) (6 entries),
+//   F_i  = detJ sum_g M[i][g] f_g,
+// reading every table entry once for the whole batch, and writes the full
+// 64 x 64 matrices into the general path's element buffer.  The contraction
+// runs in double-float arithmetic on the FP32 pipe (the tables are stored as
+// hi + lo pairs; GB300's FP64 rate is 1/64 of FP32).  Without
+// constraint rows the homogeneous Dirichlet rows are applied here (zero row
+// and column, 1 on the diagonal, zero load: constrain_element_matrix_and_vector
+// with empty rows) and the constraint kernel is skipped; with rows the
+// constraint kernel applies C^T K C.  In the masked case the element
+// matrices stay double-float pairs and the gather sums them in double-float
+// (k_gather_full_df), rounding each CSR entry to FP64 once.
 #include <cuda_runtime.h>
 
 #include <string>
 #include <vector>
 
 #include "context_internal.cuh"
+#include "df.cuh"
 #include "general.cuh"
 
 namespace lmg {
 
 namespace {
 
-constexpr int H3N = 64, H3T = 256;
+constexpr int H3N = 64, H3T = 256, H3B = 8;
 
 struct H3Args {
-  int64_t n_elem;
+  int64_t n_batch;
+  const int32_t *batch;     // [n_batch][3]: pattern, first index in order, count
+  const int32_t *order;     // element ids sorted by pattern
   const double *xyz;
   const int32_t *conn;      // [n_elem][27]
   const double *coef;       // [n_elem] or null
   const double *nodal_f;    // [n_nodes] or null
-  const uint16_t *var;      // [n_elem][64]
-  const double *D;          // [V][V][6]
-  const double *M;          // [V][27]
+  const uint64_t *cmask;    // [n_elem] constrained local dofs, or null (no mask)
+  const float2 *D;          // [P][6][64*64] double-float pairs
+  const double *M;          // [P][64][27]
   const double *gd0;        // [27][3]
-  int V;
-  double *Kraw;             // [n_elem][64][64]
+  double *Kraw;             // [n_elem][64][64] (double-float pairs when the kernel masks)
   double *Fraw;             // [n_elem][64]
   int *status;
   unsigned long long *bad_elem;
 };
 
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// DFOUT: element matrices stay double-float pairs for the double-float gather.
+template <bool DFOUT>
 __global__ void __launch_bounds__(H3T) k_elem_hier3(H3Args a) {
-  __shared__ double sJ[27][9];
-  __shared__ double sA[8];   // A_0..A_5, detJ
-  __shared__ double sf[27];
-  __shared__ uint16_t sv[H3N];
-  const int t = threadIdx.x;
-  for (int64_t e = blockIdx.x; e < a.n_elem; e += gridDim.x) {
-    // compute_affine_map: J = sum_g X_g (x) dphi_g(qp 0), per-node partials reduced below
-    if (t < 27) {
-      const int64_t nd = a.conn[e * 27 + t];
-      const double x[3] = {a.xyz[3 * nd], a.xyz[3 * nd + 1], a.xyz[3 * nd + 2]};
-#pragma unroll
-      for (int m = 0; m < 3; ++m)
-#pragma unroll
-        for (int d = 0; d < 3; ++d) sJ[t][3 * m + d] = x[d] * a.gd0[3 * t + m];
-      sf[t] = a.nodal_f ? a.nodal_f[nd] : 0.0;
-    }
-    if (t < H3N) sv[t] = a.var[e * H3N + t];
+  __shared__ double sA[H3B][8];   // A_0..A_5, detJ
+  __shared__ DF sA2[H3B][6];
+  __shared__ double sf[H3B][27];
+  __shared__ uint64_t sm[H3B];
+  __shared__ int32_t se[H3B];
+  const int t = threadIdx.x, w = t >> 5, lane = t & 31;
+  for (int64_t bi = blockIdx.x; bi < a.n_batch; bi += gridDim.x) {
+    const int p = a.batch[3 * bi], first = a.batch[3 * bi + 1], cnt = a.batch[3 * bi + 2];
     __syncthreads();
-    if (t == 0) {
+    if (w < cnt) {  // warp w: geometry of the batch's element w (compute_affine_map)
+      const int32_t e = a.order[first + w];
       double jp[9];
 #pragma unroll
-      for (int k = 0; k < 9; ++k) {
-        double s = 0.0;
-        for (int g = 0; g < 27; ++g) s += sJ[g][k];
-        jp[k] = s;
+      for (int k = 0; k < 9; ++k) jp[k] = 0.0;
+      if (lane < 27) {
+        const int64_t nd = a.conn[(int64_t)e * 27 + lane];
+        const double x[3] = {a.xyz[3 * nd], a.xyz[3 * nd + 1], a.xyz[3 * nd + 2]};
+#pragma unroll
+        for (int m = 0; m < 3; ++m)
+#pragma unroll
+          for (int d = 0; d < 3; ++d) jp[3 * m + d] = x[d] * a.gd0[3 * lane + m];
+        sf[w][lane] = a.nodal_f ? a.nodal_f[nd] : 0.0;
       }
-      // jp[3m+d] = dx_d/dxi_m; G[3m+d] = dxi_m/dx_d (fe_map.C:1046-1068)
-      const double c0 = jp[4] * jp[8] - jp[5] * jp[7], c1 = jp[5] * jp[6] - jp[3] * jp[8],
-                   c2 = jp[3] * jp[7] - jp[4] * jp[6];
-      const double det = jp[0] * c0 + jp[1] * c1 + jp[2] * c2;
-      const double inv = 1.0 / det;
-      double G[9];
-      G[0] = c0 * inv;
-      G[1] = c1 * inv;
-      G[2] = c2 * inv;
-      G[3] = (jp[2] * jp[7] - jp[1] * jp[8]) * inv;
-      G[4] = (jp[0] * jp[8] - jp[2] * jp[6]) * inv;
-      G[5] = (jp[1] * jp[6] - jp[0] * jp[7]) * inv;
-      G[6] = (jp[1] * jp[5] - jp[2] * jp[4]) * inv;
-      G[7] = (jp[2] * jp[3] - jp[0] * jp[5]) * inv;
-      G[8] = (jp[0] * jp[4] - jp[1] * jp[3]) * inv;
-      if (!(det > 0.0)) {
-        atomicCAS(a.status, 0, LMG_ERR_DEGENERATE);
-        atomicMin(a.bad_elem, (unsigned long long)e);
+#pragma unroll
+      for (int k = 0; k < 9; ++k) jp[k] = warp_sum(jp[k]);
+      if (lane == 0) {
+        // jp[3m+d] = dx_d/dxi_m; G[3m+d] = dxi_m/dx_d (fe_map.C:1046-1068)
+        const double c0 = jp[4] * jp[8] - jp[5] * jp[7], c1 = jp[5] * jp[6] - jp[3] * jp[8],
+                     c2 = jp[3] * jp[7] - jp[4] * jp[6];
+        const double det = jp[0] * c0 + jp[1] * c1 + jp[2] * c2;
+        const double inv = 1.0 / det;
+        double G[9];
+        G[0] = c0 * inv;
+        G[1] = c1 * inv;
+        G[2] = c2 * inv;
+        G[3] = (jp[2] * jp[7] - jp[1] * jp[8]) * inv;
+        G[4] = (jp[0] * jp[8] - jp[2] * jp[6]) * inv;
+        G[5] = (jp[1] * jp[6] - jp[0] * jp[7]) * inv;
+        G[6] = (jp[1] * jp[5] - jp[2] * jp[4]) * inv;
+        G[7] = (jp[2] * jp[3] - jp[0] * jp[5]) * inv;
+        G[8] = (jp[0] * jp[4] - jp[1] * jp[3]) * inv;
+        if (!(det > 0.0)) {
+          atomicCAS(a.status, 0, LMG_ERR_DEGENERATE);
+          atomicMin(a.bad_elem, (unsigned long long)e);
+        }
+        const double kap = (a.coef ? a.coef[e] : 1.0) * det;
+        sA[w][0] = kap * (G[0] * G[0] + G[1] * G[1] + G[2] * G[2]);
+        sA[w][1] = kap * (G[3] * G[3] + G[4] * G[4] + G[5] * G[5]);
+        sA[w][2] = kap * (G[6] * G[6] + G[7] * G[7] + G[8] * G[8]);
+        sA[w][3] = kap * (G[0] * G[3] + G[1] * G[4] + G[2] * G[5]);
+        sA[w][4] = kap * (G[0] * G[6] + G[1] * G[7] + G[2] * G[8]);
+        sA[w][5] = kap * (G[3] * G[6] + G[4] * G[7] + G[5] * G[8]);
+        sA[w][6] = det;
+#pragma unroll
+        for (int k = 0; k < 6; ++k) sA2[w][k] = df_split(sA[w][k]);
+        sm[w] = a.cmask ? a.cmask[e] : 0ull;
+        se[w] = e;
       }
-      const double kap = (a.coef ? a.coef[e] : 1.0) * det;
-      sA[0] = kap * (G[0] * G[0] + G[1] * G[1] + G[2] * G[2]);
-      sA[1] = kap * (G[3] * G[3] + G[4] * G[4] + G[5] * G[5]);
-      sA[2] = kap * (G[6] * G[6] + G[7] * G[7] + G[8] * G[8]);
-      sA[3] = kap * (G[0] * G[3] + G[1] * G[4] + G[2] * G[5]);
-      sA[4] = kap * (G[0] * G[6] + G[1] * G[7] + G[2] * G[8]);
-      sA[5] = kap * (G[3] * G[6] + G[4] * G[7] + G[5] * G[8]);
-      sA[6] = det;
     }
     __syncthreads();
-    const double A0 = sA[0], A1 = sA[1], A2 = sA[2], A3 = sA[3], A4 = sA[4], A5 = sA[5];
-    double *Ko = a.Kraw + e * (H3N * H3N);
+    // K_ij = sum_k A_k D_k[i][j] in double-float arithmetic (FP32 pipe)
+    const float2 *Dp = a.D + (size_t)p * 6 * (H3N * H3N);
     for (int idx = t; idx < H3N * H3N; idx += H3T) {
       const int i = idx >> 6, j = idx & 63;
-      const double *d = a.D + ((size_t)sv[i] * a.V + sv[j]) * 6;
-      Ko[idx] = A0 * d[0] + A1 * d[1] + A2 * d[2] + A3 * d[3] + A4 * d[4] + A5 * d[5];
+      DF d[6];
+#pragma unroll
+      for (int k = 0; k < 6; ++k) {
+        const float2 x = Dp[k * 4096 + idx];
+        d[k] = DF{x.x, x.y};
+      }
+      for (int b = 0; b < cnt; ++b) {
+        DF v = {0.f, 0.f};
+#pragma unroll
+        for (int k = 0; k < 6; ++k) v = df_fma_lazy(v, sA2[b][k], d[k]);
+        v = df_norm(v);
+        if (((sm[b] >> i) | (sm[b] >> j)) & 1ull) v = DF{(i == j) ? 1.f : 0.f, 0.f};
+        if (DFOUT)
+          reinterpret_cast<float2 *>(a.Kraw)[(int64_t)se[b] * (H3N * H3N) + idx] = make_float2(v.hi, v.lo);
+        else
+          a.Kraw[(int64_t)se[b] * (H3N * H3N) + idx] = df_to_double(v);
+      }
     }
-    if (t < H3N) {
-      const double *mv = a.M + (size_t)sv[t] * 27;
+    const double *Mp = a.M + (size_t)p * H3N * 27;
+    for (int idx = t; idx < H3N * cnt; idx += H3T) {
+      const int b = idx >> 6, i = idx & 63;
       double s = 0.0;
-      for (int g = 0; g < 27; ++g) s += mv[g] * sf[g];
-      a.Fraw[e * H3N + t] = sA[6] * s;
+      for (int g = 0; g < 27; ++g) s += Mp[i * 27 + g] * sf[b][g];
+      a.Fraw[(int64_t)se[b] * H3N + i] = ((sm[b] >> i) & 1ull) ? 0.0 : sA[b][6] * s;
     }
-    __syncthreads();
   }
 }
 
 }  // namespace
 
 void hier3_free(lmg_ctx *c) {
-  dfree(c->d_h3var);
+  dfree(c->d_h3batch);
+  dfree(c->d_h3order);
   dfree(c->d_h3D);
   dfree(c->d_h3M);
   dfree(c->d_h3gd);
-  c->h3V = 0;
+  c->h3_nbatch = 0;
 }
 
 // lmg_form_set for FEType{THIRD, HIERARCHIC} on HEX27.
@@ -141,11 +180,18 @@ lmg_status hier3_form_set(lmg_ctx *c, int32_t form, int32_t q_order, const doubl
   std::string err = build_hier3_tables(h, q_order, c->n_elem, c->h_xyz.data(), c->h_conn.data());
   if (!err.empty()) return fail(c, LMG_ERR_UNSUPPORTED, "form_set: " + err);
   hier3_free(c);
-  LMG_CUDA(c, dupload(c, c->d_h3var, h.var.data(), h.var.size()));
-  LMG_CUDA(c, dupload(c, c->d_h3D, h.D.data(), h.D.size()));
-  LMG_CUDA(c, dupload(c, c->d_h3M, h.M.data(), h.M.size()));
+  LMG_CUDA(c, dupload(c, c->d_h3batch, h.batch.data(), h.batch.size()));
+  LMG_CUDA(c, dupload(c, c->d_h3order, h.order.data(), h.order.size()));
+  std::vector<float2> dp(h.Dp.size());
+  for (size_t i = 0; i < dp.size(); ++i) {
+    const DF x = df_split(h.Dp[i]);
+    dp[i] = make_float2(x.hi, x.lo);
+  }
+  LMG_CUDA(c, dupload(c, c->d_h3D, dp.data(), dp.size()));
+  LMG_CUDA(c, dupload(c, c->d_h3M, h.Mp.data(), h.Mp.size()));
   LMG_CUDA(c, dupload(c, c->d_h3gd, h.gd0.data(), h.gd0.size()));
-  c->h3V = h.V;
+  c->h3_nbatch = (int64_t)h.batch.size() / 3;
+  c->h3_patterns = h.P;
   FETables t;
   t.elem_type = LMG_HEX27;
   t.fe_order = 3;
@@ -172,25 +218,30 @@ lmg_status hier3_form_set(lmg_ctx *c, int32_t form, int32_t q_order, const doubl
   return LMG_OK;
 }
 
+bool hier3_masks(const lmg_ctx *c) { return c->hier3 && !c->has_rows; }
+
 void launch_hier3(lmg_ctx *c) {
   H3Args a{};
-  a.n_elem = c->n_elem;
+  a.n_batch = c->h3_nbatch;
+  a.batch = c->d_h3batch;
+  a.order = c->d_h3order;
   a.xyz = c->d_xyz;
   a.conn = c->d_conn;
   a.coef = c->d_coef;
   a.nodal_f = c->d_f;
-  a.var = c->d_h3var;
+  a.cmask = hier3_masks(c) ? c->d_cmask : nullptr;
   a.D = c->d_h3D;
   a.M = c->d_h3M;
   a.gd0 = c->d_h3gd;
-  a.V = c->h3V;
   a.Kraw = c->d_Ebuf;
   a.Fraw = c->d_Fbuf;
   a.status = c->d_status;
   a.bad_elem = c->d_bad;
   const int64_t want = (int64_t)c->n_sm * 8;
-  const int grid = (int)(c->n_elem < want ? c->n_elem : want);
-  if (grid > 0) k_elem_hier3<<<grid, H3T, 0, c->stream>>>(a);
+  const int grid = (int)(a.n_batch < want ? a.n_batch : want);
+  if (grid <= 0) return;
+  if (a.cmask) k_elem_hier3<true><<<grid, H3T, 0, c->stream>>>(a);
+  else k_elem_hier3<false><<<grid, H3T, 0, c->stream>>>(a);
 }
 
 }  // namespace lmg

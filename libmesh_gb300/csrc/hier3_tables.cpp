@@ -16,7 +16,9 @@
 //                                                     off-diagonal pairs summed)
 //   M[v][g]   = sum_q w_q phi_v(q) phi^geo_g(q)     (load through the HEX27 map basis)
 // so that the device forms K_ij = sum_k A_k D_k[var_i][var_j] per element.
+#include <algorithm>
 #include <cmath>
+#include <map>
 #include <unordered_map>
 
 #include "lmg_internal.h"
@@ -211,6 +213,45 @@ std::string build_hier3_tables(Hier3Tables &h, int q_order, int64_t n_elem, cons
       for (int q = 0; q < Q; ++q) s += geo.qw[(size_t)q] * phi[(size_t)v * Q + q] * geo.gphi[(size_t)q * 27 + g];
       h.M[(size_t)v * 27 + g] = s;
     }
+  // patterns: distinct 64-variant vectors (one on build_cube meshes, where
+  // every element has the same orientation)
+  std::map<std::vector<uint16_t>, int> pat;
+  std::vector<int32_t> pid((size_t)n_elem);
+  std::vector<const uint16_t *> first;
+  for (int64_t e = 0; e < n_elem; ++e) {
+    std::vector<uint16_t> key(h.var.begin() + e * 64, h.var.begin() + (e + 1) * 64);
+    auto it = pat.find(key);
+    if (it == pat.end()) {
+      it = pat.emplace(std::move(key), (int)first.size()).first;
+      first.push_back(&h.var[(size_t)e * 64]);
+    }
+    pid[(size_t)e] = it->second;
+  }
+  h.P = (int)first.size();
+  if ((size_t)h.P * 6 * 4096 * sizeof(double) > ((size_t)2 << 30)) return "too many orientation patterns";
+  h.Dp.resize((size_t)h.P * 6 * 4096);
+  h.Mp.resize((size_t)h.P * 64 * 27);
+  for (int p = 0; p < h.P; ++p) {
+    const uint16_t *vr = first[(size_t)p];
+    for (int k = 0; k < 6; ++k)
+      for (int i = 0; i < 64; ++i)
+        for (int j = 0; j < 64; ++j)
+          h.Dp[((size_t)p * 6 + k) * 4096 + i * 64 + j] = h.D[((size_t)vr[i] * V + vr[j]) * 6 + k];
+    for (int i = 0; i < 64; ++i)
+      for (int g = 0; g < 27; ++g) h.Mp[((size_t)p * 64 + i) * 27 + g] = h.M[(size_t)vr[i] * 27 + g];
+  }
+  h.order.resize((size_t)n_elem);
+  for (int64_t e = 0; e < n_elem; ++e) h.order[(size_t)e] = (int32_t)e;
+  std::stable_sort(h.order.begin(), h.order.end(), [&](int32_t a, int32_t b) { return pid[(size_t)a] < pid[(size_t)b]; });
+  for (int64_t i = 0; i < n_elem;) {
+    const int p = pid[(size_t)h.order[(size_t)i]];
+    int64_t j = i;
+    while (j < n_elem && j - i < 8 && pid[(size_t)h.order[(size_t)j]] == p) ++j;
+    h.batch.push_back(p);
+    h.batch.push_back((int32_t)i);
+    h.batch.push_back((int32_t)(j - i));
+    i = j;
+  }
   return "";
 }
 

@@ -121,6 +121,14 @@ struct Hier3Tables {
   std::vector<double> D;         // [V][V][6] affine reference tensors
   std::vector<double> M;         // [V][27]   sum_q w phi_v phi^geo_g
   std::vector<double> gd0;       // [27][3]   HEX27 map derivatives at qp 0
+  // Elements grouped by their 64-variant pattern: per pattern the tensors in
+  // the element's own shape order, the elements sorted by pattern, and
+  // batches of at most 8 elements of one pattern.
+  int P = 0;
+  std::vector<double> Dp;        // [P][6][64*64]
+  std::vector<double> Mp;        // [P][64][27]
+  std::vector<int32_t> order;    // [n_elem] element ids sorted by pattern (stable)
+  std::vector<int32_t> batch;    // [n_batch][3]: pattern, first index in order, count
 };
 std::string build_hier3_tables(Hier3Tables &h, int q_order, int64_t n_elem, const double *xyz, const int32_t *conn);
 

@@ -1,5 +1,6 @@
-"""Batched assembly (lmg_batch_*): systems of different element types, forms
-and FE families tuned and replayed as one CUDA graph give the same K and F
+"""Batched assembly (lmg_batch_*): systems of different element types (hexes,
+tets, prisms), forms and FE families (HIERARCHIC up to cubic) tuned and
+replayed as one CUDA graph give the same K and F
 as each system assembled on its own, bit for bit, over repeated replays and
 after an input update."""
 import numpy as np
@@ -22,6 +23,14 @@ def members():
     out.append((lm.GpuAssembly(lm.ADVDIFF, 2, 5, elem_coef=k, nodal_f=f, params=cd_params()), m, dm))
     m, dm, k, f = make_problem(4, lm.HEX27, 1, lm.POISSON, seed=4)
     out.append((lm.GpuAssembly(lm.POISSON, 2, 5, elem_coef=k, nodal_f=f), m, dm))
+    m = lm.Mesh.build_cube(3, 3, 3, lm.HEX27)
+    dm = lm.DofMap(m, 1, fe_order=3 | lm.HIERARCHIC)
+    dm.add_dirichlet_boundary([0, 1, 2, 3, 4, 5], [0])
+    rng = np.random.default_rng(5)
+    out.append((lm.GpuAssembly(lm.POISSON, 3 | lm.HIERARCHIC, 7, elem_coef=rng.uniform(0.1, 10, m.n_elem),
+                               nodal_f=rng.uniform(-1, 1, (m.n_nodes, 1))), m, dm))
+    m, dm, k, f = make_problem(4, lm.PRISM6, 1, lm.POISSON, jitter=0.2, seed=6)
+    out.append((lm.GpuAssembly(lm.POISSON, 1 | lm.HIERARCHIC, 3, elem_coef=k, nodal_f=f), m, dm))
     for a, m, dm in out:
         a.init(m, dm)
     return out
