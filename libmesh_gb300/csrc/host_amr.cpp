@@ -68,13 +68,62 @@ struct LatKey {
   int64_t x, y, z;
   bool operator==(const LatKey &o) const { return x == o.x && y == o.y && z == o.z; }
 };
-struct LatHash {
-  size_t operator()(const LatKey &k) const {
-    uint64_t h = (uint64_t)k.x * 0x9E3779B97F4A7C15ull;
-    h ^= (uint64_t)k.y * 0xC2B2AE3D27D4EB4Full + (h << 6) + (h >> 2);
-    h ^= (uint64_t)k.z * 0x165667B19E3779F9ull + (h << 6) + (h >> 2);
-    return (size_t)h;
+// Node lookup by lattice point: open addressing over the packed point
+// (21 bits per coordinate; init_tree bounds the grid so that every lattice
+// coordinate fits), linear probing, power-of-two capacity kept under half full.
+class LatMap {
+ public:
+  explicit LatMap(size_t expect) {
+    size_t cap = 16;
+    while (cap < 2 * expect + 16) cap <<= 1;
+    keys_.assign(cap, EMPTY);
+    vals_.assign(cap, -1);
   }
+  // id of point k, or -1
+  int32_t find(const LatKey &k) const {
+    const uint64_t key = pack(k);
+    for (size_t i = slot(key);; i = (i + 1) & (keys_.size() - 1)) {
+      if (keys_[i] == key) return vals_[i];
+      if (keys_[i] == EMPTY) return -1;
+    }
+  }
+  void insert(const LatKey &k, int32_t id) {
+    if (2 * (n_ + 1) > keys_.size()) grow();
+    place(pack(k), id);
+  }
+
+ private:
+  static constexpr uint64_t EMPTY = ~0ull;
+  static uint64_t pack(const LatKey &k) {
+    return (uint64_t)k.x | ((uint64_t)k.y << 21) | ((uint64_t)k.z << 42);
+  }
+  size_t slot(uint64_t key) const {  // splitmix64 finaliser
+    uint64_t h = key + 0x9E3779B97F4A7C15ull;
+    h = (h ^ (h >> 30)) * 0xBF58476D1CE4E5B9ull;
+    h = (h ^ (h >> 27)) * 0x94D049BB133111EBull;
+    return (size_t)(h ^ (h >> 31)) & (keys_.size() - 1);
+  }
+  void place(uint64_t key, int32_t id) {
+    size_t i = slot(key);
+    while (keys_[i] != EMPTY && keys_[i] != key) i = (i + 1) & (keys_.size() - 1);
+    if (keys_[i] == EMPTY) ++n_;
+    keys_[i] = key;
+    vals_[i] = id;
+  }
+  void grow() {
+    std::vector<uint64_t> k;
+    std::vector<int32_t> v;
+    k.swap(keys_);
+    v.swap(vals_);
+    keys_.assign(k.size() * 2, EMPTY);
+    vals_.assign(k.size() * 2, -1);
+    n_ = 0;
+    for (size_t i = 0; i < k.size(); ++i)
+      if (k[i] != EMPTY) place(k[i], v[i]);
+  }
+  std::vector<uint64_t> keys_;
+  std::vector<int32_t> vals_;
+  size_t n_ = 0;
 };
 
 int64_t elem_size(const AmrTree &t, int32_t e) { return AMR_S0 >> t.level[(size_t)e]; }
@@ -192,7 +241,7 @@ void finish(HostMesh &m) {
   }
 }
 
-void refine_elem(HostMesh &m, int32_t e, std::unordered_map<LatKey, int32_t, LatHash> &nodes) {
+void refine_elem(HostMesh &m, int32_t e, LatMap &nodes) {
   AmrTree &t = m.amr;
   const int npe = m.npe, order = (npe == 27) ? 2 : 1;
   const int64_t S = elem_size(t, e), Sc = S / 2;
@@ -213,11 +262,8 @@ void refine_elem(HostMesh &m, int32_t e, std::unordered_map<LatKey, int32_t, Lat
       int o[3];
       node_offset(npe, a, o);
       LatKey k{oc[0] + o[0] * (Sc / 2), oc[1] + o[1] * (Sc / 2), oc[2] + o[2] * (Sc / 2)};
-      auto it = nodes.find(k);
-      int32_t id;
-      if (it != nodes.end()) {
-        id = it->second;
-      } else {
+      int32_t id = nodes.find(k);
+      if (id < 0) {
         // embedding weights: tensor product of 1-D shapes at the child node's
         // parent-reference coordinates, summed over parent nodes in order
         const int64_t L[3] = {k.x, k.y, k.z};
@@ -239,7 +285,7 @@ void refine_elem(HostMesh &m, int32_t e, std::unordered_map<LatKey, int32_t, Lat
         t.node_lat.push_back(k.x);
         t.node_lat.push_back(k.y);
         t.node_lat.push_back(k.z);
-        nodes.emplace(k, id);
+        nodes.insert(k, id);
       }
       t.conn.push_back(id);
     }
@@ -283,10 +329,9 @@ std::string amr_refine(HostMesh &m, int cycles, double fraction, uint64_t seed) 
     }
     for (int32_t e : act)
       if (flag[(size_t)e] && t.level[(size_t)e] >= AMR_MAX_LEVEL) return "refine: maximum level reached";
-    std::unordered_map<LatKey, int32_t, LatHash> nodes;
-    nodes.reserve((size_t)m.n_nodes() * 2);
+    LatMap nodes((size_t)m.n_nodes() * 2);
     for (int64_t n = 0; n < m.n_nodes(); ++n)
-      nodes.emplace(LatKey{t.node_lat[3 * n], t.node_lat[3 * n + 1], t.node_lat[3 * n + 2]}, (int32_t)n);
+      nodes.insert(LatKey{t.node_lat[3 * n], t.node_lat[3 * n + 1], t.node_lat[3 * n + 2]}, (int32_t)n);
     for (int32_t e : act)
       if (flag[(size_t)e]) refine_elem(m, e, nodes);
     finish(m);
@@ -309,9 +354,22 @@ typedef std::map<int32_t, double> Row;
 
 }  // namespace
 
+// Rows keyed by dof in a dense table: the same ascending order and lookups as
+// the reference's std::map<dof_id_type, DofConstraintRow>, without the tree.
+struct RowTable {
+  std::vector<Row> row;
+  std::vector<uint8_t> has;
+  explicit RowTable(int64_t n) : row((size_t)n), has((size_t)n, 0) {}
+  bool count(int32_t d) const { return d >= 0 && (size_t)d < has.size() && has[(size_t)d]; }
+  Row &operator[](int32_t d) {
+    has[(size_t)d] = 1;
+    return row[(size_t)d];
+  }
+};
+
 std::string amr_constraint_rows(const HostMesh &m, int n_vars, const int32_t *elem_dofs, int64_t n_dofs,
                                 const uint8_t *dirichlet, ConstraintRows &out) {
-  std::map<int32_t, Row> rows;
+  RowTable rows(n_dofs);
   const int npe = m.npe, nl = npe * n_vars;
   const int64_t E = m.n_elem();
   if (m.amr.on) {
@@ -355,6 +413,7 @@ std::string amr_constraint_rows(const HostMesh &m, int n_vars, const int32_t *el
             bool self = false;
             for (int j = 0; j < ns; ++j) self |= (pd[j] == my_dof);
             if (self || rows.count(my_dof)) continue;
+            if (my_dof < 0 || my_dof >= n_dofs) return "constraints: dof out of range";
             const int64_t *Lp = &t.node_lat[3 * (size_t)my_node];
             int64_t pu = 0, pw = 0;
             for (int d = 0; d < 3; ++d) {
@@ -377,7 +436,8 @@ std::string amr_constraint_rows(const HostMesh &m, int n_vars, const int32_t *el
   // process_constraints: substitute constrained dofs inside rows until every
   // row refers to free dofs only (sweeps over the ascending set of unexpanded rows)
   std::set<int32_t> unexpanded;
-  for (const auto &r : rows) unexpanded.insert(r.first);
+  for (int64_t d = 0; d < n_dofs; ++d)
+    if (rows.has[(size_t)d]) unexpanded.insert(unexpanded.end(), (int32_t)d);
   while (!unexpanded.empty())
     for (auto i = unexpanded.begin(); i != unexpanded.end();) {
       Row &row = rows[*i];
@@ -399,10 +459,10 @@ std::string amr_constraint_rows(const HostMesh &m, int n_vars, const int32_t *el
   out.ptr.assign(1, 0);
   out.col.clear();
   out.val.clear();
-  for (const auto &r : rows) {
-    if (r.first < 0 || r.first >= n_dofs) return "constraints: dof out of range";
-    out.dofs.push_back(r.first);
-    for (const auto &item : r.second) {
+  for (int64_t d = 0; d < n_dofs; ++d) {
+    if (!rows.has[(size_t)d]) continue;
+    out.dofs.push_back((int32_t)d);
+    for (const auto &item : rows.row[(size_t)d]) {
       out.col.push_back(item.first);
       out.val.push_back(item.second);
     }
@@ -417,6 +477,7 @@ extern "C" {
 
 lmg_status lmg_mesh_refine(lmg_mesh *mesh, int32_t cycles, double fraction, uint64_t seed) {
   if (!mesh) return LMG_ERR_ARG;
+  mesh->rows_valid = false;
   try {
     const std::string err = lmg::amr_refine(mesh->m, cycles, fraction, seed);
     return err.empty() ? LMG_OK : LMG_ERR_ARG;
@@ -453,9 +514,24 @@ lmg_status lmg_constraint_rows(const lmg_mesh *mesh, int32_t n_vars, const int32
                                int32_t *cons_col, double *cons_val, int64_t cap) {
   if (!mesh || n_vars <= 0 || !elem_dofs || n_dofs <= 0 || !cons_ptr) return LMG_ERR_ARG;
   try {
-    lmg::ConstraintRows r;
-    const std::string err = lmg::amr_constraint_rows(mesh->m, n_vars, elem_dofs, n_dofs, dirichlet, r);
-    if (!err.empty()) return LMG_ERR_BOUNDS;
+    // The count call and the fill call of a caller see the same inputs: keep
+    // the rows of the last call, keyed by a checksum of the inputs.
+    uint64_t key = 1469598103934665603ull;
+    auto mix = [&](uint64_t x) { key = (key ^ x) * 1099511628211ull; };
+    mix((uint64_t)n_vars);
+    mix((uint64_t)n_dofs);
+    const int64_t nl = (int64_t)mesh->m.npe * n_vars;
+    for (int64_t i = 0; i < mesh->m.n_elem() * nl; ++i) mix((uint64_t)(uint32_t)elem_dofs[i]);
+    for (int64_t d = 0; d < n_dofs; ++d) mix(dirichlet ? dirichlet[d] : 0);
+    lmg_mesh *mm = const_cast<lmg_mesh *>(mesh);
+    if (!mm->rows_valid || mm->rows_key != key) {
+      mm->rows_valid = false;
+      const std::string err = lmg::amr_constraint_rows(mesh->m, n_vars, elem_dofs, n_dofs, dirichlet, mm->rows);
+      if (!err.empty()) return LMG_ERR_BOUNDS;
+      mm->rows_key = key;
+      mm->rows_valid = true;
+    }
+    const lmg::ConstraintRows &r = mm->rows;
     std::vector<int64_t> len((size_t)n_dofs, 0);
     for (size_t i = 0; i < r.dofs.size(); ++i) len[(size_t)r.dofs[i]] = r.ptr[i + 1] - r.ptr[i];
     cons_ptr[0] = 0;

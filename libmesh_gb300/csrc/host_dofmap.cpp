@@ -83,69 +83,116 @@ static void build_var_graph(int64_t n_elem, const std::vector<int64_t> &eptr, co
   }
   if (n_threads < 1) n_threads = 1;
   std::vector<int64_t> deg((size_t)n_rows, 0);
-  auto row_cols = [&](int64_t r, std::vector<int32_t> &buf) {
+  // columns of row r: the union of its elements' dof lists, deduplicated with
+  // a per-thread stamp array (last row that saw each dof), then sorted
+  auto row_cols = [&](int64_t r, std::vector<int32_t> &buf, std::vector<int64_t> &stamp) {
     buf.clear();
     for (int64_t k = rptr[(size_t)r]; k < rptr[(size_t)r + 1]; ++k) {
       const int64_t e = relem[(size_t)k];
-      buf.insert(buf.end(), elist.begin() + eptr[(size_t)e], elist.begin() + eptr[(size_t)e + 1]);
+      for (int64_t j = eptr[(size_t)e]; j < eptr[(size_t)e + 1]; ++j) {
+        const int32_t d = elist[(size_t)j];
+        if (stamp[(size_t)d] != r) {
+          stamp[(size_t)d] = r;
+          buf.push_back(d);
+        }
+      }
     }
     std::sort(buf.begin(), buf.end());
-    buf.erase(std::unique(buf.begin(), buf.end()), buf.end());
   };
-  auto run = [&](auto &&fn) {
+  // rows in chunks; each thread keeps its chunks' columns until the row
+  // pointer is known, then copies them into place
+  const int64_t CH = 4096, n_ch = (n_rows + CH - 1) / CH;
+  std::vector<std::vector<int32_t>> chunk_cols((size_t)n_ch);
+  {
     std::atomic<int64_t> next{0};
     std::vector<std::thread> th;
     for (int t = 0; t < n_threads; ++t)
       th.emplace_back([&]() {
         std::vector<int32_t> buf;
+        std::vector<int64_t> stamp((size_t)n_rows, -1);
         for (;;) {
-          const int64_t s0 = next.fetch_add(4096);
-          if (s0 >= n_rows) break;
-          const int64_t s1 = std::min(n_rows, s0 + 4096);
-          for (int64_t r = s0; r < s1; ++r) fn(r, buf);
+          const int64_t c = next.fetch_add(1);
+          if (c >= n_ch) break;
+          std::vector<int32_t> &out = chunk_cols[(size_t)c];
+          for (int64_t r = c * CH; r < std::min(n_rows, (c + 1) * CH); ++r) {
+            row_cols(r, buf, stamp);
+            deg[(size_t)r] = (int64_t)buf.size();
+            out.insert(out.end(), buf.begin(), buf.end());
+          }
         }
       });
     for (auto &t : th) t.join();
-  };
-  run([&](int64_t r, std::vector<int32_t> &buf) {
-    row_cols(r, buf);
-    deg[(size_t)r] = (int64_t)buf.size();
-  });
+  }
   row_ptr.assign((size_t)n_rows + 1, 0);
   for (int64_t r = 0; r < n_rows; ++r) row_ptr[(size_t)r + 1] = row_ptr[(size_t)r] + deg[(size_t)r];
   cols.resize((size_t)row_ptr[(size_t)n_rows]);
-  run([&](int64_t r, std::vector<int32_t> &buf) {
-    row_cols(r, buf);
-    std::copy(buf.begin(), buf.end(), cols.begin() + row_ptr[(size_t)r]);
-  });
+  {
+    std::atomic<int64_t> next{0};
+    std::vector<std::thread> th;
+    for (int t = 0; t < n_threads; ++t)
+      th.emplace_back([&]() {
+        for (;;) {
+          const int64_t c = next.fetch_add(1);
+          if (c >= n_ch) break;
+          std::vector<int32_t> &v = chunk_cols[(size_t)c];
+          std::copy(v.begin(), v.end(), cols.begin() + row_ptr[(size_t)(c * CH)]);
+          std::vector<int32_t>().swap(v);
+        }
+      });
+    for (auto &t : th) t.join();
+  }
 }
 
 void build_constrained_graph(int64_t n_elem, int nl, const int32_t *ed, int64_t n_dofs, const int64_t *cons_ptr,
                              const int32_t *cons_col, std::vector<int64_t> &row_ptr, std::vector<int32_t> &cols,
                              int n_threads) {
   // find_connected_dofs: close each element's dof set under "constrained by"
-  std::vector<int64_t> eptr((size_t)n_elem + 1, 0);
-  std::vector<int32_t> elist;
-  elist.reserve((size_t)(n_elem * nl));
-  std::vector<int32_t> set, add;
-  for (int64_t e = 0; e < n_elem; ++e) {
-    set.assign(ed + e * nl, ed + (e + 1) * nl);
-    std::sort(set.begin(), set.end());
-    set.erase(std::unique(set.begin(), set.end()), set.end());
-    for (bool done = false; !done;) {
-      add.clear();
-      for (int32_t d : set)
-        for (int64_t k = cons_ptr[d]; k < cons_ptr[d + 1]; ++k)
-          if (!std::binary_search(set.begin(), set.end(), cons_col[k])) add.push_back(cons_col[k]);
-      done = add.empty();
-      if (!done) {
-        set.insert(set.end(), add.begin(), add.end());
+  // (elements in contiguous ranges per thread, lists concatenated in order)
+  const int T = std::max(1, std::min<int>(n_threads, (int)std::max<int64_t>(1, n_elem / 1024)));
+  std::vector<std::vector<int32_t>> part((size_t)T);
+  std::vector<std::vector<int64_t>> plen((size_t)T);
+  std::vector<std::thread> th;
+  for (int tid = 0; tid < T; ++tid)
+    th.emplace_back([&, tid]() {
+      const int64_t e0 = n_elem * tid / T, e1 = n_elem * (tid + 1) / T;
+      std::vector<int32_t> &out = part[(size_t)tid];
+      std::vector<int64_t> &len = plen[(size_t)tid];
+      out.reserve((size_t)((e1 - e0) * nl));
+      std::vector<int32_t> set, add;
+      for (int64_t e = e0; e < e1; ++e) {
+        set.assign(ed + e * nl, ed + (e + 1) * nl);
         std::sort(set.begin(), set.end());
         set.erase(std::unique(set.begin(), set.end()), set.end());
+        for (bool done = false; !done;) {
+          add.clear();
+          for (int32_t d : set)
+            for (int64_t k = cons_ptr[d]; k < cons_ptr[d + 1]; ++k)
+              if (!std::binary_search(set.begin(), set.end(), cons_col[k])) add.push_back(cons_col[k]);
+          done = add.empty();
+          if (!done) {
+            set.insert(set.end(), add.begin(), add.end());
+            std::sort(set.begin(), set.end());
+            set.erase(std::unique(set.begin(), set.end()), set.end());
+          }
+        }
+        out.insert(out.end(), set.begin(), set.end());
+        len.push_back((int64_t)set.size());
       }
+    });
+  for (auto &t : th) t.join();
+  std::vector<int64_t> eptr((size_t)n_elem + 1, 0);
+  std::vector<int32_t> elist;
+  size_t total = 0;
+  for (auto &p : part) total += p.size();
+  elist.reserve(total);
+  int64_t e = 0;
+  for (int tid = 0; tid < T; ++tid) {
+    elist.insert(elist.end(), part[(size_t)tid].begin(), part[(size_t)tid].end());
+    for (int64_t l : plen[(size_t)tid]) {
+      eptr[(size_t)e + 1] = eptr[(size_t)e] + l;
+      ++e;
     }
-    elist.insert(elist.end(), set.begin(), set.end());
-    eptr[(size_t)e + 1] = (int64_t)elist.size();
+    std::vector<int32_t>().swap(part[(size_t)tid]);
   }
   build_var_graph(n_elem, eptr, elist, n_dofs, row_ptr, cols, n_threads);
 }

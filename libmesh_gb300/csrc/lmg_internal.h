@@ -160,4 +160,8 @@ void build_block_graph(int64_t n_elem, int nb_per_elem, const int32_t *elem_bloc
 // The opaque mesh handle of the C ABI.
 struct lmg_mesh {
   lmg::HostMesh m;
+  // constraint rows of the last lmg_constraint_rows call and its input checksum
+  lmg::ConstraintRows rows;
+  uint64_t rows_key = 0;
+  bool rows_valid = false;
 };
