@@ -268,7 +268,7 @@ lmg_status general_assemble(lmg_ctx *c) {
   a.kappa = c->kappa;
   a.n_modes = c->n_modes;
   a.modes = c->d_modes;
-  a.Kraw = c->d_Ebuf;
+  a.Kraw = reinterpret_cast<float2 *>(c->d_Ebuf);
   a.Fraw = c->d_Fbuf;
   a.status = c->d_status;
   a.bad_elem = c->d_bad;
@@ -292,9 +292,9 @@ lmg_status general_assemble(lmg_ctx *c) {
     k.ci = c->d_cci;
     k.cv = c->d_ccv;
     k.rowmask = c->d_crow;
-    k.Kraw = c->d_Ebuf;
+    k.Kraw = reinterpret_cast<const float2 *>(c->d_Ebuf);
     k.Fraw = c->d_Fbuf;
-    k.Ebuf = c->d_Ebuf;
+    k.Ebuf = reinterpret_cast<float2 *>(c->d_Ebuf);
     k.Fbuf = c->d_Fbuf;
     launch_constrain(k, c->n_sm, c->stream);
     c->launches++;
@@ -303,12 +303,9 @@ lmg_status general_assemble(lmg_ctx *c) {
 }
 
 void general_gather(lmg_ctx *c) {
-  if (hier3_masks(c))  // cubic hexes write double-float element matrices
-    launch_gather_full_df(c->nnz, c->d_cptr, c->d_coff, reinterpret_cast<const float2 *>(c->d_Ebuf), c->d_K,
-                          c->n_dofs, c->d_gfptr, c->d_gfoff, c->d_Fbuf, c->d_F, c->n_sm, c->stream);
-  else
-    launch_gather_full(c->nnz, c->d_cptr, c->d_coff, c->d_Ebuf, c->d_K, c->n_dofs, c->d_gfptr, c->d_gfoff,
-                       c->d_Fbuf, c->d_F, c->n_sm, c->stream);
+  // element matrices are double-float pairs (element and constraint kernels)
+  launch_gather_full_df(c->nnz, c->d_cptr, c->d_coff, reinterpret_cast<const float2 *>(c->d_Ebuf), c->d_K,
+                        c->n_dofs, c->d_gfptr, c->d_gfoff, c->d_Fbuf, c->d_F, c->n_sm, c->stream);
   c->launches++;
 }
 

@@ -9,13 +9,15 @@
 //   DofMap::build_constraint_matrix              src/base/dof_map_constraints.C:3433-3540
 //   SparseMatrix::add_matrix / add_vector        src/numerics/petsc_matrix.C:735-755
 //
-// Element kernel: one warp per element, lane b computes column b of Ke.
+// Element kernel: one warp per element, lane b computes column b of Ke, in
+// double-float arithmetic on the FP32 pipe (geometry and transport velocity in
+// FP64); element matrices are stored as double-float pairs.
 // Affine hexahedra only: the diffusion block is the reference-tensor
 // contraction K_ab = sum_k A_k D^k_ab (D = symmetrized sum_q w dphi_m dphi_n
 // tables), the convection block C_ab = sum_q phi_a(q) sum_m beta_m(q) dphi_m,b(q)
 // with beta_m(q) = w_q detJ (dxi_m/dx . b(x_q)), summed over q by sum
 // factorization (phi_a(q) is a product of 1-D shapes on the tensor Gauss
-// rule).  All FP64.
+// rule).
 //
 // Constraint kernel: one CTA per constrained element.  K' = C^T K C over the
 // element's dofs followed by its constraining dofs (sorted), with C given by
@@ -61,30 +63,31 @@ __host__ __device__ constexpr int hex_tensor(int n, int a) {
 }
 
 // C_rb = sum_q phi_r(q) P(q) for the tensor-product element: phi_r(q) =
-// L_i(x_q1) L_j(x_q2) L_k(x_q3), q = q1 + Q1 (q2 + Q1 q3); three 1-D passes.
+// L_i(x_q1) L_j(x_q2) L_k(x_q3), q = q1 + Q1 (q2 + Q1 q3); three 1-D passes,
+// in double-float arithmetic (FP32 pipe), every inner sum renormalised once.
 template <int N1, int Q1>
-__device__ __forceinline__ void tensor_contract(const double *L1, const double *P, double *Cc) {
-  double T1[N1 * Q1 * Q1];
+__device__ __forceinline__ void tensor_contract_df(const DF *L1, const DF *P, DF *Cc) {
+  DF T1[N1 * Q1 * Q1];
 #pragma unroll
   for (int i = 0; i < N1; ++i)
 #pragma unroll
     for (int r = 0; r < Q1 * Q1; ++r) {
-      double t = 0.0;
+      DF t = {0.f, 0.f};
 #pragma unroll
-      for (int q1 = 0; q1 < Q1; ++q1) t += L1[i * Q1 + q1] * P[q1 + Q1 * r];
-      T1[i * Q1 * Q1 + r] = t;
+      for (int q1 = 0; q1 < Q1; ++q1) t = df_fma_lazy(t, L1[i * Q1 + q1], P[q1 + Q1 * r]);
+      T1[i * Q1 * Q1 + r] = df_norm(t);
     }
-  double T2[N1 * N1 * Q1];
+  DF T2[N1 * N1 * Q1];
 #pragma unroll
   for (int i = 0; i < N1; ++i)
 #pragma unroll
     for (int j = 0; j < N1; ++j)
 #pragma unroll
       for (int q3 = 0; q3 < Q1; ++q3) {
-        double t = 0.0;
+        DF t = {0.f, 0.f};
 #pragma unroll
-        for (int q2 = 0; q2 < Q1; ++q2) t += L1[j * Q1 + q2] * T1[i * Q1 * Q1 + q2 + Q1 * q3];
-        T2[(i * N1 + j) * Q1 + q3] = t;
+        for (int q2 = 0; q2 < Q1; ++q2) t = df_fma_lazy(t, L1[j * Q1 + q2], T1[i * Q1 * Q1 + q2 + Q1 * q3]);
+        T2[(i * N1 + j) * Q1 + q3] = df_norm(t);
       }
 #pragma unroll
   for (int i = 0; i < N1; ++i)
@@ -92,11 +95,16 @@ __device__ __forceinline__ void tensor_contract(const double *L1, const double *
     for (int j = 0; j < N1; ++j)
 #pragma unroll
       for (int k = 0; k < N1; ++k) {
-        double t = 0.0;
+        DF t = {0.f, 0.f};
 #pragma unroll
-        for (int q3 = 0; q3 < Q1; ++q3) t += L1[k * Q1 + q3] * T2[(i * N1 + j) * Q1 + q3];
-        Cc[i + 3 * j + 9 * k] = t;
+        for (int q3 = 0; q3 < Q1; ++q3) t = df_fma_lazy(t, L1[k * Q1 + q3], T2[(i * N1 + j) * Q1 + q3]);
+        Cc[i + 3 * j + 9 * k] = df_norm(t);
       }
+}
+
+inline __device__ DF ld_df(const float2 *p) {
+  const float2 v = *p;
+  return DF{v.x, v.y};
 }
 
 template <int FORM, int N, int Q>
@@ -104,9 +112,9 @@ __global__ void __launch_bounds__(WARPS * 32) k_elem_full(GenElemArgs a) {
   constexpr int N1 = (N == 8) ? 2 : 3, Q1 = (Q == 8) ? 2 : 3;
   extern __shared__ double sm[];
   double *sphi = sm;                  // [Q][N]
-  double *sdphi = sphi + Q * N;       // [Q][N][3]
-  double *sD = sdphi + Q * N * 3;     // [6][N][N]
-  double *sqw = sD + 6 * N * N;       // [Q]
+  float2 *sdphi = reinterpret_cast<float2 *>(sphi + Q * N);        // [Q][N][3] double-float
+  float2 *sD = sdphi + Q * N * 3;                                   // [6][N][N] double-float
+  double *sqw = reinterpret_cast<double *>(sD + 6 * N * N);       // [Q]
   double *sgd = sqw + Q;              // [N][3] mapping derivatives at qp 0
   double *sgp = sgd + N * 3;          // [Q][N] mapping shapes (isoparametric geometry)
   double *smode = sgp + Q * N;        // [7 * n_modes]
@@ -114,18 +122,24 @@ __global__ void __launch_bounds__(WARPS * 32) k_elem_full(GenElemArgs a) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   double *sX = wbase + warp * (N * 3 + N + 4 * Q + 8 * a.n_modes);  // [N][3]
   double *sf = sX + N * 3;                            // [N]
-  double *sbeta = sf + N;                             // [Q][3]
-  double *sfq = sbeta + 3 * Q;                        // [Q]
+  float2 *sbeta = reinterpret_cast<float2 *>(sf + N); // [Q][3] double-float
+  double *sfq = reinterpret_cast<double *>(sbeta + 3 * Q);  // [Q]
   double *sE = sfq + Q;                               // [n_modes][4] (cos, sin)
   for (int i = threadIdx.x; i < Q * N; i += blockDim.x) sphi[i] = a.fe.phi[i];
-  for (int i = threadIdx.x; i < Q * N * 3; i += blockDim.x) sdphi[i] = a.fe.dphi[i];
-  for (int i = threadIdx.x; i < 6 * N * N; i += blockDim.x) sD[i] = a.D6[i];
+  for (int i = threadIdx.x; i < Q * N * 3; i += blockDim.x) {
+    const DF x = df_split(a.fe.dphi[i]);
+    sdphi[i] = make_float2(x.hi, x.lo);
+  }
+  for (int i = threadIdx.x; i < 6 * N * N; i += blockDim.x) {
+    const DF x = df_split(a.D6[i]);
+    sD[i] = make_float2(x.hi, x.lo);
+  }
   for (int i = threadIdx.x; i < Q; i += blockDim.x) sqw[i] = a.fe.qw[i];
   for (int i = threadIdx.x; i < N * 3; i += blockDim.x) sgd[i] = a.fe.gdphi[i];
   for (int i = threadIdx.x; i < Q * N; i += blockDim.x) sgp[i] = a.fe.gphi[i];
   for (int i = threadIdx.x; i < 7 * a.n_modes; i += blockDim.x) smode[i] = a.modes[i];
-  __shared__ double sL1[9];
-  for (int i = threadIdx.x; i < N1 * Q1; i += blockDim.x) sL1[i] = a.D6[6 * N * N + i];
+  __shared__ DF sL1[9];
+  for (int i = threadIdx.x; i < N1 * Q1; i += blockDim.x) sL1[i] = df_split(a.D6[6 * N * N + i]);
   const double gp = a.D6[6 * N * N + N1 * Q1];  // outer 1-D Gauss point (+gp, -gp, and 0 when Q1 = 3)
   __syncthreads();
   const int64_t stride = (int64_t)gridDim.x * WARPS;
@@ -237,36 +251,47 @@ __global__ void __launch_bounds__(WARPS * 32) k_elem_full(GenElemArgs a) {
           b[2] += cs * (md[3] * md[1] - md[4] * md[0]);
         }
 #pragma unroll
-        for (int m = 0; m < 3; ++m)
-          sbeta[3 * q + m] = jxw * (G[3 * m] * b[0] + G[3 * m + 1] * b[1] + G[3 * m + 2] * b[2]);
+        for (int m = 0; m < 3; ++m) {
+          const DF x = df_split(jxw * (G[3 * m] * b[0] + G[3 * m + 1] * b[1] + G[3 * m + 2] * b[2]));
+          sbeta[3 * q + m] = make_float2(x.hi, x.lo);
+        }
       }
     }
     __syncwarp();
     if (lane < N) {
+      // column b of Ke in double-float arithmetic: convection by sum
+      // factorisation, diffusion from the reference tensors
       const int b = lane;
-      double P[Q];
+      DF P[Q];
       if (FORM == LMG_ADVDIFF) {
 #pragma unroll
         for (int q = 0; q < Q; ++q) {
-          const double *d = sdphi + (q * N + b) * 3;
-          P[q] = sbeta[3 * q] * d[0] + sbeta[3 * q + 1] * d[1] + sbeta[3 * q + 2] * d[2];
+          const float2 *d = sdphi + (q * N + b) * 3;
+          DF t = {0.f, 0.f};
+#pragma unroll
+          for (int m = 0; m < 3; ++m) t = df_fma_lazy(t, ld_df(sbeta + 3 * q + m), ld_df(d + m));
+          P[q] = df_norm(t);
         }
       }
-      double Cc[27];
+      DF Cc[27];
       if (FORM == LMG_ADVDIFF) {
-        double L1[N1 * Q1];
+        DF L1[N1 * Q1];
 #pragma unroll
         for (int i = 0; i < N1 * Q1; ++i) L1[i] = sL1[i];
-        tensor_contract<N1, Q1>(L1, P, Cc);
+        tensor_contract_df<N1, Q1>(L1, P, Cc);
       }
-      double *Ke = a.Kraw + e * (N * N);
+      DF A2[6];
+#pragma unroll
+      for (int t = 0; t < 6; ++t) A2[t] = df_split(A[t]);
+      float2 *Ke = a.Kraw + e * (N * N);
 #pragma unroll
       for (int r = 0; r < N; ++r) {
-        double k = A[0] * sD[r * N + b];
+        DF k = {0.f, 0.f};
 #pragma unroll
-        for (int t = 1; t < 6; ++t) k += A[t] * sD[(t * N + r) * N + b];
-        if (FORM == LMG_ADVDIFF) k += Cc[hex_tensor(N, r)];
-        Ke[r * N + b] = k;
+        for (int t = 0; t < 6; ++t) k = df_fma_lazy(k, A2[t], ld_df(sD + (t * N + r) * N + b));
+        k = df_norm(k);
+        if (FORM == LMG_ADVDIFF) k = df_add(k, Cc[hex_tensor(N, r)]);
+        Ke[r * N + b] = make_float2(k.hi, k.lo);
       }
       double fe = 0.0;
 #pragma unroll
@@ -291,16 +316,19 @@ void launch_full(const GenElemArgs &a, int max_ctas, cudaStream_t s) {
   if (grid > 0) k_elem_full<FORM, N, Q><<<grid, WARPS * 32, smem, s>>>(a);
 }
 
-// Dynamic shared memory: K [N][N], F [N], L = C^T K [max_ne][N], coefficients
-// [max_ent], column pointers [max_ne + 1], row indices [max_ent].
+// Dynamic shared memory: K [N][N] (double-float), F [N], L = C^T K [max_ne][N]
+// (double-float), coefficients [max_ent] (FP64 and double-float), column
+// pointers [max_ne + 1], row indices [max_ent].  The matrix products run in
+// double-float arithmetic on the FP32 pipe; the load in FP64.
 __global__ void __launch_bounds__(128) k_constrain(ConsArgs c) {
   extern __shared__ double csm[];
   const int N = c.N;
-  double *sK = csm;
-  double *sF = sK + N * N;
-  double *sL = sF + N;
-  double *scv = sL + c.max_ne * N;
-  int32_t *scp = reinterpret_cast<int32_t *>(scv + c.max_ent);
+  float2 *sK = reinterpret_cast<float2 *>(csm);
+  double *sF = reinterpret_cast<double *>(sK + N * N);
+  float2 *sL = reinterpret_cast<float2 *>(sF + N);
+  double *scv = reinterpret_cast<double *>(sL + c.max_ne * N);
+  float2 *scv2 = reinterpret_cast<float2 *>(scv + c.max_ent);
+  int32_t *scp = reinterpret_cast<int32_t *>(scv2 + c.max_ent);
   uint8_t *sci = reinterpret_cast<uint8_t *>(scp + c.max_ne + 1);
   for (int64_t k = blockIdx.x; k < c.n_cons; k += gridDim.x) {
     const int64_t e = c.elem[k];
@@ -315,34 +343,45 @@ __global__ void __launch_bounds__(128) k_constrain(ConsArgs c) {
     const int n_ent = scp[ne];
     for (int i = threadIdx.x; i < n_ent; i += blockDim.x) {
       sci[i] = c.ci[eb + i];
-      scv[i] = c.cv[eb + i];
+      const double v = c.cv[eb + i];
+      scv[i] = v;
+      const DF x = df_split(v);
+      scv2[i] = make_float2(x.hi, x.lo);
     }
     __syncthreads();
     // L_pj = sum_i C_ip K_ij (rows of constrained local dofs are replaced below)
     for (int idx = threadIdx.x; idx < ne * N; idx += blockDim.x) {
       const int p = idx / N, j = idx - p * N;
-      double l = 0.0;
+      DF l = {0.f, 0.f};
       if (!(p < N && ((rows >> p) & 1ull)))
-        for (int u = scp[p]; u < scp[p + 1]; ++u) l += scv[u] * sK[sci[u] * N + j];
-      sL[idx] = l;
+        for (int u = scp[p]; u < scp[p + 1]; ++u) {
+          const float2 cv = scv2[u], kv = sK[sci[u] * N + j];
+          l = df_fma_lazy(l, DF{cv.x, cv.y}, DF{kv.x, kv.y});
+        }
+      l = df_norm(l);
+      sL[idx] = make_float2(l.hi, l.lo);
     }
     __syncthreads();
-    double *out = c.Ebuf + c.kout[k];
+    float2 *out = c.Ebuf + c.kout[k];
     for (int idx = threadIdx.x; idx < ne * ne; idx += blockDim.x) {
       const int p = idx / ne, q = idx - p * ne;
-      double v = 0.0;
+      DF v = {0.f, 0.f};
       if (p < N && ((rows >> p) & 1ull)) {
         if (p == q) {
-          v = 1.0;
+          v = DF{1.f, 0.f};
         } else {
           for (int t = scp[q]; t < scp[q + 1]; ++t)
-            if (sci[t] == p) v = -scv[t];
+            if (sci[t] == p) v = DF{-scv2[t].x, -scv2[t].y};
         }
       } else {
-        const double *lp = sL + p * N;
-        for (int t = scp[q]; t < scp[q + 1]; ++t) v += lp[sci[t]] * scv[t];
+        const float2 *lp = sL + p * N;
+        for (int t = scp[q]; t < scp[q + 1]; ++t) {
+          const float2 lv = lp[sci[t]], cv = scv2[t];
+          v = df_fma_lazy(v, DF{lv.x, lv.y}, DF{cv.x, cv.y});
+        }
+        v = df_norm(v);
       }
-      out[idx] = v;
+      out[idx] = make_float2(v.hi, v.lo);
     }
     double *fo = c.Fbuf + c.fout[k];
     for (int p = threadIdx.x; p < ne; p += blockDim.x) {
@@ -353,29 +392,9 @@ __global__ void __launch_bounds__(128) k_constrain(ConsArgs c) {
   }
 }
 
-// K[s] = sum of the slot's contributions in element order; F likewise per dof.
-__global__ void k_gather_full(int64_t nnz, const int64_t *__restrict__ cptr, const uint32_t *__restrict__ coff,
-                              const double *__restrict__ E, double *__restrict__ K, int64_t n_dofs,
-                              const int64_t *__restrict__ fptr, const uint32_t *__restrict__ foff,
-                              const double *__restrict__ Fb, double *__restrict__ F) {
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < nnz + n_dofs; s += stride) {
-    if (s < nnz) {
-      double v = 0.0;
-      for (int64_t t = cptr[s]; t < cptr[s + 1]; ++t) v += E[coff[t]];
-      K[s] = v;
-    } else {
-      const int64_t d = s - nnz;
-      double v = 0.0;
-      for (int64_t t = fptr[d]; t < fptr[d + 1]; ++t) v += Fb[foff[t]];
-      F[d] = v;
-    }
-  }
-}
-
-// The same gather over element matrices stored as double-float pairs: the
-// contributions of a slot are summed in double-float arithmetic on the FP32
-// pipe and rounded to FP64 once per entry.
+// K[s] = sum of the slot's contributions in element order, over element
+// matrices stored as double-float pairs: summed in double-float arithmetic on
+// the FP32 pipe and rounded to FP64 once per entry; F likewise per dof in FP64.
 __global__ void k_gather_full_df(int64_t nnz, const int64_t *__restrict__ cptr, const uint32_t *__restrict__ coff,
                                  const float2 *__restrict__ E, double *__restrict__ K, int64_t n_dofs,
                                  const int64_t *__restrict__ fptr, const uint32_t *__restrict__ foff,
@@ -422,7 +441,7 @@ void launch_gen_elements(int form, int n, int q, const GenElemArgs &a, int max_c
 void launch_constrain(const ConsArgs &c, int n_sm, cudaStream_t s) {
   if (c.n_cons <= 0) return;
   const int64_t g = c.n_cons < (int64_t)n_sm * 16 ? c.n_cons : (int64_t)n_sm * 16;
-  const size_t smem = sizeof(double) * ((size_t)c.N * c.N + c.N + (size_t)c.max_ne * c.N + c.max_ent) +
+  const size_t smem = sizeof(double) * ((size_t)c.N * c.N + c.N + (size_t)c.max_ne * c.N + 2 * (size_t)c.max_ent) +
                       sizeof(int32_t) * (c.max_ne + 1) + c.max_ent;
   static size_t attr = 0;
   if (smem > attr) {
@@ -430,15 +449,6 @@ void launch_constrain(const ConsArgs &c, int n_sm, cudaStream_t s) {
     attr = smem;
   }
   k_constrain<<<(int)g, 128, smem, s>>>(c);
-}
-
-void launch_gather_full(int64_t nnz, const int64_t *cptr, const uint32_t *coff, const double *E, double *K,
-                        int64_t n_dofs, const int64_t *fptr, const uint32_t *foff, const double *Fb, double *F,
-                        int n_sm, cudaStream_t s) {
-  const int64_t items = nnz + n_dofs;
-  const int64_t blocks = (items + 255) / 256;
-  const int g = (int)(blocks < (int64_t)n_sm * 16 ? blocks : (int64_t)n_sm * 16);
-  k_gather_full<<<g, 256, 0, s>>>(nnz, cptr, coff, E, K, n_dofs, fptr, foff, Fb, F);
 }
 
 void launch_gather_full_df(int64_t nnz, const int64_t *cptr, const uint32_t *coff, const float2 *E, double *K,

@@ -21,9 +21,9 @@
 // constraint rows the homogeneous Dirichlet rows are applied here (zero row
 // and column, 1 on the diagonal, zero load: constrain_element_matrix_and_vector
 // with empty rows) and the constraint kernel is skipped; with rows the
-// constraint kernel applies C^T K C.  In the masked case the element
-// matrices stay double-float pairs and the gather sums them in double-float
-// (k_gather_full_df), rounding each CSR entry to FP64 once.
+// constraint kernel applies C^T K C.  The element matrices stay double-float
+// pairs; the gather sums them in double-float (k_gather_full_df), rounding
+// each CSR entry to FP64 once.
 #include <cuda_runtime.h>
 
 #include <string>
@@ -51,7 +51,7 @@ struct H3Args {
   const float2 *D;          // [P][6][64*64] double-float pairs
   const double *M;          // [P][64][27]
   const double *gd0;        // [27][3]
-  double *Kraw;             // [n_elem][64][64] (double-float pairs when the kernel masks)
+  float2 *Kraw;             // [n_elem][64][64] double-float pairs
   double *Fraw;             // [n_elem][64]
   int *status;
   unsigned long long *bad_elem;
@@ -63,8 +63,6 @@ __device__ __forceinline__ double warp_sum(double v) {
   return v;
 }
 
-// DFOUT: element matrices stay double-float pairs for the double-float gather.
-template <bool DFOUT>
 __global__ void __launch_bounds__(H3T) k_elem_hier3(H3Args a) {
   __shared__ double sA[H3B][8];   // A_0..A_5, detJ
   __shared__ DF sA2[H3B][6];
@@ -142,10 +140,7 @@ __global__ void __launch_bounds__(H3T) k_elem_hier3(H3Args a) {
         for (int k = 0; k < 6; ++k) v = df_fma_lazy(v, sA2[b][k], d[k]);
         v = df_norm(v);
         if (((sm[b] >> i) | (sm[b] >> j)) & 1ull) v = DF{(i == j) ? 1.f : 0.f, 0.f};
-        if (DFOUT)
-          reinterpret_cast<float2 *>(a.Kraw)[(int64_t)se[b] * (H3N * H3N) + idx] = make_float2(v.hi, v.lo);
-        else
-          a.Kraw[(int64_t)se[b] * (H3N * H3N) + idx] = df_to_double(v);
+        a.Kraw[(int64_t)se[b] * (H3N * H3N) + idx] = make_float2(v.hi, v.lo);
       }
     }
     const double *Mp = a.M + (size_t)p * H3N * 27;
@@ -233,15 +228,14 @@ void launch_hier3(lmg_ctx *c) {
   a.D = c->d_h3D;
   a.M = c->d_h3M;
   a.gd0 = c->d_h3gd;
-  a.Kraw = c->d_Ebuf;
+  a.Kraw = reinterpret_cast<float2 *>(c->d_Ebuf);
   a.Fraw = c->d_Fbuf;
   a.status = c->d_status;
   a.bad_elem = c->d_bad;
   const int64_t want = (int64_t)c->n_sm * 8;
   const int grid = (int)(a.n_batch < want ? a.n_batch : want);
   if (grid <= 0) return;
-  if (a.cmask) k_elem_hier3<true><<<grid, H3T, 0, c->stream>>>(a);
-  else k_elem_hier3<false><<<grid, H3T, 0, c->stream>>>(a);
+  k_elem_hier3<<<grid, H3T, 0, c->stream>>>(a);
 }
 
 }  // namespace lmg
