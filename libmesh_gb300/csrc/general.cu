@@ -111,21 +111,25 @@ template <int FORM, int N, int Q>
 __global__ void __launch_bounds__(WARPS * 32) k_elem_full(GenElemArgs a) {
   constexpr int N1 = (N == 8) ? 2 : 3, Q1 = (Q == 8) ? 2 : 3;
   extern __shared__ double sm[];
-  double *sphi = sm;                  // [Q][N]
-  float2 *sdphi = reinterpret_cast<float2 *>(sphi + Q * N);        // [Q][N][3] double-float
+  float2 *sphi = reinterpret_cast<float2 *>(sm);                   // [Q][N] double-float
+  float2 *sdphi = sphi + Q * N;                                     // [Q][N][3] double-float
   float2 *sD = sdphi + Q * N * 3;                                   // [6][N][N] double-float
   double *sqw = reinterpret_cast<double *>(sD + 6 * N * N);       // [Q]
   double *sgd = sqw + Q;              // [N][3] mapping derivatives at qp 0
   double *sgp = sgd + N * 3;          // [Q][N] mapping shapes (isoparametric geometry)
   double *smode = sgp + Q * N;        // [7 * n_modes]
-  double *wbase = smode + 7 * a.n_modes;
+  float2 *scurl = reinterpret_cast<float2 *>(smode + 7 * a.n_modes);  // [n_modes][3] k x a, double-float
+  double *wbase = reinterpret_cast<double *>(scurl + 3 * a.n_modes);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   double *sX = wbase + warp * (N * 3 + N + 4 * Q + 8 * a.n_modes);  // [N][3]
-  double *sf = sX + N * 3;                            // [N]
-  float2 *sbeta = reinterpret_cast<float2 *>(sf + N); // [Q][3] double-float
-  double *sfq = reinterpret_cast<double *>(sbeta + 3 * Q);  // [Q]
-  double *sE = sfq + Q;                               // [n_modes][4] (cos, sin)
-  for (int i = threadIdx.x; i < Q * N; i += blockDim.x) sphi[i] = a.fe.phi[i];
+  float2 *sf = reinterpret_cast<float2 *>(sX + N * 3);  // [N] nodal load, double-float
+  float2 *sbeta = sf + N;                               // [Q][3] double-float
+  float2 *sfq = sbeta + 3 * Q;                          // [Q] JxW f(x_q), double-float
+  float2 *sE = sfq + Q;                                 // [n_modes][4] (cos, sin), double-float
+  for (int i = threadIdx.x; i < Q * N; i += blockDim.x) {
+    const DF x = df_split(a.fe.phi[i]);
+    sphi[i] = make_float2(x.hi, x.lo);
+  }
   for (int i = threadIdx.x; i < Q * N * 3; i += blockDim.x) {
     const DF x = df_split(a.fe.dphi[i]);
     sdphi[i] = make_float2(x.hi, x.lo);
@@ -138,6 +142,15 @@ __global__ void __launch_bounds__(WARPS * 32) k_elem_full(GenElemArgs a) {
   for (int i = threadIdx.x; i < N * 3; i += blockDim.x) sgd[i] = a.fe.gdphi[i];
   for (int i = threadIdx.x; i < Q * N; i += blockDim.x) sgp[i] = a.fe.gphi[i];
   for (int i = threadIdx.x; i < 7 * a.n_modes; i += blockDim.x) smode[i] = a.modes[i];
+  for (int i = threadIdx.x; i < 3 * a.n_modes; i += blockDim.x) {  // b = sum_m cos(.) k_m x a_m
+    const double *md = a.modes + 7 * (i / 3);
+    const int d = i % 3;
+    const double v = d == 0 ? md[4] * md[2] - md[5] * md[1]
+                     : d == 1 ? md[5] * md[0] - md[3] * md[2]
+                              : md[3] * md[1] - md[4] * md[0];
+    const DF x = df_split(v);
+    scurl[i] = make_float2(x.hi, x.lo);
+  }
   __shared__ DF sL1[9];
   for (int i = threadIdx.x; i < N1 * Q1; i += blockDim.x) sL1[i] = df_split(a.D6[6 * N * N + i]);
   const double gp = a.D6[6 * N * N + N1 * Q1];  // outer 1-D Gauss point (+gp, -gp, and 0 when Q1 = 3)
@@ -154,7 +167,8 @@ __global__ void __launch_bounds__(WARPS * 32) k_elem_full(GenElemArgs a) {
       sX[3 * lane] = x;
       sX[3 * lane + 1] = y;
       sX[3 * lane + 2] = z;
-      sf[lane] = a.nodal_f ? a.nodal_f[nd] : 0.0;
+      const DF fv = df_split(a.nodal_f ? a.nodal_f[nd] : 0.0);
+      sf[lane] = make_float2(fv.hi, fv.lo);
 #pragma unroll
       for (int m = 0; m < 3; ++m) {
         const double g = sgd[3 * lane + m];
@@ -211,49 +225,53 @@ __global__ void __launch_bounds__(WARPS * 32) k_elem_full(GenElemArgs a) {
         }
         double sn, cs;
         sincos(ang, &sn, &cs);
-        sE[2 * t] = cs;
-        sE[2 * t + 1] = sn;
+        const DF c2 = df_split(cs), s2 = df_split(sn);
+        sE[2 * t] = make_float2(c2.hi, c2.lo);
+        sE[2 * t + 1] = make_float2(s2.hi, s2.lo);
       }
       __syncwarp();
     }
-    // per quadrature point: transport coefficients and the load
+    // per quadrature point: transport coefficients and the load, in
+    // double-float arithmetic (FP32 pipe)
     if (lane < Q) {
       const int q = lane;
-      double xq[3] = {0.0, 0.0, 0.0}, fx = 0.0;
-      for (int c = 0; c < N; ++c) {
-        const double g = sgp[q * N + c], s = sphi[q * N + c];
-        xq[0] += g * sX[3 * c];
-        xq[1] += g * sX[3 * c + 1];
-        xq[2] += g * sX[3 * c + 2];
-        fx += s * sf[c];   // the load is interpolated with the FE shapes
-      }
+      DF fx = {0.f, 0.f};
+      for (int c = 0; c < N; ++c) fx = df_fma_lazy(fx, ld_df(sphi + q * N + c), ld_df(sf + c));  // FE-interpolated load
+      fx = df_norm(fx);
       const double jxw = det * sqw[q];
-      sfq[q] = jxw * fx;
+      const DF jw = df_split(jxw);
+      const DF fq = df_norm(df_fma_lazy(DF{0.f, 0.f}, jw, fx));
+      sfq[q] = make_float2(fq.hi, fq.lo);
       if (FORM == LMG_ADVDIFF) {
-        double b[3] = {0.0, 0.0, 0.0};
+        DF b[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
         // offset of this point along each reference axis: -1, 0 or +1 times gp
         const int qi[3] = {q % Q1, (q / Q1) % Q1, q / (Q1 * Q1)};
         for (int m = 0; m < a.n_modes; ++m) {
-          const double *md = smode + 7 * m;
-          const double *E = sE + 8 * m;
-          double re = E[0], im = E[1];
+          const float2 *E = sE + 8 * m;
+          DF re = ld_df(E), im = ld_df(E + 1);
 #pragma unroll
           for (int d = 0; d < 3; ++d) {
             if (Q1 == 3 && qi[d] == 1) continue;
-            const double c = E[2 * (d + 1)], sn = qi[d] == 0 ? -E[2 * (d + 1) + 1] : E[2 * (d + 1) + 1];
-            const double r2 = re * c - im * sn;
-            im = re * sn + im * c;
+            const DF c = ld_df(E + 2 * (d + 1));
+            DF sn = ld_df(E + 2 * (d + 1) + 1);
+            if (qi[d] == 0) sn = DF{-sn.hi, -sn.lo};
+            const DF nim = DF{-im.hi, -im.lo};
+            const DF r2 = df_norm(df_fma_lazy(df_fma_lazy(DF{0.f, 0.f}, re, c), nim, sn));
+            im = df_norm(df_fma_lazy(df_fma_lazy(DF{0.f, 0.f}, re, sn), im, c));
             re = r2;
           }
-          const double cs = re;
-          b[0] += cs * (md[4] * md[2] - md[5] * md[1]);
-          b[1] += cs * (md[5] * md[0] - md[3] * md[2]);
-          b[2] += cs * (md[3] * md[1] - md[4] * md[0]);
+#pragma unroll
+          for (int d = 0; d < 3; ++d) b[d] = df_fma_lazy(b[d], re, ld_df(scurl + 3 * m + d));
         }
 #pragma unroll
+        for (int d = 0; d < 3; ++d) b[d] = df_norm(b[d]);
+#pragma unroll
         for (int m = 0; m < 3; ++m) {
-          const DF x = df_split(jxw * (G[3 * m] * b[0] + G[3 * m + 1] * b[1] + G[3 * m + 2] * b[2]));
-          sbeta[3 * q + m] = make_float2(x.hi, x.lo);
+          DF t = {0.f, 0.f};
+#pragma unroll
+          for (int d = 0; d < 3; ++d) t = df_fma_lazy(t, df_split(jxw * G[3 * m + d]), b[d]);
+          t = df_norm(t);
+          sbeta[3 * q + m] = make_float2(t.hi, t.lo);
         }
       }
     }
@@ -293,10 +311,10 @@ __global__ void __launch_bounds__(WARPS * 32) k_elem_full(GenElemArgs a) {
         if (FORM == LMG_ADVDIFF) k = df_add(k, Cc[hex_tensor(N, r)]);
         Ke[r * N + b] = make_float2(k.hi, k.lo);
       }
-      double fe = 0.0;
+      DF fe = {0.f, 0.f};
 #pragma unroll
-      for (int q = 0; q < Q; ++q) fe += sfq[q] * sphi[q * N + b];
-      a.Fraw[e * N + b] = fe;
+      for (int q = 0; q < Q; ++q) fe = df_fma_lazy(fe, ld_df(sfq + q), ld_df(sphi + q * N + b));
+      a.Fraw[e * N + b] = df_to_double(df_norm(fe));
     }
     __syncwarp();
   }
@@ -304,7 +322,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_elem_full(GenElemArgs a) {
 
 template <int FORM, int N, int Q>
 void launch_full(const GenElemArgs &a, int max_ctas, cudaStream_t s) {
-  const size_t smem = sizeof(double) * ((size_t)Q * N * 5 + 6 * N * N + Q + N * 3 + 7 * a.n_modes +
+  const size_t smem = sizeof(double) * ((size_t)Q * N * 5 + 6 * N * N + Q + N * 3 + 10 * a.n_modes +
                                         (size_t)WARPS * (N * 3 + N + 4 * Q + 8 * a.n_modes));
   static size_t attr = 0;  // largest dynamic shared memory granted so far
   if (smem > attr) {
