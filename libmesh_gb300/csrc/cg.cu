@@ -43,15 +43,44 @@ __device__ __forceinline__ double block_sum(double v) {
   return s;  // valid in thread 0
 }
 
-__global__ void k_spmv(int64_t n, const int32_t *rp, const int32_t *col, const double *val, const double *x,
-                       double *y) {
-  const int lane = threadIdx.x & 31;
-  for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < n;
-       r += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+// y = A x, G lanes per row (32 / G rows per warp and pass), G chosen from the
+// mean row length so that every lane has a few entries and a warp keeps
+// several rows' loads in flight.  The loop bound is warp-uniform so that the
+// shuffles see every lane.
+template <int G>
+__global__ void k_spmv(int64_t n, const int32_t *__restrict__ rp, const int32_t *__restrict__ col,
+                       const double *__restrict__ val, const double *__restrict__ x, double *__restrict__ y) {
+  constexpr int RPW = 32 / G;  // rows per warp and pass
+  const int lane = threadIdx.x & 31, sub = lane & (G - 1), grp = lane / G;
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t n_warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t w0 = warp * RPW; w0 < n; w0 += n_warps * RPW) {
+    const int64_t r = w0 + grp;
     double s = 0.0;
-    for (int32_t k = rp[r] + lane; k < rp[r + 1]; k += 32) s += val[k] * x[col[k]];
-    s = warp_sum(s);
-    if (lane == 0) y[r] = s;
+    if (r < n) {
+      const int32_t b = __ldg(rp + r), e = __ldg(rp + r + 1);
+#pragma unroll 4
+      for (int32_t k = b + sub; k < e; k += G) s += __ldg(val + k) * __ldg(x + __ldg(col + k));
+    }
+#pragma unroll
+    for (int o = G / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, G);
+    if (r < n && sub == 0) y[r] = s;
+  }
+}
+
+// lanes per row for a mean row length
+inline int spmv_lanes(int64_t n, int64_t nnz) {
+  const int64_t m = n > 0 ? nnz / n : 0;
+  return m <= 16 ? 4 : (m <= 32 ? 8 : (m <= 64 ? 16 : 32));
+}
+
+void launch_spmv(int g, int grid, cudaStream_t s, int64_t n, const int32_t *rp, const int32_t *col, const double *val,
+                 const double *x, double *y) {
+  switch (g) {
+    case 4: k_spmv<4><<<grid, 256, 0, s>>>(n, rp, col, val, x, y); break;
+    case 8: k_spmv<8><<<grid, 256, 0, s>>>(n, rp, col, val, x, y); break;
+    case 16: k_spmv<16><<<grid, 256, 0, s>>>(n, rp, col, val, x, y); break;
+    default: k_spmv<32><<<grid, 256, 0, s>>>(n, rp, col, val, x, y); break;
   }
 }
 
@@ -139,6 +168,10 @@ int cg_solve(int64_t n, const int32_t *rp, const int32_t *col, const double *val
   const int g1 = n_sm * 8, gs = n_sm * 16;
   int nblk = (int)std::min<int64_t>(RBLK, (n + RT - 1) / RT);
   int64_t L = 0;
+  int32_t nnz = 0;
+  cudaMemcpyAsync(&nnz, rp + n, sizeof(int32_t), cudaMemcpyDeviceToHost, s);
+  cudaStreamSynchronize(s);
+  const int sg = spmv_lanes(n, nnz);
   k_diag_inv<<<g1, 256, 0, s>>>(n, rp, col, val, dinv);
   k_init<<<g1, 256, 0, s>>>(n, b, x, r, z, p, dinv);
   k_dot2<<<nblk, RT, 0, s>>>(n, r, z, r, r, partial);
@@ -155,7 +188,7 @@ int cg_solve(int64_t n, const int32_t *rp, const int32_t *col, const double *val
     *relres = 0.0;
   } else {
     for (it = 0; it < maxit; ++it) {
-      k_spmv<<<gs, 256, 0, s>>>(n, rp, col, val, p, q);
+      launch_spmv(sg, gs, s, n, rp, col, val, p, q);
       k_dot2<<<nblk, RT, 0, s>>>(n, p, q, nullptr, nullptr, partial);
       k_dot2_final<<<1, RT, 0, s>>>(nblk, partial, sc + 2);  // sc[2] = pq
       k_update_xr<<<g1, 256, 0, s>>>(n, sc, x, r, z, p, q, dinv);
@@ -253,6 +286,11 @@ extern "C" lmg_status lmg_cg_solve_noalloc(int64_t n, const int32_t *rp, const i
     return na_fail(msg, msg_len, LMG_ERR_CUDA, "cg_solve_noalloc: clearing the scalar slots failed");
   const int g1 = n_sm * 8, gs = n_sm * 16;
   const int nblk = (int)std::min<int64_t>(RBLK, (n + RT - 1) / RT);
+  int32_t nnz = 0;  // the row pointer's last entry sets the SpMV lane count
+  if (cudaMemcpyAsync(&nnz, rp + n, sizeof(int32_t), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess)
+    return na_fail(msg, msg_len, LMG_ERR_CUDA, "cg_solve_noalloc: reading the row pointer failed");
+  const int sg = spmv_lanes(n, nnz);
   k_diag_inv<<<g1, 256, 0, s>>>(n, rp, col, val, dinv);
   k_init<<<g1, 256, 0, s>>>(n, b, x, r, z, p, dinv);
   k_dot2<<<nblk, RT, 0, s>>>(n, r, z, r, r, partial);
@@ -266,7 +304,7 @@ extern "C" lmg_status lmg_cg_solve_noalloc(int64_t n, const int32_t *rp, const i
   int it = 0;
   if (bnorm > 0.0) {
     for (it = 0; it < maxit; ++it) {
-      k_spmv<<<gs, 256, 0, s>>>(n, rp, col, val, p, q);
+      launch_spmv(sg, gs, s, n, rp, col, val, p, q);
       k_dot2<<<nblk, RT, 0, s>>>(n, p, q, nullptr, nullptr, partial);
       k_dot2_final<<<1, RT, 0, s>>>(nblk, partial, sc + 2);  // sc[2] = pq
       k_update_xr<<<g1, 256, 0, s>>>(n, sc, x, r, z, p, q, dinv);
