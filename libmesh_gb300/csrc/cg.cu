@@ -3,9 +3,12 @@
 // (src/systems/linear_implicit_system.C:122-165; KSPCG as set up in
 // systems_of_equations_ex6.C:90-100; Eigen CG semantics in
 // src/solvers/eigen_sparse_linear_solver.C:132-170).  Stops when
-// ||r||_2 <= rtol ||b||_2.  Every reduction is a fixed two-stage tree, so
-// repeated solves give identical iterates.  Scalars stay on the device; the
-// host reads the residual every few iterations.
+// ||r||_2 <= rtol ||b||_2.  An iteration is three launches: the product
+// q = A p fused with p.q, the x / r / z update fused with r.z and r.r, and the
+// p update.  Every reduction is a fixed two-stage tree (block sums, then the
+// last block to finish sums the partials in block order), so repeated solves
+// give identical iterates.  Scalars stay on the device; the host reads the
+// residual every 16 iterations.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -21,7 +24,7 @@ namespace lmg {
 namespace {
 
 constexpr int RT = 256;      // threads per reduction block
-constexpr int RBLK = 1024;   // reduction blocks
+constexpr int RBLK = 16384;  // reduction blocks (largest grid of a reducing kernel)
 
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
@@ -41,47 +44,6 @@ __device__ __forceinline__ double block_sum(double v) {
   }
   __syncthreads();
   return s;  // valid in thread 0
-}
-
-// y = A x, G lanes per row (32 / G rows per warp and pass), G chosen from the
-// mean row length so that every lane has a few entries and a warp keeps
-// several rows' loads in flight.  The loop bound is warp-uniform so that the
-// shuffles see every lane.
-template <int G>
-__global__ void k_spmv(int64_t n, const int32_t *__restrict__ rp, const int32_t *__restrict__ col,
-                       const double *__restrict__ val, const double *__restrict__ x, double *__restrict__ y) {
-  constexpr int RPW = 32 / G;  // rows per warp and pass
-  const int lane = threadIdx.x & 31, sub = lane & (G - 1), grp = lane / G;
-  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int64_t n_warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t w0 = warp * RPW; w0 < n; w0 += n_warps * RPW) {
-    const int64_t r = w0 + grp;
-    double s = 0.0;
-    if (r < n) {
-      const int32_t b = __ldg(rp + r), e = __ldg(rp + r + 1);
-#pragma unroll 4
-      for (int32_t k = b + sub; k < e; k += G) s += __ldg(val + k) * __ldg(x + __ldg(col + k));
-    }
-#pragma unroll
-    for (int o = G / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, G);
-    if (r < n && sub == 0) y[r] = s;
-  }
-}
-
-// lanes per row for a mean row length
-inline int spmv_lanes(int64_t n, int64_t nnz) {
-  const int64_t m = n > 0 ? nnz / n : 0;
-  return m <= 16 ? 4 : (m <= 32 ? 8 : (m <= 64 ? 16 : 32));
-}
-
-void launch_spmv(int g, int grid, cudaStream_t s, int64_t n, const int32_t *rp, const int32_t *col, const double *val,
-                 const double *x, double *y) {
-  switch (g) {
-    case 4: k_spmv<4><<<grid, 256, 0, s>>>(n, rp, col, val, x, y); break;
-    case 8: k_spmv<8><<<grid, 256, 0, s>>>(n, rp, col, val, x, y); break;
-    case 16: k_spmv<16><<<grid, 256, 0, s>>>(n, rp, col, val, x, y); break;
-    default: k_spmv<32><<<grid, 256, 0, s>>>(n, rp, col, val, x, y); break;
-  }
 }
 
 // partial[b] for two dot products at once: (x1.y1, x2.y2)
@@ -123,23 +85,126 @@ __global__ void k_diag_inv(int64_t n, const int32_t *rp, const int32_t *col, con
   }
 }
 
-// x += a p; r -= a q; z = dinv r   with a = rz / pq read from the device
-__global__ void k_update_xr(int64_t n, const double *sc, double *x, double *r, double *z, const double *p,
-                            const double *q, const double *dinv) {
-  const double a = sc[0] / sc[2];
+// The last block to finish a reducing kernel sums the per-block partials in
+// block order (the order does not depend on which block came last), so the
+// reductions stay deterministic without a second launch.
+__device__ __forceinline__ bool last_block(unsigned int *cnt) {
+  __shared__ bool last;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    last = atomicAdd(cnt, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  return last;
+}
+
+// q = A p (G lanes per row) and pq = p.q: per-block partials, the last block
+// writes sc[2] = pq and resets the counter.
+template <int G>
+__global__ void __launch_bounds__(RT) k_spmv_pq(int64_t n, const int32_t *__restrict__ rp,
+                                                 const int32_t *__restrict__ col, const double *__restrict__ val,
+                                                 const double *__restrict__ p, double *__restrict__ q,
+                                                 double *partial, double *sc, unsigned int *cnt) {
+  constexpr int RPW = 32 / G;
+  const int lane = threadIdx.x & 31, sub = lane & (G - 1), grp = lane / G;
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t n_warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  double pq = 0.0;
+  for (int64_t w0 = warp * RPW; w0 < n; w0 += n_warps * RPW) {
+    const int64_t r = w0 + grp;
+    double s = 0.0;
+    if (r < n) {
+      const int32_t b = __ldg(rp + r), e = __ldg(rp + r + 1);
+#pragma unroll 4
+      for (int32_t k = b + sub; k < e; k += G) s += __ldg(val + k) * __ldg(p + __ldg(col + k));
+    }
+#pragma unroll
+    for (int o = G / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, G);
+    if (r < n && sub == 0) {
+      q[r] = s;
+      pq += p[r] * s;
+    }
+  }
+  pq = block_sum(pq);
+  if (threadIdx.x == 0) partial[blockIdx.x] = pq;
+  if (last_block(cnt)) {
+    double t = 0.0;
+    const volatile double *vp = partial;
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += RT) t += vp[i];
+    t = block_sum(t);
+    if (threadIdx.x == 0) {
+      sc[2] = t;
+      *cnt = 0u;
+    }
+  }
+}
+
+// x += a p; r -= a q; z = dinv r with a = rz / pq, rz = sc[cur]; then
+// rz_new = r.z into sc[1 - cur] and rr = r.r into sc[3] (last block).
+__global__ void __launch_bounds__(RT) k_update_xr_dots(int64_t n, double *sc, int cur, double *x, double *r,
+                                                        double *z, const double *p, const double *q,
+                                                        const double *dinv, double *partial, unsigned int *cnt) {
+  const double a = sc[cur] / sc[2];
+  double rz = 0.0, rr = 0.0;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     x[i] += a * p[i];
     const double ri = r[i] - a * q[i];
     r[i] = ri;
-    z[i] = dinv[i] * ri;
+    const double zi = dinv[i] * ri;
+    z[i] = zi;
+    rz += ri * zi;
+    rr += ri * ri;
+  }
+  rz = block_sum(rz);
+  rr = block_sum(rr);
+  if (threadIdx.x == 0) {
+    partial[2 * blockIdx.x] = rz;
+    partial[2 * blockIdx.x + 1] = rr;
+  }
+  if (last_block(cnt)) {
+    double t1 = 0.0, t2 = 0.0;
+    const volatile double *vp = partial;
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += RT) {
+      t1 += vp[2 * i];
+      t2 += vp[2 * i + 1];
+    }
+    t1 = block_sum(t1);
+    t2 = block_sum(t2);
+    if (threadIdx.x == 0) {
+      sc[1 - cur] = t1;
+      sc[3] = t2;
+      *cnt = 0u;
+    }
   }
 }
 
-// p = z + (rz_new / rz) p ; rz <- rz_new
-__global__ void k_update_p(int64_t n, double *sc, double *p, const double *z) {
-  const double b = sc[3] / sc[0];
+// p = z + (rz_new / rz) p with rz = sc[cur], rz_new = sc[1 - cur]
+__global__ void k_update_p2(int64_t n, const double *sc, int cur, double *p, const double *z) {
+  const double b = sc[1 - cur] / sc[cur];
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
     p[i] = z[i] + b * p[i];
+}
+
+// Lanes per row of the product for a mean row length (measured on the
+// 27-point Q1 pattern of 129^3 nodes: 4 lanes 152 us, 8 lanes 322 us, 32 lanes
+// 846 us per product).
+inline int spmv_lanes(int64_t n, int64_t nnz) {
+  const int64_t m = n > 0 ? nnz / n : 0;
+  return m <= 48 ? 4 : (m <= 128 ? 8 : 16);
+}
+
+// One CG iteration in three launches, shared by both solvers.
+void cg_iteration(int sg, int gs, int g1, cudaStream_t s, int64_t n, const int32_t *rp, const int32_t *col,
+                  const double *val, double *x, double *r, double *z, double *p, double *q, const double *dinv,
+                  double *partial, double *sc, unsigned int *cnt, int cur) {
+  switch (sg) {
+    case 4: k_spmv_pq<4><<<gs, RT, 0, s>>>(n, rp, col, val, p, q, partial, sc, cnt); break;
+    case 8: k_spmv_pq<8><<<gs, RT, 0, s>>>(n, rp, col, val, p, q, partial, sc, cnt); break;
+    default: k_spmv_pq<16><<<gs, RT, 0, s>>>(n, rp, col, val, p, q, partial, sc, cnt); break;
+  }
+  k_update_xr_dots<<<g1, RT, 0, s>>>(n, sc, cur, x, r, z, p, q, dinv, partial, cnt + 1);
+  k_update_p2<<<g1, 256, 0, s>>>(n, sc, cur, p, z);
 }
 
 __global__ void k_init(int64_t n, const double *b, double *x, double *r, double *z, double *p, const double *dinv) {
@@ -151,13 +216,10 @@ __global__ void k_init(int64_t n, const double *b, double *x, double *r, double 
   }
 }
 
-__global__ void k_copy2(double *dst, const double *src) {
-  dst[0] = src[0];
-}
-
 }  // namespace
 
-// sc layout: [0] rz, [1] rr, [2] pq, [3] rz_new, [4] rr_new
+// sc layout: [0], [1] rz of the current / next iteration (the initial rr in
+// [1]), [2] pq, [3] rr, [4] two block counters of the reducing kernels
 int cg_solve(int64_t n, const int32_t *rp, const int32_t *col, const double *val, const double *b, double *x,
              double rtol, int maxit, cudaStream_t s, int n_sm, int *iters, double *relres, int64_t *launches) {
   double *r, *z, *p, *q, *dinv, *partial, *sc;
@@ -165,7 +227,9 @@ int cg_solve(int64_t n, const int32_t *rp, const int32_t *col, const double *val
   if (cudaMalloc(&r, bytes) || cudaMalloc(&z, bytes) || cudaMalloc(&p, bytes) || cudaMalloc(&q, bytes) ||
       cudaMalloc(&dinv, bytes) || cudaMalloc(&partial, sizeof(double) * 2 * RBLK) || cudaMalloc(&sc, sizeof(double) * 8))
     return 7;
-  const int g1 = n_sm * 8, gs = n_sm * 16;
+  cudaMemsetAsync(sc, 0, sizeof(double) * 8, s);  // sc[4] holds the two block counters
+  unsigned int *cnt = reinterpret_cast<unsigned int *>(sc + 4);
+  const int g1 = n_sm * 8, gs = n_sm * 64;
   int nblk = (int)std::min<int64_t>(RBLK, (n + RT - 1) / RT);
   int64_t L = 0;
   int32_t nnz = 0;
@@ -188,17 +252,10 @@ int cg_solve(int64_t n, const int32_t *rp, const int32_t *col, const double *val
     *relres = 0.0;
   } else {
     for (it = 0; it < maxit; ++it) {
-      launch_spmv(sg, gs, s, n, rp, col, val, p, q);
-      k_dot2<<<nblk, RT, 0, s>>>(n, p, q, nullptr, nullptr, partial);
-      k_dot2_final<<<1, RT, 0, s>>>(nblk, partial, sc + 2);  // sc[2] = pq
-      k_update_xr<<<g1, 256, 0, s>>>(n, sc, x, r, z, p, q, dinv);
-      k_dot2<<<nblk, RT, 0, s>>>(n, r, z, r, r, partial);
-      k_dot2_final<<<1, RT, 0, s>>>(nblk, partial, sc + 3);  // sc[3] = rz_new, sc[4] = rr
-      k_update_p<<<g1, 256, 0, s>>>(n, sc, p, z);
-      k_copy2<<<1, 1, 0, s>>>(sc, sc + 3);                   // rz <- rz_new
-      L += 8;
+      cg_iteration(sg, gs, g1, s, n, rp, col, val, x, r, z, p, q, dinv, partial, sc, cnt, it & 1);
+      L += 3;
       if ((it + 1) % 16 == 0 || it + 1 == maxit) {
-        cudaMemcpyAsync(h, sc + 4, sizeof(double), cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(h, sc + 3, sizeof(double), cudaMemcpyDeviceToHost, s);
         cudaStreamSynchronize(s);
         rn = std::sqrt(h[0]);
         if (!(rn > rtol * bnorm)) { ++it; break; }
@@ -284,7 +341,7 @@ extern "C" lmg_status lmg_cg_solve_noalloc(int64_t n, const int32_t *rp, const i
   // The scalar slots start every call at zero; every other word is written before it is read.
   if (cudaMemsetAsync(sc, 0, sizeof(double) * 8, s) != cudaSuccess)
     return na_fail(msg, msg_len, LMG_ERR_CUDA, "cg_solve_noalloc: clearing the scalar slots failed");
-  const int g1 = n_sm * 8, gs = n_sm * 16;
+  const int g1 = n_sm * 8, gs = n_sm * 64;
   const int nblk = (int)std::min<int64_t>(RBLK, (n + RT - 1) / RT);
   int32_t nnz = 0;  // the row pointer's last entry sets the SpMV lane count
   if (cudaMemcpyAsync(&nnz, rp + n, sizeof(int32_t), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
@@ -303,17 +360,11 @@ extern "C" lmg_status lmg_cg_solve_noalloc(int64_t n, const int32_t *rp, const i
   double rn = bnorm;
   int it = 0;
   if (bnorm > 0.0) {
+    unsigned int *cnt = reinterpret_cast<unsigned int *>(sc + 4);  // cleared with the scalar slots
     for (it = 0; it < maxit; ++it) {
-      launch_spmv(sg, gs, s, n, rp, col, val, p, q);
-      k_dot2<<<nblk, RT, 0, s>>>(n, p, q, nullptr, nullptr, partial);
-      k_dot2_final<<<1, RT, 0, s>>>(nblk, partial, sc + 2);  // sc[2] = pq
-      k_update_xr<<<g1, 256, 0, s>>>(n, sc, x, r, z, p, q, dinv);
-      k_dot2<<<nblk, RT, 0, s>>>(n, r, z, r, r, partial);
-      k_dot2_final<<<1, RT, 0, s>>>(nblk, partial, sc + 3);  // sc[3] = rz_new, sc[4] = rr
-      k_update_p<<<g1, 256, 0, s>>>(n, sc, p, z);
-      k_copy2<<<1, 1, 0, s>>>(sc, sc + 3);                   // rz <- rz_new
+      cg_iteration(sg, gs, g1, s, n, rp, col, val, x, r, z, p, q, dinv, partial, sc, cnt, it & 1);
       if ((it + 1) % 16 == 0 || it + 1 == maxit) {
-        if (cudaMemcpyAsync(h, sc + 4, sizeof(double), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        if (cudaMemcpyAsync(h, sc + 3, sizeof(double), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
             cudaStreamSynchronize(s) != cudaSuccess)
           return na_fail(msg, msg_len, LMG_ERR_CUDA, "cg_solve_noalloc: device failure");
         rn = std::sqrt(h[0]);
