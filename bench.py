@@ -488,6 +488,26 @@ def main():
                  "value": world * mesh.n_elem / (ms32 * 1e-3) / 1e6, "unit": "Melem/s", "ms_per_step": ms32,
                  "speedup_vs_fp64": ms / ms32, "k_rel_frobenius_vs_fp64": krel}
 
+    # matrix-free residual R = K u - F (no K), against assembling K and one product
+    resid = None
+    if prec == lm.FP64:
+        ud = torch.randn(dm.n_dofs, dtype=torch.float64, device="cuda")
+        Rd = torch.empty(dm.n_dofs, dtype=torch.float64, device="cuda")
+        for _ in range(2):
+            asm.residual_device(ud.data_ptr(), Rd.data_ptr())
+        asm.synchronize()
+        ev0.record(stream)
+        for _ in range(args.steps):
+            asm.residual_device(ud.data_ptr(), Rd.data_ptr())
+        ev1.record(stream)
+        ev1.synchronize()
+        asm.synchronize()
+        rms = ev0.elapsed_time(ev1) / args.steps
+        resid = {"what": "R = K u - F without forming K (lmg_residual, device vectors)", "ms_per_step": rms,
+                 "value": world * mesh.n_elem / (rms * 1e-3) / 1e6, "unit": "Melem/s",
+                 "vs_assembly": ms / rms}
+        del ud, Rd
+
     # per-stage times (PerfLog events) for the roofline
     asm.perflog_enable(True)
     for _ in range(5):
@@ -576,7 +596,7 @@ def main():
                     "d2h_bytes_per_step": 8 * (asm.nnz + dm.n_dofs), "d2h_link_gbs": link_gbs,
                     "copy_floor_melem_s": mesh.n_elem / (8 * (asm.nnz + dm.n_dofs) / (link_gbs * 1e9)) / 1e6},
             "gpu_launches": launches, "clocks": clk, "roofline": dom, "cpu_baseline": cpu,
-            "mixed": other}))
+            "mixed": other, "residual": resid}))
     if dist:
         dist.destroy_process_group()
 

@@ -297,6 +297,15 @@ lmg_status lmg_cg_solve_noalloc(int64_t n_dofs, const int32_t *row_ptr, const in
                                 int32_t maxit, void *stream, int32_t *iters, double *relres,
                                 char *msg, int32_t msg_len);
 
+/* R = K u - F for the current form and inputs without forming K: what
+ * LinearImplicitSystem::assembly computes as the residual (R = A u - b,
+ * src/systems/linear_implicit_system.C:367-381) on the assembled,
+ * constrained system (a Dirichlet row gives (elements touching the dof) * u_i).
+ * Affine elements of the block path (POISSON, ELASTICITY), FP64 arithmetic as
+ * the drop-in's (double-float contraction).  u, R [n_dofs] are host arrays, or
+ * device arrays when on_device = 1 (then the call returns asynchronously). */
+lmg_status lmg_residual(lmg_ctx *ctx, const double *u, double *R, int32_t on_device);
+
 /* Adjoint sensitivities (ImplicitSystem::adjoint_qoi_parameter_sensitivity,
  * src/systems/implicit_system.C:517-623, with the element coefficients of the
  * form as parameters; ParameterVector, src/systems/parameter_vector.C:28-132).

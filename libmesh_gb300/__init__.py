@@ -270,6 +270,16 @@ class GpuAssembly:
                                     ptr(np.ascontiguousarray(z, np.float64)), ptr(g)))
         return g
 
+    def residual(self, u):
+        """R = K u - F without forming K (affine elements of the block path)."""
+        R = np.empty(self.dof_map.n_dofs, np.float64)
+        self._ok(lib().lmg_residual(self.ctx, ptr(np.ascontiguousarray(u, np.float64)), ptr(R), 0))
+        return R
+
+    def residual_device(self, u_dev, R_dev):
+        """The same on device vectors (raw pointers); asynchronous."""
+        self._ok(lib().lmg_residual(self.ctx, C.c_void_p(u_dev), C.c_void_p(R_dev), 1))
+
     def vjp_xyz(self, u, z, in_region=None):
         """dq/dx for every node coordinate (Poisson form): [n_nodes, 3]."""
         g = np.empty((self.mesh.n_nodes, 3), np.float64)

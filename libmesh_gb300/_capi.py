@@ -64,6 +64,7 @@ SIGNATURES = {
     "lmg_cg_solve_noalloc": [_i64, _p, _p, _p, _p, _p, _f64, _i32, _p, _pi32, _pf64, C.c_char_p, _i32],
     "lmg_qoi_region_load": [_p, _p, _p],
     "lmg_vjp_coef": [_p, _p, _p, _p],
+    "lmg_residual": [_p, _p, _p, _i32],
     "lmg_vjp_xyz": [_p, _p, _p, _p, _p],
     "lmg_perflog_enable": [_p, _i32],
     "lmg_perflog_read": [_p, _pf64, _pf64, _pi64],

@@ -42,6 +42,11 @@ struct ElemArgs {
   int *status;                // [0] error code
   unsigned long long *bad_elem;  // first failing element id
   DevFE fe;
+  // matrix-free residual (k_residual_affine): element block ids, the vector
+  // u [n_dofs] and the per-element residual R_e = K_e u_e - F_e [n_elem][N][nv]
+  const int32_t *eb;
+  const double *u;
+  float2 *Re2;
 };
 
 // Fused mixed assembly (element contraction and insertion in one row kernel).
@@ -122,6 +127,10 @@ bool fused_built(int form, int n, int nv);
 bool launch_fused_mixed(int form, int n, int nv, const FusedArgs &f, int grid, cudaStream_t s, bool geo = true,
                         bool rows = true);
 bool elements_built(int form, int n, int nv);
+// R = K u - F without K (affine elements): residual kernel, then the per-dof
+// sums over the load-vector plan; false when no kernel is built for the form.
+bool launch_residual(int form, int n, int nv, const ElemArgs &a, int64_t n_brows, const int32_t *fptr,
+                     const int32_t *fcontrib, double *R, int grid, cudaStream_t s);
 void launch_elements(int form, int n, int nv, bool affine, bool mixed, const ElemArgs &a, int grid,
                      cudaStream_t s);
 bool gather_built(int bs);

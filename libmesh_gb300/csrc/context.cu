@@ -416,6 +416,7 @@ lmg_status lmg_context_destroy(lmg_ctx *c) {
   general_free(c);
   hier3_free(c);
   dfree(c->d_D6); dfree(c->d_modes);
+  dfree(c->d_Re2);
   for (cudaEvent_t e : c->chunk_ev) cudaEventDestroy(e);
   if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
@@ -1030,6 +1031,54 @@ lmg_status lmg_vjp_coef(lmg_ctx *c, const double *u, const double *z, double *dq
   dfree(du);
   dfree(dz);
   dfree(dout);
+  return st;
+}
+
+lmg_status lmg_residual(lmg_ctx *c, const double *u, double *R, int32_t on_device) {
+  if (!c || !u || !R) return fail(c, LMG_ERR_ARG, "residual: bad argument");
+  if (!c->have_sparsity || !c->have_form) return fail(c, LMG_ERR_STATE, "residual: set up the system first");
+  if (c->general || !c->h_gen.empty())
+    return fail(c, LMG_ERR_UNSUPPORTED, "residual: built for affine elements of the block path");
+  cudaSetDevice(c->device);
+  if (!c->d_Re2) LMG_CUDA(c, dalloc(c->d_Re2, (size_t)(c->n_elem * c->nl)));
+  double *du = nullptr, *dR = nullptr;
+  if (on_device) {
+    du = const_cast<double *>(u);
+    dR = R;
+  } else {
+    LMG_CUDA(c, dalloc(du, (size_t)c->n_dofs));
+    LMG_CUDA(c, dalloc(dR, (size_t)c->n_dofs));
+    LMG_CUDA(c, cudaMemcpyAsync(du, u, sizeof(double) * c->n_dofs, cudaMemcpyHostToDevice, c->stream));
+  }
+  lmg_status st = reset_status(c);
+  if (st) return st;
+  ElemArgs a{};
+  a.n_list = (int64_t)c->h_aff.size();
+  a.list = c->d_aff;
+  a.npe = c->npe;
+  a.xyz = c->d_xyz;
+  a.conn = c->d_conn;
+  a.coef = c->d_coef;
+  a.nodal_f = c->d_f;
+  a.nodal_f2 = c->d_f2;
+  a.cmask = c->d_cmask;
+  a.nu = c->nu;
+  a.status = c->d_status;
+  a.bad_elem = c->d_bad;
+  a.fe = c->dfe;
+  a.eb = c->d_eb;
+  a.u = du;
+  a.Re2 = c->d_Re2;
+  if (!launch_residual(c->form, c->tab.n, c->n_vars, a, c->n_blocks, c->d_fptr, c->d_fcontrib, dR,
+                       c->n_sm * c->ctas_per_sm, c->stream))
+    return fail(c, LMG_ERR_UNSUPPORTED, "residual: no kernel for this form / element");
+  c->launches += 2;
+  LMG_CUDA(c, cudaGetLastError());
+  if (on_device) return LMG_OK;
+  LMG_CUDA(c, cudaMemcpyAsync(R, dR, sizeof(double) * c->n_dofs, cudaMemcpyDeviceToHost, c->stream));
+  st = check_status(c, "residual");
+  dfree(du);
+  dfree(dR);
   return st;
 }
 

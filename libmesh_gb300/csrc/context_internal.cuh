@@ -62,6 +62,7 @@ struct lmg_ctx {
   // work and result buffers
   float2 *d_Kdiag2 = nullptr, *d_Koff2 = nullptr;
   float2 *d_Fe2 = nullptr;
+  float2 *d_Re2 = nullptr;  // per-element residuals of lmg_residual
   double *d_K = nullptr, *d_F = nullptr;
   float *d_Koff32 = nullptr;
   int *d_status = nullptr;

@@ -326,6 +326,169 @@ __global__ void __launch_bounds__(128) k_elem_affine(ElemArgs a) {
   }
 }
 
+// Matrix-free residual R = K u - F without forming K (affine elements, the
+// FP64 drop-in's arithmetic): LinearImplicitSystem::assembly's residual
+// (src/systems/linear_implicit_system.C:367-381) as a per-element product.
+// A warp takes 32 elements: lane = element for the FP64 map, the element's
+// operands, its u_e and its load vector (the same code as k_elem_affine);
+// then lanes (slot, a) take SL = 32 / N elements at a time, lane a forming
+// row block a of K_e from the reference tensors and multiplying it into u_e
+// in double-float.  Dirichlet rows / columns as the assembled matrix has them:
+// a constrained row gives u_a (its row is e_a), a constrained column adds
+// nothing.  R_e goes to Re2 and is summed per dof by the load-vector plan.
+template <int FORM, int N, int NV>
+struct ResidualSmem {
+  static constexpr int NG = Geo<FORM>::NG;
+  static constexpr size_t S = 0;                                        // [9][N][N] float2
+  static constexpr size_t M = S + al16(sizeof(float2) * 9 * N * N);     // [N][N] float2
+  static constexpr size_t G = M + al16(sizeof(float2) * N * N);         // [4][32][NG] float2
+  static constexpr size_t MASK = G + al16(sizeof(float2) * 4 * 32 * NG);  // [4][32] u64
+  static constexpr size_t U = MASK + al16(sizeof(uint64_t) * 4 * 32);  // [4][32][N*NV] float2
+  static constexpr size_t BYTES = U + al16(sizeof(float2) * 4 * 32 * N * NV);
+};
+
+template <int FORM, int N, int NV>
+__global__ void __launch_bounds__(128) k_residual_affine(ElemArgs a) {
+  using R = Ar<float2>;
+  using V = DF;
+  constexpr int NG = Geo<FORM>::NG, NB = N * N, SL = 32 / N, NL = N * NV;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  using L = ResidualSmem<FORM, N, NV>;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  float2 *sS = reinterpret_cast<float2 *>(smem_raw + L::S);
+  float2 *sM = reinterpret_cast<float2 *>(smem_raw + L::M);
+  float2 *sG = reinterpret_cast<float2 *>(smem_raw + L::G) + warp * 32 * NG;
+  uint64_t *sMask = reinterpret_cast<uint64_t *>(smem_raw + L::MASK) + warp * 32;
+  float2 *sU = reinterpret_cast<float2 *>(smem_raw + L::U) + warp * 32 * NL;
+  for (int i = threadIdx.x; i < 9 * NB; i += blockDim.x) st(sS[i], R::from(a.fe.S[i]));
+  for (int i = threadIdx.x; i < NB; i += blockDim.x) st(sM[i], df_split(a.fe.M[i]));
+  __syncthreads();
+  const int64_t n_tiles = (a.n_list + 31) / 32;
+  for (int64_t tile = (int64_t)blockIdx.x * 4 + warp; tile < n_tiles; tile += (int64_t)gridDim.x * 4) {
+    const int64_t li = tile * 32 + lane;
+    const int32_t e = (li < a.n_list) ? a.list[li] : -1;
+    if (e >= 0) {  // lane = element: FP64 geometry at qp 0 (compute_affine_map), u_e, F_e
+      const int32_t *c = a.conn + (int64_t)e * a.npe;
+      double G[9];
+      double det;
+      {
+        double X[N * 3];
+#pragma unroll
+        for (int g = 0; g < N; ++g) {
+          const double *p = a.xyz + 3 * (int64_t)c[g];
+          X[3 * g] = p[0];
+          X[3 * g + 1] = p[1];
+          X[3 * g + 2] = p[2];
+        }
+        det = jacobian(X, a.fe.gdphi, N, G);
+      }
+      if (!(det > 0.0)) report_bad(a, LMG_ERR_DEGENERATE, e);
+      const double coef = a.coef ? a.coef[e] : 1.0;
+      float2 *g = sG + lane * NG;
+      if (FORM == LMG_POISSON) {
+        const double s = coef * det;
+#pragma unroll
+        for (int m = 0; m < 3; ++m)
+#pragma unroll
+          for (int n = 0; n < 3; ++n)
+            st(g[3 * m + n], R::from(s * (G[3 * m] * G[3 * n] + G[3 * m + 1] * G[3 * n + 1] + G[3 * m + 2] * G[3 * n + 2])));
+      } else {
+        double lam, mu;
+        lame(coef, a.nu, lam, mu);
+#pragma unroll
+        for (int i = 0; i < 9; ++i) st(g[i], R::from(G[i]));
+        st(g[9], R::from(lam * det));
+        st(g[10], R::from(mu * det));
+      }
+      const uint64_t mask = a.cmask[e];
+      sMask[lane] = mask;
+      const int32_t *eb = a.eb + (int64_t)e * N;
+      for (int b = 0; b < N; ++b)
+#pragma unroll
+        for (int v = 0; v < NV; ++v) st(sU[lane * NL + b * NV + v], df_split(a.u[(int64_t)eb[b] * NV + v]));
+      // load vector Fe_a^i = detJ sum_b M_ab f_b^i (the element kernel's), into Re2
+      float2 *Fo = a.Re2 + (int64_t)e * NL;
+      const DF dd = df_split(det);
+      for (int ai = 0; ai < N; ++ai)
+#pragma unroll
+        for (int v = 0; v < NV; ++v) {
+          DF s = {0.f, 0.f};
+          if (a.nodal_f2)
+            for (int b = 0; b < N; ++b) {
+              const float2 fb = a.nodal_f2[(int64_t)c[b] * NV + v], mb = sM[ai * N + b];
+              s = df_fma_lazy(s, DF{mb.x, mb.y}, DF{fb.x, fb.y});
+            }
+          s = df_norm(df_fma_lazy(DF{0.f, 0.f}, df_norm(s), dd));
+          Fo[ai * NV + v] = ((mask >> (v * N + ai)) & 1ull) ? make_float2(0.f, 0.f) : make_float2(s.hi, s.lo);
+        }
+    }
+    __syncwarp();
+    const int slot = lane / N, ra = lane - slot * N;
+    for (int t0 = 0; t0 < 32; t0 += SL) {
+      const int t = t0 + slot;
+      const int32_t et = __shfl_sync(FULL, e, t < 32 ? t : 0);
+      if (slot < SL && t < 32 && et >= 0) {
+        const float2 *gt = sG + t * NG;
+        V gv[NG];
+#pragma unroll
+        for (int i = 0; i < NG; ++i) gv[i] = R::ld(gt[i]);
+        const uint64_t mask = sMask[t];
+        const float2 *ut = sU + t * NL;
+        V y[NV];
+#pragma unroll
+        for (int i = 0; i < NV; ++i) y[i] = R::zero();
+        for (int cb = 0; cb < N; ++cb) {
+          V sv[9];
+#pragma unroll
+          for (int mn = 0; mn < 9; ++mn) sv[mn] = R::ld(sS[mn * NB + ra * N + cb]);
+          V out[NV * NV];
+          contract_block<FORM, R>(gv, sv, out);
+#pragma unroll
+          for (int k = 0; k < NV; ++k) {
+            if ((mask >> (k * N + cb)) & 1ull) continue;  // constrained column
+            const V uk = R::ld(ut[cb * NV + k]);
+#pragma unroll
+            for (int i = 0; i < NV; ++i) y[i] = df_fma_lazy(y[i], out[i * NV + k], uk);
+          }
+        }
+        float2 *Ro = a.Re2 + (int64_t)et * NL + ra * NV;
+#pragma unroll
+        for (int i = 0; i < NV; ++i) {
+          V r = df_norm(y[i]);
+          if ((mask >> (i * N + ra)) & 1ull) r = R::ld(ut[ra * NV + i]);  // row e_a: u_a
+          const float2 f = Ro[i];
+          r = df_add(r, DF{-f.x, -f.y});
+          Ro[i] = make_float2(r.hi, r.lo);
+        }
+      }
+      __syncwarp();
+    }
+    __syncwarp();
+  }
+}
+
+template <int BS>
+__global__ void __launch_bounds__(256) k_gather_vec(int64_t n_brows, const int32_t *fptr, const int32_t *fcontrib,
+                                                    const float2 *Re2, double *R) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t P = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; P < n_brows;
+       P += ((int64_t)gridDim.x * blockDim.x) >> 5)
+    row_load_f<BS>(fptr, fcontrib, Re2, R, P, lane);
+}
+
+template <int FORM, int N, int NV>
+void launch_residual_t(const ElemArgs &a, int grid, cudaStream_t s) {
+  using L = ResidualSmem<FORM, N, NV>;
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_residual_affine<FORM, N, NV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L::BYTES);
+    attr = true;
+  }
+  const int64_t tiles = (a.n_list + 31) / 32, blocks = (tiles + 3) / 4;
+  const int g = (int)(blocks < grid ? blocks : grid);
+  if (g > 0) k_residual_affine<FORM, N, NV><<<g, 128, L::BYTES, s>>>(a);
+}
+
 template <int FORM, int N, int NV, typename T>
 __global__ void __launch_bounds__(128) k_elem_general(ElemArgs a) {
   constexpr bool MIXED = sizeof(T) == 4;
@@ -681,6 +844,34 @@ bool launch_fused_mixed(int form, int n, int nv, const FusedArgs &f, int grid, c
   LMG_F(LMG_ELASTICITY, 10, 3)
 #undef LMG_F
   return false;
+}
+
+bool launch_residual(int form, int n, int nv, const ElemArgs &a, int64_t n_brows, const int32_t *fptr,
+                     const int32_t *fcontrib, double *R, int grid, cudaStream_t s) {
+#define LMG_R(F, NN, V)                                   \
+  if (form == F && n == NN && nv == V) {                  \
+    launch_residual_t<F, NN, V>(a, grid, s);              \
+    ok = true;                                            \
+  }
+  bool ok = false;
+  LMG_R(LMG_POISSON, 4, 1)
+  LMG_R(LMG_POISSON, 6, 1)
+  LMG_R(LMG_POISSON, 8, 1)
+  LMG_R(LMG_POISSON, 10, 1)
+  LMG_R(LMG_POISSON, 27, 1)
+  LMG_R(LMG_ELASTICITY, 4, 3)
+  LMG_R(LMG_ELASTICITY, 6, 3)
+  LMG_R(LMG_ELASTICITY, 8, 3)
+  LMG_R(LMG_ELASTICITY, 10, 3)
+#undef LMG_R
+  if (!ok) return false;
+  const int64_t blocks = (n_brows * 32 + 255) / 256;
+  const int g = (int)(blocks < grid ? blocks : grid);
+  if (g > 0) {
+    if (nv == 3) k_gather_vec<3><<<g, 256, 0, s>>>(n_brows, fptr, fcontrib, a.Re2, R);
+    else k_gather_vec<1><<<g, 256, 0, s>>>(n_brows, fptr, fcontrib, a.Re2, R);
+  }
+  return true;
 }
 
 void launch_elements(int form, int n, int nv, bool affine, bool mixed, const ElemArgs &a, int grid,
