@@ -317,8 +317,10 @@ lmg_status lmg_residual(lmg_ctx *ctx, const double *u, double *R, int32_t on_dev
  * geometry recomputed per quadrature point.  u, z, q, dq_dcoef are host arrays. */
 lmg_status lmg_qoi_region_load(lmg_ctx *ctx, const uint8_t *in_region, double *q);
 lmg_status lmg_vjp_coef(lmg_ctx *ctx, const double *u, const double *z, double *dq_dcoef);
-/* Node-coordinate sensitivities of the same QoI (Poisson form; the reference's
- * ParameterVector over node coordinates): dq/dx = dq/dx|_u - z^T d(K u - F)/dx
+/* Node-coordinate sensitivities of the same QoI (Poisson and elasticity forms;
+ * for elasticity the QoI integrates the sum of u's components, as
+ * lmg_qoi_region_load's vector does; the reference's ParameterVector over node
+ * coordinates): dq/dx = dq/dx|_u - z^T d(K u - F)/dx
  * for every node, by reverse mode through detJ and J^{-1} at every quadrature
  * point.  in_region[n_elem] marks the QoI elements (NULL: no explicit term);
  * dq_dxyz [n_nodes][3]; all arrays on the host. */

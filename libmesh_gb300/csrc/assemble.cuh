@@ -105,7 +105,7 @@ struct VjpArgs {
   double nu;
   double *out;                // [n_elem] dq/dp_e
   const double *coef;         // [n_elem] or null (=1): element coefficients (coordinate sensitivities)
-  const double *nodal_f;      // [n_nodes] or null: Poisson load (coordinate sensitivities)
+  const double *nodal_f;      // [n_nodes][nv] or null: nodal load (coordinate sensitivities)
   double *xout;               // [n_elem][n][3] d q / d X of each element's nodes
   int64_t n_rows;             // rows of the per-dof gather
   const int32_t *fptr;        // [n_rows+1] incidences (e*n + a) of each dof row
@@ -117,8 +117,8 @@ struct VjpArgs {
   DevFE fe;
 };
 bool launch_vjp(int form, int n, int nv, bool region, const VjpArgs &v, int grid, cudaStream_t s);
-// Coordinate sensitivities of the Poisson form: element pass then per-dof gather.
-bool launch_vjp_xyz(int n, const VjpArgs &v, int grid, cudaStream_t s);
+// Coordinate sensitivities (Poisson and elasticity): element pass then per-node gather.
+bool launch_vjp_xyz(int form, int n, const VjpArgs &v, int grid, cudaStream_t s);
 void launch_gather_f(const GatherArgs &g, cudaStream_t s);
 
 // Whether an element kernel is instantiated for (form, shapes per variable, variables).

@@ -1084,8 +1084,9 @@ lmg_status lmg_residual(lmg_ctx *c, const double *u, double *R, int32_t on_devic
 
 lmg_status lmg_vjp_xyz(lmg_ctx *c, const double *u, const double *z, const uint8_t *in_region, double *dq_dxyz) {
   if (!c || !u || !z || !dq_dxyz) return fail(c, LMG_ERR_ARG, "vjp_xyz: bad argument");
-  if (c->general || c->form != LMG_POISSON || c->n_vars != 1)
-    return fail(c, LMG_ERR_UNSUPPORTED, "vjp_xyz: built for the Poisson form");
+  if (c->general || !((c->form == LMG_POISSON && c->n_vars == 1) || (c->form == LMG_ELASTICITY && c->n_vars == 3)) ||
+      c->bs != c->n_vars)
+    return fail(c, LMG_ERR_UNSUPPORTED, "vjp_xyz: built for the Poisson and elasticity forms");
   if (!c->have_sparsity || !c->have_form) return fail(c, LMG_ERR_STATE, "vjp_xyz: set up the system first");
   cudaSetDevice(c->device);
   double *du = nullptr, *dz = nullptr, *dx = nullptr, *drow = nullptr;
@@ -1108,7 +1109,7 @@ lmg_status lmg_vjp_xyz(lmg_ctx *c, const double *u, const double *z, const uint8
   v.fptr = c->d_fptr;
   v.fcontrib = c->d_fcontrib;
   v.row_out = drow;
-  if (!launch_vjp_xyz(c->tab.n, v, c->n_sm * 8, c->stream))
+  if (!launch_vjp_xyz(c->form, c->tab.n, v, c->n_sm * 8, c->stream))
     return fail(c, LMG_ERR_UNSUPPORTED, "vjp_xyz: element not built");
   c->launches += 2;
   LMG_CUDA(c, cudaGetLastError());
@@ -1118,10 +1119,10 @@ lmg_status lmg_vjp_xyz(lmg_ctx *c, const double *u, const double *z, const uint8
   dfree(du); dfree(dz); dfree(dreg); dfree(dx); dfree(drow);
   if (st) return st;
   std::fill(dq_dxyz, dq_dxyz + 3 * c->n_nodes, 0.0);
-  for (int64_t e = 0; e < c->n_elem; ++e)  // node of every dof (one variable)
+  for (int64_t e = 0; e < c->n_elem; ++e)  // node of every block row
     for (int a = 0; a < c->npe; ++a) {
-      const int64_t node = c->h_conn[(size_t)(e * c->npe + a)], dof = c->h_elem_dofs[(size_t)(e * c->nl + a)];
-      for (int d = 0; d < 3; ++d) dq_dxyz[3 * node + d] = row[(size_t)(3 * dof + d)];
+      const int64_t node = c->h_conn[(size_t)(e * c->npe + a)], blk = c->h_eb[(size_t)(e * c->nb + a)];
+      for (int d = 0; d < 3; ++d) dq_dxyz[3 * node + d] = row[(size_t)(3 * blk + d)];
     }
   return LMG_OK;
 }

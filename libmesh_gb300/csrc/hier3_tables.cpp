@@ -27,8 +27,6 @@ namespace lmg {
 
 namespace {
 
-struct P3 { double v[3]; };
-
 bool pt_less(const double *a, const double *b) {  // TypeVector::operator<
   for (int i = 0; i < 3; i++) {
     if (a[i] < b[i]) return true;

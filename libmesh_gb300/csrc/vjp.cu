@@ -244,6 +244,109 @@ __global__ void k_vjp_xyz(VjpArgs v) {
   }
 }
 
+// Coordinate sensitivities of the elasticity form, the same reverse mode: per
+// quadrature point, with P_u = grad u, P_z = grad z (3 x 3, rows = components),
+//   W = lam tr P_z tr P_u + mu sum_ij P_z,ij (P_u,ij + P_u,ji)
+//   S_u = dW/dP_u = lam tr P_z I + mu (P_z + P_z^T),  S_z likewise,
+//   d P_u,kd / dJ_en = -G_nd P_u,ke,
+// so -dW/dJ_en = sum_k (S_u G^T)_kn P_u,ke + (S_z G^T)_kn P_z,ke; the QoI is the
+// integral of the sum of u's components over the marked elements and the load
+// term sum_k f_k z_k (what k_region_fe and the element kernel use).
+template <int N>
+__global__ void k_vjp_xyz_el(VjpArgs v) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < v.n_elem;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    double X[N * 3], dX[N * 3];
+    const int32_t *c = v.conn + e * N;
+#pragma unroll
+    for (int a = 0; a < N; ++a)
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        X[3 * a + d] = v.xyz[3 * (int64_t)c[a] + d];
+        dX[3 * a + d] = 0.0;
+      }
+    const double E = v.coef ? v.coef[e] : 1.0;
+    const double lam = (E * v.nu) / ((1. + v.nu) * (1. - 2. * v.nu)), mu = E / (2. * (1. + v.nu));
+    const bool in_q = v.region && v.region[e];
+    bool bad = false;
+    for (int q = 0; q < v.fe.q; ++q) {
+      const double *gd = v.fe.gdphi + (int64_t)q * N * 3;
+      double G[9];
+      const double det = jac_inv(X, gd, N, G);
+      bad |= !(det > 0.0);
+      const double *dp = v.fe.dphi + (int64_t)q * N * 3, *ph = v.fe.phi + (int64_t)q * N;
+      double gu[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, gz[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};  // [k][m]
+      double usum = 0.0, fz = 0.0;
+      double fq[3] = {0.0, 0.0, 0.0}, zq[3] = {0.0, 0.0, 0.0};
+      for (int a = 0; a < N; ++a) {
+        const int64_t b3 = (int64_t)v.eb[e * N + a] * 3;
+        const double pa = ph[a];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          const double uk = v.u[b3 + k], zk = v.z[b3 + k];
+#pragma unroll
+          for (int m = 0; m < 3; ++m) {
+            gu[3 * k + m] += dp[3 * a + m] * uk;
+            gz[3 * k + m] += dp[3 * a + m] * zk;
+          }
+          usum += pa * uk;
+          zq[k] += pa * zk;
+          if (v.nodal_f) fq[k] += pa * v.nodal_f[3 * (int64_t)c[a] + k];
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < 3; ++k) fz += fq[k] * zq[k];
+      double Pu[9], Pz[9];  // [k][d] = sum_m G[3m+d] g[k][m]
+#pragma unroll
+      for (int k = 0; k < 3; ++k)
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          Pu[3 * k + d] = G[d] * gu[3 * k] + G[3 + d] * gu[3 * k + 1] + G[6 + d] * gu[3 * k + 2];
+          Pz[3 * k + d] = G[d] * gz[3 * k] + G[3 + d] * gz[3 * k + 1] + G[6 + d] * gz[3 * k + 2];
+        }
+      const double tu = Pu[0] + Pu[4] + Pu[8], tz = Pz[0] + Pz[4] + Pz[8];
+      double W = lam * tz * tu;
+      double Su[9], Sz[9];
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          W += mu * Pz[3 * i + j] * (Pu[3 * i + j] + Pu[3 * j + i]);
+          Su[3 * i + j] = mu * (Pz[3 * i + j] + Pz[3 * j + i]) + (i == j ? lam * tz : 0.0);
+          Sz[3 * i + j] = mu * (Pu[3 * i + j] + Pu[3 * j + i]) + (i == j ? lam * tu : 0.0);
+        }
+      const double jw = det * v.fe.qw[q];
+      const double scal = (in_q ? jw * usum : 0.0) - jw * W + jw * fz;
+      // SG[k][n] = sum_d S[k][d] G[3n+d]
+      double SGu[9], SGz[9];
+#pragma unroll
+      for (int k = 0; k < 3; ++k)
+#pragma unroll
+        for (int n = 0; n < 3; ++n) {
+          SGu[3 * k + n] = Su[3 * k] * G[3 * n] + Su[3 * k + 1] * G[3 * n + 1] + Su[3 * k + 2] * G[3 * n + 2];
+          SGz[3 * k + n] = Sz[3 * k] * G[3 * n] + Sz[3 * k + 1] * G[3 * n + 1] + Sz[3 * k + 2] * G[3 * n + 2];
+        }
+#pragma unroll
+      for (int ee = 0; ee < 3; ++ee)
+#pragma unroll
+        for (int n = 0; n < 3; ++n) {
+          double dw = 0.0;
+#pragma unroll
+          for (int k = 0; k < 3; ++k) dw += SGu[3 * k + n] * Pu[3 * k + ee] + SGz[3 * k + n] * Pz[3 * k + ee];
+          const double cj = G[3 * n + ee] * scal + jw * dw;
+#pragma unroll
+          for (int a = 0; a < N; ++a) dX[3 * a + ee] += cj * gd[3 * a + n];
+        }
+    }
+    if (bad) {
+      atomicCAS(v.status, 0, LMG_ERR_DEGENERATE);
+      atomicMin(v.bad_elem, (unsigned long long)e);
+    }
+#pragma unroll
+    for (int i = 0; i < N * 3; ++i) v.xout[e * N * 3 + i] = dX[i];
+  }
+}
+
 // Per-dof sums of the element node contributions, in element order.
 __global__ void k_gather_xyz(VjpArgs v) {
   for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < v.n_rows;
@@ -269,10 +372,16 @@ void launch_v(bool region, const VjpArgs &v, int grid, cudaStream_t s) {
 
 }  // namespace
 
-bool launch_vjp_xyz(int n, const VjpArgs &v, int grid, cudaStream_t s) {
+bool launch_vjp_xyz(int form, int n, const VjpArgs &v, int grid, cudaStream_t s) {
   const int64_t blocks = (v.n_elem + 127) / 128;
   const int g = (int)(blocks < grid ? blocks : grid);
-  if (n == 4) k_vjp_xyz<4><<<g, 128, 0, s>>>(v);
+  if (form == LMG_ELASTICITY) {
+    if (n == 4) k_vjp_xyz_el<4><<<g, 128, 0, s>>>(v);
+    else if (n == 6) k_vjp_xyz_el<6><<<g, 128, 0, s>>>(v);
+    else if (n == 8) k_vjp_xyz_el<8><<<g, 128, 0, s>>>(v);
+    else if (n == 10) k_vjp_xyz_el<10><<<g, 128, 0, s>>>(v);
+    else return false;
+  } else if (n == 4) k_vjp_xyz<4><<<g, 128, 0, s>>>(v);
   else if (n == 6) k_vjp_xyz<6><<<g, 128, 0, s>>>(v);
   else if (n == 8) k_vjp_xyz<8><<<g, 128, 0, s>>>(v);
   else if (n == 10) k_vjp_xyz<10><<<g, 128, 0, s>>>(v);

@@ -235,28 +235,29 @@ def adjoint_qoi_parameter_sensitivity(form, elem_type, fe_order, q_order, xyz, c
 
 
 def coordinate_sensitivity(form, elem_type, fe_order, q_order, xyz, conn, elem_dofs, n_dofs, constrained, row_ptr,
-                           col, coef, nodal_f, in_region, params):
+                           col, coef, nodal_f, in_region, params, n_vars=1):
     """adjoint_qoi_parameter_sensitivity (src/systems/implicit_system.C:474-623)
     with node coordinates as the ParameterVector: params = [(node, direction)].
     For each p = xyz[node, direction]: delta = 1e-6 max(|p|, 1e-3);
     dq/dp = (q(u; p+d) - q(u; p-d)) / 2d at the fixed primal u (the QoI is the
     integral of u over the marked elements, so it moves with the geometry);
     -dR/dp = (R(p-d) - R(p+d)) / 2d with R = K u - F;
-    sensitivity = dq/dp + (-dR/dp) . z.  Scalar forms, small meshes."""
+    sensitivity = dq/dp + (-dR/dp) . z.  n_vars = 3 (elasticity): the QoI
+    integrates the sum of the components.  Small meshes."""
     import scipy.sparse as sp
     import scipy.sparse.linalg as spla
     n = n_dofs
     sel = np.nonzero(np.asarray(in_region) != 0)[0]
 
     def system(x):
-        K, F, st, _ = assemble(form, elem_type, fe_order, q_order, x, conn, 1, elem_dofs, n_dofs, constrained,
+        K, F, st, _ = assemble(form, elem_type, fe_order, q_order, x, conn, n_vars, elem_dofs, n_dofs, constrained,
                                row_ptr, col, coef=coef, nodal_f=nodal_f)
         assert st == 0
         return sp.csr_matrix((K, col, row_ptr), shape=(n, n)), F
 
     def qload(x):
-        ones = np.ones((x.shape[0], 1))
-        _, qv, st, _ = assemble(form, elem_type, fe_order, q_order, x, conn[sel], 1, elem_dofs[sel], n_dofs,
+        ones = np.ones((x.shape[0], n_vars))
+        _, qv, st, _ = assemble(form, elem_type, fe_order, q_order, x, conn[sel], n_vars, elem_dofs[sel], n_dofs,
                                 np.zeros(n_dofs, np.uint8), row_ptr, col, coef=coef[sel], nodal_f=ones)
         assert st == 0
         qv[np.asarray(constrained) != 0] = 0.0

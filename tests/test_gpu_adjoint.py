@@ -92,3 +92,30 @@ def test_coordinate_sensitivity_matches_reference_adjoint(et, fo, qo, n, jit):
     # a rigid translation of the whole mesh leaves q unchanged: the interior-plus-boundary sum vanishes
     assert np.all(np.abs(g.sum(0)) <= 1e-9 * np.abs(g).sum(0))
     asm.close()
+
+
+@pytest.mark.parametrize("et,fo,qo,n,jit", [(lm.TET10, 2, 4, 2, 0.1), (lm.HEX8, 1, 2, 3, 0.1)])
+def test_elasticity_coordinate_sensitivity_matches_reference_adjoint(et, fo, qo, n, jit):
+    """Elasticity: dq/dx for q = integral of the sum of u's components over the
+    marked elements, against the oracle's central-difference restatement."""
+    mesh, dm, k, f = make_problem(n, et, 3, lm.ELASTICITY, jitter=jit, seed=5)
+    region = (centroid_x(mesh) < 0.5).astype(np.uint8)
+    asm = lm.GpuAssembly(lm.ELASTICITY, fo, qo, elem_coef=k, nodal_f=f)
+    system = lm.LinearImplicitSystem(mesh, 3)
+    system.dof_map = dm
+    system.attach_assemble_object(asm)
+    system.init()
+    asm.assemble()
+    u, _, _ = asm.solve(rtol=1e-14, maxit=100000)
+    z, _, _ = asm.solve(rhs=asm.qoi_region_load(region), rtol=1e-14, maxit=100000)
+    g = asm.vjp_xyz(u, z, region)
+    x = mesh.xyz
+    interior = np.nonzero(np.all((x > 1e-9) & (x < 1 - 1e-9), axis=1))[0]
+    rng = np.random.default_rng(7)
+    params = [(int(nd), int(d)) for nd, d in zip(rng.choice(interior, 5, replace=False), rng.integers(0, 3, 5))]
+    _, ref = orc.coordinate_sensitivity(lm.ELASTICITY, et, fo, qo, x, mesh.conn, dm.elem_dofs, dm.n_dofs,
+                                        dm.constrained, system.row_ptr, system.col_idx, k, f, region, params,
+                                        n_vars=3)
+    got = np.array([g[nd, d] for nd, d in params])
+    np.testing.assert_allclose(got, ref, rtol=1e-6, atol=1e-6 * np.abs(g).max())
+    asm.close()
