@@ -172,6 +172,66 @@ __global__ void k_scan_add(int64_t n, int32_t *out, const int32_t *boff) {
 
 }  // namespace
 
+// DofMap::compute_sparsity on the device (block pattern of the block path):
+// warp per block row P gathers the blocks of every element incident on P
+// (the row's incidence list), sorts them in shared memory (bitonic) and keeps
+// the distinct ones; pass 0 writes the degree, pass 1 the columns.  Rows with
+// more than GRAPH_CAP candidates raise a flag and the host build takes over.
+constexpr int GRAPH_CAP = 1024, GRAPH_WARPS = 4;
+template <int PASS>
+__global__ void __launch_bounds__(GRAPH_WARPS * 32) k_block_graph(int64_t n_rows, int nb, const int32_t *eb,
+                                                                  const int32_t *iptr, const int32_t *icon,
+                                                                  int32_t *deg, const int32_t *bptr, int32_t *bcol,
+                                                                  int *overflow) {
+  __shared__ int32_t buf[GRAPH_WARPS][GRAPH_CAP];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int32_t *b = buf[warp];
+  for (int64_t P = (int64_t)blockIdx.x * GRAPH_WARPS + warp; P < n_rows; P += (int64_t)gridDim.x * GRAPH_WARPS) {
+    const int32_t i0 = iptr[P], i1 = iptr[P + 1];
+    const int n = (i1 - i0) * nb;
+    if (n > GRAPH_CAP) {
+      if (lane == 0) *overflow = 1;
+      continue;
+    }
+    int S = 1;
+    while (S < n) S <<= 1;
+    for (int t = lane; t < S; t += 32) {
+      int32_t v = 0x7fffffff;
+      if (t < n) {
+        const int32_t entry = icon[i0 + t / nb];  // e * nb + a
+        v = eb[(int64_t)(entry / nb) * nb + t % nb];
+      }
+      b[t] = v;
+    }
+    __syncwarp();
+    for (int k = 2; k <= S; k <<= 1)
+      for (int j = k >> 1; j > 0; j >>= 1) {
+        for (int t = lane; t < S; t += 32) {
+          const int u = t ^ j;
+          if (u > t) {
+            const int32_t x = b[t], y = b[u];
+            const bool up = (t & k) == 0;
+            if ((x > y) == up) {
+              b[t] = y;
+              b[u] = x;
+            }
+          }
+        }
+        __syncwarp();
+      }
+    int count = 0;
+    for (int t0 = 0; t0 < S; t0 += 32) {
+      const int t = t0 + lane;
+      const bool keep = t < S && b[t] != 0x7fffffff && (t == 0 || b[t] != b[t - 1]);
+      const unsigned m = __ballot_sync(0xffffffffu, keep);
+      if (PASS == 1 && keep) bcol[bptr[P] + count + __popc(m & ((1u << lane) - 1u))] = b[t];
+      count += __popc(m);
+    }
+    if (PASS == 0 && lane == 0) deg[P] = count;
+    __syncwarp();
+  }
+}
+
 namespace {
 
 int grid_for(lmg_ctx *c, int64_t items, int threads) {
@@ -206,6 +266,55 @@ lmg_status scan_i32(lmg_ctx *c, const int32_t *in, int32_t *out, int64_t n) {
   LMG_CUDA(c, cudaStreamSynchronize(c->stream));
   dfree(bsum);
   dfree(boff);
+  return LMG_OK;
+}
+
+// Block graph on the device; LMG_ERR_UNSUPPORTED when a row has too many
+// candidates (the caller then builds it on the host).
+lmg_status device_block_graph(lmg_ctx *c, std::vector<int64_t> &brow) {
+  const int nb = c->nb;
+  const int64_t nrow = c->n_elem * nb, nbk = c->n_blocks;
+  int32_t *cnt = nullptr, *cur = nullptr, *iptr = nullptr, *icon = nullptr, *deg = nullptr, *bptr = nullptr,
+          *dcol = nullptr;
+  int *ovf = nullptr;
+  auto cleanup = [&]() { dfree(cnt); dfree(cur); dfree(iptr); dfree(icon); dfree(deg); dfree(bptr); dfree(dcol); dfree(ovf); };
+  LMG_CUDA(c, dalloc(cnt, (size_t)nbk));
+  LMG_CUDA(c, dalloc(cur, (size_t)nbk));
+  LMG_CUDA(c, dalloc(iptr, (size_t)nbk + 1));
+  LMG_CUDA(c, dalloc(icon, (size_t)nrow));
+  LMG_CUDA(c, dalloc(deg, (size_t)nbk));
+  LMG_CUDA(c, dalloc(bptr, (size_t)nbk + 1));
+  LMG_CUDA(c, dalloc(ovf, 1));
+  LMG_CUDA(c, cudaMemsetAsync(ovf, 0, sizeof(int), c->stream));
+  // incidence of every block row: (e*nb + a) entries in element order
+  LMG_CUDA(c, cudaMemsetAsync(cnt, 0, sizeof(int32_t) * nbk, c->stream));
+  k_count_rows<<<grid_for(c, nrow, 256), 256, 0, c->stream>>>(nrow, c->d_eb, cnt);
+  lmg_status st = scan_i32(c, cnt, iptr, nbk);
+  if (st) { cleanup(); return st; }
+  LMG_CUDA(c, cudaMemsetAsync(cur, 0, sizeof(int32_t) * nbk, c->stream));
+  k_fill<<<grid_for(c, nrow, 256), 256, 0, c->stream>>>(nrow, c->d_eb, iptr, cur, icon);
+  const int g = grid_for(c, nbk * 32, GRAPH_WARPS * 32);
+  k_block_graph<0><<<g, GRAPH_WARPS * 32, 0, c->stream>>>(nbk, nb, c->d_eb, iptr, icon, deg, nullptr, nullptr, ovf);
+  c->launches += 3;
+  int h_ovf = 0;
+  LMG_CUDA(c, cudaMemcpyAsync(&h_ovf, ovf, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  LMG_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (h_ovf) { cleanup(); return LMG_ERR_UNSUPPORTED; }
+  if ((st = scan_i32(c, deg, bptr, nbk))) { cleanup(); return st; }
+  int32_t total = 0;
+  LMG_CUDA(c, cudaMemcpyAsync(&total, bptr + nbk, sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream));
+  LMG_CUDA(c, cudaStreamSynchronize(c->stream));
+  LMG_CUDA(c, dalloc(dcol, (size_t)total));
+  k_block_graph<1><<<g, GRAPH_WARPS * 32, 0, c->stream>>>(nbk, nb, c->d_eb, iptr, icon, nullptr, bptr, dcol, ovf);
+  c->launches++;
+  std::vector<int32_t> hp((size_t)nbk + 1);
+  LMG_CUDA(c, cudaMemcpyAsync(hp.data(), bptr, sizeof(int32_t) * (nbk + 1), cudaMemcpyDeviceToHost, c->stream));
+  LMG_CUDA(c, cudaStreamSynchronize(c->stream));
+  brow.assign(hp.begin(), hp.end());
+  dfree(c->d_bcol);
+  c->d_bcol = dcol;  // the columns stay on the device
+  dcol = nullptr;
+  cleanup();
   return LMG_OK;
 }
 
@@ -546,9 +655,17 @@ lmg_status lmg_sparsity_build(lmg_ctx *c, int64_t *nnz) {
   }
   std::vector<int64_t> brow;
   std::vector<int32_t> bcol;
-  const unsigned hw = std::thread::hardware_concurrency();
-  build_block_graph(c->n_elem, c->nb, c->h_eb.data(), c->n_blocks, brow, bcol, hw ? (int)hw : 4);
-  c->nnzb = (int64_t)bcol.size();
+  // the block pattern on the device; the host builds rows the device buffer cannot hold
+  // (32-bit incidence and column offsets: every element adds at most nb^2 block pairs)
+  lmg_status gs = c->n_elem * c->nb * c->nb < INT32_MAX ? device_block_graph(c, brow) : LMG_ERR_UNSUPPORTED;
+  if (gs == LMG_ERR_UNSUPPORTED) {
+    const unsigned hw = std::thread::hardware_concurrency();
+    build_block_graph(c->n_elem, c->nb, c->h_eb.data(), c->n_blocks, brow, bcol, hw ? (int)hw : 4);
+    LMG_CUDA(c, dupload(c, c->d_bcol, bcol.data(), bcol.size()));
+  } else if (gs) {
+    return gs;
+  }
+  c->nnzb = brow.back();
   c->nnz = c->nnzb * c->bs * c->bs;
   c->max_bdeg = 0;
   for (size_t P = 0; P + 1 < brow.size(); ++P) c->max_bdeg = std::max(c->max_bdeg, (int)(brow[P + 1] - brow[P]));
@@ -560,7 +677,6 @@ lmg_status lmg_sparsity_build(lmg_ctx *c, int64_t *nnz) {
     row_ptr[(size_t)r + 1] = row_ptr[(size_t)r] + (int32_t)((brow[(size_t)P + 1] - brow[(size_t)P]) * c->bs);
   }
   LMG_CUDA(c, dupload(c, c->d_brow_ptr, brow.data(), brow.size()));
-  LMG_CUDA(c, dupload(c, c->d_bcol, bcol.data(), bcol.size()));
   LMG_CUDA(c, dupload(c, c->d_row_ptr, row_ptr.data(), row_ptr.size()));
   c->h_rowptr_blk = row_ptr;
   LMG_CUDA(c, dalloc(c->d_col, (size_t)c->nnz));

@@ -143,6 +143,15 @@ def test_c2_full_size_properties():
     ones = np.ones((mesh.n_nodes, 3))
     asm, rp, col = gpu_system(mesh, dm, lm.ELASTICITY, 2, 4, k, ones)
     assert len(col) == 231797385
+    # the device block graph against the host compute_sparsity restatement
+    import ctypes
+    from libmesh_gb300._capi import lib, ptr
+    nnz = ctypes.c_int64()
+    rph = np.empty(dm.n_dofs + 1, np.int32)
+    colh = np.empty(len(col), np.int32)
+    assert lib().lmg_host_sparsity(mesh.n_elem, 10, 3, dm.n_dofs, ptr(dm.elem_dofs), nnz, ptr(rph), ptr(colh)) == 0
+    assert nnz.value == len(col) and np.array_equal(rp, rph) and np.array_equal(col, colh)
+    del rph, colh
     K, F = asm.assemble()
     asm.close()
     assert abs(F.sum() - 3.0) < 1e-10  # f = 1 per component integrates to the unit volume
