@@ -574,7 +574,7 @@ def main():
     dom["frac"] = dom["achieved"] / dom["peak"]
     # DRAM bytes of one launch from ncu on the 24^3 case (profiles/elasticity_tet10_24_kernels.md),
     # scaled by the element count; traffic grows in proportion to the mesh.
-    per24 = {"k_gather<double,3>": 787445248 + 221671936,
+    per24 = {"k_gather<double,3>": 731908864 + 245608192,
              "k_elem_affine<ELASTICITY,10,3,double>": 15557120 + 291394560}
     dom["traffic"] = per24[dom["kernel"]] * mesh.n_elem / 82944.0 if args.n == N_CUBE else None
     dom["traffic_source"] = "ncu dram__bytes_read+write on build_cube 24^3, scaled x%.1f" % (mesh.n_elem / 82944.0)
