@@ -15,12 +15,12 @@ import numpy as np
 
 from . import _capi
 from ._capi import (ADVDIFF, ELASTICITY, FP64, HEX8, HEX27, HIERARCHIC, MIXED, POISSON, PRISM6, TET4, TET10,
-                    DegenerateMap, LmgError, check, lib, ptr)
+                    TET14, DegenerateMap, LmgError, check, lib, ptr)
 
 FIRST, SECOND, THIRD, FOURTH, FIFTH = 1, 2, 3, 4, 5
 
 __all__ = ["Mesh", "DofMap", "GpuAssembly", "Batch", "LinearImplicitSystem", "DegenerateMap", "LmgError",
-           "HEX8", "HEX27", "TET4", "TET10", "PRISM6", "POISSON", "ELASTICITY", "ADVDIFF", "FP64", "MIXED", "HIERARCHIC",
+           "HEX8", "HEX27", "TET4", "TET10", "TET14", "PRISM6", "POISSON", "ELASTICITY", "ADVDIFF", "FP64", "MIXED", "HIERARCHIC",
            "FIRST", "SECOND", "THIRD", "FOURTH", "FIFTH"]
 
 
@@ -109,7 +109,7 @@ class DofMap:
     """Var-major first-touch numbering of n_vars variables (one VariableGroup);
     elem_dofs[e] is DofMap::dof_indices(elem).  fe_order (| HIERARCHIC) picks
     the FEType whose dofs are numbered: nodal types give one dof per node and
-    variable; 3 | HIERARCHIC on HEX27 gives 64 dofs per element."""
+    variable; 3 | HIERARCHIC gives 64 dofs per element on HEX27 and 20 on TET14."""
 
     def __init__(self, mesh, n_vars=1, fe_order=None):
         self.mesh = mesh

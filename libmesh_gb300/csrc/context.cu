@@ -599,8 +599,9 @@ lmg_status lmg_dofmap_upload_fe(lmg_ctx *c, int32_t n_vars, int32_t fe_order, in
   if (fe_order != (3 | LMG_HIERARCHIC)) return lmg_dofmap_upload(c, n_vars, n_dofs, elem_dofs);
   if (!c || !elem_dofs || n_vars != 1 || n_dofs <= 0) return fail(c, LMG_ERR_ARG, "dofmap_upload: bad argument");
   if (!c->n_elem) return fail(c, LMG_ERR_STATE, "dofmap_upload: upload the mesh first");
-  if (c->elem_type != LMG_HEX27) return fail(c, LMG_ERR_UNSUPPORTED, "dofmap_upload: THIRD HIERARCHIC needs HEX27");
-  const int nl = 64;
+  if (c->elem_type != LMG_HEX27 && c->elem_type != LMG_TET14)
+    return fail(c, LMG_ERR_UNSUPPORTED, "dofmap_upload: THIRD HIERARCHIC needs HEX27 or TET14");
+  const int nl = c->elem_type == LMG_TET14 ? 20 : 64;
   for (int64_t i = 0; i < c->n_elem * nl; ++i)
     if (elem_dofs[i] < 0 || elem_dofs[i] >= n_dofs) return fail(c, LMG_ERR_BOUNDS, "dof id out of range", i / nl);
   cudaSetDevice(c->device);

@@ -89,7 +89,35 @@ void tet_rule(int order, std::vector<double> &p, std::vector<double> &w) {
     add(0.25, 0.25, 0.25, -2.0 / 15.0);
     add(0.5, 1.0 / 6, 1.0 / 6, 0.075); add(1.0 / 6, 0.5, 1.0 / 6, 0.075);
     add(1.0 / 6, 1.0 / 6, 0.5, 0.075); add(1.0 / 6, 1.0 / 6, 1.0 / 6, 0.075);
-  } else {
+  } else if (order == 5) {
+    // Walkington's 14-point degree-5 rule (quadrature_gauss_3D.C:231-287): two
+    // 4-orbits (a, a, a), (a, b, a), (b, a, a), (a, a, b) with b = 1 - 3a, and
+    // a 6-orbit with b = (1 - 2a) / 2, in the reference's point order.
+    const double a[3] = {0.31088591926330060980, 0.092735250310891226402, 0.045503704125649649492};
+    const double wt[3] = {0.018781320953002641800, 0.012248840519393658257, 0.0070910034628469110730};
+    for (int i = 0; i < 2; ++i) {
+      const double b = 1. - 3. * a[i];
+      add(a[i], a[i], a[i], wt[i]); add(a[i], b, a[i], wt[i]); add(b, a[i], a[i], wt[i]); add(a[i], a[i], b, wt[i]);
+    }
+    const double b = 0.5 * (1. - 2. * a[2]), c = a[2], w6 = wt[2];
+    add(b, b, c, w6); add(b, c, c, w6); add(c, c, b, w6); add(c, b, c, w6); add(b, c, b, w6); add(c, b, b, w6);
+  } else if (order == 6) {
+    // Keast's 24-point degree-6 rule (quadrature_gauss_3D.C:401-420 through
+    // keast_rule, quadrature_gauss.C:43-180): three 4-orbits (a, b, b),
+    // (b, a, b), (b, b, a), (b, b, b) and one 12-orbit, with the reference's
+    // 18-digit values.
+    const double r[3][3] = {{0.356191386222544953e+00, 0.214602871259151684e+00, 0.00665379170969464506e+00},
+                            {0.877978124396165982e+00, 0.0406739585346113397e+00, 0.00167953517588677620e+00},
+                            {0.0329863295731730594e+00, 0.322337890142275646e+00, 0.00922619692394239843e+00}};
+    for (int i = 0; i < 3; ++i) {
+      const double a = r[i][0], b = r[i][1], wt = r[i][2];
+      add(a, b, b, wt); add(b, a, b, wt); add(b, b, a, wt); add(b, b, b, wt);
+    }
+    const double a = 0.0636610018750175299e+00, b = 0.269672331458315867e+00, c = 0.603005664791649076e+00,
+                 wt = 0.00803571428571428248e+00;
+    add(a, a, b, wt); add(a, a, c, wt); add(b, a, a, wt); add(c, a, a, wt); add(a, b, a, wt); add(a, c, a, wt);
+    add(a, b, c, wt); add(a, c, b, wt); add(b, a, c, wt); add(b, c, a, wt); add(c, a, b, wt); add(c, b, a, wt);
+  } else if (order == 4) {
     // Keast (1986) degree-4 rule: centroid, a 4-orbit and a 6-orbit, with the
     // 18-digit values libMesh tabulates (quadrature_gauss_3D.C:198-226), so
     // that difference quotients of shapes at these points agree bit for bit.
@@ -192,7 +220,7 @@ int lagrange_shapes(int type, int order, const double *p, double *v, double *g) 
     }
     return 6;
   }
-  if (type == LMG_TET4 || type == LMG_TET10) {
+  if (type == LMG_TET4 || type == LMG_TET10 || type == LMG_TET14) {
     const double z[4] = {1.0 - p[0] - p[1] - p[2], p[0], p[1], p[2]};
     const double dz[4][3] = {{-1, -1, -1}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
     if (order == 1) {
@@ -201,6 +229,36 @@ int lagrange_shapes(int type, int order, const double *p, double *v, double *g) 
         for (int m = 0; m < 3; ++m) g[3 * a + m] = dz[a][m];
       }
       return 4;
+    }
+    if (type == LMG_TET14) {
+      // TET14 (fe_lagrange_shape_3D.C:1402-1460, derivatives :2931-3260):
+      // quadratic functions corrected by the face bubbles z_a z_b z_c.
+      const double b[4] = {z[0] * z[1] * z[2], z[0] * z[1] * z[3], z[1] * z[2] * z[3], z[0] * z[2] * z[3]};
+      // d bubble / d xi_j for bubbles 012, 013, 123, 023
+      const double db[3][4] = {{(z[0] - z[1]) * z[2], (z[0] - z[1]) * z[3], z[2] * z[3], -z[2] * z[3]},
+                               {(z[0] - z[2]) * z[1], -z[1] * z[3], z[1] * z[3], (z[0] - z[2]) * z[3]},
+                               {-z[1] * z[2], (z[0] - z[3]) * z[1], z[1] * z[2], (z[0] - z[3]) * z[2]}};
+      static const int VB[4][3] = {{0, 1, 3}, {0, 1, 2}, {0, 3, 2}, {1, 3, 2}};  // bubbles at each vertex
+      static const int EN[6][2] = {{0, 1}, {1, 2}, {0, 2}, {0, 3}, {1, 3}, {2, 3}};
+      static const int EB[6][2] = {{0, 1}, {0, 2}, {0, 3}, {1, 3}, {1, 2}, {3, 2}};  // bubbles at each edge
+      static const int FB[4] = {0, 1, 2, 3};
+      for (int a = 0; a < 4; ++a) {
+        v[a] = z[a] * (2. * z[a] - 1.) + 3. * (b[VB[a][0]] + b[VB[a][1]] + b[VB[a][2]]);
+        for (int m = 0; m < 3; ++m)
+          g[3 * a + m] = (4. * z[a] - 1.) * dz[a][m] + 3. * (db[m][VB[a][0]] + db[m][VB[a][1]] + db[m][VB[a][2]]);
+      }
+      for (int k = 0; k < 6; ++k) {
+        const int i = EN[k][0], j = EN[k][1];
+        // node 6 is written 4 z2 z0 in the reference
+        v[4 + k] = (k == 2 ? 4. * z[2] * z[0] : 4. * z[i] * z[j]) - 12. * (b[EB[k][0]] + b[EB[k][1]]);
+        for (int m = 0; m < 3; ++m)
+          g[3 * (4 + k) + m] = 4. * (z[i] * dz[j][m] + dz[i][m] * z[j]) - 12. * (db[m][EB[k][0]] + db[m][EB[k][1]]);
+      }
+      for (int f = 0; f < 4; ++f) {
+        v[10 + f] = 27. * b[FB[f]];
+        for (int m = 0; m < 3; ++m) g[3 * (10 + f) + m] = 27. * db[m][FB[f]];
+      }
+      return 14;
     }
     if (type != LMG_TET10) return 0;
     static const int EV[6][2] = {{0, 1}, {1, 2}, {2, 0}, {0, 3}, {1, 3}, {2, 3}};
@@ -264,8 +322,9 @@ double hier_prism6(int a, const double *x) {
 
 int hierarchic_shapes(int type, int order, const double *p, double *v, double *g) {
   const bool tet = (type == LMG_TET4 && order == 1) || (type == LMG_TET10 && order == 2);
+  const bool tet3 = false;  // cubic tets depend on the element: hier_tet3_shapes
   const bool prism = type == LMG_PRISM6 && order == 1;
-  if (!((type == LMG_HEX8 && order == 1) || (type == LMG_HEX27 && order == 2) || tet || prism)) return 0;
+  if (!((type == LMG_HEX8 && order == 1) || (type == LMG_HEX27 && order == 2) || tet || prism) || tet3) return 0;
   const int n = prism ? 6 : tet ? (order == 1 ? 4 : 10) : (order == 1) ? 8 : 27;
   auto shape = [&](int a, const double *x) {
     if (prism) return hier_prism6(a, x);
@@ -289,6 +348,78 @@ int hierarchic_shapes(int type, int order, const double *p, double *v, double *g
 
 }  // namespace
 
+// Cubic HIERARCHIC tets (FEType{THIRD, HIERARCHIC} on TET14,
+// fe_hierarchic_shape_3D.C:2361-2440): vertices; per edge e the bases of
+// order 2 and 3, c^order * hier1d(order, (z1 - z0) / c) with c = z0 + z1
+// ((z1 - z0)^order / order! where c is exactly 0), the order-3 one negated
+// when positive_edge_orientation(e) holds (elem.C:3634-3640: the edge's first
+// vertex is lexicographically greater); per face f the bubble
+// ((1 * z_a) * z_b) * z_c over the face's vertices as orient_triangle sorts
+// them (fe_hierarchic_shape_3D.C:2193-2243).
+TetOrient tet_orient(const double *X) {
+  auto greater = [&](int a, int b) {  // TypeVector::operator> (type_vector.C:95-105)
+    for (int d = 0; d < 3; ++d) {
+      if (X[3 * a + d] > X[3 * b + d]) return true;
+      if (X[3 * a + d] < X[3 * b + d]) return false;
+    }
+    return false;
+  };
+  static const int EN[6][2] = {{0, 1}, {1, 2}, {0, 2}, {0, 3}, {1, 3}, {2, 3}};
+  static const int SV[4][3] = {{0, 2, 1}, {0, 1, 3}, {1, 2, 3}, {2, 0, 3}};  // Tet4 side vertices
+  TetOrient o;
+  o.flip = 0;
+  for (int e = 0; e < 6; ++e)
+    if (greater(EN[e][0], EN[e][1])) o.flip |= (uint8_t)(1u << e);
+  for (int f = 0; f < 4; ++f) {
+    int v[3] = {SV[f][0], SV[f][1], SV[f][2]};
+    bool lastcheck = true;
+    if (greater(v[0], v[1])) { std::swap(v[0], v[1]); lastcheck = true; }
+    if (greater(v[1], v[2])) std::swap(v[1], v[2]);
+    if (lastcheck && greater(v[0], v[1])) std::swap(v[0], v[1]);
+    for (int k = 0; k < 3; ++k) o.fv[f][k] = (uint8_t)v[k];
+  }
+  return o;
+}
+
+static double hier_tet3(const TetOrient &o, int a, const double *x) {
+  const double zeta[4] = {1 - x[0] - x[1] - x[2], x[0], x[1], x[2]};
+  if (a < 4) return zeta[a];
+  static const int EN[6][2] = {{0, 1}, {1, 2}, {0, 2}, {0, 3}, {1, 3}, {2, 3}};
+  if (a < 16) {
+    const int edge = (a - 4) / 2;
+    const unsigned basisorder = (unsigned)(a - 2 - 2 * edge);
+    double flip = 1;
+    if (basisorder % 2 && ((o.flip >> edge) & 1u)) flip = -1;
+    const double c = zeta[EN[edge][0]] + zeta[EN[edge][1]], num = zeta[EN[edge][1]] - zeta[EN[edge][0]];
+    if (c == 0.) {
+      unsigned fact = 1;
+      for (unsigned n = 2; n <= basisorder; ++n) fact *= n;
+      return std::pow(num, basisorder) / fact;
+    }
+    return flip * std::pow(c, basisorder) * hier1d((int)basisorder, num / c);
+  }
+  const int f = a - 16;
+  double r = 1;
+  r *= zeta[o.fv[f][0]];
+  r *= zeta[o.fv[f][1]];
+  r *= zeta[o.fv[f][2]];
+  return r;
+}
+
+int hier_tet3_shapes(const TetOrient &o, const double *p, double *v, double *g) {
+  const double eps = 1.e-6;
+  for (int a = 0; a < 20; ++a) {
+    v[a] = hier_tet3(o, a, p);
+    for (int j = 0; j < 3; ++j) {
+      double pp[3] = {p[0], p[1], p[2]}, pm[3] = {p[0], p[1], p[2]};
+      pp[j] += eps;
+      pm[j] -= eps;
+      g[3 * a + j] = (hier_tet3(o, a, pp) - hier_tet3(o, a, pm)) / 2. / eps;
+    }
+  }
+  return 20;
+}
+
 std::string build_fe_tables(FETables &t, int type, int fe_order, int q_order, int family) {
   t = FETables();
   t.elem_type = type;
@@ -305,10 +436,10 @@ std::string build_fe_tables(FETables &t, int type, int fe_order, int q_order, in
     return family == 1 ? hierarchic_shapes(type, fe_order, p, v, g) : lagrange_shapes(type, fe_order, p, v, g);
   };
   const bool hex = (type == LMG_HEX8 || type == LMG_HEX27);
-  const bool tet = (type == LMG_TET4 || type == LMG_TET10);
+  const bool tet = (type == LMG_TET4 || type == LMG_TET10 || type == LMG_TET14);
   const bool prism = type == LMG_PRISM6;
   if (!hex && !tet && !prism) return "unsupported element type";
-  const int geo_order = (type == LMG_HEX27 || type == LMG_TET10) ? 2 : 1;
+  const int geo_order = (type == LMG_HEX27 || type == LMG_TET10) ? 2 : type == LMG_TET14 ? 3 : 1;
   if (hex) {
     std::vector<double> x, w;
     gauss_legendre(q_order / 2 + 1, x, w);
@@ -332,7 +463,7 @@ std::string build_fe_tables(FETables &t, int type, int fe_order, int q_order, in
         t.qw.push_back(tw[i] * w[j]);
       }
   } else {
-    if (q_order > 4) return "tet quadrature above FOURTH is not built";
+    if (q_order > 6) return "tet quadrature above SIXTH is not built";
     tet_rule(q_order, t.qp, t.qw);
   }
   t.q = (int)t.qw.size();
@@ -399,12 +530,26 @@ bool elem_has_affine_map(int type, const double *P) {
     }
     case LMG_TET4:
       return true;
-    case LMG_TET10: {  // cell_tet10.C:143-172
+    case LMG_TET10:    // cell_tet10.C:143-172
+    case LMG_TET14: {  // cell_tet14.C:153-194: straight edges, then midface nodes
       static const int E[6][3] = {{1, 0, 4}, {2, 1, 5}, {2, 0, 6}, {3, 0, 7}, {3, 1, 8}, {3, 2, 9}};
       for (int k = 0; k < 6; ++k) {
         sub(P, E[k][0], E[k][1], v);
         sub(P, E[k][2], E[k][1], w);
         for (int d = 0; d < 3; ++d) w[d] *= 2;
+        if (!rfe(v, w)) return false;
+      }
+      if (type == LMG_TET10) return true;
+      // (v_b0 + v_c0) against 3 (p_face - p_0), with v_ij = p_i - p_j
+      static const int F[4][5] = {{2, 0, 1, 0, 10}, {3, 0, 1, 0, 11}, {3, 1, 2, 1, 12}, {3, 0, 2, 0, 13}};
+      double a[3], b[3];
+      for (int f = 0; f < 4; ++f) {
+        sub(P, F[f][0], F[f][1], a);
+        sub(P, F[f][2], F[f][3], b);
+        const int base = f == 2 ? 1 : 0;
+        for (int d = 0; d < 3; ++d) v[d] = a[d] + b[d];
+        sub(P, F[f][4], base, w);
+        for (int d = 0; d < 3; ++d) w[d] *= 3;
         if (!rfe(v, w)) return false;
       }
       return true;

@@ -37,22 +37,22 @@ namespace lmg {
 
 namespace {
 
-constexpr int H3N = 64, H3T = 256, H3B = 8;
+constexpr int H3T = 256, H3B = 8;
 
 struct H3Args {
   int64_t n_batch;
   const int32_t *batch;     // [n_batch][3]: pattern, first index in order, count
   const int32_t *order;     // element ids sorted by pattern
   const double *xyz;
-  const int32_t *conn;      // [n_elem][27]
+  const int32_t *conn;      // [n_elem][G]
   const double *coef;       // [n_elem] or null
   const double *nodal_f;    // [n_nodes] or null
   const uint64_t *cmask;    // [n_elem] constrained local dofs, or null (no mask)
-  const float2 *D;          // [P][6][64*64] double-float pairs
-  const double *M;          // [P][64][27]
-  const double *gd0;        // [27][3]
-  float2 *Kraw;             // [n_elem][64][64] double-float pairs
-  double *Fraw;             // [n_elem][64]
+  const float2 *D;          // [P][6][N*N] double-float pairs
+  const double *M;          // [P][N][G]
+  const double *gd0;        // [G][3]
+  float2 *Kraw;             // [n_elem][N][N] double-float pairs
+  double *Fraw;             // [n_elem][N]
   int *status;
   unsigned long long *bad_elem;
 };
@@ -63,10 +63,13 @@ __device__ __forceinline__ double warp_sum(double v) {
   return v;
 }
 
-__global__ void __launch_bounds__(H3T) k_elem_hier3(H3Args a) {
+// N dofs and G map nodes per element (cubic hexes 64 / 27, cubic tets 20 / 14)
+template <int N, int G>
+__global__ void __launch_bounds__(H3T) k_elem_pattern(H3Args a) {
+  static_assert(N <= 64 && G <= 32, "one mask word per element, one lane per map node");
   __shared__ double sA[H3B][8];   // A_0..A_5, detJ
   __shared__ DF sA2[H3B][6];
-  __shared__ double sf[H3B][27];
+  __shared__ double sf[H3B][G];
   __shared__ uint64_t sm[H3B];
   __shared__ int32_t se[H3B];
   const int t = threadIdx.x, w = t >> 5, lane = t & 31;
@@ -78,8 +81,8 @@ __global__ void __launch_bounds__(H3T) k_elem_hier3(H3Args a) {
       double jp[9];
 #pragma unroll
       for (int k = 0; k < 9; ++k) jp[k] = 0.0;
-      if (lane < 27) {
-        const int64_t nd = a.conn[(int64_t)e * 27 + lane];
+      if (lane < G) {
+        const int64_t nd = a.conn[(int64_t)e * G + lane];
         const double x[3] = {a.xyz[3 * nd], a.xyz[3 * nd + 1], a.xyz[3 * nd + 2]};
 #pragma unroll
         for (int m = 0; m < 3; ++m)
@@ -125,13 +128,13 @@ __global__ void __launch_bounds__(H3T) k_elem_hier3(H3Args a) {
     }
     __syncthreads();
     // K_ij = sum_k A_k D_k[i][j] in double-float arithmetic (FP32 pipe)
-    const float2 *Dp = a.D + (size_t)p * 6 * (H3N * H3N);
-    for (int idx = t; idx < H3N * H3N; idx += H3T) {
-      const int i = idx >> 6, j = idx & 63;
+    const float2 *Dp = a.D + (size_t)p * 6 * (N * N);
+    for (int idx = t; idx < N * N; idx += H3T) {
+      const int i = idx / N, j = idx - i * N;
       DF d[6];
 #pragma unroll
       for (int k = 0; k < 6; ++k) {
-        const float2 x = Dp[k * 4096 + idx];
+        const float2 x = Dp[k * (N * N) + idx];
         d[k] = DF{x.x, x.y};
       }
       for (int b = 0; b < cnt; ++b) {
@@ -140,15 +143,15 @@ __global__ void __launch_bounds__(H3T) k_elem_hier3(H3Args a) {
         for (int k = 0; k < 6; ++k) v = df_fma_lazy(v, sA2[b][k], d[k]);
         v = df_norm(v);
         if (((sm[b] >> i) | (sm[b] >> j)) & 1ull) v = DF{(i == j) ? 1.f : 0.f, 0.f};
-        a.Kraw[(int64_t)se[b] * (H3N * H3N) + idx] = make_float2(v.hi, v.lo);
+        a.Kraw[(int64_t)se[b] * (N * N) + idx] = make_float2(v.hi, v.lo);
       }
     }
-    const double *Mp = a.M + (size_t)p * H3N * 27;
-    for (int idx = t; idx < H3N * cnt; idx += H3T) {
-      const int b = idx >> 6, i = idx & 63;
+    const double *Mp = a.M + (size_t)p * N * G;
+    for (int idx = t; idx < N * cnt; idx += H3T) {
+      const int b = idx / N, i = idx - b * N;
       double s = 0.0;
-      for (int g = 0; g < 27; ++g) s += Mp[i * 27 + g] * sf[b][g];
-      a.Fraw[(int64_t)se[b] * H3N + i] = ((sm[b] >> i) & 1ull) ? 0.0 : sA[b][6] * s;
+      for (int g = 0; g < G; ++g) s += Mp[i * G + g] * sf[b][g];
+      a.Fraw[(int64_t)se[b] * N + i] = ((sm[b] >> i) & 1ull) ? 0.0 : sA[b][6] * s;
     }
   }
 }
@@ -164,15 +167,17 @@ void hier3_free(lmg_ctx *c) {
   c->h3_nbatch = 0;
 }
 
-// lmg_form_set for FEType{THIRD, HIERARCHIC} on HEX27.
+// lmg_form_set for FEType{THIRD, HIERARCHIC} on HEX27 and TET14.
 lmg_status hier3_form_set(lmg_ctx *c, int32_t form, int32_t q_order, const double *elem_coef,
                           const double *nodal_f) {
-  if (form != LMG_POISSON || c->n_vars != 1 || c->elem_type != LMG_HEX27)
-    return fail(c, LMG_ERR_UNSUPPORTED, "form_set: THIRD HIERARCHIC is built for POISSON on HEX27");
+  if (form != LMG_POISSON || c->n_vars != 1 || (c->elem_type != LMG_HEX27 && c->elem_type != LMG_TET14))
+    return fail(c, LMG_ERR_UNSUPPORTED, "form_set: THIRD HIERARCHIC is built for POISSON on HEX27 and TET14");
   if (!c->h_gen.empty())
     return fail(c, LMG_ERR_UNSUPPORTED, "form_set: THIRD HIERARCHIC takes affine elements only");
   Hier3Tables h;
-  std::string err = build_hier3_tables(h, q_order, c->n_elem, c->h_xyz.data(), c->h_conn.data());
+  std::string err = c->elem_type == LMG_TET14
+                        ? build_tet3_tables(h, q_order, c->n_elem, c->h_xyz.data(), c->h_conn.data())
+                        : build_hier3_tables(h, q_order, c->n_elem, c->h_xyz.data(), c->h_conn.data());
   if (!err.empty()) return fail(c, LMG_ERR_UNSUPPORTED, "form_set: " + err);
   hier3_free(c);
   LMG_CUDA(c, dupload(c, c->d_h3batch, h.batch.data(), h.batch.size()));
@@ -188,13 +193,13 @@ lmg_status hier3_form_set(lmg_ctx *c, int32_t form, int32_t q_order, const doubl
   c->h3_nbatch = (int64_t)h.batch.size() / 3;
   c->h3_patterns = h.P;
   FETables t;
-  t.elem_type = LMG_HEX27;
+  t.elem_type = c->elem_type;
   t.fe_order = 3;
   t.q_order = q_order;
   t.family = 1;
-  t.n = H3N;
+  t.n = h.N;
   t.q = h.q;
-  t.n_geo = 27;
+  t.n_geo = h.G;
   c->tab = t;
   c->form = form;
   c->fe_order = 3;
@@ -235,7 +240,8 @@ void launch_hier3(lmg_ctx *c) {
   const int64_t want = (int64_t)c->n_sm * 8;
   const int grid = (int)(a.n_batch < want ? a.n_batch : want);
   if (grid <= 0) return;
-  k_elem_hier3<<<grid, H3T, 0, c->stream>>>(a);
+  if (c->tab.n == 20) k_elem_pattern<20, 14><<<grid, H3T, 0, c->stream>>>(a);
+  else k_elem_pattern<64, 27><<<grid, H3T, 0, c->stream>>>(a);
 }
 
 }  // namespace lmg

@@ -253,4 +253,76 @@ std::string build_hier3_tables(Hier3Tables &h, int q_order, int64_t n_elem, cons
   return "";
 }
 
+// Cubic HIERARCHIC tets on TET14: a pattern is the element's orientation
+// (edge flips and sorted face vertices, tet_orient); per pattern the shapes are
+// evaluated at the quadrature points as the reference evaluates them for such
+// an element, and tabulated as for the hexahedra: D_k (the affine reference
+// tensors S^00, S^11, S^22, S^01+S^10, S^02+S^20, S^12+S^21), M (shape x TET14
+// map basis) and the TET14 map derivatives at qp 0.
+std::string build_tet3_tables(Hier3Tables &h, int q_order, int64_t n_elem, const double *xyz, const int32_t *conn) {
+  h = Hier3Tables();
+  h.N = 20;
+  h.G = 14;
+  FETables geo;
+  std::string err = build_fe_tables(geo, LMG_TET14, 1, q_order, 0);  // QGauss and the TET14 map basis
+  if (!err.empty()) return err;
+  if (geo.n_geo != 14) return "TET14 map basis";
+  h.q = geo.q;
+  h.gd0.assign(geo.gdphi.begin(), geo.gdphi.begin() + 14 * 3);
+  std::unordered_map<uint32_t, int> id;
+  std::vector<TetOrient> pats;
+  std::vector<int> pid((size_t)n_elem);
+  double X[12];
+  for (int64_t e = 0; e < n_elem; ++e) {
+    for (int a = 0; a < 4; ++a)
+      for (int d = 0; d < 3; ++d) X[3 * a + d] = xyz[3 * (int64_t)conn[e * 14 + a] + d];
+    const TetOrient o = tet_orient(X);
+    auto it = id.find(o.key());
+    if (it == id.end()) {
+      it = id.emplace(o.key(), (int)pats.size()).first;
+      pats.push_back(o);
+    }
+    pid[(size_t)e] = it->second;
+  }
+  const int N = 20, G = 14, Q = geo.q;
+  h.P = (int)pats.size();
+  h.Dp.assign((size_t)h.P * 6 * N * N, 0.0);
+  h.Mp.assign((size_t)h.P * N * G, 0.0);
+  std::vector<double> v((size_t)Q * N), g((size_t)Q * N * 3);
+  for (int p = 0; p < h.P; ++p) {
+    for (int q = 0; q < Q; ++q) hier_tet3_shapes(pats[(size_t)p], &geo.qp[3 * q], &v[(size_t)q * N], &g[(size_t)q * N * 3]);
+    double *D = &h.Dp[(size_t)p * 6 * N * N];
+    double *M = &h.Mp[(size_t)p * N * G];
+    for (int i = 0; i < N; ++i)
+      for (int j = 0; j < N; ++j) {
+        double S[3][3] = {};
+        for (int q = 0; q < Q; ++q)
+          for (int m = 0; m < 3; ++m)
+            for (int n = 0; n < 3; ++n)
+              S[m][n] += geo.qw[q] * g[((size_t)q * N + i) * 3 + m] * g[((size_t)q * N + j) * 3 + n];
+        const double d6[6] = {S[0][0], S[1][1], S[2][2], S[0][1] + S[1][0], S[0][2] + S[2][0], S[1][2] + S[2][1]};
+        for (int k = 0; k < 6; ++k) D[(size_t)k * N * N + i * N + j] = d6[k];
+      }
+    for (int i = 0; i < N; ++i)
+      for (int gg = 0; gg < G; ++gg) {
+        double m = 0.0;
+        for (int q = 0; q < Q; ++q) m += geo.qw[q] * v[(size_t)q * N + i] * geo.gphi[(size_t)q * G + gg];
+        M[i * G + gg] = m;
+      }
+  }
+  h.order.resize((size_t)n_elem);
+  for (int64_t e = 0; e < n_elem; ++e) h.order[(size_t)e] = (int32_t)e;
+  std::stable_sort(h.order.begin(), h.order.end(), [&](int32_t a, int32_t b) { return pid[(size_t)a] < pid[(size_t)b]; });
+  for (int64_t i = 0; i < n_elem;) {
+    const int p = pid[(size_t)h.order[(size_t)i]];
+    int64_t j = i;
+    while (j < n_elem && j - i < 8 && pid[(size_t)h.order[(size_t)j]] == p) ++j;
+    h.batch.push_back(p);
+    h.batch.push_back((int32_t)i);
+    h.batch.push_back((int32_t)(j - i));
+    i = j;
+  }
+  return "";
+}
+
 }  // namespace lmg

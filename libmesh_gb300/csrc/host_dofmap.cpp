@@ -321,13 +321,28 @@ lmg_status lmg_dofmap_distribute(int64_t n_nodes, int64_t n_elem, int32_t npe, c
 // distribute_local_dofs_var_major numbers, per element, the nodes not yet
 // numbered and then the element's dofs; dof_indices lists a non-vertex node's
 // dofs last to first (extra_hanging_dofs, dof_map.h:2685-2712).
-static int hier3_node_dofs(int a) { return a < 8 ? 1 : (a < 20 ? 2 : (a < 26 ? 4 : 0)); }
+// On TET14 (HIERARCHIC_n_dofs_at_node, fe_hierarchic.C:440-470) a vertex
+// carries 1 dof, an edge node 2, a face node 1, and no dof is the element's.
+struct P3Layout {
+  int npe, nl, n_interior, nsides;
+  int node_dofs(int a) const {
+    if (npe == 27) return a < 8 ? 1 : (a < 20 ? 2 : (a < 26 ? 4 : 0));
+    return a < 4 ? 1 : (a < 10 ? 2 : 1);
+  }
+};
+static bool p3_layout(int32_t elem_type, P3Layout &l) {
+  if (elem_type == LMG_HEX27) l = {27, 64, 8, 6};
+  else if (elem_type == LMG_TET14) l = {14, 20, 0, 4};
+  else return false;
+  return true;
+}
 
 lmg_status lmg_fe_dofs_per_elem(int32_t elem_type, int32_t fe_order, int32_t n_vars, int32_t *n) {
   if (!n || n_vars <= 0) return LMG_ERR_ARG;
   if (fe_order == (3 | LMG_HIERARCHIC)) {
-    if (elem_type != LMG_HEX27 || n_vars != 1) return LMG_ERR_UNSUPPORTED;
-    *n = 64;
+    P3Layout l;
+    if (!p3_layout(elem_type, l) || n_vars != 1) return LMG_ERR_UNSUPPORTED;
+    *n = l.nl;
     return LMG_OK;
   }
   const int npe = lmg::nodes_per_elem(elem_type);
@@ -341,33 +356,35 @@ lmg_status lmg_dofmap_distribute_fe(int64_t n_nodes, int64_t n_elem, int32_t ele
   if (fe_order != (3 | LMG_HIERARCHIC))
     return lmg_dofmap_distribute(n_nodes, n_elem, lmg::nodes_per_elem(elem_type), conn, n_vars, n_dofs, elem_dofs);
   if (!conn || !n_dofs || n_nodes < 0 || n_elem < 0) return LMG_ERR_ARG;
-  if (elem_type != LMG_HEX27 || n_vars != 1) return LMG_ERR_UNSUPPORTED;
+  P3Layout l;
+  if (!p3_layout(elem_type, l) || n_vars != 1) return LMG_ERR_UNSUPPORTED;
+  const int npe = l.npe, nv = lmg::vertices_per_elem(elem_type);
   try {
     std::vector<int64_t> base((size_t)n_nodes, -1), ebase((size_t)n_elem);
     int64_t next = 0;
     for (int64_t e = 0; e < n_elem; ++e) {
-      for (int a = 0; a < 27; ++a) {
-        const int32_t n = conn[e * 27 + a];
+      for (int a = 0; a < npe; ++a) {
+        const int32_t n = conn[e * npe + a];
         if (n < 0 || n >= n_nodes) return LMG_ERR_BOUNDS;
-        if (hier3_node_dofs(a) && base[(size_t)n] < 0) {
+        if (l.node_dofs(a) && base[(size_t)n] < 0) {
           base[(size_t)n] = next;
-          next += hier3_node_dofs(a);
+          next += l.node_dofs(a);
         }
       }
       ebase[(size_t)e] = next;
-      next += 8;
+      next += l.n_interior;
     }
     if (next > INT32_MAX) return LMG_ERR_UNSUPPORTED;
     *n_dofs = next;
     if (elem_dofs)
       for (int64_t e = 0; e < n_elem; ++e) {
-        int32_t *d = elem_dofs + e * 64;
-        for (int a = 0; a < 27; ++a) {
-          const int c = hier3_node_dofs(a);
-          const int64_t b = base[(size_t)conn[e * 27 + a]];
-          for (int i = 0; i < c; ++i) *d++ = (int32_t)(b + (a < 8 ? i : c - 1 - i));
+        int32_t *d = elem_dofs + e * l.nl;
+        for (int a = 0; a < npe; ++a) {
+          const int c = l.node_dofs(a);
+          const int64_t b = base[(size_t)conn[e * npe + a]];
+          for (int i = 0; i < c; ++i) *d++ = (int32_t)(b + (a < nv ? i : c - 1 - i));
         }
-        for (int i = 0; i < 8; ++i) *d++ = (int32_t)(ebase[(size_t)e] + i);
+        for (int i = 0; i < l.n_interior; ++i) *d++ = (int32_t)(ebase[(size_t)e] + i);
       }
   } catch (const std::bad_alloc &) {
     return LMG_ERR_OOM;
@@ -383,26 +400,27 @@ lmg_status lmg_dirichlet_dofs_fe(int64_t n_elem, int32_t elem_type, int32_t fe_o
     return lmg_dirichlet_dofs(n_elem, elem_type, n_vars, elem_dofs, side_bid, bids, n_bids, vars, n_vars_bc,
                               n_dofs, constrained);
   if (!elem_dofs || !side_bid || !constrained || (n_bids > 0 && !bids)) return LMG_ERR_ARG;
-  if (elem_type != LMG_HEX27 || n_vars != 1) return LMG_ERR_UNSUPPORTED;
+  P3Layout l;
+  if (!p3_layout(elem_type, l) || n_vars != 1) return LMG_ERR_UNSUPPORTED;
   std::fill(constrained, constrained + n_dofs, (uint8_t)0);
   if (n_vars_bc == 0) return LMG_OK;
   int first[27];
-  for (int a = 0, k = 0; a < 27; ++a) {
+  for (int a = 0, k = 0; a < l.npe; ++a) {
     first[a] = k;
-    k += hier3_node_dofs(a);
+    k += l.node_dofs(a);
   }
   int sn[9];
   for (int64_t e = 0; e < n_elem; ++e)
-    for (int s = 0; s < 6; ++s) {
-      const int b = side_bid[e * 6 + s];
+    for (int s = 0; s < l.nsides; ++s) {
+      const int b = side_bid[e * l.nsides + s];
       if (b < 0) continue;
       bool hit = false;
       for (int i = 0; i < n_bids; ++i) hit |= (bids[i] == b);
       if (!hit) continue;
-      const int k = lmg::side_nodes(LMG_HEX27, s, sn);
+      const int k = lmg::side_nodes(elem_type, s, sn);
       for (int j = 0; j < k; ++j)
-        for (int i = 0; i < hier3_node_dofs(sn[j]); ++i) {
-          const int32_t d = elem_dofs[e * 64 + first[sn[j]] + i];
+        for (int i = 0; i < l.node_dofs(sn[j]); ++i) {
+          const int32_t d = elem_dofs[e * l.nl + first[sn[j]] + i];
           if (d < 0 || d >= n_dofs) return LMG_ERR_BOUNDS;
           constrained[d] = 1;
         }

@@ -34,6 +34,9 @@ static const int HEX27_SIDES[6][9] = {{0, 3, 2, 1, 11, 10, 9, 8, 20},
 static const int TET4_SIDES[4][3] = {{0, 2, 1}, {0, 1, 3}, {1, 2, 3}, {2, 0, 3}};
 static const int TET10_SIDES[4][6] = {
     {0, 2, 1, 6, 5, 4}, {0, 1, 3, 4, 8, 7}, {1, 2, 3, 5, 9, 8}, {2, 0, 3, 6, 7, 9}};
+// TET14 sides (cell_tet14.C side_nodes_map): the TET10 side and its face node.
+static const int TET14_SIDES[4][7] = {
+    {0, 2, 1, 6, 5, 4, 10}, {0, 1, 3, 4, 8, 7, 11}, {1, 2, 3, 5, 9, 8, 12}, {2, 0, 3, 6, 7, 9, 13}};
 // PRISM6 sides (cell_prism6.C side_nodes_map): two triangles, three quads.
 static const int PRISM6_SIDES[5][4] = {{0, 2, 1, -1}, {0, 1, 4, 3}, {1, 2, 5, 4}, {2, 0, 3, 5}, {3, 4, 5, -1}};
 // Vertices adjacent to TET10 mid-edge nodes 4..9 (cell_tet10.C _second_order_adjacent_vertices).
@@ -43,6 +46,7 @@ int nodes_per_elem(int t) {
   switch (t) {
     case LMG_TET4: return 4;
     case LMG_TET10: return 10;
+    case LMG_TET14: return 14;
     case LMG_HEX8: return 8;
     case LMG_HEX27: return 27;
     case LMG_PRISM6: return 6;
@@ -51,7 +55,7 @@ int nodes_per_elem(int t) {
 }
 int sides_per_elem(int t) {
   switch (t) {
-    case LMG_TET4: case LMG_TET10: return 4;
+    case LMG_TET4: case LMG_TET10: case LMG_TET14: return 4;
     case LMG_HEX8: case LMG_HEX27: return 6;
     case LMG_PRISM6: return 5;
     default: return 0;
@@ -59,7 +63,7 @@ int sides_per_elem(int t) {
 }
 int vertices_per_elem(int t) {
   switch (t) {
-    case LMG_TET4: case LMG_TET10: return 4;
+    case LMG_TET4: case LMG_TET10: case LMG_TET14: return 4;
     case LMG_HEX8: case LMG_HEX27: return 8;
     case LMG_PRISM6: return 6;
     default: return 0;
@@ -71,6 +75,7 @@ int side_nodes(int t, int s, int *out) {
     case LMG_HEX27: for (int i = 0; i < 9; ++i) out[i] = HEX27_SIDES[s][i]; return 9;
     case LMG_TET4: for (int i = 0; i < 3; ++i) out[i] = TET4_SIDES[s][i]; return 3;
     case LMG_TET10: for (int i = 0; i < 6; ++i) out[i] = TET10_SIDES[s][i]; return 6;
+    case LMG_TET14: for (int i = 0; i < 7; ++i) out[i] = TET14_SIDES[s][i]; return 7;
     case LMG_PRISM6: {
       const int k = (s == 0 || s == 4) ? 3 : 4;
       for (int i = 0; i < k; ++i) out[i] = PRISM6_SIDES[s][i];

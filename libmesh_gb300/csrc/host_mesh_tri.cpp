@@ -193,6 +193,49 @@ std::string all_second_order_tet4(HostMesh &m) {
   return "";
 }
 
+// TET4 -> TET14 (MeshBase::all_complete_order, unstructured_mesh.C:60-170):
+// per element in order, the new nodes 4..13 in local order, each keyed by its
+// sorted adjacent vertices (Tet14 _second_order_adjacent_vertices: the edge's
+// two vertices for 4..9, the face's three for 10..13) and placed, when first
+// seen, at ((0 + p_a) + p_b [+ p_c]) / k over the sorted vertex ids.
+std::string all_complete_order_tet4(HostMesh &m) {
+  if (m.elem_type != LMG_TET4) return "all_complete_order: mesh is not TET4";
+  static const int ADJ[10][3] = {{0, 1, -1}, {1, 2, -1}, {0, 2, -1}, {0, 3, -1}, {1, 3, -1},
+                                 {2, 3, -1}, {0, 1, 2},  {0, 1, 3},  {1, 2, 3},  {0, 2, 3}};
+  const int64_t E = m.n_elem();
+  int64_t next = m.n_nodes();
+  std::map<std::array<int32_t, 3>, int32_t> ho_node;
+  std::vector<int32_t> conn((size_t)E * 14);
+  std::vector<double> xyz = m.xyz;
+  for (int64_t e = 0; e < E; ++e) {
+    const int32_t *c4 = &m.conn[(size_t)(e * 4)];
+    int32_t *c14 = &conn[(size_t)(e * 14)];
+    for (int a = 0; a < 4; ++a) c14[a] = c4[a];
+    for (int k = 0; k < 10; ++k) {
+      const int nv = ADJ[k][2] < 0 ? 2 : 3;
+      std::array<int32_t, 3> key = {c4[ADJ[k][0]], c4[ADJ[k][1]], nv == 3 ? c4[ADJ[k][2]] : -1};
+      std::sort(key.begin(), key.begin() + nv);
+      auto it = ho_node.find(key);
+      if (it == ho_node.end()) {
+        for (int d = 0; d < 3; ++d) {
+          double v = 0.0;
+          for (int t = 0; t < nv; ++t) v += xyz[(size_t)(3 * key[t] + d)];
+          v /= (double)nv;
+          xyz.push_back(v);
+        }
+        it = ho_node.emplace(key, (int32_t)next++).first;
+      }
+      c14[4 + k] = it->second;
+    }
+  }
+  m.elem_type = LMG_TET14;
+  m.npe = 14;
+  m.conn.swap(conn);
+  m.xyz.swap(xyz);
+  renumber_nodes_first_touch(m);
+  return "";
+}
+
 }  // namespace lmg
 
 extern "C" {
@@ -205,7 +248,7 @@ lmg_status lmg_mesh_cube(int32_t nx, int32_t ny, int32_t nz, int32_t elem_type, 
   lmg_mesh *mesh = new (std::nothrow) lmg_mesh;
   if (!mesh) return LMG_ERR_OOM;
   try {
-    const bool tets = (elem_type == LMG_TET4 || elem_type == LMG_TET10);
+    const bool tets = (elem_type == LMG_TET4 || elem_type == LMG_TET10 || elem_type == LMG_TET14);
     const int base = tets ? LMG_HEX8 : elem_type;
     std::string err = lmg::build_cube_hex(mesh->m, nx, ny, nz, base);
     if (err.empty()) lmg::jitter_interior(mesh->m, jitter, nx, ny, nz, seed);
@@ -216,6 +259,7 @@ lmg_status lmg_mesh_cube(int32_t nx, int32_t ny, int32_t nz, int32_t elem_type, 
     }
     if (err.empty() && tets) err = lmg::all_tri_hex8(mesh->m);
     if (err.empty() && elem_type == LMG_TET10) err = lmg::all_second_order_tet4(mesh->m);
+    if (err.empty() && elem_type == LMG_TET14) err = lmg::all_complete_order_tet4(mesh->m);
     if (!err.empty()) {
       delete mesh;
       return (elem_type == LMG_HEX8 || elem_type == LMG_HEX27 || elem_type == LMG_PRISM6 || tets)

@@ -115,6 +115,7 @@ std::string build_fe_tables(FETables &t, int elem_type, int fe_order, int q_orde
 // Cubic HIERARCHIC hex tables (hier3_tables.cpp): each element's 64 shape
 // variants and the tables over the variants that occur.
 struct Hier3Tables {
+  int N = 64, G = 27;            // dofs and map nodes per element
   int V = 0;                     // variants
   int q = 0;                     // quadrature points
   std::vector<uint16_t> var;     // [n_elem][64] variant of each shape
@@ -125,12 +126,29 @@ struct Hier3Tables {
   // the element's own shape order, the elements sorted by pattern, and
   // batches of at most 8 elements of one pattern.
   int P = 0;
-  std::vector<double> Dp;        // [P][6][64*64]
-  std::vector<double> Mp;        // [P][64][27]
+  std::vector<double> Dp;        // [P][6][N*N]
+  std::vector<double> Mp;        // [P][N][G]
   std::vector<int32_t> order;    // [n_elem] element ids sorted by pattern (stable)
   std::vector<int32_t> batch;    // [n_batch][3]: pattern, first index in order, count
 };
 std::string build_hier3_tables(Hier3Tables &h, int q_order, int64_t n_elem, const double *xyz, const int32_t *conn);
+
+// Orientation of a TET14 for the cubic HIERARCHIC basis: bit e of flip set
+// when edge e's order-3 basis is negated, fv[f] the vertices of face f as
+// orient_triangle sorts them.
+struct TetOrient {
+  uint8_t flip = 0;
+  uint8_t fv[4][3] = {};
+  uint32_t key() const {
+    uint32_t k = flip;
+    for (int f = 0; f < 4; ++f) k = (k << 6) | (uint32_t)(fv[f][0] << 4) | (uint32_t)(fv[f][1] << 2) | fv[f][2];
+    return k;
+  }
+};
+TetOrient tet_orient(const double *X /* [4][3] vertex coordinates */);
+// values [20] and reference gradients [20][3] (central differences, eps = 1e-6)
+int hier_tet3_shapes(const TetOrient &o, const double *p, double *v, double *g);
+std::string build_tet3_tables(Hier3Tables &h, int q_order, int64_t n_elem, const double *xyz, const int32_t *conn);
 
 // libMesh Elem::has_affine_map for one element (cell_hex8.C:121, cell_hex27.C:125,
 // cell_tet4 always, cell_tet10.C:143).

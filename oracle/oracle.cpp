@@ -30,7 +30,7 @@
 
 namespace {
 
-enum { TET4 = 8, TET10 = 9, HEX8 = 10, HEX27 = 12, PRISM6 = 13 };
+enum { TET4 = 8, TET10 = 9, HEX8 = 10, HEX27 = 12, PRISM6 = 13, TET14 = 34 };
 enum { POISSON = 0, ELASTICITY = 1 };
 
 // libMesh's _R literal: a long double literal narrowed to Real
@@ -89,6 +89,11 @@ void keast_rule(const double rule[][4], int n_pts, std::vector<Pt> &P, std::vect
       P.push_back({{a, a, b}}); P.push_back({{a, b, b}}); P.push_back({{b, b, a}});
       P.push_back({{b, a, b}}); P.push_back({{b, a, a}}); P.push_back({{a, b, a}});
       for (int j = 0; j < 6; ++j) W.push_back(wt);
+    } else {  // 12-permutation (quadrature_gauss.C:154-175), slots 0..11 in order
+      const double b = rule[p][1], c = rule[p][2];
+      const Pt o[12] = {{{a, a, b}}, {{a, a, c}}, {{b, a, a}}, {{c, a, a}}, {{a, b, a}}, {{a, c, a}},
+                        {{a, b, c}}, {{a, c, b}}, {{b, a, c}}, {{b, c, a}}, {{c, a, b}}, {{c, b, a}}};
+      for (int j = 0; j < 12; ++j) { P.push_back(o[j]); W.push_back(wt); }
     }
   }
 }
@@ -155,7 +160,7 @@ bool qgauss_3d(int type, int order, std::vector<Pt> &P, std::vector<double> &W) 
         }
     return true;
   }
-  if (type != TET4 && type != TET10) return false;
+  if (type != TET4 && type != TET10 && type != TET14) return false;
   switch (order) {
     case 0: case 1:
       P.push_back({{.25, .25, .25}}); W.push_back(1.0 / 6); return true;
@@ -177,6 +182,32 @@ bool qgauss_3d(int type, int order, std::vector<Pt> &P, std::vector<double> &W) 
           {R_(0.785714285714285714e+00), R_(0.714285714285714285e-01), 0., R_(0.762222222222222222e-02)},
           {R_(0.399403576166799219e+00), 0., R_(0.100596423833200785e+00), R_(0.248888888888888889e-01)}};
       keast_rule(rule, 3, P, W);
+      return true;
+    }
+    case 5: {  // quadrature_gauss_3D.C:231-287
+      const double a[3] = {R_(0.31088591926330060980), R_(0.092735250310891226402), R_(0.045503704125649649492)};
+      const double wt[3] = {R_(0.018781320953002641800), R_(0.012248840519393658257),
+                            R_(0.0070910034628469110730)};
+      for (int i = 0; i < 2; ++i) {
+        const double b = 1. - 3. * a[i];
+        P.push_back({{a[i], a[i], a[i]}}); P.push_back({{a[i], b, a[i]}});
+        P.push_back({{b, a[i], a[i]}}); P.push_back({{a[i], a[i], b}});
+        for (int j = 0; j < 4; ++j) W.push_back(wt[i]);
+      }
+      const double b = 0.5 * (1. - 2. * a[2]);
+      P.push_back({{b, b, a[2]}}); P.push_back({{b, a[2], a[2]}}); P.push_back({{a[2], a[2], b}});
+      P.push_back({{a[2], b, a[2]}}); P.push_back({{b, a[2], b}}); P.push_back({{a[2], b, b}});
+      for (int j = 0; j < 6; ++j) W.push_back(wt[2]);
+      return true;
+    }
+    case 6: {  // quadrature_gauss_3D.C:401-420
+      const double rule[4][4] = {
+          {R_(0.356191386222544953e+00), R_(0.214602871259151684e+00), 0., R_(0.00665379170969464506e+00)},
+          {R_(0.877978124396165982e+00), R_(0.0406739585346113397e+00), 0., R_(0.00167953517588677620e+00)},
+          {R_(0.0329863295731730594e+00), R_(0.322337890142275646e+00), 0., R_(0.00922619692394239843e+00)},
+          {R_(0.0636610018750175299e+00), R_(0.269672331458315867e+00), R_(0.603005664791649076e+00),
+           R_(0.00803571428571428248e+00)}};
+      keast_rule(rule, 4, P, W);
       return true;
     }
     default:
@@ -211,7 +242,59 @@ int n_shapes(int type, int order) {
   if (type == PRISM6) return order == 1 ? 6 : 0;
   if (type == HEX8 || type == HEX27) return order == 1 ? 8 : (type == HEX27 ? 27 : 0);
   if (type == TET4 || type == TET10) return order == 1 ? 4 : (type == TET10 ? 10 : 0);
+  if (type == TET14) return order == 1 ? 4 : 14;
   return 0;
+}
+
+// TET14 (fe_lagrange_shape_3D.C:1402-1460): quadratic shapes plus multiples
+// of the face bubbles; derivatives as written at :2931-3260.
+double tet14_shape(int i, const Pt &p) {
+  const double zeta1 = p.v[0], zeta2 = p.v[1], zeta3 = p.v[2];
+  const double zeta0 = 1. - zeta1 - zeta2 - zeta3;
+  const double bubble_012 = zeta0 * zeta1 * zeta2, bubble_013 = zeta0 * zeta1 * zeta3,
+               bubble_123 = zeta1 * zeta2 * zeta3, bubble_023 = zeta0 * zeta2 * zeta3;
+  switch (i) {
+    case 0: return zeta0 * (2. * zeta0 - 1.) + 3. * (bubble_012 + bubble_013 + bubble_023);
+    case 1: return zeta1 * (2. * zeta1 - 1.) + 3. * (bubble_012 + bubble_013 + bubble_123);
+    case 2: return zeta2 * (2. * zeta2 - 1.) + 3. * (bubble_012 + bubble_023 + bubble_123);
+    case 3: return zeta3 * (2. * zeta3 - 1.) + 3. * (bubble_013 + bubble_023 + bubble_123);
+    case 4: return 4. * zeta0 * zeta1 - 12. * (bubble_012 + bubble_013);
+    case 5: return 4. * zeta1 * zeta2 - 12. * (bubble_012 + bubble_123);
+    case 6: return 4. * zeta2 * zeta0 - 12. * (bubble_012 + bubble_023);
+    case 7: return 4. * zeta0 * zeta3 - 12. * (bubble_013 + bubble_023);
+    case 8: return 4. * zeta1 * zeta3 - 12. * (bubble_013 + bubble_123);
+    case 9: return 4. * zeta2 * zeta3 - 12. * (bubble_023 + bubble_123);
+    case 10: return 27. * bubble_012;
+    case 11: return 27. * bubble_013;
+    case 12: return 27. * bubble_123;
+    default: return 27. * bubble_023;
+  }
+}
+double tet14_deriv(int i, int j, const Pt &p) {
+  const double zeta1 = p.v[0], zeta2 = p.v[1], zeta3 = p.v[2];
+  const double zeta0 = 1. - zeta1 - zeta2 - zeta3;
+  const double dz[3][4] = {{-1., 1., 0., 0.}, {-1., 0., 1., 0.}, {-1., 0., 0., 1.}};
+  double b012, b013, b123, b023;
+  if (j == 0) { b012 = (zeta0 - zeta1) * zeta2; b013 = (zeta0 - zeta1) * zeta3; b123 = zeta2 * zeta3; b023 = -zeta2 * zeta3; }
+  else if (j == 1) { b012 = (zeta0 - zeta2) * zeta1; b013 = -zeta1 * zeta3; b123 = zeta1 * zeta3; b023 = (zeta0 - zeta2) * zeta3; }
+  else { b012 = -zeta1 * zeta2; b013 = (zeta0 - zeta3) * zeta1; b123 = zeta1 * zeta2; b023 = (zeta0 - zeta3) * zeta2; }
+  const double *d = dz[j];
+  switch (i) {
+    case 0: return (4. * zeta0 - 1.) * d[0] + 3. * (b012 + b013 + b023);
+    case 1: return (4. * zeta1 - 1.) * d[1] + 3. * (b012 + b013 + b123);
+    case 2: return (4. * zeta2 - 1.) * d[2] + 3. * (b012 + b023 + b123);
+    case 3: return (4. * zeta3 - 1.) * d[3] + 3. * (b013 + b023 + b123);
+    case 4: return 4. * (zeta0 * d[1] + d[0] * zeta1) - 12. * (b012 + b013);
+    case 5: return 4. * (zeta1 * d[2] + d[1] * zeta2) - 12. * (b012 + b123);
+    case 6: return 4. * (zeta0 * d[2] + d[0] * zeta2) - 12. * (b012 + b023);
+    case 7: return 4. * (zeta0 * d[3] + d[0] * zeta3) - 12. * (b013 + b023);
+    case 8: return 4. * (zeta1 * d[3] + d[1] * zeta3) - 12. * (b013 + b123);
+    case 9: return 4. * (zeta2 * d[3] + d[2] * zeta3) - 12. * (b023 + b123);
+    case 10: return 27. * b012;
+    case 11: return 27. * b013;
+    case 12: return 27. * b123;
+    default: return 27. * b023;
+  }
 }
 
 // fe_lagrange_3D_shape for TET4/TET10 (src/fe/fe_lagrange_shape_3D.C:710-740, 957-1010).
@@ -222,6 +305,7 @@ double tet_shape(int order, int i, const Pt &p) {
     const double z[4] = {zeta0, zeta1, zeta2, zeta3};
     return z[i];
   }
+  if (order == 3) return tet14_shape(i, p);
   switch (i) {
     case 0: return zeta0 * (2. * zeta0 - 1.);
     case 1: return zeta1 * (2. * zeta1 - 1.);
@@ -240,6 +324,7 @@ double tet_shape(int order, int i, const Pt &p) {
 double tet_shape_deriv(int order, int i, int j, const Pt &p) {
   const double dz[4][3] = {{-1., -1., -1.}, {1., 0., 0.}, {0., 1., 0.}, {0., 0., 1.}};
   if (order == 1) return dz[i][j];
+  if (order == 3) return tet14_deriv(i, j, p);
   const double zeta1 = p.v[0], zeta2 = p.v[1], zeta3 = p.v[2];
   const double zeta0 = 1. - zeta1 - zeta2 - zeta3;
   const double z[4] = {zeta0, zeta1, zeta2, zeta3};
@@ -524,6 +609,66 @@ double hier_tet_shape(unsigned i, const Pt &p) {
   return flip * crossfunc * hier_1d(basisorder, edgeval);
 }
 
+// FE<3,HIERARCHIC>::shape on a TET14 at totalorder 3
+// (fe_hierarchic_shape_3D.C:2361-2440).  Edge e of Tet4::edge_nodes_map has
+// the bases of order 2 and 3; the odd one is negated when
+// Elem::positive_edge_orientation(e) holds, i.e. the edge's first vertex is
+// greater in TypeVector's lexicographic order (elem.C:3634-3640,
+// type_vector.C:95-105).  Face f's one basis is the triangular monomial with
+// exponents (1, 1) times the third coordinate, over the face's vertices
+// sorted by orient_triangle (fe_hierarchic_shape_3D.C:2193-2243).
+bool pt_greater(const Pt &a, const Pt &b) {
+  for (int d = 0; d < 3; ++d) {
+    if (a.v[d] > b.v[d]) return true;
+    if (a.v[d] < b.v[d]) return false;
+  }
+  return false;
+}
+double hier_tet3_shape(const std::vector<Pt> &X, unsigned i, const Pt &p) {
+  const double zeta[4] = {1 - p.v[0] - p.v[1] - p.v[2], p.v[0], p.v[1], p.v[2]};
+  const unsigned totalorder = 3;
+  if (i < 4) return zeta[i];
+  static const unsigned EN[6][2] = {{0, 1}, {1, 2}, {0, 2}, {0, 3}, {1, 3}, {2, 3}};
+  if (i < 6u * totalorder - 2u) {
+    const unsigned edge_num = (i - 4) / (totalorder - 1u);
+    const unsigned basisorder = i - 2 - ((totalorder - 1u) * edge_num);
+    const unsigned v0 = EN[edge_num][0], v1 = EN[edge_num][1];
+    double flip = 1;
+    if (basisorder % 2 && pt_greater(X[v0], X[v1])) flip = -1;
+    const double crossval = zeta[v0] + zeta[v1];
+    const double edgenumerator = zeta[v1] - zeta[v0];
+    if (crossval == 0.) {
+      unsigned basisfactorial = 1;
+      for (unsigned n = 2; n <= basisorder; ++n) basisfactorial *= n;
+      return std::pow(edgenumerator, basisorder) / basisfactorial;
+    }
+    const double edgeval = edgenumerator / crossval;
+    const double crossfunc = std::pow(crossval, basisorder);
+    return flip * crossfunc * hier_1d(basisorder, edgeval);
+  }
+  static const unsigned SN[4][3] = {{0, 2, 1}, {0, 1, 3}, {1, 2, 3}, {2, 0, 3}};  // Tet4::side_nodes_map
+  const unsigned face_num = i - (6u * totalorder - 2u);
+  unsigned fv[3] = {SN[face_num][0], SN[face_num][1], SN[face_num][2]};
+  bool lastcheck = true;
+  if (pt_greater(X[fv[0]], X[fv[1]])) { std::swap(fv[0], fv[1]); lastcheck = true; }
+  if (pt_greater(X[fv[1]], X[fv[2]])) std::swap(fv[1], fv[2]);
+  if (lastcheck && pt_greater(X[fv[0]], X[fv[1]])) std::swap(fv[0], fv[1]);
+  // basisnum 0: triangular_number_column[0] = triangular_number_row[0] = 0
+  const unsigned exp0 = 0 + 1, exp1 = 0 + 1 - 0;
+  double returnval = 1;
+  for (unsigned n = 0; n != exp0; ++n) returnval *= zeta[fv[0]];
+  for (unsigned n = 0; n != exp1; ++n) returnval *= zeta[fv[1]];
+  returnval *= zeta[fv[2]];
+  return returnval;
+}
+double hier_tet3_deriv(const std::vector<Pt> &X, unsigned i, unsigned j, const Pt &p) {
+  const double eps = 1.e-6;
+  Pt pp = p, pm = p;
+  pp.v[j] += eps;
+  pm.v[j] -= eps;
+  return (hier_tet3_shape(X, i, pp) - hier_tet3_shape(X, i, pm)) / 2. / eps;
+}
+
 // FE<3,HIERARCHIC>::shape on a PRISM6, totalorder 1 (prism_indices vertices,
 // fe_hierarchic_shape_3D.C:764-810): the TRI vertex function (zeta0 =
 // 1 - xi - eta, xi, eta; fe_hierarchic_shape_2D.C:969-983) times the 1-D
@@ -595,11 +740,17 @@ bool has_affine_map(int type, const std::vector<Pt> &p) {
     const Pt v = sub(p[3], p[0]);
     return rfe(v, sub(p[4], p[1])) && rfe(v, sub(p[5], p[2]));
   }
-  if (type == TET10) {
+  if (type == TET10 || type == TET14) {
     const int E[6][3] = {{1, 0, 4}, {2, 1, 5}, {2, 0, 6}, {3, 0, 7}, {3, 1, 8}, {3, 2, 9}};
     for (auto &e : E)
       if (!rfe(sub(p[e[0]], p[e[1]]), scl(sub(p[e[2]], p[e[1]]), 2))) return false;
-    return true;
+    if (type == TET10) return true;
+    // cell_tet14.C:181-193: each face node at the face centroid
+    const Pt v10 = sub(p[1], p[0]), v20 = sub(p[2], p[0]), v30 = sub(p[3], p[0]), v21 = sub(p[2], p[1]),
+             v31 = sub(p[3], p[1]);
+    auto add = [](const Pt &a, const Pt &b) { return Pt{{a.v[0] + b.v[0], a.v[1] + b.v[1], a.v[2] + b.v[2]}}; };
+    return rfe(add(v20, v10), scl(sub(p[10], p[0]), 3)) && rfe(add(v30, v10), scl(sub(p[11], p[0]), 3)) &&
+           rfe(add(v31, v21), scl(sub(p[12], p[1]), 3)) && rfe(add(v30, v20), scl(sub(p[13], p[0]), 3));
   }
   Pt v = sub(p[1], p[0]);
   if (!rfe(v, sub(p[2], p[3])) || !rfe(v, sub(p[5], p[4])) || !rfe(v, sub(p[6], p[7]))) return false;
@@ -642,9 +793,9 @@ struct OracleFE {
     type = type_; order = order_;
     if (!qgauss_3d(type, q_order, qp, qw)) return false;
     nq = (int)qp.size();
-    const bool p3 = family == 1 && order == 3 && type == HEX27;
-    n = p3 ? 64 : n_shapes(type, order);
-    const int geo_order = (type == HEX27 || type == TET10) ? 2 : 1;
+    const bool p3 = family == 1 && order == 3 && (type == HEX27 || type == TET14);
+    n = p3 ? (type == HEX27 ? 64 : 20) : n_shapes(type, order);
+    const int geo_order = (type == HEX27 || type == TET10) ? 2 : (type == TET14 ? 3 : 1);
     n_geo = n_shapes(type, geo_order);
     if (!n || !n_geo) return false;
     if (p3) {  // element-dependent: filled by orient() per element
@@ -695,10 +846,12 @@ struct OracleFE {
   // element does not match).
   void orient(const std::vector<Pt> &X) {
     if (!(family == 1 && order == 3)) return;
+    const bool tet = type == TET14;
     for (int q = 0; q < nq; ++q)
       for (int i = 0; i < n; ++i) {
-        phi[i][q] = hier_hex3_shape(X, i, qp[q]);
-        for (int c = 0; c < 3; ++c) dref[c][i][q] = hier_hex3_deriv(X, i, c, qp[q]);
+        phi[i][q] = tet ? hier_tet3_shape(X, i, qp[q]) : hier_hex3_shape(X, i, qp[q]);
+        for (int c = 0; c < 3; ++c)
+          dref[c][i][q] = tet ? hier_tet3_deriv(X, i, c, qp[q]) : hier_hex3_deriv(X, i, c, qp[q]);
       }
   }
 
@@ -1026,8 +1179,24 @@ int orc_shapes_hier3(const double *X27, int np, const double *pts, double *phi, 
   return 64;
 }
 
+// Cubic HIERARCHIC shapes of one TET14 (node coordinates X14 [14][3]).
+int orc_shapes_tet3(const double *X14, int np, const double *pts, double *phi, double *dphi) {
+  std::vector<Pt> X(14);
+  for (int a = 0; a < 14; ++a)
+    for (int d = 0; d < 3; ++d) X[a].v[d] = X14[3 * a + d];
+  for (int q = 0; q < np; ++q) {
+    const Pt p = {{pts[3 * q], pts[3 * q + 1], pts[3 * q + 2]}};
+    for (int i = 0; i < 20; ++i) {
+      phi[i * np + q] = hier_tet3_shape(X, i, p);
+      for (int c = 0; c < 3; ++c) dphi[(c * 20 + i) * np + q] = hier_tet3_deriv(X, i, c, p);
+    }
+  }
+  return 20;
+}
+
 int orc_has_affine_map(int type, const double *X) {
-  const int n = (type == TET4) ? 4 : (type == TET10) ? 10 : (type == HEX8) ? 8 : (type == PRISM6) ? 6 : 27;
+  const int n = (type == TET4) ? 4 : (type == TET10) ? 10 : (type == TET14) ? 14 : (type == HEX8) ? 8
+              : (type == PRISM6) ? 6 : 27;
   std::vector<Pt> p(n);
   for (int a = 0; a < n; ++a)
     for (int d = 0; d < 3; ++d) p[a].v[d] = X[3 * a + d];
@@ -1101,6 +1270,57 @@ int orc_distribute_dofs_hier3(int64_t n_nodes, int64_t n_elem, const int32_t *co
     }
     for (int i = 0; i < 8; ++i) d[k++] = (int32_t)(ebase[e] + i);
   }
+  return 0;
+}
+
+// FEType{THIRD, HIERARCHIC} on TET14 (HIERARCHIC_n_dofs_at_node,
+// fe_hierarchic.C:440-470): vertex 1, edge node p - 1 = 2, face node
+// (p - 1)(p - 2)/2 = 1, no element dofs; first-touch numbering per element
+// and dof_indices listing a non-vertex node's dofs last to first.
+static int tet3_node_dofs(int n) { return n < 4 ? 1 : (n < 10 ? 2 : 1); }
+
+int orc_distribute_dofs_tet3(int64_t n_nodes, int64_t n_elem, const int32_t *conn, int32_t *elem_dofs,
+                             int64_t *n_dofs) {
+  std::vector<int64_t> base(n_nodes, -1);
+  int64_t next_free_dof = 0;
+  for (int64_t e = 0; e < n_elem; ++e)
+    for (int n = 0; n < 14; ++n) {
+      const int32_t node = conn[e * 14 + n];
+      if (base[node] == -1) {
+        base[node] = next_free_dof;
+        next_free_dof += tet3_node_dofs(n);
+      }
+    }
+  *n_dofs = next_free_dof;
+  for (int64_t e = 0; e < n_elem; ++e) {
+    int32_t *d = elem_dofs + e * 20;
+    int k = 0;
+    for (int n = 0; n < 14; ++n) {
+      const int nc = tet3_node_dofs(n);
+      const int64_t b = base[conn[e * 14 + n]];
+      if (n < 4) {
+        for (int i = 0; i < nc; ++i) d[k++] = (int32_t)(b + i);
+      } else {
+        for (int i = nc - 1; i >= 0; --i) d[k++] = (int32_t)(b + i);
+      }
+    }
+  }
+  return 0;
+}
+
+int orc_dirichlet_tet3(int64_t n_elem, const int32_t *elem_dofs, const int8_t *side_bid, const int32_t *bids,
+                       int n_bids, uint8_t *constrained) {
+  static const int T14[4][7] = {{0, 2, 1, 6, 5, 4, 10}, {0, 1, 3, 4, 8, 7, 11}, {1, 2, 3, 5, 9, 8, 12},
+                                {2, 0, 3, 6, 7, 9, 13}};  // cell_tet14.C:45-51
+  int first[14];
+  for (int n = 0, k = 0; n < 14; ++n) { first[n] = k; k += tet3_node_dofs(n); }
+  for (int64_t e = 0; e < n_elem; ++e)
+    for (int s = 0; s < 4; ++s) {
+      const int b = side_bid[e * 4 + s];
+      if (b < 0 || std::find(bids, bids + n_bids, b) == bids + n_bids) continue;
+      for (int a : T14[s])
+        for (int i = 0; i < tet3_node_dofs(a); ++i) constrained[elem_dofs[e * 20 + first[a] + i]] = 1;
+    }
   return 0;
 }
 
@@ -1214,15 +1434,15 @@ int orc_assemble2(int form, int type, int fe_order, int q_order, int64_t n_nodes
   Problem P{};
   const int family = (fe_order & 0x100) ? 1 : 0;  // HIERARCHIC flag (FEType family)
   fe_order &= 0xff;
-  const bool p3 = family == 1 && fe_order == 3 && type == HEX27;
+  const bool p3 = family == 1 && fe_order == 3 && (type == HEX27 || type == TET14);
   if (family == 1 && !hierarchic_built(type, fe_order) && !p3) return 8;
   if (p3 && (n_vars != 1 || form == ELASTICITY)) return 8;
   P.cons_ptr = cons_ptr; P.cons_col = cons_col; P.cons_val = cons_val;
   P.params = params; P.n_params = n_params;
   if (form == ADVDIFF && n_params < 2) return 1;
   P.form = form; P.type = type; P.fe_order = fe_order; P.q_order = q_order;
-  P.npe = n_shapes(type, (type == HEX27 || type == TET10) ? 2 : 1);
-  P.n_vars = n_vars; P.nl = n_vars * (p3 ? 64 : P.npe);
+  P.npe = n_shapes(type, (type == HEX27 || type == TET10) ? 2 : (type == TET14 ? 3 : 1));
+  P.n_vars = n_vars; P.nl = n_vars * (p3 ? (type == HEX27 ? 64 : 20) : P.npe);
   P.n_nodes = n_nodes; P.n_elem = n_elem; P.n_dofs = n_dofs;
   P.xyz = xyz; P.conn = conn; P.elem_dofs = elem_dofs; P.constrained = constrained;
   P.coef = coef; P.nodal_f = nodal_f; P.nu = nu; P.row_ptr = row_ptr; P.col = col;

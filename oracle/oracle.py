@@ -32,10 +32,14 @@ def lib():
         _lib.orc_shapes_hier3.argtypes = [v, i32, v, v, v]
         _lib.orc_distribute_dofs_hier3.argtypes = [i64, i64, v, v, C.POINTER(i64)]
         _lib.orc_dirichlet_hier3.argtypes = [i64, v, v, v, i32, v]
+        _lib.orc_shapes_tet3.argtypes = [v, i32, v, v, v]
+        _lib.orc_distribute_dofs_tet3.argtypes = [i64, i64, v, v, C.POINTER(i64)]
+        _lib.orc_dirichlet_tet3.argtypes = [i64, v, v, v, i32, v]
         for f in (_lib.orc_qgauss, _lib.orc_shapes, _lib.orc_has_affine_map, _lib.orc_distribute_dofs,
                   _lib.orc_dirichlet, _lib.orc_sparsity, _lib.orc_assemble, _lib.orc_assemble2,
                   _lib.orc_sparsity_constrained, _lib.orc_shapes_hier3, _lib.orc_distribute_dofs_hier3,
-                  _lib.orc_dirichlet_hier3):
+                  _lib.orc_dirichlet_hier3, _lib.orc_shapes_tet3, _lib.orc_distribute_dofs_tet3,
+                  _lib.orc_dirichlet_tet3):
             f.restype = C.c_int32
     return _lib
 
@@ -99,6 +103,33 @@ def dirichlet_hier3(elem_dofs, side_bid, bids, n_dofs):
     c = np.zeros(n_dofs, np.uint8)
     lib().orc_dirichlet_hier3(elem_dofs.shape[0], _p(np.ascontiguousarray(elem_dofs, np.int32)),
                               _p(np.ascontiguousarray(side_bid, np.int8)), _p(bids), len(bids), _p(c))
+    return c
+
+
+def shapes_tet3(X14, pts):
+    """Cubic HIERARCHIC shapes of one TET14 (node coordinates X14 [14][3]) at
+    reference points: phi [20][np], dphi [3][20][np]."""
+    pts = np.ascontiguousarray(pts, np.float64)
+    phi = np.zeros((20, len(pts)))
+    dphi = np.zeros((3, 20, len(pts)))
+    lib().orc_shapes_tet3(_p(np.ascontiguousarray(X14, np.float64)), len(pts), _p(pts), _p(phi), _p(dphi))
+    return phi, dphi
+
+
+def distribute_dofs_tet3(n_nodes, conn):
+    """FEType{THIRD, HIERARCHIC} dof numbering and dof_indices on TET14: [n_elem][20]."""
+    conn = np.ascontiguousarray(conn, np.int32)
+    ed = np.zeros((conn.shape[0], 20), np.int32)
+    nd = C.c_int64()
+    lib().orc_distribute_dofs_tet3(n_nodes, conn.shape[0], _p(conn), _p(ed), C.byref(nd))
+    return ed, nd.value
+
+
+def dirichlet_tet3(elem_dofs, side_bid, bids, n_dofs):
+    bids = np.ascontiguousarray(bids, np.int32)
+    c = np.zeros(n_dofs, np.uint8)
+    lib().orc_dirichlet_tet3(elem_dofs.shape[0], _p(np.ascontiguousarray(elem_dofs, np.int32)),
+                             _p(np.ascontiguousarray(side_bid, np.int8)), _p(bids), len(bids), _p(c))
     return c
 
 

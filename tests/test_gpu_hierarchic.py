@@ -95,3 +95,31 @@ def test_hierarchic_cubic_hex_matches_oracle(rotate, qo, n):
     assert np.all(np.abs(K - Kr) <= tol), np.max(np.abs(K - Kr) / np.maximum(tol, 1e-300))
     ftol = 1e-13 * np.abs(Fr).max()
     assert np.all(np.abs(F - Fr) <= np.maximum(1e-13 * np.abs(Fr), ftol))
+
+
+@pytest.mark.parametrize("n,jit,qo", [(2, 0.0, 6), (3, 0.25, 6), (3, 0.1, 5)])
+def test_hierarchic_cubic_tet_matches_oracle(n, jit, qo):
+    """FEType{THIRD, HIERARCHIC} on TET14 (20 dofs per element): the order-3
+    edge bases flipped by positive_edge_orientation and the face bubbles
+    multiplied in orient_triangle's order, per element; homogeneous Dirichlet
+    on every side; QGauss SIXTH / FIFTH."""
+    m = lm.Mesh.build_cube(n, n, n, lm.TET14, jitter=jit, seed=5)
+    dm = lm.DofMap(m, 1, fe_order=3 | lm.HIERARCHIC)
+    dm.add_dirichlet_boundary([0, 1, 2, 3, 4, 5], [0])
+    rng = np.random.default_rng(11)
+    k = np.exp(rng.normal(0, 0.5, m.n_elem))
+    f = rng.uniform(-1, 1, (m.n_nodes, 1))
+    asm = lm.GpuAssembly(lm.POISSON, 3 | lm.HIERARCHIC, qo, elem_coef=k, nodal_f=f)
+    asm.init(m, dm)
+    rp, ci = asm.sparsity()
+    K, F = asm.assemble()
+    asm.close()
+    rpo, cio = orc.sparsity(dm.n_dofs, dm.elem_dofs)
+    assert np.array_equal(rp, rpo) and np.array_equal(ci, cio)
+    Kr, Fr, st, _ = orc.assemble(lm.POISSON, m.elem_type, 3 | 0x100, qo, m.xyz, m.conn, 1, dm.elem_dofs, dm.n_dofs,
+                                 dm.constrained, rp, ci, coef=k, nodal_f=f)
+    assert st == 0
+    tol = k_tolerance(Kr, rp)
+    assert np.all(np.abs(K - Kr) <= tol), np.max(np.abs(K - Kr) / np.maximum(tol, 1e-300))
+    ftol = 1e-13 * np.abs(Fr).max()
+    assert np.all(np.abs(F - Fr) <= np.maximum(1e-13 * np.abs(Fr), ftol))

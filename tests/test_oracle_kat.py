@@ -35,7 +35,7 @@ def test_qgauss_hex_monomials(order):
                 assert abs(val - hex_exact(i, j, k)) < 1e-14
 
 
-@pytest.mark.parametrize("order,npts", [(1, 1), (2, 4), (3, 5), (4, 11)])
+@pytest.mark.parametrize("order,npts", [(1, 1), (2, 4), (3, 5), (4, 11), (5, 14), (6, 24)])
 def test_qgauss_tet_monomials(order, npts):
     pts, w = orc.qgauss(lm.TET10, order)
     assert len(w) == npts
@@ -109,7 +109,8 @@ def test_lagrange_reproduces_polynomials(et, order):
 
 @pytest.mark.parametrize("et,n,ne,nn", [(lm.HEX8, 3, 27, 64), (lm.HEX27, 2, 8, 125),
                                         (lm.TET4, 2, 48, 27), (lm.TET10, 2, 48, 125),
-                                        (lm.TET10, 48, 663552, 912673), (lm.PRISM6, 3, 54, 64)])
+                                        (lm.TET10, 48, 663552, 912673), (lm.TET14, 2, 48, 245),
+                                        (lm.PRISM6, 3, 54, 64)])
 def test_build_cube_counts(et, n, ne, nn):
     m = lm.Mesh.build_cube(n, n, n, et, jitter=0.2 if et in (lm.TET4, lm.TET10) else 0.0, seed=1)
     assert (m.n_elem, m.n_nodes) == (ne, nn)
