@@ -244,12 +244,13 @@ BATCH_KINDS = [  # (element, HIERARCHIC order, QGauss order, elements per grid c
     (8, 1, 2, 6),    # TET4   FIRST
     (9, 2, 4, 6),    # TET10  SECOND
     (13, 1, 3, 2),   # PRISM6 FIRST
+    (34, 3, 6, 6),   # TET14  THIRD
 ]
 
 
 def batch_members(n_meshes, seed=3, lo=1e3, hi=5e4):
     """The config-4 mix, scaled: meshes with log-uniform element counts in
-    [lo, hi], cycling through HIERARCHIC hexes (p = 1, 2, 3), tets (p = 1, 2)
+    [lo, hi], cycling through HIERARCHIC hexes (p = 1, 2, 3), tets (p = 1, 2, 3)
     and prisms (p = 1), Poisson with k_e ~ U[0.1, 10], Dirichlet on every side."""
     import libmesh_gb300 as lm
     rng = np.random.default_rng(seed)
@@ -279,7 +280,7 @@ def run_batch(args, local):
     torch.cuda.set_device(local)
     n_meshes = args.meshes
     t0 = time.perf_counter()
-    mem = batch_members(n_meshes)
+    mem = batch_members(n_meshes, hi=args.max_elems)
     setup_s = time.perf_counter() - t0
     total = sum(e for _, e in mem)
     # (a) one after another, default grids
@@ -326,9 +327,9 @@ def run_batch(args, local):
         "metric": METRIC, "value": total / (ms * 1e-3) / 1e6, "unit": "Melem/s", "n_gpus": 1, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64", "data": "synthetic (seeded sizes, coefficients, loads)",
-        "config": {"workload": "batch of %d systems (config-4 mix, scaled), element counts log-uniform in "
-                               "[1e3, 5e4]: HIERARCHIC Poisson on HEX8 p1, HEX27 p2, HEX27 p3, TET4 p1, TET10 p2, "
-                               "PRISM6 p1, k_e ~ U[0.1, 10]" % n_meshes,
+        "config": {"workload": "batch of %d systems (config-4 mix), element counts log-uniform in "
+                               "[1e3, %.0e]: HIERARCHIC Poisson on HEX8 p1, HEX27 p2, HEX27 p3, TET4 p1, TET10 p2, "
+                               "PRISM6 p1, TET14 p3, k_e ~ U[0.1, 10]" % (n_meshes, args.max_elems),
                    "total_elements": total, "total_dofs": n_dofs_total,
                    "setup_s": setup_s, "tune_s": tune_s},
         "sequential": {"ms_per_step": seq_ms, "value": total / (seq_ms * 1e-3) / 1e6, "unit": "Melem/s",
@@ -411,6 +412,8 @@ def main():
                     help="elasticity = the headline; amr-cd = refined HEX27 convection-diffusion; "
                          "batch = many mixed systems as one CUDA graph; adjoint = 128^3 sensitivities")
     ap.add_argument("--meshes", type=int, default=64, help="systems in the batch workload")
+    ap.add_argument("--max-elems", type=float, default=5e4,
+                    help="largest system of the batch workload (2e5 with --meshes 256 is the full config-4 mix)")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))

@@ -31,6 +31,11 @@ def members():
                                nodal_f=rng.uniform(-1, 1, (m.n_nodes, 1))), m, dm))
     m, dm, k, f = make_problem(4, lm.PRISM6, 1, lm.POISSON, jitter=0.2, seed=6)
     out.append((lm.GpuAssembly(lm.POISSON, 1 | lm.HIERARCHIC, 3, elem_coef=k, nodal_f=f), m, dm))
+    m = lm.Mesh.build_cube(3, 3, 3, lm.TET14, jitter=0.2, seed=7)
+    dm = lm.DofMap(m, 1, fe_order=3 | lm.HIERARCHIC)
+    dm.add_dirichlet_boundary([0, 1, 2, 3, 4, 5], [0])
+    out.append((lm.GpuAssembly(lm.POISSON, 3 | lm.HIERARCHIC, 6, elem_coef=rng.uniform(0.1, 10, m.n_elem),
+                               nodal_f=rng.uniform(-1, 1, (m.n_nodes, 1))), m, dm))
     for a, m, dm in out:
         a.init(m, dm)
     return out
