@@ -413,7 +413,7 @@ lmg_status build_plan(lmg_ctx *c) {
 // stream and copied on a second stream while the next range runs.
 // launch_elems(E0, E1) enqueues the element work of elements [E0, E1);
 // launch_rows(P0, P1) the insertion of block rows [P0, P1).
-constexpr int OUT_CHUNKS = 8;
+constexpr int OUT_CHUNKS = 32;
 template <typename LaunchElems, typename LaunchRows>
 lmg_status pipelined_copy(lmg_ctx *c, double *K, LaunchElems &&launch_elems, LaunchRows &&launch_rows) {
   if (!c->copy_stream) LMG_CUDA(c, cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
