@@ -293,7 +293,9 @@ __global__ void __launch_bounds__(128) k_elem_affine(ElemArgs a) {
 #pragma unroll
       for (int i = 0; i < NG; ++i) gv[i] = R::ld(gt[i]);
       const uint64_t mask = sMask[t];
-#pragma unroll
+      // not unrolled: one copy of the contraction keeps the hot code within
+      // the instruction caches (unrolled, the warps stalled on fetch)
+#pragma unroll 1
       for (int k = 0; k < BPL; ++k) {
         const int w = lane + 32 * k;
         if (w < NWORK) {
@@ -437,6 +439,7 @@ __global__ void __launch_bounds__(128) k_residual_affine(ElemArgs a) {
         V y[NV];
 #pragma unroll
         for (int i = 0; i < NV; ++i) y[i] = R::zero();
+#pragma unroll 1  // one copy of the contraction (instruction-cache footprint)
         for (int cb = 0; cb < N; ++cb) {
           V sv[9];
 #pragma unroll
