@@ -79,11 +79,13 @@ typedef struct lmg_mesh lmg_mesh;
  * prepare_for_use (first-touch node renumbering), src/mesh/mesh_generation.C:317-1937.
  * elem_type LMG_HEX8 or LMG_HEX27 gives the hex mesh; LMG_TET4 / LMG_TET10 gives
  * build_cube(HEX8) -> jitter -> MeshTools::Modification::all_tri (6 tets per hex,
- * src/mesh/mesh_modification.C:449-1180) [-> all_second_order for TET10].
+ * src/mesh/mesh_modification.C:449-1180) [-> all_second_order for TET10,
+ * -> all_complete_order for TET14: edge nodes and face nodes at the face
+ * centroids, src/mesh/unstructured_mesh.C:60-170, 1800-1860].
  * jitter > 0 moves every interior vertex of the HEX8 grid by an independent
  * uniform offset in [-jitter*h, +jitter*h] per coordinate, drawn from a
- * splitmix64 stream seeded with `seed`, before the tet split (so TET10 mid-edge
- * nodes sit at edge midpoints and every tet stays affine). */
+ * splitmix64 stream seeded with `seed`, before the tet split (so TET10 / TET14
+ * edge and face nodes sit at midpoints and centroids and every tet stays affine). */
 lmg_status lmg_mesh_cube(int32_t nx, int32_t ny, int32_t nz, int32_t elem_type,
                          double jitter, uint64_t seed, lmg_mesh **out);
 lmg_status lmg_mesh_info(const lmg_mesh *m, int64_t *n_nodes, int64_t *n_elem,
@@ -114,13 +116,15 @@ lmg_status lmg_dirichlet_dofs(int64_t n_elem, int32_t elem_type, int32_t n_vars,
 
 /* Dofs per element of FEType fe_order (| LMG_HIERARCHIC) on elem_type for
  * n_vars variables: n_vars * nodes for the nodal cases, 64 for
- * FEType{THIRD, HIERARCHIC} on HEX27 (HIERARCHIC_n_dofs, src/fe/fe_hierarchic.C:94-141). */
+ * FEType{THIRD, HIERARCHIC} on HEX27 and 20 on TET14 (HIERARCHIC_n_dofs,
+ * src/fe/fe_hierarchic.C:94-141, 440-470). */
 lmg_status lmg_fe_dofs_per_elem(int32_t elem_type, int32_t fe_order, int32_t n_vars, int32_t *n);
 
 /* DofMap::distribute_dofs + dof_indices for an FEType: the nodal cases as
  * lmg_dofmap_distribute; FEType{THIRD, HIERARCHIC} on HEX27 (one variable)
  * with HIERARCHIC_n_dofs_at_node's per-node counts (vertex 1, edge node 2,
- * face node 4, centre 0) and 8 element-interior dofs, numbered per element
+ * face node 4, centre 0) and 8 element-interior dofs, or on TET14 (vertex 1,
+ * edge node 2, face node 1, no interior dofs), numbered per element
  * nodes-then-element (src/base/dof_map.C:1417-1537), non-vertex node dofs
  * listed last to first (include/base/dof_map.h:2685-2712).
  * elem_dofs [n_elem][lmg_fe_dofs_per_elem]. */
@@ -202,9 +206,10 @@ lmg_status lmg_dofmap_upload(lmg_ctx *ctx, int32_t n_vars, int64_t n_dofs,
 
 /* dof_indices output for an FEType whose dofs are not one per node and
  * variable: elem_dofs[e][0 .. lmg_fe_dofs_per_elem) as
- * lmg_dofmap_distribute_fe lists them.  FEType{THIRD, HIERARCHIC} on HEX27
- * (one variable, affine elements, POISSON, LMG_FP64) assembles on the
- * general path: full element matrices, constraint product, slot gather. */
+ * lmg_dofmap_distribute_fe lists them.  FEType{THIRD, HIERARCHIC} on HEX27 or
+ * TET14 (one variable, affine elements, POISSON, LMG_FP64) assembles on the
+ * general path: full element matrices per orientation pattern, constraint
+ * product, slot gather. */
 lmg_status lmg_dofmap_upload_fe(lmg_ctx *ctx, int32_t n_vars, int32_t fe_order, int64_t n_dofs,
                                 const int32_t *elem_dofs);
 
@@ -231,8 +236,9 @@ lmg_status lmg_sparsity_copy(lmg_ctx *ctx, int32_t *row_ptr, int32_t *col_idx);
 
 /* FE family flag OR'ed into fe_order (libMesh FEType{order, family}):
  * LMG_HIERARCHIC selects HIERARCHIC (FIRST on HEX8 / TET4 / PRISM6, SECOND on
- * HEX27 / TET10, THIRD on HEX27; shapes of src/fe/fe_hierarchic_shape_3D.C with
- * cube_indices' edge and face orientation, derivatives by central differences
+ * HEX27 / TET10, THIRD on HEX27 and TET14; shapes of src/fe/fe_hierarchic_shape_3D.C
+ * with cube_indices' edge and face orientation on hexes and the edge flips and
+ * orient_triangle face order on tets, derivatives by central differences
  * as FE<3,HIERARCHIC>::shape_deriv takes them).  Without it the family is LAGRANGE. */
 enum { LMG_HIERARCHIC = 0x100 };
 
