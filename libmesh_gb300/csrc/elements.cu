@@ -122,6 +122,7 @@ template <> struct Ar<float> {
   static __device__ __forceinline__ V from(double x) { return (float)x; }
   static __device__ __forceinline__ V ld(float x) { return x; }
   static __device__ __forceinline__ V fma(V acc, V a, V b) { return fmaf(a, b, acc); }
+  static __device__ __forceinline__ V mul(V a, V b) { return __fmul_rn(a, b); }
   static __device__ __forceinline__ V norm(V x) { return x; }
 };
 template <> struct Ar<float2> {
@@ -130,6 +131,15 @@ template <> struct Ar<float2> {
   static __device__ __forceinline__ V from(double x) { return df_split(x); }
   static __device__ __forceinline__ V ld(float2 x) { return {x.x, x.y}; }
   static __device__ __forceinline__ V fma(V acc, V a, V b) { return df_fma_lazy(acc, a, b); }
+  // a * b as an unevaluated pair: TwoProduct's high part, the rounding error
+  // and the cross terms in the low part (df_fma_lazy into zero, without the sum)
+  static __device__ __forceinline__ V mul(V a, V b) {
+    const float p = __fmul_rn(a.hi, b.hi);
+    float e = __fmaf_rn(a.hi, b.hi, -p);
+    e = __fmaf_rn(a.hi, b.lo, e);
+    e = __fmaf_rn(a.lo, b.hi, e);
+    return {p, e};
+  }
   static __device__ __forceinline__ V norm(V x) { return df_norm(x); }
 };
 __device__ __forceinline__ void st(float &o, float v) { o = v; }
@@ -150,10 +160,13 @@ template <int FORM, typename R>
 __device__ __forceinline__ void contract_block(const typename R::V *gv, const typename R::V *sv,
                                                typename R::V *out) {
   using V = typename R::V;
+  // Each chain starts with a plain product; the intermediate pairs stay
+  // unnormalised (the lazy products take both parts, so the low parts only
+  // need to stay small, and every consumer of the output sums both parts).
   if (FORM == LMG_POISSON) {
-    V acc = R::zero();
+    V acc = R::mul(gv[0], sv[0]);
 #pragma unroll
-    for (int mn = 0; mn < 9; ++mn) acc = R::fma(acc, gv[mn], sv[mn]);
+    for (int mn = 1; mn < 9; ++mn) acc = R::fma(acc, gv[mn], sv[mn]);
     out[0] = R::norm(acc);
   } else {
     // P = G^T S_ab G (T = S_ab G, then G^T T); K^{ik} = lam' P^{ik} + mu' P^{ki} + d_ik mu' tr P
@@ -162,33 +175,32 @@ __device__ __forceinline__ void contract_block(const typename R::V *gv, const ty
     for (int m = 0; m < 3; ++m)
 #pragma unroll
       for (int kk = 0; kk < 3; ++kk) {
-        V acc = R::zero();
+        V acc = R::mul(sv[3 * m], gv[kk]);
 #pragma unroll
-        for (int n = 0; n < 3; ++n) acc = R::fma(acc, sv[3 * m + n], gv[3 * n + kk]);
-        Tm[3 * m + kk] = R::norm(acc);
+        for (int n = 1; n < 3; ++n) acc = R::fma(acc, sv[3 * m + n], gv[3 * n + kk]);
+        Tm[3 * m + kk] = acc;
       }
     V Pm[9];
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
       for (int kk = 0; kk < 3; ++kk) {
-        V acc = R::zero();
+        V acc = R::mul(gv[i], Tm[kk]);
 #pragma unroll
-        for (int m = 0; m < 3; ++m) acc = R::fma(acc, gv[3 * m + i], Tm[3 * m + kk]);
-        Pm[3 * i + kk] = R::norm(acc);
+        for (int m = 1; m < 3; ++m) acc = R::fma(acc, gv[3 * m + i], Tm[3 * m + kk]);
+        Pm[3 * i + kk] = acc;
       }
-    V tr = R::zero();
+    V tr = R::mul(Pm[0], R::from(1.0));
 #pragma unroll
-    for (int i = 0; i < 3; ++i) tr = R::fma(tr, Pm[4 * i], R::from(1.0));
-    tr = R::norm(tr);
+    for (int i = 1; i < 3; ++i) tr = R::fma(tr, Pm[4 * i], R::from(1.0));
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
       for (int kk = 0; kk < 3; ++kk) {
-        V acc = R::fma(R::zero(), gv[9], Pm[3 * i + kk]);
+        V acc = R::mul(gv[9], Pm[3 * i + kk]);
         acc = R::fma(acc, gv[10], Pm[3 * kk + i]);
         if (i == kk) acc = R::fma(acc, gv[10], tr);
-        out[3 * i + kk] = R::norm(acc);
+        out[3 * i + kk] = acc;
       }
   }
 }
