@@ -67,6 +67,26 @@ __device__ __forceinline__ double f2d(float f) {
 
 __device__ __forceinline__ double df_to_double(DF x) { return f2d(x.hi) + f2d(x.lo); }
 
+// Normalised double-float product (TwoProduct by FMA plus the cross terms).
+__device__ __forceinline__ DF df_mul(DF a, DF b) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  float e = __fmaf_rn(a.hi, b.hi, -p);
+  e = __fmaf_rn(a.hi, b.lo, e);
+  e = __fmaf_rn(a.lo, b.hi, e);
+  return fast_two_sum(p, e);
+}
+
+__device__ __forceinline__ DF df_sub(DF a, DF b) { return df_add(a, DF{-b.hi, -b.lo}); }
+
+// 1 / x: the rounded FP32 reciprocal refined by one Newton step in
+// double-float, r + r (1 - x r), about 2^-46 relative for normal x.
+__device__ __forceinline__ DF df_recip(DF x) {
+  const float r = __frcp_rn(x.hi);
+  const DF xr = df_mul(x, DF{r, 0.f});
+  const DF e = df_sub(DF{1.f, 0.f}, xr);
+  return fast_two_sum(r, __fmul_rn(r, e.hi));
+}
+
 __host__ __device__ __forceinline__ DF df_split(double x) {
   const float hi = (float)x;
   return {hi, (float)(x - (double)hi)};

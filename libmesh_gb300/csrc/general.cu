@@ -36,12 +36,6 @@ namespace {
 
 constexpr int WARPS = 8;
 
-__device__ __forceinline__ double warp_allsum(double v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
-}
-
 // Tensor indices of a hex node in the 1-D Lagrange bases (0 at -1, 1 at +1,
 // 2 at 0), packed as i + 3 j + 9 k: HEX27 node order of cell_hex27.C, HEX8
 // node order of cell_hex8.C.
@@ -152,61 +146,69 @@ __global__ void __launch_bounds__(WARPS * 32) k_elem_full(GenElemArgs a) {
     scurl[i] = make_float2(x.hi, x.lo);
   }
   __shared__ DF sL1[9];
+  __shared__ DF sJd[WARPS][9];  // map derivatives of each warp's element
   for (int i = threadIdx.x; i < N1 * Q1; i += blockDim.x) sL1[i] = df_split(a.D6[6 * N * N + i]);
   const double gp = a.D6[6 * N * N + N1 * Q1];  // outer 1-D Gauss point (+gp, -gp, and 0 when Q1 = 3)
   __syncthreads();
   const int64_t stride = (int64_t)gridDim.x * WARPS;
   for (int64_t e = (int64_t)blockIdx.x * WARPS + warp; e < a.n_elem; e += stride) {
     // geometry and nodal load of this element
-    double jp[9];
-#pragma unroll
-    for (int i = 0; i < 9; ++i) jp[i] = 0.0;
     if (lane < N) {
       const int64_t nd = a.conn[e * N + lane];
-      const double x = a.xyz[3 * nd], y = a.xyz[3 * nd + 1], z = a.xyz[3 * nd + 2];
-      sX[3 * lane] = x;
-      sX[3 * lane + 1] = y;
-      sX[3 * lane + 2] = z;
+      sX[3 * lane] = a.xyz[3 * nd];
+      sX[3 * lane + 1] = a.xyz[3 * nd + 1];
+      sX[3 * lane + 2] = a.xyz[3 * nd + 2];
       const DF fv = df_split(a.nodal_f ? a.nodal_f[nd] : 0.0);
       sf[lane] = make_float2(fv.hi, fv.lo);
-#pragma unroll
-      for (int m = 0; m < 3; ++m) {
-        const double g = sgd[3 * lane + m];
-        jp[3 * m + 0] = x * g;
-        jp[3 * m + 1] = y * g;
-        jp[3 * m + 2] = z * g;
-      }
     }
+    __syncwarp();
+    // The elements here are affine hexahedra (form_set refuses the others), so
+    // the constant map derivatives are the edge vectors from vertex 0 to
+    // vertices 1, 3 and 4 over the reference edge length 2: the value of
+    // compute_affine_map's sum over the nodes, in 9 subtractions.  Lane j < 9
+    // forms entry j in FP64 and splits it; the inverse map, detJ and the
+    // diffusion tensor then run in double-float on the FP32 pipe.
+    if (lane < 9) {
+      const int m = lane / 3, d = lane - 3 * m, v = m == 0 ? 1 : (m == 1 ? 3 : 4);
+      sJd[warp][lane] = df_split(0.5 * (sX[3 * v + d] - sX[d]));
+    }
+    __syncwarp();
+    DF J[9];
 #pragma unroll
-    for (int i = 0; i < 9; ++i) jp[i] = warp_allsum(jp[i]);
-    // jp[m*3+d] = d x_d / d xi_m; G[3m+d] = d xi_m / d x_d (fe_map.C:1046-1068)
-    const double c0 = jp[4] * jp[8] - jp[5] * jp[7], c1 = jp[5] * jp[6] - jp[3] * jp[8],
-                 c2 = jp[3] * jp[7] - jp[4] * jp[6];
-    const double det = jp[0] * c0 + jp[1] * c1 + jp[2] * c2;
-    const double inv = 1.0 / det;
-    double G[9];
-    G[0] = c0 * inv;
-    G[1] = c1 * inv;
-    G[2] = c2 * inv;
-    G[3] = (jp[2] * jp[7] - jp[1] * jp[8]) * inv;
-    G[4] = (jp[0] * jp[8] - jp[2] * jp[6]) * inv;
-    G[5] = (jp[1] * jp[6] - jp[0] * jp[7]) * inv;
-    G[6] = (jp[1] * jp[5] - jp[2] * jp[4]) * inv;
-    G[7] = (jp[2] * jp[3] - jp[0] * jp[5]) * inv;
-    G[8] = (jp[0] * jp[4] - jp[1] * jp[3]) * inv;
-    if (lane == 0 && !(det > 0.0)) {
+    for (int j = 0; j < 9; ++j) J[j] = sJd[warp][j];
+    // J[m*3+d] = d x_d / d xi_m; G[3m+d] = d xi_m / d x_d (fe_map.C:1046-1068)
+    const DF c0 = df_sub(df_mul(J[4], J[8]), df_mul(J[5], J[7]));
+    const DF c1 = df_sub(df_mul(J[5], J[6]), df_mul(J[3], J[8]));
+    const DF c2 = df_sub(df_mul(J[3], J[7]), df_mul(J[4], J[6]));
+    const DF det = df_add(df_add(df_mul(J[0], c0), df_mul(J[1], c1)), df_mul(J[2], c2));
+    const DF inv = df_recip(det);
+    DF G[9];
+    G[0] = df_mul(c0, inv);
+    G[1] = df_mul(c1, inv);
+    G[2] = df_mul(c2, inv);
+    G[3] = df_mul(df_sub(df_mul(J[2], J[7]), df_mul(J[1], J[8])), inv);
+    G[4] = df_mul(df_sub(df_mul(J[0], J[8]), df_mul(J[2], J[6])), inv);
+    G[5] = df_mul(df_sub(df_mul(J[1], J[6]), df_mul(J[0], J[7])), inv);
+    G[6] = df_mul(df_sub(df_mul(J[1], J[5]), df_mul(J[2], J[4])), inv);
+    G[7] = df_mul(df_sub(df_mul(J[2], J[3]), df_mul(J[0], J[5])), inv);
+    G[8] = df_mul(df_sub(df_mul(J[0], J[4]), df_mul(J[1], J[3])), inv);
+    if (lane == 0 && !(det.hi > 0.f)) {
       atomicCAS(a.status, 0, LMG_ERR_DEGENERATE);
       atomicMin(a.bad_elem, (unsigned long long)e);
     }
     const double coef = a.coef ? a.coef[e] : 1.0;
-    const double kap = (FORM == LMG_ADVDIFF ? a.kappa * coef : coef) * det;
-    double A[6];
-    A[0] = kap * (G[0] * G[0] + G[1] * G[1] + G[2] * G[2]);
-    A[1] = kap * (G[3] * G[3] + G[4] * G[4] + G[5] * G[5]);
-    A[2] = kap * (G[6] * G[6] + G[7] * G[7] + G[8] * G[8]);
-    A[3] = kap * (G[0] * G[3] + G[1] * G[4] + G[2] * G[5]);
-    A[4] = kap * (G[0] * G[6] + G[1] * G[7] + G[2] * G[8]);
-    A[5] = kap * (G[3] * G[6] + G[4] * G[7] + G[5] * G[8]);
+    const DF kap = df_mul(df_split(FORM == LMG_ADVDIFF ? a.kappa * coef : coef), det);
+    auto gg = [&](int m, int n) {
+      return df_add(df_add(df_mul(G[3 * m], G[3 * n]), df_mul(G[3 * m + 1], G[3 * n + 1])),
+                    df_mul(G[3 * m + 2], G[3 * n + 2]));
+    };
+    DF A2[6];
+    A2[0] = df_mul(kap, gg(0, 0));
+    A2[1] = df_mul(kap, gg(1, 1));
+    A2[2] = df_mul(kap, gg(2, 2));
+    A2[3] = df_mul(kap, gg(0, 1));
+    A2[4] = df_mul(kap, gg(0, 2));
+    A2[5] = df_mul(kap, gg(1, 2));
     __syncwarp();
     if (FORM == LMG_ADVDIFF) {
       // exp(i (k.x + phase)) at the element centre and exp(i gp k.dx/dxi_m):
@@ -220,8 +222,10 @@ __global__ void __launch_bounds__(WARPS * 32) k_elem_full(GenElemArgs a) {
         if (w == 0) {
           ang = md[3] * xc[0] + md[4] * xc[1] + md[5] * xc[2] + md[6];
         } else {
-          const int m = w - 1;
-          ang = gp * (md[3] * jp[3 * m] + md[4] * jp[3 * m + 1] + md[5] * jp[3 * m + 2]);
+          const int v = w == 1 ? 1 : (w == 2 ? 3 : 4);  // d x / d xi_{w-1}
+          const double j0 = 0.5 * (sX[3 * v] - sX[0]), j1 = 0.5 * (sX[3 * v + 1] - sX[1]),
+                       j2 = 0.5 * (sX[3 * v + 2] - sX[2]);
+          ang = gp * (md[3] * j0 + md[4] * j1 + md[5] * j2);
         }
         double sn, cs;
         sincos(ang, &sn, &cs);
@@ -238,9 +242,8 @@ __global__ void __launch_bounds__(WARPS * 32) k_elem_full(GenElemArgs a) {
       DF fx = {0.f, 0.f};
       for (int c = 0; c < N; ++c) fx = df_fma_lazy(fx, ld_df(sphi + q * N + c), ld_df(sf + c));  // FE-interpolated load
       fx = df_norm(fx);
-      const double jxw = det * sqw[q];
-      const DF jw = df_split(jxw);
-      const DF fq = df_norm(df_fma_lazy(DF{0.f, 0.f}, jw, fx));
+      const DF jw = df_mul(det, df_split(sqw[q]));
+      const DF fq = df_mul(jw, fx);
       sfq[q] = make_float2(fq.hi, fq.lo);
       if (FORM == LMG_ADVDIFF) {
         DF b[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
@@ -269,8 +272,8 @@ __global__ void __launch_bounds__(WARPS * 32) k_elem_full(GenElemArgs a) {
         for (int m = 0; m < 3; ++m) {
           DF t = {0.f, 0.f};
 #pragma unroll
-          for (int d = 0; d < 3; ++d) t = df_fma_lazy(t, df_split(jxw * G[3 * m + d]), b[d]);
-          t = df_norm(t);
+          for (int d = 0; d < 3; ++d) t = df_fma_lazy(t, G[3 * m + d], b[d]);
+          t = df_mul(jw, df_norm(t));
           sbeta[3 * q + m] = make_float2(t.hi, t.lo);
         }
       }
@@ -298,9 +301,6 @@ __global__ void __launch_bounds__(WARPS * 32) k_elem_full(GenElemArgs a) {
         for (int i = 0; i < N1 * Q1; ++i) L1[i] = sL1[i];
         tensor_contract_df<N1, Q1>(L1, P, Cc);
       }
-      DF A2[6];
-#pragma unroll
-      for (int t = 0; t < 6; ++t) A2[t] = df_split(A[t]);
       float2 *Ke = a.Kraw + e * (N * N);
 #pragma unroll
       for (int r = 0; r < N; ++r) {
