@@ -36,6 +36,55 @@ namespace {
 
 constexpr int WARPS = 8;
 
+// sin and cos of x, the series in double-float arithmetic (FP32 pipe).  Cody
+// and Waite's reduction in FP64, x = k pi/2 + r, k = rint(x 2/pi),
+// r = ((x - k P1) - k P2) - k P3 with pi/2 = P1 + P2 + P3 as doubles, each
+// step one FMA (one rounding), so that r keeps the absolute accuracy of x;
+// then r as a double-float pair and the Taylor series of sin and cos in r^2 on
+// |r| <= pi/4 (9 and 10 terms: the first neglected term is below 2^-54 of the
+// leading one) by Horner in double-float, and the quadrant's signs.  The
+// coefficients (-1)^i / (2i+1)! and (-1)^i / (2i)! are stored as float pairs.
+__device__ __forceinline__ void df_sincos(double xd, DF &s, DF &c) {
+  constexpr float SIN[9][2] = {{1.0f, 0.f},
+                               {-0.1666666716337204f, 4.967053879312289e-09f},
+                               {0.008333333767950535f, -4.34617203337595e-10f},
+                               {-0.00019841270113829523f, 2.725596874933456e-12f},
+                               {2.7557318844628753e-06f, 3.793571224297229e-14f},
+                               {-2.5052107943679403e-08f, -4.4176230446483665e-16f},
+                               {1.6059044372074283e-10f, -5.352526511562726e-18f},
+                               {-7.647163609812713e-13f, -1.2200710471178288e-20f},
+                               {2.8114573589663704e-15f, -1.0462084739763658e-22f}};
+  constexpr float COS[10][2] = {{1.0f, 0.f},
+                                {-0.5f, 0.f},
+                                {0.0416666679084301f, -1.2417634698280722e-09f},
+                                {-0.0013888889225199819f, 3.3631094437103215e-11f},
+                                {2.4801587642286904e-05f, -3.40699609366682e-13f},
+                                {-2.755731998149713e-07f, 7.575112209051195e-15f},
+                                {2.0876755879584152e-09f, 1.1082839147459852e-16f},
+                                {-1.147074536050896e-11f, -2.372207689231238e-19f},
+                                {4.7794772561329454e-14f, 7.62544404448643e-22f},
+                                {-1.5619206814541513e-16f, -1.5404471465941993e-24f}};
+  const double kd = rint(xd * 0.6366197723675814);
+  const double rd = fma(-kd, -1.4973849048591698e-33, fma(-kd, 6.123233995736766e-17, fma(-kd, 1.5707963267948966, xd)));
+  const DF r = df_split(rd);
+  const float k = (float)kd;
+  const DF r2 = df_mul(r, r);
+  DF ps = DF{SIN[8][0], SIN[8][1]};
+#pragma unroll
+  for (int i = 7; i >= 0; --i) ps = df_add(df_mul(ps, r2), DF{SIN[i][0], SIN[i][1]});
+  const DF sr = df_mul(ps, r);
+  DF pc = DF{COS[9][0], COS[9][1]};
+#pragma unroll
+  for (int i = 8; i >= 0; --i) pc = df_add(df_mul(pc, r2), DF{COS[i][0], COS[i][1]});
+  const DF nsr = DF{-sr.hi, -sr.lo}, npc = DF{-pc.hi, -pc.lo};
+  switch (((int)k) & 3) {
+    case 0: s = sr; c = pc; break;
+    case 1: s = pc; c = nsr; break;
+    case 2: s = nsr; c = npc; break;
+    default: s = npc; c = sr; break;
+  }
+}
+
 // Tensor indices of a hex node in the 1-D Lagrange bases (0 at -1, 1 at +1,
 // 2 at 0), packed as i + 3 j + 9 k: HEX27 node order of cell_hex27.C, HEX8
 // node order of cell_hex8.C.
@@ -227,9 +276,8 @@ __global__ void __launch_bounds__(WARPS * 32) k_elem_full(GenElemArgs a) {
                        j2 = 0.5 * (sX[3 * v + 2] - sX[2]);
           ang = gp * (md[3] * j0 + md[4] * j1 + md[5] * j2);
         }
-        double sn, cs;
-        sincos(ang, &sn, &cs);
-        const DF c2 = df_split(cs), s2 = df_split(sn);
+        DF s2, c2;
+        df_sincos(ang, s2, c2);
         sE[2 * t] = make_float2(c2.hi, c2.lo);
         sE[2 * t + 1] = make_float2(s2.hi, s2.lo);
       }
