@@ -51,6 +51,8 @@ constexpr unsigned FULL = 0xffffffffu;
 
 // Jacobian at one point from the mapping shape derivatives gd [n_geo][3] and
 // element coordinates X [n_geo][3]; returns detJ and G[m][d] = dxi_m / dx_d.
+__device__ __forceinline__ double invert_map(const double J[9], double G[9]);
+
 __device__ __forceinline__ double jacobian(const double *X, const double *gd, int n_geo,
                                            double G[9]) {
   double J[9];  // J[m*3+d] = d x_d / d xi_m
@@ -66,6 +68,28 @@ __device__ __forceinline__ double jacobian(const double *X, const double *gd, in
       J[3 * m + 2] += z * g;
     }
   }
+  return invert_map(J, G);
+}
+
+// The constant map of an affine element (compute_affine_map's value) from the
+// edge vectors of its vertices: tets v1 - v0, v2 - v0, v3 - v0; hexahedra
+// (v1 - v0) / 2, (v3 - v0) / 2, (v4 - v0) / 2 (reference edge length 2);
+// prisms v1 - v0, v2 - v0, (v3 - v0) / 2.  N, the element's node count,
+// identifies the type (4, 10 tets; 8, 27 hexahedra; 6 prisms).
+template <int N>
+__device__ __forceinline__ double jacobian_affine(const double *X, double G[9]) {
+  constexpr bool hex = (N == 8 || N == 27);
+  constexpr int v[3] = {1, hex ? 3 : 2, hex ? 4 : 3};
+  constexpr double sc[3] = {hex ? 0.5 : 1.0, hex ? 0.5 : 1.0, (hex || N == 6) ? 0.5 : 1.0};
+  double J[9];
+#pragma unroll
+  for (int m = 0; m < 3; ++m)
+#pragma unroll
+    for (int d = 0; d < 3; ++d) J[3 * m + d] = sc[m] * (X[3 * v[m] + d] - X[d]);
+  return invert_map(J, G);
+}
+
+__device__ __forceinline__ double invert_map(const double J[9], double G[9]) {
   const double xxi = J[0], yxi = J[1], zxi = J[2];
   const double xet = J[3], yet = J[4], zet = J[5];
   const double xze = J[6], yze = J[7], zze = J[8];
@@ -258,7 +282,7 @@ __global__ void __launch_bounds__(128) k_elem_affine(ElemArgs a) {
           X[3 * g + 1] = p[1];
           X[3 * g + 2] = p[2];
         }
-        det = jacobian(X, a.fe.gdphi, N, G);
+        det = jacobian_affine<N>(X, G);
       }
       if (!(det > 0.0)) report_bad(a, LMG_ERR_DEGENERATE, e);
       const double coef = a.coef ? a.coef[e] : 1.0;
@@ -394,7 +418,7 @@ __global__ void __launch_bounds__(128) k_residual_affine(ElemArgs a) {
           X[3 * g + 1] = p[1];
           X[3 * g + 2] = p[2];
         }
-        det = jacobian(X, a.fe.gdphi, N, G);
+        det = jacobian_affine<N>(X, G);
       }
       if (!(det > 0.0)) report_bad(a, LMG_ERR_DEGENERATE, e);
       const double coef = a.coef ? a.coef[e] : 1.0;
@@ -674,7 +698,7 @@ __global__ void __launch_bounds__(128) k_geo(FusedArgs f) {
         X[3 * g + 1] = p[1];
         X[3 * g + 2] = p[2];
       }
-      det = jacobian(X, a.fe.gdphi, N, G);
+      det = jacobian_affine<N>(X, G);
     }
     if (!(det > 0.0)) report_bad(a, LMG_ERR_DEGENERATE, e);
     const double coef = a.coef ? a.coef[e] : 1.0;
