@@ -738,7 +738,7 @@ __global__ void __launch_bounds__(128) k_geo(FusedArgs f) {
 }
 
 template <int FORM, int N, int NV>
-__global__ void __launch_bounds__(256) k_rows_mixed(FusedArgs f) {
+__global__ void __launch_bounds__(256, 6) k_rows_mixed(FusedArgs f) {
   using R = Ar<float>;
   constexpr int NG = Geo<FORM>::NG, B2 = NV * NV, NPASS = 32 / N, SPL = 32 / B2;
   extern __shared__ float fsm[];
