@@ -272,7 +272,8 @@ lmg_status lmg_synchronize(lmg_ctx *ctx);
 /* Jacobi-preconditioned CG on the last assembled K (LinearImplicitSystem::solve
  * with KSPCG, src/systems/linear_implicit_system.C:122-165): solves K x = rhs
  * (host array; NULL = the last assembled F) until ||r|| <= rtol ||rhs|| or maxit
- * iterations; x is a host array of n_dofs. */
+ * iterations; x is a host array of n_dofs.  A right-hand side holding NaN or
+ * Inf returns LMG_ERR_ARG without iterating. */
 lmg_status lmg_cg_solve(lmg_ctx *ctx, const double *rhs, double *x, double rtol, int32_t maxit,
                         int32_t *iters, double *relres);
 
@@ -289,14 +290,19 @@ lmg_status lmg_cg_solve(lmg_ctx *ctx, const double *rhs, double *x, double rtol,
  * lmg_assemble), rhs[n_dofs], x[n_dofs] (output).  Its work vectors live in one
  * fixed device array inside the library, 5 x LMG_CG_NOALLOC_MAX_DOFS doubles
  * (20 MiB); n_dofs above LMG_CG_NOALLOC_MAX_DOFS returns LMG_ERR_ARG and says
- * so in msg.  The first call on each device looks up that array's address on
- * the current device (cudaGetSymbolAddress): make that first call before any
- * stream capture.  Every call on a device shares the one array, so calls whose
+ * so in msg.  The first call on each device does the set-up: it looks up that
+ * array's address on the current device (cudaGetSymbolAddress), and looks it up
+ * again whenever the current driver context is a new one (after
+ * cudaDeviceReset, say); make that first call before any stream capture
+ * begins.  Every call on a device shares the one array, so calls whose
  * work overlaps on the GPU (other streams, other host threads) race and give
  * wrong results: serialize them.  The scalar slots are cleared at the start of
  * every call; every other word is written before it is read.  stream is a
- * cudaStream_t (NULL = the legacy default stream); the call returns once the
- * solve has finished on it.  msg (may be NULL) receives the error text. */
+ * cudaStream_t (NULL = the legacy default stream); each call synchronizes that
+ * stream and reads the residual back to the host while it iterates, and
+ * returns once the solve has finished on it.  A right-hand side holding NaN or
+ * Inf returns LMG_ERR_ARG, as lmg_cg_solve does.  msg (may be NULL) receives
+ * the error text. */
 #define LMG_CG_NOALLOC_MAX_DOFS 524288
 lmg_status lmg_cg_solve_noalloc(int64_t n_dofs, const int32_t *row_ptr, const int32_t *col_idx,
                                 const double *val, const double *rhs, double *x, double rtol,

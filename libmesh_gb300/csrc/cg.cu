@@ -9,6 +9,7 @@
 // last block to finish sums the partials in block order), so repeated solves
 // give identical iterates.  Scalars stay on the device; the host reads the
 // residual every 16 iterations.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -220,13 +221,27 @@ __global__ void k_init(int64_t n, const double *b, double *x, double *r, double 
 
 // sc layout: [0], [1] rz of the current / next iteration (the initial rr in
 // [1]), [2] pq, [3] rr, [4] two block counters of the reducing kernels
+namespace {
+// The solver's work vectors, freed on every return path.
+struct CgWork {
+  double *r = nullptr, *z = nullptr, *p = nullptr, *q = nullptr, *dinv = nullptr, *partial = nullptr,
+         *sc = nullptr;
+  ~CgWork() {
+    for (double *v : {r, z, p, q, dinv, partial, sc})
+      if (v) cudaFree(v);
+  }
+};
+}  // namespace
+
 int cg_solve(int64_t n, const int32_t *rp, const int32_t *col, const double *val, const double *b, double *x,
              double rtol, int maxit, cudaStream_t s, int n_sm, int *iters, double *relres, int64_t *launches) {
-  double *r, *z, *p, *q, *dinv, *partial, *sc;
+  CgWork w;
   const size_t bytes = sizeof(double) * (size_t)n;
-  if (cudaMalloc(&r, bytes) || cudaMalloc(&z, bytes) || cudaMalloc(&p, bytes) || cudaMalloc(&q, bytes) ||
-      cudaMalloc(&dinv, bytes) || cudaMalloc(&partial, sizeof(double) * 2 * RBLK) || cudaMalloc(&sc, sizeof(double) * 8))
+  if (cudaMalloc(&w.r, bytes) || cudaMalloc(&w.z, bytes) || cudaMalloc(&w.p, bytes) || cudaMalloc(&w.q, bytes) ||
+      cudaMalloc(&w.dinv, bytes) || cudaMalloc(&w.partial, sizeof(double) * 2 * RBLK) ||
+      cudaMalloc(&w.sc, sizeof(double) * 8))
     return 7;
+  double *r = w.r, *z = w.z, *p = w.p, *q = w.q, *dinv = w.dinv, *partial = w.partial, *sc = w.sc;
   cudaMemsetAsync(sc, 0, sizeof(double) * 8, s);  // sc[4] holds the two block counters
   unsigned int *cnt = reinterpret_cast<unsigned int *>(sc + 4);
   const int g1 = n_sm * 8, gs = n_sm * 64;
@@ -247,6 +262,10 @@ int cg_solve(int64_t n, const int32_t *rp, const int32_t *col, const double *val
   const double bnorm = std::sqrt(h[1]);
   double rn = bnorm;
   int it = 0;
+  if (!std::isfinite(bnorm)) {  // NaN or Inf in the right-hand side: nothing to iterate on
+    *launches += L;
+    return cudaStreamSynchronize(s) == cudaSuccess ? 3 : 2;
+  }
   if (bnorm == 0.0) {
     *iters = 0;
     *relres = 0.0;
@@ -266,7 +285,6 @@ int cg_solve(int64_t n, const int32_t *rp, const int32_t *col, const double *val
   }
   *launches += L;
   cudaError_t e = cudaStreamSynchronize(s);
-  cudaFree(r); cudaFree(z); cudaFree(p); cudaFree(q); cudaFree(dinv); cudaFree(partial); cudaFree(sc);
   return e == cudaSuccess ? 0 : 2;
 }
 
@@ -290,16 +308,48 @@ static __device__ __align__(256) double g_cg_scratch[5 * NA_DOFS + 2 * lmg::RBLK
 std::mutex g_na_mutex;
 double *g_na_base[NA_DEVICES] = {};
 int g_na_sm[NA_DEVICES] = {};
+unsigned long long g_na_ctx[NA_DEVICES] = {};  // driver context the cached address belongs to
 
 lmg_status na_fail(char *msg, int32_t len, lmg_status code, const char *text) {
   if (msg && len > 0) std::snprintf(msg, (size_t)len, "%s", text);
   return code;
 }
 
-// Once per device, with that device current: the array's device address.
+// Unique id of the calling thread's current driver context (cuCtxGetId ids
+// are never reused, so a context re-created by cudaDeviceReset gets a new one).
+// The two driver calls are looked up through the runtime; 0 if unavailable.
+unsigned long long na_context_id() {
+  using GetCur = CUresult (*)(CUcontext *);
+  using GetId = CUresult (*)(CUcontext, unsigned long long *);
+  static GetCur get_cur = nullptr;
+  static GetId get_id = nullptr;
+  static bool looked = false;
+  if (!looked) {
+    looked = true;
+    void *f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_cur = reinterpret_cast<GetCur>(f);
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<GetId>(f);
+  }
+  CUcontext ctx = nullptr;
+  unsigned long long id = 0;
+  if (!get_cur || !get_id || get_cur(&ctx) != CUDA_SUCCESS || !ctx || get_id(ctx, &id) != CUDA_SUCCESS) return 0;
+  return id;
+}
+
+// Set-up, with the device current: the array's device address on that device.
+// Done on the first call on each device and again whenever the current
+// context differs from the one the address was taken in (after
+// cudaDeviceReset, or under a context the caller made current); when the
+// context id cannot be read, the address is looked up on every call.
 cudaError_t na_setup(int dev, double **base, int *n_sm) {
   std::lock_guard<std::mutex> lock(g_na_mutex);
-  if (!g_na_base[dev]) {
+  const unsigned long long ctx = na_context_id();
+  if (!g_na_base[dev] || ctx == 0 || ctx != g_na_ctx[dev]) {
     void *p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, g_cg_scratch);
     if (e != cudaSuccess) return e;
@@ -308,6 +358,7 @@ cudaError_t na_setup(int dev, double **base, int *n_sm) {
     if (e != cudaSuccess) return e;
     g_na_sm[dev] = sm;
     g_na_base[dev] = static_cast<double *>(p);
+    g_na_ctx[dev] = ctx;
   }
   *base = g_na_base[dev];
   *n_sm = g_na_sm[dev];
@@ -359,6 +410,8 @@ extern "C" lmg_status lmg_cg_solve_noalloc(int64_t n, const int32_t *rp, const i
   const double bnorm = std::sqrt(h[1]);
   double rn = bnorm;
   int it = 0;
+  if (!std::isfinite(bnorm))  // the same status lmg_cg_solve returns
+    return na_fail(msg, msg_len, LMG_ERR_ARG, "cg_solve_noalloc: the right-hand side is not finite");
   if (bnorm > 0.0) {
     unsigned int *cnt = reinterpret_cast<unsigned int *>(sc + 4);  // cleared with the scalar slots
     for (it = 0; it < maxit; ++it) {

@@ -1249,21 +1249,24 @@ lmg_status lmg_cg_solve(lmg_ctx *c, const double *rhs, double *x, double rtol, i
   if (!c || !x || rtol <= 0 || maxit <= 0) return fail(c, LMG_ERR_ARG, "cg_solve: bad argument");
   if (!c->have_sparsity) return fail(c, LMG_ERR_STATE, "cg_solve: assemble first");
   cudaSetDevice(c->device);
-  double *b = c->d_F, *dx = nullptr, *db = nullptr;
-  LMG_CUDA(c, dalloc(dx, (size_t)c->n_dofs));
+  struct Bufs {  // the solution and right-hand side on the device, freed on every return path
+    double *dx = nullptr, *db = nullptr;
+    ~Bufs() { dfree(dx); dfree(db); }
+  } w;
+  double *b = c->d_F;
+  LMG_CUDA(c, dalloc(w.dx, (size_t)c->n_dofs));
   if (rhs) {
-    LMG_CUDA(c, dupload(c, db, rhs, (size_t)c->n_dofs));
-    b = db;
+    LMG_CUDA(c, dupload(c, w.db, rhs, (size_t)c->n_dofs));
+    b = w.db;
   }
   int it = 0;
   double rr = 0.0;
-  const int st = cg_solve(c->n_dofs, c->d_row_ptr, c->d_col, c->d_K, b, dx, rtol, maxit, c->stream, c->n_sm,
+  const int st = cg_solve(c->n_dofs, c->d_row_ptr, c->d_col, c->d_K, b, w.dx, rtol, maxit, c->stream, c->n_sm,
                           &it, &rr, &c->launches);
   if (st == 0)
-    LMG_CUDA(c, cudaMemcpyAsync(x, dx, sizeof(double) * c->n_dofs, cudaMemcpyDeviceToHost, c->stream));
+    LMG_CUDA(c, cudaMemcpyAsync(x, w.dx, sizeof(double) * c->n_dofs, cudaMemcpyDeviceToHost, c->stream));
   LMG_CUDA(c, cudaStreamSynchronize(c->stream));
-  dfree(dx);
-  dfree(db);
+  if (st == 3) return fail(c, LMG_ERR_ARG, "cg_solve: the right-hand side is not finite");
   if (st) return fail(c, st == 7 ? LMG_ERR_OOM : LMG_ERR_CUDA, "cg_solve: device failure");
   if (iters) *iters = it;
   if (relres) *relres = rr;

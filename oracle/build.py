@@ -1,6 +1,7 @@
-"""Build recipe for the CPU oracle (test infrastructure): oracle/oracle.cpp and
-oracle/oracle_constraints.cpp -> oracle/_build/liboracle.so, compiled with
--ffp-contract=off so that no multiply-add is fused."""
+"""Build recipe for the CPU oracle (test infrastructure): oracle/oracle.cpp,
+oracle/oracle_constraints.cpp and oracle/oracle_mesh.cpp ->
+oracle/_build/liboracle.so, compiled with -ffp-contract=off so that no
+multiply-add is fused."""
 import os
 import subprocess
 
@@ -9,7 +10,7 @@ LIB = os.path.join(HERE, "_build", "liboracle.so")
 
 
 def build(force=False):
-    srcs = [os.path.join(HERE, f) for f in ("oracle.cpp", "oracle_constraints.cpp")]
+    srcs = [os.path.join(HERE, f) for f in ("oracle.cpp", "oracle_constraints.cpp", "oracle_mesh.cpp")]
     if not force and os.path.exists(LIB) and all(os.path.getmtime(LIB) >= os.path.getmtime(s) for s in srcs):
         return LIB
     os.makedirs(os.path.dirname(LIB), exist_ok=True)

@@ -35,6 +35,14 @@ def lib():
         _lib.orc_shapes_tet3.argtypes = [v, i32, v, v, v]
         _lib.orc_distribute_dofs_tet3.argtypes = [i64, i64, v, v, C.POINTER(i64)]
         _lib.orc_dirichlet_tet3.argtypes = [i64, v, v, v, i32, v]
+        _lib.orc_mesh_cube.argtypes = [i32, i32, i32, i32, f64, C.c_uint64]
+        _lib.orc_mesh_cube.restype = v
+        _lib.orc_mesh_info.argtypes = [v, C.POINTER(i64), C.POINTER(i64), C.POINTER(i32), C.POINTER(i32)]
+        _lib.orc_mesh_info.restype = None
+        _lib.orc_mesh_copy.argtypes = [v, v, v, v]
+        _lib.orc_mesh_copy.restype = None
+        _lib.orc_mesh_free.argtypes = [v]
+        _lib.orc_mesh_free.restype = None
         for f in (_lib.orc_qgauss, _lib.orc_shapes, _lib.orc_has_affine_map, _lib.orc_distribute_dofs,
                   _lib.orc_dirichlet, _lib.orc_sparsity, _lib.orc_assemble, _lib.orc_assemble2,
                   _lib.orc_sparsity_constrained, _lib.orc_shapes_hier3, _lib.orc_distribute_dofs_hier3,
@@ -65,6 +73,25 @@ def shapes(elem_type, order, pts):
     assert n > 0
     dphi = dphi.reshape(-1)[:3 * n * np_].reshape(3, n, np_)
     return phi.reshape(-1)[:n * np_].reshape(n, np_).copy(), dphi.copy()
+
+
+def mesh_cube(n, elem_type, jitter=0.0, seed=0):
+    """build_cube(n^3) restated (oracle_mesh.cpp): HEX8 / HEX27 directly, TET4 /
+    TET10 through all_tri [and all_second_order], interior vertices jittered
+    by +-jitter*h before the split.  Returns (xyz [n_nodes][3], conn
+    [n_elem][npe], side_bid [n_elem][n_sides])."""
+    h = lib().orc_mesh_cube(n, n, n, elem_type, float(jitter), seed)
+    assert h, "orc_mesh_cube: bad argument"
+    try:
+        nn, ne, npe, ns = C.c_int64(), C.c_int64(), C.c_int32(), C.c_int32()
+        lib().orc_mesh_info(h, C.byref(nn), C.byref(ne), C.byref(npe), C.byref(ns))
+        xyz = np.zeros((nn.value, 3))
+        conn = np.zeros((ne.value, npe.value), np.int32)
+        sb = np.zeros((ne.value, ns.value), np.int8)
+        lib().orc_mesh_copy(h, _p(xyz), _p(conn), _p(sb))
+    finally:
+        lib().orc_mesh_free(h)
+    return xyz, conn, sb
 
 
 def has_affine_map(elem_type, X):

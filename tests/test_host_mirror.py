@@ -125,3 +125,16 @@ def test_hier3_dofs_and_dirichlet_match_oracle(rotate):
     for bids in ([0, 1, 2, 3, 4, 5], [2], [0, 5]):
         c = lm.DofMap(m, 1, fe_order=3 | lm.HIERARCHIC).add_dirichlet_boundary(bids, [0])
         assert np.array_equal(c, orc.dirichlet_hier3(ed, m.side_bid, bids, nd))
+
+
+@pytest.mark.parametrize("et,n,jit", [(lm.HEX8, 5, 0.0), (lm.HEX8, 4, 0.2), (lm.HEX27, 3, 0.0), (lm.TET4, 4, 0.2),
+                                      (lm.TET10, 5, 0.2), (lm.TET10, 6, 0.0), (lm.TET10, 16, 0.2)])
+def test_mesh_generation_matches_oracle(et, n, jit):
+    """build_cube (+ all_tri, all_second_order) through the C ABI against the
+    oracle's step-by-step restatement: coordinates, connectivity and side
+    boundary ids bit for bit."""
+    m = lm.Mesh.build_cube(n, n, n, et, jitter=jit, seed=1)
+    xyz, conn, sb = orc.mesh_cube(n, et, jit, 1)
+    assert np.array_equal(xyz, m.xyz)
+    assert np.array_equal(conn, m.conn)
+    assert np.array_equal(sb, m.side_bid)
