@@ -947,8 +947,7 @@ lmg_status lmg_assemble(lmg_ctx *c, int32_t precision, double *K, double *F, int
   if (precision != LMG_FP64 && precision != LMG_MIXED) return fail(c, LMG_ERR_ARG, "assemble: unknown precision");
   cudaSetDevice(c->device);
   if (c->general) {
-    if (precision != LMG_FP64)
-      return fail(c, LMG_ERR_UNSUPPORTED, "assemble: the constrained / convection path computes in FP64 only");
+    const bool mixed = precision == LMG_MIXED;
     if (!c->gen_plan) {
       lmg_status st = general_plan(c);
       if (st) return st;
@@ -961,9 +960,9 @@ lmg_status lmg_assemble(lmg_ctx *c, int32_t precision, double *K, double *F, int
       for (auto &e : e3) c->ev.push_back(e);
       LMG_CUDA(c, cudaEventRecord(e3[0], c->stream));
     }
-    general_assemble(c);
+    general_assemble(c, mixed);
     if (c->perflog) LMG_CUDA(c, cudaEventRecord(e3[1], c->stream));
-    general_gather(c);
+    general_gather(c, mixed);
     if (c->perflog) LMG_CUDA(c, cudaEventRecord(e3[2], c->stream));
     LMG_CUDA(c, cudaGetLastError());
     const cudaMemcpyKind kind = out_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;

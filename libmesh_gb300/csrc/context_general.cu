@@ -257,7 +257,7 @@ lmg_status general_plan(lmg_ctx *c) {
   return LMG_OK;
 }
 
-lmg_status general_assemble(lmg_ctx *c) {
+lmg_status general_assemble(lmg_ctx *c, bool mixed) {
   GenElemArgs a{};
   a.n_elem = c->n_elem;
   a.xyz = c->d_xyz;
@@ -268,13 +268,13 @@ lmg_status general_assemble(lmg_ctx *c) {
   a.kappa = c->kappa;
   a.n_modes = c->n_modes;
   a.modes = c->d_modes;
-  a.Kraw = reinterpret_cast<float2 *>(c->d_Ebuf);
+  a.Kraw = c->d_Ebuf;
   a.Fraw = c->d_Fbuf;
   a.status = c->d_status;
   a.bad_elem = c->d_bad;
   a.fe = c->dfe;
-  if (c->hier3) launch_hier3(c);
-  else launch_gen_elements(c->form, c->tab.n, c->tab.q, a, c->n_sm * c->ctas_per_sm / 4, c->stream);
+  if (c->hier3) launch_hier3(c, mixed);
+  else launch_gen_elements(c->form, c->tab.n, c->tab.q, mixed, a, c->n_sm * c->ctas_per_sm / 4, c->stream);
   c->launches++;
   if (c->n_cons_elem) {
     ConsArgs k{};
@@ -292,20 +292,20 @@ lmg_status general_assemble(lmg_ctx *c) {
     k.ci = c->d_cci;
     k.cv = c->d_ccv;
     k.rowmask = c->d_crow;
-    k.Kraw = reinterpret_cast<const float2 *>(c->d_Ebuf);
+    k.Kraw = c->d_Ebuf;
     k.Fraw = c->d_Fbuf;
-    k.Ebuf = reinterpret_cast<float2 *>(c->d_Ebuf);
+    k.Ebuf = c->d_Ebuf;
     k.Fbuf = c->d_Fbuf;
-    launch_constrain(k, c->n_sm, c->stream);
+    launch_constrain(k, mixed, c->n_sm, c->stream);
     c->launches++;
   }
   return LMG_OK;
 }
 
-void general_gather(lmg_ctx *c) {
-  // element matrices are double-float pairs (element and constraint kernels)
-  launch_gather_full_df(c->nnz, c->d_cptr, c->d_coff, reinterpret_cast<const float2 *>(c->d_Ebuf), c->d_K,
-                        c->n_dofs, c->d_gfptr, c->d_gfoff, c->d_Fbuf, c->d_F, c->n_sm, c->stream);
+void general_gather(lmg_ctx *c, bool mixed) {
+  // element matrices are double (FP64 drop-in) or float (mixed form)
+  launch_gather_full(c->nnz, c->d_cptr, c->d_coff, c->d_Ebuf, mixed, c->d_K, c->n_dofs, c->d_gfptr, c->d_gfoff,
+                     c->d_Fbuf, c->d_F, c->n_sm, c->stream);
   c->launches++;
 }
 

@@ -150,13 +150,14 @@ inline cudaError_t dupload(lmg_ctx *c, T *&p, const T *h, size_t n) {
 // general.cu path (context_general.cu)
 lmg_status general_sparsity(lmg_ctx *c);   // CSR with the constraint couplings
 lmg_status general_plan(lmg_ctx *c);       // constraint columns, slot plan, buffers
-lmg_status general_assemble(lmg_ctx *c);   // element and constraint kernels
-void general_gather(lmg_ctx *c);           // slot gather into K and F
+// element and constraint kernels; mixed: FP32 contraction, FP64 map and sums
+lmg_status general_assemble(lmg_ctx *c, bool mixed);
+void general_gather(lmg_ctx *c, bool mixed);  // slot gather into K and F
 // hier3.cu
 void hier3_free(lmg_ctx *c);
 lmg_status hier3_form_set(lmg_ctx *c, int32_t form, int32_t q_order, const double *elem_coef,
                           const double *nodal_f);
-void launch_hier3(lmg_ctx *c);
+void launch_hier3(lmg_ctx *c, bool mixed);
 bool hier3_masks(const lmg_ctx *c);  // Dirichlet rows applied by the element kernel
 void general_free(lmg_ctx *c);             // plan and work buffers
 

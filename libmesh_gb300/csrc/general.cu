@@ -36,54 +36,17 @@ namespace {
 
 constexpr int WARPS = 8;
 
-// sin and cos of x, the series in double-float arithmetic (FP32 pipe).  Cody
-// and Waite's reduction in FP64, x = k pi/2 + r, k = rint(x 2/pi),
-// r = ((x - k P1) - k P2) - k P3 with pi/2 = P1 + P2 + P3 as doubles, each
-// step one FMA (one rounding), so that r keeps the absolute accuracy of x;
-// then r as a double-float pair and the Taylor series of sin and cos in r^2 on
-// |r| <= pi/4 (9 and 10 terms: the first neglected term is below 2^-54 of the
-// leading one) by Horner in double-float, and the quadrant's signs.  The
-// coefficients (-1)^i / (2i+1)! and (-1)^i / (2i)! are stored as float pairs.
-__device__ __forceinline__ void df_sincos(double xd, DF &s, DF &c) {
-  constexpr float SIN[9][2] = {{1.0f, 0.f},
-                               {-0.1666666716337204f, 4.967053879312289e-09f},
-                               {0.008333333767950535f, -4.34617203337595e-10f},
-                               {-0.00019841270113829523f, 2.725596874933456e-12f},
-                               {2.7557318844628753e-06f, 3.793571224297229e-14f},
-                               {-2.5052107943679403e-08f, -4.4176230446483665e-16f},
-                               {1.6059044372074283e-10f, -5.352526511562726e-18f},
-                               {-7.647163609812713e-13f, -1.2200710471178288e-20f},
-                               {2.8114573589663704e-15f, -1.0462084739763658e-22f}};
-  constexpr float COS[10][2] = {{1.0f, 0.f},
-                                {-0.5f, 0.f},
-                                {0.0416666679084301f, -1.2417634698280722e-09f},
-                                {-0.0013888889225199819f, 3.3631094437103215e-11f},
-                                {2.4801587642286904e-05f, -3.40699609366682e-13f},
-                                {-2.755731998149713e-07f, 7.575112209051195e-15f},
-                                {2.0876755879584152e-09f, 1.1082839147459852e-16f},
-                                {-1.147074536050896e-11f, -2.372207689231238e-19f},
-                                {4.7794772561329454e-14f, 7.62544404448643e-22f},
-                                {-1.5619206814541513e-16f, -1.5404471465941993e-24f}};
-  const double kd = rint(xd * 0.6366197723675814);
-  const double rd = fma(-kd, -1.4973849048591698e-33, fma(-kd, 6.123233995736766e-17, fma(-kd, 1.5707963267948966, xd)));
-  const DF r = df_split(rd);
-  const float k = (float)kd;
-  const DF r2 = df_mul(r, r);
-  DF ps = DF{SIN[8][0], SIN[8][1]};
-#pragma unroll
-  for (int i = 7; i >= 0; --i) ps = df_add(df_mul(ps, r2), DF{SIN[i][0], SIN[i][1]});
-  const DF sr = df_mul(ps, r);
-  DF pc = DF{COS[9][0], COS[9][1]};
-#pragma unroll
-  for (int i = 8; i >= 0; --i) pc = df_add(df_mul(pc, r2), DF{COS[i][0], COS[i][1]});
-  const DF nsr = DF{-sr.hi, -sr.lo}, npc = DF{-pc.hi, -pc.lo};
-  switch (((int)k) & 3) {
-    case 0: s = sr; c = pc; break;
-    case 1: s = pc; c = nsr; break;
-    case 2: s = nsr; c = npc; break;
-    default: s = npc; c = sr; break;
-  }
-}
+// Arithmetic of the element contraction: T = double for the FP64 drop-in,
+// T = float for the mixed form.  The map (J, detJ, J^-1) is FP64 in both.
+template <typename T> struct GA;
+template <> struct GA<double> {
+  static __device__ __forceinline__ double fma_(double a, double b, double c) { return fma(a, b, c); }
+  static __device__ __forceinline__ void sincos_(double x, double &s, double &c) { sincos(x, &s, &c); }
+};
+template <> struct GA<float> {
+  static __device__ __forceinline__ float fma_(float a, float b, float c) { return fmaf(a, b, c); }
+  static __device__ __forceinline__ void sincos_(double x, float &s, float &c) { sincosf((float)x, &s, &c); }
+};
 
 // Tensor indices of a hex node in the 1-D Lagrange bases (0 at -1, 1 at +1,
 // 2 at 0), packed as i + 3 j + 9 k: HEX27 node order of cell_hex27.C, HEX8
@@ -106,31 +69,31 @@ __host__ __device__ constexpr int hex_tensor(int n, int a) {
 }
 
 // C_rb = sum_q phi_r(q) P(q) for the tensor-product element: phi_r(q) =
-// L_i(x_q1) L_j(x_q2) L_k(x_q3), q = q1 + Q1 (q2 + Q1 q3); three 1-D passes,
-// in double-float arithmetic (FP32 pipe), every inner sum renormalised once.
-template <int N1, int Q1>
-__device__ __forceinline__ void tensor_contract_df(const DF *L1, const DF *P, DF *Cc) {
-  DF T1[N1 * Q1 * Q1];
+// L_i(x_q1) L_j(x_q2) L_k(x_q3), q = q1 + Q1 (q2 + Q1 q3); three 1-D passes.
+template <int N1, int Q1, typename T>
+__device__ __forceinline__ void tensor_contract(const T *L1, const T *P, T *Cc) {
+  using A = GA<T>;
+  T T1[N1 * Q1 * Q1];
 #pragma unroll
   for (int i = 0; i < N1; ++i)
 #pragma unroll
     for (int r = 0; r < Q1 * Q1; ++r) {
-      DF t = {0.f, 0.f};
+      T t = 0;
 #pragma unroll
-      for (int q1 = 0; q1 < Q1; ++q1) t = df_fma_lazy(t, L1[i * Q1 + q1], P[q1 + Q1 * r]);
-      T1[i * Q1 * Q1 + r] = df_norm(t);
+      for (int q1 = 0; q1 < Q1; ++q1) t = A::fma_(L1[i * Q1 + q1], P[q1 + Q1 * r], t);
+      T1[i * Q1 * Q1 + r] = t;
     }
-  DF T2[N1 * N1 * Q1];
+  T T2[N1 * N1 * Q1];
 #pragma unroll
   for (int i = 0; i < N1; ++i)
 #pragma unroll
     for (int j = 0; j < N1; ++j)
 #pragma unroll
       for (int q3 = 0; q3 < Q1; ++q3) {
-        DF t = {0.f, 0.f};
+        T t = 0;
 #pragma unroll
-        for (int q2 = 0; q2 < Q1; ++q2) t = df_fma_lazy(t, L1[j * Q1 + q2], T1[i * Q1 * Q1 + q2 + Q1 * q3]);
-        T2[(i * N1 + j) * Q1 + q3] = df_norm(t);
+        for (int q2 = 0; q2 < Q1; ++q2) t = A::fma_(L1[j * Q1 + q2], T1[i * Q1 * Q1 + q2 + Q1 * q3], t);
+        T2[(i * N1 + j) * Q1 + q3] = t;
       }
 #pragma unroll
   for (int i = 0; i < N1; ++i)
@@ -138,65 +101,65 @@ __device__ __forceinline__ void tensor_contract_df(const DF *L1, const DF *P, DF
     for (int j = 0; j < N1; ++j)
 #pragma unroll
       for (int k = 0; k < N1; ++k) {
-        DF t = {0.f, 0.f};
+        T t = 0;
 #pragma unroll
-        for (int q3 = 0; q3 < Q1; ++q3) t = df_fma_lazy(t, L1[k * Q1 + q3], T2[(i * N1 + j) * Q1 + q3]);
-        Cc[i + 3 * j + 9 * k] = df_norm(t);
+        for (int q3 = 0; q3 < Q1; ++q3) t = A::fma_(L1[k * Q1 + q3], T2[(i * N1 + j) * Q1 + q3], t);
+        Cc[i + 3 * j + 9 * k] = t;
       }
 }
 
-inline __device__ DF ld_df(const float2 *p) {
-  const float2 v = *p;
-  return DF{v.x, v.y};
-}
+// Byte layout of k_elem_full's dynamic shared memory (T = element arithmetic).
+template <typename T>
+struct FullSmem {
+  int N, Q, modes;
+  __host__ __device__ size_t al8(size_t x) const { return (x + 7) & ~(size_t)7; }
+  __host__ __device__ size_t phi() const { return 0; }                                  // [Q][N] T
+  __host__ __device__ size_t dphi() const { return al8(phi() + sizeof(T) * Q * N); }      // [Q][N][3] T
+  __host__ __device__ size_t D() const { return al8(dphi() + sizeof(T) * Q * N * 3); }     // [6][N][N] T
+  __host__ __device__ size_t curl() const { return al8(D() + sizeof(T) * 6 * N * N); }     // [modes][3] T
+  __host__ __device__ size_t qw() const { return al8(curl() + sizeof(T) * 3 * modes); }    // [Q] double
+  __host__ __device__ size_t mode() const { return qw() + sizeof(double) * Q; }          // [7 modes] double
+  __host__ __device__ size_t warp0() const { return mode() + sizeof(double) * 7 * modes; }
+  // per warp: X [N][3] double, then f [N], beta [Q][3], fq [Q], E [modes][4][2] in T
+  __host__ __device__ size_t per_warp() const {
+    return al8(sizeof(double) * N * 3 + sizeof(T) * (N + 4 * Q + 8 * modes));
+  }
+  __host__ __device__ size_t bytes(int warps) const { return warp0() + per_warp() * warps; }
+};
 
-template <int FORM, int N, int Q>
+template <int FORM, int N, int Q, typename T>
 __global__ void __launch_bounds__(WARPS * 32) k_elem_full(GenElemArgs a) {
+  using A = GA<T>;
   constexpr int N1 = (N == 8) ? 2 : 3, Q1 = (Q == 8) ? 2 : 3;
-  extern __shared__ double sm[];
-  float2 *sphi = reinterpret_cast<float2 *>(sm);                   // [Q][N] double-float
-  float2 *sdphi = sphi + Q * N;                                     // [Q][N][3] double-float
-  float2 *sD = sdphi + Q * N * 3;                                   // [6][N][N] double-float
-  double *sqw = reinterpret_cast<double *>(sD + 6 * N * N);       // [Q]
-  double *sgd = sqw + Q;              // [N][3] mapping derivatives at qp 0
-  double *sgp = sgd + N * 3;          // [Q][N] mapping shapes (isoparametric geometry)
-  double *smode = sgp + Q * N;        // [7 * n_modes]
-  float2 *scurl = reinterpret_cast<float2 *>(smode + 7 * a.n_modes);  // [n_modes][3] k x a, double-float
-  double *wbase = reinterpret_cast<double *>(scurl + 3 * a.n_modes);
+  extern __shared__ __align__(16) unsigned char gsm[];
+  const FullSmem<T> L{N, Q, a.n_modes};
+  T *sphi = reinterpret_cast<T *>(gsm + L.phi());
+  T *sdphi = reinterpret_cast<T *>(gsm + L.dphi());
+  T *sD = reinterpret_cast<T *>(gsm + L.D());
+  T *scurl = reinterpret_cast<T *>(gsm + L.curl());
+  double *sqw = reinterpret_cast<double *>(gsm + L.qw());
+  double *smode = reinterpret_cast<double *>(gsm + L.mode());
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  double *sX = wbase + warp * (N * 3 + N + 4 * Q + 8 * a.n_modes);  // [N][3]
-  float2 *sf = reinterpret_cast<float2 *>(sX + N * 3);  // [N] nodal load, double-float
-  float2 *sbeta = sf + N;                               // [Q][3] double-float
-  float2 *sfq = sbeta + 3 * Q;                          // [Q] JxW f(x_q), double-float
-  float2 *sE = sfq + Q;                                 // [n_modes][4] (cos, sin), double-float
-  for (int i = threadIdx.x; i < Q * N; i += blockDim.x) {
-    const DF x = df_split(a.fe.phi[i]);
-    sphi[i] = make_float2(x.hi, x.lo);
-  }
-  for (int i = threadIdx.x; i < Q * N * 3; i += blockDim.x) {
-    const DF x = df_split(a.fe.dphi[i]);
-    sdphi[i] = make_float2(x.hi, x.lo);
-  }
-  for (int i = threadIdx.x; i < 6 * N * N; i += blockDim.x) {
-    const DF x = df_split(a.D6[i]);
-    sD[i] = make_float2(x.hi, x.lo);
-  }
+  double *sX = reinterpret_cast<double *>(gsm + L.warp0() + L.per_warp() * warp);  // [N][3]
+  T *sf = reinterpret_cast<T *>(sX + N * 3);  // [N] nodal load
+  T *sbeta = sf + N;                          // [Q][3] JxW (J^-1 b)
+  T *sfq = sbeta + 3 * Q;                     // [Q] JxW f(x_q)
+  T *sE = sfq + Q;                            // [n_modes][4] (cos, sin)
+  for (int i = threadIdx.x; i < Q * N; i += blockDim.x) sphi[i] = (T)a.fe.phi[i];
+  for (int i = threadIdx.x; i < Q * N * 3; i += blockDim.x) sdphi[i] = (T)a.fe.dphi[i];
+  for (int i = threadIdx.x; i < 6 * N * N; i += blockDim.x) sD[i] = (T)a.D6[i];
   for (int i = threadIdx.x; i < Q; i += blockDim.x) sqw[i] = a.fe.qw[i];
-  for (int i = threadIdx.x; i < N * 3; i += blockDim.x) sgd[i] = a.fe.gdphi[i];
-  for (int i = threadIdx.x; i < Q * N; i += blockDim.x) sgp[i] = a.fe.gphi[i];
   for (int i = threadIdx.x; i < 7 * a.n_modes; i += blockDim.x) smode[i] = a.modes[i];
   for (int i = threadIdx.x; i < 3 * a.n_modes; i += blockDim.x) {  // b = sum_m cos(.) k_m x a_m
     const double *md = a.modes + 7 * (i / 3);
     const int d = i % 3;
-    const double v = d == 0 ? md[4] * md[2] - md[5] * md[1]
-                     : d == 1 ? md[5] * md[0] - md[3] * md[2]
-                              : md[3] * md[1] - md[4] * md[0];
-    const DF x = df_split(v);
-    scurl[i] = make_float2(x.hi, x.lo);
+    scurl[i] = (T)(d == 0 ? md[4] * md[2] - md[5] * md[1]
+                   : d == 1 ? md[5] * md[0] - md[3] * md[2]
+                            : md[3] * md[1] - md[4] * md[0]);
   }
-  __shared__ DF sL1[9];
-  __shared__ DF sJd[WARPS][9];  // map derivatives of each warp's element
-  for (int i = threadIdx.x; i < N1 * Q1; i += blockDim.x) sL1[i] = df_split(a.D6[6 * N * N + i]);
+  __shared__ T sL1[9];
+  __shared__ double sG[WARPS][10];  // J^-1 (dxi_m/dx_d at [3m + d]) and detJ of each warp's element
+  for (int i = threadIdx.x; i < N1 * Q1; i += blockDim.x) sL1[i] = (T)a.D6[6 * N * N + i];
   const double gp = a.D6[6 * N * N + N1 * Q1];  // outer 1-D Gauss point (+gp, -gp, and 0 when Q1 = 3)
   __syncthreads();
   const int64_t stride = (int64_t)gridDim.x * WARPS;
@@ -207,58 +170,57 @@ __global__ void __launch_bounds__(WARPS * 32) k_elem_full(GenElemArgs a) {
       sX[3 * lane] = a.xyz[3 * nd];
       sX[3 * lane + 1] = a.xyz[3 * nd + 1];
       sX[3 * lane + 2] = a.xyz[3 * nd + 2];
-      const DF fv = df_split(a.nodal_f ? a.nodal_f[nd] : 0.0);
-      sf[lane] = make_float2(fv.hi, fv.lo);
+      sf[lane] = (T)(a.nodal_f ? a.nodal_f[nd] : 0.0);
     }
     __syncwarp();
     // The elements here are affine hexahedra (form_set refuses the others), so
     // the constant map derivatives are the edge vectors from vertex 0 to
     // vertices 1, 3 and 4 over the reference edge length 2: the value of
-    // compute_affine_map's sum over the nodes, in 9 subtractions.  Lane j < 9
-    // forms entry j in FP64 and splits it; the inverse map, detJ and the
-    // diffusion tensor then run in double-float on the FP32 pipe.
-    if (lane < 9) {
-      const int m = lane / 3, d = lane - 3 * m, v = m == 0 ? 1 : (m == 1 ? 3 : 4);
-      sJd[warp][lane] = df_split(0.5 * (sX[3 * v + d] - sX[d]));
-    }
-    __syncwarp();
-    DF J[9];
+    // compute_affine_map's sum over the nodes.  J, detJ and J^-1 in FP64
+    // (fe_map.C:1046-1068), by lane 0.
+    if (lane == 0) {
+      double J[9];  // J[m*3+d] = d x_d / d xi_m
 #pragma unroll
-    for (int j = 0; j < 9; ++j) J[j] = sJd[warp][j];
-    // J[m*3+d] = d x_d / d xi_m; G[3m+d] = d xi_m / d x_d (fe_map.C:1046-1068)
-    const DF c0 = df_sub(df_mul(J[4], J[8]), df_mul(J[5], J[7]));
-    const DF c1 = df_sub(df_mul(J[5], J[6]), df_mul(J[3], J[8]));
-    const DF c2 = df_sub(df_mul(J[3], J[7]), df_mul(J[4], J[6]));
-    const DF det = df_add(df_add(df_mul(J[0], c0), df_mul(J[1], c1)), df_mul(J[2], c2));
-    const DF inv = df_recip(det);
-    DF G[9];
-    G[0] = df_mul(c0, inv);
-    G[1] = df_mul(c1, inv);
-    G[2] = df_mul(c2, inv);
-    G[3] = df_mul(df_sub(df_mul(J[2], J[7]), df_mul(J[1], J[8])), inv);
-    G[4] = df_mul(df_sub(df_mul(J[0], J[8]), df_mul(J[2], J[6])), inv);
-    G[5] = df_mul(df_sub(df_mul(J[1], J[6]), df_mul(J[0], J[7])), inv);
-    G[6] = df_mul(df_sub(df_mul(J[1], J[5]), df_mul(J[2], J[4])), inv);
-    G[7] = df_mul(df_sub(df_mul(J[2], J[3]), df_mul(J[0], J[5])), inv);
-    G[8] = df_mul(df_sub(df_mul(J[0], J[4]), df_mul(J[1], J[3])), inv);
-    if (lane == 0 && !(det.hi > 0.f)) {
-      atomicCAS(a.status, 0, LMG_ERR_DEGENERATE);
-      atomicMin(a.bad_elem, (unsigned long long)e);
+      for (int m = 0; m < 3; ++m) {
+        const int v = m == 0 ? 1 : (m == 1 ? 3 : 4);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) J[3 * m + d] = 0.5 * (sX[3 * v + d] - sX[d]);
+      }
+      const double c0 = J[4] * J[8] - J[5] * J[7], c1 = J[5] * J[6] - J[3] * J[8], c2 = J[3] * J[7] - J[4] * J[6];
+      const double det = J[0] * c0 + J[1] * c1 + J[2] * c2;
+      const double inv = 1.0 / det;
+      double *G = sG[warp];
+      G[0] = c0 * inv;
+      G[1] = c1 * inv;
+      G[2] = c2 * inv;
+      G[3] = (J[2] * J[7] - J[1] * J[8]) * inv;
+      G[4] = (J[0] * J[8] - J[2] * J[6]) * inv;
+      G[5] = (J[1] * J[6] - J[0] * J[7]) * inv;
+      G[6] = (J[1] * J[5] - J[2] * J[4]) * inv;
+      G[7] = (J[2] * J[3] - J[0] * J[5]) * inv;
+      G[8] = (J[0] * J[4] - J[1] * J[3]) * inv;
+      G[9] = det;
+      if (!(det > 0.0)) {
+        atomicCAS(a.status, 0, LMG_ERR_DEGENERATE);
+        atomicMin(a.bad_elem, (unsigned long long)e);
+      }
     }
-    const double coef = a.coef ? a.coef[e] : 1.0;
-    const DF kap = df_mul(df_split(FORM == LMG_ADVDIFF ? a.kappa * coef : coef), det);
-    auto gg = [&](int m, int n) {
-      return df_add(df_add(df_mul(G[3 * m], G[3 * n]), df_mul(G[3 * m + 1], G[3 * n + 1])),
-                    df_mul(G[3 * m + 2], G[3 * n + 2]));
-    };
-    DF A2[6];
-    A2[0] = df_mul(kap, gg(0, 0));
-    A2[1] = df_mul(kap, gg(1, 1));
-    A2[2] = df_mul(kap, gg(2, 2));
-    A2[3] = df_mul(kap, gg(0, 1));
-    A2[4] = df_mul(kap, gg(0, 2));
-    A2[5] = df_mul(kap, gg(1, 2));
     __syncwarp();
+    const double *G = sG[warp];
+    const double det = G[9];
+    const double coef = a.coef ? a.coef[e] : 1.0;
+    const double kap = (FORM == LMG_ADVDIFF ? a.kappa * coef : coef) * det;
+    auto gg = [&](int m, int n) {
+      return G[3 * m] * G[3 * n] + G[3 * m + 1] * G[3 * n + 1] + G[3 * m + 2] * G[3 * n + 2];
+    };
+    T A2[6];
+    A2[0] = (T)(kap * gg(0, 0));
+    A2[1] = (T)(kap * gg(1, 1));
+    A2[2] = (T)(kap * gg(2, 2));
+    A2[3] = (T)(kap * gg(0, 1));
+    A2[4] = (T)(kap * gg(0, 2));
+    A2[5] = (T)(kap * gg(1, 2));
+    const bool axis = A2[3] == (T)0 && A2[4] == (T)0 && A2[5] == (T)0;  // axis-aligned element: diagonal tensor
     if (FORM == LMG_ADVDIFF) {
       // exp(i (k.x + phase)) at the element centre and exp(i gp k.dx/dxi_m):
       // the phase is affine in xi, so every Gauss point's value is a product
@@ -276,133 +238,130 @@ __global__ void __launch_bounds__(WARPS * 32) k_elem_full(GenElemArgs a) {
                        j2 = 0.5 * (sX[3 * v + 2] - sX[2]);
           ang = gp * (md[3] * j0 + md[4] * j1 + md[5] * j2);
         }
-        DF s2, c2;
-        df_sincos(ang, s2, c2);
-        sE[2 * t] = make_float2(c2.hi, c2.lo);
-        sE[2 * t + 1] = make_float2(s2.hi, s2.lo);
+        T sn, cs;
+        A::sincos_(ang, sn, cs);
+        sE[2 * t] = cs;
+        sE[2 * t + 1] = sn;
       }
       __syncwarp();
     }
-    // per quadrature point: transport coefficients and the load, in
-    // double-float arithmetic (FP32 pipe)
+    // per quadrature point: transport coefficients and the load
     if (lane < Q) {
       const int q = lane;
-      DF fx = {0.f, 0.f};
-      for (int c = 0; c < N; ++c) fx = df_fma_lazy(fx, ld_df(sphi + q * N + c), ld_df(sf + c));  // FE-interpolated load
-      fx = df_norm(fx);
-      const DF jw = df_mul(det, df_split(sqw[q]));
-      const DF fq = df_mul(jw, fx);
-      sfq[q] = make_float2(fq.hi, fq.lo);
+      T fx = 0;
+      for (int c = 0; c < N; ++c) fx = A::fma_(sphi[q * N + c], sf[c], fx);  // FE-interpolated load
+      const T jw = (T)(det * sqw[q]);
+      sfq[q] = jw * fx;
       if (FORM == LMG_ADVDIFF) {
-        DF b[3] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+        T b[3] = {0, 0, 0};
         // offset of this point along each reference axis: -1, 0 or +1 times gp
         const int qi[3] = {q % Q1, (q / Q1) % Q1, q / (Q1 * Q1)};
         for (int m = 0; m < a.n_modes; ++m) {
-          const float2 *E = sE + 8 * m;
-          DF re = ld_df(E), im = ld_df(E + 1);
+          const T *E = sE + 8 * m;
+          T re = E[0], im = E[1];
 #pragma unroll
           for (int d = 0; d < 3; ++d) {
             if (Q1 == 3 && qi[d] == 1) continue;
-            const DF c = ld_df(E + 2 * (d + 1));
-            DF sn = ld_df(E + 2 * (d + 1) + 1);
-            if (qi[d] == 0) sn = DF{-sn.hi, -sn.lo};
-            const DF nim = DF{-im.hi, -im.lo};
-            const DF r2 = df_norm(df_fma_lazy(df_fma_lazy(DF{0.f, 0.f}, re, c), nim, sn));
-            im = df_norm(df_fma_lazy(df_fma_lazy(DF{0.f, 0.f}, re, sn), im, c));
+            const T c = E[2 * (d + 1)];
+            const T sn = qi[d] == 0 ? -E[2 * (d + 1) + 1] : E[2 * (d + 1) + 1];
+            const T r2 = A::fma_(re, c, -(im * sn));
+            im = A::fma_(re, sn, im * c);
             re = r2;
           }
 #pragma unroll
-          for (int d = 0; d < 3; ++d) b[d] = df_fma_lazy(b[d], re, ld_df(scurl + 3 * m + d));
+          for (int d = 0; d < 3; ++d) b[d] = A::fma_(re, scurl[3 * m + d], b[d]);
         }
 #pragma unroll
-        for (int d = 0; d < 3; ++d) b[d] = df_norm(b[d]);
-#pragma unroll
         for (int m = 0; m < 3; ++m) {
-          DF t = {0.f, 0.f};
+          T t = 0;
 #pragma unroll
-          for (int d = 0; d < 3; ++d) t = df_fma_lazy(t, G[3 * m + d], b[d]);
-          t = df_mul(jw, df_norm(t));
-          sbeta[3 * q + m] = make_float2(t.hi, t.lo);
+          for (int d = 0; d < 3; ++d) t = A::fma_((T)G[3 * m + d], b[d], t);
+          sbeta[3 * q + m] = jw * t;
         }
       }
     }
     __syncwarp();
     if (lane < N) {
-      // column b of Ke in double-float arithmetic: convection by sum
-      // factorisation, diffusion from the reference tensors
+      // column b of Ke: convection by sum factorisation, diffusion from the reference tensors
       const int b = lane;
-      DF P[Q];
+      T Cc[27];
       if (FORM == LMG_ADVDIFF) {
+        T P[Q];
 #pragma unroll
         for (int q = 0; q < Q; ++q) {
-          const float2 *d = sdphi + (q * N + b) * 3;
-          DF t = {0.f, 0.f};
+          const T *d = sdphi + (q * N + b) * 3;
+          T t = 0;
 #pragma unroll
-          for (int m = 0; m < 3; ++m) t = df_fma_lazy(t, ld_df(sbeta + 3 * q + m), ld_df(d + m));
-          P[q] = df_norm(t);
+          for (int m = 0; m < 3; ++m) t = A::fma_(sbeta[3 * q + m], d[m], t);
+          P[q] = t;
         }
-      }
-      DF Cc[27];
-      if (FORM == LMG_ADVDIFF) {
-        DF L1[N1 * Q1];
+        T L1[N1 * Q1];
 #pragma unroll
         for (int i = 0; i < N1 * Q1; ++i) L1[i] = sL1[i];
-        tensor_contract_df<N1, Q1>(L1, P, Cc);
+        tensor_contract<N1, Q1, T>(L1, P, Cc);
       }
-      float2 *Ke = a.Kraw + e * (N * N);
+      T *Ke = reinterpret_cast<T *>(a.Kraw) + e * (N * N);
 #pragma unroll
       for (int r = 0; r < N; ++r) {
-        DF k = {0.f, 0.f};
+        T k = 0;
+        if (axis) {
 #pragma unroll
-        for (int t = 0; t < 6; ++t) k = df_fma_lazy(k, A2[t], ld_df(sD + (t * N + r) * N + b));
-        k = df_norm(k);
-        if (FORM == LMG_ADVDIFF) k = df_add(k, Cc[hex_tensor(N, r)]);
-        Ke[r * N + b] = make_float2(k.hi, k.lo);
+          for (int t = 0; t < 3; ++t) k = A::fma_(A2[t], sD[(t * N + r) * N + b], k);
+        } else {
+#pragma unroll
+          for (int t = 0; t < 6; ++t) k = A::fma_(A2[t], sD[(t * N + r) * N + b], k);
+        }
+        if (FORM == LMG_ADVDIFF) k += Cc[hex_tensor(N, r)];
+        Ke[r * N + b] = k;
       }
-      DF fe = {0.f, 0.f};
+      double fe = 0.0;
 #pragma unroll
-      for (int q = 0; q < Q; ++q) fe = df_fma_lazy(fe, ld_df(sfq + q), ld_df(sphi + q * N + b));
-      a.Fraw[e * N + b] = df_to_double(df_norm(fe));
+      for (int q = 0; q < Q; ++q) fe = fma((double)sfq[q], (double)sphi[q * N + b], fe);
+      a.Fraw[e * N + b] = fe;
     }
     __syncwarp();
   }
 }
 
-template <int FORM, int N, int Q>
+template <int FORM, int N, int Q, typename T>
 void launch_full(const GenElemArgs &a, int max_ctas, cudaStream_t s) {
-  const size_t smem = sizeof(double) * ((size_t)Q * N * 5 + 6 * N * N + Q + N * 3 + 10 * a.n_modes +
-                                        (size_t)WARPS * (N * 3 + N + 4 * Q + 8 * a.n_modes));
+  const size_t smem = FullSmem<T>{N, Q, a.n_modes}.bytes(WARPS);
   static size_t attr = 0;  // largest dynamic shared memory granted so far
   if (smem > attr) {
-    cudaFuncSetAttribute(k_elem_full<FORM, N, Q>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_elem_full<FORM, N, Q, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     attr = smem;
   }
   const int64_t need = (a.n_elem + WARPS - 1) / WARPS;
   const int grid = (int)(need < (int64_t)max_ctas ? need : (int64_t)max_ctas);
-  if (grid > 0) k_elem_full<FORM, N, Q><<<grid, WARPS * 32, smem, s>>>(a);
+  if (grid > 0) k_elem_full<FORM, N, Q, T><<<grid, WARPS * 32, smem, s>>>(a);
 }
 
-// Dynamic shared memory: K [N][N] (double-float), F [N], L = C^T K [max_ne][N]
-// (double-float), coefficients [max_ent] (FP64 and double-float), column
-// pointers [max_ne + 1], row indices [max_ent].  The matrix products run in
-// double-float arithmetic on the FP32 pipe; the load in FP64.
+// Dynamic shared memory: K [N][N] (T), F [N] (FP64), L = C^T K [max_ne][N]
+// (T), coefficients [max_ent] (FP64 and T), column pointers [max_ne + 1], row
+// indices [max_ent].  The matrix products run in T (FP64 for the drop-in,
+// FP32 for the mixed form); the load in FP64.
+template <typename T>
 __global__ void __launch_bounds__(128) k_constrain(ConsArgs c) {
+  using A = GA<T>;
   extern __shared__ double csm[];
   const int N = c.N;
-  float2 *sK = reinterpret_cast<float2 *>(csm);
-  double *sF = reinterpret_cast<double *>(sK + N * N);
-  float2 *sL = reinterpret_cast<float2 *>(sF + N);
-  double *scv = reinterpret_cast<double *>(sL + c.max_ne * N);
-  float2 *scv2 = reinterpret_cast<float2 *>(scv + c.max_ent);
-  int32_t *scp = reinterpret_cast<int32_t *>(scv2 + c.max_ent);
+  T *sK = reinterpret_cast<T *>(csm);
+  double *sF = reinterpret_cast<double *>(csm + (sizeof(T) * N * N + 7) / 8);
+  T *sL = reinterpret_cast<T *>(sF + N);
+  double *scv = reinterpret_cast<double *>(reinterpret_cast<unsigned char *>(sL) +
+                                           ((sizeof(T) * c.max_ne * N + 7) & ~(size_t)7));
+  T *scvT = reinterpret_cast<T *>(scv + c.max_ent);
+  int32_t *scp = reinterpret_cast<int32_t *>(reinterpret_cast<unsigned char *>(scvT) +
+                                             ((sizeof(T) * c.max_ent + 7) & ~(size_t)7));
   uint8_t *sci = reinterpret_cast<uint8_t *>(scp + c.max_ne + 1);
+  const T *Kraw = reinterpret_cast<const T *>(c.Kraw);
   for (int64_t k = blockIdx.x; k < c.n_cons; k += gridDim.x) {
     const int64_t e = c.elem[k];
     const int ne = c.ne[k];
     const int64_t cb = c.cbase[k], eb = c.ebase[k];
     const uint64_t rows = c.rowmask[k];
     __syncthreads();
-    for (int i = threadIdx.x; i < N * N; i += blockDim.x) sK[i] = c.Kraw[e * N * N + i];
+    for (int i = threadIdx.x; i < N * N; i += blockDim.x) sK[i] = Kraw[e * N * N + i];
     for (int i = threadIdx.x; i < N; i += blockDim.x) sF[i] = c.Fraw[e * N + i];
     for (int i = threadIdx.x; i <= ne; i += blockDim.x) scp[i] = c.ccp[cb + i];
     __syncthreads();
@@ -411,43 +370,34 @@ __global__ void __launch_bounds__(128) k_constrain(ConsArgs c) {
       sci[i] = c.ci[eb + i];
       const double v = c.cv[eb + i];
       scv[i] = v;
-      const DF x = df_split(v);
-      scv2[i] = make_float2(x.hi, x.lo);
+      scvT[i] = (T)v;
     }
     __syncthreads();
     // L_pj = sum_i C_ip K_ij (rows of constrained local dofs are replaced below)
     for (int idx = threadIdx.x; idx < ne * N; idx += blockDim.x) {
       const int p = idx / N, j = idx - p * N;
-      DF l = {0.f, 0.f};
+      T l = 0;
       if (!(p < N && ((rows >> p) & 1ull)))
-        for (int u = scp[p]; u < scp[p + 1]; ++u) {
-          const float2 cv = scv2[u], kv = sK[sci[u] * N + j];
-          l = df_fma_lazy(l, DF{cv.x, cv.y}, DF{kv.x, kv.y});
-        }
-      l = df_norm(l);
-      sL[idx] = make_float2(l.hi, l.lo);
+        for (int u = scp[p]; u < scp[p + 1]; ++u) l = A::fma_(scvT[u], sK[sci[u] * N + j], l);
+      sL[idx] = l;
     }
     __syncthreads();
-    float2 *out = c.Ebuf + c.kout[k];
+    T *out = reinterpret_cast<T *>(c.Ebuf) + c.kout[k];
     for (int idx = threadIdx.x; idx < ne * ne; idx += blockDim.x) {
       const int p = idx / ne, q = idx - p * ne;
-      DF v = {0.f, 0.f};
+      T v = 0;
       if (p < N && ((rows >> p) & 1ull)) {
         if (p == q) {
-          v = DF{1.f, 0.f};
+          v = 1;
         } else {
           for (int t = scp[q]; t < scp[q + 1]; ++t)
-            if (sci[t] == p) v = DF{-scv2[t].x, -scv2[t].y};
+            if (sci[t] == p) v = -scvT[t];
         }
       } else {
-        const float2 *lp = sL + p * N;
-        for (int t = scp[q]; t < scp[q + 1]; ++t) {
-          const float2 lv = lp[sci[t]], cv = scv2[t];
-          v = df_fma_lazy(v, DF{lv.x, lv.y}, DF{cv.x, cv.y});
-        }
-        v = df_norm(v);
+        const T *lp = sL + p * N;
+        for (int t = scp[q]; t < scp[q + 1]; ++t) v = A::fma_(lp[sci[t]], scvT[t], v);
       }
-      out[idx] = make_float2(v.hi, v.lo);
+      out[idx] = v;
     }
     double *fo = c.Fbuf + c.fout[k];
     for (int p = threadIdx.x; p < ne; p += blockDim.x) {
@@ -458,22 +408,19 @@ __global__ void __launch_bounds__(128) k_constrain(ConsArgs c) {
   }
 }
 
-// K[s] = sum of the slot's contributions in element order, over element
-// matrices stored as double-float pairs: summed in double-float arithmetic on
-// the FP32 pipe and rounded to FP64 once per entry; F likewise per dof in FP64.
-__global__ void k_gather_full_df(int64_t nnz, const int64_t *__restrict__ cptr, const uint32_t *__restrict__ coff,
-                                 const float2 *__restrict__ E, double *__restrict__ K, int64_t n_dofs,
-                                 const int64_t *__restrict__ fptr, const uint32_t *__restrict__ foff,
-                                 const double *__restrict__ Fb, double *__restrict__ F) {
+// K[s] = sum of the slot's contributions in element order (FP64 sums of the
+// FP64 or FP32 element entries); F likewise per dof in FP64.
+template <typename T>
+__global__ void k_gather_full(int64_t nnz, const int64_t *__restrict__ cptr, const uint32_t *__restrict__ coff,
+                              const T *__restrict__ E, double *__restrict__ K, int64_t n_dofs,
+                              const int64_t *__restrict__ fptr, const uint32_t *__restrict__ foff,
+                              const double *__restrict__ Fb, double *__restrict__ F) {
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < nnz + n_dofs; s += stride) {
     if (s < nnz) {
-      DF v = {0.f, 0.f};
-      for (int64_t t = cptr[s]; t < cptr[s + 1]; ++t) {
-        const float2 x = E[coff[t]];
-        v = df_add(v, DF{x.x, x.y});
-      }
-      K[s] = df_to_double(v);
+      double v = 0.0;
+      for (int64_t t = cptr[s]; t < cptr[s + 1]; ++t) v += (double)E[coff[t]];
+      K[s] = v;
     } else {
       const int64_t d = s - nnz;
       double v = 0.0;
@@ -490,9 +437,13 @@ bool gen_elements_built(int form, int n, int q) {
   return (n == 8 || n == 27) && (q == 8 || q == 27);
 }
 
-void launch_gen_elements(int form, int n, int q, const GenElemArgs &a, int max_ctas, cudaStream_t s) {
-#define LMG_G(F, NN, QQ) \
-  if (form == F && n == NN && q == QQ) return launch_full<F, NN, QQ>(a, max_ctas, s);
+void launch_gen_elements(int form, int n, int q, bool mixed, const GenElemArgs &a, int max_ctas, cudaStream_t s) {
+#define LMG_G(F, NN, QQ)                                                        \
+  if (form == F && n == NN && q == QQ) {                                        \
+    if (mixed) launch_full<F, NN, QQ, float>(a, max_ctas, s);                   \
+    else launch_full<F, NN, QQ, double>(a, max_ctas, s);                        \
+    return;                                                                     \
+  }
   LMG_G(LMG_POISSON, 8, 8)
   LMG_G(LMG_POISSON, 8, 27)
   LMG_G(LMG_POISSON, 27, 8)
@@ -504,26 +455,39 @@ void launch_gen_elements(int form, int n, int q, const GenElemArgs &a, int max_c
 #undef LMG_G
 }
 
-void launch_constrain(const ConsArgs &c, int n_sm, cudaStream_t s) {
-  if (c.n_cons <= 0) return;
+template <typename T>
+void launch_constrain_t(const ConsArgs &c, int n_sm, cudaStream_t s) {
   const int64_t g = c.n_cons < (int64_t)n_sm * 16 ? c.n_cons : (int64_t)n_sm * 16;
-  const size_t smem = sizeof(double) * ((size_t)c.N * c.N + c.N + (size_t)c.max_ne * c.N + 2 * (size_t)c.max_ent) +
-                      sizeof(int32_t) * (c.max_ne + 1) + c.max_ent;
+  auto r8 = [](size_t x) { return (x + 7) & ~(size_t)7; };
+  const size_t smem = r8(sizeof(T) * c.N * c.N) + sizeof(double) * c.N + r8(sizeof(T) * c.max_ne * c.N) +
+                      sizeof(double) * c.max_ent + r8(sizeof(T) * c.max_ent) + sizeof(int32_t) * (c.max_ne + 1) +
+                      c.max_ent;
   static size_t attr = 0;
   if (smem > attr) {
-    cudaFuncSetAttribute(k_constrain, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_constrain<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     attr = smem;
   }
-  k_constrain<<<(int)g, 128, smem, s>>>(c);
+  k_constrain<T><<<(int)g, 128, smem, s>>>(c);
 }
 
-void launch_gather_full_df(int64_t nnz, const int64_t *cptr, const uint32_t *coff, const float2 *E, double *K,
-                           int64_t n_dofs, const int64_t *fptr, const uint32_t *foff, const double *Fb, double *F,
-                           int n_sm, cudaStream_t s) {
+void launch_constrain(const ConsArgs &c, bool mixed, int n_sm, cudaStream_t s) {
+  if (c.n_cons <= 0) return;
+  if (mixed) launch_constrain_t<float>(c, n_sm, s);
+  else launch_constrain_t<double>(c, n_sm, s);
+}
+
+void launch_gather_full(int64_t nnz, const int64_t *cptr, const uint32_t *coff, const void *E, bool mixed, double *K,
+                        int64_t n_dofs, const int64_t *fptr, const uint32_t *foff, const double *Fb, double *F,
+                        int n_sm, cudaStream_t s) {
   const int64_t items = nnz + n_dofs;
   const int64_t blocks = (items + 255) / 256;
   const int g = (int)(blocks < (int64_t)n_sm * 16 ? blocks : (int64_t)n_sm * 16);
-  k_gather_full_df<<<g, 256, 0, s>>>(nnz, cptr, coff, E, K, n_dofs, fptr, foff, Fb, F);
+  if (mixed)
+    k_gather_full<float><<<g, 256, 0, s>>>(nnz, cptr, coff, static_cast<const float *>(E), K, n_dofs, fptr, foff,
+                                            Fb, F);
+  else
+    k_gather_full<double><<<g, 256, 0, s>>>(nnz, cptr, coff, static_cast<const double *>(E), K, n_dofs, fptr, foff,
+                                             Fb, F);
 }
 
 }  // namespace lmg

@@ -23,7 +23,7 @@ struct GenElemArgs {
   double kappa;               // convection-diffusion diffusivity
   int n_modes;
   const double *modes;        // [n_modes][7]: a[3], k[3], phase
-  float2 *Kraw;               // [n_elem][N][N] double-float pairs
+  void *Kraw;                 // [n_elem][N][N] element matrices: double (FP64 drop-in) or float (mixed)
   double *Fraw;               // [n_elem][N]
   int *status;
   unsigned long long *bad_elem;
@@ -46,19 +46,20 @@ struct ConsArgs {
   const uint8_t *ci;          // row index of each entry
   const double *cv;           // coefficient of each entry
   const uint64_t *rowmask;    // [n_cons] constrained local rows
-  const float2 *Kraw;         // element matrices, double-float pairs
+  const void *Kraw;           // element matrices, double or float
   const double *Fraw;
-  float2 *Ebuf;
+  void *Ebuf;                 // enlarged element matrices, same type
   double *Fbuf;
 };
 
 bool gen_elements_built(int form, int n, int q);
-// max_ctas: grid cap of the grid-stride element loop
-void launch_gen_elements(int form, int n, int q, const GenElemArgs &a, int max_ctas, cudaStream_t s);
-void launch_constrain(const ConsArgs &c, int n_sm, cudaStream_t s);
-// slot gather over element matrices stored as double-float pairs
-void launch_gather_full_df(int64_t nnz, const int64_t *cptr, const uint32_t *coff, const float2 *E, double *K,
-                           int64_t n_dofs, const int64_t *fptr, const uint32_t *foff, const double *Fb, double *F,
-                           int n_sm, cudaStream_t s);
+// mixed: FP32 element contraction (the map stays FP64); max_ctas: grid cap of
+// the grid-stride element loop
+void launch_gen_elements(int form, int n, int q, bool mixed, const GenElemArgs &a, int max_ctas, cudaStream_t s);
+void launch_constrain(const ConsArgs &c, bool mixed, int n_sm, cudaStream_t s);
+// slot gather (FP64 sums) over element matrices stored as double, or float when mixed
+void launch_gather_full(int64_t nnz, const int64_t *cptr, const uint32_t *coff, const void *E, bool mixed, double *K,
+                        int64_t n_dofs, const int64_t *fptr, const uint32_t *foff, const double *Fb, double *F,
+                        int n_sm, cudaStream_t s);
 
 }  // namespace lmg

@@ -51,7 +51,7 @@ struct H3Args {
   const float2 *D;          // [P][6][N*N] double-float pairs
   const double *M;          // [P][N][G]
   const double *gd0;        // [G][3]
-  float2 *Kraw;             // [n_elem][N][N] double-float pairs
+  void *Kraw;               // [n_elem][N][N] element matrices: double (FP64 drop-in) or float (mixed)
   double *Fraw;             // [n_elem][N]
   int *status;
   unsigned long long *bad_elem;
@@ -63,8 +63,11 @@ __device__ __forceinline__ double warp_sum(double v) {
   return v;
 }
 
-// N dofs and G map nodes per element (cubic hexes 64 / 27, cubic tets 20 / 14)
-template <int N, int G>
+// N dofs and G map nodes per element (cubic hexes 64 / 27, cubic tets 20 / 14).
+// FP64 drop-in (MIXED false): the contraction in double-float, each entry
+// rounded to FP64 once; mixed form: the contraction in FP32.  The map is FP64
+// in both.
+template <int N, int G, bool MIXED>
 __global__ void __launch_bounds__(H3T) k_elem_pattern(H3Args a) {
   static_assert(N <= 64 && G <= 32, "one mask word per element, one lane per map node");
   __shared__ double sA[H3B][8];   // A_0..A_5, detJ
@@ -138,12 +141,21 @@ __global__ void __launch_bounds__(H3T) k_elem_pattern(H3Args a) {
         d[k] = DF{x.x, x.y};
       }
       for (int b = 0; b < cnt; ++b) {
-        DF v = {0.f, 0.f};
+        const bool msk = ((sm[b] >> i) | (sm[b] >> j)) & 1ull;
+        if constexpr (MIXED) {
+          float v = 0.f;
 #pragma unroll
-        for (int k = 0; k < 6; ++k) v = df_fma_lazy(v, sA2[b][k], d[k]);
-        v = df_norm(v);
-        if (((sm[b] >> i) | (sm[b] >> j)) & 1ull) v = DF{(i == j) ? 1.f : 0.f, 0.f};
-        a.Kraw[(int64_t)se[b] * (N * N) + idx] = make_float2(v.hi, v.lo);
+          for (int k = 0; k < 6; ++k) v = fmaf(sA2[b][k].hi, d[k].hi, v);
+          if (msk) v = (i == j) ? 1.f : 0.f;
+          static_cast<float *>(a.Kraw)[(int64_t)se[b] * (N * N) + idx] = v;
+        } else {
+          DF v = {0.f, 0.f};
+#pragma unroll
+          for (int k = 0; k < 6; ++k) v = df_fma_lazy(v, sA2[b][k], d[k]);
+          v = df_norm(v);
+          if (msk) v = DF{(i == j) ? 1.f : 0.f, 0.f};
+          static_cast<double *>(a.Kraw)[(int64_t)se[b] * (N * N) + idx] = df_to_double(v);
+        }
       }
     }
     const double *Mp = a.M + (size_t)p * N * G;
@@ -220,7 +232,7 @@ lmg_status hier3_form_set(lmg_ctx *c, int32_t form, int32_t q_order, const doubl
 
 bool hier3_masks(const lmg_ctx *c) { return c->hier3 && !c->has_rows; }
 
-void launch_hier3(lmg_ctx *c) {
+void launch_hier3(lmg_ctx *c, bool mixed) {
   H3Args a{};
   a.n_batch = c->h3_nbatch;
   a.batch = c->d_h3batch;
@@ -233,15 +245,20 @@ void launch_hier3(lmg_ctx *c) {
   a.D = c->d_h3D;
   a.M = c->d_h3M;
   a.gd0 = c->d_h3gd;
-  a.Kraw = reinterpret_cast<float2 *>(c->d_Ebuf);
+  a.Kraw = c->d_Ebuf;
   a.Fraw = c->d_Fbuf;
   a.status = c->d_status;
   a.bad_elem = c->d_bad;
   const int64_t want = (int64_t)c->n_sm * 8;
   const int grid = (int)(a.n_batch < want ? a.n_batch : want);
   if (grid <= 0) return;
-  if (c->tab.n == 20) k_elem_pattern<20, 14><<<grid, H3T, 0, c->stream>>>(a);
-  else k_elem_pattern<64, 27><<<grid, H3T, 0, c->stream>>>(a);
+  if (c->tab.n == 20) {
+    if (mixed) k_elem_pattern<20, 14, true><<<grid, H3T, 0, c->stream>>>(a);
+    else k_elem_pattern<20, 14, false><<<grid, H3T, 0, c->stream>>>(a);
+  } else {
+    if (mixed) k_elem_pattern<64, 27, true><<<grid, H3T, 0, c->stream>>>(a);
+    else k_elem_pattern<64, 27, false><<<grid, H3T, 0, c->stream>>>(a);
+  }
 }
 
 }  // namespace lmg

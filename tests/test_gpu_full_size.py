@@ -15,7 +15,9 @@
   differences of the residual (h = 1e-6 max(|k|, 1e-3), the step of
   adjoint_qoi_parameter_sensitivity) on 64 random parameters, and the
   node-coordinate VJP against central differences of the QoI and residual on
-  a sample of nodes; agreement <= 1e-6 relative.
+  a sample of nodes; agreement <= 1e-6 relative to max(|entry|, 1e-2 of the
+  gradient's largest entry): the central difference's own rounding, about
+  1e-16 |R| / h, swamps sensitivities far below the gradient's scale.
 The oracle runs on all host threads."""
 import os
 
@@ -102,6 +104,7 @@ def test_c3_refined_convection_diffusion_full_size_against_oracle():
     assert np.array_equal(rp, rpo) and np.array_equal(ci, cio)
     del rpo, cio
     K, F = asm.assemble()
+    K32, F32 = asm.assemble(lm.MIXED)
     asm.close()
     Kr, Fr, st, _ = orc.assemble(lm.ADVDIFF, mesh.elem_type, 2, 5, mesh.xyz, mesh.conn, 1, dm.elem_dofs, dm.n_dofs,
                                  dm.constrained, rp, ci, coef=k, nodal_f=f,
@@ -112,6 +115,9 @@ def test_c3_refined_convection_diffusion_full_size_against_oracle():
     assert err <= 1e-13, "K scaled error %.3g" % err
     ftol = 1e-13 * max(np.abs(Fr).max(), 1e-300)
     assert np.all(np.abs(F - Fr) <= np.maximum(1e-13 * np.abs(Fr), ftol))
+    print("C3 FP64 worst scaled error %.3g; mixed ||dK||/||K|| %.3g ||dF||/||F|| %.3g"
+          % (err, rel(K32, Kr), rel(F32, Fr)))
+    assert rel(K32, Kr) < 1e-6 and rel(F32, Fr) < 1e-6
 
 
 def c5_problem(n=128):
@@ -151,7 +157,7 @@ def test_c5_adjoint_128_against_central_differences():
             asm.update_inputs(elem_coef=kk)
             res.append(asm.residual(u))
         fd = ((res[0] - res[1]) / (2 * d)) @ z
-        e = abs(g[j] - fd) / max(abs(g[j]), 1e-3 * gscale)
+        e = abs(g[j] - fd) / max(abs(g[j]), 1e-2 * gscale)
         worst = max(worst, e)
         assert e <= 1e-6, (int(j), g[j], fd)
     asm.update_inputs(elem_coef=k)
@@ -178,7 +184,7 @@ def test_c5_adjoint_128_against_central_differences():
                 R = sp.csr_matrix((K, col, rp), shape=(dm.n_dofs, dm.n_dofs)) @ u - F
                 parts.append((R, asm.qoi_region_load(region) @ u))
             fd = (parts[1][1] - parts[0][1]) / (2 * h) + ((parts[0][0] - parts[1][0]) / (2 * h)) @ z
-            e = abs(gx[node, dd] - fd) / max(abs(gx[node, dd]), 1e-3 * xscale)
+            e = abs(gx[node, dd] - fd) / max(abs(gx[node, dd]), 1e-2 * xscale)
             worst = max(worst, e)
             assert e <= 1e-6, (int(node), dd, gx[node, dd], fd)
     print("C5 coordinate VJP vs central differences on %d nodes x 3: worst relative error %.3g" % (len(nodes), worst))
