@@ -173,32 +173,39 @@ __global__ void __launch_bounds__(WARPS * 32) k_elem_full(GenElemArgs a) {
       sf[lane] = (T)(a.nodal_f ? a.nodal_f[nd] : 0.0);
     }
     __syncwarp();
-    // The elements here are affine hexahedra (form_set refuses the others), so
-    // the constant map derivatives are the edge vectors from vertex 0 to
-    // vertices 1, 3 and 4 over the reference edge length 2: the value of
-    // compute_affine_map's sum over the nodes.  J, detJ and J^-1 in FP64
-    // (fe_map.C:1046-1068), by lane 0.
+    // The elements here are affine hexahedra (form_set refuses the others):
+    // compute_affine_map takes the map at the first quadrature point,
+    // J[m][d] = sum_a dphi_a/dxi_m x_a[d] over the N map nodes in node order
+    // (fe_map.C:1167-1245, 980-1044), then detJ and J^-1 by cofactors
+    // (fe_map.C:1046-1068).  On small elements far from the origin the node
+    // sum cancels to a few digits, so it is formed exactly as the reference
+    // forms it: FP64, node order, every product and sum rounded separately
+    // (no fused multiply-adds).  Lane j < 9 forms J[j]; lane 0 the rest.
+    if (lane < 9) {
+      const int m = lane / 3, d = lane - 3 * m;
+      double acc = 0.0;
+      for (int g = 0; g < N; ++g) acc = __dadd_rn(acc, __dmul_rn(a.fe.gdphi[3 * g + m], sX[3 * g + d]));
+      sG[warp][lane] = acc;
+    }
+    __syncwarp();
     if (lane == 0) {
       double J[9];  // J[m*3+d] = d x_d / d xi_m
 #pragma unroll
-      for (int m = 0; m < 3; ++m) {
-        const int v = m == 0 ? 1 : (m == 1 ? 3 : 4);
-#pragma unroll
-        for (int d = 0; d < 3; ++d) J[3 * m + d] = 0.5 * (sX[3 * v + d] - sX[d]);
-      }
-      const double c0 = J[4] * J[8] - J[5] * J[7], c1 = J[5] * J[6] - J[3] * J[8], c2 = J[3] * J[7] - J[4] * J[6];
-      const double det = J[0] * c0 + J[1] * c1 + J[2] * c2;
-      const double inv = 1.0 / det;
+      for (int j = 0; j < 9; ++j) J[j] = sG[warp][j];
+      auto cof = [](double a, double b, double c, double d) { return __dsub_rn(__dmul_rn(a, b), __dmul_rn(c, d)); };
+      const double c0 = cof(J[4], J[8], J[5], J[7]), c1 = cof(J[5], J[6], J[3], J[8]), c2 = cof(J[3], J[7], J[4], J[6]);
+      const double det = __dadd_rn(__dadd_rn(__dmul_rn(J[0], c0), __dmul_rn(J[1], c1)), __dmul_rn(J[2], c2));
+      const double inv = __ddiv_rn(1.0, det);
       double *G = sG[warp];
-      G[0] = c0 * inv;
-      G[1] = c1 * inv;
-      G[2] = c2 * inv;
-      G[3] = (J[2] * J[7] - J[1] * J[8]) * inv;
-      G[4] = (J[0] * J[8] - J[2] * J[6]) * inv;
-      G[5] = (J[1] * J[6] - J[0] * J[7]) * inv;
-      G[6] = (J[1] * J[5] - J[2] * J[4]) * inv;
-      G[7] = (J[2] * J[3] - J[0] * J[5]) * inv;
-      G[8] = (J[0] * J[4] - J[1] * J[3]) * inv;
+      G[0] = __dmul_rn(c0, inv);
+      G[1] = __dmul_rn(c1, inv);
+      G[2] = __dmul_rn(c2, inv);
+      G[3] = __dmul_rn(cof(J[2], J[7], J[1], J[8]), inv);
+      G[4] = __dmul_rn(cof(J[0], J[8], J[2], J[6]), inv);
+      G[5] = __dmul_rn(cof(J[1], J[6], J[0], J[7]), inv);
+      G[6] = __dmul_rn(cof(J[1], J[5], J[2], J[4]), inv);
+      G[7] = __dmul_rn(cof(J[2], J[3], J[0], J[5]), inv);
+      G[8] = __dmul_rn(cof(J[0], J[4], J[1], J[3]), inv);
       G[9] = det;
       if (!(det > 0.0)) {
         atomicCAS(a.status, 0, LMG_ERR_DEGENERATE);

@@ -15,15 +15,15 @@
 //   K_ij = sum_k A_k D_k[i][j],  A = coef detJ (G G^T) (6 entries),
 //   F_i  = detJ sum_g M[i][g] f_g,
 // reading every table entry once for the whole batch, and writes the full
-// 64 x 64 matrices into the general path's element buffer.  The contraction
+// 64 x 64 matrices into the general path's element buffer.  The map is formed
+// in FP64 in the reference's node order.  For the FP64 drop-in the contraction
 // runs in double-float arithmetic on the FP32 pipe (the tables are stored as
-// hi + lo pairs; GB300's FP64 rate is 1/64 of FP32).  Without
+// hi + lo pairs; GB300's FP64 rate is 1/64 of FP32) and each entry is rounded
+// to FP64; the mixed form contracts in FP32.  Without
 // constraint rows the homogeneous Dirichlet rows are applied here (zero row
 // and column, 1 on the diagonal, zero load: constrain_element_matrix_and_vector
 // with empty rows) and the constraint kernel is skipped; with rows the
-// constraint kernel applies C^T K C.  The element matrices stay double-float
-// pairs; the gather sums them in double-float (k_gather_full_df), rounding
-// each CSR entry to FP64 once.
+// constraint kernel applies C^T K C.  The gather sums the entries in FP64.
 #include <cuda_runtime.h>
 
 #include <string>
@@ -57,12 +57,6 @@ struct H3Args {
   unsigned long long *bad_elem;
 };
 
-__device__ __forceinline__ double warp_sum(double v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
-}
-
 // N dofs and G map nodes per element (cubic hexes 64 / 27, cubic tets 20 / 14).
 // FP64 drop-in (MIXED false): the contraction in double-float, each entry
 // rounded to FP64 once; mixed form: the contraction in FP32.  The map is FP64
@@ -73,6 +67,8 @@ __global__ void __launch_bounds__(H3T) k_elem_pattern(H3Args a) {
   __shared__ double sA[H3B][8];   // A_0..A_5, detJ
   __shared__ DF sA2[H3B][6];
   __shared__ double sf[H3B][G];
+  __shared__ double sX[H3B][3 * G];  // map node coordinates of each warp's element
+  __shared__ double sJ[H3B][9];      // map derivatives J[m*3+d] = dx_d/dxi_m
   __shared__ uint64_t sm[H3B];
   __shared__ int32_t se[H3B];
   const int t = threadIdx.x, w = t >> 5, lane = t & 31;
@@ -81,36 +77,44 @@ __global__ void __launch_bounds__(H3T) k_elem_pattern(H3Args a) {
     __syncthreads();
     if (w < cnt) {  // warp w: geometry of the batch's element w (compute_affine_map)
       const int32_t e = a.order[first + w];
-      double jp[9];
-#pragma unroll
-      for (int k = 0; k < 9; ++k) jp[k] = 0.0;
       if (lane < G) {
         const int64_t nd = a.conn[(int64_t)e * G + lane];
-        const double x[3] = {a.xyz[3 * nd], a.xyz[3 * nd + 1], a.xyz[3 * nd + 2]};
-#pragma unroll
-        for (int m = 0; m < 3; ++m)
-#pragma unroll
-          for (int d = 0; d < 3; ++d) jp[3 * m + d] = x[d] * a.gd0[3 * lane + m];
+        sX[w][3 * lane] = a.xyz[3 * nd];
+        sX[w][3 * lane + 1] = a.xyz[3 * nd + 1];
+        sX[w][3 * lane + 2] = a.xyz[3 * nd + 2];
         sf[w][lane] = a.nodal_f ? a.nodal_f[nd] : 0.0;
       }
+      __syncwarp();
+      // J[m][d] = sum_g dphi_g/dxi_m x_g[d] in node order, every product and
+      // sum rounded separately, as compute_affine_map forms it (fe_map.C:980-1044):
+      // lane j < 9 forms entry j
+      if (lane < 9) {
+        const int m = lane / 3, d = lane - 3 * m;
+        double acc = 0.0;
+        for (int g = 0; g < G; ++g) acc = __dadd_rn(acc, __dmul_rn(a.gd0[3 * g + m], sX[w][3 * g + d]));
+        sJ[w][lane] = acc;
+      }
+      __syncwarp();
+      double jp[9];
 #pragma unroll
-      for (int k = 0; k < 9; ++k) jp[k] = warp_sum(jp[k]);
+      for (int k = 0; k < 9; ++k) jp[k] = sJ[w][k];
       if (lane == 0) {
         // jp[3m+d] = dx_d/dxi_m; G[3m+d] = dxi_m/dx_d (fe_map.C:1046-1068)
-        const double c0 = jp[4] * jp[8] - jp[5] * jp[7], c1 = jp[5] * jp[6] - jp[3] * jp[8],
-                     c2 = jp[3] * jp[7] - jp[4] * jp[6];
-        const double det = jp[0] * c0 + jp[1] * c1 + jp[2] * c2;
-        const double inv = 1.0 / det;
+        auto cof = [](double a, double b, double c, double d) { return __dsub_rn(__dmul_rn(a, b), __dmul_rn(c, d)); };
+        const double c0 = cof(jp[4], jp[8], jp[5], jp[7]), c1 = cof(jp[5], jp[6], jp[3], jp[8]),
+                     c2 = cof(jp[3], jp[7], jp[4], jp[6]);
+        const double det = __dadd_rn(__dadd_rn(__dmul_rn(jp[0], c0), __dmul_rn(jp[1], c1)), __dmul_rn(jp[2], c2));
+        const double inv = __ddiv_rn(1.0, det);
         double G[9];
-        G[0] = c0 * inv;
-        G[1] = c1 * inv;
-        G[2] = c2 * inv;
-        G[3] = (jp[2] * jp[7] - jp[1] * jp[8]) * inv;
-        G[4] = (jp[0] * jp[8] - jp[2] * jp[6]) * inv;
-        G[5] = (jp[1] * jp[6] - jp[0] * jp[7]) * inv;
-        G[6] = (jp[1] * jp[5] - jp[2] * jp[4]) * inv;
-        G[7] = (jp[2] * jp[3] - jp[0] * jp[5]) * inv;
-        G[8] = (jp[0] * jp[4] - jp[1] * jp[3]) * inv;
+        G[0] = __dmul_rn(c0, inv);
+        G[1] = __dmul_rn(c1, inv);
+        G[2] = __dmul_rn(c2, inv);
+        G[3] = __dmul_rn(cof(jp[2], jp[7], jp[1], jp[8]), inv);
+        G[4] = __dmul_rn(cof(jp[0], jp[8], jp[2], jp[6]), inv);
+        G[5] = __dmul_rn(cof(jp[1], jp[6], jp[0], jp[7]), inv);
+        G[6] = __dmul_rn(cof(jp[1], jp[5], jp[2], jp[4]), inv);
+        G[7] = __dmul_rn(cof(jp[2], jp[3], jp[0], jp[5]), inv);
+        G[8] = __dmul_rn(cof(jp[0], jp[4], jp[1], jp[3]), inv);
         if (!(det > 0.0)) {
           atomicCAS(a.status, 0, LMG_ERR_DEGENERATE);
           atomicMin(a.bad_elem, (unsigned long long)e);
