@@ -32,14 +32,12 @@ struct ElemArgs {
   double nu;                  // Poisson ratio (elasticity)
   // Symmetric element matrices are stored as nv x nv blocks: the n diagonal
   // blocks and the n(n-1)/2 strictly upper blocks (a < b, row-major over a
-  // then b), written to their positions in the slot-ordered store:
-  // upos[e*(n + n(n-1)/2) + w] (w < n: diagonal block w, else upper block
-  // w - n), bit 31 set when the block is stored transposed.  The FP64 drop-in
-  // stores every entry as a double-float pair (hi + lo, 48-bit significand);
-  // the mixed form stores only the off-diagonal blocks, in FP32.
-  const int32_t *upos;
-  float2 *Kso;                // [positions][nv][nv]           (FP64 drop-in)
-  float *Kso32;               // [positions][nv][nv]           (mixed)
+  // then b).  The FP64 drop-in stores every entry as a double-float pair
+  // (hi + lo, 48-bit significand); the mixed form stores only the off-diagonal
+  // blocks, in FP32.
+  float2 *Kdiag2;             // [n_elem][n][nv][nv]          (FP64 drop-in)
+  float2 *Koff2;              // [n_elem][n(n-1)/2][nv][nv]   (FP64 drop-in)
+  float *Koff32;              // [n_elem][n(n-1)/2][nv][nv]   (mixed)
   float2 *Fe2;                // [n_elem][n][nv] load vector, double-float pairs
   int *status;                // [0] error code
   unsigned long long *bad_elem;  // first failing element id
@@ -79,14 +77,16 @@ struct GatherArgs {
   const int32_t *row_ptr;     // [n_dofs+1]
   const int32_t *bcol;        // [nnzb]
   const int32_t *bptr;        // [nnzb+1] contributions per block slot
-  // Run of every block slot in the slot-ordered store: {first position,
-  // count | t << 31}; t = 1 for a slot below the diagonal, which reads the
-  // run of its mirror slot transposed.
-  const int2 *srange;
+  // Per slot, ascending in element: diagonal slots hold e*nb + a (a Kdiag
+  // block); off-diagonal slots hold 2*(e*no + o) + t, o the strictly upper
+  // block of the element pair and t = 1 when the slot takes its transpose.
+  const int32_t *bcontrib;
+  int no;                     // strictly upper blocks per element
   const int32_t *fptr;        // [n_blocks+1]
   const int32_t *fcontrib;    // e*nb + a, ascending per block row
-  const float2 *Kso;
-  const float *Kso32;
+  const float2 *Kdiag2;
+  const float2 *Koff2;
+  const float *Koff32;
   const float2 *Fe2;
   const uint8_t *constrained; // [n_dofs] (mixed form applies the Dirichlet rows here)
   double *K;

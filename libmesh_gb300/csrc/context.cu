@@ -129,69 +129,6 @@ __global__ void k_encode(int64_t n, int nb, int32_t *v) {
   }
 }
 
-// ---- slot-ordered element-block store
-// The element kernels write every stored block (the nb diagonal and the
-// nb(nb-1)/2 strictly upper blocks of each element) straight into the
-// position where the insertion reads it: one array ordered by the upper
-// block slots of the CSR (block row P, then column Q >= P), each slot's
-// contributions contiguous and in element order.  A slot (P, Q) with Q < P
-// reads its mirror slot's run transposed.  So the insertion streams
-// contiguous runs instead of gathering blocks one index at a time.
-
-// Contributions stored for every slot: the slot's count when Q >= P, else 0.
-__global__ void k_upper_count(int64_t n_rows, const int64_t *brow_ptr, const int32_t *bcol, const int32_t *bptr,
-                              int32_t *ucnt) {
-  for (int64_t P = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; P < n_rows;
-       P += (int64_t)gridDim.x * blockDim.x)
-    for (int64_t j = brow_ptr[P]; j < brow_ptr[P + 1]; ++j)
-      ucnt[j] = bcol[j] >= (int32_t)P ? bptr[j + 1] - bptr[j] : 0;
-}
-
-// Store position of every element block, from the encoded contribution
-// lists of the upper slots: upos[e*ns + a] (diagonal block a) and
-// upos[e*ns + nb + o] (upper block o), bit 31 set when the slot takes the
-// transpose of the element's stored block (the kernel then stores it transposed).
-__global__ void k_upos(int64_t n_rows, int nb, const int64_t *brow_ptr, const int32_t *bcol, const int32_t *bptr,
-                       const int32_t *contrib, const int32_t *ustart, int32_t *upos) {
-  const int no = nb * (nb - 1) / 2, ns = nb + no;
-  for (int64_t P = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; P < n_rows;
-       P += (int64_t)gridDim.x * blockDim.x)
-    for (int64_t j = brow_ptr[P]; j < brow_ptr[P + 1]; ++j) {
-      const int32_t Q = bcol[j];
-      if (Q < (int32_t)P) continue;
-      for (int32_t c = bptr[j]; c < bptr[j + 1]; ++c) {
-        const int32_t x = contrib[c], u = ustart[j] + (c - bptr[j]);
-        if (Q == (int32_t)P) {
-          const int64_t e = x / nb;
-          upos[e * ns + (x - e * nb)] = u;
-        } else {
-          const int64_t y = x >> 1, e = y / no;
-          upos[e * ns + nb + (y - e * no)] = (int32_t)((uint32_t)u | ((uint32_t)(x & 1) << 31));
-        }
-      }
-    }
-}
-
-// Run of every slot in the store: {first position, count | transposed << 31}.
-__global__ void k_srange(int64_t n_rows, const int64_t *brow_ptr, const int32_t *bcol, const int32_t *bptr,
-                         const int32_t *ustart, int2 *srange) {
-  for (int64_t P = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; P < n_rows;
-       P += (int64_t)gridDim.x * blockDim.x)
-    for (int64_t j = brow_ptr[P]; j < brow_ptr[P + 1]; ++j) {
-      const int32_t Q = bcol[j], cnt = bptr[j + 1] - bptr[j];
-      if (Q >= (int32_t)P) {
-        srange[j] = make_int2(ustart[j], cnt);
-        continue;
-      }
-      int64_t lo = brow_ptr[Q], hi = brow_ptr[Q + 1];  // the mirror slot (Q, P)
-      while (lo < hi) {
-        const int64_t mid = (lo + hi) >> 1;
-        if (bcol[mid] < (int32_t)P) lo = mid + 1; else hi = mid;
-      }
-      srange[j] = make_int2(ustart[lo], (int32_t)((uint32_t)cnt | 0x80000000u));
-    }
-}
-
 // Nodal load split into double-float pairs (read by the affine element kernels).
 __global__ void k_split(int64_t n, const double *x, float2 *y) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
@@ -437,26 +374,6 @@ lmg_status build_plan(lmg_ctx *c) {
   k_segsort<<<grid_for(c, c->nnzb, 256), 256, 0, c->stream>>>(c->nnzb, c->d_bptr, c->d_bcontrib);
   k_encode<<<grid_for(c, npair, 256), 256, 0, c->stream>>>(npair, nb, c->d_bcontrib);
   c->launches += 3;
-  // slot-ordered store: positions of the element blocks and runs of the slots
-  {
-    int32_t *ustart = nullptr;
-    LMG_CUDA(c, dalloc(ustart, (size_t)c->nnzb + 1));
-    k_upper_count<<<grid_for(c, c->n_blocks, 256), 256, 0, c->stream>>>(c->n_blocks, c->d_brow_ptr, c->d_bcol,
-                                                                        c->d_bptr, cnt);
-    c->launches++;
-    if ((st = scan_i32(c, cnt, ustart, c->nnzb))) return st;
-    const int64_t ns = nb + (int64_t)nb * (nb - 1) / 2;
-    LMG_CUDA(c, dalloc(c->d_upos, (size_t)(c->n_elem * ns)));
-    LMG_CUDA(c, dalloc(c->d_srange, (size_t)c->nnzb));
-    k_upos<<<grid_for(c, c->n_blocks, 256), 256, 0, c->stream>>>(c->n_blocks, nb, c->d_brow_ptr, c->d_bcol, c->d_bptr,
-                                                                 c->d_bcontrib, ustart, c->d_upos);
-    k_srange<<<grid_for(c, c->n_blocks, 256), 256, 0, c->stream>>>(c->n_blocks, c->d_brow_ptr, c->d_bcol, c->d_bptr,
-                                                                   ustart, c->d_srange);
-    c->launches += 2;
-    LMG_CUDA(c, cudaStreamSynchronize(c->stream));
-    dfree(ustart);
-    dfree(c->d_bcontrib);  // the store positions replace the contribution lists
-  }
   dfree(c->d_relslot);
   if (c->max_bdeg <= 255) {  // the fused mixed form addresses slots with one byte
     LMG_CUDA(c, dalloc(c->d_relslot, (size_t)npair));
@@ -602,8 +519,8 @@ lmg_status lmg_context_destroy(lmg_ctx *c) {
   dfree(c->d_xyz); dfree(c->d_conn); dfree(c->d_aff); dfree(c->d_gen); dfree(c->d_eb);
   dfree(c->d_cmask); dfree(c->d_cons); dfree(c->d_brow_ptr); dfree(c->d_bcol); dfree(c->d_row_ptr); dfree(c->d_col);
   dfree(c->d_bptr); dfree(c->d_bcontrib); dfree(c->d_fptr); dfree(c->d_fcontrib); dfree(c->d_tab);
-  dfree(c->d_coef); dfree(c->d_f); dfree(c->d_f2); dfree(c->d_Kso); dfree(c->d_Fe2); dfree(c->d_K);
-  dfree(c->d_F); dfree(c->d_Kso32); dfree(c->d_status); dfree(c->d_bad); dfree(c->d_upos); dfree(c->d_srange);
+  dfree(c->d_coef); dfree(c->d_f); dfree(c->d_f2); dfree(c->d_Kdiag2); dfree(c->d_Koff2); dfree(c->d_Fe2); dfree(c->d_K);
+  dfree(c->d_F); dfree(c->d_Koff32); dfree(c->d_status); dfree(c->d_bad);
   dfree(c->d_relslot); dfree(c->d_geo);
   general_free(c);
   hier3_free(c);
@@ -772,8 +689,9 @@ lmg_status lmg_sparsity_build(lmg_ctx *c, int64_t *nnz) {
   LMG_CUDA(c, dalloc(c->d_K, (size_t)c->nnz));
   LMG_CUDA(c, dalloc(c->d_F, (size_t)c->n_dofs));
   const size_t b2 = (size_t)c->bs * c->bs, no = (size_t)c->nb * (c->nb - 1) / 2;
-  LMG_CUDA(c, dalloc(c->d_Kso, (size_t)c->n_elem * (c->nb + no) * b2));
-  dfree(c->d_Kso32);  // allocated on the first unfused mixed assembly
+  LMG_CUDA(c, dalloc(c->d_Kdiag2, (size_t)c->n_elem * c->nb * b2));
+  LMG_CUDA(c, dalloc(c->d_Koff2, (size_t)c->n_elem * no * b2));
+  dfree(c->d_Koff32);  // allocated on the first mixed assembly
   LMG_CUDA(c, dalloc(c->d_Fe2, (size_t)(c->n_elem * c->nl)));
   c->have_sparsity = true;
   if (nnz) *nnz = c->nnz;
@@ -973,8 +891,8 @@ lmg_status lmg_assemble(lmg_ctx *c, int32_t precision, double *K, double *F, int
   }
   const bool mixed = precision == LMG_MIXED;
   const bool fused = mixed && c->h_gen.empty() && c->d_relslot && fused_built(c->form, c->tab.n, c->n_vars);
-  if (mixed && !fused && !c->d_Kso32)
-    LMG_CUDA(c, dalloc(c->d_Kso32, (size_t)c->n_elem * (c->nb + c->nb * (c->nb - 1) / 2) * c->bs * c->bs));
+  if (mixed && !fused && !c->d_Koff32)
+    LMG_CUDA(c, dalloc(c->d_Koff32, (size_t)c->n_elem * c->nb * (c->nb - 1) / 2 * c->bs * c->bs));
   if (fused && !c->d_geo)
     LMG_CUDA(c, dalloc(c->d_geo, (size_t)c->n_elem * (c->form == LMG_POISSON ? 9 : 11)));
   lmg_status st = reset_status(c);
@@ -988,9 +906,9 @@ lmg_status lmg_assemble(lmg_ctx *c, int32_t precision, double *K, double *F, int
   a.nodal_f2 = c->d_f2;
   a.cmask = c->d_cmask;
   a.nu = c->nu;
-  a.upos = c->d_upos;
-  a.Kso = c->d_Kso;
-  a.Kso32 = c->d_Kso32;
+  a.Kdiag2 = c->d_Kdiag2;
+  a.Koff2 = c->d_Koff2;
+  a.Koff32 = c->d_Koff32;
   a.Fe2 = c->d_Fe2;
   a.status = c->d_status;
   a.bad_elem = c->d_bad;
@@ -1088,11 +1006,13 @@ lmg_status lmg_assemble(lmg_ctx *c, int32_t precision, double *K, double *F, int
   g.row_ptr = c->d_row_ptr;
   g.bcol = c->d_bcol;
   g.bptr = c->d_bptr;
-  g.srange = c->d_srange;
+  g.bcontrib = c->d_bcontrib;
+  g.no = c->nb * (c->nb - 1) / 2;
   g.fptr = c->d_fptr;
   g.fcontrib = c->d_fcontrib;
-  g.Kso = c->d_Kso;
-  g.Kso32 = c->d_Kso32;
+  g.Kdiag2 = c->d_Kdiag2;
+  g.Koff2 = c->d_Koff2;
+  g.Koff32 = c->d_Koff32;
   g.Fe2 = c->d_Fe2;
   g.constrained = c->d_cons;
   g.K = c->d_K;

@@ -60,16 +60,11 @@ struct lmg_ctx {
   double *d_coef = nullptr, *d_f = nullptr;
   float2 *d_f2 = nullptr;  // nodal load as double-float pairs
   // work and result buffers
-  // slot-ordered element-block store (build_plan): upos [E][nb + nb(nb-1)/2]
-  // store position of each stored element block (bit 31: store it transposed),
-  // srange [nnzb] run of each block slot {first position, count | transposed << 31}
-  int32_t *d_upos = nullptr;
-  int2 *d_srange = nullptr;
-  float2 *d_Kso = nullptr;   // [E (nb + nb(nb-1)/2)][bs][bs] double-float pairs (FP64 drop-in)
+  float2 *d_Kdiag2 = nullptr, *d_Koff2 = nullptr;
   float2 *d_Fe2 = nullptr;
   float2 *d_Re2 = nullptr;  // per-element residuals of lmg_residual
   double *d_K = nullptr, *d_F = nullptr;
-  float *d_Kso32 = nullptr;  // the same positions in FP32 (mixed form; diagonal positions unused)
+  float *d_Koff32 = nullptr;
   int *d_status = nullptr;
   unsigned long long *d_bad = nullptr;
   // general path (general.cu): constraint rows with coefficients or a

@@ -342,23 +342,19 @@ __global__ void __launch_bounds__(128) k_elem_affine(ElemArgs a) {
           V sv[9];
 #pragma unroll
           for (int mn = 0; mn < 9; ++mn) sv[mn] = R::ld(sS[mn * NB + blk]);
-          // store position of the block (read before the contraction so the load is in flight)
-          const int32_t up = a.upos[(int64_t)et * (N + NO) + (o < 0 ? ra : N + o)];
           V out[B2];
           contract_block<FORM, R>(gv, sv, out);
-          const bool tr = up < 0;
-          const int64_t base = (int64_t)(up & 0x7fffffff) * B2;
 #pragma unroll
           for (int ik = 0; ik < B2; ++ik) {
             const int i = ik / NV, kk = ik - i * NV;
             const int lr = i * N + ra, lc = kk * N + cb;
-            const int dst = tr ? kk * NV + i : ik;
             if constexpr (MIXED) {
-              a.Kso32[base + dst] = out[ik];
+              a.Koff32[((int64_t)et * NO + o) * B2 + ik] = out[ik];
             } else {
               float2 v = make_float2(out[ik].hi, out[ik].lo);
               if (((mask >> lr) | (mask >> lc)) & 1ull) v = make_float2(lr == lc ? 1.f : 0.f, 0.f);
-              a.Kso[base + dst] = v;
+              if (o < 0) a.Kdiag2[((int64_t)et * N + ra) * B2 + ik] = v;
+              else a.Koff2[((int64_t)et * NO + o) * B2 + ik] = v;
             }
           }
         }
@@ -622,18 +618,15 @@ __global__ void __launch_bounds__(128) k_elem_general(ElemArgs a) {
       if (blk < NB) {
         const int ra = blk / N, cb = blk - ra * N;
         if (ra > cb || (MIXED && ra == cb)) continue;
-        const int32_t up = a.upos[(int64_t)e * (N + NO) + (ra == cb ? ra : N + off_index(N, ra, cb))];
-        const bool tr = up < 0;
-        const int64_t base = (int64_t)(up & 0x7fffffff) * B2;
 #pragma unroll
         for (int ik = 0; ik < B2; ++ik) {
           const int i = ik / NV, kk = ik - i * NV;
-          const int dst = tr ? kk * NV + i : ik;
           if (MIXED) {
-            a.Kso32[base + dst] = (float)acc[k][ik];
+            a.Koff32[((int64_t)e * NO + off_index(N, ra, cb)) * B2 + ik] = (float)acc[k][ik];
           } else {
             const DF v = df_split(masked((double)acc[k][ik], mask, i * N + ra, kk * N + cb));
-            a.Kso[base + dst] = make_float2(v.hi, v.lo);
+            if (ra == cb) a.Kdiag2[((int64_t)e * N + ra) * B2 + ik] = make_float2(v.hi, v.lo);
+            else a.Koff2[((int64_t)e * NO + off_index(N, ra, cb)) * B2 + ik] = make_float2(v.hi, v.lo);
           }
         }
       }

@@ -4,18 +4,17 @@
 // (SparseMatrix::add_matrix -> MatSetValues(ADD_VALUES), src/numerics/petsc_matrix.C:735-755;
 // NumericVector::add_vector, src/numerics/petsc_vector.C:174-195), so every CSR
 // value is ((0 + c_e1) + c_e2) + ... over the elements touching it, in element
-// order.  Here the scatter is inverted into a gather: the element kernels
-// write every stored element block into the slot-ordered store, where the
-// contributions of each block slot of the upper triangle lie contiguous and
-// in element order, and one warp per block row sums the runs of its slots (a
-// slot below the diagonal reads its mirror's run transposed).  The result is
-// deterministic and the summation order is the reference's.
+// order.  Here the scatter is inverted into a gather: the plan lists, for every
+// block slot of the CSR, the element blocks that land on it in ascending element
+// order, and one warp per block row sums them.  The result is deterministic and
+// the summation order is the reference's.
 //
-// Lanes own the bs*bs entries of consecutive slots, so the bs*bs values of
-// one stored block are read by bs*bs neighbouring lanes (one contiguous
-// chunk) and consecutive contributions of a slot are consecutive chunks.
-// Sums run in double-float (df.cuh) on the FP32 pipe; GB300's FP64 pipe
-// would otherwise bound this memory-streaming kernel.
+// Lanes walk the bs*bs values of consecutive block slots, so the bs*bs values of
+// one stored element block are read by bs*bs neighbouring lanes (one contiguous
+// chunk); each lane loads its contribution indices four at a time before
+// summing, to keep several independent loads in flight.  Sums run in
+// double-float (df.cuh) on the FP32 pipe; GB300's FP64 pipe would otherwise
+// bound this memory-streaming kernel.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -48,47 +47,166 @@ __device__ __forceinline__ void acc_add(DFAcc &a, float2 v) {
   a.hi = s;
 }
 
-// FP64 drop-in insertion, warp per block row P (persistent grid).  Lane
-// l < (32/B2)*B2 owns entry (i, k) of the slots jj = l / B2 + (32/B2) t: it
-// sums that entry over the slot's run in element order (the first term starts
-// the sum, four loads in flight), in double-float, and writes
-// K[BS P + i][BS Q + k] rounded once to FP64.  Every row of K is written
-// contiguously; a slot and its transpose sum the same entries in the same
-// order, so K_QP = K_PQ^T bit for bit.
+// FP64 drop-in insertion, warp per block row P.  Lane l < (32/BS)*BS owns row
+// i = l % BS of the slots jj = l / BS + (32/BS) t, i.e. the BS entries
+// K[BS P + i][BS Q + k], k < BS: one decoded contribution index serves BS
+// loads, and the row's values are written contiguously.  Every slot of the row
+// is summed (a lower slot reads the stored upper element block transposed), so
+// each row of K is written contiguously: writing the upper values into their
+// transposed slots instead scatters 8-byte stores over other rows and measured
+// slower.  Both forms are symmetric and a slot and its transpose sum the same
+// entries in the same element order, so K_QP = K_PQ^T bit for bit.  Each value
+// is the double-float sum, in element order, of the double-float element
+// entries that land on it, rounded once to FP64.
+//
+// The row's plan is staged in shared memory first (slot offsets, then the
+// contribution indices, each one coalesced load), so that the element-block
+// loads of all its slots are independent of one another; rows larger than the
+// staging buffers read the plan from global memory (same sums).  The load
+// vector's first 32 contributions are fetched before the slots.
+constexpr int GW = 8;      // warps (block rows in flight) per CTA
+constexpr int DCAP = 128;  // staged slots per block row
+constexpr int CCAP = 640;  // staged contributions per block row
+
+// Slots jj = js, js + SPI, ... of block row P; `ptr[jj]` is the slot's first
+// contribution relative to `con`.
 template <int BS>
-__global__ void __launch_bounds__(256) k_gather(GatherArgs g) {
-  constexpr int B2 = BS * BS, SPL = 32 / B2;
-  const int lane = threadIdx.x & 31;
-  const int js = lane / B2, rem = lane - js * B2;
-  const bool act = lane < SPL * B2;
-  const int i = rem / BS, k = rem - i * BS, trn = k * BS + i;
-  for (int64_t P = g.row_begin + (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5); P < g.row_end;
-       P += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+__device__ __forceinline__ void row_slots(const GatherArgs &g, const int32_t *ptr, const int32_t *con, int deg,
+                                          int jdiag, int js, int i, int32_t rowp) {
+  constexpr int B2 = BS * BS, SPI = 32 / BS;
+  for (int jj = js; jj < deg; jj += SPI) {
+    const int32_t a0 = ptr[jj], a1 = ptr[jj + 1];
+    const bool diag = jj == jdiag;
+    const float2 *Kp = diag ? g.Kdiag2 : g.Koff2;
+    DFAcc s[BS];
+#pragma unroll
+    for (int k = 0; k < BS; ++k) s[k] = {0.f, 0.f};
+    if (a0 < a1) {  // the first term starts the sum
+      const int32_t x = con[a0];
+      const int64_t b = diag ? (int64_t)x * B2 : (int64_t)(x >> 1) * B2;
+      const bool t = !diag && (x & 1);
+#pragma unroll
+      for (int k = 0; k < BS; ++k) {
+        const float2 v = __ldg(Kp + b + (t ? k * BS + i : i * BS + k));
+        s[k] = {v.x, v.y};
+      }
+    }
+    for (int32_t u = a0 + 1; u < a1; u += 2) {
+      const bool two = u + 1 < a1;
+      const int32_t x0 = con[u], x1 = two ? con[u + 1] : x0;
+      // diagonal slots list e*nb + a (no transpose), the others 2*(e*no + o) + t
+      const int64_t b0 = diag ? (int64_t)x0 * B2 : (int64_t)(x0 >> 1) * B2;
+      const int64_t b1 = diag ? (int64_t)x1 * B2 : (int64_t)(x1 >> 1) * B2;
+      const bool t0 = !diag && (x0 & 1), t1 = !diag && (x1 & 1);
+      float2 v0[BS], v1[BS];
+#pragma unroll
+      for (int k = 0; k < BS; ++k) {
+        v0[k] = __ldg(Kp + b0 + (t0 ? k * BS + i : i * BS + k));
+        v1[k] = two ? __ldg(Kp + b1 + (t1 ? k * BS + i : i * BS + k)) : float2{0.f, 0.f};
+      }
+#pragma unroll
+      for (int k = 0; k < BS; ++k) {
+        acc_add(s[k], v0[k]);
+        if (two) acc_add(s[k], v1[k]);
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < BS; ++k) g.K[rowp + jj * BS + k] = f2d(s[k].hi) + f2d(s[k].lo);
+  }
+}
+
+template <int BS>
+__global__ void __launch_bounds__(GW * 32, 6) k_gather(GatherArgs g) {
+  constexpr int SPI = 32 / BS;
+  static_assert(BS <= 4, "the load-vector butterfly carries at most 4 components");
+  __shared__ int32_t s_ptr[GW][DCAP + 1];
+  __shared__ int32_t s_con[GW][CCAP];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int js = lane / BS, i = lane - js * BS;
+  const bool act = lane < SPI * BS;
+  int32_t *sp = s_ptr[warp], *sc = s_con[warp];
+  for (int64_t P = g.row_begin + (int64_t)blockIdx.x * GW + warp; P < g.row_end; P += (int64_t)gridDim.x * GW) {
     const int64_t rb = g.brow_ptr[P];
     const int deg = (int)(g.brow_ptr[P + 1] - rb);
     const int32_t rowp = act ? g.row_ptr[BS * P + i] : 0;
-    for (int jj = js; act && jj < deg; jj += SPL) {
-      const int2 r = __ldg(g.srange + rb + jj);
-      const int cnt = r.y & 0x7fffffff;
-      const float2 *src = g.Kso + (int64_t)r.x * B2 + (r.y < 0 ? trn : rem);
-      DFAcc s = {0.f, 0.f};
-      if (cnt > 0) {
-        const float2 v = __ldg(src);
-        s = {v.x, v.y};
+    const int32_t f0 = g.fptr[P], f1 = g.fptr[P + 1];
+    const int32_t fc = f0 + lane < f1 ? __ldg(g.fcontrib + f0 + lane) : -1;
+    float2 fv[BS];
+#pragma unroll
+    for (int q = 0; q < BS; ++q) fv[q] = fc >= 0 ? __ldg(g.Fe2 + (int64_t)fc * BS + q) : float2{0.f, 0.f};
+    int jdiag = -1;
+    for (int t = lane; t < deg; t += 32)
+      if (g.bcol[rb + t] == (int32_t)P) jdiag = t;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) jdiag = max(jdiag, __shfl_xor_sync(0xffffffffu, jdiag, o));
+    bool staged = false;
+    if (deg <= DCAP) {
+      for (int t = lane; t <= deg; t += 32) sp[t] = __ldg(g.bptr + rb + t);
+      __syncwarp();
+      const int32_t cb = sp[0], nc = sp[deg] - cb;
+      __syncwarp();  // every lane has read cb before sp is rebased
+      if (nc <= CCAP) {
+        staged = true;
+        for (int t = lane; t < nc; t += 32) sc[t] = __ldg(g.bcontrib + cb + t);
+        for (int t = lane; t <= deg; t += 32) sp[t] -= cb;
+        __syncwarp();
+        if (act) row_slots<BS>(g, sp, sc, deg, jdiag, js, i, rowp);
       }
-      int c = 1;
-      for (; c + 3 < cnt; c += 4) {
-        const float2 v0 = __ldg(src + (int64_t)c * B2), v1 = __ldg(src + (int64_t)(c + 1) * B2);
-        const float2 v2 = __ldg(src + (int64_t)(c + 2) * B2), v3 = __ldg(src + (int64_t)(c + 3) * B2);
-        acc_add(s, v0);
-        acc_add(s, v1);
-        acc_add(s, v2);
-        acc_add(s, v3);
-      }
-      for (; c < cnt; ++c) acc_add(s, __ldg(src + (int64_t)c * B2));
-      g.K[rowp + jj * BS + k] = f2d(s.hi) + f2d(s.lo);
     }
-    row_load<BS>(g, P, lane);
+    if (!staged && act) row_slots<BS>(g, g.bptr + rb, g.bcontrib, deg, jdiag, js, i, rowp);
+    // load vector: lane l sums contributions l, l + 32, ... in element order;
+    // one butterfly then reduces all BS components (halving the set carried
+    // per lane at the first two steps), the lower lane's value first.
+    DF s[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) s[q] = q < BS ? df_add(DF{0.f, 0.f}, DF{fv[q < BS ? q : 0].x, fv[q < BS ? q : 0].y})
+                                              : DF{0.f, 0.f};
+    for (int32_t c = f0 + 32 + lane; c < f1; c += 32) {
+      const int64_t base = (int64_t)g.fcontrib[c] * BS;
+#pragma unroll
+      for (int q = 0; q < BS; ++q) {
+        const float2 v = g.Fe2[base + q];
+        s[q] = df_add(s[q], DF{v.x, v.y});
+      }
+    }
+    DF r;
+    if constexpr (BS == 1) {
+      r = s[0];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        DF y;
+        y.hi = __shfl_xor_sync(0xffffffffu, r.hi, o);
+        y.lo = __shfl_xor_sync(0xffffffffu, r.lo, o);
+        r = (lane & o) ? df_add(y, r) : df_add(r, y);
+      }
+    } else {
+      const bool u16 = lane & 16, u8 = lane & 8;
+      DF k0 = u16 ? s[2] : s[0], k1 = u16 ? s[3] : s[1];  // kept: components 2h, 2h + 1
+      DF e0 = u16 ? s[0] : s[2], e1 = u16 ? s[1] : s[3];  // sent to the partner
+      DF y0, y1;
+      y0.hi = __shfl_xor_sync(0xffffffffu, e0.hi, 16);
+      y0.lo = __shfl_xor_sync(0xffffffffu, e0.lo, 16);
+      y1.hi = __shfl_xor_sync(0xffffffffu, e1.hi, 16);
+      y1.lo = __shfl_xor_sync(0xffffffffu, e1.lo, 16);
+      k0 = u16 ? df_add(y0, k0) : df_add(k0, y0);
+      k1 = u16 ? df_add(y1, k1) : df_add(k1, y1);
+      r = u8 ? k1 : k0;                                   // component 2h + b
+      const DF e = u8 ? k0 : k1;
+      DF y;
+      y.hi = __shfl_xor_sync(0xffffffffu, e.hi, 8);
+      y.lo = __shfl_xor_sync(0xffffffffu, e.lo, 8);
+      r = u8 ? df_add(y, r) : df_add(r, y);
+#pragma unroll
+      for (int o = 4; o > 0; o >>= 1) {
+        y.hi = __shfl_xor_sync(0xffffffffu, r.hi, o);
+        y.lo = __shfl_xor_sync(0xffffffffu, r.lo, o);
+        r = (lane & o) ? df_add(y, r) : df_add(r, y);
+      }
+    }
+    // lane 16 h + 8 b holds component 2h + b
+    const int comp = BS == 1 ? lane : ((lane >> 4) << 1) + ((lane >> 3) & 1);
+    if ((BS == 1 ? lane == 0 : (lane & 7) == 0) && comp < BS) g.F[BS * P + comp] = df_to_double(r);
+    __syncwarp();
   }
 }
 
@@ -117,18 +235,21 @@ __global__ void __launch_bounds__(256) k_gather_mixed(GatherArgs g) {
       const int64_t j = rb + jj;
       const int32_t Q = g.bcol[j];
       if (Q == (int32_t)P) { jdiag = jj; continue; }
-      // FP32 sum of the FP32 contributions, in element order
-      const int2 r = __ldg(g.srange + j);
-      const int cnt = r.y & 0x7fffffff;
-      const float *src = g.Kso32 + (int64_t)r.x * B2 + (r.y < 0 ? tr : rem);
+      // FP32 sum of the FP32 contributions, in element order (32-bit offsets:
+      // the plan guarantees n_contributions * bs^2 < 2^31)
+      const int32_t c0 = g.bptr[j], c1 = g.bptr[j + 1];
       float kv = 0.f;
-      int c = 0;
-      for (; c + 3 < cnt; c += 4) {
-        const float v0 = __ldg(src + (int64_t)c * B2), v1 = __ldg(src + (int64_t)(c + 1) * B2);
-        const float v2 = __ldg(src + (int64_t)(c + 2) * B2), v3 = __ldg(src + (int64_t)(c + 3) * B2);
-        kv = __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(kv, v0), v1), v2), v3);
+      for (int32_t c = c0; c < c1; c += 4) {
+        float v[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int32_t x = (c + u < c1) ? __ldg(g.bcontrib + c + u) : -1;
+          v[u] = (x >= 0) ? __ldg(g.Koff32 + (x >> 1) * B2 + ((x & 1) ? tr : rem)) : 0.f;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+          if (c + u < c1) kv = __fadd_rn(kv, v[u]);
       }
-      for (; c < cnt; ++c) kv = __fadd_rn(kv, __ldg(src + (int64_t)c * B2));
       acc = df_add1(acc, kv);  // row sums stay double-float over the stored entries
       const bool masked = rc || g.constrained[(int64_t)BS * Q + k] != 0;
       g.K[rowp + jj * BS + k] = masked ? 0.0 : f2d(kv);
@@ -207,11 +328,11 @@ void launch_gather(const GatherArgs &g0, bool mixed, cudaStream_t s) {
     else if (g.bs == 3) k_gather_mixed<3><<<(int)blocks, 256, 0, s>>>(g);
   } else {  // persistent: every resident warp walks block rows P, P + all warps, ...
     int per_sm = 1;
-    if (g.bs == 1) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gather<1>, 256, 0);
-    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gather<3>, 256, 0);
-    const int64_t rows = std::min<int64_t>((warps + 7) / 8, (int64_t)n_sm * std::max(per_sm, 1));
-    if (g.bs == 1) k_gather<1><<<(unsigned)rows, 256, 0, s>>>(g);
-    else if (g.bs == 3) k_gather<3><<<(unsigned)rows, 256, 0, s>>>(g);
+    if (g.bs == 1) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gather<1>, GW * 32, 0);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gather<3>, GW * 32, 0);
+    const int64_t rows = std::min<int64_t>((warps + GW - 1) / GW, (int64_t)n_sm * std::max(per_sm, 1));
+    if (g.bs == 1) k_gather<1><<<(unsigned)rows, GW * 32, 0, s>>>(g);
+    else if (g.bs == 3) k_gather<3><<<(unsigned)rows, GW * 32, 0, s>>>(g);
   }
 }
 
