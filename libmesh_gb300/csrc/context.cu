@@ -738,8 +738,30 @@ lmg_status lmg_form_set(lmg_ctx *c, int32_t form, int32_t fe_order, int32_t q_or
   if (c->hier3) return hier3_form_set(c, form, q_order, elem_coef, nodal_f);
   const int family = (fe_order & LMG_HIERARCHIC) ? 1 : 0;
   fe_order &= 0xff;
+  // HIERARCHIC SECOND on HEX27: the shapes follow the elements' orientation
+  // pattern (cube_indices' face swaps), built here for a mesh whose elements
+  // all share one pattern (build_cube meshes)
+  double X8[8][3];
+  const double *xp = nullptr;
+  if (family == 1 && fe_order == 2 && c->elem_type == LMG_HEX27 && c->n_elem > 0) {
+    uint64_t pat0 = 0;
+    for (int64_t e = 0; e < c->n_elem; ++e) {
+      double X[8][3];
+      for (int a = 0; a < 8; ++a)
+        for (int d = 0; d < 3; ++d) X[a][d] = c->h_xyz[(size_t)(3 * (int64_t)c->h_conn[(size_t)(e * c->npe + a)] + d)];
+      const uint64_t p = hex27_p2_pattern(X);
+      if (e == 0) {
+        pat0 = p;
+        std::copy(&X[0][0], &X[0][0] + 24, &X8[0][0]);
+      } else if (p != pat0) {
+        return fail(c, LMG_ERR_UNSUPPORTED,
+                    "form_set: HIERARCHIC SECOND on HEX27 needs one element orientation pattern per mesh", e);
+      }
+    }
+    xp = &X8[0][0];
+  }
   FETables t;
-  std::string err = build_fe_tables(t, c->elem_type, fe_order, q_order, family);
+  std::string err = build_fe_tables(t, c->elem_type, fe_order, q_order, family, xp);
   if (!err.empty()) return fail(c, LMG_ERR_UNSUPPORTED, "form_set: " + err);
   if (t.n != c->npe || t.n_geo != c->npe)
     return fail(c, LMG_ERR_UNSUPPORTED, "form_set: only isoparametric LAGRANGE elements are built");

@@ -289,9 +289,11 @@ double hier1d(int i, double xi) {
 
 // HIERARCHIC hex shapes for p <= 2 (fe_hierarchic_shape_3D.C:2249-2290 with
 // cube_indices, :166-760): the tensor index of dof i is the HEX27 node index
-// table (vertices, one edge dof per edge, one dof per face, one interior dof),
-// and the bases are even in every coordinate, so the edge / face orientation
-// flips of cube_indices leave them unchanged.  Value = (s0 s1) s2;
+// table (vertices, one edge dof per edge, one dof per face, one interior dof).
+// The bases are even in every coordinate, so the reflections of cube_indices
+// leave them unchanged, but its face swaps move coordinates between the
+// product's factors: at SECOND order the shapes follow the element's
+// orientation pattern (hex27_p2_shape, given its vertices X8).  Value = (s0 s1) s2;
 // derivative = (shape(p + eps e_j) - shape(p - eps e_j)) / 2. / eps with
 // eps = 1e-6 (fe_fdm_deriv, src/fe/fe.C:794-811, 929-944).
 //
@@ -320,7 +322,7 @@ double hier_prism6(int a, const double *x) {
   return t[i01] * (i2 == 0 ? .5 * (1. - x[2]) : .5 * (1. + x[2]));
 }
 
-int hierarchic_shapes(int type, int order, const double *p, double *v, double *g) {
+int hierarchic_shapes(int type, int order, const double *p, double *v, double *g, const double *X8) {
   const bool tet = (type == LMG_TET4 && order == 1) || (type == LMG_TET10 && order == 2);
   const bool tet3 = false;  // cubic tets depend on the element: hier_tet3_shapes
   const bool prism = type == LMG_PRISM6 && order == 1;
@@ -329,6 +331,7 @@ int hierarchic_shapes(int type, int order, const double *p, double *v, double *g
   auto shape = [&](int a, const double *x) {
     if (prism) return hier_prism6(a, x);
     if (tet) return hier_tet(a, x);
+    if (order == 2 && X8) return hex27_p2_shape(reinterpret_cast<const double(*)[3]>(X8), a, x);
     const int i0 = (order == 1) ? HEX8_I[0][a] : HEX27_I[0][a], i1 = (order == 1) ? HEX8_I[1][a] : HEX27_I[1][a],
               i2 = (order == 1) ? HEX8_I[2][a] : HEX27_I[2][a];
     return hier1d(i0, x[0]) * hier1d(i1, x[1]) * hier1d(i2, x[2]);
@@ -420,7 +423,7 @@ int hier_tet3_shapes(const TetOrient &o, const double *p, double *v, double *g) 
   return 20;
 }
 
-std::string build_fe_tables(FETables &t, int type, int fe_order, int q_order, int family) {
+std::string build_fe_tables(FETables &t, int type, int fe_order, int q_order, int family, const double *X8) {
   t = FETables();
   t.elem_type = type;
   t.fe_order = fe_order;
@@ -433,7 +436,7 @@ std::string build_fe_tables(FETables &t, int type, int fe_order, int q_order, in
                        (type == LMG_PRISM6 && fe_order == 1)))
     return "HIERARCHIC is built for FIRST on HEX8 / TET4 / PRISM6 and SECOND on HEX27 / TET10";
   auto fe_shapes = [&](const double *p, double *v, double *g) {
-    return family == 1 ? hierarchic_shapes(type, fe_order, p, v, g) : lagrange_shapes(type, fe_order, p, v, g);
+    return family == 1 ? hierarchic_shapes(type, fe_order, p, v, g, X8) : lagrange_shapes(type, fe_order, p, v, g);
   };
   const bool hex = (type == LMG_HEX8 || type == LMG_HEX27);
   const bool tet = (type == LMG_TET4 || type == LMG_TET10 || type == LMG_TET14);

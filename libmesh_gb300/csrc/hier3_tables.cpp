@@ -53,26 +53,27 @@ struct Sig {
   }
 };
 
-// cube_indices at totalorder 3 for the element with vertex coordinates X[8][3].
-Sig cube_sig(const double (*X)[3], int i) {
+// cube_indices at totalorder e + 1 (e = 1 or 2 dofs per edge) for the element
+// with vertex coordinates X[8][3].
+Sig cube_sig(const double (*X)[3], int i, int e = 2) {
   Sig g = {{0, 0, 0}, {0, 1, 2}, {0, 0, 0}};
   static const int V[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0}, {0, 0, 1}, {1, 0, 1}, {1, 1, 1}, {0, 1, 1}};
   if (i < 8) {
     for (int s = 0; s < 3; ++s) g.idx[s] = V[i][s];
     return g;
   }
-  if (i < 32) {  // two dofs per edge; the edge's own coordinate flips by orientation
+  if (i < 8 + 12 * e) {  // e dofs per edge; the edge's own coordinate flips by orientation
     static const int DIR[12] = {0, 1, 0, 1, 2, 2, 2, 2, 0, 1, 0, 1};
     static const int FIX[12][2] = {{0, 0}, {1, 0}, {1, 0}, {0, 0}, {0, 0}, {1, 0},
                                    {1, 1}, {0, 1}, {0, 1}, {1, 1}, {1, 1}, {0, 1}};
-    const int ed = (i - 8) / 2, k = i - 2 * ed - 6, d = DIR[ed];
+    const int ed = (i - 8) / e, k = i - e * ed - 6, d = DIR[ed];
     const bool pos = pt_less(X[EDGE[ed][1]], X[EDGE[ed][0]]);  // Elem::positive_edge_orientation
     const bool flip = (ed == 2 || ed == 10) ? !pos : pos;
     for (int s = 0, f = 0; s < 3; ++s) g.idx[s] = (s == d) ? k : FIX[ed][f++];
     g.neg[d] = flip ? 1 : 0;
     return g;
   }
-  if (i < 56) {  // four dofs per face: in-face coordinates swapped / reflected by the face case
+  if (i < 8 + 12 * e + 6 * e * e) {  // e^2 dofs per face: in-face coordinates swapped / reflected by the face case
     static const int SQ_ROW[4] = {0, 1, 1, 0}, SQ_COL[4] = {0, 0, 1, 1};
     static const int AX[6][2] = {{0, 1}, {0, 2}, {1, 2}, {0, 2}, {1, 2}, {0, 1}};  // slots A, B
     static const int FIXED[6][2] = {{2, 0}, {1, 0}, {0, 1}, {1, 1}, {0, 0}, {2, 1}};  // slot, index
@@ -89,7 +90,7 @@ Sig cube_sig(const double (*X)[3], int i) {
                                       {{ID, SW}, {TA, TB}, {NG, NS}, {TC, TD}},
                                       {{ID, SW}, {TA, TB}, {NG, NS}, {TC, TD}},
                                       {{ID, SW}, {TC, TD}, {NG, NS}, {TA, ID}}};
-    const int f = (i - 32) / 4, b = i - 32 - 4 * f;
+    const int f = (i - 8 - 12 * e) / (e * e), b = i - 8 - 12 * e - e * e * f;
     const int sa = AX[f][0], sb = AX[f][1];
     g.idx[sa] = SQ_ROW[b] + 2;
     g.idx[sb] = SQ_COL[b] + 2;
@@ -117,7 +118,7 @@ Sig cube_sig(const double (*X)[3], int i) {
   }
   static const int CB_COL[8] = {0, 0, 1, 1, 0, 1, 1, 0}, CB_ROW[8] = {0, 1, 1, 0, 1, 1, 0, 0},
                    CB_PAGE[8] = {0, 0, 0, 0, 1, 1, 1, 1};
-  const int b = i - 56;
+  const int b = i - 8 - 12 * e - 6 * e * e;
   g.idx[0] = CB_COL[b] + 2;
   g.idx[1] = CB_ROW[b] + 2;
   g.idx[2] = CB_PAGE[b] + 2;
@@ -141,6 +142,23 @@ double sig_value(const Sig &g, const double *p) {
 }
 
 }  // namespace
+
+// HIERARCHIC SECOND on HEX27: the per-shape signature of an element (from its
+// vertex coordinates X[8][3]) and the evaluation of shape a at p in the
+// reference's order (s0 s1) s2 at the remapped coordinates.  The face swaps
+// of cube_indices change the rounding of the face shapes and, through the
+// central differences, their derivatives; elements of one mesh that share a
+// signature share their reference tables.
+uint64_t hex27_p2_pattern(const double (*X)[3]) {
+  uint64_t k = 0;
+  for (int i = 20; i < 26; ++i) {  // only the face shapes' signatures vary at this order
+    const Sig g = cube_sig(X, i, 1);
+    k = k * 64 + (uint64_t)(g.src[0] * 16 + g.src[1] * 4 + g.src[2]);
+  }
+  return k;
+}
+
+double hex27_p2_shape(const double (*X)[3], int a, const double *p) { return sig_value(cube_sig(X, a, 1), p); }
 
 std::string build_hier3_tables(Hier3Tables &h, int q_order, int64_t n_elem, const double *xyz, const int32_t *conn) {
   h = Hier3Tables();

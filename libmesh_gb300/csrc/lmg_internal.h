@@ -110,7 +110,11 @@ struct FETables {
 };
 // family 1 (HIERARCHIC, hexahedra, p <= 2): products of the 1-D hierarchic
 // shapes, reference derivatives by libMesh's central differences (eps = 1e-6).
-std::string build_fe_tables(FETables &t, int elem_type, int fe_order, int q_order, int family = 0);
+// X8: for HIERARCHIC SECOND on HEX27, the vertex coordinates [8][3] of an
+// element whose orientation pattern every element of the mesh shares (the
+// tables then follow that pattern's evaluation order).
+std::string build_fe_tables(FETables &t, int elem_type, int fe_order, int q_order, int family = 0,
+                            const double *X8 = nullptr);
 
 // Cubic HIERARCHIC hex tables (hier3_tables.cpp): each element's 64 shape
 // variants and the tables over the variants that occur.
@@ -132,6 +136,11 @@ struct Hier3Tables {
   std::vector<int32_t> batch;    // [n_batch][3]: pattern, first index in order, count
 };
 std::string build_hier3_tables(Hier3Tables &h, int q_order, int64_t n_elem, const double *xyz, const int32_t *conn);
+// HIERARCHIC SECOND on HEX27 (cube_indices at totalorder 2): the orientation
+// pattern of an element from its vertex coordinates, and shape a at p as the
+// reference evaluates it on such an element.
+uint64_t hex27_p2_pattern(const double (*X)[3]);
+double hex27_p2_shape(const double (*X)[3], int a, const double *p);
 
 // Orientation of a TET14 for the cubic HIERARCHIC basis: bit e of flip set
 // when edge e's order-3 basis is negated, fv[f] the vertices of face f as

@@ -480,14 +480,18 @@ Pt min_point(const std::vector<Pt> &X, unsigned a, unsigned b, unsigned c, unsig
   return mn(mn(X[a], X[b]), mn(X[c], X[d]));
 }
 
-void cube_indices_p3(const std::vector<Pt> &X, unsigned i, double &xi, double &eta, double &zeta, unsigned &i0,
-                     unsigned &i1, unsigned &i2) {
+// e = totalorder - 1 dofs per edge (e <= 2: totalorder 2 or 3).  At
+// totalorder 2 the edge flips and face reflections negate arguments of even
+// 1-D functions (no change), but the face swaps move coordinates between the
+// product's factors, which changes its rounding -- and, through the central
+// differences, the derivatives by ~1e-11 -- so the remap is applied there too.
+void cube_indices_hex(const std::vector<Pt> &X, unsigned e, unsigned i, double &xi, double &eta, double &zeta,
+                      unsigned &i0, unsigned &i1, unsigned &i2) {
   static const unsigned SQ_ROW[4] = {0, 1, 1, 0}, SQ_COL[4] = {0, 0, 1, 1};
   static const unsigned CB_COL[8] = {0, 0, 1, 1, 0, 1, 1, 0}, CB_ROW[8] = {0, 1, 1, 0, 1, 1, 0, 0},
                         CB_PAGE[8] = {0, 0, 0, 0, 1, 1, 1, 1};
   static const unsigned V[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0},
                                    {0, 0, 1}, {1, 0, 1}, {1, 1, 1}, {0, 1, 1}};
-  const unsigned e = 2;
   const double xs = xi, es = eta, zs = zeta;
   if (i < 8) {
     i0 = V[i][0]; i1 = V[i][1]; i2 = V[i][2];
@@ -562,18 +566,22 @@ void cube_indices_p3(const std::vector<Pt> &X, unsigned i, double &xi, double &e
 
 // FE<3,HIERARCHIC>::shape at totalorder 3 on one element: cube_indices, then
 // (s0 * s1) * s2 at the remapped coordinates.
-double hier_hex3_shape(const std::vector<Pt> &X, unsigned i, const Pt &p) {
+double hier_hexo_shape(const std::vector<Pt> &X, unsigned order, unsigned i, const Pt &p) {
   double xi = p.v[0], eta = p.v[1], zeta = p.v[2];
   unsigned i0, i1, i2;
-  cube_indices_p3(X, i, xi, eta, zeta, i0, i1, i2);
+  cube_indices_hex(X, order - 1, i, xi, eta, zeta, i0, i1, i2);
   return hier_1d(i0, xi) * hier_1d(i1, eta) * hier_1d(i2, zeta);
 }
-double hier_hex3_deriv(const std::vector<Pt> &X, unsigned i, unsigned j, const Pt &p) {
+double hier_hexo_deriv(const std::vector<Pt> &X, unsigned order, unsigned i, unsigned j, const Pt &p) {
   const double eps = 1.e-6;
   Pt pp = p, pm = p;
   pp.v[j] += eps;
   pm.v[j] -= eps;
-  return (hier_hex3_shape(X, i, pp) - hier_hex3_shape(X, i, pm)) / 2. / eps;
+  return (hier_hexo_shape(X, order, i, pp) - hier_hexo_shape(X, order, i, pm)) / 2. / eps;
+}
+double hier_hex3_shape(const std::vector<Pt> &X, unsigned i, const Pt &p) { return hier_hexo_shape(X, 3, i, p); }
+double hier_hex3_deriv(const std::vector<Pt> &X, unsigned i, unsigned j, const Pt &p) {
+  return hier_hexo_deriv(X, 3, i, j, p);
 }
 
 // fe_fdm_deriv (src/fe/fe.C:794-811, 929-944): central difference, eps = 1e-6.
@@ -793,8 +801,8 @@ struct OracleFE {
     type = type_; order = order_;
     if (!qgauss_3d(type, q_order, qp, qw)) return false;
     nq = (int)qp.size();
-    const bool p3 = family == 1 && order == 3 && (type == HEX27 || type == TET14);
-    n = p3 ? (type == HEX27 ? 64 : 20) : n_shapes(type, order);
+    const bool p3 = family == 1 && ((order == 3 && (type == HEX27 || type == TET14)) || (order == 2 && type == HEX27));
+    n = p3 ? (type == HEX27 ? (order + 1) * (order + 1) * (order + 1) : 20) : n_shapes(type, order);
     const int geo_order = (type == HEX27 || type == TET10) ? 2 : (type == TET14 ? 3 : 1);
     n_geo = n_shapes(type, geo_order);
     if (!n || !n_geo) return false;
@@ -845,13 +853,13 @@ struct OracleFE {
   // recomputed for every element (fe.C:174-192 re-inits when the cached
   // element does not match).
   void orient(const std::vector<Pt> &X) {
-    if (!(family == 1 && order == 3)) return;
+    if (!(family == 1 && ((order == 3 && (type == HEX27 || type == TET14)) || (order == 2 && type == HEX27)))) return;
     const bool tet = type == TET14;
     for (int q = 0; q < nq; ++q)
       for (int i = 0; i < n; ++i) {
-        phi[i][q] = tet ? hier_tet3_shape(X, i, qp[q]) : hier_hex3_shape(X, i, qp[q]);
+        phi[i][q] = tet ? hier_tet3_shape(X, i, qp[q]) : hier_hexo_shape(X, order, i, qp[q]);
         for (int c = 0; c < 3; ++c)
-          dref[c][i][q] = tet ? hier_tet3_deriv(X, i, c, qp[q]) : hier_hex3_deriv(X, i, c, qp[q]);
+          dref[c][i][q] = tet ? hier_tet3_deriv(X, i, c, qp[q]) : hier_hexo_deriv(X, order, i, c, qp[q]);
       }
   }
 
@@ -1177,6 +1185,25 @@ int orc_shapes_hier3(const double *X27, int np, const double *pts, double *phi, 
     }
   }
   return 64;
+}
+
+// HIERARCHIC shapes of one HEX27 (node coordinates X27 [27][3]) at order 2
+// or 3 with the element's edge and face orientation: phi [n][np], dphi
+// [3][n][np], n = (order + 1)^3.
+int orc_shapes_hier_hex(const double *X27, int order, int np, const double *pts, double *phi, double *dphi) {
+  if (order < 2 || order > 3) return -1;
+  std::vector<Pt> X(27);
+  for (int a = 0; a < 27; ++a)
+    for (int d = 0; d < 3; ++d) X[a].v[d] = X27[3 * a + d];
+  const int n = (order + 1) * (order + 1) * (order + 1);
+  for (int q = 0; q < np; ++q) {
+    const Pt p = {{pts[3 * q], pts[3 * q + 1], pts[3 * q + 2]}};
+    for (int i = 0; i < n; ++i) {
+      phi[i * np + q] = hier_hexo_shape(X, (unsigned)order, i, p);
+      for (int c = 0; c < 3; ++c) dphi[(c * n + i) * np + q] = hier_hexo_deriv(X, (unsigned)order, i, c, p);
+    }
+  }
+  return n;
 }
 
 // Cubic HIERARCHIC shapes of one TET14 (node coordinates X14 [14][3]).

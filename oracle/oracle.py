@@ -33,6 +33,8 @@ def lib():
         _lib.orc_distribute_dofs_hier3.argtypes = [i64, i64, v, v, C.POINTER(i64)]
         _lib.orc_dirichlet_hier3.argtypes = [i64, v, v, v, i32, v]
         _lib.orc_shapes_tet3.argtypes = [v, i32, v, v, v]
+        _lib.orc_shapes_hier_hex.argtypes = [v, i32, i32, v, v, v]
+        _lib.orc_shapes_hier_hex.restype = C.c_int32
         _lib.orc_distribute_dofs_tet3.argtypes = [i64, i64, v, v, C.POINTER(i64)]
         _lib.orc_dirichlet_tet3.argtypes = [i64, v, v, v, i32, v]
         _lib.orc_mesh_cube.argtypes = [i32, i32, i32, i32, f64, C.c_uint64]
@@ -131,6 +133,18 @@ def dirichlet_hier3(elem_dofs, side_bid, bids, n_dofs):
     lib().orc_dirichlet_hier3(elem_dofs.shape[0], _p(np.ascontiguousarray(elem_dofs, np.int32)),
                               _p(np.ascontiguousarray(side_bid, np.int8)), _p(bids), len(bids), _p(c))
     return c
+
+
+def shapes_hier_hex(X27, order, pts):
+    """HIERARCHIC shapes of order 2 or 3 of one HEX27 (node coordinates X27
+    [27][3]) with its edge and face orientation: phi [n][np], dphi [3][n][np]."""
+    pts = np.ascontiguousarray(pts, np.float64)
+    n = (order + 1) ** 3
+    phi = np.zeros((n, len(pts)))
+    dphi = np.zeros((3, n, len(pts)))
+    assert lib().orc_shapes_hier_hex(_p(np.ascontiguousarray(X27, np.float64)), order, len(pts), _p(pts), _p(phi),
+                                     _p(dphi)) == n
+    return phi, dphi
 
 
 def shapes_tet3(X14, pts):
