@@ -453,6 +453,77 @@ def run_adjoint(args, local):
         "e2e_note": "host timers around the public calls; u, z, q and the gradient cross the host boundary"}))
 
 
+def run_curved(args, local):
+    """Secondary workload: the headline elasticity problem with every TET10
+    non-affine (mid-edge nodes moved off their edges by up to 0.02 h), so every
+    element takes the reference's per-point form.  Times the FP64 drop-in and
+    the mixed form with the per-point Gram products on the tensor cores and on
+    the CUDA cores."""
+    import torch
+    import libmesh_gb300 as lm
+    torch.cuda.set_device(local)
+    mesh, dm, E, f = build_problem(args.n)
+    rng = np.random.default_rng(11)
+    mid = np.unique(mesh.conn[:, 4:])
+    xyz = mesh.xyz.copy()
+    inner = ~((xyz[mid] == 0) | (xyz[mid] == 1)).any(1)
+    xyz[mid[inner]] += rng.uniform(-0.02, 0.02, (inner.sum(), 3)) / args.n
+    mesh.xyz = xyz
+    asm = lm.GpuAssembly(lm.ELASTICITY, 2, 4, elem_coef=E, nodal_f=f, nu=0.3, device=local)
+    asm.init(mesh, dm)
+    stream = torch.cuda.current_stream()
+    asm.set_stream(stream.cuda_stream)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def timed(prec, tc=True):
+        asm.set_tensor_cores(tc)
+        for _ in range(max(3, args.warmup)):
+            asm.assemble_device(prec)
+        asm.synchronize()
+        ev0.record(stream)
+        for _ in range(args.steps):
+            asm.assemble_device(prec)
+        ev1.record(stream)
+        ev1.synchronize()
+        asm.synchronize()
+        return ev0.elapsed_time(ev1) / args.steps
+
+    clocks = Clocks(local)
+    clocks.start()
+    ms64 = timed(lm.FP64)
+    clk = clocks.stop()
+    ms_tc = timed(lm.MIXED, True)
+    ms_cc = timed(lm.MIXED, False)
+    Ks = {}
+    for name, prec, tc in (("fp64", lm.FP64, True), ("tc", lm.MIXED, True), ("cc", lm.MIXED, False)):
+        asm.set_tensor_cores(tc)
+        Kd = torch.empty(asm.nnz, dtype=torch.float64, device="cuda")
+        Fd = torch.empty(dm.n_dofs, dtype=torch.float64, device="cuda")
+        asm.assemble_device(prec, Kd.data_ptr(), Fd.data_ptr())
+        asm.synchronize()
+        Ks[name] = Kd
+    asm.perflog_enable(True)
+    asm.set_tensor_cores(True)
+    for _ in range(5):
+        asm.assemble_device(lm.MIXED)
+    el_ms, ga_ms, calls = asm.perflog_read()
+    asm.close()
+    n_el = mesh.n_elem
+    rk = lambda a: float(torch.linalg.norm(Ks[a] - Ks["fp64"]) / torch.linalg.norm(Ks["fp64"]))  # noqa: E731
+    print(json.dumps({
+        "metric": METRIC, "value": n_el / (ms64 * 1e-3) / 1e6, "unit": "Melem/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms64, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic (seeded mesh jitter, mid-edge offsets, E_e, f)",
+        "config": {"workload": "elasticity TET10 build_cube %d^3 x6 tets, mid-edge nodes moved (every element "
+                               "non-affine), QGauss FOURTH" % args.n, "n_elem": n_el, "n_dofs": dm.n_dofs},
+        "clocks": clk,
+        "mixed_tensor_cores": {"ms_per_step": ms_tc, "value": n_el / (ms_tc * 1e-3) / 1e6,
+                               "speedup_vs_fp64": ms64 / ms_tc, "k_rel_frobenius_vs_fp64": rk("tc"),
+                               "stages_ms": {"elements": el_ms / calls, "insertion": ga_ms / calls}},
+        "mixed_cuda_cores": {"ms_per_step": ms_cc, "value": n_el / (ms_cc * 1e-3) / 1e6,
+                             "speedup_vs_fp64": ms64 / ms_cc, "k_rel_frobenius_vs_fp64": rk("cc")}}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -463,9 +534,11 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
     ap.add_argument("--n", type=int, default=N_CUBE, help="cube divisions (48 = the headline mesh)")
     ap.add_argument("--no-mixed", action="store_true", help="skip timing the mixed form beside FP64")
-    ap.add_argument("--workload", default="elasticity", choices=["elasticity", "amr-cd", "batch", "adjoint"],
+    ap.add_argument("--workload", default="elasticity",
+                    choices=["elasticity", "amr-cd", "batch", "adjoint", "curved"],
                     help="elasticity = the headline; amr-cd = refined HEX27 convection-diffusion; "
-                         "batch = many mixed systems as one CUDA graph; adjoint = 128^3 sensitivities")
+                         "batch = many mixed systems as one CUDA graph; adjoint = 128^3 sensitivities; "
+                         "curved = the headline mesh with every element non-affine")
     ap.add_argument("--meshes", type=int, default=64, help="systems in the batch workload")
     ap.add_argument("--max-elems", type=float, default=5e4,
                     help="largest system of the batch workload (2e5 with --meshes 256 is the full config-4 mix)")
@@ -475,10 +548,11 @@ def main():
     local = int(os.environ.get("LOCAL_RANK", 0))
     if args.impl == "reference":
         return run_reference(args, rank)
-    if args.workload in ("amr-cd", "batch", "adjoint"):
+    if args.workload in ("amr-cd", "batch", "adjoint", "curved"):
         from libmesh_gb300 import _build
         _build.build()
-        return {"amr-cd": run_amr, "batch": run_batch, "adjoint": run_adjoint}[args.workload](args, local)
+        return {"amr-cd": run_amr, "batch": run_batch, "adjoint": run_adjoint,
+                "curved": run_curved}[args.workload](args, local)
 
     import torch
     import libmesh_gb300 as lm

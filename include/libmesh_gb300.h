@@ -350,6 +350,15 @@ lmg_status lmg_last_error(lmg_ctx *ctx, int64_t *elem_id, char *msg, int32_t msg
 lmg_status lmg_perflog_enable(lmg_ctx *ctx, int32_t on);
 lmg_status lmg_perflog_read(lmg_ctx *ctx, double *elements_ms, double *gather_ms, int64_t *calls);
 
+/* Mixed form on non-affine elements (the reference's per-point form, where
+ * the affine reference-tensor shortcut does not apply): with on = 1 (the
+ * default) the per-point products sum_q JxW B_q^T D B_q run as Gram products
+ * E^T E on the tensor cores (tcgen05, BF16 three-way split, FP32 accumulation;
+ * TET4 / TET10 elasticity, TET10 / HEX8 Poisson), with on = 0 on the CUDA
+ * cores in FP32.  Same weak form (systems_of_equations_ex6.C:222-230,
+ * introduction_ex4.C:467); the FP64 drop-in is unaffected. */
+lmg_status lmg_context_set_tensor_cores(lmg_ctx *ctx, int32_t on);
+
 /* Element-kernel grid of this context in CTAs per SM (0 = default 32); the
  * batch autotuner sets it. */
 lmg_status lmg_context_set_grid(lmg_ctx *ctx, int32_t ctas_per_sm);

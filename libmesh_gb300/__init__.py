@@ -288,6 +288,11 @@ class GpuAssembly:
                                    ptr(np.ascontiguousarray(z, np.float64)), ptr(reg), ptr(g)))
         return g
 
+    def set_tensor_cores(self, on=True):
+        """Mixed form on non-affine elements: per-point Gram products on the
+        tensor cores (default) or on the CUDA cores."""
+        self._ok(lib().lmg_context_set_tensor_cores(self.ctx, 1 if on else 0))
+
     def perflog_enable(self, on=True):
         self._ok(lib().lmg_perflog_enable(self.ctx, 1 if on else 0))
 

@@ -66,6 +66,7 @@ SIGNATURES = {
     "lmg_vjp_coef": [_p, _p, _p, _p],
     "lmg_residual": [_p, _p, _p, _i32],
     "lmg_vjp_xyz": [_p, _p, _p, _p, _p],
+    "lmg_context_set_tensor_cores": [_p, _i32],
     "lmg_perflog_enable": [_p, _i32],
     "lmg_perflog_read": [_p, _pf64, _pf64, _pi64],
     "lmg_launch_count": [_p, _pi64],

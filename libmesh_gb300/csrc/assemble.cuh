@@ -133,6 +133,12 @@ bool launch_residual(int form, int n, int nv, const ElemArgs &a, int64_t n_brows
                      const int32_t *fcontrib, double *R, int grid, cudaStream_t s);
 void launch_elements(int form, int n, int nv, bool affine, bool mixed, const ElemArgs &a, int grid,
                      cudaStream_t s);
+// Mixed-form element matrices of any (affine or not) elements as per-point
+// Gram products E^T E on the tensor cores (tc.cu): built for (form, shapes per
+// variable, variables, quadrature points) when tc_built says so; writes the
+// strictly upper blocks to Koff32 and the FP64 path's load vector to Fe2.
+bool tc_built(int form, int n, int nv, int q);
+bool launch_elements_tc(int form, int n, int nv, int q, const ElemArgs &a, int n_sm, cudaStream_t s);
 bool gather_built(int bs);
 // PCG (Jacobi) on a CSR matrix; returns 0 on success, 7 out of memory, 2 CUDA error.
 int cg_solve(int64_t n, const int32_t *rp, const int32_t *col, const double *val, const double *b, double *x,

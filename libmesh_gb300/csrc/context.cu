@@ -1013,7 +1013,10 @@ lmg_status lmg_assemble(lmg_ctx *c, int32_t precision, double *K, double *F, int
       ElemArgs aa = a;
       aa.n_list = cnt;
       aa.list = c->d_gen + off;
-      launch_elements(c->form, c->tab.n, c->n_vars, false, mixed, aa, grid, c->stream);
+      // mixed form: the per-point B^T D B products on the tensor cores where built
+      if (!(mixed && c->tensor_cores && tc_built(c->form, c->tab.n, c->n_vars, c->tab.q) &&
+            launch_elements_tc(c->form, c->tab.n, c->n_vars, c->tab.q, aa, c->n_sm, c->stream)))
+        launch_elements(c->form, c->tab.n, c->n_vars, false, mixed, aa, grid, c->stream);
       c->launches++;
     }
   };
@@ -1291,6 +1294,12 @@ lmg_status lmg_cg_solve(lmg_ctx *c, const double *rhs, double *x, double rtol, i
   if (st) return fail(c, st == 7 ? LMG_ERR_OOM : LMG_ERR_CUDA, "cg_solve: device failure");
   if (iters) *iters = it;
   if (relres) *relres = rr;
+  return LMG_OK;
+}
+
+lmg_status lmg_context_set_tensor_cores(lmg_ctx *c, int32_t on) {
+  if (!c) return LMG_ERR_ARG;
+  c->tensor_cores = on != 0;
   return LMG_OK;
 }
 
