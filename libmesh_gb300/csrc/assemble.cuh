@@ -138,7 +138,10 @@ void launch_elements(int form, int n, int nv, bool affine, bool mixed, const Ele
 // variable, variables, quadrature points) when tc_built says so; writes the
 // strictly upper blocks to Koff32 and the FP64 path's load vector to Fe2.
 bool tc_built(int form, int n, int nv, int q);
-bool launch_elements_tc(int form, int n, int nv, int q, const ElemArgs &a, int n_sm, cudaStream_t s);
+// neg_weights: the rule's first point has a negative weight (Keast's 11-point
+// rule); a rule with a negative weight elsewhere is not built
+bool launch_elements_tc(int form, int n, int nv, int q, bool neg_weights, const ElemArgs &a, int n_sm,
+                        cudaStream_t s);
 bool gather_built(int bs);
 // PCG (Jacobi) on a CSR matrix; returns 0 on success, 7 out of memory, 2 CUDA error.
 int cg_solve(int64_t n, const int32_t *rp, const int32_t *col, const double *val, const double *b, double *x,

@@ -1014,8 +1014,10 @@ lmg_status lmg_assemble(lmg_ctx *c, int32_t precision, double *K, double *F, int
       aa.n_list = cnt;
       aa.list = c->d_gen + off;
       // mixed form: the per-point B^T D B products on the tensor cores where built
-      if (!(mixed && c->tensor_cores && tc_built(c->form, c->tab.n, c->n_vars, c->tab.q) &&
-            launch_elements_tc(c->form, c->tab.n, c->n_vars, c->tab.q, aa, c->n_sm, c->stream)))
+      const bool later_neg = std::any_of(c->tab.qw.begin() + 1, c->tab.qw.end(), [](double x) { return x < 0.0; });
+      if (!(mixed && c->tensor_cores && !later_neg && tc_built(c->form, c->tab.n, c->n_vars, c->tab.q) &&
+            launch_elements_tc(c->form, c->tab.n, c->n_vars, c->tab.q, c->tab.qw[0] < 0.0, aa, c->n_sm,
+                               c->stream)))
         launch_elements(c->form, c->tab.n, c->n_vars, false, mixed, aa, grid, c->stream);
       c->launches++;
     }

@@ -11,8 +11,11 @@
 //     + d_l phi_a d_ij) for (j, l) = (0,1), (0,2), (1,2) (shear strains);
 //   Poisson (R = 3): sqrt(k JxW) d_j phi_a.
 // Summed over the R rows this is exactly the reference's integrand, so Ke =
-// E^T E is one GEMM per element with K = Q R (77 for TET10 with Keast's 11
-// points).  That is what runs here, for the elements the reference-tensor
+// E^T S E is one GEMM per element with K = Q R (77 for TET10 with Keast's 11
+// points), S = diag(sign w_q) on each point's rows: a rule with a negative
+// weight at its first point (Keast's centre point, -0.01315...) enters with
+// sqrt(|w_q| detJ), and the first 16-wide K slab of the B operand, which holds
+// that point's rows, is a separate copy with those rows negated.  That is what runs here, for the elements the reference-tensor
 // shortcut does not cover (non-affine maps, libMesh's compute_map branch).
 //
 // A CTA (4 warps) takes 4 elements per tile.  Warp w builds element w's E:
@@ -67,14 +70,22 @@ struct TcShape {
   static constexpr int KG = KD / 8;                          // core matrices along K
   static constexpr int NO = N * (N - 1) / 2, B2 = NV * NV;
   static constexpr size_t PIECE = (size_t)128 * KD * 2;      // one 128 x KD BF16 tile
-  static constexpr size_t DPHI = 3 * PIECE;                  // [Q][N][3] float
-  static constexpr size_t PHI = (DPHI + sizeof(float) * Q * N * 3 + 15) & ~(size_t)15;  // [Q][N] double
-  static constexpr size_t WARP0 = PHI + sizeof(double) * Q * N;
-  // per warp: X [N][3] double, f [N][NV] double, JxW [Q] double, G [Q][9] float, scales [Q][3] float
-  static constexpr size_t PER_WARP = ((sizeof(double) * (N * 3 + N * NV + Q) + sizeof(float) * Q * 12) + 15) & ~(size_t)15;
+  static constexpr size_t SLAB = (size_t)128 * 16 * 2;       // one 128 x 16 BF16 slab (one K step)
+  static_assert(R <= 16, "the first point's rows fit the first K step");
+  // dynamic shared memory: the three pieces of E, then (signed rules) the
+  // three signed slabs of the first K step, then the tables and per-warp data;
+  // npc = 3 or 6 (with the slabs)
+  __host__ __device__ static size_t dphi(int npc) { return 3 * PIECE + (npc > 3 ? 3 * SLAB : 0); }  // [Q][N][3] float
+  __host__ __device__ static size_t phi(int npc) { return (dphi(npc) + sizeof(float) * Q * N * 3 + 15) & ~(size_t)15; }  // [Q][N] double
+  __host__ __device__ static size_t warp0(int npc) { return phi(npc) + sizeof(double) * Q * N; }
+  // per warp: X [N][3] double, f [N][NV] double, JxW [Q] double, G [Q][9] float, scales and sign [Q][4] float
+  static constexpr size_t PER_WARP = ((sizeof(double) * (N * 3 + N * NV + Q) + sizeof(float) * Q * 13) + 15) & ~(size_t)15;
   // at least 60 KB, so that no more than three CTAs share an SM and their
   // accumulators (128 tensor-memory columns each) fit the SM's 512 columns
-  static constexpr size_t BYTES = (WARP0 + 4 * PER_WARP) > 61440 ? (WARP0 + 4 * PER_WARP) : 61440;
+  __host__ __device__ static size_t bytes(int npc) {
+    const size_t b = warp0(npc) + 4 * PER_WARP;
+    return b > 61440 ? b : 61440;
+  }
   static_assert(NCOL <= 32, "one warp lane per element dof");
   static_assert(PIECE % 1024 == 0, "tiles keep the 1 KB alignment");
 };
@@ -84,24 +95,27 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
   return (uint32_t)__bfloat16_as_ushort(a) | ((uint32_t)__bfloat16_as_ushort(b) << 16);
 }
 
+// is_signed: the rule's first point has a negative weight (and no other
+// point has); the B operand's first K step then reads the signed slabs.
 template <int FORM, int N, int NV, int Q>
-__global__ void __launch_bounds__(128) k_elem_tc(ElemArgs a) {
+__global__ void __launch_bounds__(128) k_elem_tc(ElemArgs a, int is_signed) {
   using S = TcShape<FORM, N, NV, Q>;
   extern __shared__ __align__(1024) unsigned char tsm[];
   __shared__ __align__(8) uint64_t mbar;
   __shared__ uint32_t tmem_base;
   const int t = threadIdx.x, w = t >> 5, lane = t & 31;
-  float *sdphi = reinterpret_cast<float *>(tsm + S::DPHI);
-  double *sphi = reinterpret_cast<double *>(tsm + S::PHI);
-  unsigned char *wb = tsm + S::WARP0 + S::PER_WARP * w;
+  const int npc = is_signed ? 6 : 3;
+  float *sdphi = reinterpret_cast<float *>(tsm + S::dphi(npc));
+  double *sphi = reinterpret_cast<double *>(tsm + S::phi(npc));
+  unsigned char *wb = tsm + S::warp0(npc) + S::PER_WARP * w;
   double *sX = reinterpret_cast<double *>(wb);
   double *sF = sX + N * 3;
   double *sJxW = sF + N * NV;
   float *sG = reinterpret_cast<float *>(sJxW + Q);
-  float *sSc = sG + Q * 9;
+  float *sSc = sG + Q * 9;  // [Q][4]: row scales and the sign of the weight
   for (int i = t; i < Q * N * 3; i += blockDim.x) sdphi[i] = (float)a.fe.dphi[i];
   for (int i = t; i < Q * N; i += blockDim.x) sphi[i] = a.fe.phi[i];
-  for (size_t i = t; i < 3 * S::PIECE / 16; i += blockDim.x) reinterpret_cast<uint4 *>(tsm)[i] = make_uint4(0, 0, 0, 0);
+  for (size_t i = t; i < S::dphi(npc) / 16; i += blockDim.x) reinterpret_cast<uint4 *>(tsm)[i] = make_uint4(0, 0, 0, 0);
   if (w == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base)),
                  "r"(128));
@@ -142,13 +156,15 @@ __global__ void __launch_bounds__(128) k_elem_tc(ElemArgs a) {
         sJxW[q] = jxw;
 #pragma unroll
         for (int i = 0; i < 9; ++i) sG[q * 9 + i] = (float)G[i];
+        const double aj = fabs(jxw);  // detJ > 0: the sign is the weight's
         if (FORM == LMG_ELASTICITY) {
-          sSc[q * 3 + 0] = (float)sqrt(fmax(lam * jxw, 0.0));
-          sSc[q * 3 + 1] = (float)sqrt(fmax(2.0 * mu * jxw, 0.0));
-          sSc[q * 3 + 2] = (float)sqrt(fmax(mu * jxw, 0.0));
+          sSc[q * 4 + 0] = (float)sqrt(lam * aj);
+          sSc[q * 4 + 1] = (float)sqrt(2.0 * mu * aj);
+          sSc[q * 4 + 2] = (float)sqrt(mu * aj);
         } else {
-          sSc[q * 3] = (float)sqrt(fmax(coef * jxw, 0.0));
+          sSc[q * 4] = (float)sqrt(coef * aj);
         }
+        sSc[q * 4 + 3] = jxw < 0.0 ? -1.f : 1.f;
       }
     }
     __syncwarp();
@@ -166,7 +182,7 @@ __global__ void __launch_bounds__(128) k_elem_tc(ElemArgs a) {
 #pragma unroll
         for (int j = 0; j < 3; ++j) g[j] = fmaf(dh[0], G[j], fmaf(dh[1], G[3 + j], dh[2] * G[6 + j]));
         if (FORM == LMG_ELASTICITY) {
-          const float sl = sSc[q * 3], sd = sSc[q * 3 + 1], so = sSc[q * 3 + 2];
+          const float sl = sSc[q * 4], sd = sSc[q * 4 + 1], so = sSc[q * 4 + 2];
           float *r = col + q * 7;
           r[0] = sl * g[i];
           r[1] = i == 0 ? sd * g[0] : 0.f;
@@ -176,7 +192,7 @@ __global__ void __launch_bounds__(128) k_elem_tc(ElemArgs a) {
           r[5] = i == 0 ? so * g[2] : (i == 2 ? so * g[0] : 0.f);
           r[6] = i == 1 ? so * g[2] : (i == 2 ? so * g[1] : 0.f);
         } else {
-          const float s = sSc[q * 3];
+          const float s = sSc[q * 4];
           col[q * 3] = s * g[0];
           col[q * 3 + 1] = s * g[1];
           col[q * 3 + 2] = s * g[2];
@@ -206,6 +222,19 @@ __global__ void __launch_bounds__(128) k_elem_tc(ElemArgs a) {
         for (int pc = 0; pc < 3; ++pc)
           *reinterpret_cast<uint4 *>(tsm + pc * S::PIECE + roff + (size_t)kg * 128) =
               make_uint4(p[pc][0], p[pc][1], p[pc][2], p[pc][3]);
+        if (is_signed && kg < 2) {  // B's first K step: sign bit flipped on the first point's rows (k < R)
+          uint32_t neg[4];
+#pragma unroll
+          for (int h = 0; h < 4; ++h) {
+            const int k0 = kg * 8 + 2 * h;
+            neg[h] = (k0 < S::R ? 0x8000u : 0u) | (k0 + 1 < S::R ? 0x80000000u : 0u);
+          }
+          const size_t soff = (size_t)(row >> 3) * 256 + (size_t)(row & 7) * 16 + (size_t)kg * 128;
+#pragma unroll
+          for (int pc = 0; pc < 3; ++pc)
+            *reinterpret_cast<uint4 *>(tsm + 3 * S::PIECE + pc * S::SLAB + soff) =
+                make_uint4(p[pc][0] ^ neg[0], p[pc][1] ^ neg[1], p[pc][2] ^ neg[2], p[pc][3] ^ neg[3]);
+        }
       }
     }
     // load vector, FP64, exactly as the FP64 path forms it
@@ -235,7 +264,9 @@ __global__ void __launch_bounds__(128) k_elem_tc(ElemArgs a) {
 #pragma unroll
         for (int pr = 0; pr < 6; ++pr) {
           const uint64_t da = umma_desc(base + PA[pr] * (uint32_t)S::PIECE + ks * 256, 128, sbo);
-          const uint64_t db = umma_desc(base + PB[pr] * (uint32_t)S::PIECE + ks * 256, 128, sbo);
+          const uint64_t db =
+              (is_signed && ks == 0) ? umma_desc(base + 3 * (uint32_t)S::PIECE + PB[pr] * (uint32_t)S::SLAB, 128, 256)
+                                     : umma_desc(base + PB[pr] * (uint32_t)S::PIECE + ks * 256, 128, sbo);
           const uint32_t acc = (ks > 0 || pr > 0) ? 1u : 0u;
           asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
                        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
@@ -286,17 +317,18 @@ __global__ void __launch_bounds__(128) k_elem_tc(ElemArgs a) {
 }
 
 template <int FORM, int N, int NV, int Q>
-void launch_tc_t(const ElemArgs &a, int n_sm, cudaStream_t s) {
+void launch_tc_t(const ElemArgs &a, bool is_signed, int n_sm, cudaStream_t s) {
   using S = TcShape<FORM, N, NV, Q>;
-  static bool attr = false;  // set once, before any stream capture of this launch
-  if (!attr) {
-    cudaFuncSetAttribute(k_elem_tc<FORM, N, NV, Q>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::BYTES);
-    attr = true;
+  const size_t bytes = S::bytes(is_signed ? 6 : 3);
+  static size_t attr = 0;  // largest dynamic shared memory granted so far
+  if (bytes > attr) {
+    cudaFuncSetAttribute(k_elem_tc<FORM, N, NV, Q>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    attr = bytes;
   }
   const int64_t tiles = (a.n_list + 3) / 4;
-  const int64_t cap = (int64_t)n_sm * 3;  // three CTAs per SM (shared memory and tensor memory allow it)
+  const int64_t cap = (int64_t)n_sm * 3;  // at most three CTAs per SM (shared memory and tensor memory)
   const int g = (int)(tiles < cap ? tiles : cap);
-  if (g > 0) k_elem_tc<FORM, N, NV, Q><<<g, 128, S::BYTES, s>>>(a);
+  if (g > 0) k_elem_tc<FORM, N, NV, Q><<<g, 128, bytes, s>>>(a, is_signed ? 1 : 0);
 }
 
 }  // namespace
@@ -308,12 +340,13 @@ bool tc_built(int form, int n, int nv, int q) {
          (form == LMG_POISSON && n == 8 && nv == 1 && q == 8);
 }
 
-bool launch_elements_tc(int form, int n, int nv, int q, const ElemArgs &a, int n_sm, cudaStream_t s) {
+bool launch_elements_tc(int form, int n, int nv, int q, bool neg_weights, const ElemArgs &a, int n_sm,
+                        cudaStream_t s) {
   if (a.n_list <= 0) return true;
-#define LMG_TC(F, NN, V, QQ)                         \
-  if (form == F && n == NN && nv == V && q == QQ) {  \
-    launch_tc_t<F, NN, V, QQ>(a, n_sm, s);           \
-    return true;                                     \
+#define LMG_TC(F, NN, V, QQ)                              \
+  if (form == F && n == NN && nv == V && q == QQ) {       \
+    launch_tc_t<F, NN, V, QQ>(a, neg_weights, n_sm, s);   \
+    return true;                                          \
   }
   LMG_TC(LMG_ELASTICITY, 10, 3, 11)
   LMG_TC(LMG_ELASTICITY, 4, 3, 4)
