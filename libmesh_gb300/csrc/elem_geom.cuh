@@ -74,18 +74,29 @@ __device__ __forceinline__ void lame(double E, double nu, double &lam, double &m
   mu = E / (2. * (1. + nu));
 }
 
-// Load-vector contribution of quadrature point q to local shape a:
-// f(x_q) = sum_b phi_b(q) f_b (the FE interpolation of the nodal load), then
-// facc += JxW_q f(x_q) phi_a(q), per variable, with explicit fused
-// multiply-adds.  ph = phi at q [N], f = nodal load [N][NV].
-template <int N, int NV>
-__device__ __forceinline__ void load_qp(const double *ph, const double *f, double jxw, int a, double *facc) {
-#pragma unroll
-  for (int v = 0; v < NV; ++v) {
-    double fq = 0.0;
-    for (int b = 0; b < N; ++b) fq = fma(ph[b], f[b * NV + v], fq);
-    facc[v] = fma(jxw * fq, ph[a], facc[v]);
+// Load vector of one element, F_a^v = sum_q (JxW_q f^v(x_q)) phi_a(q) with
+// f^v(x_q) = sum_b phi_b(q) f_b^v (the FE interpolation of the nodal load),
+// both sums in order with explicit fused multiply-adds, by one warp: first
+// lane (q, v) forms f^v(x_q) into fq [Q][NV], then lane (a, v) the sum over q.
+// ph = phi [Q][N], f = nodal load [N][NV], jxw [Q] (stride jstride), fq scratch
+// [Q][NV]; out(a, v, value) receives each entry.
+template <int N, int NV, typename Out>
+__device__ __forceinline__ void element_load(const double *ph, const double *f, const double *jxw, int jstride, int Q,
+                                             double *fq, int lane, Out &&out) {
+  for (int idx = lane; idx < Q * NV; idx += 32) {
+    const int q = idx / NV, v = idx - q * NV;
+    double s = 0.0;
+    for (int b = 0; b < N; ++b) s = fma(ph[q * N + b], f[b * NV + v], s);
+    fq[idx] = s;
   }
+  __syncwarp();
+  for (int idx = lane; idx < N * NV; idx += 32) {
+    const int a = idx / NV, v = idx - a * NV;
+    double acc = 0.0;
+    for (int q = 0; q < Q; ++q) acc = fma(jxw[q * jstride] * fq[q * NV + v], ph[q * N + a], acc);
+    out(a, v, acc);
+  }
+  __syncwarp();
 }
 
 }  // namespace lmg

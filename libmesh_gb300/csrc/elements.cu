@@ -474,6 +474,7 @@ __global__ void __launch_bounds__(128) k_elem_general(ElemArgs a) {
   __shared__ double sGeo[4][MAXQ][10];  // G (9) and JxW per qp
   __shared__ double sGr[4][N * 3];      // physical gradients at the current qp
   __shared__ double sF[4][N * NV];      // nodal load of the element
+  __shared__ double sFq[4][MAXQ * NV];  // the load at every point
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int Q = a.fe.q;
   for (int64_t li = (int64_t)blockIdx.x * 4 + warp; li < a.n_list; li += (int64_t)gridDim.x * 4) {
@@ -499,9 +500,6 @@ __global__ void __launch_bounds__(128) k_elem_general(ElemArgs a) {
     for (int k = 0; k < BPL; ++k)
 #pragma unroll
       for (int ik = 0; ik < B2; ++ik) acc[k][ik] = 0;
-    double facc[NV];
-#pragma unroll
-    for (int v = 0; v < NV; ++v) facc[v] = 0.0;
     for (int q = 0; q < Q; ++q) {
       const double *Gq = sGeo[warp][q];
       for (int i = lane; i < N * 3; i += 32) {
@@ -536,7 +534,7 @@ __global__ void __launch_bounds__(128) k_elem_general(ElemArgs a) {
           }
         }
       }
-      if (lane < N) load_qp<N, NV>(a.fe.phi + (int64_t)q * N, sF[warp], Gq[9], lane, facc);  // lane = shape a (FP64)
+
       __syncwarp();
     }
     const uint64_t mask = a.cmask[e];
@@ -559,14 +557,11 @@ __global__ void __launch_bounds__(128) k_elem_general(ElemArgs a) {
         }
       }
     }
-    if (lane < N) {
-#pragma unroll
-      for (int v = 0; v < NV; ++v) {
-        const DF s = df_split(((mask >> (v * N + lane)) & 1ull) ? 0.0 : facc[v]);
-        a.Fe2[((int64_t)e * N + lane) * NV + v] = make_float2(s.hi, s.lo);
-      }
-    }
-    __syncwarp();
+    // load vector in FP64 (element_load: lane (q, v), then lane (a, v))
+    element_load<N, NV>(a.fe.phi, sF[warp], &sGeo[warp][0][9], 10, Q, sFq[warp], lane, [&](int ai, int v, double f) {
+      const DF s = df_split(((mask >> (v * N + ai)) & 1ull) ? 0.0 : f);
+      a.Fe2[((int64_t)e * N + ai) * NV + v] = make_float2(s.hi, s.lo);
+    });
   }
 }
 

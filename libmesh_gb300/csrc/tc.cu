@@ -78,8 +78,10 @@ struct TcShape {
   __host__ __device__ static size_t dphi(int npc) { return 3 * PIECE + (npc > 3 ? 3 * SLAB : 0); }  // [Q][N][3] float
   __host__ __device__ static size_t phi(int npc) { return (dphi(npc) + sizeof(float) * Q * N * 3 + 15) & ~(size_t)15; }  // [Q][N] double
   __host__ __device__ static size_t warp0(int npc) { return phi(npc) + sizeof(double) * Q * N; }
-  // per warp: X [N][3] double, f [N][NV] double, JxW [Q] double, G [Q][9] float, scales and sign [Q][4] float
-  static constexpr size_t PER_WARP = ((sizeof(double) * (N * 3 + N * NV + Q) + sizeof(float) * Q * 13) + 15) & ~(size_t)15;
+  // per warp: X [N][3] double, f [N][NV] double, JxW [Q] double, load at the points [Q][NV] double,
+  // G [Q][9] float, scales and sign [Q][4] float
+  static constexpr size_t PER_WARP =
+      ((sizeof(double) * (N * 3 + N * NV + Q + Q * NV) + sizeof(float) * Q * 13) + 15) & ~(size_t)15;
   // at least 60 KB, so that no more than three CTAs share an SM and their
   // accumulators (128 tensor-memory columns each) fit the SM's 512 columns
   __host__ __device__ static size_t bytes(int npc) {
@@ -111,7 +113,8 @@ __global__ void __launch_bounds__(128) k_elem_tc(ElemArgs a, int is_signed) {
   double *sX = reinterpret_cast<double *>(wb);
   double *sF = sX + N * 3;
   double *sJxW = sF + N * NV;
-  float *sG = reinterpret_cast<float *>(sJxW + Q);
+  double *sFq = sJxW + Q;
+  float *sG = reinterpret_cast<float *>(sFq + Q * NV);
   float *sSc = sG + Q * 9;  // [Q][4]: row scales and the sign of the weight
   for (int i = t; i < Q * N * 3; i += blockDim.x) sdphi[i] = (float)a.fe.dphi[i];
   for (int i = t; i < Q * N; i += blockDim.x) sphi[i] = a.fe.phi[i];
@@ -238,17 +241,12 @@ __global__ void __launch_bounds__(128) k_elem_tc(ElemArgs a, int is_signed) {
       }
     }
     // load vector, FP64, exactly as the FP64 path forms it
-    if (e >= 0 && lane < N) {
-      double facc[NV];
-#pragma unroll
-      for (int v = 0; v < NV; ++v) facc[v] = 0.0;
-      for (int q = 0; q < Q; ++q) load_qp<N, NV>(sphi + q * N, sF, sJxW[q], lane, facc);
+    if (e >= 0) {
       const uint64_t mask = a.cmask[e];
-#pragma unroll
-      for (int v = 0; v < NV; ++v) {
-        const DF s = df_split(((mask >> (v * N + lane)) & 1ull) ? 0.0 : facc[v]);
-        a.Fe2[((int64_t)e * N + lane) * NV + v] = make_float2(s.hi, s.lo);
-      }
+      element_load<N, NV>(sphi, sF, sJxW, 1, Q, sFq, lane, [&](int ai, int v, double f) {
+        const DF s = df_split(((mask >> (v * N + ai)) & 1ull) ? 0.0 : f);
+        a.Fe2[((int64_t)e * N + ai) * NV + v] = make_float2(s.hi, s.lo);
+      });
     }
     // the tile's MMAs: generic-proxy stores made visible to the tensor core
     asm volatile("fence.proxy.async.shared::cta;");
