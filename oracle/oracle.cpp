@@ -677,6 +677,195 @@ double hier_tet3_deriv(const std::vector<Pt> &X, unsigned i, unsigned j, const P
   return (hier_tet3_shape(X, i, pp) - hier_tet3_shape(X, i, pm)) / 2. / eps;
 }
 
+// ------------------------------------------------ HIERARCHIC prisms, p = 2, 3
+// FE<3,HIERARCHIC>::shape on PRISM18 / PRISM20 / PRISM21
+// (fe_hierarchic_shape_3D.C:2290-2345): prism_indices (:764-1150) picks the
+// triangle index i01 and the 1-D index i2, remapping (xi, eta) and zeta for
+// the quadrilateral faces by the face's minimum vertex and
+// positive_face_orientation, and reflecting zeta on a vertical edge with
+// positive_edge_orientation; the value is the 2-D HIERARCHIC triangle shape
+// i01 (fe_hierarchic_shape_2D.C:965-1026, edge bases through
+// fe_triangle_helper :915-948, negated for odd orders when the triangle's
+// edge runs from the greater point) on a Tri3 built from vertices 0-2 or 3-5
+// (with the two nodes of an odd square-face basis's edge put in ascending
+// order), times the 1-D HIERARCHIC shape i2 of zeta.  Derivatives are central
+// differences, eps = 1e-6 (fe_fdm_deriv, fe.C:911-928).  Restated literally,
+// including face 2's first orientation case, which takes triangle basis
+// s0 + 1 + 3 where its other cases take s0 + 1 + e.
+namespace prism {
+const unsigned EDGE[9][2] = {{0, 1}, {1, 2}, {0, 2}, {0, 3}, {1, 4}, {2, 5}, {3, 4}, {4, 5}, {3, 5}};
+const unsigned SIDE[5][4] = {{0, 2, 1, 99}, {0, 1, 4, 3}, {1, 2, 5, 4}, {2, 0, 3, 5}, {3, 4, 5, 99}};
+const unsigned SQ_ROW[4] = {0, 1, 1, 0}, SQ_COL[4] = {0, 0, 1, 1};  // square_number_row / _column
+const unsigned TRI_ROW[1] = {0}, TRI_COL[1] = {0};                  // triangular_number_row / _column
+const unsigned PR_TRI[2] = {0, 0}, PR_PAGE[2] = {0, 1};             // prism_number_triangle / _page
+
+bool edge_positive(const std::vector<Pt> &X, unsigned e) { return pt_greater(X[EDGE[e][0]], X[EDGE[e][1]]); }
+
+bool face_positive(const std::vector<Pt> &X, unsigned s) {
+  const unsigned *nodes = SIDE[s];
+  const unsigned N = (s == 0 || s == 4) ? 3 : 4;
+  unsigned v = 0;
+  for (unsigned k = 1; k < N; ++k)
+    if (pt_less(X[nodes[k]], X[nodes[v]])) v = k;
+  return pt_less(X[nodes[(v + N - 1) % N]], X[nodes[(v + 1) % N]]);
+}
+
+void indices(const std::vector<Pt> &X, unsigned totalorder, unsigned i, double &xi, double &eta, double &zeta,
+             unsigned &i01, unsigned &i2) {
+  const unsigned e = totalorder - 1u;
+  const double xs = xi, es = eta, zs = zeta;
+  if (i < 6) {
+    i01 = i % 3;
+    i2 = i / 3;
+  } else if (i < 6 + 3 * e) {
+    i01 = i - 3;
+    i2 = 0;
+  } else if (i < 6 + 6 * e) {
+    i01 = (i - 6 - 3 * e) / e;
+    i2 = (i - 6 - 3 * e) % e + 2;
+    if (edge_positive(X, i01 + 3)) zeta = -zeta;
+  } else if (i < 6 + 9 * e) {
+    i01 = i - 3 - 6 * e;
+    i2 = 1;
+  } else if (i < 6 + 9 * e + e * e) {  // face 1
+    const unsigned b = i - 6 - 9 * e;
+    const double xe_scale = 1 - es;
+    const double xe_fraction = (xe_scale == 0) ? 0 : xs / xe_scale;
+    const unsigned s0 = SQ_ROW[b] + 2, s1 = SQ_COL[b] + 2;
+    const Pt mp = min_point(X, 0, 1, 3, 4);
+    const bool pos = face_positive(X, 1);
+    if (pt_eq(X[0], mp)) {
+      if (!pos) { i01 = s0 + 1; i2 = s1; }
+      else { i01 = s1 + 1; i2 = s0; zeta = 2 * xe_fraction - 1; xi = (zs + 1) * xe_scale / 2; }
+    } else if (pt_eq(X[3], mp)) {
+      if (!pos) { i01 = s1 + 1; i2 = s0; zeta = 1 - 2 * xe_fraction; xi = (zs + 1) * xe_scale / 2; }
+      else { i01 = s0 + 1; i2 = s1; zeta = -zs; }
+    } else if (pt_eq(X[1], mp)) {
+      if (!pos) { i01 = s1 + 1; i2 = s0; zeta = 2 * xe_fraction - 1; xi = (1 - zs) * xe_scale / 2; }
+      else { i01 = s0 + 1; i2 = s1; xi = (1 - xe_fraction) * xe_scale; }
+    } else if (pt_eq(X[4], mp)) {
+      if (!pos) { i01 = s0 + 1; i2 = s1; xi = (1 - xe_fraction) * xe_scale; zeta = -zs; }
+      else { i01 = s1 + 1; i2 = s0; zeta = 1 - 2 * xe_fraction; xi = (1 - zs) * xe_scale / 2; }
+    }
+  } else if (i < 6 + 9 * e + 2 * e * e) {  // face 2
+    const unsigned b = i - 6 - 9 * e - e * e;
+    const double xe_scale = xs + es;
+    const double xe_fraction = (xe_scale == 0) ? 0 : xs / xe_scale;
+    const unsigned s0 = SQ_ROW[b] + 2, s1 = SQ_COL[b] + 2;
+    const Pt mp = min_point(X, 1, 2, 4, 5);
+    const bool pos = face_positive(X, 2);
+    auto set_xe = [&](double xe) {
+      eta = xe * xe_scale;
+      xi = xe_scale - eta;
+    };
+    if (pt_eq(X[1], mp)) {
+      if (!pos) { i01 = s0 + 1 + 3; i2 = s1; }
+      else { i01 = s1 + 1 + e; i2 = s0; zeta = 2 * xe_fraction - 1; set_xe((zs + 1) / 2); }
+    } else if (pt_eq(X[4], mp)) {
+      if (!pos) { i01 = s1 + 1 + e; i2 = s0; zeta = 1 - 2 * xe_fraction; set_xe((zs + 1) / 2); }
+      else { i01 = s0 + 1 + e; i2 = s1; zeta = -zs; }
+    } else if (pt_eq(X[2], mp)) {
+      if (!pos) { i01 = s1 + 1 + e; i2 = s0; zeta = 2 * xe_fraction - 1; set_xe((1 - zs) / 2); }
+      else { i01 = s0 + 1 + e; i2 = s1; set_xe(1 - xe_fraction); }
+    } else if (pt_eq(X[5], mp)) {
+      if (!pos) { i01 = s0 + 1 + e; i2 = s1; zeta = -zs; set_xe(1 - xe_fraction); }
+      else { i01 = s1 + 1 + e; i2 = s0; zeta = 1 - 2 * xe_fraction; set_xe((1 - zs) / 2); }
+    }
+  } else if (i < 6 + 9 * e + 3 * e * e) {  // face 3
+    const unsigned b = i - 6 - 9 * e - 2 * e * e;
+    const double xe_scale = 1 - xs;
+    const double xe_fraction = (xe_scale == 0) ? 0 : (xe_scale - es) / xe_scale;
+    const unsigned s0 = SQ_ROW[b] + 2, s1 = SQ_COL[b] + 2;
+    const Pt mp = min_point(X, 0, 2, 3, 5);
+    const bool pos = face_positive(X, 3);
+    auto set_xe = [&](double xe) { eta = xe_scale - xe * xe_scale; };
+    if (pt_eq(X[2], mp)) {
+      if (!pos) { i01 = s0 + 1 + 2 * e; i2 = s1; }
+      else { i01 = s1 + 1 + 2 * e; i2 = s0; zeta = 2 * xe_fraction - 1; set_xe((zs + 1) / 2); }
+    } else if (pt_eq(X[5], mp)) {
+      if (!pos) { i01 = s1 + 1 + 2 * e; i2 = s0; zeta = 1 - 2 * xe_fraction; set_xe((zs + 1) / 2); }
+      else { i01 = s0 + 1 + 2 * e; i2 = s1; zeta = -zs; }
+    } else if (pt_eq(X[0], mp)) {
+      if (!pos) { i01 = s1 + 1 + 2 * e; i2 = s0; zeta = 2 * xe_fraction - 1; set_xe((1 - zs) / 2); }
+      else { i01 = s0 + 1 + 2 * e; i2 = s1; set_xe(1 - xe_fraction); }
+    } else if (pt_eq(X[3], mp)) {
+      if (!pos) { i01 = s0 + 1 + 2 * e; i2 = s1; zeta = -zs; set_xe(1 - xe_fraction); }
+      else { i01 = s1 + 1 + 2 * e; i2 = s0; zeta = 1 - 2 * xe_fraction; set_xe((1 - zs) / 2); }
+    }
+  } else if (i < 6 + 9 * e + 3 * e * e + e * (e - 1) / 2) {  // face 0
+    i01 = i - 3 - 6 * e - 3 * e * e;
+    i2 = 0;
+  } else if (i < 6 + 9 * e + 3 * e * e + e * (e - 1)) {  // face 4
+    i01 = i - 3 - 6 * e - 3 * e * e - e * (e - 1) / 2;
+    i2 = 1;
+  } else {  // interior
+    const unsigned b = i - 6 - 9 * e - 3 * e * e - e * (e - 1);
+    i01 = PR_TRI[b] + 3 + 3 * e;
+    i2 = PR_PAGE[b] + 2;
+  }
+}
+
+// fe_triangle_helper on the triangle with vertex points T[0..2].
+double tri_edge(const Pt *T, double num, double cross, unsigned basisorder, unsigned noden) {
+  double flip = 1;
+  if (basisorder % 2 && pt_greater(T[noden], T[(noden + 1) % 3])) flip = -1.;
+  if (cross == 0.) {
+    unsigned basisfactorial = 1;
+    for (unsigned n = 2; n <= basisorder; ++n) basisfactorial *= n;
+    return std::pow(num, basisorder) / basisfactorial;
+  }
+  const double edgeval = num / cross;
+  const double crossfunc = std::pow(cross, basisorder);
+  return flip * crossfunc * hier_1d(basisorder, edgeval);
+}
+
+// FE<2,L2_HIERARCHIC>::shape on a TRI3 with vertex points T.
+double tri_shape(const Pt *T, unsigned totalorder, unsigned i, double x, double y) {
+  const double zeta1 = x, zeta2 = y, zeta0 = 1. - zeta1 - zeta2;
+  if (i == 0) return zeta0;
+  if (i == 1) return zeta1;
+  if (i == 2) return zeta2;
+  if (i < totalorder + 2u) return tri_edge(T, zeta1 - zeta0, zeta0 + zeta1, i - 1, 0);
+  if (i < 2u * totalorder + 1) return tri_edge(T, zeta2 - zeta1, zeta2 + zeta1, i - totalorder, 1);
+  if (i < 3u * totalorder) return tri_edge(T, zeta0 - zeta2, zeta0 + zeta2, i - (2u * totalorder) + 1, 2);
+  const unsigned basisnum = i - (3u * totalorder);
+  const unsigned exp0 = TRI_COL[basisnum] + 1, exp1 = TRI_ROW[basisnum] + 1 - TRI_COL[basisnum];
+  double r = 1;
+  for (unsigned n = 0; n != exp0; ++n) r *= zeta0;
+  for (unsigned n = 0; n != exp1; ++n) r *= zeta1;
+  r *= zeta2;
+  return r;
+}
+
+double shape(const std::vector<Pt> &X, unsigned totalorder, unsigned i, const Pt &p) {
+  double xi = p.v[0], eta = p.v[1], zeta = p.v[2];
+  unsigned i01 = 0, i2 = 0;
+  indices(X, totalorder, i, xi, eta, zeta, i01, i2);
+  Pt T[3];
+  if (i2 == 1) {
+    T[0] = X[3]; T[1] = X[4]; T[2] = X[5];
+  } else {
+    T[0] = X[0]; T[1] = X[1]; T[2] = X[2];
+    if (i2 > 1 && i01 > 2 && i01 < 3u * totalorder) {
+      const bool odd_basis = ((i01 - 1) % (totalorder - 1)) % 2;
+      if (odd_basis) {
+        const unsigned te = (i01 - 3) / (totalorder - 1);
+        if (pt_greater(T[te], T[(te + 1) % 3])) std::swap(T[te], T[(te + 1) % 3]);
+      }
+    }
+  }
+  return tri_shape(T, totalorder, i01, xi, eta) * hier_1d(i2, zeta);
+}
+
+double deriv(const std::vector<Pt> &X, unsigned totalorder, unsigned i, unsigned j, const Pt &p) {
+  const double eps = 1.e-6;
+  Pt pp = p, pm = p;
+  pp.v[j] += eps;
+  pm.v[j] -= eps;
+  return (shape(X, totalorder, i, pp) - shape(X, totalorder, i, pm)) / 2. / eps;
+}
+}  // namespace prism
+
 // FE<3,HIERARCHIC>::shape on a PRISM6, totalorder 1 (prism_indices vertices,
 // fe_hierarchic_shape_3D.C:764-810): the TRI vertex function (zeta0 =
 // 1 - xi - eta, xi, eta; fe_hierarchic_shape_2D.C:969-983) times the 1-D
@@ -1201,6 +1390,23 @@ int orc_shapes_hier_hex(const double *X27, int order, int np, const double *pts,
     for (int i = 0; i < n; ++i) {
       phi[i * np + q] = hier_hexo_shape(X, (unsigned)order, i, p);
       for (int c = 0; c < 3; ++c) dphi[(c * n + i) * np + q] = hier_hexo_deriv(X, (unsigned)order, i, c, p);
+    }
+  }
+  return n;
+}
+
+// HIERARCHIC shapes of order 2 or 3 on one prism (vertex coordinates X6 [6][3]).
+int orc_shapes_hier_prism(const double *X6, int order, int np, const double *pts, double *phi, double *dphi) {
+  if (order < 2 || order > 3) return -1;
+  std::vector<Pt> X(6);
+  for (int a = 0; a < 6; ++a)
+    for (int d = 0; d < 3; ++d) X[a].v[d] = X6[3 * a + d];
+  const int n = (order + 1) * (order + 1) * (order + 2) / 2;
+  for (int q = 0; q < np; ++q) {
+    const Pt p = {{pts[3 * q], pts[3 * q + 1], pts[3 * q + 2]}};
+    for (int i = 0; i < n; ++i) {
+      phi[i * np + q] = prism::shape(X, (unsigned)order, i, p);
+      for (int c = 0; c < 3; ++c) dphi[(c * n + i) * np + q] = prism::deriv(X, (unsigned)order, i, c, p);
     }
   }
   return n;

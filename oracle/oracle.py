@@ -35,6 +35,8 @@ def lib():
         _lib.orc_shapes_tet3.argtypes = [v, i32, v, v, v]
         _lib.orc_shapes_hier_hex.argtypes = [v, i32, i32, v, v, v]
         _lib.orc_shapes_hier_hex.restype = C.c_int32
+        _lib.orc_shapes_hier_prism.argtypes = [v, i32, i32, v, v, v]
+        _lib.orc_shapes_hier_prism.restype = C.c_int32
         _lib.orc_distribute_dofs_tet3.argtypes = [i64, i64, v, v, C.POINTER(i64)]
         _lib.orc_dirichlet_tet3.argtypes = [i64, v, v, v, i32, v]
         _lib.orc_mesh_cube.argtypes = [i32, i32, i32, i32, f64, C.c_uint64]
@@ -144,6 +146,18 @@ def shapes_hier_hex(X27, order, pts):
     dphi = np.zeros((3, n, len(pts)))
     assert lib().orc_shapes_hier_hex(_p(np.ascontiguousarray(X27, np.float64)), order, len(pts), _p(pts), _p(phi),
                                      _p(dphi)) == n
+    return phi, dphi
+
+
+def shapes_hier_prism(X6, order, pts):
+    """HIERARCHIC shapes of order 2 or 3 on one prism (vertex coordinates X6
+    [6][3]) at reference points: phi [n][np], dphi [3][n][np]."""
+    pts = np.ascontiguousarray(pts, np.float64)
+    n = (order + 1) * (order + 1) * (order + 2) // 2
+    phi = np.zeros((n, len(pts)))
+    dphi = np.zeros((3, n, len(pts)))
+    assert lib().orc_shapes_hier_prism(_p(np.ascontiguousarray(np.asarray(X6)[:6], np.float64)), order, len(pts),
+                                       _p(pts), _p(phi), _p(dphi)) == n
     return phi, dphi
 
 
