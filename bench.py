@@ -374,6 +374,18 @@ def run_batch(args, local):
     b.synchronize()
     ms = ev0.elapsed_time(ev1) / args.steps
     clk = clocks.stop()
+    # the mixed form through the same graph machinery, tuned for it
+    b.tune(lm.MIXED, reps=2)
+    for _ in range(max(3, args.warmup)):
+        b.assemble(lm.MIXED)
+    b.synchronize()
+    ev0.record(stream)
+    for _ in range(args.steps):
+        b.assemble(lm.MIXED)
+    ev1.record(stream)
+    ev1.synchronize()
+    b.synchronize()
+    ms32 = ev0.elapsed_time(ev1) / args.steps
     b.close()
     n_dofs_total = sum(a.dof_map.n_dofs for a, _ in mem)
     for a, _ in mem:
@@ -389,6 +401,8 @@ def run_batch(args, local):
                    "setup_s": setup_s, "tune_s": tune_s},
         "sequential": {"ms_per_step": seq_ms, "value": total / (seq_ms * 1e-3) / 1e6, "unit": "Melem/s",
                        "how": "lmg_assemble per system on its own stream, host loop, default grids"},
+        "mixed": {"ms_per_step": ms32, "value": total / (ms32 * 1e-3) / 1e6, "unit": "Melem/s",
+                  "speedup_vs_fp64": ms / ms32},
         "graph_speedup": seq_ms / ms, "gpu_launches": launches * args.steps, "launches_per_replay": launches,
         "tuned_ctas_per_sm": {str(g): int((grids == g).sum()) for g in sorted(set(grids.tolist()))},
         "clocks": clk}))
@@ -669,9 +683,12 @@ def main():
     if dist:
         dist.barrier()
     t0 = time.perf_counter()
+    e2e_ms = []
     for _ in range(e2e_steps):
+        t1 = time.perf_counter()
         asm.update_inputs(elem_coef=Eh.numpy(), nodal_f=fh.numpy())
         asm.assemble_into(Kh.data_ptr(), Fh.data_ptr(), prec)
+        e2e_ms.append(1e3 * (time.perf_counter() - t1))
     e2e_s = (time.perf_counter() - t0) / e2e_steps
     if dist:
         t = torch.tensor([e2e_s], device="cuda")
@@ -692,6 +709,7 @@ def main():
     B, ref_flops, our_flops = algorithmic(mesh, dm, asm.nnz)
     hbm, hbm_src = peaks()
     fp64 = lm.probe_fp64(local)
+    fp64_tc = lm.probe_fp64_tensor(local)
     if el_ms >= ga_ms:
         dom = {"kernel": "k_elem_affine<ELASTICITY,10,3,double>", "bound": "fp64", "unit": "TFLOP/s",
                "achieved": our_flops * mesh.n_elem / (el_ms * 1e-3) / 1e12, "peak": fp64,
@@ -740,9 +758,13 @@ def main():
             "mdofs_per_s": value * dm.n_dofs / mesh.n_elem,
             "e2e": {"value": e2e, "unit": "Melem/s", "h2d_bytes_per_step": 8 * (mesh.n_elem + 3 * mesh.n_nodes),
                     "d2h_bytes_per_step": 8 * (asm.nnz + dm.n_dofs), "d2h_link_gbs": link_gbs,
-                    "copy_floor_melem_s": mesh.n_elem / (8 * (asm.nnz + dm.n_dofs) / (link_gbs * 1e9)) / 1e6},
+                    "copy_floor_melem_s": mesh.n_elem / (8 * (asm.nnz + dm.n_dofs) / (link_gbs * 1e9)) / 1e6,
+                    "step_ms": [round(x, 2) for x in e2e_ms]},
             "gpu_launches": launches, "clocks": clk, "roofline": dom, "cpu_baseline": cpu,
-            "mixed": other, "residual": resid}))
+            "mixed": other, "residual": resid,
+            "fp64_probe_tflops": {"dfma": fp64, "dmma_m8n8k4": fp64_tc,
+                                  "note": "measured in this run; the drop-in contracts in double-float on the "
+                                          "FP32 pipe instead"}}))
     if dist:
         dist.destroy_process_group()
 

@@ -401,6 +401,11 @@ lmg_status lmg_launch_count(lmg_ctx *ctx, int64_t *count);
  * chains on every SM): the roofline denominator of the FP64 element kernels. */
 lmg_status lmg_probe_fp64(int32_t device, double *tflops);
 
+/* Measured FP64 tensor-core throughput of `device` in TFLOP/s (chains of
+ * mma.sync m8n8k4 f64 products on every SM): the rate an FP64 DMMA form of the
+ * element contractions would be bound by. */
+lmg_status lmg_probe_fp64_tensor(int32_t device, double *tflops);
+
 #ifdef __cplusplus
 }
 #endif

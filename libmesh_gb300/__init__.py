@@ -341,6 +341,13 @@ def probe_fp64(device=0):
     return t.value
 
 
+def probe_fp64_tensor(device=0):
+    """Measured FP64 tensor-core (DMMA m8n8k4) throughput (TFLOP/s) of the device."""
+    t = C.c_double()
+    check(lib().lmg_probe_fp64_tensor(device, C.byref(t)))
+    return t.value
+
+
 class LinearImplicitSystem:
     """The parts of libMesh's LinearImplicitSystem the assembly path uses."""
 

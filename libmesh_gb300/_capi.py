@@ -79,6 +79,7 @@ SIGNATURES = {
     "lmg_batch_synchronize": [_p, _pi64],
     "lmg_batch_info": [_p, C.POINTER(_p), _pi64, _p, _i32],
     "lmg_probe_fp64": [_i32, _pf64],
+    "lmg_probe_fp64_tensor": [_i32, _pf64],
 }
 
 _lib = None

@@ -1,6 +1,8 @@
-// FP64 pipe throughput probe: independent DFMA chains on every SM, timed with
-// CUDA events.  Gives the FP64 roofline denominator the assembly kernels are
-// measured against (GB300 FP64 is not among the measured peaks).
+// FP64 throughput probes, timed with CUDA events: independent DFMA chains on
+// every SM (the FP64 roofline denominator the assembly kernels are measured
+// against; GB300 FP64 is not among the measured peaks), and the same
+// with FP64 tensor-core products (mma.sync m8n8k4 f64, DMMA), to compare the
+// two routes an FP64 contraction could take.
 #include <cuda_runtime.h>
 
 #include "../../include/libmesh_gb300.h"
@@ -19,7 +21,58 @@ __global__ void k_dfma(int iters, double a, double b, double *sink) {
   for (int c = 0; c < CHAINS; ++c) s += x[c];
   if (s == 1234.5678) sink[0] = s;  // keeps the chains live
 }
+// CHAINS independent accumulators per warp, each a chain of m8n8k4 FP64
+// products (512 flops per warp-wide instruction).
+__global__ void k_dmma(int iters, double *sink) {
+  const double a = 1.0 + threadIdx.x * 1e-6, b = 0.5;
+  double d[CHAINS][2];
+#pragma unroll
+  for (int c = 0; c < CHAINS; ++c) d[c][0] = d[c][1] = c;
+  for (int i = 0; i < iters; ++i)
+#pragma unroll
+    for (int c = 0; c < CHAINS; ++c)
+      asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0, %1}, {%2}, {%3}, {%0, %1};"
+                   : "+d"(d[c][0]), "+d"(d[c][1])
+                   : "d"(a), "d"(b));
+  double s = 0;
+#pragma unroll
+  for (int c = 0; c < CHAINS; ++c) s += d[c][0] + d[c][1];
+  if (s == 1234.5678) sink[0] = s;
+}
+
+template <typename Launch>
+lmg_status time_probe(int32_t device, double flops_per_launch, Launch &&launch, double *tflops) {
+  if (cudaSetDevice(device) != cudaSuccess) return LMG_ERR_CUDA;
+  double *sink = nullptr;
+  if (cudaMalloc((void **)&sink, sizeof(double)) != cudaSuccess) return LMG_ERR_OOM;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  launch(64, sink);  // warm-up
+  cudaEventRecord(e0);
+  launch(4096, sink);
+  cudaEventRecord(e1);
+  cudaError_t err = cudaEventSynchronize(e1);
+  float ms = 0;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(sink);
+  if (err != cudaSuccess || ms <= 0) return LMG_ERR_CUDA;
+  *tflops = flops_per_launch / (ms * 1e-3) / 1e12;
+  return LMG_OK;
+}
 }  // namespace
+
+extern "C" lmg_status lmg_probe_fp64_tensor(int32_t device, double *tflops) {
+  if (!tflops) return LMG_ERR_ARG;
+  int n_sm = 0;
+  if (cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) return LMG_ERR_CUDA;
+  const int blocks = n_sm * 4, threads = 256;
+  const double flops = 512.0 * CHAINS * 4096.0 * blocks * (threads / 32);
+  return time_probe(
+      device, flops, [&](int iters, double *sink) { k_dmma<<<blocks, threads>>>(iters, sink); }, tflops);
+}
 
 extern "C" lmg_status lmg_probe_fp64(int32_t device, double *tflops) {
   if (!tflops) return LMG_ERR_ARG;

@@ -18,7 +18,9 @@
 // that point's rows, is a separate copy with those rows negated.  That is what runs here, for the elements the reference-tensor
 // shortcut does not cover (non-affine maps, libMesh's compute_map branch).
 //
-// A CTA (4 warps) takes 4 elements per tile.  Warp w builds element w's E:
+// A CTA (4 warps) takes 4 elements per tile; their connectivity rows arrive
+// in shared memory by one bulk asynchronous copy (cp.async.bulk, completing
+// on an mbarrier) when the four are consecutive ids.  Warp w builds element w's E:
 // the Jacobian, detJ and J^-1 at every point in FP64 (compute_single_point_map,
 // fe_map.C:980-1078), the scale factors in FP64, the physical gradients and E
 // in FP32; every entry is split into three BF16 pieces (hi + mid + lo carry
@@ -40,6 +42,7 @@
 #include <cuda_runtime.h>
 
 #include "assemble.cuh"
+#include "bulk_copy.cuh"
 #include "df.cuh"
 #include "elem_geom.cuh"
 #include "../../include/libmesh_gb300.h"
@@ -48,7 +51,7 @@ namespace lmg {
 
 namespace {
 
-__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return smem_addr(p); }
 
 // Shared-memory matrix descriptor of a K-major tile without swizzling:
 // start address, leading byte offset (between core matrices adjacent in K),
@@ -103,7 +106,9 @@ template <int FORM, int N, int NV, int Q>
 __global__ void __launch_bounds__(128) k_elem_tc(ElemArgs a, int is_signed) {
   using S = TcShape<FORM, N, NV, Q>;
   extern __shared__ __align__(1024) unsigned char tsm[];
-  __shared__ __align__(8) uint64_t mbar;
+  __shared__ __align__(8) uint64_t mbar, mbar_tma;
+  __shared__ __align__(16) int32_t sConn[4 * N];  // connectivity rows of the tile's elements
+  __shared__ int tile_bulk;
   __shared__ uint32_t tmem_base;
   const int t = threadIdx.x, w = t >> 5, lane = t & 31;
   const int npc = is_signed ? 6 : 3;
@@ -125,20 +130,50 @@ __global__ void __launch_bounds__(128) k_elem_tc(ElemArgs a, int is_signed) {
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   if (t == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&mbar)), "r"(1));
-    asm volatile("fence.mbarrier_init.release.cluster;");
+    mbar_init(&mbar, 1);
+    mbar_init(&mbar_tma, 1);
+    mbar_fence_init();
   }
   asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;");
   const uint32_t tmem = tmem_base;
-  uint32_t phase = 0;
+  uint32_t phase = 0, phase_tma = 0;
   const int64_t n_tiles = (a.n_list + 3) / 4;
   for (int64_t tile = blockIdx.x; tile < n_tiles; tile += gridDim.x) {
     const int64_t li = tile * 4 + w;
     const int32_t e = li < a.n_list ? a.list[li] : -1;
+    // Connectivity of the tile: when its four elements are consecutive ids
+    // with 16-byte aligned rows (a mesh whose elements all take this kernel),
+    // one bulk asynchronous copy (TMA) into shared memory; otherwise each
+    // warp loads its element's row.
+    if (t == 0) {
+      const int64_t l0 = tile * 4;
+      int bulk = l0 + 3 < a.n_list && a.npe == N;
+      const int32_t e0 = bulk ? a.list[l0] : 0;
+      for (int j = 1; bulk && j < 4; ++j) bulk = a.list[l0 + j] == e0 + j;
+      const uint64_t src = (uint64_t)(a.conn + (int64_t)e0 * N);
+      bulk = bulk && (src % 16 == 0) && ((4 * N * sizeof(int32_t)) % 16 == 0);
+      tile_bulk = bulk;
+      if (bulk) {
+        mbar_expect_tx(&mbar_tma, (uint32_t)(4 * N * sizeof(int32_t)));
+        bulk_g2s(sConn, (const void *)src, (uint32_t)(4 * N * sizeof(int32_t)), &mbar_tma);
+      }
+    }
+    __syncthreads();
+    if (tile_bulk) {
+      const uint32_t got = mbar_wait(&mbar_tma, phase_tma, 1 << 24) ? 1u : 0u;
+      phase_tma ^= 1u;
+      if (!__syncthreads_and((int)got)) {
+        if (t == 0) atomicCAS(a.status, 0, LMG_ERR_CUDA);
+        break;
+      }
+    } else if (e >= 0) {
+      for (int i = lane; i < N; i += 32) sConn[w * N + i] = a.conn[(int64_t)e * a.npe + i];
+    }
+    __syncwarp();
     if (e >= 0) {
-      const int32_t *c = a.conn + (int64_t)e * a.npe;
+      const int32_t *c = sConn + w * N;
       for (int i = lane; i < N * 3; i += 32) sX[i] = a.xyz[3 * (int64_t)c[i / 3] + i % 3];
       for (int i = lane; i < N * NV; i += 32) sF[i] = a.nodal_f ? a.nodal_f[(int64_t)c[i / NV] * NV + i % NV] : 0.0;
     }
@@ -273,12 +308,7 @@ __global__ void __launch_bounds__(128) k_elem_tc(ElemArgs a, int is_signed) {
       asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
           smem_u32(&mbar)));
     }
-    uint32_t done = 0;
-    for (int it = 0; it < (1 << 24) && !done; ++it)
-      asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-                   " selp.u32 %0, 1, 0, p;\n}\n"
-                   : "=r"(done)
-                   : "r"(smem_u32(&mbar)), "r"(phase));
+    const uint32_t done = mbar_wait(&mbar, phase, 1 << 24) ? 1u : 0u;
     phase ^= 1u;
     if (!__syncthreads_and((int)done)) {
       if (t == 0) atomicCAS(a.status, 0, LMG_ERR_CUDA);

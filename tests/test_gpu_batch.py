@@ -79,16 +79,20 @@ def test_batch_matches_individual_assembly():
 
 
 def test_batch_mixed_precision_graph():
+    """Every member in the mixed form (fused row kernel, FP32 element blocks,
+    FP32 general-path contraction) replays bit for bit as assembled alone."""
     mem = members()
-    for other, _, _ in mem[:1] + mem[2:]:
-        other.close()
-    a = mem[1][0]                                     # elasticity: the mixed form is built for it
-    K32, F32 = a.assemble(lm.MIXED)
+    ref = [a.assemble(lm.MIXED) for a, _, _ in mem]
     b = lm.Batch()
-    b.add(a)
-    b.assemble(lm.MIXED)
-    b.synchronize()
-    K, F = a.result()
-    assert np.array_equal(K, K32) and np.array_equal(F, F32)
+    for a, _, _ in mem:
+        b.add(a)
+    b.tune(lm.MIXED, reps=2)
+    for _ in range(2):
+        b.assemble(lm.MIXED)
+        b.synchronize()
+        for (a, _, _), (K0, F0) in zip(mem, ref):
+            K, F = a.result()
+            assert np.array_equal(K, K0) and np.array_equal(F, F0)
     b.close()
-    a.close()
+    for a, _, _ in mem:
+        a.close()
