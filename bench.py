@@ -299,6 +299,8 @@ BATCH_KINDS = [  # (element, HIERARCHIC order, QGauss order, elements per grid c
     (8, 1, 2, 6),    # TET4   FIRST
     (9, 2, 4, 6),    # TET10  SECOND
     (13, 1, 3, 2),   # PRISM6 FIRST
+    (15, 2, 4, 2),   # PRISM18 SECOND
+    (36, 3, 5, 2),   # PRISM21 THIRD
     (34, 3, 6, 6),   # TET14  THIRD
 ]
 
@@ -396,7 +398,7 @@ def run_batch(args, local):
         "dtype": "f64", "data": "synthetic (seeded sizes, coefficients, loads)",
         "config": {"workload": "batch of %d systems (config-4 mix), element counts log-uniform in "
                                "[1e3, %.0e]: HIERARCHIC Poisson on HEX8 p1, HEX27 p2, HEX27 p3, TET4 p1, TET10 p2, "
-                               "PRISM6 p1, TET14 p3, k_e ~ U[0.1, 10]" % (n_meshes, args.max_elems),
+                               "PRISM6 p1, PRISM18 p2, PRISM21 p3, TET14 p3, k_e ~ U[0.1, 10]" % (n_meshes, args.max_elems),
                    "total_elements": total, "total_dofs": n_dofs_total,
                    "setup_s": setup_s, "tune_s": tune_s},
         "sequential": {"ms_per_step": seq_ms, "value": total / (seq_ms * 1e-3) / 1e6, "unit": "Melem/s",

@@ -52,7 +52,10 @@ enum {
 };
 
 /* Element types: the numeric values of libMesh's ElemType (include/enums/enum_elem_type.h). */
-enum { LMG_TET4 = 8, LMG_TET10 = 9, LMG_HEX8 = 10, LMG_HEX27 = 12, LMG_PRISM6 = 13, LMG_TET14 = 34 };
+enum {
+  LMG_TET4 = 8, LMG_TET10 = 9, LMG_HEX8 = 10, LMG_HEX27 = 12, LMG_PRISM6 = 13, LMG_PRISM18 = 15,
+  LMG_TET14 = 34, LMG_PRISM21 = 36
+};
 
 /* Weak forms registered with the element kernels (examples the forms follow):
  *   LMG_POISSON    Ke += k_e JxW dphi_i.dphi_j, Fe += JxW f phi_i

@@ -14,13 +14,13 @@ import ctypes as C
 import numpy as np
 
 from . import _capi
-from ._capi import (ADVDIFF, ELASTICITY, FP64, HEX8, HEX27, HIERARCHIC, MIXED, POISSON, PRISM6, TET4, TET10,
-                    TET14, DegenerateMap, LmgError, check, lib, ptr)
+from ._capi import (ADVDIFF, ELASTICITY, FP64, HEX8, HEX27, HIERARCHIC, MIXED, POISSON, PRISM6, PRISM18, PRISM21,
+                    TET4, TET10, TET14, DegenerateMap, LmgError, check, lib, ptr)
 
 FIRST, SECOND, THIRD, FOURTH, FIFTH = 1, 2, 3, 4, 5
 
 __all__ = ["Mesh", "DofMap", "GpuAssembly", "Batch", "LinearImplicitSystem", "DegenerateMap", "LmgError",
-           "HEX8", "HEX27", "TET4", "TET10", "TET14", "PRISM6", "POISSON", "ELASTICITY", "ADVDIFF", "FP64", "MIXED", "HIERARCHIC",
+           "HEX8", "HEX27", "TET4", "TET10", "TET14", "PRISM6", "PRISM18", "PRISM21", "POISSON", "ELASTICITY", "ADVDIFF", "FP64", "MIXED", "HIERARCHIC",
            "FIRST", "SECOND", "THIRD", "FOURTH", "FIFTH"]
 
 
@@ -109,7 +109,8 @@ class DofMap:
     """Var-major first-touch numbering of n_vars variables (one VariableGroup);
     elem_dofs[e] is DofMap::dof_indices(elem).  fe_order (| HIERARCHIC) picks
     the FEType whose dofs are numbered: nodal types give one dof per node and
-    variable; 3 | HIERARCHIC gives 64 dofs per element on HEX27 and 20 on TET14."""
+    variable; 3 | HIERARCHIC gives 64 dofs per element on HEX27, 20 on TET14
+    and 40 on PRISM21; 2 | HIERARCHIC 18 on PRISM18."""
 
     def __init__(self, mesh, n_vars=1, fe_order=None):
         self.mesh = mesh

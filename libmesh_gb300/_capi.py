@@ -14,7 +14,7 @@ OK, ERR_ARG, ERR_CUDA, ERR_STATE, ERR_DEGENERATE, ERR_BOUNDS, ERR_NEW_NONZERO, E
 STATUS_NAMES = {0: "OK", 1: "ERR_ARG", 2: "ERR_CUDA", 3: "ERR_STATE", 4: "ERR_DEGENERATE",
                 5: "ERR_BOUNDS", 6: "ERR_NEW_NONZERO", 7: "ERR_OOM", 8: "ERR_UNSUPPORTED"}
 # element types (libMesh ElemType values)
-TET4, TET10, HEX8, HEX27, PRISM6, TET14 = 8, 9, 10, 12, 13, 34
+TET4, TET10, HEX8, HEX27, PRISM6, PRISM18, TET14, PRISM21 = 8, 9, 10, 12, 13, 15, 34, 36
 # forms and precisions
 POISSON, ELASTICITY, ADVDIFF = 0, 1, 2
 FP64, MIXED = 0, 1

@@ -596,12 +596,13 @@ lmg_status lmg_dofmap_upload(lmg_ctx *c, int32_t n_vars, int64_t n_dofs, const i
 
 lmg_status lmg_dofmap_upload_fe(lmg_ctx *c, int32_t n_vars, int32_t fe_order, int64_t n_dofs,
                                 const int32_t *elem_dofs) {
-  if (fe_order != (3 | LMG_HIERARCHIC)) return lmg_dofmap_upload(c, n_vars, n_dofs, elem_dofs);
+  const bool prism2 = c && fe_order == (2 | LMG_HIERARCHIC) && c->elem_type == LMG_PRISM18;
+  if (fe_order != (3 | LMG_HIERARCHIC) && !prism2) return lmg_dofmap_upload(c, n_vars, n_dofs, elem_dofs);
   if (!c || !elem_dofs || n_vars != 1 || n_dofs <= 0) return fail(c, LMG_ERR_ARG, "dofmap_upload: bad argument");
   if (!c->n_elem) return fail(c, LMG_ERR_STATE, "dofmap_upload: upload the mesh first");
-  if (c->elem_type != LMG_HEX27 && c->elem_type != LMG_TET14)
-    return fail(c, LMG_ERR_UNSUPPORTED, "dofmap_upload: THIRD HIERARCHIC needs HEX27 or TET14");
-  const int nl = c->elem_type == LMG_TET14 ? 20 : 64;
+  const int nl = pattern_fe_dofs(c->elem_type, fe_order);
+  if (!nl)
+    return fail(c, LMG_ERR_UNSUPPORTED, "dofmap_upload: THIRD HIERARCHIC needs HEX27, TET14 or PRISM21");
   for (int64_t i = 0; i < c->n_elem * nl; ++i)
     if (elem_dofs[i] < 0 || elem_dofs[i] >= n_dofs) return fail(c, LMG_ERR_BOUNDS, "dof id out of range", i / nl);
   cudaSetDevice(c->device);
@@ -733,7 +734,7 @@ lmg_status lmg_form_set(lmg_ctx *c, int32_t form, int32_t fe_order, int32_t q_or
       return fail(c, LMG_ERR_ARG, "form_set: ADVDIFF parameter count does not match n_modes");
   }
   cudaSetDevice(c->device);
-  if (c->hier3 != (fe_order == (3 | LMG_HIERARCHIC)))
+  if (c->hier3 != (pattern_fe_dofs(c->elem_type, fe_order) > 0))
     return fail(c, LMG_ERR_STATE, "form_set: the dof lists were uploaded for another FE type");
   if (c->hier3) return hier3_form_set(c, form, q_order, elem_coef, nodal_f);
   const int family = (fe_order & LMG_HIERARCHIC) ? 1 : 0;

@@ -74,7 +74,7 @@ lmg_status general_sparsity(lmg_ctx *c) {
 lmg_status general_plan(lmg_ctx *c) {
   const int N = c->nl;
   const int64_t E = c->n_elem;
-  if (c->n_vars != 1 || (N > GEN_MAX_N && !(c->hier3 && N == 64)))
+  if (c->n_vars != 1 || (N > GEN_MAX_N && !(c->hier3 && N <= 64)))
     return fail(c, LMG_ERR_UNSUPPORTED, "general path: one variable and at most 27 dofs per element");
   if (c->h_row_ptr.empty()) {  // pattern built by the block path: bring it to the host
     c->h_row_ptr.resize((size_t)c->n_dofs + 1);

@@ -89,7 +89,8 @@ struct lmg_ctx {
   uint8_t *d_cci = nullptr;
   double *d_ccv = nullptr;
   uint64_t *d_crow = nullptr;
-  // cubic HIERARCHIC hexes (hier3.cu): dof lists of 64 per element, general path
+  // per-pattern HIERARCHIC elements (hier3.cu): cubic hexes, tets and prisms,
+  // quadratic prisms; general path
   bool hier3 = false;
   int32_t *d_h3batch = nullptr, *d_h3order = nullptr;  // element batches of one orientation pattern
   float2 *d_h3D = nullptr;           // per-pattern reference tensors, double-float pairs
@@ -150,6 +151,11 @@ lmg_status general_plan(lmg_ctx *c);       // constraint columns, slot plan, buf
 lmg_status general_assemble(lmg_ctx *c, bool mixed);
 void general_gather(lmg_ctx *c, bool mixed);  // slot gather into K and F
 // hier3.cu
+// FE types whose shapes follow each element's orientation pattern and that
+// take the per-pattern tables of hier3.cu: HIERARCHIC THIRD on HEX27, TET14
+// and PRISM21, HIERARCHIC SECOND on PRISM18; their dofs per element (0 for
+// any other type).
+int pattern_fe_dofs(int elem_type, int fe_order);
 void hier3_free(lmg_ctx *c);
 lmg_status hier3_form_set(lmg_ctx *c, int32_t form, int32_t q_order, const double *elem_coef,
                           const double *nodal_f);

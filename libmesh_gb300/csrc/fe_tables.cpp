@@ -508,6 +508,15 @@ std::string build_fe_tables(FETables &t, int type, int fe_order, int q_order, in
 namespace {
 // libMesh relative_fuzzy_equals on 3-vectors (include/utils/fuzzy_equals.h:78-84):
 // l1(a - b) <= tol * (l1(a) + l1(b)), with affine_tol = TOLERANCE^2 = 1e-12.
+bool rfe_tol(const double *a, const double *b, double tol) {
+  double d = 0, na = 0, nb = 0;
+  for (int i = 0; i < 3; ++i) {
+    d += std::fabs(a[i] - b[i]);
+    na += std::fabs(a[i]);
+    nb += std::fabs(b[i]);
+  }
+  return d <= tol * (na + nb);
+}
 bool rfe(const double *a, const double *b) {
   const double tol = 1e-6 * 1e-6;
   double d = 0, na = 0, nb = 0;
@@ -530,6 +539,35 @@ bool elem_has_affine_map(int type, const double *P) {
       sub(P, 3, 0, v);
       sub(P, 4, 1, w); if (!rfe(v, w)) return false;
       sub(P, 5, 2, w); return rfe(v, w);
+    }
+    case LMG_PRISM18:    // cell_prism18.C:122-150
+    case LMG_PRISM21: {  // cell_prism21.C:139-180: straight edges, then centred triangle-face nodes
+      sub(P, 3, 0, v);
+      sub(P, 4, 1, w); if (!rfe(v, w)) return false;
+      sub(P, 5, 2, w); if (!rfe(v, w)) return false;
+      for (int d = 0; d < 3; ++d) v[d] /= 2;
+      static const int Z[6][2] = {{9, 0}, {10, 1}, {11, 2}, {15, 6}, {16, 7}, {17, 8}};
+      for (auto &z : Z) {
+        sub(P, z[0], z[1], w);
+        if (!rfe(v, w)) return false;
+      }
+      static const int T[3][4] = {{1, 0, 6, 0}, {2, 0, 8, 0}, {2, 1, 7, 1}};  // v = (b - a) / 2 against m - a, m' - a'
+      for (auto &t : T) {
+        sub(P, t[0], t[1], v);
+        for (int d = 0; d < 3; ++d) v[d] /= 2;
+        sub(P, t[2], t[3], w); if (!rfe(v, w)) return false;
+        sub(P, t[2] + 6, t[3] + 3, w); if (!rfe(v, w)) return false;
+      }
+      if (type == LMG_PRISM18) return true;
+      static const int F[3][4] = {{2, 1, 0, 18}, {5, 4, 3, 19}, {11, 10, 9, 20}};  // c + b - 2 a against 3 (m - a)
+      for (auto &f : F) {
+        for (int d = 0; d < 3; ++d) {
+          v[d] = P[3 * f[0] + d] + P[3 * f[1] + d] - 2 * P[3 * f[2] + d];
+          w[d] = (P[3 * f[3] + d] - P[3 * f[2] + d]) * 3;
+        }
+        if (!rfe_tol(v, w, 1e-6)) return false;
+      }
+      return true;
     }
     case LMG_TET4:
       return true;

@@ -44,7 +44,8 @@ struct H3Args {
   const int32_t *batch;     // [n_batch][3]: pattern, first index in order, count
   const int32_t *order;     // element ids sorted by pattern
   const double *xyz;
-  const int32_t *conn;      // [n_elem][G]
+  const int32_t *conn;      // [n_elem][npe], the G map nodes first
+  int npe;
   const double *coef;       // [n_elem] or null
   const double *nodal_f;    // [n_nodes] or null
   const uint64_t *cmask;    // [n_elem] constrained local dofs, or null (no mask)
@@ -57,7 +58,8 @@ struct H3Args {
   unsigned long long *bad_elem;
 };
 
-// N dofs and G map nodes per element (cubic hexes 64 / 27, cubic tets 20 / 14).
+// N dofs and G map nodes per element (cubic hexes 64 / 27, cubic tets 20 / 14,
+// quadratic and cubic prisms 18 / 6 and 40 / 6).
 // FP64 drop-in (MIXED false): the contraction in double-float, each entry
 // rounded to FP64 once; mixed form: the contraction in FP32.  The map is FP64
 // in both.
@@ -78,7 +80,7 @@ __global__ void __launch_bounds__(H3T) k_elem_pattern(H3Args a) {
     if (w < cnt) {  // warp w: geometry of the batch's element w (compute_affine_map)
       const int32_t e = a.order[first + w];
       if (lane < G) {
-        const int64_t nd = a.conn[(int64_t)e * G + lane];
+        const int64_t nd = a.conn[(int64_t)e * a.npe + lane];
         sX[w][3 * lane] = a.xyz[3 * nd];
         sX[w][3 * lane + 1] = a.xyz[3 * nd + 1];
         sX[w][3 * lane + 2] = a.xyz[3 * nd + 2];
@@ -183,17 +185,30 @@ void hier3_free(lmg_ctx *c) {
   c->h3_nbatch = 0;
 }
 
-// lmg_form_set for FEType{THIRD, HIERARCHIC} on HEX27 and TET14.
+// lmg_form_set for the per-pattern HIERARCHIC elements.
+int pattern_fe_dofs(int elem_type, int fe_order) {
+  if (fe_order == (3 | LMG_HIERARCHIC))
+    return elem_type == LMG_HEX27 ? 64 : (elem_type == LMG_TET14 ? 20 : (elem_type == LMG_PRISM21 ? 40 : 0));
+  if (fe_order == (2 | LMG_HIERARCHIC) && elem_type == LMG_PRISM18) return 18;
+  return 0;
+}
+
 lmg_status hier3_form_set(lmg_ctx *c, int32_t form, int32_t q_order, const double *elem_coef,
                           const double *nodal_f) {
-  if (form != LMG_POISSON || c->n_vars != 1 || (c->elem_type != LMG_HEX27 && c->elem_type != LMG_TET14))
-    return fail(c, LMG_ERR_UNSUPPORTED, "form_set: THIRD HIERARCHIC is built for POISSON on HEX27 and TET14");
+  if (form != LMG_POISSON || c->n_vars != 1 || c->nl > 64)
+    return fail(c, LMG_ERR_UNSUPPORTED,
+                "form_set: per-pattern HIERARCHIC elements are built for POISSON (HEX27 / TET14 / PRISM21 "
+                "THIRD, PRISM18 SECOND)");
   if (!c->h_gen.empty())
-    return fail(c, LMG_ERR_UNSUPPORTED, "form_set: THIRD HIERARCHIC takes affine elements only");
+    return fail(c, LMG_ERR_UNSUPPORTED, "form_set: per-pattern HIERARCHIC elements take affine elements only");
   Hier3Tables h;
-  std::string err = c->elem_type == LMG_TET14
-                        ? build_tet3_tables(h, q_order, c->n_elem, c->h_xyz.data(), c->h_conn.data())
-                        : build_hier3_tables(h, q_order, c->n_elem, c->h_xyz.data(), c->h_conn.data());
+  const int order = c->elem_type == LMG_PRISM18 ? 2 : 3;
+  std::string err =
+      c->elem_type == LMG_TET14
+          ? build_tet3_tables(h, q_order, c->n_elem, c->h_xyz.data(), c->h_conn.data())
+          : (c->elem_type == LMG_HEX27
+                 ? build_hier3_tables(h, q_order, c->n_elem, c->h_xyz.data(), c->h_conn.data())
+                 : build_prism_tables(h, order, q_order, c->n_elem, c->h_xyz.data(), c->h_conn.data(), c->npe));
   if (!err.empty()) return fail(c, LMG_ERR_UNSUPPORTED, "form_set: " + err);
   hier3_free(c);
   LMG_CUDA(c, dupload(c, c->d_h3batch, h.batch.data(), h.batch.size()));
@@ -210,7 +225,7 @@ lmg_status hier3_form_set(lmg_ctx *c, int32_t form, int32_t q_order, const doubl
   c->h3_patterns = h.P;
   FETables t;
   t.elem_type = c->elem_type;
-  t.fe_order = 3;
+  t.fe_order = order;
   t.q_order = q_order;
   t.family = 1;
   t.n = h.N;
@@ -218,7 +233,7 @@ lmg_status hier3_form_set(lmg_ctx *c, int32_t form, int32_t q_order, const doubl
   t.n_geo = h.G;
   c->tab = t;
   c->form = form;
-  c->fe_order = 3;
+  c->fe_order = order;
   c->q_order = q_order;
   c->kappa = 0.0;
   c->n_modes = 0;
@@ -243,6 +258,7 @@ void launch_hier3(lmg_ctx *c, bool mixed) {
   a.order = c->d_h3order;
   a.xyz = c->d_xyz;
   a.conn = c->d_conn;
+  a.npe = c->npe;
   a.coef = c->d_coef;
   a.nodal_f = c->d_f;
   a.cmask = hier3_masks(c) ? c->d_cmask : nullptr;
@@ -259,6 +275,12 @@ void launch_hier3(lmg_ctx *c, bool mixed) {
   if (c->tab.n == 20) {
     if (mixed) k_elem_pattern<20, 14, true><<<grid, H3T, 0, c->stream>>>(a);
     else k_elem_pattern<20, 14, false><<<grid, H3T, 0, c->stream>>>(a);
+  } else if (c->tab.n == 18) {
+    if (mixed) k_elem_pattern<18, 6, true><<<grid, H3T, 0, c->stream>>>(a);
+    else k_elem_pattern<18, 6, false><<<grid, H3T, 0, c->stream>>>(a);
+  } else if (c->tab.n == 40) {
+    if (mixed) k_elem_pattern<40, 6, true><<<grid, H3T, 0, c->stream>>>(a);
+    else k_elem_pattern<40, 6, false><<<grid, H3T, 0, c->stream>>>(a);
   } else {
     if (mixed) k_elem_pattern<64, 27, true><<<grid, H3T, 0, c->stream>>>(a);
     else k_elem_pattern<64, 27, false><<<grid, H3T, 0, c->stream>>>(a);

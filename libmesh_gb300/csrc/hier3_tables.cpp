@@ -343,4 +343,270 @@ std::string build_tet3_tables(Hier3Tables &h, int q_order, int64_t n_elem, const
   return "";
 }
 
+// ------------------------------------------------------------------ prisms
+// HIERARCHIC of order 2 on PRISM18 and order 3 on PRISM21.  libMesh forms
+// shape i of a prism (fe_hierarchic_shape_3D.C:2290-2345, prism_indices
+// :764-1150) as a 2-D HIERARCHIC triangle shape of (xi, eta) times a 1-D
+// HIERARCHIC shape of zeta, after moving the coordinates of the quadrilateral
+// faces' bases by the face's orientation, and negates odd triangle-edge bases
+// on the bottom and top triangles by the edge's direction.  An element's
+// orientation record holds every decision that evaluation makes; the shapes
+// of a record are tabulated once (value and central-difference gradient,
+// eps = 1e-6, evaluated operation for operation as the reference does so the
+// difference quotients are its bits) and shared by the elements that have it.
+namespace {
+
+struct PrismOrient {
+  uint8_t zflip[3] = {};     // vertical edge 3 + v: its 1-D bases take -zeta (positive_edge_orientation)
+  uint8_t fcase[3] = {};     // quad face 1 + f: 2 * (rank of its minimum vertex in the test order) + positive
+  uint8_t tflip[2][3] = {};  // bottom / top triangle edge t: odd bases negated
+  uint32_t key() const {
+    uint32_t k = 0;
+    for (int v = 0; v < 3; ++v) k = (k << 1) | zflip[v];
+    for (int f = 0; f < 3; ++f) k = (k << 3) | fcase[f];
+    for (int b = 0; b < 2; ++b)
+      for (int t = 0; t < 3; ++t) k = (k << 1) | tflip[b][t];
+    return k;
+  }
+};
+
+// Prism6 side and edge maps (cell_prism6.C:113-142) for the faces and edges used.
+const int PR_QUAD[3][4] = {{0, 1, 4, 3}, {1, 2, 5, 4}, {2, 0, 3, 5}};
+const int PR_MINTEST[3][4] = {{0, 3, 1, 4}, {1, 4, 2, 5}, {2, 5, 0, 3}};  // order of the == min_point tests
+const int PR_SQ_ROW[4] = {0, 1, 1, 0}, PR_SQ_COL[4] = {0, 0, 1, 1};     // square_number_row / _column
+const int PR_INT_PAGE[2] = {0, 1};                                       // prism_number_page (triangle index 0)
+
+PrismOrient prism_orient(const double (*X)[3]) {
+  PrismOrient o;
+  for (int v = 0; v < 3; ++v) o.zflip[v] = pt_less(X[v + 3], X[v]);  // edge (v, v + 3): first vertex greater
+  for (int f = 0; f < 3; ++f) {
+    const int *q = PR_QUAD[f];
+    // std::min(std::min(a, b), std::min(c, d)) over the face's vertices in get_min_point's argument order
+    auto mn = [&](const double *a, const double *b) { return pt_less(b, a) ? b : a; };
+    const int *t = PR_MINTEST[f];
+    const double *m = mn(mn(X[q[0]], X[q[1]]), mn(X[q[3]], X[q[2]]));
+    int v = 0;
+    for (int k = 1; k < 4; ++k)
+      if (pt_less(X[q[k]], X[q[v]])) v = k;
+    const bool pos = pt_less(X[q[(v + 3) % 4]], X[q[(v + 1) % 4]]);
+    int rank = 0;
+    while (rank < 4 && !pt_eq(X[t[rank]], m)) ++rank;
+    o.fcase[f] = (uint8_t)(2 * rank + (pos ? 1 : 0));
+  }
+  for (int b = 0; b < 2; ++b)
+    for (int k = 0; k < 3; ++k) o.tflip[b][k] = pt_less(X[3 * b + (k + 1) % 3], X[3 * b + k]);
+  return o;
+}
+
+// HIERARCHIC triangle shape i01 at (x, y); edge bases of odd order negated
+// when `flip` has the edge's bit (fe_hierarchic_shape_2D.C:915-1026).
+double prism_tri(int order, int i01, double x, double y, const uint8_t *flip) {
+  const double zeta1 = x, zeta2 = y, zeta0 = 1. - zeta1 - zeta2;
+  if (i01 == 0) return zeta0;
+  if (i01 == 1) return zeta1;
+  if (i01 == 2) return zeta2;
+  double num, cross;
+  int bo, t;
+  if (i01 < order + 2) {
+    bo = i01 - 1; t = 0; num = zeta1 - zeta0; cross = zeta0 + zeta1;
+  } else if (i01 < 2 * order + 1) {
+    bo = i01 - order; t = 1; num = zeta2 - zeta1; cross = zeta2 + zeta1;
+  } else if (i01 < 3 * order) {
+    bo = i01 - 2 * order + 1; t = 2; num = zeta0 - zeta2; cross = zeta0 + zeta2;
+  } else {  // the first interior basis: zeta0 zeta1 zeta2
+    double r = 1;
+    r *= zeta0;
+    r *= zeta1;
+    r *= zeta2;
+    return r;
+  }
+  if (cross == 0.) {
+    unsigned fact = 1;
+    for (int n = 2; n <= bo; ++n) fact *= (unsigned)n;
+    return std::pow(num, bo) / fact;
+  }
+  const double sgn = (bo % 2 && flip && flip[t]) ? -1. : 1.;
+  return sgn * std::pow(cross, bo) * h1(bo, num / cross);
+}
+
+// Shape i of a prism with record o at reference point p.
+double prism_shape(const PrismOrient &o, int order, int i, const double *p) {
+  const int e = order - 1;
+  double xi = p[0], eta = p[1], zeta = p[2];
+  const double xs = xi, es = eta, zs = zeta;
+  int i01, i2;
+  const uint8_t *flip = nullptr;  // triangle-edge flips apply to the bottom and top triangles' bases only
+  if (i < 6) {
+    i01 = i % 3;
+    i2 = i / 3;
+  } else if (i < 6 + 3 * e) {
+    i01 = i - 3;
+    i2 = 0;
+  } else if (i < 6 + 6 * e) {
+    i01 = (i - 6 - 3 * e) / e;
+    i2 = (i - 6 - 3 * e) % e + 2;
+    if (o.zflip[i01]) zeta = -zeta;
+  } else if (i < 6 + 9 * e) {
+    i01 = i - 3 - 6 * e;
+    i2 = 1;
+  } else if (i < 6 + 9 * e + 3 * e * e) {
+    const int f = (i - 6 - 9 * e) / (e * e), b = (i - 6 - 9 * e) % (e * e);
+    const int s0 = PR_SQ_ROW[b] + 2, s1 = PR_SQ_COL[b] + 2, c = o.fcase[f];
+    const bool swap = c == 1 || c == 2 || c == 4 || c == 7;
+    // triangle edge f numbering; face 2's first case takes index s0 + 1 + 3 as the reference does
+    const int off = f == 0 ? 0 : (f == 1 ? (c == 0 ? 3 : e) : 2 * e);
+    i01 = (swap ? s1 : s0) + 1 + off;
+    i2 = swap ? s0 : s1;
+    double xsc, xf;
+    if (f == 0) {
+      xsc = 1 - es;
+      xf = (xsc == 0) ? 0 : xs / xsc;
+    } else if (f == 1) {
+      xsc = xs + es;
+      xf = (xsc == 0) ? 0 : xs / xsc;
+    } else {
+      xsc = 1 - xs;
+      xf = (xsc == 0) ? 0 : (xsc - es) / xsc;
+    }
+    // the in-face coordinate that runs along the triangle edge, set from v
+    auto along = [&](double v) {
+      if (f == 1) {
+        eta = v * xsc;
+        xi = xsc - eta;
+      } else {
+        eta = xsc - v * xsc;
+      }
+    };
+    switch (c) {
+      case 1:
+        zeta = 2 * xf - 1;
+        if (f == 0) xi = (zs + 1) * xsc / 2; else along((zs + 1) / 2);
+        break;
+      case 2:
+        zeta = 1 - 2 * xf;
+        if (f == 0) xi = (zs + 1) * xsc / 2; else along((zs + 1) / 2);
+        break;
+      case 3:
+        zeta = -zs;
+        break;
+      case 4:
+        zeta = 2 * xf - 1;
+        if (f == 0) xi = (1 - zs) * xsc / 2; else along((1 - zs) / 2);
+        break;
+      case 5:
+        if (f == 0) xi = (1 - xf) * xsc; else along(1 - xf);
+        break;
+      case 6:
+        zeta = -zs;
+        if (f == 0) xi = (1 - xf) * xsc; else along(1 - xf);
+        break;
+      case 7:
+        zeta = 1 - 2 * xf;
+        if (f == 0) xi = (1 - zs) * xsc / 2; else along((1 - zs) / 2);
+        break;
+      default: break;
+    }
+  } else if (i < 6 + 9 * e + 3 * e * e + e * (e - 1) / 2) {
+    i01 = i - 3 - 6 * e - 3 * e * e;
+    i2 = 0;
+  } else if (i < 6 + 9 * e + 3 * e * e + e * (e - 1)) {
+    i01 = i - 3 - 6 * e - 3 * e * e - e * (e - 1) / 2;
+    i2 = 1;
+  } else {
+    const int b = i - 6 - 9 * e - 3 * e * e - e * (e - 1);
+    i01 = 3 + 3 * e;  // prism_number_triangle = 0 for the first bases
+    i2 = PR_INT_PAGE[b] + 2;
+  }
+  if (i2 < 2) flip = o.tflip[i2];
+  return prism_tri(order, i01, xi, eta, flip) * h1(i2, zeta);
+}
+
+}  // namespace
+
+// HIERARCHIC prisms (order 2 on PRISM18, 3 on PRISM21), affine elements:
+// patterns are the elements' orientation records; per pattern the shapes at
+// the quadrature points, D_k and M as for the cubic tets.  The map and the
+// nodal load use the six vertices with the PRISM6 LAGRANGE basis (the same
+// affine map as the elements' own 18- / 21-node bases, up to rounding).
+std::string build_prism_tables(Hier3Tables &h, int order, int q_order, int64_t n_elem, const double *xyz,
+                               const int32_t *conn, int npe) {
+  if (order != 2 && order != 3) return "HIERARCHIC prisms are built for orders 2 and 3";
+  h = Hier3Tables();
+  const int N = (order + 1) * (order + 1) * (order + 2) / 2, G = 6;
+  h.N = N;
+  h.G = G;
+  FETables geo;
+  std::string err = build_fe_tables(geo, LMG_PRISM6, 1, q_order, 0);  // QGauss and the PRISM6 map basis
+  if (!err.empty()) return err;
+  if (geo.n_geo != G) return "PRISM6 map basis";
+  const int Q = geo.q;
+  h.q = Q;
+  h.gd0.assign(geo.gdphi.begin(), geo.gdphi.begin() + G * 3);
+  std::unordered_map<uint32_t, int> id;
+  std::vector<PrismOrient> pats;
+  std::vector<int> pid((size_t)n_elem);
+  double X[6][3];
+  for (int64_t e = 0; e < n_elem; ++e) {
+    for (int a = 0; a < 6; ++a)
+      for (int d = 0; d < 3; ++d) X[a][d] = xyz[3 * (int64_t)conn[e * npe + a] + d];
+    const PrismOrient o = prism_orient(X);
+    auto it = id.find(o.key());
+    if (it == id.end()) {
+      it = id.emplace(o.key(), (int)pats.size()).first;
+      pats.push_back(o);
+    }
+    pid[(size_t)e] = it->second;
+  }
+  h.P = (int)pats.size();
+  h.Dp.assign((size_t)h.P * 6 * N * N, 0.0);
+  h.Mp.assign((size_t)h.P * N * G, 0.0);
+  std::vector<double> v((size_t)Q * N), g((size_t)Q * N * 3);
+  const double eps = 1.e-6;
+  for (int pp = 0; pp < h.P; ++pp) {
+    const PrismOrient &o = pats[(size_t)pp];
+    for (int q = 0; q < Q; ++q)
+      for (int i = 0; i < N; ++i) {
+        const double *x = &geo.qp[3 * q];
+        v[(size_t)q * N + i] = prism_shape(o, order, i, x);
+        for (int j = 0; j < 3; ++j) {
+          double xp[3] = {x[0], x[1], x[2]}, xm[3] = {x[0], x[1], x[2]};
+          xp[j] += eps;
+          xm[j] -= eps;
+          g[((size_t)q * N + i) * 3 + j] = (prism_shape(o, order, i, xp) - prism_shape(o, order, i, xm)) / 2. / eps;
+        }
+      }
+    double *D = &h.Dp[(size_t)pp * 6 * N * N];
+    double *M = &h.Mp[(size_t)pp * N * G];
+    for (int i = 0; i < N; ++i)
+      for (int j = 0; j < N; ++j) {
+        double S[3][3] = {};
+        for (int q = 0; q < Q; ++q)
+          for (int m = 0; m < 3; ++m)
+            for (int n = 0; n < 3; ++n)
+              S[m][n] += geo.qw[q] * g[((size_t)q * N + i) * 3 + m] * g[((size_t)q * N + j) * 3 + n];
+        const double d6[6] = {S[0][0], S[1][1], S[2][2], S[0][1] + S[1][0], S[0][2] + S[2][0], S[1][2] + S[2][1]};
+        for (int k = 0; k < 6; ++k) D[(size_t)k * N * N + i * N + j] = d6[k];
+      }
+    for (int i = 0; i < N; ++i)
+      for (int gg = 0; gg < G; ++gg) {
+        double m = 0.0;
+        for (int q = 0; q < Q; ++q) m += geo.qw[q] * v[(size_t)q * N + i] * geo.gphi[(size_t)q * G + gg];
+        M[i * G + gg] = m;
+      }
+  }
+  h.order.resize((size_t)n_elem);
+  for (int64_t e = 0; e < n_elem; ++e) h.order[(size_t)e] = (int32_t)e;
+  std::stable_sort(h.order.begin(), h.order.end(), [&](int32_t a, int32_t b) { return pid[(size_t)a] < pid[(size_t)b]; });
+  for (int64_t i = 0; i < n_elem;) {
+    const int p = pid[(size_t)h.order[(size_t)i]];
+    int64_t j = i;
+    while (j < n_elem && j - i < 8 && pid[(size_t)h.order[(size_t)j]] == p) ++j;
+    h.batch.push_back(p);
+    h.batch.push_back((int32_t)i);
+    h.batch.push_back((int32_t)(j - i));
+    i = j;
+  }
+  return "";
+}
+
 }  // namespace lmg

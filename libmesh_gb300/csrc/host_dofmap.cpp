@@ -323,16 +323,21 @@ lmg_status lmg_dofmap_distribute(int64_t n_nodes, int64_t n_elem, int32_t npe, c
 // dofs last to first (extra_hanging_dofs, dof_map.h:2685-2712).
 // On TET14 (HIERARCHIC_n_dofs_at_node, fe_hierarchic.C:440-470) a vertex
 // carries 1 dof, an edge node 2, a face node 1, and no dof is the element's.
+// On PRISM21 (HIERARCHIC_n_dofs_at_node, fe_hierarchic.C:289-340) a vertex
+// carries 1 dof, an edge node 2, a quadrilateral-face node 4, a triangle-face
+// node 1 and the interior node 20 the element's 2; no dof is the element's.
 struct P3Layout {
   int npe, nl, n_interior, nsides;
   int node_dofs(int a) const {
     if (npe == 27) return a < 8 ? 1 : (a < 20 ? 2 : (a < 26 ? 4 : 0));
+    if (npe == 21) return a < 6 ? 1 : (a < 15 ? 2 : (a < 18 ? 4 : (a < 20 ? 1 : 2)));
     return a < 4 ? 1 : (a < 10 ? 2 : 1);
   }
 };
 static bool p3_layout(int32_t elem_type, P3Layout &l) {
   if (elem_type == LMG_HEX27) l = {27, 64, 8, 6};
   else if (elem_type == LMG_TET14) l = {14, 20, 0, 4};
+  else if (elem_type == LMG_PRISM21) l = {21, 40, 0, 5};
   else return false;
   return true;
 }

@@ -39,6 +39,14 @@ static const int TET14_SIDES[4][7] = {
     {0, 2, 1, 6, 5, 4, 10}, {0, 1, 3, 4, 8, 7, 11}, {1, 2, 3, 5, 9, 8, 12}, {2, 0, 3, 6, 7, 9, 13}};
 // PRISM6 sides (cell_prism6.C side_nodes_map): two triangles, three quads.
 static const int PRISM6_SIDES[5][4] = {{0, 2, 1, -1}, {0, 1, 4, 3}, {1, 2, 5, 4}, {2, 0, 3, 5}, {3, 4, 5, -1}};
+// PRISM18 / PRISM21 sides (cell_prism18.C, cell_prism21.C side_nodes_map): the
+// triangles with their mid-edge nodes (and face node 18 / 19 on PRISM21), the
+// quadrilaterals with mid-edge nodes and face node.
+static const int PRISM21_SIDES[5][9] = {{0, 2, 1, 8, 7, 6, 18, -1, -1},
+                                        {0, 1, 4, 3, 6, 10, 12, 9, 15},
+                                        {1, 2, 5, 4, 7, 11, 13, 10, 16},
+                                        {2, 0, 3, 5, 8, 9, 14, 11, 17},
+                                        {3, 4, 5, 12, 13, 14, 19, -1, -1}};
 // Vertices adjacent to TET10 mid-edge nodes 4..9 (cell_tet10.C _second_order_adjacent_vertices).
 static const int TET10_EDGE_VERTS[6][2] = {{0, 1}, {1, 2}, {0, 2}, {0, 3}, {1, 3}, {2, 3}};
 
@@ -50,6 +58,8 @@ int nodes_per_elem(int t) {
     case LMG_HEX8: return 8;
     case LMG_HEX27: return 27;
     case LMG_PRISM6: return 6;
+    case LMG_PRISM18: return 18;
+    case LMG_PRISM21: return 21;
     default: return 0;
   }
 }
@@ -57,7 +67,7 @@ int sides_per_elem(int t) {
   switch (t) {
     case LMG_TET4: case LMG_TET10: case LMG_TET14: return 4;
     case LMG_HEX8: case LMG_HEX27: return 6;
-    case LMG_PRISM6: return 5;
+    case LMG_PRISM6: case LMG_PRISM18: case LMG_PRISM21: return 5;
     default: return 0;
   }
 }
@@ -65,7 +75,7 @@ int vertices_per_elem(int t) {
   switch (t) {
     case LMG_TET4: case LMG_TET10: case LMG_TET14: return 4;
     case LMG_HEX8: case LMG_HEX27: return 8;
-    case LMG_PRISM6: return 6;
+    case LMG_PRISM6: case LMG_PRISM18: case LMG_PRISM21: return 6;
     default: return 0;
   }
 }
@@ -79,6 +89,12 @@ int side_nodes(int t, int s, int *out) {
     case LMG_PRISM6: {
       const int k = (s == 0 || s == 4) ? 3 : 4;
       for (int i = 0; i < k; ++i) out[i] = PRISM6_SIDES[s][i];
+      return k;
+    }
+    case LMG_PRISM18:
+    case LMG_PRISM21: {
+      const int k = (s == 0 || s == 4) ? (t == LMG_PRISM21 ? 7 : 6) : 9;
+      for (int i = 0; i < k; ++i) out[i] = PRISM21_SIDES[s][i];
       return k;
     }
     default: return 0;
@@ -148,11 +164,87 @@ static std::string build_cube_prism6(HostMesh &m, int nx, int ny, int nz) {
   return "";
 }
 
+// PRISM18 / PRISM21 build_cube (mesh_generation.C:1324-1377, 1634-1745): the
+// doubled node grid, for PRISM21 followed by two triangle-centre nodes per grid
+// cell on each of the 2 nz + 1 levels, at ((i + 1/3) / nx, (j + 1/3) / ny) and
+// ((i + 2/3) / nx, (j + 2/3) / ny); two prisms per cell as for PRISM6, with
+// their mid-edge nodes, quad-face nodes and (PRISM21) triangle-face and
+// interior nodes taken from the grid.
+static std::string build_cube_prism_hi(HostMesh &m, int nx, int ny, int nz, int type) {
+  const int64_t gx = 2 * (int64_t)nx + 1, gy = 2 * (int64_t)ny + 1, gz = 2 * (int64_t)nz + 1;
+  const bool p21 = type == LMG_PRISM21;
+  const int npe = p21 ? 21 : 18;
+  m.elem_type = type;
+  m.npe = npe;
+  m.nsides = 5;
+  const int64_t n_grid = gx * gy * gz, n_tri = p21 ? gz * (int64_t)nx * ny * 2 : 0;
+  m.xyz.resize((size_t)(n_grid + n_tri) * 3);
+  for (int64_t k = 0; k < gz; ++k)
+    for (int64_t j = 0; j < gy; ++j)
+      for (int64_t i = 0; i < gx; ++i) {
+        const int64_t id = grid_idx(gx, gy, i, j, k);
+        m.xyz[3 * id + 0] = (double)i / (double)(2 * nx) * (1.0 - 0.0) + 0.0;
+        m.xyz[3 * id + 1] = (double)j / (double)(2 * ny) * (1.0 - 0.0) + 0.0;
+        m.xyz[3 * id + 2] = (double)k / (double)(2 * nz) * (1.0 - 0.0) + 0.0;
+      }
+  if (p21) {
+    const double kmax = (double)(2 * nz);
+    int64_t id = n_grid;
+    for (int64_t k = 0; k < gz; ++k)
+      for (int64_t j = 0; j < ny; ++j)
+        for (int64_t i = 0; i < nx; ++i)
+          for (int t = 1; t <= 2; ++t, ++id) {
+            const double third = (double)t / 3.0;
+            m.xyz[3 * id + 0] = ((double)i + third) / (double)nx * (1.0 - 0.0) + 0.0;
+            m.xyz[3 * id + 1] = ((double)j + third) / (double)ny * (1.0 - 0.0) + 0.0;
+            m.xyz[3 * id + 2] = (double)k / kmax * (1.0 - 0.0) + 0.0;
+          }
+  }
+  const int64_t E = 2 * (int64_t)nx * ny * nz;
+  m.conn.resize((size_t)(E * npe));
+  m.side_bid.assign((size_t)(E * 5), (int8_t)-1);
+  // grid offsets (i, j, k) of nodes 0..17 of the first and second prism of a cell
+  static const int A[18][3] = {{0, 0, 0}, {2, 0, 0}, {0, 2, 0}, {0, 0, 2}, {2, 0, 2}, {0, 2, 2},
+                               {1, 0, 0}, {1, 1, 0}, {0, 1, 0}, {0, 0, 1}, {2, 0, 1}, {0, 2, 1},
+                               {1, 0, 2}, {1, 1, 2}, {0, 1, 2}, {1, 0, 1}, {1, 1, 1}, {0, 1, 1}};
+  static const int B[18][3] = {{2, 0, 0}, {2, 2, 0}, {0, 2, 0}, {2, 0, 2}, {2, 2, 2}, {0, 2, 2},
+                               {2, 1, 0}, {1, 2, 0}, {1, 1, 0}, {2, 0, 1}, {2, 2, 1}, {0, 2, 1},
+                               {2, 1, 2}, {1, 2, 2}, {1, 1, 2}, {2, 1, 1}, {1, 2, 1}, {1, 1, 1}};
+  int64_t e = 0;
+  for (int k = 0; k < 2 * nz; k += 2)
+    for (int j = 0; j < 2 * ny; j += 2)
+      for (int i = 0; i < 2 * nx; i += 2)
+        for (int second = 0; second < 2; ++second, ++e) {
+          const int (*off)[3] = second ? B : A;
+          int32_t *c = &m.conn[(size_t)(e * npe)];
+          for (int a = 0; a < 18; ++a) c[a] = (int32_t)grid_idx(gx, gy, i + off[a][0], j + off[a][1], k + off[a][2]);
+          if (p21) {  // triangle-face nodes 18 (bottom), 19 (top) and interior node 20
+            const int64_t cell = (int64_t)(j / 2) * nx + i / 2;
+            c[18] = (int32_t)(n_grid + ((int64_t)k * nx * ny + cell) * 2 + second);
+            c[19] = (int32_t)(n_grid + ((int64_t)(k + 2) * nx * ny + cell) * 2 + second);
+            c[20] = (int32_t)(n_grid + ((int64_t)(k + 1) * nx * ny + cell) * 2 + second);
+          }
+          int8_t *sb = &m.side_bid[(size_t)(e * 5)];
+          if (!second) {
+            if (i == 0) sb[3] = 4;
+            if (j == 0) sb[1] = 1;
+          } else {
+            if (i == 2 * (nx - 1)) sb[1] = 2;
+            if (j == 2 * (ny - 1)) sb[2] = 3;
+          }
+          if (k == 0) sb[0] = 0;
+          if (k == 2 * (nz - 1)) sb[4] = 5;
+        }
+  renumber_nodes_first_touch(m);
+  return "";
+}
+
 std::string build_cube_hex(HostMesh &m, int nx, int ny, int nz, int type) {
   if (nx <= 0 || ny <= 0 || nz <= 0) return "build_cube: nx, ny, nz must be positive";
-  if (type != LMG_HEX8 && type != LMG_HEX27 && type != LMG_PRISM6)
-    return "build_cube: type must be HEX8, HEX27 or PRISM6";
+  if (type != LMG_HEX8 && type != LMG_HEX27 && type != LMG_PRISM6 && type != LMG_PRISM18 && type != LMG_PRISM21)
+    return "build_cube: type must be HEX8, HEX27, PRISM6, PRISM18 or PRISM21";
   if (type == LMG_PRISM6) return build_cube_prism6(m, nx, ny, nz);
+  if (type == LMG_PRISM18 || type == LMG_PRISM21) return build_cube_prism_hi(m, nx, ny, nz, type);
   const int f = (type == LMG_HEX8) ? 1 : 2;  // grid refinement factor
   const int64_t gx = (int64_t)f * nx + 1, gy = (int64_t)f * ny + 1, gz = (int64_t)f * nz + 1;
   m.elem_type = type;

@@ -251,8 +251,10 @@ lmg_status lmg_mesh_cube(int32_t nx, int32_t ny, int32_t nz, int32_t elem_type, 
     const bool tets = (elem_type == LMG_TET4 || elem_type == LMG_TET10 || elem_type == LMG_TET14);
     const int base = tets ? LMG_HEX8 : elem_type;
     std::string err = lmg::build_cube_hex(mesh->m, nx, ny, nz, base);
+    const bool prism_hi = elem_type == LMG_PRISM18 || elem_type == LMG_PRISM21;
+    if (err.empty() && prism_hi && jitter != 0.0) err = "build_cube: PRISM18 / PRISM21 meshes are not jittered";
     if (err.empty()) lmg::jitter_interior(mesh->m, jitter, nx, ny, nz, seed);
-    if (err.empty() && !tets && elem_type != LMG_PRISM6 && jitter == 0.0) {  // unjittered hex cube: lattice for refinement
+    if (err.empty() && !tets && elem_type != LMG_PRISM6 && !prism_hi && jitter == 0.0) {  // unjittered hex cube: lattice for refinement
       mesh->m.cube[0] = nx;
       mesh->m.cube[1] = ny;
       mesh->m.cube[2] = nz;
@@ -262,7 +264,7 @@ lmg_status lmg_mesh_cube(int32_t nx, int32_t ny, int32_t nz, int32_t elem_type, 
     if (err.empty() && elem_type == LMG_TET14) err = lmg::all_complete_order_tet4(mesh->m);
     if (!err.empty()) {
       delete mesh;
-      return (elem_type == LMG_HEX8 || elem_type == LMG_HEX27 || elem_type == LMG_PRISM6 || tets)
+      return (elem_type == LMG_HEX8 || elem_type == LMG_HEX27 || elem_type == LMG_PRISM6 || prism_hi || tets)
                  ? LMG_ERR_ARG
                  : LMG_ERR_UNSUPPORTED;
     }

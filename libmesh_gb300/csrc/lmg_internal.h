@@ -158,6 +158,11 @@ TetOrient tet_orient(const double *X /* [4][3] vertex coordinates */);
 // values [20] and reference gradients [20][3] (central differences, eps = 1e-6)
 int hier_tet3_shapes(const TetOrient &o, const double *p, double *v, double *g);
 std::string build_tet3_tables(Hier3Tables &h, int q_order, int64_t n_elem, const double *xyz, const int32_t *conn);
+// HIERARCHIC of order 2 on PRISM18 or 3 on PRISM21 (npe = 18 / 21 nodes per
+// connectivity row): the same tables over the elements' orientation records,
+// with the six vertices' PRISM6 basis for the map and the load.
+std::string build_prism_tables(Hier3Tables &h, int order, int q_order, int64_t n_elem, const double *xyz,
+                               const int32_t *conn, int npe);
 
 // libMesh Elem::has_affine_map for one element (cell_hex8.C:121, cell_hex27.C:125,
 // cell_tet4 always, cell_tet10.C:143).

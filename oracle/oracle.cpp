@@ -30,7 +30,7 @@
 
 namespace {
 
-enum { TET4 = 8, TET10 = 9, HEX8 = 10, HEX27 = 12, PRISM6 = 13, TET14 = 34 };
+enum { TET4 = 8, TET10 = 9, HEX8 = 10, HEX27 = 12, PRISM6 = 13, PRISM18 = 15, TET14 = 34, PRISM21 = 36 };
 enum { POISSON = 0, ELASTICITY = 1 };
 
 // libMesh's _R literal: a long double literal narrowed to Real
@@ -136,7 +136,7 @@ void qgauss_tri(int order, std::vector<double> &x, std::vector<double> &y, std::
 
 bool qgauss_3d(int type, int order, std::vector<Pt> &P, std::vector<double> &W) {
   P.clear(); W.clear();
-  if (type == PRISM6) {  // quadrature_gauss_3D.C:507-525, tensor_product_prism (quadrature.C:310-331)
+  if (type == PRISM6 || type == PRISM18 || type == PRISM21) {  // quadrature_gauss_3D.C:507-525, tensor_product_prism (quadrature.C:310-331)
     if (order > 5) return false;
     std::vector<double> z, wz, tx, ty, tw;
     qgauss_1d(order, z, wz);
@@ -985,22 +985,30 @@ struct OracleFE {
   std::vector<std::vector<Pt>> dphi;                  // dphi[i][q]
 
   int family = 0;  // 0 LAGRANGE, 1 HIERARCHIC (order <= 2)
+  bool prism_hi = false;  // HIERARCHIC order 2 on PRISM18 / 3 on PRISM21
   bool init(int type_, int order_, int q_order, int family_ = 0) {
     family = family_;
     type = type_; order = order_;
     if (!qgauss_3d(type, q_order, qp, qw)) return false;
     nq = (int)qp.size();
-    const bool p3 = family == 1 && ((order == 3 && (type == HEX27 || type == TET14)) || (order == 2 && type == HEX27));
-    n = p3 ? (type == HEX27 ? (order + 1) * (order + 1) * (order + 1) : 20) : n_shapes(type, order);
+    prism_hi = family == 1 && ((order == 2 && type == PRISM18) || (order == 3 && type == PRISM21));
+    const bool p3 = prism_hi ||
+                    (family == 1 && ((order == 3 && (type == HEX27 || type == TET14)) || (order == 2 && type == HEX27)));
+    n = prism_hi ? (order + 1) * (order + 1) * (order + 2) / 2
+                 : (p3 ? (type == HEX27 ? (order + 1) * (order + 1) * (order + 1) : 20) : n_shapes(type, order));
+    // PRISM18 / PRISM21 (affine only): the map and the load interpolation by
+    // the six vertices' PRISM6 basis -- the same affine Jacobian as their own
+    // 18- / 21-node bases up to rounding
+    const int geo_type = prism_hi ? PRISM6 : type;
     const int geo_order = (type == HEX27 || type == TET10) ? 2 : (type == TET14 ? 3 : 1);
-    n_geo = n_shapes(type, geo_order);
+    n_geo = n_shapes(geo_type, geo_order);
     if (!n || !n_geo) return false;
     if (p3) {  // element-dependent: filled by orient() per element
       phi.assign(n, std::vector<double>(nq));
       for (int c = 0; c < 3; ++c) dref[c].assign(n, std::vector<double>(nq));
     } else if (family == 1) all_shapes_hierarchic(type, order, qp, phi, dref);
     else all_shapes(type, order, qp, phi, dref);
-    all_shapes(type, geo_order, qp, phi_map, dmap);
+    all_shapes(geo_type, geo_order, qp, phi_map, dmap);
     JxW.assign(nq, 0); jac.assign(nq, 0);
     for (auto &g : G) g.assign(nq, 0);
     dphi.assign(n, std::vector<Pt>(nq));
@@ -1042,6 +1050,14 @@ struct OracleFE {
   // recomputed for every element (fe.C:174-192 re-inits when the cached
   // element does not match).
   void orient(const std::vector<Pt> &X) {
+    if (prism_hi) {
+      for (int q = 0; q < nq; ++q)
+        for (int i = 0; i < n; ++i) {
+          phi[i][q] = prism::shape(X, (unsigned)order, i, qp[q]);
+          for (int c = 0; c < 3; ++c) dref[c][i][q] = prism::deriv(X, (unsigned)order, i, c, qp[q]);
+        }
+      return;
+    }
     if (!(family == 1 && ((order == 3 && (type == HEX27 || type == TET14)) || (order == 2 && type == HEX27)))) return;
     const bool tet = type == TET14;
     for (int q = 0; q < nq; ++q)
@@ -1054,7 +1070,7 @@ struct OracleFE {
 
   bool reinit(const std::vector<Pt> &X) {
     bool ok = true;
-    if (has_affine_map(type, X)) {  // compute_affine_map, fe_map.C:1167-1245
+    if (has_affine_map(prism_hi ? PRISM6 : type, X)) {  // compute_affine_map, fe_map.C:1167-1245
       ok = single_point_map(X, 0);
       for (int p = 1; p < nq; ++p) {
         for (int k = 0; k < 9; ++k) G[k][p] = G[k][0];
@@ -1212,7 +1228,7 @@ bool element_matrix(const Problem &P, OracleFE &fe, int64_t e, Dense &Ke, std::v
       for (int v = 0; v < P.n_vars; ++v) f[a * P.n_vars + v] = P.nodal_f[(int64_t)P.conn[e * P.npe + a] * P.n_vars + v];
   // More shapes than nodes (HIERARCHIC cubic on HEX27): the nodal load is
   // interpolated by the mapping basis, f(x_q) = sum_g phi_map_g(q) f_g.
-  const bool geo_load = n != P.npe;
+  const bool geo_load = n != P.npe || fe.prism_hi;
   std::vector<double> fq(fe.nq, 0.0);
   if (P.nodal_f && geo_load)
     for (int qp = 0; qp < fe.nq; qp++)
@@ -1557,6 +1573,70 @@ int orc_dirichlet_tet3(int64_t n_elem, const int32_t *elem_dofs, const int8_t *s
   return 0;
 }
 
+// HIERARCHIC of order p = 2 on PRISM18 or p = 3 on PRISM21
+// (HIERARCHIC_n_dofs_at_node, fe_hierarchic.C:289-340; no element dofs,
+// fe_hierarchic.C:433-439): vertex 1, edge node p - 1, quad-face node
+// (p - 1)^2, triangle-face node (p - 1)(p - 2)/2, interior node 20 of PRISM21
+// (p - 1)^2 (p - 2)/2; first-touch numbering per element, dof_indices listing
+// a non-vertex node's dofs last to first.
+static int prism_node_dofs(int p, int n) {
+  if (n < 6) return 1;
+  if (n < 15) return p - 1;
+  if (n < 18) return (p - 1) * (p - 1);
+  if (n < 20) return (p - 1) * (p - 2) / 2;
+  return (p - 1) * (p - 1) * (p - 2) / 2;
+}
+
+int orc_distribute_dofs_prism(int p, int64_t n_nodes, int64_t n_elem, const int32_t *conn, int32_t *elem_dofs,
+                              int64_t *n_dofs) {
+  const int npe = p == 2 ? 18 : 21, nl = (p + 1) * (p + 1) * (p + 2) / 2;
+  std::vector<int64_t> base(n_nodes, -1);
+  int64_t next_free_dof = 0;
+  for (int64_t e = 0; e < n_elem; ++e)
+    for (int n = 0; n < npe; ++n) {
+      const int32_t node = conn[e * npe + n];
+      if (prism_node_dofs(p, n) > 0 && base[node] == -1) {
+        base[node] = next_free_dof;
+        next_free_dof += prism_node_dofs(p, n);
+      }
+    }
+  *n_dofs = next_free_dof;
+  for (int64_t e = 0; e < n_elem; ++e) {
+    int32_t *d = elem_dofs + e * nl;
+    int k = 0;
+    for (int n = 0; n < npe; ++n) {
+      const int nc = prism_node_dofs(p, n);
+      const int64_t b = base[conn[e * npe + n]];
+      if (n < 6) {
+        for (int i = 0; i < nc; ++i) d[k++] = (int32_t)(b + i);
+      } else {
+        for (int i = nc - 1; i >= 0; --i) d[k++] = (int32_t)(b + i);
+      }
+    }
+  }
+  return 0;
+}
+
+int orc_dirichlet_prism(int p, int64_t n_elem, const int32_t *elem_dofs, const int8_t *side_bid, const int32_t *bids,
+                        int n_bids, uint8_t *constrained) {
+  // cell_prism21.C side_nodes_map (PRISM18: the same without nodes 18, 19)
+  static const int P21[5][9] = {{0, 2, 1, 8, 7, 6, 18, -1, -1}, {0, 1, 4, 3, 6, 10, 12, 9, 15},
+                                {1, 2, 5, 4, 7, 11, 13, 10, 16}, {2, 0, 3, 5, 8, 9, 14, 11, 17},
+                                {3, 4, 5, 12, 13, 14, 19, -1, -1}};
+  const int npe = p == 2 ? 18 : 21, nl = (p + 1) * (p + 1) * (p + 2) / 2;
+  int first[21];
+  for (int n = 0, k = 0; n < npe; ++n) { first[n] = k; k += prism_node_dofs(p, n); }
+  for (int64_t e = 0; e < n_elem; ++e)
+    for (int s = 0; s < 5; ++s) {
+      const int b = side_bid[e * 5 + s];
+      if (b < 0 || std::find(bids, bids + n_bids, b) == bids + n_bids) continue;
+      for (int a : P21[s])
+        if (a >= 0 && a < npe)
+          for (int i = 0; i < prism_node_dofs(p, a); ++i) constrained[elem_dofs[e * nl + first[a] + i]] = 1;
+    }
+  return 0;
+}
+
 // Homogeneous Dirichlet for the cubic HIERARCHIC hex: every dof on a node of
 // a boundary side (vertex, edge and face dofs) has an empty row.
 int orc_dirichlet_hier3(int64_t n_elem, const int32_t *elem_dofs, const int8_t *side_bid, const int32_t *bids,
@@ -1667,15 +1747,19 @@ int orc_assemble2(int form, int type, int fe_order, int q_order, int64_t n_nodes
   Problem P{};
   const int family = (fe_order & 0x100) ? 1 : 0;  // HIERARCHIC flag (FEType family)
   fe_order &= 0xff;
-  const bool p3 = family == 1 && fe_order == 3 && (type == HEX27 || type == TET14);
+  const bool prism_hi = family == 1 && ((fe_order == 2 && type == PRISM18) || (fe_order == 3 && type == PRISM21));
+  const bool p3 = prism_hi || (family == 1 && fe_order == 3 && (type == HEX27 || type == TET14));
   if (family == 1 && !hierarchic_built(type, fe_order) && !p3) return 8;
   if (p3 && (n_vars != 1 || form == ELASTICITY)) return 8;
   P.cons_ptr = cons_ptr; P.cons_col = cons_col; P.cons_val = cons_val;
   P.params = params; P.n_params = n_params;
   if (form == ADVDIFF && n_params < 2) return 1;
   P.form = form; P.type = type; P.fe_order = fe_order; P.q_order = q_order;
-  P.npe = n_shapes(type, (type == HEX27 || type == TET10) ? 2 : (type == TET14 ? 3 : 1));
-  P.n_vars = n_vars; P.nl = n_vars * (p3 ? (type == HEX27 ? 64 : 20) : P.npe);
+  P.npe = prism_hi ? (type == PRISM18 ? 18 : 21)
+                   : n_shapes(type, (type == HEX27 || type == TET10) ? 2 : (type == TET14 ? 3 : 1));
+  P.n_vars = n_vars;
+  P.nl = n_vars * (prism_hi ? (fe_order + 1) * (fe_order + 1) * (fe_order + 2) / 2
+                            : (p3 ? (type == HEX27 ? 64 : 20) : P.npe));
   P.n_nodes = n_nodes; P.n_elem = n_elem; P.n_dofs = n_dofs;
   P.xyz = xyz; P.conn = conn; P.elem_dofs = elem_dofs; P.constrained = constrained;
   P.coef = coef; P.nodal_f = nodal_f; P.nu = nu; P.row_ptr = row_ptr; P.col = col;

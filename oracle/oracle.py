@@ -37,6 +37,10 @@ def lib():
         _lib.orc_shapes_hier_hex.restype = C.c_int32
         _lib.orc_shapes_hier_prism.argtypes = [v, i32, i32, v, v, v]
         _lib.orc_shapes_hier_prism.restype = C.c_int32
+        _lib.orc_distribute_dofs_prism.argtypes = [i32, i64, i64, v, v, C.POINTER(i64)]
+        _lib.orc_distribute_dofs_prism.restype = C.c_int32
+        _lib.orc_dirichlet_prism.argtypes = [i32, i64, v, v, v, i32, v]
+        _lib.orc_dirichlet_prism.restype = C.c_int32
         _lib.orc_distribute_dofs_tet3.argtypes = [i64, i64, v, v, C.POINTER(i64)]
         _lib.orc_dirichlet_tet3.argtypes = [i64, v, v, v, i32, v]
         _lib.orc_mesh_cube.argtypes = [i32, i32, i32, i32, f64, C.c_uint64]
@@ -159,6 +163,26 @@ def shapes_hier_prism(X6, order, pts):
     assert lib().orc_shapes_hier_prism(_p(np.ascontiguousarray(np.asarray(X6)[:6], np.float64)), order, len(pts),
                                        _p(pts), _p(phi), _p(dphi)) == n
     return phi, dphi
+
+
+def distribute_dofs_prism(p, n_nodes, conn):
+    """HIERARCHIC dof numbering and dof_indices of order p = 2 on PRISM18 or
+    p = 3 on PRISM21: [n_elem][(p+1)^2 (p+2)/2]."""
+    conn = np.ascontiguousarray(conn, np.int32)
+    nl = (p + 1) * (p + 1) * (p + 2) // 2
+    ed = np.zeros((conn.shape[0], nl), np.int32)
+    nd = C.c_int64()
+    lib().orc_distribute_dofs_prism(p, n_nodes, conn.shape[0], _p(conn), _p(ed), C.byref(nd))
+    return ed, nd.value
+
+
+def dirichlet_prism(p, elem_dofs, side_bid, bids, n_dofs):
+    """Dofs on the nodes of the boundary sides with ids in bids (homogeneous Dirichlet)."""
+    cons = np.zeros(n_dofs, np.uint8)
+    bids = np.ascontiguousarray(bids, np.int32)
+    lib().orc_dirichlet_prism(p, elem_dofs.shape[0], _p(np.ascontiguousarray(elem_dofs, np.int32)),
+                              _p(np.ascontiguousarray(side_bid, np.int8)), _p(bids), len(bids), _p(cons))
+    return cons
 
 
 def shapes_tet3(X14, pts):

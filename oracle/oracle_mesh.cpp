@@ -3,8 +3,9 @@
 //
 // Restatement of libMesh's structured mesh generation for the benchmark
 // meshes, written from the reference sources step by step:
-//   MeshTools::Generation::build_cube (HEX8 / HEX27 node grid and element
-//     loops, boundary ids)                   src/mesh/mesh_generation.C:1281-1377, 1398-1430, 1569-1604, 1776-1786
+//   MeshTools::Generation::build_cube (HEX8 / HEX27 / PRISM18 / PRISM21 node
+//     grids and element loops, boundary ids) src/mesh/mesh_generation.C:1281-1377, 1398-1430, 1569-1604,
+//                                            1634-1745, 1776-1786
 //   MeshBase::prepare_for_use -> ReplicatedMesh::renumber_nodes_and_elements
 //     (elements compacted in id order, nodes renumbered by the swap walk)
 //                                            src/mesh/replicated_mesh.C:700-800
@@ -126,6 +127,82 @@ void build_cube(OMesh &m, int nx, int ny, int nz, int type) {
         if (j == ny - 1) (*b)[3] = 3;
         if (i == 0) (*b)[4] = 4;
         if (i == nx - 1) (*b)[2] = 2;
+        m.elems.push_back(std::move(e));
+        m.bids.push_back(std::move(b));
+      }
+  renumber(m);
+}
+
+// build_cube(nx, ny, nz, 0..1 x3, PRISM18 | PRISM21) + prepare_for_use
+// (mesh_generation.C:1324-1377 nodes, 1634-1745 elements): the (2n+1)^3 node
+// grid in k, j, i order, for PRISM21 then two nodes per (k, j, i) with k over
+// all 2 nz + 1 grid levels and (j, i) over the cells; two prisms per cell.
+void build_cube_prism(OMesh &m, int nx, int ny, int nz, int type) {
+  const bool p21 = type == 36;
+  const int64_t gx = 2 * (int64_t)nx + 1, gy = 2 * (int64_t)ny + 1, gz = 2 * (int64_t)nz + 1;
+  auto idx = [&](int64_t i, int64_t j, int64_t k) { return i + gx * (j + gy * k); };
+  m.type = type;
+  m.npe = p21 ? 21 : 18;
+  m.nsides = 5;
+  m.nodes.clear();
+  for (int64_t k = 0; k <= 2 * nz; ++k)
+    for (int64_t j = 0; j <= 2 * ny; ++j)
+      for (int64_t i = 0; i <= 2 * nx; ++i)
+        m.nodes.push_back({(double)i / (double)(2 * nx), (double)j / (double)(2 * ny), (double)k / (double)(2 * nz)});
+  if (p21) {
+    const int64_t kmax = 2 * (int64_t)nz;
+    for (int64_t k = 0; k <= kmax; k++)
+      for (int64_t j = 0; j < ny; j++)
+        for (int64_t i = 0; i < nx; i++) {
+          m.nodes.push_back({((double)i + 1 / 3.0) / (double)nx, ((double)j + 1 / 3.0) / (double)ny,
+                             (double)k / (double)kmax});
+          m.nodes.push_back({((double)i + 2 / 3.0) / (double)nx, ((double)j + 2 / 3.0) / (double)ny,
+                             (double)k / (double)kmax});
+        }
+  }
+  for (auto &p : m.nodes)
+    for (int d = 0; d < 3; ++d) p[d] = p[d] * (1.0 - 0.0) + 0.0;
+  const int64_t base = gx * gy * gz;
+  m.elems.clear();
+  m.bids.clear();
+  for (int64_t k = 0; k < 2 * nz; k += 2)
+    for (int64_t j = 0; j < 2 * ny; j += 2)
+      for (int64_t i = 0; i < 2 * nx; i += 2) {
+        // first prism
+        auto e = std::make_unique<std::vector<int64_t>>(std::vector<int64_t>{
+            idx(i, j, k), idx(i + 2, j, k), idx(i, j + 2, k), idx(i, j, k + 2), idx(i + 2, j, k + 2),
+            idx(i, j + 2, k + 2), idx(i + 1, j, k), idx(i + 1, j + 1, k), idx(i, j + 1, k), idx(i, j, k + 1),
+            idx(i + 2, j, k + 1), idx(i, j + 2, k + 1), idx(i + 1, j, k + 2), idx(i + 1, j + 1, k + 2),
+            idx(i, j + 1, k + 2), idx(i + 1, j, k + 1), idx(i + 1, j + 1, k + 1), idx(i, j + 1, k + 1)});
+        if (p21) {
+          e->push_back(base + (k * (nx * ny) + j / 2 * nx + i / 2) * 2);
+          e->push_back(base + ((k + 2) * (nx * ny) + j / 2 * nx + i / 2) * 2);
+          e->push_back(base + ((k + 1) * (nx * ny) + j / 2 * nx + i / 2) * 2);
+        }
+        auto b = std::make_unique<std::vector<int>>(5, -1);
+        if (i == 0) (*b)[3] = 4;
+        if (j == 0) (*b)[1] = 1;
+        if (k == 0) (*b)[0] = 0;
+        if (k == 2 * (nz - 1)) (*b)[4] = 5;
+        m.elems.push_back(std::move(e));
+        m.bids.push_back(std::move(b));
+        // second prism
+        e = std::make_unique<std::vector<int64_t>>(std::vector<int64_t>{
+            idx(i + 2, j, k), idx(i + 2, j + 2, k), idx(i, j + 2, k), idx(i + 2, j, k + 2), idx(i + 2, j + 2, k + 2),
+            idx(i, j + 2, k + 2), idx(i + 2, j + 1, k), idx(i + 1, j + 2, k), idx(i + 1, j + 1, k),
+            idx(i + 2, j, k + 1), idx(i + 2, j + 2, k + 1), idx(i, j + 2, k + 1), idx(i + 2, j + 1, k + 2),
+            idx(i + 1, j + 2, k + 2), idx(i + 1, j + 1, k + 2), idx(i + 2, j + 1, k + 1), idx(i + 1, j + 2, k + 1),
+            idx(i + 1, j + 1, k + 1)});
+        if (p21) {
+          e->push_back(base + (k * (nx * ny) + j / 2 * nx + i / 2) * 2 + 1);
+          e->push_back(base + ((k + 2) * (nx * ny) + j / 2 * nx + i / 2) * 2 + 1);
+          e->push_back(base + ((k + 1) * (nx * ny) + j / 2 * nx + i / 2) * 2 + 1);
+        }
+        b = std::make_unique<std::vector<int>>(5, -1);
+        if (i == 2 * (nx - 1)) (*b)[1] = 2;
+        if (j == 2 * (ny - 1)) (*b)[2] = 3;
+        if (k == 0) (*b)[0] = 0;
+        if (k == 2 * (nz - 1)) (*b)[4] = 5;
         m.elems.push_back(std::move(e));
         m.bids.push_back(std::move(b));
       }
@@ -286,12 +363,22 @@ void second_order(OMesh &m) {
 extern "C" {
 
 // The benchmark meshes: elem_type 10 HEX8 / 12 HEX27 (build_cube, jitter),
-// 8 TET4 / 9 TET10 (build_cube HEX8, jitter, all_tri [, all_second_order]).
+// 8 TET4 / 9 TET10 (build_cube HEX8, jitter, all_tri [, all_second_order]),
+// 15 PRISM18 / 36 PRISM21 (build_cube, no jitter).
 // Returns a handle (null on a bad argument).
 void *orc_mesh_cube(int nx, int ny, int nz, int elem_type, double amp, uint64_t seed) {
   if (nx <= 0 || ny <= 0 || nz <= 0) return nullptr;
-  if (elem_type != 10 && elem_type != 12 && elem_type != 8 && elem_type != 9) return nullptr;
+  if (elem_type != 10 && elem_type != 12 && elem_type != 8 && elem_type != 9 && elem_type != 15 && elem_type != 36)
+    return nullptr;
   auto *m = new OMesh;
+  if (elem_type == 15 || elem_type == 36) {  // unjittered prisms of order 2 / 3
+    if (amp != 0.0) {
+      delete m;
+      return nullptr;
+    }
+    build_cube_prism(*m, nx, ny, nz, elem_type);
+    return m;
+  }
   const bool tets = elem_type == 8 || elem_type == 9;
   build_cube(*m, nx, ny, nz, tets ? 10 : elem_type);
   jitter(*m, amp, nx, ny, nz, seed);

@@ -36,6 +36,12 @@ def members():
     dm.add_dirichlet_boundary([0, 1, 2, 3, 4, 5], [0])
     out.append((lm.GpuAssembly(lm.POISSON, 3 | lm.HIERARCHIC, 6, elem_coef=rng.uniform(0.1, 10, m.n_elem),
                                nodal_f=rng.uniform(-1, 1, (m.n_nodes, 1))), m, dm))
+    for et, p, q in ((lm.PRISM18, 2, 4), (lm.PRISM21, 3, 5)):
+        m = lm.Mesh.build_cube(3, 2, 2, et)
+        dm = lm.DofMap(m, 1, fe_order=p | lm.HIERARCHIC)
+        dm.add_dirichlet_boundary([0, 1, 2, 3, 4, 5], [0])
+        out.append((lm.GpuAssembly(lm.POISSON, p | lm.HIERARCHIC, q, elem_coef=rng.uniform(0.1, 10, m.n_elem),
+                                   nodal_f=rng.uniform(-1, 1, (m.n_nodes, 1))), m, dm))
     for a, m, dm in out:
         a.init(m, dm)
     return out

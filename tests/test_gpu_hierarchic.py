@@ -123,3 +123,29 @@ def test_hierarchic_cubic_tet_matches_oracle(n, jit, qo):
     assert np.all(np.abs(K - Kr) <= tol), np.max(np.abs(K - Kr) / np.maximum(tol, 1e-300))
     ftol = 1e-13 * np.abs(Fr).max()
     assert np.all(np.abs(F - Fr) <= np.maximum(1e-13 * np.abs(Fr), ftol))
+
+
+@pytest.mark.parametrize("et,p,dims,qo", [(lm.PRISM18, 2, (3, 3, 3), 4), (lm.PRISM18, 2, (2, 3, 2), 5),
+                                          (lm.PRISM21, 3, (2, 2, 2), 5), (lm.PRISM21, 3, (3, 2, 3), 4)])
+def test_hierarchic_prism_matches_oracle(et, p, dims, qo):
+    """HIERARCHIC SECOND on PRISM18 and THIRD on PRISM21: the per-element
+    shapes of prism_indices (quadrilateral-face cases, vertical-edge
+    reflections, triangle-edge flips, face 2's first case as the reference
+    indexes it) grouped by orientation pattern; homogeneous Dirichlet on every
+    side; the FP64 drop-in against the oracle at 1e-13, and the mixed form
+    within FP32 rounding of it with the same load vector."""
+    m = lm.Mesh.build_cube(*dims, et)
+    dm = lm.DofMap(m, 1, fe_order=p | lm.HIERARCHIC)
+    dm.add_dirichlet_boundary([0, 1, 2, 3, 4, 5], [0])
+    rng = np.random.default_rng(13)
+    k = np.exp(rng.normal(0, 0.5, m.n_elem))
+    f = rng.uniform(-1, 1, (m.n_nodes, 1))
+    K, _ = check(lm.POISSON, m, dm, k, f, p, qo)
+    asm = lm.GpuAssembly(lm.POISSON, p | lm.HIERARCHIC, qo, elem_coef=k, nodal_f=f)
+    asm.init(m, dm)
+    K64, F64 = asm.assemble(lm.FP64)
+    K32, F32 = asm.assemble(lm.MIXED)
+    asm.close()
+    assert np.array_equal(K64, K)
+    assert np.linalg.norm(K32 - K64) <= 1e-6 * np.linalg.norm(K64)
+    assert np.abs(F32 - F64).max() <= 1e-13 * np.abs(F64).max()

@@ -127,8 +127,23 @@ def test_hier3_dofs_and_dirichlet_match_oracle(rotate):
         assert np.array_equal(c, orc.dirichlet_hier3(ed, m.side_bid, bids, nd))
 
 
+@pytest.mark.parametrize("et,p", [(lm.PRISM18, 2), (lm.PRISM21, 3)])
+def test_prism_dofs_and_dirichlet_match_oracle(et, p):
+    """HIERARCHIC SECOND on PRISM18 and THIRD on PRISM21: per-node dof counts
+    (edge, quad-face, triangle-face and interior nodes), element dofs with
+    reversed non-vertex dofs, and the Dirichlet set, against the oracle."""
+    m = lm.Mesh.build_cube(3, 2, 2, et)
+    dm = lm.DofMap(m, 1, fe_order=p | lm.HIERARCHIC)
+    ed, nd = orc.distribute_dofs_prism(p, m.n_nodes, m.conn)
+    assert nd == dm.n_dofs and np.array_equal(ed, dm.elem_dofs)
+    for bids in ([0, 1, 2, 3, 4, 5], [2], [0, 5], [1, 4]):
+        c = lm.DofMap(m, 1, fe_order=p | lm.HIERARCHIC).add_dirichlet_boundary(bids, [0])
+        assert np.array_equal(c, orc.dirichlet_prism(p, ed, m.side_bid, bids, nd))
+
+
 @pytest.mark.parametrize("et,n,jit", [(lm.HEX8, 5, 0.0), (lm.HEX8, 4, 0.2), (lm.HEX27, 3, 0.0), (lm.TET4, 4, 0.2),
-                                      (lm.TET10, 5, 0.2), (lm.TET10, 6, 0.0), (lm.TET10, 16, 0.2)])
+                                      (lm.TET10, 5, 0.2), (lm.TET10, 6, 0.0), (lm.TET10, 16, 0.2),
+                                      (lm.PRISM18, 3, 0.0), (lm.PRISM21, 3, 0.0), (lm.PRISM21, 1, 0.0)])
 def test_mesh_generation_matches_oracle(et, n, jit):
     """build_cube (+ all_tri, all_second_order) through the C ABI against the
     oracle's step-by-step restatement: coordinates, connectivity and side
