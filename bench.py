@@ -209,9 +209,19 @@ def run_amr(args, local):
     t0 = time.perf_counter()
     n = 24 if args.n == N_CUBE else args.n      # build_cube 24^3 HEX27 unless --n is given
     mesh = lm.Mesh.build_refined_cube(n, lm.HEX27, 3, 0.2, 2)
+    t_mesh = time.perf_counter() - t0
     dm = lm.DofMap(mesh, 1)
     dm.add_dirichlet_boundary([0, 1, 2, 3, 4, 5], [0])
-    dm.create_dof_constraints()
+    dm_host = lm.DofMap(mesh, 1)
+    dm_host.add_dirichlet_boundary([0, 1, 2, 3, 4, 5], [0])
+    t1 = time.perf_counter()
+    dm_host.create_dof_constraints()            # hanging-node rows on the host (timed for comparison)
+    t_rows_host = time.perf_counter() - t1
+    t1 = time.perf_counter()
+    dm.create_dof_constraints(device=local)     # the same rows formed on the GPU
+    t_rows_dev = time.perf_counter() - t1
+    del dm_host
+    t0 += t_rows_host
     rng = np.random.default_rng(2)
     k = np.exp(rng.normal(0.0, 0.5, mesh.n_elem))
     f = rng.uniform(-1.0, 1.0, (mesh.n_nodes, 1))
@@ -282,6 +292,8 @@ def run_amr(args, local):
         "metric": METRIC, "value": mesh.n_elem / (ms * 1e-3) / 1e6, "unit": "Melem/s", "n_gpus": 1,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded refinement, k_e, f, b)",
+        "setup_breakdown_s": {"refined_mesh": t_mesh, "constraint_rows_host": t_rows_host,
+                              "constraint_rows_device": t_rows_dev},
         "config": {"workload": "convection-diffusion HEX27 build_cube %d^3, 3 cycles x 20%% h-refinement, "
                                "QGauss FIFTH, hanging-node + Dirichlet constraints" % n,
                    "n_elem": mesh.n_elem, "n_dofs": dm.n_dofs, "nnz": asm.nnz, "constrained_elements": n_cons,
@@ -395,7 +407,8 @@ def run_batch(args, local):
     print(json.dumps({
         "metric": METRIC, "value": total / (ms * 1e-3) / 1e6, "unit": "Melem/s", "n_gpus": 1, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64", "data": "synthetic (seeded sizes, coefficients, loads)",
+        "dtype": "double-float (FP32 pairs) contraction, FP64 geometry, FP64 / double-float sums",
+        "data": "synthetic (seeded sizes, coefficients, loads)",
         "config": {"workload": "batch of %d systems (config-4 mix), element counts log-uniform in "
                                "[1e3, %.0e]: HIERARCHIC Poisson on HEX8 p1, HEX27 p2, HEX27 p3, TET4 p1, TET10 p2, "
                                "PRISM6 p1, PRISM18 p2, PRISM21 p3, TET14 p3, k_e ~ U[0.1, 10]" % (n_meshes, args.max_elems),
@@ -635,15 +648,19 @@ def main():
         ms32 = ev0.elapsed_time(ev1) / args.steps
         K32 = torch.empty(asm.nnz, dtype=torch.float64, device="cuda")
         K64 = torch.empty(asm.nnz, dtype=torch.float64, device="cuda")
-        Fd = torch.empty(dm.n_dofs, dtype=torch.float64, device="cuda")
-        asm.assemble_device(lm.MIXED, K32.data_ptr(), Fd.data_ptr())
-        asm.assemble_device(lm.FP64, K64.data_ptr(), Fd.data_ptr())
+        F32 = torch.empty(dm.n_dofs, dtype=torch.float64, device="cuda")
+        F64 = torch.empty(dm.n_dofs, dtype=torch.float64, device="cuda")
+        asm.assemble_device(lm.MIXED, K32.data_ptr(), F32.data_ptr())
+        asm.assemble_device(lm.FP64, K64.data_ptr(), F64.data_ptr())
         asm.synchronize()
         krel = float(torch.linalg.norm(K32 - K64) / torch.linalg.norm(K64))
-        del K32, K64, Fd
+        frel = float(torch.linalg.norm(F32 - F64) / torch.linalg.norm(F64))
+        del K32, K64, F32, F64
         other = {"form": "mixed (FP32 contraction, FP64 Jacobian/diagonal/accumulation)",
                  "value": world * mesh.n_elem / (ms32 * 1e-3) / 1e6, "unit": "Melem/s", "ms_per_step": ms32,
-                 "speedup_vs_fp64": ms / ms32, "k_rel_frobenius_vs_fp64": krel}
+                 "speedup_vs_fp64": ms / ms32, "k_rel_frobenius_vs_fp64": krel, "f_rel_vs_fp64": frel,
+                 "solved_field": "relative error of the CG-solved field against the FP64 solve: "
+                                 "tests/test_gpu_full_size.py (C2 at full size, bar 1e-6)"}
 
     # matrix-free residual R = K u - F (no K), against assembling K and one product
     resid = None
@@ -751,7 +768,9 @@ def main():
         print(json.dumps({
             "metric": METRIC, "value": value, "unit": "Melem/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64" if prec == lm.FP64 else "f32+f64",
+            "vs_baseline": None,
+            "dtype": ("double-float (FP32 pairs) contraction and sums, FP64 geometry" if prec == lm.FP64
+                      else "f32 contraction, FP64 geometry, double-float sums"),
             "data": "synthetic (seeded mesh jitter, E_e, f)",
             "config": {"workload": "elasticity TET10 build_cube %d^3 x6 tets, QGauss FOURTH" % args.n,
                        "n_elem": mesh.n_elem, "n_dofs": dm.n_dofs, "nnz": asm.nnz,

@@ -134,6 +134,16 @@ lmg_status lmg_fe_dofs_per_elem(int32_t elem_type, int32_t fe_order, int32_t n_v
 lmg_status lmg_dofmap_distribute_fe(int64_t n_nodes, int64_t n_elem, int32_t elem_type, const int32_t *conn,
                                     int32_t n_vars, int32_t fe_order, int64_t *n_dofs, int32_t *elem_dofs);
 
+/* The same numbering and dof_indices formed on `device`: the sequential sweep
+ * of distribute_local_dofs_var_major as an exclusive scan (each node's first
+ * touch, the smallest element position holding it, carries its dof count;
+ * each element's interior dofs follow its nodes).  Host arrays in and out,
+ * bit for bit the lists of lmg_dofmap_distribute_fe; the call synchronizes
+ * the device and allocates device memory for its duration. */
+lmg_status lmg_dofmap_distribute_device(int32_t device, int64_t n_nodes, int64_t n_elem, int32_t elem_type,
+                                        const int32_t *conn, int32_t n_vars, int32_t fe_order, int64_t *n_dofs,
+                                        int32_t *elem_dofs);
+
 /* lmg_dirichlet_dofs for an FEType: for FEType{THIRD, HIERARCHIC} every dof
  * of every node of a matching side (vertex, edge and face dofs). */
 lmg_status lmg_dirichlet_dofs_fe(int64_t n_elem, int32_t elem_type, int32_t fe_order, int32_t n_vars,
@@ -178,6 +188,18 @@ lmg_status lmg_mesh_tree(const lmg_mesh *m, int64_t *n_all, int32_t *all_conn, i
 lmg_status lmg_constraint_rows(const lmg_mesh *m, int32_t n_vars, const int32_t *elem_dofs,
                                int64_t n_dofs, const uint8_t *dirichlet, uint8_t *constrained,
                                int64_t *cons_ptr, int32_t *cons_col, double *cons_val, int64_t cap);
+
+/* The same rows with the hanging-node rows formed on `device`
+ * (lagrange_compute_constraints, src/fe/fe_lagrange.C:867-1063, one thread
+ * per (variable, active element, side), the first visit of a dof in
+ * libMesh's loop order writing its row); the Dirichlet rows and
+ * process_constraints (dof_map_constraints.C:4341-4490) follow on the host.
+ * Same arguments and outputs as lmg_constraint_rows, bit for bit; the call
+ * synchronizes the device and allocates device memory for its duration. */
+lmg_status lmg_constraint_rows_device(const lmg_mesh *m, int32_t device, int32_t n_vars,
+                                      const int32_t *elem_dofs, int64_t n_dofs, const uint8_t *dirichlet,
+                                      uint8_t *constrained, int64_t *cons_ptr, int32_t *cons_col,
+                                      double *cons_val, int64_t cap);
 
 /* DofMap::compute_sparsity with constraints (find_connected_dofs,
  * src/base/dof_map.C:2915-2970): every element couples the union of its dofs
@@ -233,8 +255,13 @@ lmg_status lmg_constraints_upload(lmg_ctx *ctx, const uint8_t *constrained);
 lmg_status lmg_constraint_rows_upload(lmg_ctx *ctx, const uint8_t *constrained, const int64_t *cons_ptr,
                                       const int32_t *cons_col, const double *cons_val);
 
-/* DofMap::compute_sparsity: PETSc-AIJ CSR (sorted column indices per row). */
+/* DofMap::compute_sparsity: PETSc-AIJ CSR (sorted column indices per row).
+ * Built on the device: the block path's block graph, and with constraint
+ * rows the enlarged element lists of find_connected_dofs and their union per
+ * row; the host builds a pattern whose rows outgrow the device buffers. */
 lmg_status lmg_sparsity_build(lmg_ctx *ctx, int64_t *nnz);
+/* 1 when the last lmg_sparsity_build formed the pattern on the device, else 0. */
+lmg_status lmg_sparsity_on_device(lmg_ctx *ctx, int32_t *on_device);
 lmg_status lmg_sparsity_copy(lmg_ctx *ctx, int32_t *row_ptr, int32_t *col_idx);
 
 /* FE family flag OR'ed into fe_order (libMesh FEType{order, family}):

@@ -110,9 +110,10 @@ class DofMap:
     elem_dofs[e] is DofMap::dof_indices(elem).  fe_order (| HIERARCHIC) picks
     the FEType whose dofs are numbered: nodal types give one dof per node and
     variable; 3 | HIERARCHIC gives 64 dofs per element on HEX27, 20 on TET14
-    and 40 on PRISM21; 2 | HIERARCHIC 18 on PRISM18."""
+    and 40 on PRISM21; 2 | HIERARCHIC 18 on PRISM18.  device: number on that
+    GPU (the same lists bit for bit)."""
 
-    def __init__(self, mesh, n_vars=1, fe_order=None):
+    def __init__(self, mesh, n_vars=1, fe_order=None, device=None):
         self.mesh = mesh
         self.n_vars = int(n_vars)
         self.fe_order = 0 if fe_order is None else int(fe_order)
@@ -123,8 +124,13 @@ class DofMap:
             n.value = self.n_vars * mesh.conn.shape[1]
         self.elem_dofs = np.empty((mesh.n_elem, n.value), np.int32)
         nd = C.c_int64()
-        check(lib().lmg_dofmap_distribute_fe(mesh.n_nodes, mesh.n_elem, mesh.elem_type, ptr(mesh.conn),
-                                             self.n_vars, self.fe_order, C.byref(nd), ptr(self.elem_dofs)))
+        if device is None:
+            check(lib().lmg_dofmap_distribute_fe(mesh.n_nodes, mesh.n_elem, mesh.elem_type, ptr(mesh.conn),
+                                                 self.n_vars, self.fe_order, C.byref(nd), ptr(self.elem_dofs)))
+        else:
+            check(lib().lmg_dofmap_distribute_device(int(device), mesh.n_nodes, mesh.n_elem, mesh.elem_type,
+                                                     ptr(mesh.conn), self.n_vars, self.fe_order, C.byref(nd),
+                                                     ptr(self.elem_dofs)))
         self.n_dofs = nd.value
         self.constrained = np.zeros(self.n_dofs, np.uint8)
 
@@ -151,11 +157,12 @@ class DofMap:
 
     cons_ptr = cons_col = cons_val = None
 
-    def create_dof_constraints(self):
+    def create_dof_constraints(self, device=None):
         """DofMap::create_dof_constraints + process_constraints: hanging-node
         rows of a refined mesh, then empty rows for the Dirichlet dofs still
         free, chains substituted.  Sets constrained and the rows (CSR over all
-        dofs: cons_ptr, cons_col, cons_val)."""
+        dofs: cons_ptr, cons_col, cons_val).  device: form the hanging-node
+        rows on that GPU (the same rows bit for bit)."""
         L = lib()
         h = self.mesh._handle
         owned = h is None
@@ -168,13 +175,16 @@ class DofMap:
         dirichlet = self.constrained.copy()
         cons = np.zeros(self.n_dofs, np.uint8)
         cp = np.zeros(self.n_dofs + 1, np.int64)
-        check(L.lmg_constraint_rows(h, self.n_vars, ptr(self.elem_dofs), self.n_dofs, ptr(dirichlet), ptr(cons),
-                                    ptr(cp), None, None, 0))
+        if device is None:
+            rows = lambda *a: L.lmg_constraint_rows(h, *a)  # noqa: E731
+        else:
+            rows = lambda *a: L.lmg_constraint_rows_device(h, int(device), *a)  # noqa: E731
+        check(rows(self.n_vars, ptr(self.elem_dofs), self.n_dofs, ptr(dirichlet), ptr(cons), ptr(cp), None, None, 0))
         total = int(cp[-1])
         col = np.zeros(max(total, 1), np.int32)
         val = np.zeros(max(total, 1), np.float64)
-        check(L.lmg_constraint_rows(h, self.n_vars, ptr(self.elem_dofs), self.n_dofs, ptr(dirichlet), ptr(cons),
-                                    ptr(cp), ptr(col), ptr(val), total))
+        check(rows(self.n_vars, ptr(self.elem_dofs), self.n_dofs, ptr(dirichlet), ptr(cons), ptr(cp), ptr(col),
+                   ptr(val), total))
         self.constrained = cons
         self.cons_ptr, self.cons_col, self.cons_val = cp, col[:total], val[:total]
 
@@ -229,6 +239,12 @@ class GpuAssembly:
 
     def update_inputs(self, xyz=None, elem_coef=None, nodal_f=None):
         self._ok(lib().lmg_inputs_update(self.ctx, ptr(xyz), ptr(elem_coef), ptr(nodal_f)))
+
+    def sparsity_on_device(self):
+        """Whether the sparsity pattern was formed on the device."""
+        v = C.c_int32()
+        self._ok(lib().lmg_sparsity_on_device(self.ctx, C.byref(v)))
+        return bool(v.value)
 
     def assemble(self, precision=FP64):
         K = np.empty(self.nnz, np.float64)

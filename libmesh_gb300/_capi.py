@@ -37,11 +37,13 @@ SIGNATURES = {
     "lmg_dirichlet_dofs": [_i64, _i32, _i32, _p, _p, _p, _i32, _p, _i32, _i64, _p],
     "lmg_fe_dofs_per_elem": [_i32, _i32, _i32, _pi32],
     "lmg_dofmap_distribute_fe": [_i64, _i64, _i32, _p, _i32, _i32, _pi64, _p],
+    "lmg_dofmap_distribute_device": [_i32, _i64, _i64, _i32, _p, _i32, _i32, _pi64, _p],
     "lmg_dirichlet_dofs_fe": [_i64, _i32, _i32, _i32, _p, _p, _p, _i32, _p, _i32, _i64, _p],
     "lmg_host_sparsity": [_i64, _i32, _i32, _i64, _p, _pi64, _p, _p],
     "lmg_mesh_refine": [_p, _i32, _f64, _u64],
     "lmg_mesh_tree": [_p, _pi64, _p, _p, _p, _p],
     "lmg_constraint_rows": [_p, _i32, _p, _i64, _p, _p, _p, _p, _p, _i64],
+    "lmg_constraint_rows_device": [_p, _i32, _i32, _p, _i64, _p, _p, _p, _p, _p, _i64],
     "lmg_host_sparsity_constrained": [_i64, _i32, _i64, _p, _p, _p, _pi64, _p, _p],
     "lmg_context_create": [C.POINTER(_p), _i32],
     "lmg_context_destroy": [_p],
@@ -53,6 +55,7 @@ SIGNATURES = {
     "lmg_constraint_rows_upload": [_p, _p, _p, _p, _p],
     "lmg_sparsity_build": [_p, _pi64],
     "lmg_sparsity_copy": [_p, _p, _p],
+    "lmg_sparsity_on_device": [_p, _pi32],
     "lmg_form_set": [_p, _i32, _i32, _i32, _p, _i32, _p, _p],
     "lmg_inputs_update": [_p, _p, _p, _p],
     "lmg_assemble": [_p, _i32, _p, _p, _i32],

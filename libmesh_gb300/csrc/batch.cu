@@ -5,7 +5,10 @@
 // autotuner has picked each system's element-kernel grid.
 //
 // Life cycle: lmg_batch_add registers a fully set-up context (sparsity,
-// form); lmg_batch_tune times a few grid sizes per context; lmg_batch_assemble
+// form); lmg_batch_tune times a few grid sizes per context, and for the
+// per-pattern HIERARCHIC members the number of elements each CTA takes per
+// tile (4 to 32: more elements share one read of the pattern's tables, fewer
+// spread a small system over more SMs); lmg_batch_assemble
 // warms every context up once (lazy plans, buffers), then captures their
 // assemblies into a graph per precision and replays it.  The capture forks
 // from the batch stream into every context's own stream and joins back, so
@@ -127,19 +130,27 @@ lmg_status lmg_batch_tune(lmg_batch *b, int32_t precision, int32_t reps) {
   cudaEvent_t e0, e1;
   if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
     return bfail(b, LMG_ERR_CUDA, "batch_tune: event creation failed");
+  // one timed measurement of a context's assembly under its current settings
+  auto time_one = [&](lmg_ctx *c, float &ms) -> lmg_status {
+    lmg_status s = lmg_assemble(c, precision, nullptr, nullptr, 1);
+    if (s) return s;
+    cudaEventRecord(e0, c->stream);
+    for (int r = 0; r < reps && !s; ++r) s = lmg_assemble(c, precision, nullptr, nullptr, 1);
+    cudaEventRecord(e1, c->stream);
+    if (s) return s;
+    if (cudaEventSynchronize(e1) != cudaSuccess) return LMG_ERR_CUDA;
+    cudaEventElapsedTime(&ms, e0, e1);
+    return LMG_OK;
+  };
+  static const int tiles[] = {4, 8, 16, 32};
   for (lmg_ctx *c : b->ctx) {
+    // CTAs per SM of the element kernels
     float best = 1e30f;
     int best_c = c->ctas_per_sm;
     for (int k : cand) {
       c->ctas_per_sm = k;
-      st = lmg_assemble(c, precision, nullptr, nullptr, 1);
-      if (st) break;
-      cudaEventRecord(e0, c->stream);
-      for (int r = 0; r < reps && !st; ++r) st = lmg_assemble(c, precision, nullptr, nullptr, 1);
-      cudaEventRecord(e1, c->stream);
-      if (st || cudaEventSynchronize(e1) != cudaSuccess) break;
       float ms = 0.f;
-      cudaEventElapsedTime(&ms, e0, e1);
+      if ((st = time_one(c, ms))) break;
       if (ms < best) {
         best = ms;
         best_c = k;
@@ -147,6 +158,21 @@ lmg_status lmg_batch_tune(lmg_batch *b, int32_t precision, int32_t reps) {
     }
     c->ctas_per_sm = best_c;
     if (st) break;
+    // elements per CTA tile of the per-pattern HIERARCHIC kernels
+    if (c->hier3) {
+      best = 1e30f;
+      int best_t = c->h3_tile;
+      for (int tl : tiles) {
+        float ms = 0.f;
+        if ((st = lmg::hier3_set_tile(c, tl)) || (st = time_one(c, ms))) break;
+        if (ms < best) {
+          best = ms;
+          best_t = tl;
+        }
+      }
+      if (!st) st = lmg::hier3_set_tile(c, best_t);
+      if (st) break;
+    }
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);

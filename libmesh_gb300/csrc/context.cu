@@ -84,6 +84,149 @@ __global__ void k_fill(int64_t n, const int32_t *key, const int32_t *ptr, int32_
   }
 }
 
+// Constrained sparsity (find_connected_dofs, src/base/dof_map.C:2915-2970):
+// every element couples the union of its dofs and of the dofs their
+// constraint rows refer to.  k_enlarge: warp per element, the element's dofs
+// and its constrained dofs' row columns gathered into shared memory, bitonic
+// sort, duplicates dropped by ballot; PASS 0 records the length (and raises
+// `flag` bit 1 when an added dof is itself constrained -- a chain the host
+// closure would follow -- or bit 0 when the list outgrows the buffer),
+// PASS 1 writes the list padded with INT32_MAX to width W.
+constexpr int ENL_CAP = 1024, ENL_WARPS = 4;
+template <int PASS>
+__global__ void __launch_bounds__(ENL_WARPS * 32) k_enlarge(int64_t n_elem, int nl, const int32_t *ed,
+                                                           const int64_t *cons_ptr, const int32_t *cons_col, int W,
+                                                           int32_t *len, int32_t *out, int *flag) {
+  __shared__ int32_t buf[ENL_WARPS][ENL_CAP];
+  __shared__ int32_t sn[ENL_WARPS];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int32_t *b = buf[warp];
+  for (int64_t e = (int64_t)blockIdx.x * ENL_WARPS + warp; e < n_elem; e += (int64_t)gridDim.x * ENL_WARPS) {
+    if (lane == 0) sn[warp] = 0;
+    __syncwarp();
+    bool over = false;
+    for (int i = lane; i < nl; i += 32) {
+      const int32_t d = ed[e * nl + i];
+      const int64_t r0 = cons_ptr[d], r1 = cons_ptr[d + 1];
+      const int k = atomicAdd(&sn[warp], 1 + (int)(r1 - r0));
+      if (k + 1 + (r1 - r0) > ENL_CAP) { over = true; continue; }
+      b[k] = d;
+      for (int64_t r = r0; r < r1; ++r) b[k + 1 + (r - r0)] = cons_col[r];
+    }
+    __syncwarp();
+    if (__any_sync(0xffffffffu, over)) {
+      if (lane == 0) atomicOr(flag, 1);
+      __syncwarp();
+      continue;
+    }
+    const int n = sn[warp];
+    int S = 1;
+    while (S < n) S <<= 1;
+    for (int t = n + lane; t < S; t += 32) b[t] = 0x7fffffff;
+    __syncwarp();
+    for (int k = 2; k <= S; k <<= 1)
+      for (int j = k >> 1; j > 0; j >>= 1) {
+        for (int t = lane; t < S; t += 32) {
+          const int u = t ^ j;
+          if (u > t) {
+            const int32_t x = b[t], y = b[u];
+            if ((x > y) == ((t & k) == 0)) { b[t] = y; b[u] = x; }
+          }
+        }
+        __syncwarp();
+      }
+    int count = 0;
+    bool chain = false;
+    for (int t0 = 0; t0 < S; t0 += 32) {
+      const int t = t0 + lane;
+      const bool keep = t < S && b[t] != 0x7fffffff && (t == 0 || b[t] != b[t - 1]);
+      if (keep && PASS == 0 && cons_ptr[b[t] + 1] > cons_ptr[b[t]]) {
+        // a constrained dof in the list: it must be one of the element's own
+        bool own = false;
+        for (int i = 0; i < nl && !own; ++i) own = ed[e * nl + i] == b[t];
+        chain |= !own;
+      }
+      const unsigned m = __ballot_sync(0xffffffffu, keep);
+      if (PASS == 1 && keep) out[e * W + count + __popc(m & ((1u << lane) - 1u))] = b[t];
+      count += __popc(m);
+    }
+    if (PASS == 0) {
+      if (__any_sync(0xffffffffu, chain) && lane == 0) atomicOr(flag, 2);
+      if (lane == 0) len[e] = count;
+    } else {
+      for (int t = count + lane; t < W; t += 32) out[e * W + t] = 0x7fffffff;
+    }
+    __syncwarp();
+  }
+}
+
+__global__ void k_width(int64_t n, const int32_t *len, int *w) {
+  int m = 0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    m = max(m, len[i]);
+  atomicMax(w, m);
+}
+
+// Incidences of the padded lists (INT32_MAX entries skipped).
+__global__ void k_count_padded(int64_t n, const int32_t *v, int32_t *cnt) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    if (v[i] != 0x7fffffff) atomicAdd(&cnt[v[i]], 1);
+}
+__global__ void k_fill_padded(int64_t n, const int32_t *v, const int32_t *ptr, int32_t *cur, int32_t *out) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    if (v[i] != 0x7fffffff) out[ptr[v[i]] + atomicAdd(&cur[v[i]], 1)] = (int32_t)i;
+}
+
+// Rows of the constrained graph: warp per dof, the lists of the elements whose
+// enlarged list holds the dof, merged by a bitonic sort in a per-warp buffer of
+// `cap` entries (dynamic shared memory); rows that need more raise `flag`.
+template <int PASS>
+__global__ void __launch_bounds__(ENL_WARPS * 32) k_row_graph(int64_t n_rows, int W, const int32_t *lists,
+                                                             const int32_t *iptr, const int32_t *icon, int cap,
+                                                             int32_t *deg, const int32_t *rptr, int32_t *col,
+                                                             int *flag) {
+  extern __shared__ int32_t rbuf[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int32_t *b = rbuf + (size_t)warp * cap;
+  for (int64_t P = (int64_t)blockIdx.x * ENL_WARPS + warp; P < n_rows; P += (int64_t)gridDim.x * ENL_WARPS) {
+    const int32_t i0 = iptr[P], i1 = iptr[P + 1];
+    const int n = (i1 - i0) * W;
+    if (n > cap) {
+      if (lane == 0) atomicOr(flag, 1);
+      continue;
+    }
+    int S = 1;
+    while (S < n) S <<= 1;
+    for (int t = lane; t < S; t += 32) {
+      int32_t v = 0x7fffffff;
+      if (t < n) v = lists[(int64_t)(icon[i0 + t / W] / W) * W + t % W];
+      b[t] = v;
+    }
+    __syncwarp();
+    for (int k = 2; k <= S; k <<= 1)
+      for (int j = k >> 1; j > 0; j >>= 1) {
+        for (int t = lane; t < S; t += 32) {
+          const int u = t ^ j;
+          if (u > t) {
+            const int32_t x = b[t], y = b[u];
+            if ((x > y) == ((t & k) == 0)) { b[t] = y; b[u] = x; }
+          }
+        }
+        __syncwarp();
+      }
+    int count = 0;
+    for (int t0 = 0; t0 < S; t0 += 32) {
+      const int t = t0 + lane;
+      const bool keep = t < S && b[t] != 0x7fffffff && (t == 0 || b[t] != b[t - 1]);
+      const unsigned m = __ballot_sync(0xffffffffu, keep);
+      if (PASS == 1 && keep) col[rptr[P] + count + __popc(m & ((1u << lane) - 1u))] = b[t];
+      count += __popc(m);
+    }
+    if (PASS == 0 && lane == 0) deg[P] = count;
+    __syncwarp();
+  }
+}
+
 // Each segment is short (the elements sharing one block pair), so an
 // insertion sort per thread puts contributions in element order.
 __global__ void k_segsort(int64_t n_seg, const int32_t *ptr, int32_t *v) {
@@ -266,6 +409,91 @@ lmg_status scan_i32(lmg_ctx *c, const int32_t *in, int32_t *out, int64_t n) {
   LMG_CUDA(c, cudaStreamSynchronize(c->stream));
   dfree(bsum);
   dfree(boff);
+  return LMG_OK;
+}
+
+// Constrained graph on the device (rows and columns into rp / cols, and into
+// d_row_ptr / d_col); LMG_ERR_UNSUPPORTED when an element list or a row
+// outgrows its buffer or a constraint row refers to a constrained dof (the
+// caller then builds it on the host).
+lmg_status constrained_graph_impl(lmg_ctx *c, std::vector<int64_t> &rp, std::vector<int32_t> &cols) {
+  const int64_t E = c->n_elem, nd = c->n_dofs;
+  const int nl = c->nl;
+  std::vector<int64_t> cp = c->h_cons_ptr;
+  if (cp.empty()) cp.assign((size_t)nd + 1, 0);
+  int32_t *d_ed = nullptr, *d_ccol = nullptr, *len = nullptr, *lists = nullptr, *cnt = nullptr, *iptr = nullptr,
+          *cur = nullptr, *icon = nullptr, *deg = nullptr, *rptr = nullptr, *colv = nullptr;
+  int64_t *d_cp = nullptr;
+  int *flag = nullptr;
+  auto cleanup = [&]() {
+    dfree(d_ed); dfree(d_ccol); dfree(len); dfree(lists); dfree(cnt); dfree(iptr); dfree(cur); dfree(icon);
+    dfree(deg); dfree(d_cp); dfree(flag);
+  };
+  auto bad = [&](lmg_status st) { cleanup(); dfree(rptr); dfree(colv); return st; };
+  if (dupload(c, d_ed, c->h_elem_dofs.data(), c->h_elem_dofs.size()) != cudaSuccess ||
+      dupload(c, d_cp, cp.data(), cp.size()) != cudaSuccess ||
+      dupload(c, d_ccol, c->h_cons_col.data(), c->h_cons_col.size()) != cudaSuccess ||
+      dalloc(len, (size_t)E) != cudaSuccess || dalloc(flag, 2) != cudaSuccess)
+    return bad(LMG_ERR_CUDA);
+  cudaMemsetAsync(flag, 0, 2 * sizeof(int), c->stream);
+  const int g = grid_for(c, E * 32, ENL_WARPS * 32);
+  k_enlarge<0><<<g, ENL_WARPS * 32, 0, c->stream>>>(E, nl, d_ed, d_cp, d_ccol, 0, len, nullptr, flag);
+  k_width<<<grid_for(c, E, 256), 256, 0, c->stream>>>(E, len, flag + 1);
+  c->launches += 2;
+  int hf[2] = {0, 0};
+  if (cudaMemcpyAsync(hf, flag, sizeof(hf), cudaMemcpyDeviceToHost, c->stream) != cudaSuccess ||
+      cudaStreamSynchronize(c->stream) != cudaSuccess)
+    return bad(LMG_ERR_CUDA);
+  if (hf[0]) return bad(LMG_ERR_UNSUPPORTED);
+  const int W = std::max(hf[1], 1);
+  if (dalloc(lists, (size_t)(E * W)) != cudaSuccess || dalloc(cnt, (size_t)nd) != cudaSuccess ||
+      dalloc(cur, (size_t)nd) != cudaSuccess || dalloc(iptr, (size_t)nd + 1) != cudaSuccess ||
+      dalloc(deg, (size_t)nd) != cudaSuccess || dalloc(rptr, (size_t)nd + 1) != cudaSuccess)
+    return bad(LMG_ERR_OOM);
+  k_enlarge<1><<<g, ENL_WARPS * 32, 0, c->stream>>>(E, nl, d_ed, d_cp, d_ccol, W, len, lists, flag);
+  cudaMemsetAsync(cnt, 0, sizeof(int32_t) * nd, c->stream);
+  k_count_padded<<<grid_for(c, E * W, 256), 256, 0, c->stream>>>(E * W, lists, cnt);
+  c->launches += 2;
+  lmg_status st = scan_i32(c, cnt, iptr, nd);
+  if (st) return bad(st);
+  int32_t n_inc = 0;
+  if (cudaMemcpy(&n_inc, iptr + nd, sizeof(int32_t), cudaMemcpyDeviceToHost) != cudaSuccess) return bad(LMG_ERR_CUDA);
+  if (dalloc(icon, (size_t)std::max(n_inc, 1)) != cudaSuccess) return bad(LMG_ERR_OOM);
+  cudaMemsetAsync(cur, 0, sizeof(int32_t) * nd, c->stream);
+  k_fill_padded<<<grid_for(c, E * W, 256), 256, 0, c->stream>>>(E * W, lists, iptr, cur, icon);
+  c->launches++;
+  const int cap = 4096;
+  const size_t smem = sizeof(int32_t) * cap * ENL_WARPS;
+  cudaFuncSetAttribute(k_row_graph<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaFuncSetAttribute(k_row_graph<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  const int gr = grid_for(c, nd * 32, ENL_WARPS * 32);
+  k_row_graph<0><<<gr, ENL_WARPS * 32, smem, c->stream>>>(nd, W, lists, iptr, icon, cap, deg, nullptr, nullptr,
+                                                          flag);
+  c->launches++;
+  if (cudaMemcpyAsync(hf, flag, sizeof(int), cudaMemcpyDeviceToHost, c->stream) != cudaSuccess ||
+      cudaStreamSynchronize(c->stream) != cudaSuccess)
+    return bad(LMG_ERR_CUDA);
+  if (hf[0]) return bad(LMG_ERR_UNSUPPORTED);
+  if ((st = scan_i32(c, deg, rptr, nd))) return bad(st);
+  int32_t nnz = 0;
+  if (cudaMemcpy(&nnz, rptr + nd, sizeof(int32_t), cudaMemcpyDeviceToHost) != cudaSuccess) return bad(LMG_ERR_CUDA);
+  if (nnz < 0) return bad(LMG_ERR_UNSUPPORTED);
+  if (dalloc(colv, (size_t)std::max(nnz, 1)) != cudaSuccess) return bad(LMG_ERR_OOM);
+  k_row_graph<1><<<gr, ENL_WARPS * 32, smem, c->stream>>>(nd, W, lists, iptr, icon, cap, nullptr, rptr, colv, flag);
+  c->launches++;
+  std::vector<int32_t> r32((size_t)nd + 1);
+  cols.resize((size_t)nnz);
+  if (cudaMemcpyAsync(r32.data(), rptr, sizeof(int32_t) * (nd + 1), cudaMemcpyDeviceToHost, c->stream) !=
+          cudaSuccess ||
+      cudaMemcpyAsync(cols.data(), colv, sizeof(int32_t) * nnz, cudaMemcpyDeviceToHost, c->stream) != cudaSuccess ||
+      cudaStreamSynchronize(c->stream) != cudaSuccess)
+    return bad(LMG_ERR_CUDA);
+  rp.assign(r32.begin(), r32.end());
+  cleanup();
+  dfree(c->d_row_ptr);
+  dfree(c->d_col);
+  c->d_row_ptr = rptr;
+  c->d_col = colv;
   return LMG_OK;
 }
 
@@ -484,6 +712,10 @@ lmg_status upload_cmask(lmg_ctx *c) {
 
 }  // namespace
 
+lmg_status lmg::device_constrained_graph(lmg_ctx *c, std::vector<int64_t> &rp, std::vector<int32_t> &cols) {
+  return constrained_graph_impl(c, rp, cols);
+}
+
 extern "C" {
 
 lmg_status lmg_context_create(lmg_ctx **out, int32_t device) {
@@ -660,6 +892,7 @@ lmg_status lmg_sparsity_build(lmg_ctx *c, int64_t *nnz) {
   // the block pattern on the device; the host builds rows the device buffer cannot hold
   // (32-bit incidence and column offsets: every element adds at most nb^2 block pairs)
   lmg_status gs = c->n_elem * c->nb * c->nb < INT32_MAX ? device_block_graph(c, brow) : LMG_ERR_UNSUPPORTED;
+  c->sparsity_on_device = gs == LMG_OK;
   if (gs == LMG_ERR_UNSUPPORTED) {
     const unsigned hw = std::thread::hardware_concurrency();
     build_block_graph(c->n_elem, c->nb, c->h_eb.data(), c->n_blocks, brow, bcol, hw ? (int)hw : 4);
@@ -696,6 +929,13 @@ lmg_status lmg_sparsity_build(lmg_ctx *c, int64_t *nnz) {
   LMG_CUDA(c, dalloc(c->d_Fe2, (size_t)(c->n_elem * c->nl)));
   c->have_sparsity = true;
   if (nnz) *nnz = c->nnz;
+  return LMG_OK;
+}
+
+lmg_status lmg_sparsity_on_device(lmg_ctx *c, int32_t *on_device) {
+  if (!c || !on_device) return LMG_ERR_ARG;
+  if (!c->have_sparsity) return fail(c, LMG_ERR_STATE, "sparsity_on_device: build the sparsity first");
+  *on_device = c->sparsity_on_device ? 1 : 0;
   return LMG_OK;
 }
 

@@ -52,19 +52,28 @@ void general_free(lmg_ctx *c) {
 }
 
 lmg_status general_sparsity(lmg_ctx *c) {
-  std::vector<int64_t> cp = c->h_cons_ptr;
-  if (cp.empty()) cp.assign((size_t)c->n_dofs + 1, 0);
   std::vector<int64_t> rp;
   std::vector<int32_t> cols;
-  build_constrained_graph(c->n_elem, c->nl, c->h_elem_dofs.data(), c->n_dofs, cp.data(), c->h_cons_col.data(), rp,
-                          cols, host_threads());
+  // on the device; the host build where an element list or a row outgrows
+  // the device buffers, or a constraint row refers to a constrained dof
+  const bool on_device = c->n_dofs < INT32_MAX && c->n_elem * (int64_t)c->nl < INT32_MAX &&
+                         device_constrained_graph(c, rp, cols) == LMG_OK;
+  c->sparsity_on_device = on_device;
+  if (!on_device) {
+    std::vector<int64_t> cp = c->h_cons_ptr;
+    if (cp.empty()) cp.assign((size_t)c->n_dofs + 1, 0);
+    build_constrained_graph(c->n_elem, c->nl, c->h_elem_dofs.data(), c->n_dofs, cp.data(), c->h_cons_col.data(), rp,
+                            cols, host_threads());
+  }
   if ((int64_t)cols.size() >= INT32_MAX) return fail(c, LMG_ERR_UNSUPPORTED, "nnz exceeds 32-bit CSR");
   c->nnz = (int64_t)cols.size();
   c->h_row_ptr.resize((size_t)c->n_dofs + 1);
   for (size_t r = 0; r < rp.size(); ++r) c->h_row_ptr[r] = (int32_t)rp[r];
   c->h_col.swap(cols);
-  LMG_CUDA(c, dupload(c, c->d_row_ptr, c->h_row_ptr.data(), c->h_row_ptr.size()));
-  LMG_CUDA(c, dupload(c, c->d_col, c->h_col.data(), c->h_col.size()));
+  if (!on_device) {
+    LMG_CUDA(c, dupload(c, c->d_row_ptr, c->h_row_ptr.data(), c->h_row_ptr.size()));
+    LMG_CUDA(c, dupload(c, c->d_col, c->h_col.data(), c->h_col.size()));
+  }
   LMG_CUDA(c, dalloc(c->d_K, (size_t)c->nnz));
   LMG_CUDA(c, dalloc(c->d_F, (size_t)c->n_dofs));
   LMG_CUDA(c, cudaStreamSynchronize(c->stream));

@@ -92,11 +92,15 @@ struct lmg_ctx {
   // per-pattern HIERARCHIC elements (hier3.cu): cubic hexes, tets and prisms,
   // quadratic prisms; general path
   bool hier3 = false;
+  bool sparsity_on_device = false;  // the general path's graph came from device_constrained_graph
   int32_t *d_h3batch = nullptr, *d_h3order = nullptr;  // element batches of one orientation pattern
   float2 *d_h3D = nullptr;           // per-pattern reference tensors, double-float pairs
+  float *d_h3Df = nullptr;           // the same rounded to FP32 (mixed form)
   double *d_h3M = nullptr, *d_h3gd = nullptr;
   int64_t h3_nbatch = 0;
   int h3_patterns = 0;
+  int h3_tile = 8;                    // elements per CTA tile (4, 8, 16 or 32; the batch tuner picks it)
+  std::vector<int32_t> h3_order, h3_pid;  // host copies: elements sorted by pattern, pattern of each
   // PerfLog-style stage timing (CUDA events on the context stream)
   bool perflog = false;
   std::vector<cudaEvent_t> ev;       // 3 per logged assemble call
@@ -146,6 +150,9 @@ inline cudaError_t dupload(lmg_ctx *c, T *&p, const T *h, size_t n) {
 
 // general.cu path (context_general.cu)
 lmg_status general_sparsity(lmg_ctx *c);   // CSR with the constraint couplings
+// find_connected_dofs on the device: rows into rp / cols and d_row_ptr /
+// d_col; LMG_ERR_UNSUPPORTED when the host build must take over.
+lmg_status device_constrained_graph(lmg_ctx *c, std::vector<int64_t> &rp, std::vector<int32_t> &cols);
 lmg_status general_plan(lmg_ctx *c);       // constraint columns, slot plan, buffers
 // element and constraint kernels; mixed: FP32 contraction, FP64 map and sums
 lmg_status general_assemble(lmg_ctx *c, bool mixed);
@@ -160,6 +167,9 @@ void hier3_free(lmg_ctx *c);
 lmg_status hier3_form_set(lmg_ctx *c, int32_t form, int32_t q_order, const double *elem_coef,
                           const double *nodal_f);
 void launch_hier3(lmg_ctx *c, bool mixed);
+// Regroups the per-pattern elements into CTA tiles of `tile` elements (4, 8,
+// 16 or 32); the element matrices do not depend on the grouping.
+lmg_status hier3_set_tile(lmg_ctx *c, int tile);
 bool hier3_masks(const lmg_ctx *c);  // Dirichlet rows applied by the element kernel
 void general_free(lmg_ctx *c);             // plan and work buffers
 

@@ -415,8 +415,12 @@ __global__ void __launch_bounds__(128) k_constrain(ConsArgs c) {
   }
 }
 
-// K[s] = sum of the slot's contributions in element order (FP64 sums of the
-// FP64 or FP32 element entries); F likewise per dof in FP64.
+// K[s] = sum of the slot's contributions in element order; F likewise per
+// dof in FP64.  FP64 drop-in: FP64 sums of the FP64 element entries.  Mixed
+// form: the FP32 entries are summed in double-float on the FP32 pipe (TwoSum
+// on the high parts, errors collected in the low part, a 48-bit significand)
+// and rounded to FP64 once -- widening each entry to FP64 first would put two
+// FP64-pipe operations on every contribution.
 template <typename T>
 __global__ void k_gather_full(int64_t nnz, const int64_t *__restrict__ cptr, const uint32_t *__restrict__ coff,
                               const T *__restrict__ E, double *__restrict__ K, int64_t n_dofs,
@@ -425,9 +429,20 @@ __global__ void k_gather_full(int64_t nnz, const int64_t *__restrict__ cptr, con
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < nnz + n_dofs; s += stride) {
     if (s < nnz) {
-      double v = 0.0;
-      for (int64_t t = cptr[s]; t < cptr[s + 1]; ++t) v += (double)E[coff[t]];
-      K[s] = v;
+      if constexpr (sizeof(T) == 4) {
+        float hi = 0.f, lo = 0.f;
+        for (int64_t t = cptr[s]; t < cptr[s + 1]; ++t) {
+          const float x = E[coff[t]];
+          const float sum = __fadd_rn(hi, x), bb = __fsub_rn(sum, hi);
+          lo = __fadd_rn(lo, __fadd_rn(__fsub_rn(hi, __fsub_rn(sum, bb)), __fsub_rn(x, bb)));
+          hi = sum;
+        }
+        K[s] = (double)hi + (double)lo;
+      } else {
+        double v = 0.0;
+        for (int64_t t = cptr[s]; t < cptr[s + 1]; ++t) v += (double)E[coff[t]];
+        K[s] = v;
+      }
     } else {
       const int64_t d = s - nnz;
       double v = 0.0;

@@ -37,7 +37,7 @@ namespace lmg {
 
 namespace {
 
-constexpr int H3T = 256, H3B = 8;
+constexpr int H3T = 256;
 
 struct H3Args {
   int64_t n_batch;
@@ -50,6 +50,7 @@ struct H3Args {
   const double *nodal_f;    // [n_nodes] or null
   const uint64_t *cmask;    // [n_elem] constrained local dofs, or null (no mask)
   const float2 *D;          // [P][6][N*N] double-float pairs
+  const float *Df;          // [P][6][N*N] FP32 (mixed form)
   const double *M;          // [P][N][G]
   const double *gd0;        // [G][3]
   void *Kraw;               // [n_elem][N][N] element matrices: double (FP64 drop-in) or float (mixed)
@@ -63,7 +64,7 @@ struct H3Args {
 // FP64 drop-in (MIXED false): the contraction in double-float, each entry
 // rounded to FP64 once; mixed form: the contraction in FP32.  The map is FP64
 // in both.
-template <int N, int G, bool MIXED>
+template <int N, int G, bool MIXED, int H3B>
 __global__ void __launch_bounds__(H3T) k_elem_pattern(H3Args a) {
   static_assert(N <= 64 && G <= 32, "one mask word per element, one lane per map node");
   __shared__ double sA[H3B][8];   // A_0..A_5, detJ
@@ -73,11 +74,11 @@ __global__ void __launch_bounds__(H3T) k_elem_pattern(H3Args a) {
   __shared__ double sJ[H3B][9];      // map derivatives J[m*3+d] = dx_d/dxi_m
   __shared__ uint64_t sm[H3B];
   __shared__ int32_t se[H3B];
-  const int t = threadIdx.x, w = t >> 5, lane = t & 31;
+  const int t = threadIdx.x, lane = t & 31;
   for (int64_t bi = blockIdx.x; bi < a.n_batch; bi += gridDim.x) {
     const int p = a.batch[3 * bi], first = a.batch[3 * bi + 1], cnt = a.batch[3 * bi + 2];
     __syncthreads();
-    if (w < cnt) {  // warp w: geometry of the batch's element w (compute_affine_map)
+    for (int w = t >> 5; w < cnt; w += H3T / 32) {  // warp: geometry of the tile's element w (compute_affine_map)
       const int32_t e = a.order[first + w];
       if (lane < G) {
         const int64_t nd = a.conn[(int64_t)e * a.npe + lane];
@@ -138,13 +139,18 @@ __global__ void __launch_bounds__(H3T) k_elem_pattern(H3Args a) {
     __syncthreads();
     // K_ij = sum_k A_k D_k[i][j] in double-float arithmetic (FP32 pipe)
     const float2 *Dp = a.D + (size_t)p * 6 * (N * N);
+    const float *Dfp = a.Df + (size_t)p * 6 * (N * N);
     for (int idx = t; idx < N * N; idx += H3T) {
       const int i = idx / N, j = idx - i * N;
       DF d[6];
 #pragma unroll
       for (int k = 0; k < 6; ++k) {
-        const float2 x = Dp[k * (N * N) + idx];
-        d[k] = DF{x.x, x.y};
+        if constexpr (MIXED) {
+          d[k] = DF{Dfp[k * (N * N) + idx], 0.f};
+        } else {
+          const float2 x = Dp[k * (N * N) + idx];
+          d[k] = DF{x.x, x.y};
+        }
       }
       for (int b = 0; b < cnt; ++b) {
         const bool msk = ((sm[b] >> i) | (sm[b] >> j)) & 1ull;
@@ -180,6 +186,7 @@ void hier3_free(lmg_ctx *c) {
   dfree(c->d_h3batch);
   dfree(c->d_h3order);
   dfree(c->d_h3D);
+  dfree(c->d_h3Df);
   dfree(c->d_h3M);
   dfree(c->d_h3gd);
   c->h3_nbatch = 0;
@@ -211,18 +218,24 @@ lmg_status hier3_form_set(lmg_ctx *c, int32_t form, int32_t q_order, const doubl
                  : build_prism_tables(h, order, q_order, c->n_elem, c->h_xyz.data(), c->h_conn.data(), c->npe));
   if (!err.empty()) return fail(c, LMG_ERR_UNSUPPORTED, "form_set: " + err);
   hier3_free(c);
-  LMG_CUDA(c, dupload(c, c->d_h3batch, h.batch.data(), h.batch.size()));
   LMG_CUDA(c, dupload(c, c->d_h3order, h.order.data(), h.order.size()));
+  c->h3_order = h.order;
+  c->h3_pid.assign((size_t)c->n_elem, 0);
+  for (size_t b = 0; b + 2 < h.batch.size(); b += 3)
+    for (int32_t k = 0; k < h.batch[b + 2]; ++k) c->h3_pid[(size_t)(h.batch[b + 1] + k)] = h.batch[b];
   std::vector<float2> dp(h.Dp.size());
+  std::vector<float> df(h.Dp.size());
   for (size_t i = 0; i < dp.size(); ++i) {
     const DF x = df_split(h.Dp[i]);
     dp[i] = make_float2(x.hi, x.lo);
+    df[i] = x.hi;
   }
   LMG_CUDA(c, dupload(c, c->d_h3D, dp.data(), dp.size()));
+  LMG_CUDA(c, dupload(c, c->d_h3Df, df.data(), df.size()));
   LMG_CUDA(c, dupload(c, c->d_h3M, h.Mp.data(), h.Mp.size()));
   LMG_CUDA(c, dupload(c, c->d_h3gd, h.gd0.data(), h.gd0.size()));
-  c->h3_nbatch = (int64_t)h.batch.size() / 3;
   c->h3_patterns = h.P;
+  if (lmg_status st = hier3_set_tile(c, c->h3_tile)) return st;
   FETables t;
   t.elem_type = c->elem_type;
   t.fe_order = order;
@@ -251,6 +264,45 @@ lmg_status hier3_form_set(lmg_ctx *c, int32_t form, int32_t q_order, const doubl
 
 bool hier3_masks(const lmg_ctx *c) { return c->hier3 && !c->has_rows; }
 
+lmg_status hier3_set_tile(lmg_ctx *c, int tile) {
+  if (tile != 4 && tile != 8 && tile != 16 && tile != 32) return fail(c, LMG_ERR_ARG, "pattern tile must be 4, 8, 16 or 32");
+  std::vector<int32_t> batch;
+  const int64_t n = (int64_t)c->h3_order.size();
+  for (int64_t i = 0; i < n;) {
+    const int32_t p = c->h3_pid[(size_t)i];
+    int64_t j = i;
+    while (j < n && j - i < tile && c->h3_pid[(size_t)j] == p) ++j;
+    batch.push_back(p);
+    batch.push_back((int32_t)i);
+    batch.push_back((int32_t)(j - i));
+    i = j;
+  }
+  LMG_CUDA(c, dupload(c, c->d_h3batch, batch.data(), batch.size()));
+  LMG_CUDA(c, cudaStreamSynchronize(c->stream));
+  c->h3_nbatch = (int64_t)batch.size() / 3;
+  c->h3_tile = tile;
+  return LMG_OK;
+}
+
+namespace {
+template <int B>
+void launch_tiles(lmg_ctx *c, bool mixed, const H3Args &a, int grid) {
+  if (c->tab.n == 20) {
+    if (mixed) k_elem_pattern<20, 14, true, B><<<grid, H3T, 0, c->stream>>>(a);
+    else k_elem_pattern<20, 14, false, B><<<grid, H3T, 0, c->stream>>>(a);
+  } else if (c->tab.n == 18) {
+    if (mixed) k_elem_pattern<18, 6, true, B><<<grid, H3T, 0, c->stream>>>(a);
+    else k_elem_pattern<18, 6, false, B><<<grid, H3T, 0, c->stream>>>(a);
+  } else if (c->tab.n == 40) {
+    if (mixed) k_elem_pattern<40, 6, true, B><<<grid, H3T, 0, c->stream>>>(a);
+    else k_elem_pattern<40, 6, false, B><<<grid, H3T, 0, c->stream>>>(a);
+  } else {
+    if (mixed) k_elem_pattern<64, 27, true, B><<<grid, H3T, 0, c->stream>>>(a);
+    else k_elem_pattern<64, 27, false, B><<<grid, H3T, 0, c->stream>>>(a);
+  }
+}
+}  // namespace
+
 void launch_hier3(lmg_ctx *c, bool mixed) {
   H3Args a{};
   a.n_batch = c->h3_nbatch;
@@ -263,6 +315,7 @@ void launch_hier3(lmg_ctx *c, bool mixed) {
   a.nodal_f = c->d_f;
   a.cmask = hier3_masks(c) ? c->d_cmask : nullptr;
   a.D = c->d_h3D;
+  a.Df = c->d_h3Df;
   a.M = c->d_h3M;
   a.gd0 = c->d_h3gd;
   a.Kraw = c->d_Ebuf;
@@ -272,18 +325,11 @@ void launch_hier3(lmg_ctx *c, bool mixed) {
   const int64_t want = (int64_t)c->n_sm * 8;
   const int grid = (int)(a.n_batch < want ? a.n_batch : want);
   if (grid <= 0) return;
-  if (c->tab.n == 20) {
-    if (mixed) k_elem_pattern<20, 14, true><<<grid, H3T, 0, c->stream>>>(a);
-    else k_elem_pattern<20, 14, false><<<grid, H3T, 0, c->stream>>>(a);
-  } else if (c->tab.n == 18) {
-    if (mixed) k_elem_pattern<18, 6, true><<<grid, H3T, 0, c->stream>>>(a);
-    else k_elem_pattern<18, 6, false><<<grid, H3T, 0, c->stream>>>(a);
-  } else if (c->tab.n == 40) {
-    if (mixed) k_elem_pattern<40, 6, true><<<grid, H3T, 0, c->stream>>>(a);
-    else k_elem_pattern<40, 6, false><<<grid, H3T, 0, c->stream>>>(a);
-  } else {
-    if (mixed) k_elem_pattern<64, 27, true><<<grid, H3T, 0, c->stream>>>(a);
-    else k_elem_pattern<64, 27, false><<<grid, H3T, 0, c->stream>>>(a);
+  switch (c->h3_tile) {
+    case 4: launch_tiles<4>(c, mixed, a, grid); break;
+    case 16: launch_tiles<16>(c, mixed, a, grid); break;
+    case 32: launch_tiles<32>(c, mixed, a, grid); break;
+    default: launch_tiles<8>(c, mixed, a, grid); break;
   }
 }
 

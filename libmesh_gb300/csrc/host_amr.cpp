@@ -367,6 +367,90 @@ struct RowTable {
   }
 };
 
+std::string finish_constraint_rows(RowTable &rows, int64_t n_dofs, const uint8_t *dirichlet, ConstraintRows &out);
+
+// The same rows from hanging-node rows formed on the device: dof d's row has
+// cnt[d] entries (-1: no row) at col / val[d * width ..], in ascending column
+// order.  Dirichlet rows are added for the dofs still free.  process_constraints
+// only changes rows that refer to another constrained dof; the sweep below
+// visits exactly those (ascending, repeated until none changes) and reads every
+// other row from the raw arrays, which gives the same substitutions in the same
+// order as a sweep over all rows (an unchanged row leaves the set at its first
+// visit without touching any other row).
+std::string constraint_rows_from_raw(int64_t n_dofs, const int32_t *cnt, const int32_t *col, const double *val,
+                                     int width, const uint8_t *dirichlet, ConstraintRows &out) {
+  std::vector<int32_t> len(cnt, cnt + n_dofs);
+  if (dirichlet)
+    for (int64_t d = 0; d < n_dofs; ++d)
+      if (dirichlet[d] && len[(size_t)d] < 0) len[(size_t)d] = 0;
+  auto has = [&](int32_t d) { return d >= 0 && d < n_dofs && len[(size_t)d] >= 0; };
+  std::map<int32_t, Row> chg;  // rows that refer to constrained dofs
+  for (int64_t d = 0; d < n_dofs; ++d)
+    for (int k = 0; k < std::max(len[(size_t)d], 0); ++k)
+      if (col[d * width + k] != (int32_t)d && has(col[d * width + k])) {
+        Row &row = chg[(int32_t)d];
+        for (int j = 0; j < len[(size_t)d]; ++j) row.emplace(col[d * width + j], val[d * width + j]);
+        break;
+      }
+  std::set<int32_t> unexpanded;
+  for (const auto &r : chg) unexpanded.insert(unexpanded.end(), r.first);
+  auto other = [&](int32_t x, std::vector<std::pair<int32_t, double>> &sub) {
+    sub.clear();
+    auto it = chg.find(x);
+    if (it != chg.end()) {
+      for (const auto &item : it->second) sub.push_back(item);
+    } else {
+      for (int j = 0; j < len[(size_t)x]; ++j) sub.emplace_back(col[(int64_t)x * width + j], val[(int64_t)x * width + j]);
+    }
+  };
+  std::vector<std::pair<int32_t, double>> sub;
+  while (!unexpanded.empty())
+    for (auto i = unexpanded.begin(); i != unexpanded.end();) {
+      auto it = chg.find(*i);
+      if (it == chg.end()) {  // a row that never changes
+        i = unexpanded.erase(i);
+        continue;
+      }
+      Row &row = it->second;
+      std::vector<int32_t> expand;
+      for (const auto &item : row)
+        if (item.first != *i && has(item.first)) {
+          unexpanded.insert(item.first);
+          expand.push_back(item.first);
+        }
+      for (int32_t x : expand) {
+        const double coef = row[x];
+        other(x, sub);
+        for (const auto &e : sub) row[e.first] += e.second * coef;
+        row.erase(x);
+      }
+      if (expand.empty()) i = unexpanded.erase(i);
+      else ++i;
+    }
+  out.dofs.clear();
+  out.ptr.assign(1, 0);
+  out.col.clear();
+  out.val.clear();
+  for (int64_t d = 0; d < n_dofs; ++d) {
+    if (len[(size_t)d] < 0) continue;
+    out.dofs.push_back((int32_t)d);
+    auto it = chg.find((int32_t)d);
+    if (it != chg.end()) {
+      for (const auto &item : it->second) {
+        out.col.push_back(item.first);
+        out.val.push_back(item.second);
+      }
+    } else {
+      for (int j = 0; j < len[(size_t)d]; ++j) {
+        out.col.push_back(col[d * width + j]);
+        out.val.push_back(val[d * width + j]);
+      }
+    }
+    out.ptr.push_back((int64_t)out.col.size());
+  }
+  return "";
+}
+
 std::string amr_constraint_rows(const HostMesh &m, int n_vars, const int32_t *elem_dofs, int64_t n_dofs,
                                 const uint8_t *dirichlet, ConstraintRows &out) {
   RowTable rows(n_dofs);
@@ -430,6 +514,12 @@ std::string amr_constraint_rows(const HostMesh &m, int n_vars, const int32_t *el
         }
       }
   }
+  return finish_constraint_rows(rows, n_dofs, dirichlet, out);
+}
+
+// Dirichlet rows for the dofs still free, process_constraints, and the
+// output in ascending dof order.
+std::string finish_constraint_rows(RowTable &rows, int64_t n_dofs, const uint8_t *dirichlet, ConstraintRows &out) {
   if (dirichlet)
     for (int64_t d = 0; d < n_dofs; ++d)
       if (dirichlet[d] && !rows.count((int32_t)d)) rows[(int32_t)d];
@@ -509,9 +599,15 @@ lmg_status lmg_mesh_tree(const lmg_mesh *mesh, int64_t *n_all, int32_t *all_conn
   return LMG_OK;
 }
 
-lmg_status lmg_constraint_rows(const lmg_mesh *mesh, int32_t n_vars, const int32_t *elem_dofs, int64_t n_dofs,
-                               const uint8_t *dirichlet, uint8_t *constrained, int64_t *cons_ptr,
-                               int32_t *cons_col, double *cons_val, int64_t cap) {
+}  // extern "C"
+
+namespace {
+
+// lmg_constraint_rows with the hanging-node rows formed on the host
+// (device < 0) or on the given device.
+lmg_status constraint_rows(const lmg_mesh *mesh, int32_t device, int32_t n_vars, const int32_t *elem_dofs,
+                           int64_t n_dofs, const uint8_t *dirichlet, uint8_t *constrained, int64_t *cons_ptr,
+                           int32_t *cons_col, double *cons_val, int64_t cap) {
   if (!mesh || n_vars <= 0 || !elem_dofs || n_dofs <= 0 || !cons_ptr) return LMG_ERR_ARG;
   try {
     // The count call and the fill call of a caller see the same inputs: keep
@@ -520,13 +616,25 @@ lmg_status lmg_constraint_rows(const lmg_mesh *mesh, int32_t n_vars, const int32
     auto mix = [&](uint64_t x) { key = (key ^ x) * 1099511628211ull; };
     mix((uint64_t)n_vars);
     mix((uint64_t)n_dofs);
+    mix((uint64_t)(int64_t)device);
     const int64_t nl = (int64_t)mesh->m.npe * n_vars;
     for (int64_t i = 0; i < mesh->m.n_elem() * nl; ++i) mix((uint64_t)(uint32_t)elem_dofs[i]);
     for (int64_t d = 0; d < n_dofs; ++d) mix(dirichlet ? dirichlet[d] : 0);
     lmg_mesh *mm = const_cast<lmg_mesh *>(mesh);
     if (!mm->rows_valid || mm->rows_key != key) {
       mm->rows_valid = false;
-      const std::string err = lmg::amr_constraint_rows(mesh->m, n_vars, elem_dofs, n_dofs, dirichlet, mm->rows);
+      std::string err;
+      if (device < 0) {
+        err = lmg::amr_constraint_rows(mesh->m, n_vars, elem_dofs, n_dofs, dirichlet, mm->rows);
+      } else {
+        std::vector<int32_t> cnt, col;
+        std::vector<double> val;
+        err = lmg::amr_raw_rows_device(mesh->m, device, n_vars, elem_dofs, n_dofs, cnt, col, val);
+        if (err.rfind("device rows", 0) == 0) return LMG_ERR_CUDA;
+        if (err.empty())
+          err = lmg::constraint_rows_from_raw(n_dofs, cnt.data(), col.data(), val.data(), lmg::AMR_ROW_WIDTH,
+                                              dirichlet, mm->rows);
+      }
       if (!err.empty()) return LMG_ERR_BOUNDS;
       mm->rows_key = key;
       mm->rows_valid = true;
@@ -554,6 +662,26 @@ lmg_status lmg_constraint_rows(const lmg_mesh *mesh, int32_t n_vars, const int32
   } catch (const std::bad_alloc &) {
     return LMG_ERR_OOM;
   }
+}
+
+}  // namespace
+
+extern "C" {
+
+lmg_status lmg_constraint_rows(const lmg_mesh *mesh, int32_t n_vars, const int32_t *elem_dofs, int64_t n_dofs,
+                               const uint8_t *dirichlet, uint8_t *constrained, int64_t *cons_ptr,
+                               int32_t *cons_col, double *cons_val, int64_t cap) {
+  return constraint_rows(mesh, -1, n_vars, elem_dofs, n_dofs, dirichlet, constrained, cons_ptr, cons_col, cons_val,
+                         cap);
+}
+
+lmg_status lmg_constraint_rows_device(const lmg_mesh *mesh, int32_t device, int32_t n_vars,
+                                      const int32_t *elem_dofs, int64_t n_dofs, const uint8_t *dirichlet,
+                                      uint8_t *constrained, int64_t *cons_ptr, int32_t *cons_col, double *cons_val,
+                                      int64_t cap) {
+  if (device < 0) return LMG_ERR_ARG;
+  return constraint_rows(mesh, device, n_vars, elem_dofs, n_dofs, dirichlet, constrained, cons_ptr, cons_col,
+                         cons_val, cap);
 }
 
 }  // extern "C"

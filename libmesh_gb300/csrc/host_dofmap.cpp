@@ -397,6 +397,26 @@ lmg_status lmg_dofmap_distribute_fe(int64_t n_nodes, int64_t n_elem, int32_t ele
   return LMG_OK;
 }
 
+lmg_status lmg_dofmap_distribute_device(int32_t device, int64_t n_nodes, int64_t n_elem, int32_t elem_type,
+                                        const int32_t *conn, int32_t n_vars, int32_t fe_order, int64_t *n_dofs,
+                                        int32_t *elem_dofs) {
+  if (!conn || !n_dofs || n_nodes < 0 || n_elem < 0 || n_vars <= 0 || device < 0) return LMG_ERR_ARG;
+  const int npe = lmg::nodes_per_elem(elem_type);
+  if (!npe) return LMG_ERR_UNSUPPORTED;
+  for (int64_t i = 0; i < n_elem * npe; ++i)
+    if (conn[i] < 0 || conn[i] >= n_nodes) return LMG_ERR_BOUNDS;
+  try {
+    int64_t nd = 0;
+    const std::string err =
+        lmg::distribute_dofs_device(device, n_nodes, n_elem, elem_type, conn, n_vars, fe_order, nd, elem_dofs);
+    if (!err.empty()) return err.rfind("device", 0) == 0 ? LMG_ERR_CUDA : LMG_ERR_UNSUPPORTED;
+    *n_dofs = nd;
+  } catch (const std::bad_alloc &) {
+    return LMG_ERR_OOM;
+  }
+  return LMG_OK;
+}
+
 lmg_status lmg_dirichlet_dofs_fe(int64_t n_elem, int32_t elem_type, int32_t fe_order, int32_t n_vars,
                                  const int32_t *elem_dofs, const int8_t *side_bid, const int32_t *bids,
                                  int32_t n_bids, const int32_t *vars, int32_t n_vars_bc, int64_t n_dofs,

@@ -76,6 +76,18 @@ struct ConstraintRows {
 };
 std::string amr_constraint_rows(const HostMesh &m, int n_vars, const int32_t *elem_dofs, int64_t n_dofs,
                                 const uint8_t *dirichlet, ConstraintRows &out);
+// The hanging-node rows formed on the device (amr_rows.cu): dof d's row has
+// cnt[d] entries (-1: none) at col / val[d * width ..]; the Dirichlet rows,
+// process_constraints and the output follow on the host as above.
+std::string constraint_rows_from_raw(int64_t n_dofs, const int32_t *cnt, const int32_t *col, const double *val,
+                                     int width, const uint8_t *dirichlet, ConstraintRows &out);
+std::string amr_raw_rows_device(const HostMesh &m, int device, int n_vars, const int32_t *elem_dofs, int64_t n_dofs,
+                                std::vector<int32_t> &cnt, std::vector<int32_t> &col, std::vector<double> &val);
+constexpr int AMR_ROW_WIDTH = 9;  // entries of a raw hanging-node row (QUAD9 side)
+// distribute_dofs on the device (dofs_device.cu): the numbering and dof_indices
+// of lmg_dofmap_distribute_fe; returns an error message or "".
+std::string distribute_dofs_device(int device, int64_t n_nodes, int64_t n_elem, int elem_type, const int32_t *conn,
+                                   int n_vars, int fe_order, int64_t &n_dofs, int32_t *elem_dofs);
 
 // ---------------------------------------------------------------- rng
 // splitmix64; u01 maps the top 53 bits to [0,1).

@@ -38,6 +38,7 @@ def run(form, m, dm, k, f, fo, qo, params=None):
     asm = lm.GpuAssembly(form, fo, qo, elem_coef=k, nodal_f=f, params=params)
     asm.init(m, dm)
     rp, ci = asm.sparsity()
+    assert asm.sparsity_on_device()  # find_connected_dofs on the device (compared with the oracle's below)
     K, F = asm.assemble()
     K2, F2 = asm.assemble()      # repeat: deterministic
     asm.close()
