@@ -421,6 +421,21 @@ lmg_status lmg_batch_assemble(lmg_batch *batch, int32_t precision);
 lmg_status lmg_batch_synchronize(lmg_batch *batch, int64_t *first_failed);
 /* The batch stream, kernels per graph replay, and the tuned CTAs per SM of
  * the first n contexts (any pointer may be NULL). */
+/* Persistent mode (on = 1): each replay is one persistent kernel launch (after
+ * a clear of its queue counters) whose CTAs take work items from a global
+ * queue -- every member's element tiles (per-pattern form: the HIERARCHIC
+ * members' own tables, and for one-variable affine Poisson members of the
+ * block path tables made from their FE tables), then ranges of every
+ * member's insertion, each waiting on its member's tiles.  Results equal the
+ * members' own assemblies to rounding (1e-13 of the entry); a member that
+ * cannot take the per-pattern form makes lmg_batch_assemble return
+ * LMG_ERR_UNSUPPORTED.  lmg_batch_tune then picks the elements per CTA tile
+ * (8, 16, 32) and the CTAs per SM of the launch by timing replays. */
+lmg_status lmg_batch_set_persistent(lmg_batch *batch, int32_t on);
+/* The message of the batch's last failure (NUL-terminated, cut to cap). */
+lmg_status lmg_batch_last_error(lmg_batch *batch, char *msg, int32_t cap);
+/* Tuned tile and CTAs per SM (0: as many as fit) and the work items of a replay. */
+lmg_status lmg_batch_persistent_info(lmg_batch *batch, int32_t *tile, int32_t *ctas_per_sm, int64_t *items);
 lmg_status lmg_batch_info(lmg_batch *batch, void **stream, int64_t *launches_per_replay,
                           int32_t *ctas_per_sm, int32_t n);
 

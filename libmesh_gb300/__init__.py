@@ -419,15 +419,31 @@ class Batch:
         check(lib().lmg_batch_add(self.h, assembly.ctx))
         self.members.append(assembly)
 
+    def _ok(self, status):
+        if status != 0:
+            buf = C.create_string_buffer(512)
+            lib().lmg_batch_last_error(self.h, buf, 512)
+            raise LmgError(status, buf.value.decode(errors="replace"))
+
     def tune(self, precision=FP64, reps=3):
-        check(lib().lmg_batch_tune(self.h, precision, reps))
+        self._ok(lib().lmg_batch_tune(self.h, precision, reps))
 
     def assemble(self, precision=FP64):
-        check(lib().lmg_batch_assemble(self.h, precision))
+        self._ok(lib().lmg_batch_assemble(self.h, precision))
 
     def synchronize(self):
         bad = C.c_int64(-1)
-        check(lib().lmg_batch_synchronize(self.h, C.byref(bad)))
+        self._ok(lib().lmg_batch_synchronize(self.h, C.byref(bad)))
+
+    def set_persistent(self, on=True):
+        """One persistent kernel launch per replay (every member's element
+        tiles and insertion from one work queue)."""
+        check(lib().lmg_batch_set_persistent(self.h, 1 if on else 0))
+
+    def persistent_info(self):
+        t, c, n = C.c_int32(), C.c_int32(), C.c_int64()
+        check(lib().lmg_batch_persistent_info(self.h, C.byref(t), C.byref(c), C.byref(n)))
+        return t.value, c.value, n.value
 
     def info(self):
         s, l = C.c_void_p(), C.c_int64()

@@ -81,6 +81,9 @@ SIGNATURES = {
     "lmg_batch_assemble": [_p, _i32],
     "lmg_batch_synchronize": [_p, _pi64],
     "lmg_batch_info": [_p, C.POINTER(_p), _pi64, _p, _i32],
+    "lmg_batch_set_persistent": [_p, _i32],
+    "lmg_batch_last_error": [_p, C.c_char_p, _i32],
+    "lmg_batch_persistent_info": [_p, _pi32, _pi32, _pi64],
     "lmg_probe_fp64": [_i32, _pf64],
     "lmg_probe_fp64_tensor": [_i32, _pf64],
 }

@@ -21,7 +21,23 @@
 #include <string>
 #include <vector>
 
+#include "batch_persistent.cuh"
 #include "context_internal.cuh"
+
+// Device state of the persistent mode: members, work items, queue head,
+// per-member tile counters and a status word.
+struct PersistentState {
+  lmg::PMember *mem = nullptr;
+  lmg::PItem *items = nullptr;
+  int64_t n_items = 0;
+  unsigned long long *head = nullptr;
+  unsigned int *done = nullptr;
+  int *status = nullptr;
+  int tile = 0, grid = 0;   // the settings the members and items were prepared for
+  bool mixed = false;
+  cudaGraphExec_t exec = nullptr;
+  cudaGraph_t graph = nullptr;
+};
 
 struct lmg_batch {
   int device = 0;
@@ -34,9 +50,21 @@ struct lmg_batch {
   bool warm[2] = {false, false};
   int64_t launches = 0;    // kernels in one replay
   std::string err;
+  bool persistent = false;     // one persistent launch per replay (lmg_batch_set_persistent)
+  int p_tile = 8, p_ctas = 0;  // its tile (elements per CTA) and CTAs per SM (0: occupancy)
+  PersistentState ps;
 };
 
 namespace {
+
+void drop_persistent(lmg_batch *b) {
+  PersistentState &ps = b->ps;
+  if (ps.exec) cudaGraphExecDestroy(ps.exec);
+  if (ps.graph) cudaGraphDestroy(ps.graph);
+  for (void *p : {(void *)ps.mem, (void *)ps.items, (void *)ps.head, (void *)ps.done, (void *)ps.status})
+    if (p) cudaFree(p);
+  ps = PersistentState();
+}
 
 void drop_graphs(lmg_batch *b) {
   for (int p = 0; p < 2; ++p) {
@@ -45,6 +73,7 @@ void drop_graphs(lmg_batch *b) {
     b->exec[p] = nullptr;
     b->graph[p] = nullptr;
   }
+  drop_persistent(b);
 }
 
 lmg_status bfail(lmg_batch *b, lmg_status code, const std::string &msg) {
@@ -63,6 +92,100 @@ lmg_status run_all(lmg_batch *b, int precision) {
     const lmg_status st = lmg_synchronize(c);
     if (st) return bfail(b, st, "batch: " + c->err);
   }
+  return LMG_OK;
+}
+
+// Members in per-pattern form with their insertion plans, the work list
+// (every member's element tiles, then every member's insertion ranges) and
+// the graph of one replay: the queue head and tile counters cleared, then the
+// persistent kernel.
+lmg_status prepare_persistent(lmg_batch *b, int precision) {
+  const bool mixed = precision == LMG_MIXED;
+  PersistentState &ps = b->ps;
+  const int tile = b->p_tile;
+  int n_sm = 0;
+  cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, b->device);
+  const int per_sm = b->p_ctas > 0 ? b->p_ctas : lmg::persistent_ctas_per_sm(mixed, tile);
+  const int grid = n_sm * per_sm;
+  if (ps.exec && ps.tile == tile && ps.grid == grid && ps.mixed == mixed) return LMG_OK;
+  drop_persistent(b);
+  std::vector<lmg::PMember> mem;
+  std::vector<lmg::PItem> items;
+  for (size_t i = 0; i < b->ctx.size(); ++i) {
+    lmg_ctx *c = b->ctx[i];
+    lmg_status st = c->hier3 ? lmg::hier3_set_tile(c, tile) : lmg::pattern_from_block(c);
+    if (!st && !c->hier3) st = lmg::hier3_set_tile(c, tile);
+    if (!st && !c->gen_plan) st = lmg::general_plan(c);
+    if (st) return bfail(b, st, "batch: member " + std::to_string(i) + ": " + c->err);
+    lmg::PMember m{};
+    m.el.n_batch = c->h3_nbatch;
+    m.el.batch = c->d_h3batch;
+    m.el.order = c->d_h3order;
+    m.el.xyz = c->d_xyz;
+    m.el.conn = c->d_conn;
+    m.el.npe = c->npe;
+    m.el.coef = c->d_coef;
+    m.el.nodal_f = c->d_f;
+    m.el.cmask = c->d_cmask;
+    m.el.D = c->d_h3D;
+    m.el.Df = c->d_h3Df;
+    m.el.M = c->d_h3M;
+    m.el.gd0 = c->d_h3gd;
+    m.el.Kraw = c->d_Ebuf;
+    m.el.Fraw = c->d_Fbuf;
+    m.el.status = c->d_status;
+    m.el.bad_elem = c->d_bad;
+    m.N = c->nl;
+    m.G = c->hier3 ? c->tab.n_geo : c->npe;
+    if (!lmg::persistent_kind_built(m.N, m.G))
+      return bfail(b, LMG_ERR_UNSUPPORTED, "batch: no persistent kernel for member " + std::to_string(i));
+    m.n_tiles = c->h3_nbatch;
+    m.nnz = c->nnz;
+    m.n_dofs = c->n_dofs;
+    m.cptr = c->d_cptr;
+    m.coff = c->d_coff;
+    m.fptr = c->d_gfptr;
+    m.foff = c->d_gfoff;
+    m.K = c->d_K;
+    m.F = c->d_F;
+    mem.push_back(m);
+  }
+  for (size_t i = 0; i < mem.size(); ++i)
+    for (int64_t t = 0; t < mem[i].n_tiles; ++t) items.push_back({(int32_t)i, 0, t});
+  for (size_t i = 0; i < mem.size(); ++i) {
+    const int64_t n = (mem[i].nnz + mem[i].n_dofs + lmg::PB_SLOTS - 1) / lmg::PB_SLOTS;
+    for (int64_t t = 0; t < n; ++t) items.push_back({(int32_t)i, 1, t});
+  }
+  auto up = [&](auto *&d, const auto *h, size_t n) {
+    return cudaMalloc((void **)&d, sizeof(*h) * (n ? n : 1)) == cudaSuccess &&
+           (n == 0 || cudaMemcpy(d, h, sizeof(*h) * n, cudaMemcpyHostToDevice) == cudaSuccess);
+  };
+  if (!up(ps.mem, mem.data(), mem.size()) || !up(ps.items, items.data(), items.size()) ||
+      cudaMalloc((void **)&ps.head, sizeof(unsigned long long)) != cudaSuccess ||
+      cudaMalloc((void **)&ps.done, sizeof(unsigned int) * (mem.size() ? mem.size() : 1)) != cudaSuccess ||
+      cudaMalloc((void **)&ps.status, sizeof(int)) != cudaSuccess ||
+      cudaMemset(ps.status, 0, sizeof(int)) != cudaSuccess) {
+    drop_persistent(b);
+    return bfail(b, LMG_ERR_OOM, "batch: persistent state allocation failed");
+  }
+  ps.n_items = (int64_t)items.size();
+  ps.tile = tile;
+  ps.grid = grid;
+  ps.mixed = mixed;
+  if (cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+    return bfail(b, LMG_ERR_CUDA, "batch: capture failed to start");
+  cudaMemsetAsync(ps.head, 0, sizeof(unsigned long long), b->stream);
+  cudaMemsetAsync(ps.done, 0, sizeof(unsigned int) * mem.size(), b->stream);
+  lmg::launch_batch_persistent(ps.mem, ps.items, ps.n_items, ps.head, ps.done, ps.status, mixed, tile, grid,
+                               b->stream);
+  const cudaError_t le = cudaGetLastError();
+  const cudaError_t ce = cudaStreamEndCapture(b->stream, &ps.graph);
+  if (le != cudaSuccess || ce != cudaSuccess || !ps.graph ||
+      cudaGraphInstantiate(&ps.exec, ps.graph, 0) != cudaSuccess) {
+    drop_persistent(b);
+    return bfail(b, LMG_ERR_CUDA, "batch: persistent graph failed");
+  }
+  b->launches = 1;
   return LMG_OK;
 }
 
@@ -124,6 +247,38 @@ lmg_status lmg_batch_tune(lmg_batch *b, int32_t precision, int32_t reps) {
   if (!b || (precision != LMG_FP64 && precision != LMG_MIXED)) return bfail(b, LMG_ERR_ARG, "batch_tune: bad argument");
   cudaSetDevice(b->device);
   if (reps <= 0) reps = 3;
+  if (b->persistent) {  // the tile (elements per CTA) and CTAs per SM of the one launch, by timing replays
+    static const int tiles[] = {8, 16, 32}, ctas[] = {1, 2, 4, 0};
+    cudaEvent_t e0, e1;
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
+      return bfail(b, LMG_ERR_CUDA, "batch_tune: event creation failed");
+    float best = 1e30f;
+    int bt = b->p_tile, bc = b->p_ctas;
+    lmg_status st = LMG_OK;
+    for (int tl : tiles)
+      for (int k : ctas) {
+        b->p_tile = tl;
+        b->p_ctas = k;
+        if ((st = lmg_batch_assemble(b, precision))) break;
+        cudaEventRecord(e0, b->stream);
+        for (int r = 0; r < reps && !st; ++r) st = lmg_batch_assemble(b, precision);
+        cudaEventRecord(e1, b->stream);
+        if (st || cudaEventSynchronize(e1) != cudaSuccess) break;
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (ms < best) {
+          best = ms;
+          bt = tl;
+          bc = k;
+        }
+      }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    b->p_tile = bt;
+    b->p_ctas = bc;
+    if (st) return st;
+    return lmg_batch_synchronize(b, nullptr);
+  }
   lmg_status st = run_all(b, precision);  // lazy plans and buffers before any timing
   if (st) return st;
   static const int cand[] = {2, 4, 8, 16, 32};
@@ -185,6 +340,19 @@ lmg_status lmg_batch_assemble(lmg_batch *b, int32_t precision) {
   if (!b || (precision != LMG_FP64 && precision != LMG_MIXED)) return bfail(b, LMG_ERR_ARG, "batch_assemble: bad argument");
   if (b->ctx.empty()) return bfail(b, LMG_ERR_STATE, "batch_assemble: no contexts");
   cudaSetDevice(b->device);
+  if (b->persistent) {
+    if (!b->warm[precision == LMG_MIXED ? 1 : 0]) {  // lazy plans and buffers of every member
+      const lmg_status st = run_all(b, precision);
+      if (st) return st;
+      b->warm[precision == LMG_MIXED ? 1 : 0] = true;
+    }
+    const lmg_status st = prepare_persistent(b, precision);
+    if (st) return st;
+    if (cudaGraphLaunch(b->ps.exec, b->stream) != cudaSuccess)
+      return bfail(b, LMG_ERR_CUDA, "batch_assemble: graph launch failed");
+    for (lmg_ctx *c : b->ctx) c->launches += 1;
+    return LMG_OK;
+  }
   const int p = precision == LMG_MIXED ? 1 : 0;
   if (!b->exec[p]) {
     if (!b->warm[p]) {
@@ -233,6 +401,11 @@ lmg_status lmg_batch_synchronize(lmg_batch *b, int64_t *first_failed) {
   if (first_failed) *first_failed = -1;
   cudaSetDevice(b->device);
   if (cudaStreamSynchronize(b->stream) != cudaSuccess) return bfail(b, LMG_ERR_CUDA, "batch: device failure");
+  if (b->persistent && b->ps.status) {
+    int st = 0;
+    if (cudaMemcpy(&st, b->ps.status, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess || st)
+      return bfail(b, st ? (lmg_status)st : LMG_ERR_CUDA, "batch: a persistent wait gave up");
+  }
   for (size_t i = 0; i < b->ctx.size(); ++i) {
     const lmg_status st = lmg_synchronize(b->ctx[i]);
     if (st) {
@@ -240,6 +413,32 @@ lmg_status lmg_batch_synchronize(lmg_batch *b, int64_t *first_failed) {
       return bfail(b, st, "batch: context " + std::to_string(i) + ": " + b->ctx[i]->err);
     }
   }
+  return LMG_OK;
+}
+
+lmg_status lmg_batch_last_error(lmg_batch *b, char *msg, int32_t cap) {
+  if (!b || !msg || cap <= 0) return LMG_ERR_ARG;
+  const size_t n = std::min((size_t)(cap - 1), b->err.size());
+  std::copy(b->err.begin(), b->err.begin() + n, msg);
+  msg[n] = 0;
+  return LMG_OK;
+}
+
+lmg_status lmg_batch_set_persistent(lmg_batch *b, int32_t on) {
+  if (!b) return LMG_ERR_ARG;
+  cudaSetDevice(b->device);
+  cudaStreamSynchronize(b->stream);
+  b->persistent = on != 0;
+  drop_graphs(b);
+  b->warm[0] = b->warm[1] = false;
+  return LMG_OK;
+}
+
+lmg_status lmg_batch_persistent_info(lmg_batch *b, int32_t *tile, int32_t *ctas_per_sm, int64_t *items) {
+  if (!b) return LMG_ERR_ARG;
+  if (tile) *tile = b->p_tile;
+  if (ctas_per_sm) *ctas_per_sm = b->p_ctas;
+  if (items) *items = b->ps.n_items;
   return LMG_OK;
 }
 

@@ -100,7 +100,8 @@ lmg_status general_plan(lmg_ctx *c) {
     e = have_rows ? c->h_cons_ptr[(size_t)d + 1] : 0;
   };
   // the cubic hex kernel masks homogeneous Dirichlet rows itself
-  const uint8_t *cons = (c->h_constrained.empty() || hier3_masks(c)) ? nullptr : c->h_constrained.data();
+  const uint8_t *cons =
+      (c->h_constrained.empty() || hier3_masks(c) || c->persist_pattern) ? nullptr : c->h_constrained.data();
   // per element: output dof list, its length and where its matrix / vector sit
   std::vector<int64_t> lptr((size_t)E + 1, 0);
   std::vector<int32_t> ldofs;

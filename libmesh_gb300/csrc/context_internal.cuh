@@ -93,6 +93,7 @@ struct lmg_ctx {
   // quadratic prisms; general path
   bool hier3 = false;
   bool sparsity_on_device = false;  // the general path's graph came from device_constrained_graph
+  bool persist_pattern = false;     // block-path system also held in per-pattern form (persistent batch)
   int32_t *d_h3batch = nullptr, *d_h3order = nullptr;  // element batches of one orientation pattern
   float2 *d_h3D = nullptr;           // per-pattern reference tensors, double-float pairs
   float *d_h3Df = nullptr;           // the same rounded to FP32 (mixed form)
@@ -170,6 +171,10 @@ void launch_hier3(lmg_ctx *c, bool mixed);
 // Regroups the per-pattern elements into CTA tiles of `tile` elements (4, 8,
 // 16 or 32); the element matrices do not depend on the grouping.
 lmg_status hier3_set_tile(lmg_ctx *c, int tile);
+// Per-pattern tables on the device (hier3.cu), and a block-path Poisson
+// system converted to that form for the persistent batch.
+lmg_status pattern_upload(lmg_ctx *c, const Hier3Tables &h);
+lmg_status pattern_from_block(lmg_ctx *c);
 bool hier3_masks(const lmg_ctx *c);  // Dirichlet rows applied by the element kernel
 void general_free(lmg_ctx *c);             // plan and work buffers
 

@@ -102,3 +102,61 @@ def test_batch_mixed_precision_graph():
     b.close()
     for a, _, _ in mem:
         a.close()
+
+
+def poisson_members():
+    """Affine one-variable Poisson systems of every element kind the
+    persistent batch takes: block-path LAGRANGE / HIERARCHIC p <= 2 and the
+    per-pattern HIERARCHIC members."""
+    rng = np.random.default_rng(21)
+    out = []
+    for et, fo, q, dims, jit in ((lm.HEX8, 1 | lm.HIERARCHIC, 3, (5, 4, 4), 0.0), (lm.HEX27, 2, 5, (3, 3, 3), 0.0),
+                                 (lm.TET4, 1, 2, (4, 4, 3), 0.2), (lm.TET10, 2, 4, (3, 3, 3), 0.2),
+                                 (lm.PRISM6, 1 | lm.HIERARCHIC, 3, (4, 3, 3), 0.0),
+                                 (lm.HEX27, 3 | lm.HIERARCHIC, 7, (3, 2, 3), 0.0),
+                                 (lm.TET14, 3 | lm.HIERARCHIC, 6, (3, 3, 2), 0.2),
+                                 (lm.PRISM18, 2 | lm.HIERARCHIC, 4, (3, 2, 2), 0.0),
+                                 (lm.PRISM21, 3 | lm.HIERARCHIC, 5, (2, 3, 2), 0.0)):
+        m = lm.Mesh.build_cube(*dims, et, jitter=jit, seed=3)
+        dm = lm.DofMap(m, 1, fe_order=fo if (fo & 0xff) == 3 or et == lm.PRISM18 else None)
+        dm.add_dirichlet_boundary([0, 1, 2, 3, 4, 5], [0])
+        a = lm.GpuAssembly(lm.POISSON, fo, q, elem_coef=rng.uniform(0.1, 10, m.n_elem),
+                           nodal_f=rng.uniform(-1, 1, (m.n_nodes, 1)))
+        a.init(m, dm)
+        out.append(a)
+    return out
+
+
+@pytest.mark.parametrize("prec", [lm.FP64, lm.MIXED])
+def test_persistent_batch_one_launch(prec):
+    """Every member in one persistent launch per replay: each member's K and F
+    equal its own assembly to rounding (the per-pattern arithmetic of the
+    element tiles: 1e-12 of the row scale for the FP64 drop-in, FP32
+    rounding for the mixed form), over repeated and re-tuned replays."""
+    mem = poisson_members()
+    own = [a.assemble(prec) for a in mem]
+    b = lm.Batch()
+    for a in mem:
+        b.add(a)
+    b.set_persistent(True)
+    b.tune(prec, reps=1)
+    tile, ctas, items = b.persistent_info()
+    assert tile in (8, 16, 32) and items > len(mem)
+    _, launches, _ = b.info()
+    assert launches == 1
+    for _ in range(2):
+        b.assemble(prec)
+        b.synchronize()
+        for a, (K0, F0) in zip(mem, own):
+            K, F = a.result()
+            if prec == lm.FP64:
+                rowmax = np.maximum.reduceat(np.abs(K0), a.sparsity()[0][:-1])
+                rows = np.repeat(np.arange(len(rowmax)), np.diff(a.sparsity()[0]))
+                assert np.all(np.abs(K - K0) <= 1e-12 * np.maximum(np.abs(K0), rowmax[rows]))
+                assert np.all(np.abs(F - F0) <= 1e-12 * np.maximum(np.abs(F0), np.abs(F0).max()))
+            else:
+                assert np.linalg.norm(K - K0) <= 1e-6 * np.linalg.norm(K0)
+                assert np.linalg.norm(F - F0) <= 1e-12 * np.linalg.norm(F0)
+    b.close()
+    for a in mem:
+        a.close()
