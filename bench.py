@@ -795,7 +795,7 @@ def main():
             "data": "synthetic (seeded mesh jitter, E_e, f)",
             "config": {"workload": "elasticity TET10 build_cube %d^3 x6 tets, QGauss FOURTH" % args.n,
                        "n_elem": mesh.n_elem, "n_dofs": dm.n_dofs, "nnz": asm.nnz,
-                       "precision": args.precision, "l2": "inputs larger than L2 (4.8 GB element buffer)",
+                       "precision": args.precision, "l2": "inputs larger than L2 (2.6 GB element buffer)",
                        "parallelism": "replica per GPU", "setup": setup},
             "mdofs_per_s": value * dm.n_dofs / mesh.n_elem,
             "e2e": {"value": e2e, "unit": "Melem/s", "h2d_bytes_per_step": 8 * (mesh.n_elem + 3 * mesh.n_nodes),

@@ -123,6 +123,8 @@ void launch_gather_f(const GatherArgs &g, cudaStream_t s);
 
 // Whether an element kernel is instantiated for (form, shapes per variable, variables).
 bool fused_built(int form, int n, int nv);
+// Whether the fused row kernel's shared-memory rows fit for rows of max_deg slots.
+bool fused_fits(int n, int nv, int max_deg);
 // k_geo (when geo) then k_rows_mixed over f's rows (when rows); false if no kernel is built.
 bool launch_fused_mixed(int form, int n, int nv, const FusedArgs &f, int grid, cudaStream_t s, bool geo = true,
                         bool rows = true);

@@ -922,9 +922,9 @@ lmg_status lmg_sparsity_build(lmg_ctx *c, int64_t *nnz) {
   if (st) return st;
   LMG_CUDA(c, dalloc(c->d_K, (size_t)c->nnz));
   LMG_CUDA(c, dalloc(c->d_F, (size_t)c->n_dofs));
-  const size_t b2 = (size_t)c->bs * c->bs, no = (size_t)c->nb * (c->nb - 1) / 2;
-  LMG_CUDA(c, dalloc(c->d_Kdiag2, (size_t)c->n_elem * c->nb * b2));
-  LMG_CUDA(c, dalloc(c->d_Koff2, (size_t)c->n_elem * no * b2));
+  // element-block buffers: allocated on the first assembly of each form
+  dfree(c->d_Kdiag2);
+  dfree(c->d_Koff2);
   dfree(c->d_Koff32);  // allocated on the first mixed assembly
   LMG_CUDA(c, dalloc(c->d_Fe2, (size_t)(c->n_elem * c->nl)));
   c->have_sparsity = true;
@@ -1153,11 +1153,17 @@ lmg_status lmg_assemble(lmg_ctx *c, int32_t precision, double *K, double *F, int
     return check_status(c, "assemble");
   }
   const bool mixed = precision == LMG_MIXED;
-  const bool fused = mixed && c->h_gen.empty() && c->d_relslot && fused_built(c->form, c->tab.n, c->n_vars);
+  const bool fused = mixed && c->h_gen.empty() && c->d_relslot && fused_built(c->form, c->tab.n, c->n_vars) &&
+                     fused_fits(c->tab.n, c->n_vars, c->max_bdeg);
   if (mixed && !fused && !c->d_Koff32)
     LMG_CUDA(c, dalloc(c->d_Koff32, (size_t)c->n_elem * c->nb * (c->nb - 1) / 2 * c->bs * c->bs));
   if (fused && !c->d_geo)
     LMG_CUDA(c, dalloc(c->d_geo, (size_t)c->n_elem * (c->form == LMG_POISSON ? 9 : 11)));
+  if (!mixed && !c->d_Kdiag2) {
+    const size_t b2 = (size_t)c->bs * c->bs, no = (size_t)c->nb * (c->nb - 1) / 2;
+    LMG_CUDA(c, dalloc(c->d_Kdiag2, (size_t)c->n_elem * c->nb * b2));
+    LMG_CUDA(c, dalloc(c->d_Koff2, (size_t)c->n_elem * no * b2));
+  }
   lmg_status st = reset_status(c);
   if (st) return st;
   ElemArgs a{};

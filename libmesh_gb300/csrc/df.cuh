@@ -53,6 +53,22 @@ __device__ __forceinline__ DF df_fma_lazy(DF acc, DF a, DF b) {
 
 __device__ __forceinline__ DF df_norm(DF x) { return fast_two_sum(x.hi, x.lo); }
 
+// Running double-float sum of double-float terms: TwoSum on the high parts,
+// the rounding error and the low parts collected in `lo` (normalised only when
+// the sum is rounded to FP64), 7 FP32 operations per term.  From {0, 0} the
+// first term is taken exactly.
+struct DFAcc {
+  float hi, lo;
+};
+
+__device__ __forceinline__ void acc_add(DFAcc &a, float2 v) {
+  const float s = __fadd_rn(a.hi, v.x);
+  const float bb = __fsub_rn(s, a.hi);
+  const float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(v.x, bb));
+  a.lo = __fadd_rn(a.lo, __fadd_rn(e, v.y));
+  a.hi = s;
+}
+
 // Exact float -> double by moving the bits (keeps the FP64 pipe free); zero,
 // subnormal, inf and NaN take the hardware conversion.
 __device__ __forceinline__ double f2d(float f) {

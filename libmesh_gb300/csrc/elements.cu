@@ -757,7 +757,7 @@ __global__ void __launch_bounds__(256, 6) k_rows_mixed(FusedArgs f) {
       if (rc || f.constrained[NV * P + k] != 0) v = (i == k) ? (double)(t1 - t0) : 0.0;
       f.K[rowp + jdiag * NV + k] = v;
     }
-    row_load_f<NV>(f.fptr, f.fcontrib, f.el.Fe2, f.F, P, lane);
+    row_load_seq<NV>(f.fptr, f.fcontrib, f.el.Fe2, f.F, P, lane);
   }
 }
 
@@ -786,6 +786,10 @@ bool elements_built(int form, int n, int nv) {
 bool fused_built(int form, int n, int nv) {
   return (form == LMG_POISSON && nv == 1 && (n == 4 || n == 6 || n == 8 || n == 10 || n == 27)) ||
          (form == LMG_ELASTICITY && nv == 3 && (n == 4 || n == 6 || n == 8 || n == 10));
+}
+
+bool fused_fits(int n, int nv, int max_deg) {
+  return sizeof(float) * (9 * (size_t)n * n + (size_t)8 * max_deg * nv * nv) <= (size_t)200 * 1024;
 }
 
 bool launch_fused_mixed(int form, int n, int nv, const FusedArgs &f, int grid, cudaStream_t s, bool geo,

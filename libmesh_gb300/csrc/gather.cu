@@ -27,25 +27,13 @@ namespace lmg {
 
 namespace {
 
+// Load vector of the mixed insertion and of the QoI load: element order (the
+// fused row kernel's sums, so that both mixed paths give the same bits).
 template <int BS>
 __device__ __forceinline__ void row_load(const GatherArgs &g, int64_t P, int lane) {
-  row_load_f<BS>(g.fptr, g.fcontrib, g.Fe2, g.F, P, lane);
+  row_load_seq<BS>(g.fptr, g.fcontrib, g.Fe2, g.F, P, lane);
 }
 
-// Running double-float sum of double-float terms: TwoSum on the high parts,
-// the rounding error and the low parts collected in `lo` (normalised only when
-// the sum is rounded to FP64), 8 FP32 operations per term.
-struct DFAcc {
-  float hi, lo;
-};
-
-__device__ __forceinline__ void acc_add(DFAcc &a, float2 v) {
-  const float s = __fadd_rn(a.hi, v.x);
-  const float bb = __fsub_rn(s, a.hi);
-  const float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(v.x, bb));
-  a.lo = __fadd_rn(a.lo, __fadd_rn(e, v.y));
-  a.hi = s;
-}
 
 // FP64 drop-in insertion, warp per block row P.  Lane l < (32/BS)*BS owns row
 // i = l % BS of the slots jj = l / BS + (32/BS) t, i.e. the BS entries
