@@ -62,6 +62,7 @@ struct FusedArgs {
   const int32_t *fcontrib;    // e*N + a, ascending (element order)
   const uint8_t *relslot;     // [n_elem][N][N] slot of block (a, b) inside block row of a
   const uint8_t *constrained; // [n_dofs]
+  const uint8_t *rowcons;     // [n_brows] 1 when the block row or one of its columns holds a constrained dof
   int max_deg;                // largest block-row degree
   double *K;
   double *F;

@@ -272,6 +272,18 @@ __global__ void k_encode(int64_t n, int nb, int32_t *v) {
   }
 }
 
+// Whether block row P touches a constrained dof: one of its own or of its
+// columns' bs dofs (thread per block row).
+__global__ void k_rowcons(int64_t n_rows, int bs, const int64_t *brow_ptr, const int32_t *bcol, const uint8_t *cons,
+                          uint8_t *out) {
+  for (int64_t P = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; P < n_rows; P += (int64_t)gridDim.x * blockDim.x) {
+    uint8_t v = 0;
+    for (int64_t j = brow_ptr[P]; j < brow_ptr[P + 1] && !v; ++j)
+      for (int k = 0; k < bs; ++k) v |= cons[(int64_t)bs * bcol[j] + k];
+    out[P] = v ? 1 : 0;
+  }
+}
+
 // Nodal load split into double-float pairs (read by the affine element kernels).
 __global__ void k_split(int64_t n, const double *x, float2 *y) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
@@ -603,6 +615,7 @@ lmg_status build_plan(lmg_ctx *c) {
   k_encode<<<grid_for(c, npair, 256), 256, 0, c->stream>>>(npair, nb, c->d_bcontrib);
   c->launches += 3;
   dfree(c->d_relslot);
+  dfree(c->d_rowcons);
   if (c->max_bdeg <= 255) {  // the fused mixed form addresses slots with one byte
     LMG_CUDA(c, dalloc(c->d_relslot, (size_t)npair));
     k_relslot<<<grid_for(c, npair, 256), 256, 0, c->stream>>>(npair, nb, c->d_eb, c->d_brow_ptr, slot,
@@ -706,6 +719,7 @@ lmg_status upload_cmask(lmg_ctx *c) {
   std::vector<uint8_t> cons = c->h_constrained;
   cons.resize((size_t)c->n_dofs, 0);
   LMG_CUDA(c, dupload(c, c->d_cons, cons.data(), cons.size()));
+  dfree(c->d_rowcons);  // re-derived on the next fused assembly
   LMG_CUDA(c, cudaStreamSynchronize(c->stream));
   return LMG_OK;
 }
@@ -749,7 +763,7 @@ lmg_status lmg_context_destroy(lmg_ctx *c) {
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
   dfree(c->d_xyz); dfree(c->d_conn); dfree(c->d_aff); dfree(c->d_gen); dfree(c->d_eb);
-  dfree(c->d_cmask); dfree(c->d_cons); dfree(c->d_brow_ptr); dfree(c->d_bcol); dfree(c->d_row_ptr); dfree(c->d_col);
+  dfree(c->d_cmask); dfree(c->d_cons); dfree(c->d_rowcons); dfree(c->d_brow_ptr); dfree(c->d_bcol); dfree(c->d_row_ptr); dfree(c->d_col);
   dfree(c->d_bptr); dfree(c->d_bcontrib); dfree(c->d_fptr); dfree(c->d_fcontrib); dfree(c->d_tab);
   dfree(c->d_coef); dfree(c->d_f); dfree(c->d_f2); dfree(c->d_Kdiag2); dfree(c->d_Koff2); dfree(c->d_Fe2); dfree(c->d_K);
   dfree(c->d_F); dfree(c->d_Koff32); dfree(c->d_status); dfree(c->d_bad);
@@ -1159,6 +1173,12 @@ lmg_status lmg_assemble(lmg_ctx *c, int32_t precision, double *K, double *F, int
     LMG_CUDA(c, dalloc(c->d_Koff32, (size_t)c->n_elem * c->nb * (c->nb - 1) / 2 * c->bs * c->bs));
   if (fused && !c->d_geo)
     LMG_CUDA(c, dalloc(c->d_geo, (size_t)c->n_elem * (c->form == LMG_POISSON ? 9 : 11)));
+  if (fused && !c->d_rowcons) {
+    LMG_CUDA(c, dalloc(c->d_rowcons, (size_t)std::max<int64_t>(c->n_blocks, 1)));
+    k_rowcons<<<grid_for(c, c->n_blocks, 256), 256, 0, c->stream>>>(c->n_blocks, c->bs, c->d_brow_ptr, c->d_bcol,
+                                                                   c->d_cons, c->d_rowcons);
+    c->launches++;
+  }
   if (!mixed && !c->d_Kdiag2) {
     const size_t b2 = (size_t)c->bs * c->bs, no = (size_t)c->nb * (c->nb - 1) / 2;
     LMG_CUDA(c, dalloc(c->d_Kdiag2, (size_t)c->n_elem * c->nb * b2));
@@ -1203,6 +1223,7 @@ lmg_status lmg_assemble(lmg_ctx *c, int32_t precision, double *K, double *F, int
     f.fcontrib = c->d_fcontrib;
     f.relslot = c->d_relslot;
     f.constrained = c->d_cons;
+    f.rowcons = c->d_rowcons;
     f.max_deg = c->max_bdeg;
     f.K = c->d_K;
     f.F = c->d_F;

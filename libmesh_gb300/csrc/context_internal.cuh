@@ -49,6 +49,7 @@ struct lmg_ctx {
   cudaStream_t copy_stream = nullptr;     // device-to-host copies overlapped with the insertion
   std::vector<cudaEvent_t> chunk_ev;
   uint8_t *d_relslot = nullptr;  // [E][nb][nb] slot of block (a, b) in block row of a (fused mixed form)
+  uint8_t *d_rowcons = nullptr;  // [n_blocks] block row touches a constrained dof (fused mixed form)
   int max_bdeg = 0;              // largest block-row degree
   float *d_geo = nullptr;        // [E][NG] per-element operands (fused mixed form)
   // form

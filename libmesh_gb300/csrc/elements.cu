@@ -664,11 +664,16 @@ template <int FORM, int N, int NV>
 __global__ void __launch_bounds__(256, 6) k_rows_mixed(FusedArgs f) {
   using R = Ar<float>;
   constexpr int NG = Geo<FORM>::NG, B2 = NV * NV, NPASS = 32 / N, SPL = 32 / B2;
-  extern __shared__ float fsm[];
-  float *sS = fsm;  // [9][N*N]
+  extern __shared__ __align__(16) float fsm[];
+  // reference tensors by block pair: S^{mn}_{ab} at sS[(a N + b) * 12 + mn]
+  // (padded to 12 floats: one pair's 9 values are three vector loads)
+  float *sS = fsm;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  float *acc = sS + 9 * N * N + (int64_t)warp * f.max_deg * B2;
-  for (int i = threadIdx.x; i < 9 * N * N; i += blockDim.x) sS[i] = R::from(f.el.fe.S[i]);
+  float *acc = sS + 12 * N * N + (int64_t)warp * f.max_deg * B2;
+  for (int i = threadIdx.x; i < 9 * N * N; i += blockDim.x) {
+    const int mn = i / (N * N), ab = i - mn * (N * N);
+    sS[ab * 12 + mn] = R::from(f.el.fe.S[i]);
+  }
   __syncthreads();
   const int wi = lane / N, bl = lane - wi * N;  // incidence slot and local column node of this lane
   const int js = lane / B2, rem = lane - js * B2;
@@ -682,10 +687,13 @@ __global__ void __launch_bounds__(256, 6) k_rows_mixed(FusedArgs f) {
     __syncwarp();
     for (int x = lane; x < deg * B2; x += 32) acc[x] = 0.f;
     __syncwarp();
+    // the incidence codes are fetched one pass ahead
+    int32_t code_next = (lane < NPASS * N && t0 + wi < t1) ? __ldg(f.fcontrib + t0 + wi) : 0;
     for (int32_t tg = t0; tg < t1; tg += NPASS) {
       const int32_t t = tg + wi;
       const bool valid = lane < NPASS * N && t < t1;
-      const int32_t code = valid ? f.fcontrib[t] : 0;
+      const int32_t code = code_next;
+      code_next = (lane < NPASS * N && t + NPASS < t1) ? __ldg(f.fcontrib + t + NPASS) : 0;
       const int32_t e = code / N, ae = code - e * N;
       const bool work = valid && bl != ae;
       float out[B2];
@@ -696,8 +704,13 @@ __global__ void __launch_bounds__(256, 6) k_rows_mixed(FusedArgs f) {
         for (int q = 0; q < NG; ++q) gv[q] = f.geo[(int64_t)e * NG + q];
         const int ra = ae < bl ? ae : bl, cb = ae < bl ? bl : ae;
         float sv[9];
-#pragma unroll
-        for (int mn = 0; mn < 9; ++mn) sv[mn] = sS[mn * N * N + ra * N + cb];
+        {
+          const float4 *s4 = reinterpret_cast<const float4 *>(sS + (ra * N + cb) * 12);
+          const float4 x0 = s4[0], x1 = s4[1], x2 = s4[2];
+          sv[0] = x0.x; sv[1] = x0.y; sv[2] = x0.z; sv[3] = x0.w;
+          sv[4] = x1.x; sv[5] = x1.y; sv[6] = x1.z; sv[7] = x1.w;
+          sv[8] = x2.x;
+        }
         contract_block<FORM, R>(gv, sv, out);
         if (NV > 1 && bl < ae) {  // the stored block is (b, a): take its transpose
 #pragma unroll
@@ -720,19 +733,28 @@ __global__ void __launch_bounds__(256, 6) k_rows_mixed(FusedArgs f) {
         __syncwarp();
       }
     }
-    // epilogue of the mixed insertion, reading the row from shared memory
+    // epilogue of the mixed insertion, reading the row from shared memory;
+    // the Dirichlet flags are read only in rows that touch a constrained dof
     const int32_t rowp = act ? f.row_ptr[NV * P + i] : 0;
     const bool rc = act && f.constrained[NV * P + i] != 0;
-    DF racc = {0.f, 0.f};
+    float rh = 0.f, rl = 0.f;  // double-float row sum, normalised after the loop
     int jdiag = -1;
-    for (int jj = js; act && jj < deg; jj += SPL) {
-      const int32_t Q = f.bcol[rb + jj];
-      if (Q == (int32_t)P) { jdiag = jj; continue; }
-      const float kv = acc[jj * B2 + rem];
-      racc = df_add1(racc, kv);
-      const bool msk = rc || f.constrained[(int64_t)NV * Q + k] != 0;
-      f.K[rowp + jj * NV + k] = msk ? 0.0 : f2d(kv);
-    }
+    auto epilogue = [&](auto masks) {
+      for (int jj = js; act && jj < deg; jj += SPL) {
+        const int32_t Q = f.bcol[rb + jj];
+        if (Q == (int32_t)P) { jdiag = jj; continue; }
+        const float kv = acc[jj * B2 + rem];
+        const float s = __fadd_rn(rh, kv), bb = __fsub_rn(s, rh);
+        rl = __fadd_rn(rl, __fadd_rn(__fsub_rn(rh, __fsub_rn(s, bb)), __fsub_rn(kv, bb)));
+        rh = s;
+        bool msk = false;
+        if constexpr (decltype(masks)::value) msk = rc || f.constrained[(int64_t)NV * Q + k] != 0;
+        f.K[rowp + jj * NV + k] = msk ? 0.0 : f2d(kv);
+      }
+    };
+    if (f.rowcons[P]) epilogue(std::true_type{});
+    else epilogue(std::false_type{});
+    DF racc = fast_two_sum(rh, rl);
     if constexpr (B2 == 1) {
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) {
@@ -766,7 +788,7 @@ void launch_fused_t(const FusedArgs &f, int grid, cudaStream_t s, bool geo, bool
   const int64_t gb = (f.el.n_list + 127) / 128;
   if (geo && gb > 0) k_geo<FORM, N, NV><<<(int)(gb < grid ? gb : grid), 128, 0, s>>>(f);
   if (!rows) return;
-  const size_t smem = sizeof(float) * (9 * N * N + (size_t)8 * f.max_deg * NV * NV);
+  const size_t smem = sizeof(float) * (12 * N * N + (size_t)8 * f.max_deg * NV * NV);
   static size_t attr = 0;
   if (smem > attr) {
     cudaFuncSetAttribute(k_rows_mixed<FORM, N, NV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -789,7 +811,7 @@ bool fused_built(int form, int n, int nv) {
 }
 
 bool fused_fits(int n, int nv, int max_deg) {
-  return sizeof(float) * (9 * (size_t)n * n + (size_t)8 * max_deg * nv * nv) <= (size_t)200 * 1024;
+  return sizeof(float) * (12 * (size_t)n * n + (size_t)8 * max_deg * nv * nv) <= (size_t)200 * 1024;
 }
 
 bool launch_fused_mixed(int form, int n, int nv, const FusedArgs &f, int grid, cudaStream_t s, bool geo,
