@@ -687,13 +687,10 @@ __global__ void __launch_bounds__(256, 6) k_rows_mixed(FusedArgs f) {
     __syncwarp();
     for (int x = lane; x < deg * B2; x += 32) acc[x] = 0.f;
     __syncwarp();
-    // the incidence codes are fetched one pass ahead
-    int32_t code_next = (lane < NPASS * N && t0 + wi < t1) ? __ldg(f.fcontrib + t0 + wi) : 0;
     for (int32_t tg = t0; tg < t1; tg += NPASS) {
       const int32_t t = tg + wi;
       const bool valid = lane < NPASS * N && t < t1;
-      const int32_t code = code_next;
-      code_next = (lane < NPASS * N && t + NPASS < t1) ? __ldg(f.fcontrib + t + NPASS) : 0;
+      const int32_t code = valid ? f.fcontrib[t] : 0;
       const int32_t e = code / N, ae = code - e * N;
       const bool work = valid && bl != ae;
       float out[B2];
@@ -735,49 +732,103 @@ __global__ void __launch_bounds__(256, 6) k_rows_mixed(FusedArgs f) {
     }
     // epilogue of the mixed insertion, reading the row from shared memory;
     // the Dirichlet flags are read only in rows that touch a constrained dof
-    const int32_t rowp = act ? f.row_ptr[NV * P + i] : 0;
-    const bool rc = act && f.constrained[NV * P + i] != 0;
-    float rh = 0.f, rl = 0.f;  // double-float row sum, normalised after the loop
-    int jdiag = -1;
-    auto epilogue = [&](auto masks) {
-      for (int jj = js; act && jj < deg; jj += SPL) {
-        const int32_t Q = f.bcol[rb + jj];
-        if (Q == (int32_t)P) { jdiag = jj; continue; }
-        const float kv = acc[jj * B2 + rem];
-        const float s = __fadd_rn(rh, kv), bb = __fsub_rn(s, rh);
-        rl = __fadd_rn(rl, __fadd_rn(__fsub_rn(rh, __fsub_rn(s, bb)), __fsub_rn(kv, bb)));
-        rh = s;
-        bool msk = false;
-        if constexpr (decltype(masks)::value) msk = rc || f.constrained[(int64_t)NV * Q + k] != 0;
-        f.K[rowp + jj * NV + k] = msk ? 0.0 : f2d(kv);
-      }
-    };
-    if (f.rowcons[P]) epilogue(std::true_type{});
-    else epilogue(std::false_type{});
-    DF racc = fast_two_sum(rh, rl);
-    if constexpr (B2 == 1) {
+    if constexpr (NV == 3) {
+      // lane (js3, i3): dof row i3 of the slots js3, js3 + 10, ..., three
+      // entries each (written contiguously), with their double-float row sums
+      const int js3 = lane / 3, i3 = lane - js3 * 3;
+      const bool act3 = lane < 30;
+      const int32_t rowp = act3 ? f.row_ptr[3 * P + i3] : 0;
+      const bool rc = act3 && f.constrained[3 * P + i3] != 0;
+      float rh[3] = {0.f, 0.f, 0.f}, rl[3] = {0.f, 0.f, 0.f};
+      int jdiag = -1;
+      auto epilogue = [&](auto masks) {
+        for (int jj = js3; act3 && jj < deg; jj += 10) {
+          const int32_t Q = f.bcol[rb + jj];
+          if (Q == (int32_t)P) { jdiag = jj; continue; }
+          const float *ar = acc + jj * 9 + i3 * 3;
+          double *Kr = f.K + rowp + jj * 3;
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        DF y;
-        y.hi = __shfl_xor_sync(0xffffffffu, racc.hi, o);
-        y.lo = __shfl_xor_sync(0xffffffffu, racc.lo, o);
-        racc = (lane & o) ? df_add(y, racc) : df_add(racc, y);
+          for (int kk = 0; kk < 3; ++kk) {
+            const float kv = ar[kk];
+            const float s = __fadd_rn(rh[kk], kv), bb = __fsub_rn(s, rh[kk]);
+            rl[kk] = __fadd_rn(rl[kk], __fadd_rn(__fsub_rn(rh[kk], __fsub_rn(s, bb)), __fsub_rn(kv, bb)));
+            rh[kk] = s;
+            bool msk = false;
+            if constexpr (decltype(masks)::value) msk = rc || f.constrained[(int64_t)3 * Q + kk] != 0;
+            Kr[kk] = msk ? 0.0 : f2d(kv);
+          }
+        }
+      };
+      if (f.rowcons[P]) epilogue(std::true_type{});
+      else epilogue(std::false_type{});
+      DF r[3];
+#pragma unroll
+      for (int kk = 0; kk < 3; ++kk) r[kk] = fast_two_sum(rh[kk], rl[kk]);
+      // sum over js3 = 0..9 (lanes i3 + 3 js3): pairs, then fours, then eights
+#pragma unroll
+      for (int d = 1; d < 10; d <<= 1)
+#pragma unroll
+        for (int kk = 0; kk < 3; ++kk) {
+          DF y;
+          y.hi = __shfl_sync(0xffffffffu, r[kk].hi, (lane + 3 * d) & 31);
+          y.lo = __shfl_sync(0xffffffffu, r[kk].lo, (lane + 3 * d) & 31);
+          if (act3 && js3 % (2 * d) == 0 && js3 + d < 10) r[kk] = df_add(r[kk], y);
+        }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) jdiag = max(jdiag, __shfl_xor_sync(0xffffffffu, jdiag, o));
+      if (lane < 3 && jdiag >= 0) {
+#pragma unroll
+        for (int kk = 0; kk < 3; ++kk) {
+          double v = -(f2d(r[kk].hi) + f2d(r[kk].lo));
+          if (rc || f.constrained[3 * P + kk] != 0) v = (i3 == kk) ? (double)(t1 - t0) : 0.0;
+          f.K[rowp + jdiag * 3 + kk] = v;
+        }
       }
     } else {
+      const int32_t rowp = act ? f.row_ptr[NV * P + i] : 0;
+      const bool rc = act && f.constrained[NV * P + i] != 0;
+      float rh = 0.f, rl = 0.f;  // double-float row sum, normalised after the loop
+      int jdiag = -1;
+      auto epilogue = [&](auto masks) {
+        for (int jj = js; act && jj < deg; jj += SPL) {
+          const int32_t Q = f.bcol[rb + jj];
+          if (Q == (int32_t)P) { jdiag = jj; continue; }
+          const float kv = acc[jj * B2 + rem];
+          const float s = __fadd_rn(rh, kv), bb = __fsub_rn(s, rh);
+          rl = __fadd_rn(rl, __fadd_rn(__fsub_rn(rh, __fsub_rn(s, bb)), __fsub_rn(kv, bb)));
+          rh = s;
+          bool msk = false;
+          if constexpr (decltype(masks)::value) msk = rc || f.constrained[(int64_t)NV * Q + k] != 0;
+          f.K[rowp + jj * NV + k] = msk ? 0.0 : f2d(kv);
+        }
+      };
+      if (f.rowcons[P]) epilogue(std::true_type{});
+      else epilogue(std::false_type{});
+      DF racc = fast_two_sum(rh, rl);
+      if constexpr (B2 == 1) {
 #pragma unroll
-      for (int t = 1; t < SPL; ++t) {
-        DF y;
-        y.hi = __shfl_sync(0xffffffffu, racc.hi, (lane + t * B2) & 31);
-        y.lo = __shfl_sync(0xffffffffu, racc.lo, (lane + t * B2) & 31);
-        if (lane < B2) racc = df_add(racc, y);
+        for (int o = 16; o > 0; o >>= 1) {
+          DF y;
+          y.hi = __shfl_xor_sync(0xffffffffu, racc.hi, o);
+          y.lo = __shfl_xor_sync(0xffffffffu, racc.lo, o);
+          racc = (lane & o) ? df_add(y, racc) : df_add(racc, y);
+        }
+      } else {
+#pragma unroll
+        for (int t = 1; t < SPL; ++t) {
+          DF y;
+          y.hi = __shfl_sync(0xffffffffu, racc.hi, (lane + t * B2) & 31);
+          y.lo = __shfl_sync(0xffffffffu, racc.lo, (lane + t * B2) & 31);
+          if (lane < B2) racc = df_add(racc, y);
+        }
       }
-    }
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) jdiag = max(jdiag, __shfl_xor_sync(0xffffffffu, jdiag, o));
-    if (lane < B2 && jdiag >= 0) {
-      double v = -(f2d(racc.hi) + f2d(racc.lo));
-      if (rc || f.constrained[NV * P + k] != 0) v = (i == k) ? (double)(t1 - t0) : 0.0;
-      f.K[rowp + jdiag * NV + k] = v;
+      for (int o = 16; o > 0; o >>= 1) jdiag = max(jdiag, __shfl_xor_sync(0xffffffffu, jdiag, o));
+      if (lane < B2 && jdiag >= 0) {
+        double v = -(f2d(racc.hi) + f2d(racc.lo));
+        if (rc || f.constrained[NV * P + k] != 0) v = (i == k) ? (double)(t1 - t0) : 0.0;
+        f.K[rowp + jdiag * NV + k] = v;
+      }
     }
     row_load_seq<NV>(f.fptr, f.fcontrib, f.el.Fe2, f.F, P, lane);
   }
