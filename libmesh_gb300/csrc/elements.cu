@@ -165,6 +165,45 @@ __device__ __forceinline__ void contract_block(const typename R::V *gv, const ty
   }
 }
 
+// Load vector of one element, Fe_a^v = detJ sum_b M_ab f_b^v, in double-float
+// (M the reference mass matrix as pairs, dd = detJ); constrained local dofs
+// (mask bit v*N + a) get 0.  For up to ten nodes the element's nodal values of
+// a component are loaded once into registers; the sums are the same either way.
+template <int N, int NV>
+__device__ __forceinline__ void element_load_df(const float2 *nodal_f2, const int32_t *c, const float2 *sM, DF dd,
+                                                uint64_t mask, float2 *Fo) {
+#pragma unroll
+  for (int v = 0; v < NV; ++v) {
+    if constexpr (N <= 10) {
+      float2 fb[N];
+#pragma unroll
+      for (int b = 0; b < N; ++b) fb[b] = nodal_f2 ? nodal_f2[(int64_t)c[b] * NV + v] : float2{0.f, 0.f};
+      for (int ai = 0; ai < N; ++ai) {
+        DF s = {0.f, 0.f};
+        if (nodal_f2)
+#pragma unroll
+          for (int b = 0; b < N; ++b) {
+            const float2 mb = sM[ai * N + b];
+            s = df_fma_lazy(s, DF{mb.x, mb.y}, DF{fb[b].x, fb[b].y});
+          }
+        s = df_norm(df_fma_lazy(DF{0.f, 0.f}, df_norm(s), dd));
+        Fo[ai * NV + v] = ((mask >> (v * N + ai)) & 1ull) ? make_float2(0.f, 0.f) : make_float2(s.hi, s.lo);
+      }
+    } else {
+      for (int ai = 0; ai < N; ++ai) {
+        DF s = {0.f, 0.f};
+        if (nodal_f2)
+          for (int b = 0; b < N; ++b) {
+            const float2 fb = nodal_f2[(int64_t)c[b] * NV + v], mb = sM[ai * N + b];
+            s = df_fma_lazy(s, DF{mb.x, mb.y}, DF{fb.x, fb.y});
+          }
+        s = df_norm(df_fma_lazy(DF{0.f, 0.f}, df_norm(s), dd));
+        Fo[ai * NV + v] = ((mask >> (v * N + ai)) & 1ull) ? make_float2(0.f, 0.f) : make_float2(s.hi, s.lo);
+      }
+    }
+  }
+}
+
 // Byte offsets of the affine kernel's dynamic shared memory (4 warps per CTA).
 __host__ __device__ constexpr size_t al16(size_t x) { return (x + 15) & ~(size_t)15; }
 template <int FORM, int N, int NV, typename T>
@@ -243,18 +282,7 @@ __global__ void __launch_bounds__(128) k_elem_affine(ElemArgs a) {
       // Load vector Fe_a^i = detJ sum_b M_ab f_b^i in double-float (both forms).
       float2 *Fo = a.Fe2 + (int64_t)e * N * NV;
       const DF dd = df_split(det);
-      for (int ai = 0; ai < N; ++ai)
-#pragma unroll
-        for (int v = 0; v < NV; ++v) {
-          DF s = {0.f, 0.f};
-          if (a.nodal_f2)
-            for (int b = 0; b < N; ++b) {
-              const float2 fb = a.nodal_f2[(int64_t)c[b] * NV + v], mb = sM[ai * N + b];
-              s = df_fma_lazy(s, DF{mb.x, mb.y}, DF{fb.x, fb.y});
-            }
-          s = df_norm(df_fma_lazy(DF{0.f, 0.f}, df_norm(s), dd));
-          Fo[ai * NV + v] = ((mask >> (v * N + ai)) & 1ull) ? make_float2(0.f, 0.f) : make_float2(s.hi, s.lo);
-        }
+      element_load_df<N, NV>(a.nodal_f2, c, sM, dd, mask, Fo);
     }
     __syncwarp();
     for (int t = 0; t < 32; ++t) {  // lane = output block
@@ -383,18 +411,7 @@ __global__ void __launch_bounds__(128) k_residual_affine(ElemArgs a) {
       // load vector Fe_a^i = detJ sum_b M_ab f_b^i (the element kernel's), into Re2
       float2 *Fo = a.Re2 + (int64_t)e * NL;
       const DF dd = df_split(det);
-      for (int ai = 0; ai < N; ++ai)
-#pragma unroll
-        for (int v = 0; v < NV; ++v) {
-          DF s = {0.f, 0.f};
-          if (a.nodal_f2)
-            for (int b = 0; b < N; ++b) {
-              const float2 fb = a.nodal_f2[(int64_t)c[b] * NV + v], mb = sM[ai * N + b];
-              s = df_fma_lazy(s, DF{mb.x, mb.y}, DF{fb.x, fb.y});
-            }
-          s = df_norm(df_fma_lazy(DF{0.f, 0.f}, df_norm(s), dd));
-          Fo[ai * NV + v] = ((mask >> (v * N + ai)) & 1ull) ? make_float2(0.f, 0.f) : make_float2(s.hi, s.lo);
-        }
+      element_load_df<N, NV>(a.nodal_f2, c, sM, dd, mask, Fo);
     }
     __syncwarp();
     const int slot = lane / N, ra = lane - slot * N;
@@ -645,18 +662,7 @@ __global__ void __launch_bounds__(128) k_geo(FusedArgs f) {
     const uint64_t mask = a.cmask[e];
     float2 *Fo = a.Fe2 + (int64_t)e * N * NV;
     const DF dd = df_split(det);
-    for (int ai = 0; ai < N; ++ai)
-#pragma unroll
-      for (int v = 0; v < NV; ++v) {
-        DF s = {0.f, 0.f};
-        if (a.nodal_f2)
-          for (int b = 0; b < N; ++b) {
-            const float2 fb = a.nodal_f2[(int64_t)c[b] * NV + v], mb = sM[ai * N + b];
-            s = df_fma_lazy(s, DF{mb.x, mb.y}, DF{fb.x, fb.y});
-          }
-        s = df_norm(df_fma_lazy(DF{0.f, 0.f}, df_norm(s), dd));
-        Fo[ai * NV + v] = ((mask >> (v * N + ai)) & 1ull) ? make_float2(0.f, 0.f) : make_float2(s.hi, s.lo);
-      }
+    element_load_df<N, NV>(a.nodal_f2, c, sM, dd, mask, Fo);
   }
 }
 
