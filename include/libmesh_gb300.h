@@ -323,8 +323,7 @@ lmg_status lmg_cg_solve(lmg_ctx *ctx, const double *rhs, double *x, double rtol,
  * so in msg.  The first call on each device does the set-up: it looks up that
  * array's address on the current device (cudaGetSymbolAddress), and looks it up
  * again whenever the current driver context is a new one (after
- * cudaDeviceReset, say); make that first call before any stream capture
- * begins.  Every call on a device shares the one array, so calls whose
+ * cudaDeviceReset, say).  Every call on a device shares the one array, so calls whose
  * work overlaps on the GPU (other streams, other host threads) race and give
  * wrong results: serialize them.  The scalar slots are cleared at the start of
  * every call; every other word is written before it is read.  stream is a
