@@ -420,6 +420,26 @@ def run_batch(args, local):
                         "tile_elements_per_cta": tile, "ctas_per_sm": ctas or "occupancy", "work_items": items}
     persist["launches_per_replay"] = 1
     persist["mixed_speedup_vs_fp64"] = persist["fp64"]["ms_per_step"] / persist["mixed"]["ms_per_step"]
+    # hybrid: one persistent launch over the per-pattern members, the others' own kernels beside it
+    hybrid = {}
+    b.set_persistent(True, hybrid=True)
+    for prec, key in ((lm.FP64, "fp64"), (lm.MIXED, "mixed")):
+        b.tune(prec, reps=2)
+        for _ in range(max(3, args.warmup)):
+            b.assemble(prec)
+        b.synchronize()
+        ev0.record(stream)
+        for _ in range(args.steps):
+            b.assemble(prec)
+        ev1.record(stream)
+        ev1.synchronize()
+        b.synchronize()
+        hms = ev0.elapsed_time(ev1) / args.steps
+        _, hl, _ = b.info()
+        hybrid[key] = {"ms_per_step": hms, "value": total / (hms * 1e-3) / 1e6, "unit": "Melem/s",
+                       "launches_per_replay": hl}
+    hybrid["mixed_speedup_vs_fp64"] = hybrid["fp64"]["ms_per_step"] / hybrid["mixed"]["ms_per_step"]
+    hybrid["vs_graph"] = ms / hybrid["fp64"]["ms_per_step"]
     b.close()
     n_dofs_total = sum(a.dof_map.n_dofs for a, _ in mem)
     for a, _ in mem:
@@ -439,6 +459,7 @@ def run_batch(args, local):
         "mixed": {"ms_per_step": ms32, "value": total / (ms32 * 1e-3) / 1e6, "unit": "Melem/s",
                   "speedup_vs_fp64": ms / ms32},
         "persistent": persist,
+        "persistent_hybrid": hybrid,
         "graph_speedup": seq_ms / ms, "gpu_launches": launches * args.steps, "launches_per_replay": launches,
         "tuned_ctas_per_sm": {str(g): int((grids == g).sum()) for g in sorted(set(grids.tolist()))},
         "clocks": clk}))

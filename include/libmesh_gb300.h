@@ -429,7 +429,11 @@ lmg_status lmg_batch_synchronize(lmg_batch *batch, int64_t *first_failed);
  * members' own assemblies to rounding (1e-13 of the entry); a member that
  * cannot take the per-pattern form makes lmg_batch_assemble return
  * LMG_ERR_UNSUPPORTED.  lmg_batch_tune then picks the elements per CTA tile
- * (8, 16, 32) and the CTAs per SM of the launch by timing replays. */
+ * (8, 16, 32) and the CTAs per SM of the launch by timing replays.  With
+ * on = 2 the persistent launch takes only the per-pattern (HIERARCHIC)
+ * members, and the other members' own kernels run beside it as branches of
+ * the same graph (their results bit-identical to their own assemblies).
+ * on = 0 returns to the graph of every member's own kernels. */
 lmg_status lmg_batch_set_persistent(lmg_batch *batch, int32_t on);
 /* The message of the batch's last failure (NUL-terminated, cut to cap). */
 lmg_status lmg_batch_last_error(lmg_batch *batch, char *msg, int32_t cap);

@@ -435,10 +435,12 @@ class Batch:
         bad = C.c_int64(-1)
         self._ok(lib().lmg_batch_synchronize(self.h, C.byref(bad)))
 
-    def set_persistent(self, on=True):
+    def set_persistent(self, on=True, hybrid=False):
         """One persistent kernel launch per replay (every member's element
-        tiles and insertion from one work queue)."""
-        check(lib().lmg_batch_set_persistent(self.h, 1 if on else 0))
+        tiles and insertion from one work queue); with hybrid=True only the
+        per-pattern (HIERARCHIC) members go through it and the others' own
+        kernels run beside it in the same graph."""
+        check(lib().lmg_batch_set_persistent(self.h, (2 if hybrid else 1) if on else 0))
 
     def persistent_info(self):
         t, c, n = C.c_int32(), C.c_int32(), C.c_int64()

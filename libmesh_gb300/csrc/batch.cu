@@ -51,6 +51,7 @@ struct lmg_batch {
   int64_t launches = 0;    // kernels in one replay
   std::string err;
   bool persistent = false;     // one persistent launch per replay (lmg_batch_set_persistent)
+  bool p_hybrid = false;       // ... over the per-pattern members only, the others' own kernels beside it
   int p_tile = 8, p_ctas = 0;  // its tile (elements per CTA) and CTAs per SM (0: occupancy)
   PersistentState ps;
 };
@@ -111,8 +112,13 @@ lmg_status prepare_persistent(lmg_batch *b, int precision) {
   drop_persistent(b);
   std::vector<lmg::PMember> mem;
   std::vector<lmg::PItem> items;
+  std::vector<size_t> own;  // hybrid: members that keep their own kernels
   for (size_t i = 0; i < b->ctx.size(); ++i) {
     lmg_ctx *c = b->ctx[i];
+    if (b->p_hybrid && !c->hier3) {
+      own.push_back(i);
+      continue;
+    }
     lmg_status st = c->hier3 ? lmg::hier3_set_tile(c, tile) : lmg::pattern_from_block(c);
     if (!st && !c->hier3) st = lmg::hier3_set_tile(c, tile);
     if (!st && !c->gen_plan) st = lmg::general_plan(c);
@@ -174,18 +180,35 @@ lmg_status prepare_persistent(lmg_batch *b, int precision) {
   ps.mixed = mixed;
   if (cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
     return bfail(b, LMG_ERR_CUDA, "batch: capture failed to start");
-  cudaMemsetAsync(ps.head, 0, sizeof(unsigned long long), b->stream);
-  cudaMemsetAsync(ps.done, 0, sizeof(unsigned int) * mem.size(), b->stream);
-  lmg::launch_batch_persistent(ps.mem, ps.items, ps.n_items, ps.head, ps.done, ps.status, mixed, tile, grid,
-                               b->stream);
+  cudaError_t fe = cudaEventRecord(b->fork, b->stream);
+  int64_t l0 = 0, l1 = 0;
+  for (size_t i : own) l0 += b->ctx[i]->launches;
+  lmg_status ast = LMG_OK;
+  // hybrid: the members with their own kernels join as branches beside the persistent launch
+  for (size_t k = 0; k < own.size() && fe == cudaSuccess && !ast; ++k) {
+    lmg_ctx *c = b->ctx[own[k]];
+    fe = cudaStreamWaitEvent(c->stream, b->fork, 0);
+    if (fe != cudaSuccess) break;
+    ast = lmg_assemble(c, precision, nullptr, nullptr, 1);
+    if (ast) break;
+    fe = cudaEventRecord(b->join[own[k]], c->stream);
+    if (fe == cudaSuccess) fe = cudaStreamWaitEvent(b->stream, b->join[own[k]], 0);
+  }
+  for (size_t i : own) l1 += b->ctx[i]->launches;
+  if (!mem.empty()) {
+    cudaMemsetAsync(ps.head, 0, sizeof(unsigned long long), b->stream);
+    cudaMemsetAsync(ps.done, 0, sizeof(unsigned int) * mem.size(), b->stream);
+    lmg::launch_batch_persistent(ps.mem, ps.items, ps.n_items, ps.head, ps.done, ps.status, mixed, tile, grid,
+                                 b->stream);
+  }
   const cudaError_t le = cudaGetLastError();
   const cudaError_t ce = cudaStreamEndCapture(b->stream, &ps.graph);
-  if (le != cudaSuccess || ce != cudaSuccess || !ps.graph ||
+  if (ast || fe != cudaSuccess || le != cudaSuccess || ce != cudaSuccess || !ps.graph ||
       cudaGraphInstantiate(&ps.exec, ps.graph, 0) != cudaSuccess) {
     drop_persistent(b);
-    return bfail(b, LMG_ERR_CUDA, "batch: persistent graph failed");
+    return bfail(b, ast ? ast : LMG_ERR_CUDA, "batch: persistent graph failed");
   }
-  b->launches = 1;
+  b->launches = (mem.empty() ? 0 : 1) + (l1 - l0);
   return LMG_OK;
 }
 
@@ -429,6 +452,7 @@ lmg_status lmg_batch_set_persistent(lmg_batch *b, int32_t on) {
   cudaSetDevice(b->device);
   cudaStreamSynchronize(b->stream);
   b->persistent = on != 0;
+  b->p_hybrid = on == 2;
   drop_graphs(b);
   b->warm[0] = b->warm[1] = false;
   return LMG_OK;

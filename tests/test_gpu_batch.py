@@ -128,6 +128,39 @@ def poisson_members():
 
 
 @pytest.mark.parametrize("prec", [lm.FP64, lm.MIXED])
+def test_persistent_hybrid_batch(prec):
+    """One persistent launch over the per-pattern members, the block-path
+    members' own kernels beside it in the same graph: the block-path members'
+    K and F equal their own assemblies bit for bit, the others to rounding."""
+    mem = poisson_members()
+    own = [a.assemble(prec) for a in mem]
+    b = lm.Batch()
+    for a in mem:
+        b.add(a)
+    b.set_persistent(True, hybrid=True)
+    b.tune(prec, reps=1)
+    _, launches, _ = b.info()
+    assert launches > 1
+    for _ in range(2):
+        b.assemble(prec)
+        b.synchronize()
+        for i, (a, (K0, F0)) in enumerate(zip(mem, own)):
+            K, F = a.result()
+            if i < 5:  # the block-path members (poisson_members lists them first)
+                assert np.array_equal(K, K0) and np.array_equal(F, F0)
+                continue
+            rp = a.sparsity()[0]
+            rowmax = np.maximum.reduceat(np.abs(K0), rp[:-1])
+            rows = np.repeat(np.arange(len(rowmax)), np.diff(rp))
+            tol = 1e-12 if prec == lm.FP64 else 1e-6
+            assert np.all(np.abs(K - K0) <= tol * np.maximum(np.abs(K0), rowmax[rows]))
+            assert np.all(np.abs(F - F0) <= 1e-12 * np.maximum(np.abs(F0), np.abs(F0).max()))
+    b.close()
+    for a in mem:
+        a.close()
+
+
+@pytest.mark.parametrize("prec", [lm.FP64, lm.MIXED])
 def test_persistent_batch_one_launch(prec):
     """Every member in one persistent launch per replay: each member's K and F
     equal its own assembly to rounding (the per-pattern arithmetic of the
