@@ -454,6 +454,11 @@ lmg_status lmg_probe_fp64(int32_t device, double *tflops);
  * element contractions would be bound by. */
 lmg_status lmg_probe_fp64_tensor(int32_t device, double *tflops);
 
+/* The exact FP32 -> FP64 conversion of the kernels' double-float results
+ * (bit moves for normal numbers), applied on `device` to n host values: out[i] is in[i]
+ * as a double (a check of that conversion against the hardware's). */
+lmg_status lmg_probe_f2d(int32_t device, int64_t n, const float *in, double *out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -365,6 +365,14 @@ def probe_fp64_tensor(device=0):
     return t.value
 
 
+def probe_f2d(values, device=0):
+    """The kernels' exact FP32 -> FP64 conversion applied on the device."""
+    x = np.ascontiguousarray(values, np.float32)
+    out = np.empty(x.shape, np.float64)
+    check(lib().lmg_probe_f2d(device, x.size, ptr(x), ptr(out)))
+    return out
+
+
 class LinearImplicitSystem:
     """The parts of libMesh's LinearImplicitSystem the assembly path uses."""
 

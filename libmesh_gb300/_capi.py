@@ -86,6 +86,7 @@ SIGNATURES = {
     "lmg_batch_persistent_info": [_p, _pi32, _pi32, _pi64],
     "lmg_probe_fp64": [_i32, _pf64],
     "lmg_probe_fp64_tensor": [_i32, _pf64],
+    "lmg_probe_f2d": [_i32, _i64, _p, _p],
 }
 
 _lib = None

@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 
 #include "../../include/libmesh_gb300.h"
+#include "df.cuh"
 
 namespace {
 constexpr int CHAINS = 8;
@@ -99,4 +100,32 @@ extern "C" lmg_status lmg_probe_fp64(int32_t device, double *tflops) {
   const double flops = 2.0 * CHAINS * (double)iters * blocks * threads;
   *tflops = flops / (ms * 1e-3) / 1e12;
   return LMG_OK;
+}
+
+// The exact float -> double conversion the kernels use (lmg::f2d), applied on
+// the device to n values: out[i] = f2d(in[i]).
+namespace {
+__global__ void k_f2d(int64_t n, const float *in, double *out) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = lmg::f2d(in[i]);
+}
+}  // namespace
+
+extern "C" lmg_status lmg_probe_f2d(int32_t device, int64_t n, const float *in, double *out) {
+  if (n < 0 || (n > 0 && (!in || !out))) return LMG_ERR_ARG;
+  if (n == 0) return LMG_OK;
+  if (cudaSetDevice(device) != cudaSuccess) return LMG_ERR_CUDA;
+  float *din = nullptr;
+  double *dout = nullptr;
+  cudaError_t e = cudaMalloc((void **)&din, sizeof(float) * (size_t)n);
+  if (e == cudaSuccess) e = cudaMalloc((void **)&dout, sizeof(double) * (size_t)n);
+  if (e == cudaSuccess) e = cudaMemcpy(din, in, sizeof(float) * (size_t)n, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) {
+    k_f2d<<<256, 256>>>(n, din, dout);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(out, dout, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost);
+  if (din) cudaFree(din);
+  if (dout) cudaFree(dout);
+  return e == cudaSuccess ? LMG_OK : LMG_ERR_CUDA;
 }
