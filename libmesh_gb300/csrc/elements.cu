@@ -675,7 +675,8 @@ __global__ void __launch_bounds__(256, 6) k_rows_mixed(FusedArgs f) {
   // (padded to 12 floats: one pair's 9 values are three vector loads)
   float *sS = fsm;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  float *acc = sS + 12 * N * N + (int64_t)warp * f.max_deg * B2;
+  constexpr int AS = NV == 3 ? 12 : B2;  // floats per slot of the shared-memory row
+  float *acc = sS + 12 * N * N + (int64_t)warp * f.max_deg * AS;
   for (int i = threadIdx.x; i < 9 * N * N; i += blockDim.x) {
     const int mn = i / (N * N), ab = i - mn * (N * N);
     sS[ab * 12 + mn] = R::from(f.el.fe.S[i]);
@@ -691,7 +692,7 @@ __global__ void __launch_bounds__(256, 6) k_rows_mixed(FusedArgs f) {
     const int deg = (int)(f.brow_ptr[P + 1] - rb);
     const int32_t t0 = f.fptr[P], t1 = f.fptr[P + 1];
     __syncwarp();
-    for (int x = lane; x < deg * B2; x += 32) acc[x] = 0.f;
+    for (int x = lane; x < deg * AS; x += 32) acc[x] = 0.f;
     __syncwarp();
     for (int32_t tg = t0; tg < t1; tg += NPASS) {
       const int32_t t = tg + wi;
@@ -730,9 +731,27 @@ __global__ void __launch_bounds__(256, 6) k_rows_mixed(FusedArgs f) {
       // element order: the incidences of this pass add one after the other
 #pragma unroll
       for (int w = 0; w < NPASS; ++w) {
-        if (work && wi == w)
+        if (work && wi == w) {
+          if constexpr (NV == 3) {
+            // a 3 x 3 block padded to 12 floats: two 16-byte and one 4-byte update
+            float4 *a4 = reinterpret_cast<float4 *>(acc + rel * AS);
+            float4 x0 = a4[0], x1 = a4[1];
+            x0.x = __fadd_rn(x0.x, out[0]);
+            x0.y = __fadd_rn(x0.y, out[1]);
+            x0.z = __fadd_rn(x0.z, out[2]);
+            x0.w = __fadd_rn(x0.w, out[3]);
+            x1.x = __fadd_rn(x1.x, out[4]);
+            x1.y = __fadd_rn(x1.y, out[5]);
+            x1.z = __fadd_rn(x1.z, out[6]);
+            x1.w = __fadd_rn(x1.w, out[7]);
+            a4[0] = x0;
+            a4[1] = x1;
+            acc[rel * AS + 8] = __fadd_rn(acc[rel * AS + 8], out[8]);
+          } else {
 #pragma unroll
-          for (int ik = 0; ik < B2; ++ik) acc[rel * B2 + ik] = __fadd_rn(acc[rel * B2 + ik], out[ik]);
+            for (int ik = 0; ik < B2; ++ik) acc[rel * AS + ik] = __fadd_rn(acc[rel * AS + ik], out[ik]);
+          }
+        }
         __syncwarp();
       }
     }
@@ -751,7 +770,7 @@ __global__ void __launch_bounds__(256, 6) k_rows_mixed(FusedArgs f) {
         for (int jj = js3; act3 && jj < deg; jj += 10) {
           const int32_t Q = f.bcol[rb + jj];
           if (Q == (int32_t)P) { jdiag = jj; continue; }
-          const float *ar = acc + jj * 9 + i3 * 3;
+          const float *ar = acc + jj * AS + i3 * 3;
           double *Kr = f.K + rowp + jj * 3;
 #pragma unroll
           for (int kk = 0; kk < 3; ++kk) {
@@ -799,7 +818,7 @@ __global__ void __launch_bounds__(256, 6) k_rows_mixed(FusedArgs f) {
         for (int jj = js; act && jj < deg; jj += SPL) {
           const int32_t Q = f.bcol[rb + jj];
           if (Q == (int32_t)P) { jdiag = jj; continue; }
-          const float kv = acc[jj * B2 + rem];
+          const float kv = acc[jj * AS + rem];
           const float s = __fadd_rn(rh, kv), bb = __fsub_rn(s, rh);
           rl = __fadd_rn(rl, __fadd_rn(__fsub_rn(rh, __fsub_rn(s, bb)), __fsub_rn(kv, bb)));
           rh = s;
@@ -845,7 +864,7 @@ void launch_fused_t(const FusedArgs &f, int grid, cudaStream_t s, bool geo, bool
   const int64_t gb = (f.el.n_list + 127) / 128;
   if (geo && gb > 0) k_geo<FORM, N, NV><<<(int)(gb < grid ? gb : grid), 128, 0, s>>>(f);
   if (!rows) return;
-  const size_t smem = sizeof(float) * (12 * N * N + (size_t)8 * f.max_deg * NV * NV);
+  const size_t smem = sizeof(float) * (12 * N * N + (size_t)8 * f.max_deg * (NV == 3 ? 12 : NV * NV));
   static size_t attr = 0;
   if (smem > attr) {
     cudaFuncSetAttribute(k_rows_mixed<FORM, N, NV>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -868,7 +887,7 @@ bool fused_built(int form, int n, int nv) {
 }
 
 bool fused_fits(int n, int nv, int max_deg) {
-  return sizeof(float) * (12 * (size_t)n * n + (size_t)8 * max_deg * nv * nv) <= (size_t)200 * 1024;
+  return sizeof(float) * (12 * (size_t)n * n + (size_t)8 * max_deg * (nv == 3 ? 12 : nv * nv)) <= (size_t)200 * 1024;
 }
 
 bool launch_fused_mixed(int form, int n, int nv, const FusedArgs &f, int grid, cudaStream_t s, bool geo,
