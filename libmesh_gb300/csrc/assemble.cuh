@@ -150,5 +150,9 @@ bool gather_built(int bs);
 int cg_solve(int64_t n, const int32_t *rp, const int32_t *col, const double *val, const double *b, double *x,
              double rtol, int maxit, cudaStream_t s, int n_sm, int *iters, double *relres, int64_t *launches);
 void launch_gather(const GatherArgs &g, bool mixed, cudaStream_t s);
+// The load vector of block rows [r0, r1): per dof the element entries in
+// element order (thread per block row; every insertion's F).
+void launch_load_vec(int bs, int64_t r0, int64_t r1, const int32_t *fptr, const int32_t *fcontrib,
+                     const float2 *Fe2, double *F, cudaStream_t s);
 
 }  // namespace lmg

@@ -1246,12 +1246,12 @@ lmg_status lmg_assemble(lmg_ctx *c, int32_t precision, double *K, double *F, int
             fc.row_begin = P0;
             fc.n_brows = P1;
             launch_fused_mixed(c->form, c->tab.n, c->n_vars, fc, grid, c->stream, false, true);
-            c->launches++;
+            c->launches += 2;  // row kernel, load vector
           });
       if (cs) return cs;
     } else {
       launch_fused_mixed(c->form, c->tab.n, c->n_vars, f, grid, c->stream, true, true);
-      c->launches += 2;
+      c->launches += 3;  // operands, row kernel, load vector
     }
     if (c->perflog) {
       LMG_CUDA(c, cudaEventRecord(e3[1], c->stream));
@@ -1318,12 +1318,12 @@ lmg_status lmg_assemble(lmg_ctx *c, int32_t precision, double *K, double *F, int
       gc.row_begin = P0;
       gc.row_end = P1;
       launch_gather(gc, mixed, c->stream);
-      c->launches++;
+      c->launches += 2;  // insertion, load vector
     });
     if (cs) return cs;
   } else {
     launch_gather(g, mixed, c->stream);
-    c->launches++;
+    c->launches += 2;  // insertion, load vector
   }
   if (c->perflog) LMG_CUDA(c, cudaEventRecord(e3[2], c->stream));
   LMG_CUDA(c, cudaGetLastError());

@@ -855,7 +855,6 @@ __global__ void __launch_bounds__(256, 6) k_rows_mixed(FusedArgs f) {
         f.K[rowp + jdiag * NV + k] = v;
       }
     }
-    row_load_seq<NV>(f.fptr, f.fcontrib, f.el.Fe2, f.F, P, lane);
   }
 }
 
@@ -872,6 +871,7 @@ void launch_fused_t(const FusedArgs &f, int grid, cudaStream_t s, bool geo, bool
   }
   const int64_t rb = (f.n_brows - f.row_begin + 7) / 8;
   if (rb > 0) k_rows_mixed<FORM, N, NV><<<(int)(rb < grid ? rb : grid), 256, smem, s>>>(f);
+  launch_load_vec(NV, f.row_begin, f.n_brows, f.fptr, f.fcontrib, f.el.Fe2, f.F, s);
 }
 
 }  // namespace

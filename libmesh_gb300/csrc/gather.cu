@@ -21,17 +21,48 @@
 
 #include "assemble.cuh"
 #include "df.cuh"
-#include "row_load.cuh"
 
 namespace lmg {
 
 namespace {
 
-// Load vector of the mixed insertion and of the QoI load: element order (the
-// fused row kernel's sums, so that both mixed paths give the same bits).
+// Load vector F: thread per block row, the element entries of each of its BS
+// dofs summed in element order (NumericVector::add_vector's order over the
+// elements, src/numerics/petsc_vector.C:174-195) in double-float from the
+// first term on, rounded once to FP64.  One kernel for every insertion (FP64,
+// mixed, fused, QoI load), so the forms give the same F bit for bit.
 template <int BS>
-__device__ __forceinline__ void row_load(const GatherArgs &g, int64_t P, int lane) {
-  row_load_seq<BS>(g.fptr, g.fcontrib, g.Fe2, g.F, P, lane);
+__global__ void __launch_bounds__(256) k_load_vec(int64_t r0, int64_t r1, const int32_t *fptr,
+                                                  const int32_t *fcontrib, const float2 *Fe2, double *F) {
+  for (int64_t P = r0 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; P < r1;
+       P += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t c0 = fptr[P], c1 = fptr[P + 1];
+    DFAcc s[BS];
+#pragma unroll
+    for (int q = 0; q < BS; ++q) s[q] = {0.f, 0.f};
+    int32_t c = c0;
+    for (; c + 1 < c1; c += 2) {  // two incidences' loads in flight
+      const int64_t b0 = (int64_t)__ldg(fcontrib + c) * BS, b1 = (int64_t)__ldg(fcontrib + c + 1) * BS;
+      float2 v0[BS], v1[BS];
+#pragma unroll
+      for (int q = 0; q < BS; ++q) {
+        v0[q] = __ldg(Fe2 + b0 + q);
+        v1[q] = __ldg(Fe2 + b1 + q);
+      }
+#pragma unroll
+      for (int q = 0; q < BS; ++q) {
+        acc_add(s[q], v0[q]);
+        acc_add(s[q], v1[q]);
+      }
+    }
+    if (c < c1) {
+      const int64_t b0 = (int64_t)__ldg(fcontrib + c) * BS;
+#pragma unroll
+      for (int q = 0; q < BS; ++q) acc_add(s[q], __ldg(Fe2 + b0 + q));
+    }
+#pragma unroll
+    for (int q = 0; q < BS; ++q) F[BS * P + q] = f2d(s[q].hi) + f2d(s[q].lo);
+  }
 }
 
 
@@ -106,7 +137,6 @@ __device__ __forceinline__ void row_slots(const GatherArgs &g, const int32_t *pt
 template <int BS>
 __global__ void __launch_bounds__(GW * 32, 6) k_gather(GatherArgs g) {
   constexpr int SPI = 32 / BS;
-  static_assert(BS <= 4, "the load-vector butterfly carries at most 4 components");
   __shared__ int32_t s_ptr[GW][DCAP + 1];
   __shared__ int32_t s_con[GW][CCAP];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -117,11 +147,6 @@ __global__ void __launch_bounds__(GW * 32, 6) k_gather(GatherArgs g) {
     const int64_t rb = g.brow_ptr[P];
     const int deg = (int)(g.brow_ptr[P + 1] - rb);
     const int32_t rowp = act ? g.row_ptr[BS * P + i] : 0;
-    const int32_t f0 = g.fptr[P], f1 = g.fptr[P + 1];
-    const int32_t fc = f0 + lane < f1 ? __ldg(g.fcontrib + f0 + lane) : -1;
-    float2 fv[BS];
-#pragma unroll
-    for (int q = 0; q < BS; ++q) fv[q] = fc >= 0 ? __ldg(g.Fe2 + (int64_t)fc * BS + q) : float2{0.f, 0.f};
     int jdiag = -1;
     for (int t = lane; t < deg; t += 32)
       if (g.bcol[rb + t] == (int32_t)P) jdiag = t;
@@ -142,58 +167,6 @@ __global__ void __launch_bounds__(GW * 32, 6) k_gather(GatherArgs g) {
       }
     }
     if (!staged && act) row_slots<BS>(g, g.bptr + rb, g.bcontrib, deg, jdiag, js, i, rowp);
-    // load vector: lane l sums contributions l, l + 32, ... in element order;
-    // one butterfly then reduces all BS components (halving the set carried
-    // per lane at the first two steps), the lower lane's value first.
-    DF s[4];
-#pragma unroll
-    for (int q = 0; q < 4; ++q) s[q] = q < BS ? df_add(DF{0.f, 0.f}, DF{fv[q < BS ? q : 0].x, fv[q < BS ? q : 0].y})
-                                              : DF{0.f, 0.f};
-    for (int32_t c = f0 + 32 + lane; c < f1; c += 32) {
-      const int64_t base = (int64_t)g.fcontrib[c] * BS;
-#pragma unroll
-      for (int q = 0; q < BS; ++q) {
-        const float2 v = g.Fe2[base + q];
-        s[q] = df_add(s[q], DF{v.x, v.y});
-      }
-    }
-    DF r;
-    if constexpr (BS == 1) {
-      r = s[0];
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        DF y;
-        y.hi = __shfl_xor_sync(0xffffffffu, r.hi, o);
-        y.lo = __shfl_xor_sync(0xffffffffu, r.lo, o);
-        r = (lane & o) ? df_add(y, r) : df_add(r, y);
-      }
-    } else {
-      const bool u16 = lane & 16, u8 = lane & 8;
-      DF k0 = u16 ? s[2] : s[0], k1 = u16 ? s[3] : s[1];  // kept: components 2h, 2h + 1
-      DF e0 = u16 ? s[0] : s[2], e1 = u16 ? s[1] : s[3];  // sent to the partner
-      DF y0, y1;
-      y0.hi = __shfl_xor_sync(0xffffffffu, e0.hi, 16);
-      y0.lo = __shfl_xor_sync(0xffffffffu, e0.lo, 16);
-      y1.hi = __shfl_xor_sync(0xffffffffu, e1.hi, 16);
-      y1.lo = __shfl_xor_sync(0xffffffffu, e1.lo, 16);
-      k0 = u16 ? df_add(y0, k0) : df_add(k0, y0);
-      k1 = u16 ? df_add(y1, k1) : df_add(k1, y1);
-      r = u8 ? k1 : k0;                                   // component 2h + b
-      const DF e = u8 ? k0 : k1;
-      DF y;
-      y.hi = __shfl_xor_sync(0xffffffffu, e.hi, 8);
-      y.lo = __shfl_xor_sync(0xffffffffu, e.lo, 8);
-      r = u8 ? df_add(y, r) : df_add(r, y);
-#pragma unroll
-      for (int o = 4; o > 0; o >>= 1) {
-        y.hi = __shfl_xor_sync(0xffffffffu, r.hi, o);
-        y.lo = __shfl_xor_sync(0xffffffffu, r.lo, o);
-        r = (lane & o) ? df_add(y, r) : df_add(r, y);
-      }
-    }
-    // lane 16 h + 8 b holds component 2h + b
-    const int comp = BS == 1 ? lane : ((lane >> 4) << 1) + ((lane >> 3) & 1);
-    if ((BS == 1 ? lane == 0 : (lane & 7) == 0) && comp < BS) g.F[BS * P + comp] = df_to_double(r);
     __syncwarp();
   }
 }
@@ -270,32 +243,25 @@ __global__ void __launch_bounds__(256) k_gather_mixed(GatherArgs g) {
       }
       g.K[rowp + jdiag * BS + k] = v;
     }
-    row_load<BS>(g, P, lane);
   }
-}
-
-// Load vector only (QoI derivative): warp per block row, F from the element loads.
-template <int BS>
-__global__ void __launch_bounds__(256) k_gather_f(GatherArgs g) {
-  const int lane = threadIdx.x & 31;
-  for (int64_t P = g.row_begin + (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5); P < g.row_end;
-       P += ((int64_t)gridDim.x * blockDim.x) >> 5)
-    row_load<BS>(g, P, lane);
 }
 
 }  // namespace
 
-void launch_gather_f(const GatherArgs &g0, cudaStream_t s) {
-  GatherArgs g = g0;
-  if (g.row_end == 0) g.row_end = g.n_dofs / g.bs;
+void launch_load_vec(int bs, int64_t r0, int64_t r1, const int32_t *fptr, const int32_t *fcontrib,
+                     const float2 *Fe2, double *F, cudaStream_t s) {
+  if (r1 <= r0) return;
   int dev = 0, n_sm = 152;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, dev);
-  int64_t blocks = (g.n_dofs / g.bs + 7) / 8;
+  int64_t blocks = (r1 - r0 + 255) / 256;
   if (blocks > (int64_t)n_sm * 16) blocks = (int64_t)n_sm * 16;
-  if (blocks < 1) blocks = 1;
-  if (g.bs == 1) k_gather_f<1><<<(int)blocks, 256, 0, s>>>(g);
-  else if (g.bs == 3) k_gather_f<3><<<(int)blocks, 256, 0, s>>>(g);
+  if (bs == 1) k_load_vec<1><<<(int)blocks, 256, 0, s>>>(r0, r1, fptr, fcontrib, Fe2, F);
+  else if (bs == 3) k_load_vec<3><<<(int)blocks, 256, 0, s>>>(r0, r1, fptr, fcontrib, Fe2, F);
+}
+
+void launch_gather_f(const GatherArgs &g, cudaStream_t s) {
+  launch_load_vec(g.bs, g.row_begin, g.row_end ? g.row_end : g.n_dofs / g.bs, g.fptr, g.fcontrib, g.Fe2, g.F, s);
 }
 
 bool gather_built(int bs) { return bs == 1 || bs == 3; }
@@ -322,6 +288,7 @@ void launch_gather(const GatherArgs &g0, bool mixed, cudaStream_t s) {
     if (g.bs == 1) k_gather<1><<<(unsigned)rows, GW * 32, 0, s>>>(g);
     else if (g.bs == 3) k_gather<3><<<(unsigned)rows, GW * 32, 0, s>>>(g);
   }
+  launch_load_vec(g.bs, g.row_begin, g.row_end, g.fptr, g.fcontrib, g.Fe2, g.F, s);
 }
 
 }  // namespace lmg

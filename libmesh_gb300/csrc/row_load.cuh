@@ -1,6 +1,6 @@
-// Load vector of one block row: row_load_seq (element order: the mixed
-// insertions, the fused row kernel) and row_load_f (a butterfly over the
-// warp: the matrix-free residual's per-dof sums).
+// Per-dof sums of element vectors over one block row by a butterfly over the
+// warp: the matrix-free residual's R (the assembled load vector F is summed
+// in element order by the insertions' k_load_vec, gather.cu).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -44,27 +44,6 @@ __device__ __forceinline__ void row_load_f(const int32_t *fptr, const int32_t *f
       if (lane == i) r = s[i];
     F[BS * P + lane] = df_to_double(r);
   }
-}
-
-// Load vector of block row P in element order: lane i < BS sums the element
-// entries of dof BS P + i one after the other (the order of
-// NumericVector::add_vector over the elements, src/numerics/petsc_vector.C:174-195)
-// in double-float, rounded once to FP64.
-template <int BS>
-__device__ __forceinline__ void row_load_seq(const int32_t *fptr, const int32_t *fcontrib, const float2 *Fe2,
-                                             double *F, int64_t P, int lane) {
-  if (lane >= BS) return;
-  const int32_t f0 = fptr[P], f1 = fptr[P + 1];
-  DFAcc s = {0.f, 0.f};
-  int32_t c = f0;
-  for (; c + 1 < f1; c += 2) {  // two loads in flight
-    const float2 v0 = __ldg(Fe2 + (int64_t)__ldg(fcontrib + c) * BS + lane);
-    const float2 v1 = __ldg(Fe2 + (int64_t)__ldg(fcontrib + c + 1) * BS + lane);
-    acc_add(s, v0);
-    acc_add(s, v1);
-  }
-  if (c < f1) acc_add(s, __ldg(Fe2 + (int64_t)__ldg(fcontrib + c) * BS + lane));
-  F[BS * P + lane] = f2d(s.hi) + f2d(s.lo);
 }
 
 }  // namespace lmg

@@ -54,7 +54,7 @@ def test_tensor_core_mixed_form(et, nv, form, fo, qo, n):
     Kcc, Fcc = asm.assemble(lm.MIXED)
     asm.close()
     assert np.array_equal(K32, K32b) and np.array_equal(F32, F32b)
-    assert np.abs(F32 - F64).max() <= 1e-13 * np.abs(F64).max()
+    assert np.array_equal(F32, F64)
     print("tensor-core mixed %d/%d: ||dK||/||K|| %.3g (CUDA-core mixed %.3g)  ||du||/||u|| %.3g"
           % (et, form, rel(K32, K64), rel(Kcc, K64), rel(u32, u64)))
     assert rel(K32, K64) < 1e-6
