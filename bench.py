@@ -789,14 +789,14 @@ def main():
         no = 45
         gbytes = 8 * asm.nnz + 8 * dm.n_dofs
         impl = 8 * mesh.n_elem * (10 * 9 + no * 9) + 8 * mesh.n_elem * 30 + 4 * mesh.n_elem * 100
-        dom = {"kernel": "k_gather<double,3>", "bound": "hbm", "unit": "GB/s",
+        dom = {"kernel": "k_gather<double,3> + k_load_vec<3>", "bound": "hbm", "unit": "GB/s",
                "achieved": gbytes / (ga_ms * 1e-3) / 1e9, "peak": hbm, "peak_source": hbm_src,
                "bytes_per_launch": gbytes, "implementation_bytes_per_launch": impl}
     dom["frac"] = dom["achieved"] / dom["peak"]
     # DRAM bytes of one launch from ncu on the 24^3 case (profiles/elasticity_tet10_24_kernels.md),
     # scaled by the element count; traffic grows in proportion to the mesh.
-    per24 = {"k_gather<double,3>": 731908864 + 245608192,
-             "k_elem_affine<ELASTICITY,10,3,double>": 15557120 + 291394560}
+    per24 = {"k_gather<double,3> + k_load_vec<3>": 644832256 + 213843712 + 23702016,
+             "k_elem_affine<ELASTICITY,10,3,double>": 20240128 + 296399360}
     dom["traffic"] = per24[dom["kernel"]] * mesh.n_elem / 82944.0 if args.n == N_CUBE else None
     dom["traffic_source"] = "ncu dram__bytes_read+write on build_cube 24^3, scaled x%.1f" % (mesh.n_elem / 82944.0)
     dom["stages_ms"] = {"elements": el_ms, "insertion": ga_ms}
