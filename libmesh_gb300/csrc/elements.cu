@@ -41,7 +41,6 @@
 #include "assemble.cuh"
 #include "df.cuh"
 #include "elem_geom.cuh"
-#include "row_load.cuh"
 #include "../../include/libmesh_gb300.h"
 
 namespace lmg {
@@ -459,14 +458,6 @@ __global__ void __launch_bounds__(128) k_residual_affine(ElemArgs a) {
   }
 }
 
-template <int BS>
-__global__ void __launch_bounds__(256) k_gather_vec(int64_t n_brows, const int32_t *fptr, const int32_t *fcontrib,
-                                                    const float2 *Re2, double *R) {
-  const int lane = threadIdx.x & 31;
-  for (int64_t P = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; P < n_brows;
-       P += ((int64_t)gridDim.x * blockDim.x) >> 5)
-    row_load_f<BS>(fptr, fcontrib, Re2, R, P, lane);
-}
 
 template <int FORM, int N, int NV>
 void launch_residual_t(const ElemArgs &a, int grid, cudaStream_t s) {
@@ -929,12 +920,8 @@ bool launch_residual(int form, int n, int nv, const ElemArgs &a, int64_t n_brows
   LMG_R(LMG_ELASTICITY, 10, 3)
 #undef LMG_R
   if (!ok) return false;
-  const int64_t blocks = (n_brows * 32 + 255) / 256;
-  const int g = (int)(blocks < grid ? blocks : grid);
-  if (g > 0) {
-    if (nv == 3) k_gather_vec<3><<<g, 256, 0, s>>>(n_brows, fptr, fcontrib, a.Re2, R);
-    else k_gather_vec<1><<<g, 256, 0, s>>>(n_brows, fptr, fcontrib, a.Re2, R);
-  }
+  (void)grid;
+  launch_load_vec(nv, 0, n_brows, fptr, fcontrib, a.Re2, R, s);  // per-dof sums in element order
   return true;
 }
 
