@@ -83,9 +83,10 @@ __global__ void __launch_bounds__(256) k_load_vec(int64_t r0, int64_t r1, const 
 // loads of all its slots are independent of one another; rows larger than the
 // staging buffers read the plan from global memory (same sums).  The load
 // vector's first 32 contributions are fetched before the slots.
-constexpr int GW = 8;      // warps (block rows in flight) per CTA
-constexpr int DCAP = 128;  // staged slots per block row
-constexpr int CCAP = 640;  // staged contributions per block row
+constexpr int GW = 8;      // warps per CTA
+constexpr int RG = 4;      // consecutive block rows per warp step (their plans are contiguous)
+constexpr int DCAP = 192;  // staged slots per warp step
+constexpr int CCAP = 768;  // staged contributions per warp step
 
 // Slots jj = js, js + SPI, ... of block row P; `ptr[jj]` is the slot's first
 // contribution relative to `con`.
@@ -143,31 +144,45 @@ __global__ void __launch_bounds__(GW * 32, 6) k_gather(GatherArgs g) {
   const int js = lane / BS, i = lane - js * BS;
   const bool act = lane < SPI * BS;
   int32_t *sp = s_ptr[warp], *sc = s_con[warp];
-  for (int64_t P = g.row_begin + (int64_t)blockIdx.x * GW + warp; P < g.row_end; P += (int64_t)gridDim.x * GW) {
-    const int64_t rb = g.brow_ptr[P];
-    const int deg = (int)(g.brow_ptr[P + 1] - rb);
-    const int32_t rowp = act ? g.row_ptr[BS * P + i] : 0;
-    int jdiag = -1;
-    for (int t = lane; t < deg; t += 32)
-      if (g.bcol[rb + t] == (int32_t)P) jdiag = t;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) jdiag = max(jdiag, __shfl_xor_sync(0xffffffffu, jdiag, o));
+  // A warp takes RG consecutive block rows at a time: their slot offsets and
+  // contribution lists are contiguous, so one round of loads stages all of
+  // them; the rows' sums then read the plan from shared memory.  A step whose
+  // plan outgrows the buffers reads it from global memory (same sums).
+  for (int64_t P0 = g.row_begin + ((int64_t)blockIdx.x * GW + warp) * RG; P0 < g.row_end;
+       P0 += (int64_t)gridDim.x * GW * RG) {
+    const int nr = (int)(g.row_end - P0 < RG ? g.row_end - P0 : RG);
+    const int64_t hb = lane <= nr ? g.brow_ptr[P0 + lane] : 0;  // the step's row offsets
+    const int64_t rb0 = __shfl_sync(0xffffffffu, hb, 0), rbn = __shfl_sync(0xffffffffu, hb, nr);
+    const int ns = (int)(rbn - rb0);
     bool staged = false;
-    if (deg <= DCAP) {
-      for (int t = lane; t <= deg; t += 32) sp[t] = __ldg(g.bptr + rb + t);
+    if (ns <= DCAP) {
+      for (int t = lane; t <= ns; t += 32) sp[t] = __ldg(g.bptr + rb0 + t);
       __syncwarp();
-      const int32_t cb = sp[0], nc = sp[deg] - cb;
+      const int32_t cb = sp[0], nc = sp[ns] - cb;
       __syncwarp();  // every lane has read cb before sp is rebased
       if (nc <= CCAP) {
         staged = true;
         for (int t = lane; t < nc; t += 32) sc[t] = __ldg(g.bcontrib + cb + t);
-        for (int t = lane; t <= deg; t += 32) sp[t] -= cb;
-        __syncwarp();
-        if (act) row_slots<BS>(g, sp, sc, deg, jdiag, js, i, rowp);
+        for (int t = lane; t <= ns; t += 32) sp[t] -= cb;
+      }
+      __syncwarp();
+    }
+    for (int r = 0; r < nr; ++r) {
+      const int64_t P = P0 + r;
+      const int64_t rb = __shfl_sync(0xffffffffu, hb, r);
+      const int deg = (int)(__shfl_sync(0xffffffffu, hb, r + 1) - rb);
+      const int32_t rowp = act ? g.row_ptr[BS * P + i] : 0;
+      int jdiag = -1;
+      for (int t = lane; t < deg; t += 32)
+        if (g.bcol[rb + t] == (int32_t)P) jdiag = t;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) jdiag = max(jdiag, __shfl_xor_sync(0xffffffffu, jdiag, o));
+      if (act) {
+        if (staged) row_slots<BS>(g, sp + (rb - rb0), sc, deg, jdiag, js, i, rowp);
+        else row_slots<BS>(g, g.bptr + rb, g.bcontrib, deg, jdiag, js, i, rowp);
       }
     }
-    if (!staged && act) row_slots<BS>(g, g.bptr + rb, g.bcontrib, deg, jdiag, js, i, rowp);
-    __syncwarp();
+    __syncwarp();  // the step's plan is read before the next step stages its own
   }
 }
 
@@ -284,7 +299,7 @@ void launch_gather(const GatherArgs &g0, bool mixed, cudaStream_t s) {
     int per_sm = 1;
     if (g.bs == 1) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gather<1>, GW * 32, 0);
     else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gather<3>, GW * 32, 0);
-    const int64_t rows = std::min<int64_t>((warps + GW - 1) / GW, (int64_t)n_sm * std::max(per_sm, 1));
+    const int64_t rows = std::min<int64_t>((warps + GW * RG - 1) / (GW * RG), (int64_t)n_sm * std::max(per_sm, 1));
     if (g.bs == 1) k_gather<1><<<(unsigned)rows, GW * 32, 0, s>>>(g);
     else if (g.bs == 3) k_gather<3><<<(unsigned)rows, GW * 32, 0, s>>>(g);
   }
