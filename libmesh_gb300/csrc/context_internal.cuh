@@ -16,6 +16,7 @@ struct lmg_ctx {
   bool own_stream = false;
   int n_sm = 152;
   int ctas_per_sm = 32;  // element-kernel grid (grid-stride), set by the batch autotuner
+  bool grid_set = false;  // ctas_per_sm chosen by the caller (lmg_context_set_grid)
   bool tensor_cores = true;  // mixed form: per-point Gram products on the tensor cores where built
   int64_t launches = 0;
   std::string err;
