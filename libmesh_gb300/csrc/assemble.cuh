@@ -78,6 +78,7 @@ struct GatherArgs {
   const int32_t *row_ptr;     // [n_dofs+1]
   const int32_t *bcol;        // [nnzb]
   const int32_t *bptr;        // [nnzb+1] contributions per block slot
+  const int32_t *bdiag;       // [n_blocks] position of the diagonal slot in each block row (or null)
   // Per slot, ascending in element: diagonal slots hold e*nb + a (a Kdiag
   // block); off-diagonal slots hold 2*(e*no + o) + t, o the strictly upper
   // block of the element pair and t = 1 when the slot takes its transpose.

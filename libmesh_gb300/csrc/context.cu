@@ -284,6 +284,20 @@ __global__ void k_rowcons(int64_t n_rows, int bs, const int64_t *brow_ptr, const
   }
 }
 
+// Position of the diagonal slot in every block row (the insertion reads it
+// with the row headers instead of searching the row's columns).
+__global__ void k_bdiag(int64_t n_rows, const int64_t *brow_ptr, const int32_t *bcol, int32_t *bdiag) {
+  for (int64_t P = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; P < n_rows; P += (int64_t)gridDim.x * blockDim.x) {
+    int64_t lo = brow_ptr[P], hi = brow_ptr[P + 1];
+    const int64_t b = lo;
+    while (lo < hi) {
+      const int64_t mid = (lo + hi) >> 1;
+      if (bcol[mid] < P) lo = mid + 1; else hi = mid;
+    }
+    bdiag[P] = (lo < brow_ptr[P + 1] && bcol[lo] == (int32_t)P) ? (int32_t)(lo - b) : -1;
+  }
+}
+
 // Nodal load split into double-float pairs (read by the affine element kernels).
 __global__ void k_split(int64_t n, const double *x, float2 *y) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
@@ -616,6 +630,10 @@ lmg_status build_plan(lmg_ctx *c) {
   c->launches += 3;
   dfree(c->d_relslot);
   dfree(c->d_rowcons);
+  dfree(c->d_bdiag);
+  LMG_CUDA(c, dalloc(c->d_bdiag, (size_t)std::max<int64_t>(c->n_blocks, 1)));
+  k_bdiag<<<grid_for(c, c->n_blocks, 256), 256, 0, c->stream>>>(c->n_blocks, c->d_brow_ptr, c->d_bcol, c->d_bdiag);
+  c->launches++;
   if (c->max_bdeg <= 255) {  // the fused mixed form addresses slots with one byte
     LMG_CUDA(c, dalloc(c->d_relslot, (size_t)npair));
     k_relslot<<<grid_for(c, npair, 256), 256, 0, c->stream>>>(npair, nb, c->d_eb, c->d_brow_ptr, slot,
@@ -763,7 +781,7 @@ lmg_status lmg_context_destroy(lmg_ctx *c) {
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
   dfree(c->d_xyz); dfree(c->d_conn); dfree(c->d_aff); dfree(c->d_gen); dfree(c->d_eb);
-  dfree(c->d_cmask); dfree(c->d_cons); dfree(c->d_rowcons); dfree(c->d_brow_ptr); dfree(c->d_bcol); dfree(c->d_row_ptr); dfree(c->d_col);
+  dfree(c->d_cmask); dfree(c->d_cons); dfree(c->d_rowcons); dfree(c->d_bdiag); dfree(c->d_brow_ptr); dfree(c->d_bcol); dfree(c->d_row_ptr); dfree(c->d_col);
   dfree(c->d_bptr); dfree(c->d_bcontrib); dfree(c->d_fptr); dfree(c->d_fcontrib); dfree(c->d_tab);
   dfree(c->d_coef); dfree(c->d_f); dfree(c->d_f2); dfree(c->d_Kdiag2); dfree(c->d_Koff2); dfree(c->d_Fe2); dfree(c->d_K);
   dfree(c->d_F); dfree(c->d_Koff32); dfree(c->d_status); dfree(c->d_bad);
@@ -1305,6 +1323,7 @@ lmg_status lmg_assemble(lmg_ctx *c, int32_t precision, double *K, double *F, int
   g.row_ptr = c->d_row_ptr;
   g.bcol = c->d_bcol;
   g.bptr = c->d_bptr;
+  g.bdiag = c->d_bdiag;
   g.bcontrib = c->d_bcontrib;
   g.no = c->nb * (c->nb - 1) / 2;
   g.fptr = c->d_fptr;

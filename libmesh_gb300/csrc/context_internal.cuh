@@ -51,6 +51,7 @@ struct lmg_ctx {
   std::vector<cudaEvent_t> chunk_ev;
   uint8_t *d_relslot = nullptr;  // [E][nb][nb] slot of block (a, b) in block row of a (fused mixed form)
   uint8_t *d_rowcons = nullptr;  // [n_blocks] block row touches a constrained dof (fused mixed form)
+  int32_t *d_bdiag = nullptr;    // [n_blocks] position of the diagonal slot in each block row
   int max_bdeg = 0;              // largest block-row degree
   float *d_geo = nullptr;        // [E][NG] per-element operands (fused mixed form)
   // form

@@ -152,6 +152,7 @@ __global__ void __launch_bounds__(GW * 32, 6) k_gather(GatherArgs g) {
        P0 += (int64_t)gridDim.x * GW * RG) {
     const int nr = (int)(g.row_end - P0 < RG ? g.row_end - P0 : RG);
     const int64_t hb = lane <= nr ? g.brow_ptr[P0 + lane] : 0;  // the step's row offsets
+    const int32_t hd = (g.bdiag && lane < nr) ? g.bdiag[P0 + lane] : -1;  // and diagonal slots
     const int64_t rb0 = __shfl_sync(0xffffffffu, hb, 0), rbn = __shfl_sync(0xffffffffu, hb, nr);
     const int ns = (int)(rbn - rb0);
     bool staged = false;
@@ -171,12 +172,15 @@ __global__ void __launch_bounds__(GW * 32, 6) k_gather(GatherArgs g) {
       const int64_t P = P0 + r;
       const int64_t rb = __shfl_sync(0xffffffffu, hb, r);
       const int deg = (int)(__shfl_sync(0xffffffffu, hb, r + 1) - rb);
-      const int32_t rowp = act ? g.row_ptr[BS * P + i] : 0;
-      int jdiag = -1;
-      for (int t = lane; t < deg; t += 32)
-        if (g.bcol[rb + t] == (int32_t)P) jdiag = t;
+      // dof row BS P + i of the block CSR starts at BS^2 brow_ptr[P] + i BS deg
+      const int32_t rowp = act ? (int32_t)(BS * BS * rb + (int64_t)i * BS * deg) : 0;
+      int jdiag = __shfl_sync(0xffffffffu, hd, r);
+      if (!g.bdiag) {
+        for (int t = lane; t < deg; t += 32)
+          if (g.bcol[rb + t] == (int32_t)P) jdiag = t;
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) jdiag = max(jdiag, __shfl_xor_sync(0xffffffffu, jdiag, o));
+        for (int o = 16; o > 0; o >>= 1) jdiag = max(jdiag, __shfl_xor_sync(0xffffffffu, jdiag, o));
+      }
       if (act) {
         if (staged) row_slots<BS>(g, sp + (rb - rb0), sc, deg, jdiag, js, i, rowp);
         else row_slots<BS>(g, g.bptr + rb, g.bcontrib, deg, jdiag, js, i, rowp);
