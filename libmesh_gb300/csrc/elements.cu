@@ -753,7 +753,8 @@ __global__ void __launch_bounds__(256, 6) k_rows_mixed(FusedArgs f) {
       // entries each (written contiguously), with their double-float row sums
       const int js3 = lane / 3, i3 = lane - js3 * 3;
       const bool act3 = lane < 30;
-      const int32_t rowp = act3 ? f.row_ptr[3 * P + i3] : 0;
+      // dof row 3 P + i3 of the block CSR starts at 9 brow_ptr[P] + 3 i3 deg
+      const int32_t rowp = act3 ? (int32_t)(9 * rb + (int64_t)3 * i3 * deg) : 0;
       const bool rc = act3 && f.constrained[3 * P + i3] != 0;
       float rh[3] = {0.f, 0.f, 0.f}, rl[3] = {0.f, 0.f, 0.f};
       int jdiag = -1;
@@ -801,7 +802,7 @@ __global__ void __launch_bounds__(256, 6) k_rows_mixed(FusedArgs f) {
         }
       }
     } else {
-      const int32_t rowp = act ? f.row_ptr[NV * P + i] : 0;
+      const int32_t rowp = act ? (int32_t)(NV * NV * rb + (int64_t)NV * i * deg) : 0;
       const bool rc = act && f.constrained[NV * P + i] != 0;
       float rh = 0.f, rl = 0.f;  // double-float row sum, normalised after the loop
       int jdiag = -1;
