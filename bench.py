@@ -402,46 +402,48 @@ def run_batch(args, local):
     ev1.synchronize()
     b.synchronize()
     ms32 = ev0.elapsed_time(ev1) / args.steps
-    # one persistent launch per replay (every member's tiles and insertion from one queue)
-    persist = {}
-    b.set_persistent(True)
-    for prec, key in ((lm.FP64, "fp64"), (lm.MIXED, "mixed")):
-        b.tune(prec, reps=2)
-        for _ in range(max(3, args.warmup)):
-            b.assemble(prec)
-        b.synchronize()
-        ev0.record(stream)
-        for _ in range(args.steps):
-            b.assemble(prec)
-        ev1.record(stream)
-        ev1.synchronize()
-        b.synchronize()
-        tile, ctas, items = b.persistent_info()
-        pms = ev0.elapsed_time(ev1) / args.steps
-        persist[key] = {"ms_per_step": pms, "value": total / (pms * 1e-3) / 1e6, "unit": "Melem/s",
-                        "tile_elements_per_cta": tile, "ctas_per_sm": ctas or "occupancy", "work_items": items}
-    persist["launches_per_replay"] = 1
-    persist["mixed_speedup_vs_fp64"] = persist["fp64"]["ms_per_step"] / persist["mixed"]["ms_per_step"]
-    # hybrid: one persistent launch over the per-pattern members, the others' own kernels beside it
-    hybrid = {}
-    b.set_persistent(True, hybrid=True)
-    for prec, key in ((lm.FP64, "fp64"), (lm.MIXED, "mixed")):
-        b.tune(prec, reps=2)
-        for _ in range(max(3, args.warmup)):
-            b.assemble(prec)
-        b.synchronize()
-        ev0.record(stream)
-        for _ in range(args.steps):
-            b.assemble(prec)
-        ev1.record(stream)
-        ev1.synchronize()
-        b.synchronize()
-        hms = ev0.elapsed_time(ev1) / args.steps
-        _, hl, _ = b.info()
-        hybrid[key] = {"ms_per_step": hms, "value": total / (hms * 1e-3) / 1e6, "unit": "Melem/s",
-                       "launches_per_replay": hl}
-    hybrid["mixed_speedup_vs_fp64"] = hybrid["fp64"]["ms_per_step"] / hybrid["mixed"]["ms_per_step"]
-    hybrid["vs_graph"] = ms / hybrid["fp64"]["ms_per_step"]
+    persist, hybrid = None, None
+    if not args.no_persistent:
+        # one persistent launch per replay (every member's tiles and insertion from one queue)
+        persist = {}
+        b.set_persistent(True)
+        for prec, key in ((lm.FP64, "fp64"), (lm.MIXED, "mixed")):
+            b.tune(prec, reps=2)
+            for _ in range(max(3, args.warmup)):
+                b.assemble(prec)
+            b.synchronize()
+            ev0.record(stream)
+            for _ in range(args.steps):
+                b.assemble(prec)
+            ev1.record(stream)
+            ev1.synchronize()
+            b.synchronize()
+            tile, ctas, items = b.persistent_info()
+            pms = ev0.elapsed_time(ev1) / args.steps
+            persist[key] = {"ms_per_step": pms, "value": total / (pms * 1e-3) / 1e6, "unit": "Melem/s",
+                            "tile_elements_per_cta": tile, "ctas_per_sm": ctas or "occupancy", "work_items": items}
+        persist["launches_per_replay"] = 1
+        persist["mixed_speedup_vs_fp64"] = persist["fp64"]["ms_per_step"] / persist["mixed"]["ms_per_step"]
+        # hybrid: one persistent launch over the per-pattern members, the others' own kernels beside it
+        hybrid = {}
+        b.set_persistent(True, hybrid=True)
+        for prec, key in ((lm.FP64, "fp64"), (lm.MIXED, "mixed")):
+            b.tune(prec, reps=2)
+            for _ in range(max(3, args.warmup)):
+                b.assemble(prec)
+            b.synchronize()
+            ev0.record(stream)
+            for _ in range(args.steps):
+                b.assemble(prec)
+            ev1.record(stream)
+            ev1.synchronize()
+            b.synchronize()
+            hms = ev0.elapsed_time(ev1) / args.steps
+            _, hl, _ = b.info()
+            hybrid[key] = {"ms_per_step": hms, "value": total / (hms * 1e-3) / 1e6, "unit": "Melem/s",
+                           "launches_per_replay": hl}
+        hybrid["mixed_speedup_vs_fp64"] = hybrid["fp64"]["ms_per_step"] / hybrid["mixed"]["ms_per_step"]
+        hybrid["vs_graph"] = ms / hybrid["fp64"]["ms_per_step"]
     b.close()
     # (c) one system after another on one stream, as System::assemble is
     # called for each system in turn (the tuned grids of the graph)
@@ -628,6 +630,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline leg")
     ap.add_argument("--n", type=int, default=N_CUBE, help="cube divisions (48 = the headline mesh)")
     ap.add_argument("--no-mixed", action="store_true", help="skip timing the mixed form beside FP64")
+    ap.add_argument("--no-persistent", action="store_true",
+                    help="batch workload: skip the persistent-launch legs (e.g. for a launch list of the graph)")
     ap.add_argument("--workload", default="elasticity",
                     choices=["elasticity", "amr-cd", "batch", "adjoint", "curved"],
                     help="elasticity = the headline; amr-cd = refined HEX27 convection-diffusion; "
