@@ -1,6 +1,7 @@
 // FP64 throughput probes, timed with CUDA events: independent DFMA chains on
 // every SM (the FP64 roofline denominator the assembly kernels are measured
-// against; GB300 FP64 is not among the measured peaks), and the same
+// against; the copy-bandwidth and BF16 peaks measured beside it say nothing
+// about FP64), and the same
 // with FP64 tensor-core products (mma.sync m8n8k4 f64, DMMA), to compare the
 // two routes an FP64 contraction could take.
 #include <cuda_runtime.h>
