@@ -211,8 +211,10 @@ def run_amr(args, local):
     n = 24 if args.n == N_CUBE else args.n      # build_cube 24^3 HEX27 unless --n is given
     mesh = lm.Mesh.build_refined_cube(n, lm.HEX27, 3, 0.2, 2)
     t_mesh = time.perf_counter() - t0
+    t1 = time.perf_counter()
     dm = lm.DofMap(mesh, 1)
     dm.add_dirichlet_boundary([0, 1, 2, 3, 4, 5], [0])
+    t_dofmap = time.perf_counter() - t1
     dm_host = lm.DofMap(mesh, 1)
     dm_host.add_dirichlet_boundary([0, 1, 2, 3, 4, 5], [0])
     t1 = time.perf_counter()
@@ -227,11 +229,15 @@ def run_amr(args, local):
     k = np.exp(rng.normal(0.0, 0.5, mesh.n_elem))
     f = rng.uniform(-1.0, 1.0, (mesh.n_nodes, 1))
     asm = lm.GpuAssembly(lm.ADVDIFF, 2, 5, elem_coef=k, nodal_f=f, params=cd_params(), device=local)
-    asm.init(mesh, dm)
+    t1 = time.perf_counter()
+    asm.init(mesh, dm)                  # uploads, constrained sparsity on the device
+    t_init = time.perf_counter() - t1
     stream = torch.cuda.current_stream()
     asm.set_stream(stream.cuda_stream)
+    t1 = time.perf_counter()
     asm.assemble_device(lm.FP64)        # builds the slot plan
     asm.synchronize()
+    t_first = time.perf_counter() - t1
     setup_s = time.perf_counter() - t0
     for _ in range(max(3, args.warmup)):
         asm.assemble_device(lm.FP64)
@@ -293,8 +299,9 @@ def run_amr(args, local):
         "metric": METRIC, "value": mesh.n_elem / (ms * 1e-3) / 1e6, "unit": "Melem/s", "n_gpus": 1,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded refinement, k_e, f, b)",
-        "setup_breakdown_s": {"refined_mesh": t_mesh, "constraint_rows_host": t_rows_host,
-                              "constraint_rows_device": t_rows_dev},
+        "setup_breakdown_s": {"refined_mesh": t_mesh, "dof_map": t_dofmap, "constraint_rows_host": t_rows_host,
+                              "constraint_rows_device": t_rows_dev, "init_uploads_sparsity": t_init,
+                              "slot_plan_and_first_assembly": t_first},
         "config": {"workload": "convection-diffusion HEX27 build_cube %d^3, 3 cycles x 20%% h-refinement, "
                                "QGauss FIFTH, hanging-node + Dirichlet constraints" % n,
                    "n_elem": mesh.n_elem, "n_dofs": dm.n_dofs, "nnz": asm.nnz, "constrained_elements": n_cons,
