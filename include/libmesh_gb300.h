@@ -263,6 +263,16 @@ lmg_status lmg_sparsity_build(lmg_ctx *ctx, int64_t *nnz);
 /* 1 when the last lmg_sparsity_build formed the pattern on the device, else 0. */
 lmg_status lmg_sparsity_on_device(lmg_ctx *ctx, int32_t *on_device);
 lmg_status lmg_sparsity_copy(lmg_ctx *ctx, int32_t *row_ptr, int32_t *col_idx);
+/* The general path's insertion plan (each element's constraint matrix of
+ * DofMap::build_constraint_matrix, dof_map_constraints.C:3433-3540, and the
+ * CSR slots' element-order contributions of PetscMatrix::add_matrix,
+ * petsc_matrix.C:735-755): built on the device with on = 1 (the default) and
+ * on the host with on = 0; both give the same arrays bit for bit.  The host
+ * build also takes over where an element's list or constraint matrix
+ * outgrows the device buffers.  Takes effect at the next plan build. */
+lmg_status lmg_context_set_plan_on_device(lmg_ctx *ctx, int32_t on);
+/* 1 when the last general-path plan was built on the device, else 0. */
+lmg_status lmg_plan_on_device(lmg_ctx *ctx, int32_t *on_device);
 
 /* FE family flag OR'ed into fe_order (libMesh FEType{order, family}):
  * LMG_HIERARCHIC selects HIERARCHIC (FIRST on HEX8 / TET4 / PRISM6, SECOND on

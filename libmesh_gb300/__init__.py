@@ -240,6 +240,17 @@ class GpuAssembly:
     def update_inputs(self, xyz=None, elem_coef=None, nodal_f=None):
         self._ok(lib().lmg_inputs_update(self.ctx, ptr(xyz), ptr(elem_coef), ptr(nodal_f)))
 
+    def set_plan_on_device(self, on=True):
+        """Build the general path's insertion plan on the device (default) or
+        on the host; both give the same plan."""
+        self._ok(lib().lmg_context_set_plan_on_device(self.ctx, 1 if on else 0))
+
+    def plan_on_device(self):
+        """Whether the last general-path plan was built on the device."""
+        v = C.c_int32()
+        self._ok(lib().lmg_plan_on_device(self.ctx, C.byref(v)))
+        return bool(v.value)
+
     def sparsity_on_device(self):
         """Whether the sparsity pattern was formed on the device."""
         v = C.c_int32()

@@ -14,7 +14,8 @@ LIB = os.path.join(OUT, "liblmg.so")
 CXX_SOURCES = ["host_mesh.cpp", "host_mesh_tri.cpp", "host_dofmap.cpp", "host_amr.cpp", "fe_tables.cpp",
                "hier3_tables.cpp"]
 CU_SOURCES = ["elements.cu", "gather.cu", "context.cu", "context_general.cu", "general.cu", "batch.cu", "cg.cu",
-              "vjp.cu", "probe.cu", "hier3.cu", "tc.cu", "amr_rows.cu", "dofs_device.cu", "batch_persistent.cu"]
+              "vjp.cu", "probe.cu", "hier3.cu", "tc.cu", "amr_rows.cu", "dofs_device.cu", "batch_persistent.cu",
+              "plan_device.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

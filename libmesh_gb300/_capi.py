@@ -56,6 +56,8 @@ SIGNATURES = {
     "lmg_sparsity_build": [_p, _pi64],
     "lmg_sparsity_copy": [_p, _p, _p],
     "lmg_sparsity_on_device": [_p, _pi32],
+    "lmg_context_set_plan_on_device": [_p, _i32],
+    "lmg_plan_on_device": [_p, _pi32],
     "lmg_form_set": [_p, _i32, _i32, _i32, _p, _i32, _p, _p],
     "lmg_inputs_update": [_p, _p, _p, _p],
     "lmg_assemble": [_p, _i32, _p, _p, _i32],

@@ -964,6 +964,18 @@ lmg_status lmg_sparsity_build(lmg_ctx *c, int64_t *nnz) {
   return LMG_OK;
 }
 
+lmg_status lmg_context_set_plan_on_device(lmg_ctx *c, int32_t on) {
+  if (!c) return LMG_ERR_ARG;
+  c->plan_on_device = on != 0;
+  return LMG_OK;
+}
+
+lmg_status lmg_plan_on_device(lmg_ctx *c, int32_t *on_device) {
+  if (!c || !on_device) return LMG_ERR_ARG;
+  *on_device = c->plan_built_on_device ? 1 : 0;
+  return LMG_OK;
+}
+
 lmg_status lmg_sparsity_on_device(lmg_ctx *c, int32_t *on_device) {
   if (!c || !on_device) return LMG_ERR_ARG;
   if (!c->have_sparsity) return fail(c, LMG_ERR_STATE, "sparsity_on_device: build the sparsity first");

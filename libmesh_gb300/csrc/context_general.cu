@@ -85,6 +85,31 @@ lmg_status general_plan(lmg_ctx *c) {
   const int64_t E = c->n_elem;
   if (c->n_vars != 1 || (N > GEN_MAX_N && !(c->hier3 && N <= 64)))
     return fail(c, LMG_ERR_UNSUPPORTED, "general path: one variable and at most 27 dofs per element");
+  // the cubic hex kernel masks homogeneous Dirichlet rows itself
+  const bool use_cons = !(c->h_constrained.empty() || hier3_masks(c) || c->persist_pattern);
+  c->plan_built_on_device = false;
+  if (c->plan_on_device && c->n_dofs < INT32_MAX && E * (int64_t)N < INT32_MAX) {
+    // on the device; the host build below where a list or a constraint
+    // matrix outgrows the device buffers
+    int64_t kr = 0, fr = 0, n_cons = 0;
+    int max_ne = 0, max_ent = 0;
+    const lmg_status st = general_plan_device(c, use_cons, kr, fr, max_ne, max_ent, n_cons);
+    if (st == LMG_ERR_NEW_NONZERO)
+      return fail(c, st, "an element couples a pair outside the sparsity pattern");
+    if (st == LMG_ERR_OOM) return fail(c, st, "general plan: device memory");
+    if (st == LMG_ERR_CUDA) return fail(c, st, "general plan: CUDA error");
+    if (st == LMG_OK) {
+      c->n_cons_elem = n_cons;
+      c->cons_max_ne = max_ne;
+      c->cons_max_ent = max_ent;
+      LMG_CUDA(c, dalloc(c->d_Ebuf, (size_t)kr));
+      LMG_CUDA(c, dalloc(c->d_Fbuf, (size_t)fr));
+      LMG_CUDA(c, cudaStreamSynchronize(c->stream));
+      c->plan_built_on_device = true;
+      c->gen_plan = true;
+      return LMG_OK;
+    }
+  }
   if (c->h_row_ptr.empty()) {  // pattern built by the block path: bring it to the host
     c->h_row_ptr.resize((size_t)c->n_dofs + 1);
     c->h_col.resize((size_t)c->nnz);
@@ -99,9 +124,7 @@ lmg_status general_plan(lmg_ctx *c) {
     b = have_rows ? c->h_cons_ptr[(size_t)d] : 0;
     e = have_rows ? c->h_cons_ptr[(size_t)d + 1] : 0;
   };
-  // the cubic hex kernel masks homogeneous Dirichlet rows itself
-  const uint8_t *cons =
-      (c->h_constrained.empty() || hier3_masks(c) || c->persist_pattern) ? nullptr : c->h_constrained.data();
+  const uint8_t *cons = use_cons ? c->h_constrained.data() : nullptr;
   // per element: output dof list, its length and where its matrix / vector sit
   std::vector<int64_t> lptr((size_t)E + 1, 0);
   std::vector<int32_t> ldofs;

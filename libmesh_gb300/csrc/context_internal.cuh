@@ -95,6 +95,8 @@ struct lmg_ctx {
   // per-pattern HIERARCHIC elements (hier3.cu): cubic hexes, tets and prisms,
   // quadratic prisms; general path
   bool hier3 = false;
+  bool plan_on_device = true;         // general_plan tries the device build first
+  bool plan_built_on_device = false;  // the last general plan came from the device
   bool sparsity_on_device = false;  // the general path's graph came from device_constrained_graph
   bool persist_pattern = false;     // block-path system also held in per-pattern form (persistent batch)
   int32_t *d_h3batch = nullptr, *d_h3order = nullptr;  // element batches of one orientation pattern
@@ -158,6 +160,11 @@ lmg_status general_sparsity(lmg_ctx *c);   // CSR with the constraint couplings
 // d_col; LMG_ERR_UNSUPPORTED when the host build must take over.
 lmg_status device_constrained_graph(lmg_ctx *c, std::vector<int64_t> &rp, std::vector<int32_t> &cols);
 lmg_status general_plan(lmg_ctx *c);       // constraint columns, slot plan, buffers
+// general_plan's arrays built on the device (plan_device.cu); kr / fr are the
+// element-matrix and element-vector buffer sizes.  LMG_ERR_UNSUPPORTED when
+// the host build must take over.
+lmg_status general_plan_device(lmg_ctx *c, bool use_cons, int64_t &kr, int64_t &fr, int &max_ne, int &max_ent,
+                               int64_t &n_cons);
 // element and constraint kernels; mixed: FP32 contraction, FP64 map and sums
 lmg_status general_assemble(lmg_ctx *c, bool mixed);
 void general_gather(lmg_ctx *c, bool mixed);  // slot gather into K and F
