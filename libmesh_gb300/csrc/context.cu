@@ -1187,12 +1187,38 @@ lmg_status lmg_assemble(lmg_ctx *c, int32_t precision, double *K, double *F, int
     }
     general_assemble(c, mixed);
     if (c->perflog) LMG_CUDA(c, cudaEventRecord(e3[1], c->stream));
-    general_gather(c, mixed);
+    // host output of a large system: the insertion in row ranges, each
+    // range's copy overlapping the next range's insertion (a refined mesh's
+    // rows complete only once nearly every element has run, so the element
+    // stage itself is not split)
+    const bool chunked = K && !out_on_device && c->nnz * (int64_t)sizeof(double) > ((int64_t)64 << 20) &&
+                         (int64_t)c->h_row_ptr.size() == c->n_dofs + 1;
+    if (chunked) {
+      if (!c->copy_stream) LMG_CUDA(c, cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+      while ((int)c->chunk_ev.size() < OUT_CHUNKS) {
+        cudaEvent_t e;
+        LMG_CUDA(c, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        c->chunk_ev.push_back(e);
+      }
+      for (int ch = 0; ch < OUT_CHUNKS; ++ch) {
+        const int64_t P0 = c->n_dofs * ch / OUT_CHUNKS, P1 = c->n_dofs * (ch + 1) / OUT_CHUNKS;
+        if (P1 <= P0) continue;
+        general_gather(c, mixed, P0, P1);
+        LMG_CUDA(c, cudaEventRecord(c->chunk_ev[ch], c->stream));
+        LMG_CUDA(c, cudaStreamWaitEvent(c->copy_stream, c->chunk_ev[ch], 0));
+        const int64_t k0 = c->h_row_ptr[(size_t)P0], k1 = c->h_row_ptr[(size_t)P1];
+        LMG_CUDA(c, cudaMemcpyAsync(K + k0, c->d_K + k0, sizeof(double) * (k1 - k0), cudaMemcpyDeviceToHost,
+                                    c->copy_stream));
+      }
+    } else {
+      general_gather(c, mixed);
+    }
     if (c->perflog) LMG_CUDA(c, cudaEventRecord(e3[2], c->stream));
     LMG_CUDA(c, cudaGetLastError());
     const cudaMemcpyKind kind = out_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
-    if (K) LMG_CUDA(c, cudaMemcpyAsync(K, c->d_K, sizeof(double) * c->nnz, kind, c->stream));
+    if (K && !chunked) LMG_CUDA(c, cudaMemcpyAsync(K, c->d_K, sizeof(double) * c->nnz, kind, c->stream));
     if (F) LMG_CUDA(c, cudaMemcpyAsync(F, c->d_F, sizeof(double) * c->n_dofs, kind, c->stream));
+    if (chunked) LMG_CUDA(c, cudaStreamSynchronize(c->copy_stream));
     if (out_on_device || (!K && !F)) return LMG_OK;
     return check_status(c, "assemble");
   }

@@ -335,10 +335,17 @@ lmg_status general_assemble(lmg_ctx *c, bool mixed) {
   return LMG_OK;
 }
 
-void general_gather(lmg_ctx *c, bool mixed) {
+void general_gather(lmg_ctx *c, bool mixed, int64_t P0, int64_t P1) {
   // element matrices are double (FP64 drop-in) or float (mixed form)
+  int64_t s0 = 0, s1 = c->nnz;
+  if (P1 < 0) {
+    P1 = c->n_dofs;
+  } else {
+    s0 = c->h_row_ptr[(size_t)P0];
+    s1 = c->h_row_ptr[(size_t)P1];
+  }
   launch_gather_full(c->nnz, c->d_cptr, c->d_coff, c->d_Ebuf, mixed, c->d_K, c->n_dofs, c->d_gfptr, c->d_gfoff,
-                     c->d_Fbuf, c->d_F, c->n_sm, c->stream);
+                     c->d_Fbuf, c->d_F, c->n_sm, c->stream, s0, s1, P0, P1);
   c->launches++;
 }
 

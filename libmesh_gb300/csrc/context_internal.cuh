@@ -167,7 +167,8 @@ lmg_status general_plan_device(lmg_ctx *c, bool use_cons, int64_t &kr, int64_t &
                                int64_t &n_cons);
 // element and constraint kernels; mixed: FP32 contraction, FP64 map and sums
 lmg_status general_assemble(lmg_ctx *c, bool mixed);
-void general_gather(lmg_ctx *c, bool mixed);  // slot gather into K and F
+// slot gather into the K rows and F entries [P0, P1) (P1 < 0: all)
+void general_gather(lmg_ctx *c, bool mixed, int64_t P0 = 0, int64_t P1 = -1);
 // hier3.cu
 // FE types whose shapes follow each element's orientation pattern and that
 // take the per-pattern tables of hier3.cu: HIERARCHIC THIRD on HEX27, TET14

@@ -425,9 +425,11 @@ template <typename T>
 __global__ void k_gather_full(int64_t nnz, const int64_t *__restrict__ cptr, const uint32_t *__restrict__ coff,
                               const T *__restrict__ E, double *__restrict__ K, int64_t n_dofs,
                               const int64_t *__restrict__ fptr, const uint32_t *__restrict__ foff,
-                              const double *__restrict__ Fb, double *__restrict__ F) {
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < nnz + n_dofs; s += stride) {
+                              const double *__restrict__ Fb, double *__restrict__ F, int64_t s0, int64_t s1,
+                              int64_t d0, int64_t d1) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x, ns = s1 - s0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < ns + d1 - d0; i += stride) {
+    const int64_t s = i < ns ? s0 + i : nnz + d0 + (i - ns);
     if (s < nnz) {
       if constexpr (sizeof(T) == 4) {
         float hi = 0.f, lo = 0.f;
@@ -500,16 +502,17 @@ void launch_constrain(const ConsArgs &c, bool mixed, int n_sm, cudaStream_t s) {
 
 void launch_gather_full(int64_t nnz, const int64_t *cptr, const uint32_t *coff, const void *E, bool mixed, double *K,
                         int64_t n_dofs, const int64_t *fptr, const uint32_t *foff, const double *Fb, double *F,
-                        int n_sm, cudaStream_t s) {
-  const int64_t items = nnz + n_dofs;
+                        int n_sm, cudaStream_t s, int64_t s0, int64_t s1, int64_t d0, int64_t d1) {
+  const int64_t items = (s1 - s0) + (d1 - d0);
+  if (items <= 0) return;
   const int64_t blocks = (items + 255) / 256;
   const int g = (int)(blocks < (int64_t)n_sm * 16 ? blocks : (int64_t)n_sm * 16);
   if (mixed)
     k_gather_full<float><<<g, 256, 0, s>>>(nnz, cptr, coff, static_cast<const float *>(E), K, n_dofs, fptr, foff,
-                                            Fb, F);
+                                            Fb, F, s0, s1, d0, d1);
   else
     k_gather_full<double><<<g, 256, 0, s>>>(nnz, cptr, coff, static_cast<const double *>(E), K, n_dofs, fptr, foff,
-                                             Fb, F);
+                                             Fb, F, s0, s1, d0, d1);
 }
 
 }  // namespace lmg

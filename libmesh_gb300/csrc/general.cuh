@@ -58,8 +58,9 @@ bool gen_elements_built(int form, int n, int q);
 void launch_gen_elements(int form, int n, int q, bool mixed, const GenElemArgs &a, int max_ctas, cudaStream_t s);
 void launch_constrain(const ConsArgs &c, bool mixed, int n_sm, cudaStream_t s);
 // slot gather (FP64 sums) over element matrices stored as double, or float when mixed
+// over the slots [s0, s1) and the dofs [d0, d1)
 void launch_gather_full(int64_t nnz, const int64_t *cptr, const uint32_t *coff, const void *E, bool mixed, double *K,
                         int64_t n_dofs, const int64_t *fptr, const uint32_t *foff, const double *Fb, double *F,
-                        int n_sm, cudaStream_t s);
+                        int n_sm, cudaStream_t s, int64_t s0, int64_t s1, int64_t d0, int64_t d1);
 
 }  // namespace lmg

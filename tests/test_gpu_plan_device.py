@@ -92,3 +92,29 @@ def test_device_plan_full_size_convection_diffusion():
     k = np.exp(rng.normal(0, 0.5, m.n_elem))
     td, th = check(both_plans(lm.ADVDIFF, m, dm, 2, 5, k, f, cd_params()))
     print("plan and first assembly (%d elements): device %.3f s, host %.3f s" % (m.n_elem, td, th))
+
+
+def test_pipelined_host_output_equals_device_output():
+    """Host outputs of a large general-path system: the insertion runs in row
+    ranges, each range's copy overlapping the next range's insertion; K and F
+    equal the device outputs of one whole-mesh insertion bit for bit."""
+    import torch
+    m = lm.Mesh.build_refined_cube(16, lm.HEX27, 3, 0.2, 2)
+    dm = lm.DofMap(m, 1)
+    dm.add_dirichlet_boundary([0, 1, 2, 3, 4, 5], [0])
+    dm.create_dof_constraints()
+    rng = np.random.default_rng(2)
+    f = rng.uniform(-1, 1, (m.n_nodes, 1))
+    k = np.exp(rng.normal(0, 0.5, m.n_elem))
+    asm = lm.GpuAssembly(lm.ADVDIFF, 2, 5, elem_coef=k, nodal_f=f, params=cd_params())
+    asm.init(m, dm)
+    assert asm.nnz * 8 > 64 << 20   # large enough for the pipelined host output
+    for prec in (lm.FP64, lm.MIXED):
+        Kh, Fh = asm.assemble(prec)
+        Kd = torch.empty(asm.nnz, dtype=torch.float64, device="cuda")
+        Fd = torch.empty(dm.n_dofs, dtype=torch.float64, device="cuda")
+        asm.assemble_device(prec, Kd.data_ptr(), Fd.data_ptr())
+        asm.synchronize()
+        assert np.array_equal(Kh.view(np.uint64), Kd.cpu().numpy().view(np.uint64))
+        assert np.array_equal(Fh.view(np.uint64), Fd.cpu().numpy().view(np.uint64))
+    asm.close()
